@@ -1,0 +1,258 @@
+"""ctypes binding of the fwant_gb300 C ABI (include/fwant_gb300.h).
+
+`Solver` mirrors the reference solver's set-up sequence (grid -> metric -> media ->
+PML -> sources -> receivers -> time loop) with numpy arrays in the reference's
+Fortran layouts.  There is no fallback: if the native library is missing or cannot
+be loaded, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libfwant_gb300.so")
+
+STORAGE_FP32, STORAGE_BF16, STORAGE_FP16, STORAGE_FP64 = 0, 1, 2, 3
+STF_RICKER, STF_GAUSS, STF_BELL, STF_STEP, STF_DELTA = 200, 220, 230, 240, 250
+SVF_BELL, SVF_TRIANGLE, SVF_GAUSS = 100, 110, 120
+COMPONENTS = ("Vx", "Vy", "Vz", "Txx", "Tyy", "Tzz", "Txy", "Txz", "Tyz")
+
+STATUS = {
+    0: "OK",
+    1: "INVALID_ARG",
+    2: "OOM",
+    3: "CUDA_ERROR",
+    4: "NUMERIC_OVERFLOW",
+    5: "TIMEOUT",
+    6: "STATE",
+}
+
+# (name, restype, argtypes); every fwant_* symbol declared in include/fwant_gb300.h
+_fp = C.POINTER(C.c_float)
+_ip = C.POINTER(C.c_int)
+_vp = C.c_void_p
+EXPORTS = [
+    ("fwant_version", C.c_char_p, []),
+    ("fwant_create", C.c_int, [_vp, C.POINTER(_vp)]),
+    ("fwant_destroy", None, [_vp]),
+    ("fwant_last_error", C.c_char_p, [_vp]),
+    ("fwant_set_coord", C.c_int, [_vp, _fp, _fp, _fp]),
+    ("fwant_set_metric", C.c_int, [_vp, _fp, _fp, _fp, _fp, _fp]),
+    ("fwant_compute_metric", C.c_int, [_vp]),
+    ("fwant_get_metric", C.c_int, [_vp, _fp, _fp, _fp, _fp, _fp]),
+    ("fwant_set_media", C.c_int, [_vp, _fp, _fp, _fp]),
+    ("fwant_set_pml", C.c_int, [_vp, _ip, _fp, _fp, _fp]),
+    ("fwant_set_forces", C.c_int, [_vp, C.c_int, C.c_int, _ip, _fp, _fp, _fp, _fp, _fp, _fp, _fp, C.c_int]),
+    ("fwant_set_moments", C.c_int, [_vp, C.c_int, C.c_int, _ip, _fp, _fp, _fp, _fp, _fp, C.c_int]),
+    ("fwant_set_receivers", C.c_int, [_vp, C.c_int, _ip, C.c_int]),
+    ("fwant_run", C.c_int, [_vp, C.c_int]),
+    ("fwant_reference_steps", C.c_int, [C.c_int]),
+    ("fwant_get_ntime", C.c_int, [_vp, _ip]),
+    ("fwant_get_seismo", C.c_int, [_vp, _fp, C.c_int, _ip]),
+    ("fwant_get_field", C.c_int, [_vp, C.c_int, _fp]),
+    ("fwant_set_field", C.c_int, [_vp, C.c_int, _fp]),
+    ("fwant_check", C.c_int, [_vp]),
+    ("fwant_last_run_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
+]
+
+
+class FwantConfig(C.Structure):
+    _fields_ = [
+        ("ni", C.c_int), ("nj", C.c_int), ("nk", C.c_int),
+        ("stept", C.c_double),
+        ("free_surface", C.c_int), ("src_surface", C.c_int),
+        ("storage", C.c_int), ("device", C.c_int),
+    ]
+
+
+class FwantError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_LIB = None
+
+
+def load_library(path: str | None = None):
+    """Load (once) and return the native library; raises if it is absent."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(
+            f"native library {p} is missing: build it with `python -m fwant_gb300.build` "
+            "(there is no CPU fallback)")
+    lib = C.CDLL(p)
+    for name, res, args in EXPORTS:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def _f32(a, n=None):
+    """Flatten in C order (callers shape arrays so that C order is the Fortran layout)."""
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1))
+    if n is not None and a.size != n:
+        raise ValueError(f"expected {n} values, got {a.size}")
+    return a
+
+
+def _fortran3(a, shape):
+    a = np.asarray(a, dtype=np.float32)
+    if a.shape != shape:
+        raise ValueError(f"expected shape {shape}, got {a.shape}")
+    return np.ascontiguousarray(a.reshape(-1, order="F"))
+
+
+def _ptr(a, t=C.c_float):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class Solver:
+    """One simulation on one GPU (the reference's per-rank solver state)."""
+
+    def __init__(self, ni, nj, nk, stept, free_surface=True, src_surface=True, storage=STORAGE_FP32, device=0):
+        self._lib = load_library()
+        cfg = FwantConfig(int(ni), int(nj), int(nk), float(stept), int(bool(free_surface)),
+                          int(bool(src_surface)), int(storage), int(device))
+        h = C.c_void_p()
+        rc = self._lib.fwant_create(C.byref(cfg), C.byref(h))
+        if rc != 0:
+            raise FwantError(rc, "fwant_create failed")
+        self._h = h
+        self.ni, self.nj, self.nk = int(ni), int(nj), int(nk)
+        self.nx, self.ny, self.nz = self.ni + 6, self.nj + 6, self.nk + 6
+        self.shape = (self.nx, self.ny, self.nz)
+        self.stept = float(stept)
+        self.num_pt = 0
+
+    def _chk(self, rc):
+        if rc != 0:
+            raise FwantError(rc, self._lib.fwant_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.fwant_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # --- inputs -----------------------------------------------------------
+    def set_coord(self, x, y, z):
+        x, y, z = _f32(x, self.nx), _f32(y, self.ny), _f32(z, self.nz)
+        self._chk(self._lib.fwant_set_coord(self._h, _ptr(x), _ptr(y), _ptr(z)))
+
+    def set_metric(self, xsin, xcot, xi_x, eta_y, zeta_z):
+        a = [_f32(xsin, self.nx), _f32(xcot, self.nx), _f32(xi_x, self.nx), _f32(eta_y, self.ny),
+             _f32(zeta_z, self.nz)]
+        self._chk(self._lib.fwant_set_metric(self._h, *[_ptr(v) for v in a]))
+
+    def compute_metric(self):
+        self._chk(self._lib.fwant_compute_metric(self._h))
+
+    def get_metric(self):
+        out = [np.zeros(self.nx, np.float32), np.zeros(self.nx, np.float32), np.zeros(self.nx, np.float32),
+               np.zeros(self.ny, np.float32), np.zeros(self.nz, np.float32)]
+        self._chk(self._lib.fwant_get_metric(self._h, *[_ptr(v) for v in out]))
+        return dict(zip(("xsin", "xcot", "xi_x", "eta_y", "zeta_z"), out))
+
+    def set_media(self, lam, mu, rho):
+        a = [_fortran3(v, self.shape) for v in (lam, mu, rho)]
+        self._chk(self._lib.fwant_set_media(self._h, *[_ptr(v) for v in a]))
+
+    def set_pml(self, number, velocity, bmax, amax):
+        n = np.ascontiguousarray(np.asarray(number, dtype=np.int32).reshape(6))
+        v, b, a = (_f32(q, 6) for q in (velocity, bmax, amax))
+        self._chk(self._lib.fwant_set_pml(self._h, _ptr(n, C.c_int), _ptr(v), _ptr(b), _ptr(a)))
+
+    def set_forces(self, indx, shift, start_time, stf_time, stf_freq, fx, fy, fz, stf_id=STF_RICKER):
+        indx = np.ascontiguousarray(np.asarray(indx, dtype=np.int32).reshape(-1, 3))
+        num = indx.shape[0]
+        stf_time = _f32(stf_time)
+        ntwin = stf_time.size
+        args = [_f32(np.asarray(shift).reshape(-1, 3), 3 * num), _f32(start_time, num), stf_time,
+                _f32(stf_freq, ntwin)]
+        # Fx etc. are (ntwin, num) column-major: index m + ntwin*n
+        f = [_f32(np.asarray(q, dtype=np.float32).reshape(num, ntwin), ntwin * num) for q in (fx, fy, fz)]
+        self._chk(self._lib.fwant_set_forces(self._h, num, ntwin, _ptr(indx, C.c_int), *[_ptr(q) for q in args],
+                                             *[_ptr(q) for q in f], int(stf_id)))
+
+    def set_moments(self, indx, shift, start_time, stf_time, stf_freq, mom, stf_id=STF_RICKER):
+        """mom: array (6, num, ntwin) of Mxx Myy Mzz Mxy Mxz Myz."""
+        indx = np.ascontiguousarray(np.asarray(indx, dtype=np.int32).reshape(-1, 3))
+        num = indx.shape[0]
+        stf_time = _f32(stf_time)
+        ntwin = stf_time.size
+        mom = _f32(np.asarray(mom, dtype=np.float32).reshape(6, num, ntwin), 6 * num * ntwin)
+        args = [_f32(np.asarray(shift).reshape(-1, 3), 3 * num), _f32(start_time, num), stf_time,
+                _f32(stf_freq, ntwin), mom]
+        self._chk(self._lib.fwant_set_moments(self._h, num, ntwin, _ptr(indx, C.c_int), *[_ptr(q) for q in args],
+                                              int(stf_id)))
+
+    def set_receivers(self, indx, tinv=1):
+        indx = np.ascontiguousarray(np.asarray(indx, dtype=np.int32).reshape(-1, 3))
+        self.num_pt = indx.shape[0]
+        self._chk(self._lib.fwant_set_receivers(self._h, self.num_pt, _ptr(indx, C.c_int), int(tinv)))
+
+    # --- time loop and outputs ---------------------------------------------
+    def run(self, nsteps):
+        self._chk(self._lib.fwant_run(self._h, int(nsteps)))
+
+    @property
+    def ntime(self):
+        v = C.c_int()
+        self._chk(self._lib.fwant_get_ntime(self._h, C.byref(v)))
+        return v.value
+
+    def last_run_ms(self):
+        v = C.c_double()
+        self._chk(self._lib.fwant_last_run_ms(self._h, C.byref(v)))
+        return v.value
+
+    def get_seismo(self, max_samples=None):
+        """Return array (9, nsamp, num_pt)."""
+        if max_samples is None:
+            max_samples = self.ntime + 1
+        out = np.zeros(9 * max(max_samples, 1) * max(self.num_pt, 1), np.float32)
+        ns = C.c_int()
+        self._chk(self._lib.fwant_get_seismo(self._h, _ptr(out), int(max_samples), C.byref(ns)))
+        n = ns.value
+        return out[: 9 * n * self.num_pt].reshape(9, n, self.num_pt)
+
+    def get_field(self, component):
+        c = COMPONENTS.index(component) if isinstance(component, str) else int(component)
+        out = np.zeros(self.nx * self.ny * self.nz, np.float32)
+        self._chk(self._lib.fwant_get_field(self._h, c, _ptr(out)))
+        return out.reshape(self.shape, order="F")
+
+    def set_field(self, component, values):
+        c = COMPONENTS.index(component) if isinstance(component, str) else int(component)
+        a = _fortran3(values, self.shape)
+        self._chk(self._lib.fwant_set_field(self._h, c, _ptr(a)))
+
+    def check(self):
+        """macdrp_check: raises FwantError(NUMERIC_OVERFLOW) on NaN/Inf/huge."""
+        self._chk(self._lib.fwant_check(self._h))
+
+
+def reference_steps(nt: int) -> int:
+    """Steps the reference executes for a configured nt (whole 8-step blocks)."""
+    return int(load_library().fwant_reference_steps(int(nt)))

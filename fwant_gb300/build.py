@@ -1,0 +1,86 @@
+"""Build the native library libfwant_gb300.so in-tree (fwant_gb300/lib/).
+
+CUDA sources are compiled for sm_103a only; host sources go through nvcc as well so
+that the CUDA include and library paths come from the toolkit.  Objects are rebuilt
+only when a source or header is newer.  Usage: ``python -m fwant_gb300.build``.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OBJ = os.path.join(HERE, "_build")
+LIB_DIR = os.path.join(HERE, "lib")
+LIB = os.path.join(LIB_DIR, "libfwant_gb300.so")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# -fmad=false: every product and sum rounds separately, as in the reference's FP32 source.
+CU_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler",
+            "-ffp-contract=off", "-Xptxas", "-O3"]
+# -ffp-contract=off: host set-up arithmetic (PML profiles, source weights) must not
+# contract into FMAs on aarch64, where GCC would otherwise do so by default.
+CPP_FLAGS = ["-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
+
+SOURCES = ["stage.cu", "aux.cu", "solver.cpp"]
+
+
+def _nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.sep not in cand or os.path.exists(cand)):
+            return cand
+    return "nvcc"
+
+
+def _headers():
+    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    hs += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
+    return hs
+
+
+def _stale(target: str, deps) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _run(cmd, verbose):
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"command failed ({r.returncode}): {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    if verbose and (r.stdout or r.stderr):
+        print(r.stdout + r.stderr, flush=True)
+    return r
+
+
+def build(verbose: bool = False, force: bool = False, jobs: int | None = None) -> str:
+    os.makedirs(OBJ, exist_ok=True)
+    os.makedirs(LIB_DIR, exist_ok=True)
+    nvcc = _nvcc()
+    hdrs = _headers()
+    jobs_todo = []
+    objs = []
+    for src in SOURCES:
+        path = os.path.join(CSRC, src)
+        obj = os.path.join(OBJ, src + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [path] + hdrs):
+            flags = CU_FLAGS + ARCH if src.endswith(".cu") else CPP_FLAGS
+            jobs_todo.append([nvcc, *flags, "-I", CSRC, "-I", INCLUDE, "-c", path, "-o", obj])
+    if jobs_todo:
+        with ThreadPoolExecutor(max_workers=jobs or min(8, len(jobs_todo))) as ex:
+            list(ex.map(lambda c: _run(c, verbose), jobs_todo))
+    if force or jobs_todo or _stale(LIB, objs):
+        _run([nvcc, "-shared", *ARCH, "-o", LIB, *objs, "-lcudart"], verbose)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv, force="-f" in sys.argv))

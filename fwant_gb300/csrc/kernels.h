@@ -1,0 +1,116 @@
+// Internal interface between the host driver (solver.cpp) and the CUDA kernels.
+// Plain structs only: they are passed to kernels by value.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+namespace fw {
+
+constexpr int NF = 9;  // Vx Vy Vz Txx Tyy Tzz Txy Txz Tyz
+enum { VX = 0, VY, VZ, TXX, TYY, TZZ, TXY, TXZ, TYZ };
+constexpr int LENFD = 3;
+constexpr int PADL = 29;  // physical column of Fortran index i is (i-1)+PADL: interior starts at 32
+
+// Geometry of one simulation in device memory.  Interior bounds are 0-based
+// (Fortran index minus one).  Element (i,j,k) of a component lives at
+// (i + PADL) + px*(j + ny*k).
+struct Geom {
+  int ni, nj, nk, nx, ny, nz;
+  int px;                 // row pitch in elements
+  long long plane;        // px*ny
+  long long fstride;      // elements between components of one register set
+  int i1, i2, j1, j2, k1, k2;  // interior, inclusive
+  int freesurf;           // free surface on k = k2
+};
+
+// One PML slab (face x1 x2 y1 y2 z1 z2).  Its six memory variables are stored compactly:
+// element (i,j,k) at (i-i1) + sx*((j-j1) + sy*(k-k1)), variables vstride apart.
+struct Slab {
+  int on;
+  int i1, i2, j1, j2, k1, k2;
+  int sx, sy;
+  long long vstride;
+};
+
+// Sources resolved on the host into per-point weights.
+struct Sources {
+  // per-stage source-time tables: value at global stage g = ntime*4 + s for window w
+  const float* disp;   // [G][nw_f]  src_stf of force windows
+  const float* rate;   // [G][nw_f]  src_svf of force windows
+  const float* mrate;  // [G][nw_m]  src_svf of moment windows
+  int G;               // table length in stages
+  int nw_f, nw_m;
+  // surface forces (SrcSurface): entries in (n, m) order, last one wins at a node
+  int nsurf;
+  const int* surf_ij;     // [nsurf][2] 0-based (i, j)
+  const float* surf_q;    // [nsurf][3] F/S of that window
+  const int* surf_w;      // [nsurf] window index into disp/rate
+  // body forces with 7^3 smoothing
+  int nforce, ntwin_f;
+  const int* force_c;     // [nforce][3] 0-based centre
+  const float* force_wt;  // [nforce][343] 1/(V rho) d, 0 where skipped
+  const unsigned char* force_on;  // [nforce][343]
+  const float* force_F;   // [nforce][ntwin][3]
+  // moment tensors with 7^3 smoothing
+  int nmom, ntwin_m;
+  const int* mom_c;
+  const float* mom_d;     // [nmom][343] weights d
+  const float* mom_vol;   // [nmom][343] cell volume V
+  const unsigned char* mom_on;
+  const float* mom_M;     // [nmom][ntwin][6] Mxx Myy Mzz Mxy Mxz Myz
+};
+
+// Everything one RK-stage launch needs.
+template <class S>
+struct StageArgs {
+  Geom g;
+  const S* win;   // stage input W (9 components)
+  const S* wm;    // step-start register m (stages 2,3)
+  S* wout;        // stage output W
+  S* wt;          // RK accumulator t
+  const float* lam;
+  const float* mu;
+  const float* rho;
+  // 1-D metric, 0-based Fortran index, with ghosts
+  const float* xi_x;
+  const float* eta_y;
+  const float* zeta_z;
+  const float* xsin;
+  const float* xcot;
+  const float* zc;
+  // PML profiles (A, B, D/B) per axis, 0-based Fortran index
+  const float* pA[3];
+  const float* pB[3];
+  const float* pD[3];
+  Slab slab[6];
+  const S* ain[6];
+  const S* am[6];
+  S* aout[6];
+  S* at[6];
+  float a, b;     // rka*stept, rkb*stept
+  int stage;      // 0..3 inside the step
+  const int* ntime;  // device step counter
+  Sources src;
+  int src_surface;
+};
+
+// Launchers (stage.cu).  variant bit 2 = x, bit 1 = y, bit 0 = z; 1 = forward operator.
+void launch_stage_f32(const StageArgs<float>& a, int variant, int rk, void* stream);
+
+struct RecvArgs {
+  Geom g;
+  const float* w;     // register set holding the step's result
+  int npt;
+  const int* idx;     // [npt][3] 0-based
+  int tinv;
+  float* seismo;      // [9][cap][npt]
+  int cap;
+  int* ntime;
+};
+void launch_advance_record(const RecvArgs& a, void* stream);
+
+void launch_metric_fp64(int n, const float* coord, float* metric_out, int lo, int hi, void* stream);
+void launch_sincot_fp64(int n, const float* x, float* xsin, float* xcot, void* stream);
+void launch_maxabs(const Geom& g, const float* w, unsigned int* out_bits, void* stream);
+
+}  // namespace fw

@@ -1,0 +1,816 @@
+// Host driver of the GB300 forward solver: owns the device state of one simulation,
+// resolves sources/receivers/PML into device tables, and runs the 8-step F/B LDDRK4
+// cycle of seis3d_wave_8op_p3.F90 as fused stage launches, replayed from a CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/fwant_gb300.h"
+#include "host_math.h"
+#include "kernels.h"
+
+namespace {
+
+constexpr float RKA[4] = {0.5f, 0.5f, 1.0f, 0.0f};                        // firRKa (mod_macdrp.F90:205)
+const float RKB[4] = {1.0f / 6.0f, 1.0f / 3.0f, 1.0f / 3.0f, 1.0f / 6.0f};  // firRKb (mod_macdrp.F90:206)
+
+// Stage-1/3 operator of each step of the 8-step cycle (seis3d_wave_8op_p3.F90:82-591);
+// bit 2 = x, bit 1 = y, bit 0 = z, 1 = forward.  Stages 2/4 use the mirror.
+constexpr int CYCLE[8] = {0b000, 0b110, 0b111, 0b001, 0b010, 0b100, 0b101, 0b011};
+
+struct ForceDesc {
+  int num = 0, ntwin = 0, stf_id = 200;
+  std::vector<int> indx;  // 1-based
+  std::vector<float> shift, t0, stf_time, stf_freq, fx, fy, fz;
+};
+struct MomentDesc {
+  int num = 0, ntwin = 0, stf_id = 200;
+  std::vector<int> indx;
+  std::vector<float> shift, t0, stf_time, stf_freq, mom;  // mom: 6 blocks of ntwin*num
+};
+
+template <class T>
+T* dalloc(size_t n) {
+  void* p = nullptr;
+  if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) return nullptr;
+  return (T*)p;
+}
+
+}  // namespace
+
+struct fwant_solver {
+  fwant_config cfg{};
+  fw::Geom g{};
+  float stept = 0.0f;
+  cudaStream_t st = nullptr;
+  std::string err;
+
+  // four register sets of nine components each (W ping-pong, m, t; see run_step)
+  float* regs = nullptr;
+  int rA = 0, rB = 1, rC = 2, rT = 3;
+  float *lam = nullptr, *mu = nullptr, *rho = nullptr;
+  std::vector<float> h_rho;
+  // 1-D arrays, each with nx/ny/nz entries
+  float *d_x = nullptr, *d_y = nullptr, *d_z = nullptr, *d_xsin = nullptr, *d_xcot = nullptr;
+  float *d_xi = nullptr, *d_eta = nullptr, *d_zeta = nullptr;
+  float* d_prof = nullptr;  // A,B,D for x (nx each), y (ny), z (nz)
+  std::vector<float> hx, hy, hz, hxsin, hxcot;
+  bool have_coord = false, have_metric = false, have_media = false;
+
+  // PML
+  int absn[6] = {0, 0, 0, 0, 0, 0};
+  fw::Slab slab[6]{};
+  float* aux[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // 4 sets each
+  long long aux_set[6] = {0, 0, 0, 0, 0, 0};                               // elements per set
+  std::vector<float> hA[3], hB[3], hD[3];
+
+  // sources
+  ForceDesc forces;
+  MomentDesc moments;
+  bool src_dirty = true;
+  fw::Sources S{};
+  std::vector<void*> src_mem;
+  int stf_cap_steps = 0;  // steps covered by the STF tables
+
+  // receivers
+  int npt = 0, tinv = 1, cap = 0, nsamp = 0;
+  std::vector<int> rec_idx;  // 0-based
+  int* d_rec = nullptr;
+  float* d_seis = nullptr;
+
+  int* d_ntime = nullptr;
+  int ntime = 0, cycle_pos = 0;
+  unsigned int* d_maxbits = nullptr;
+
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one per (rA,rT) assignment
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0.0;
+
+  ~fwant_solver() {
+    cudaSetDevice(cfg.device);
+    drop_graphs();
+    free_sources();
+    cudaFree(regs); cudaFree(lam); cudaFree(mu); cudaFree(rho);
+    cudaFree(d_x); cudaFree(d_y); cudaFree(d_z); cudaFree(d_xsin); cudaFree(d_xcot);
+    cudaFree(d_xi); cudaFree(d_eta); cudaFree(d_zeta); cudaFree(d_prof);
+    for (int f = 0; f < 6; ++f) cudaFree(aux[f]);
+    cudaFree(d_rec); cudaFree(d_seis); cudaFree(d_ntime); cudaFree(d_maxbits);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (st) cudaStreamDestroy(st);
+  }
+
+  fwant_status fail(fwant_status code, const std::string& m) {
+    err = m;
+    return code;
+  }
+  fwant_status cuda_fail(cudaError_t e, const char* where) {
+    err = std::string(where) + ": " + cudaGetErrorString(e);
+    return FWANT_ERR_CUDA;
+  }
+
+  void drop_graphs() {
+    for (auto& ge : graph)
+      if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
+  }
+  void free_sources() {
+    for (void* p : src_mem) cudaFree(p);
+    src_mem.clear();
+    S = fw::Sources{};
+    stf_cap_steps = 0;
+  }
+  template <class T>
+  T* upload(const std::vector<T>& v) {
+    if (v.empty()) return nullptr;
+    T* d = dalloc<T>(v.size());
+    if (!d) return nullptr;
+    src_mem.push_back(d);
+    cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    return d;
+  }
+
+  long long off(int i, int j, int k) const {
+    return (long long)(i + fw::PADL) + (long long)g.px * ((long long)j + (long long)g.ny * k);
+  }
+  float* set(int r) const { return regs + (long long)r * fw::NF * g.fstride; }
+  float* aset(int f, int r) const { return aux[f] + (long long)r * aux_set[f]; }
+
+  fwant_status init() {
+    const int ni = cfg.ni, nj = cfg.nj, nk = cfg.nk;
+    if (ni < 8 || nj < 8 || nk < 8) return fail(FWANT_ERR_INVALID_ARG, "ni, nj, nk must be >= 8");
+    if (!(cfg.stept > 0.0)) return fail(FWANT_ERR_INVALID_ARG, "stept must be > 0");
+    if (cfg.storage != FWANT_STORAGE_FP32)
+      return fail(FWANT_ERR_INVALID_ARG, "only FWANT_STORAGE_FP32 is available in this build");
+    cudaError_t e = cudaSetDevice(cfg.device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    stept = float(cfg.stept);
+    g.ni = ni; g.nj = nj; g.nk = nk;
+    g.nx = ni + 6; g.ny = nj + 6; g.nz = nk + 6;
+    g.px = ((fw::PADL + g.nx + 31) / 32) * 32;
+    g.plane = (long long)g.px * g.ny;
+    g.fstride = ((g.plane * g.nz + 63) / 64) * 64;
+    g.i1 = 3; g.i2 = 3 + ni - 1; g.j1 = 3; g.j2 = 3 + nj - 1; g.k1 = 3; g.k2 = 3 + nk - 1;
+    g.freesurf = cfg.free_surface ? 1 : 0;
+    if ((e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
+    cudaEventCreate(&ev0);
+    cudaEventCreate(&ev1);
+    const size_t nreg = size_t(4) * fw::NF * g.fstride;
+    regs = dalloc<float>(nreg);
+    lam = dalloc<float>(g.fstride); mu = dalloc<float>(g.fstride); rho = dalloc<float>(g.fstride);
+    d_x = dalloc<float>(g.nx); d_y = dalloc<float>(g.ny); d_z = dalloc<float>(g.nz);
+    d_xsin = dalloc<float>(g.nx); d_xcot = dalloc<float>(g.nx); d_xi = dalloc<float>(g.nx);
+    d_eta = dalloc<float>(g.ny); d_zeta = dalloc<float>(g.nz);
+    d_prof = dalloc<float>(3 * size_t(g.nx + g.ny + g.nz));
+    d_ntime = dalloc<int>(1); d_maxbits = dalloc<unsigned int>(1);
+    if (!regs || !lam || !mu || !rho || !d_x || !d_y || !d_z || !d_xsin || !d_xcot || !d_xi || !d_eta ||
+        !d_zeta || !d_prof || !d_ntime || !d_maxbits)
+      return fail(FWANT_ERR_OOM, "device allocation failed");
+    cudaMemset(regs, 0, nreg * sizeof(float));
+    cudaMemset(lam, 0, g.fstride * sizeof(float)); cudaMemset(mu, 0, g.fstride * sizeof(float));
+    cudaMemset(rho, 0, g.fstride * sizeof(float));
+    cudaMemset(d_ntime, 0, sizeof(int));
+    for (int a = 0; a < 3; ++a) {
+      const int n = a == 0 ? g.nx : a == 1 ? g.ny : g.nz;
+      hA[a].assign(n, 0.0f); hB[a].assign(n, 1.0f); hD[a].assign(n, 0.0f);
+    }
+    if ((e = upload_profiles()) != cudaSuccess) return cuda_fail(e, "profiles");
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(e, "init");
+    return FWANT_OK;
+  }
+
+  cudaError_t upload_profiles() {
+    float* p = d_prof;
+    for (int a = 0; a < 3; ++a) {
+      const size_t n = hA[a].size();
+      cudaMemcpy(p, hA[a].data(), n * 4, cudaMemcpyHostToDevice); p += n;
+      cudaMemcpy(p, hB[a].data(), n * 4, cudaMemcpyHostToDevice); p += n;
+      cudaMemcpy(p, hD[a].data(), n * 4, cudaMemcpyHostToDevice); p += n;
+    }
+    return cudaGetLastError();
+  }
+  const float* prof(int axis, int which) const {
+    const float* p = d_prof;
+    for (int a = 0; a < axis; ++a) p += 3 * hA[a].size();
+    return p + which * hA[axis].size();
+  }
+
+  // Fortran (nx,ny,nz) host array -> padded device array
+  cudaError_t put3(float* dst, const float* src) {
+    return cudaMemcpy2D(dst + fw::PADL, size_t(g.px) * 4, src, size_t(g.nx) * 4, size_t(g.nx) * 4,
+                        size_t(g.ny) * g.nz, cudaMemcpyHostToDevice);
+  }
+  cudaError_t get3(float* dst, const float* src) {
+    return cudaMemcpy2D(dst, size_t(g.nx) * 4, src + fw::PADL, size_t(g.px) * 4, size_t(g.nx) * 4,
+                        size_t(g.ny) * g.nz, cudaMemcpyDeviceToHost);
+  }
+
+  // abs_init (mod_abs_npml.F90:135-616), isotropic build.
+  fwant_status set_pml(const int* number, const float* vel, const float* bmax, const float* amax) {
+    if (!have_coord) return fail(FWANT_ERR_STATE, "fwant_set_pml needs fwant_set_coord first");
+    for (int f = 0; f < 6; ++f) {
+      absn[f] = number[f] > 0 ? number[f] : 0;
+      if (absn[f] > 0 && bmax[f] < 1.0f) return fail(FWANT_ERR_INVALID_ARG, "CFS_bmax should be >= 1");
+    }
+    if (absn[0] + absn[1] + 2 > cfg.ni || absn[2] + absn[3] + 2 > cfg.nj)
+      return fail(FWANT_ERR_INVALID_ARG, "PML thicker than the grid");
+    if (absn[5] > 0) g.freesurf = 0;  // mod_abs_npml.F90:182-184
+    if (g.freesurf && absn[4] + 5 > cfg.nk)
+      return fail(FWANT_ERR_INVALID_ARG, "the z1 PML must stay below the top four planes");
+    for (int a = 0; a < 3; ++a) {
+      std::fill(hA[a].begin(), hA[a].end(), 0.0f);
+      std::fill(hB[a].begin(), hB[a].end(), 1.0f);
+      std::fill(hD[a].begin(), hD[a].end(), 0.0f);
+    }
+    // Fortran 1-based indexing helpers on the 0-based host copies
+    auto X = [&](int i) { return hx[i - 1]; };
+    auto Y = [&](int j) { return hy[j - 1]; };
+    auto Z = [&](int k) { return hz[k - 1]; };
+    const int ni1 = 4, ni2 = 3 + cfg.ni, nj1 = 4, nj2 = 3 + cfg.nj, nk1 = 4, nk2 = 3 + cfg.nk;
+    auto face = [&](int f, int axis, int lo, int hi, float L0, float dmax, auto dist) {
+      for (int q = lo; q <= hi; ++q) {
+        const float L = dist(q);
+        hD[axis][q - 1] = fw::hm::pml_d(L, L0, dmax);
+        hA[axis][q - 1] = fw::hm::pml_a(L, L0, amax[f]);
+        hB[axis][q - 1] = fw::hm::pml_b(L, L0, bmax[f]);
+      }
+    };
+    if (absn[0] > 0) {
+      const float x0 = X(absn[0] + ni1), L0 = Z(nk2) * (x0 - X(ni1));
+      const float dm = fw::hm::pml_dmax(L0, vel[0], fw::hm::pml_R(absn[0]));
+      face(0, 0, ni1, absn[0] + ni1, L0, dm, [&](int i) { return Z(nk2) * (x0 - X(i)); });
+    }
+    if (absn[1] > 0) {
+      const float x0 = X(ni2 - absn[1]), L0 = Z(nk2) * (X(ni2) - x0);
+      const float dm = fw::hm::pml_dmax(L0, vel[1], fw::hm::pml_R(absn[1]));
+      face(1, 0, ni2 - absn[1], ni2, L0, dm, [&](int i) { return Z(nk2) * (X(i) - x0); });
+    }
+    if (absn[2] > 0) {
+      const float y0 = Y(absn[2] + nj1), L0 = Z(nk2) * (y0 - Y(nj1));
+      const float dm = fw::hm::pml_dmax(L0, vel[2], fw::hm::pml_R(absn[2]));
+      face(2, 1, nj1, absn[2] + nj1, L0, dm, [&](int j) { return Z(nk2) * (y0 - Y(j)); });
+    }
+    if (absn[3] > 0) {
+      const float y0 = Y(nj2 - absn[3]), L0 = Z(nk2) * (Y(nj2) - y0);
+      const float dm = fw::hm::pml_dmax(L0, vel[3], fw::hm::pml_R(absn[3]));
+      face(3, 1, nj2 - absn[3], nj2, L0, dm, [&](int j) { return Z(nk2) * (Y(j) - y0); });
+    }
+    if (absn[4] > 0) {
+      const float z0 = Z(absn[4] + nk1), L0 = z0 - Z(nk1);
+      const float dm = fw::hm::pml_dmax(L0, vel[4], fw::hm::pml_R(absn[4]));
+      face(4, 2, nk1, nk1 + absn[4], L0, dm, [&](int k) { return z0 - Z(k); });
+    }
+    if (absn[5] > 0) {
+      const float z0 = Z(nk2 - absn[5]), L0 = Z(nk2) - z0;
+      const float dm = fw::hm::pml_dmax(L0, vel[5], fw::hm::pml_R(absn[5]));
+      face(5, 2, nk2 - absn[5], nk2, L0, dm, [&](int k) { return Z(k) - z0; });
+    }
+    for (int a = 0; a < 3; ++a)
+      for (size_t q = 0; q < hD[a].size(); ++q) hD[a][q] = hD[a][q] / hB[a][q];  // D := d/b
+    cudaError_t e = upload_profiles();
+    if (e != cudaSuccess) return cuda_fail(e, "pml profiles");
+    // slabs (0-based bounds)
+    const int i1 = g.i1, i2 = g.i2, j1 = g.j1, j2 = g.j2, k1 = g.k1, k2 = g.k2;
+    const int b[6][6] = {{i1, i1 + absn[0], j1, j2, k1, k2}, {i2 - absn[1], i2, j1, j2, k1, k2},
+                         {i1, i2, j1, j1 + absn[2], k1, k2}, {i1, i2, j2 - absn[3], j2, k1, k2},
+                         {i1, i2, j1, j2, k1, k1 + absn[4]}, {i1, i2, j1, j2, k2 - absn[5], k2}};
+    for (int f = 0; f < 6; ++f) {
+      cudaFree(aux[f]);
+      aux[f] = nullptr;
+      fw::Slab& s = slab[f];
+      s = fw::Slab{};
+      if (absn[f] <= 0) continue;
+      s.on = 1;
+      s.i1 = b[f][0]; s.i2 = b[f][1]; s.j1 = b[f][2]; s.j2 = b[f][3]; s.k1 = b[f][4]; s.k2 = b[f][5];
+      s.sx = s.i2 - s.i1 + 1; s.sy = s.j2 - s.j1 + 1;
+      const long long n = (long long)s.sx * s.sy * (s.k2 - s.k1 + 1);
+      s.vstride = ((n + 31) / 32) * 32;
+      aux_set[f] = 6 * s.vstride;
+      aux[f] = dalloc<float>(size_t(4) * aux_set[f]);
+      if (!aux[f]) return fail(FWANT_ERR_OOM, "PML allocation failed");
+      cudaMemset(aux[f], 0, size_t(4) * aux_set[f] * sizeof(float));
+    }
+    drop_graphs();
+    src_dirty = true;  // the surface-source list depends on the free-surface flag
+    return FWANT_OK;
+  }
+
+  // Resolve sources into device tables covering at least `steps` steps.
+  fwant_status prepare_sources(int steps) {
+    if (!src_dirty && steps <= stf_cap_steps) return FWANT_OK;
+    drop_graphs();
+    free_sources();
+    const int cap_steps = std::max(steps + 8, 1024);
+    const int G = cap_steps * 4;
+    const float incr[4] = {0.0f, RKA[0], RKA[1], RKA[2]};  // set_cur_time(ntime, firRKa(s))
+    const ForceDesc& F = forces;
+    const MomentDesc& Mo = moments;
+    const int nwf = F.num * F.ntwin, nwm = Mo.num * Mo.ntwin;
+    std::vector<float> disp(size_t(G) * std::max(nwf, 1), 0.0f), rate(size_t(G) * std::max(nwf, 1), 0.0f);
+    std::vector<float> mrate(size_t(G) * std::max(nwm, 1), 0.0f);
+    for (int n = 0; n < cap_steps; ++n)
+      for (int s = 0; s < 4; ++s) {
+        const int gs = n * 4 + s;
+        const float t = (float(n) + incr[s]) * stept;
+        for (int q = 0; q < F.num; ++q)
+          for (int m = 0; m < F.ntwin; ++m) {
+            float dv, rv;
+            if (!fw::hm::stf(t - F.t0[q], F.stf_time[m], F.stf_freq[m], F.stf_id, n, stept, &dv) ||
+                !fw::hm::svf(t - F.t0[q], F.stf_time[m], F.stf_freq[m], F.stf_id, n, stept, &rv))
+              return fail(FWANT_ERR_INVALID_ARG, "unknown force stf id");
+            disp[size_t(gs) * nwf + q * F.ntwin + m] = dv;
+            rate[size_t(gs) * nwf + q * F.ntwin + m] = rv;
+          }
+        for (int q = 0; q < Mo.num; ++q)
+          for (int m = 0; m < Mo.ntwin; ++m) {
+            float rv;
+            if (!fw::hm::svf(t - Mo.t0[q], Mo.stf_time[m], Mo.stf_freq[m], Mo.stf_id, n, stept, &rv))
+              return fail(FWANT_ERR_INVALID_ARG, "unknown moment stf id");
+            mrate[size_t(gs) * nwm + q * Mo.ntwin + m] = rv;
+          }
+      }
+    auto X = [&](int i) { return hx[i]; };  // 0-based
+    auto Y = [&](int j) { return hy[j]; };
+    auto Z = [&](int k) { return hz[k]; };
+    auto interior = [&](int i, int j, int k) {
+      return i >= g.i1 && i <= g.i2 && j >= g.j1 && j <= g.j2 && k >= g.k1 && k <= g.k2;
+    };
+    // surface forces (src_surface, mod_src.F90:373-414)
+    std::vector<int> surf_ij, surf_w;
+    std::vector<float> surf_q;
+    if (g.freesurf && cfg.src_surface)
+      for (int q = 0; q < F.num; ++q) {
+        const int i = F.indx[3 * q] - 1, j = F.indx[3 * q + 1] - 1, k = F.indx[3 * q + 2] - 1;
+        if (!(i >= g.i1 && i <= g.i2 && j >= g.j1 && j <= g.j2 && k == g.k2)) continue;
+        const float Sa = (X(i + 1) - X(i - 1)) * (Y(j + 1) - Y(j - 1)) / 4.0f * (Z(k) * Z(k)) * hxsin[i];
+        for (int m = 0; m < F.ntwin; ++m) {
+          const size_t w = m + size_t(F.ntwin) * q;
+          surf_ij.push_back(i); surf_ij.push_back(j);
+          surf_q.push_back(F.fx[w] / Sa); surf_q.push_back(F.fy[w] / Sa); surf_q.push_back(F.fz[w] / Sa);
+          surf_w.push_back(q * F.ntwin + m);
+        }
+      }
+    // body forces (src_force, mod_src.F90:275-345)
+    std::vector<int> fc;
+    std::vector<float> fwt, fF;
+    std::vector<unsigned char> fon;
+    float nd[343];
+    for (int q = 0; q < F.num; ++q) {
+      const int si = F.indx[3 * q] - 1, sj = F.indx[3 * q + 1] - 1, sk = F.indx[3 * q + 2] - 1;
+      if (!fw::hm::norm_delt(nd, F.shift[3 * q], F.shift[3 * q + 1], F.shift[3 * q + 2]))
+        return fail(FWANT_ERR_INVALID_ARG, "cal_norm_delt is zero");
+      if (g.freesurf && sk + 3 > g.k2) {
+        float s = 0.0f;
+        for (int lk = -3; lk <= g.k2 - sk; ++lk)
+          for (int lj = -3; lj <= 3; ++lj)
+            for (int li = -3; li <= 3; ++li) s += nd[(li + 3) + 7 * ((lj + 3) + 7 * (lk + 3))];
+        for (int e = 0; e < 343; ++e) nd[e] = nd[e] / s;
+      }
+      fc.push_back(si); fc.push_back(sj); fc.push_back(sk);
+      for (int lk = -3; lk <= 3; ++lk)
+        for (int lj = -3; lj <= 3; ++lj)
+          for (int li = -3; li <= 3; ++li) {
+            const int i = si + li, j = sj + lj, k = sk + lk;
+            const float d = nd[(li + 3) + 7 * ((lj + 3) + 7 * (lk + 3))];
+            float wv = 0.0f;
+            unsigned char on = 0;
+            if (interior(i, j, k)) {
+              float V = (X(i + 1) - X(i - 1)) * (Y(j + 1) - Y(j - 1)) * (Z(k + 1) - Z(k - 1)) / 8.0f * (Z(k) * Z(k)) * hxsin[i];
+              const size_t pf = size_t(i) + size_t(g.nx) * (size_t(j) + size_t(g.ny) * k);
+              V = 1.0f / (V * h_rho[pf]) * d;
+              on = 1;
+              wv = V;
+              if (g.freesurf && k == g.k2) {
+                if (cfg.src_surface) on = 0;
+                else wv = 2.0f * V;  // exact: fx*2 == fx0*(2V) in binary floating point
+              }
+            }
+            fwt.push_back(wv);
+            fon.push_back(on);
+          }
+      for (int m = 0; m < F.ntwin; ++m) {
+        const size_t w = m + size_t(F.ntwin) * q;
+        fF.push_back(F.fx[w]); fF.push_back(F.fy[w]); fF.push_back(F.fz[w]);
+      }
+    }
+    // moment tensors (src_stress, mod_src.F90:207-273)
+    std::vector<int> mc;
+    std::vector<float> md, mvol, mM;
+    std::vector<unsigned char> mon;
+    for (int q = 0; q < Mo.num; ++q) {
+      const int si = Mo.indx[3 * q] - 1, sj = Mo.indx[3 * q + 1] - 1, sk = Mo.indx[3 * q + 2] - 1;
+      if (!fw::hm::norm_delt(nd, Mo.shift[3 * q], Mo.shift[3 * q + 1], Mo.shift[3 * q + 2]))
+        return fail(FWANT_ERR_INVALID_ARG, "cal_norm_delt is zero");
+      if (g.freesurf && sk + 3 > g.k2) {
+        float s = 0.0f;
+        for (int lk = -3; lk <= g.k2 - sk; ++lk)
+          for (int lj = -3; lj <= 3; ++lj)
+            for (int li = -3; li <= 3; ++li) s += nd[(li + 3) + 7 * ((lj + 3) + 7 * (lk + 3))];
+        for (int e = 0; e < 343; ++e) nd[e] = nd[e] / s;
+      }
+      mc.push_back(si); mc.push_back(sj); mc.push_back(sk);
+      for (int lk = -3; lk <= 3; ++lk)
+        for (int lj = -3; lj <= 3; ++lj)
+          for (int li = -3; li <= 3; ++li) {
+            const int i = si + li, j = sj + lj, k = sk + lk;
+            const bool in = interior(i, j, k);
+            md.push_back(nd[(li + 3) + 7 * ((lj + 3) + 7 * (lk + 3))]);
+            mvol.push_back(in ? (X(i + 1) - X(i - 1)) * (Y(j + 1) - Y(j - 1)) * (Z(k + 1) - Z(k - 1)) / 8.0f * (Z(k) * Z(k)) * hxsin[i]
+                              : 1.0f);
+            mon.push_back(in ? 1 : 0);
+          }
+      const size_t nb = size_t(Mo.ntwin) * Mo.num;
+      for (int m = 0; m < Mo.ntwin; ++m)
+        for (int c = 0; c < 6; ++c) mM.push_back(Mo.mom[c * nb + m + size_t(Mo.ntwin) * q]);
+    }
+    S.G = G;
+    S.nw_f = nwf; S.nw_m = nwm;
+    S.disp = upload(disp); S.rate = upload(rate); S.mrate = upload(mrate);
+    S.nsurf = int(surf_w.size());
+    S.surf_ij = upload(surf_ij); S.surf_q = upload(surf_q); S.surf_w = upload(surf_w);
+    S.nforce = F.num; S.ntwin_f = F.ntwin;
+    S.force_c = upload(fc); S.force_wt = upload(fwt); S.force_on = upload(fon); S.force_F = upload(fF);
+    S.nmom = Mo.num; S.ntwin_m = Mo.ntwin;
+    S.mom_c = upload(mc); S.mom_d = upload(md); S.mom_vol = upload(mvol); S.mom_on = upload(mon);
+    S.mom_M = upload(mM);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "source tables");
+    stf_cap_steps = cap_steps;
+    src_dirty = false;
+    return FWANT_OK;
+  }
+
+  fwant_status prepare_receivers(int end_step) {
+    if (npt <= 0) return FWANT_OK;
+    const int need = end_step / tinv + 1;
+    if (need <= cap && d_rec) return FWANT_OK;
+    drop_graphs();
+    const int ncap = std::max(need + 64, 2 * cap);
+    float* ns = dalloc<float>(size_t(fw::NF) * ncap * npt);
+    if (!ns) return fail(FWANT_ERR_OOM, "seismogram buffer");
+    cudaMemset(ns, 0, size_t(fw::NF) * ncap * npt * sizeof(float));
+    if (d_seis && cap > 0)
+      for (int f = 0; f < fw::NF; ++f)
+        cudaMemcpy(ns + size_t(f) * ncap * npt, d_seis + size_t(f) * cap * npt, size_t(cap) * npt * 4,
+                   cudaMemcpyDeviceToDevice);
+    cudaFree(d_seis);
+    d_seis = ns;
+    cap = ncap;
+    if (!d_rec) {
+      d_rec = dalloc<int>(rec_idx.size());
+      if (!d_rec) return fail(FWANT_ERR_OOM, "receiver index");
+      cudaMemcpy(d_rec, rec_idx.data(), rec_idx.size() * sizeof(int), cudaMemcpyHostToDevice);
+    }
+    return FWANT_OK;
+  }
+
+  fw::StageArgs<float> base_args() const {
+    fw::StageArgs<float> a{};
+    a.g = g;
+    a.lam = lam; a.mu = mu; a.rho = rho;
+    a.xi_x = d_xi; a.eta_y = d_eta; a.zeta_z = d_zeta; a.xsin = d_xsin; a.xcot = d_xcot; a.zc = d_z;
+    for (int ax = 0; ax < 3; ++ax) { a.pA[ax] = prof(ax, 0); a.pB[ax] = prof(ax, 1); a.pD[ax] = prof(ax, 2); }
+    for (int f = 0; f < 6; ++f) a.slab[f] = slab[f];
+    a.ntime = d_ntime;
+    a.src = S;
+    a.src_surface = cfg.src_surface;
+    return a;
+  }
+
+  // One time step: four fused stage launches and the receiver/counter kernel.
+  // Register-set roles: A holds W at the step start (and is the RK "m" register), T is
+  // the RK "t" accumulator; B and C are the stage outputs.  Stage 4 writes W(n+1) into
+  // T in place, after which A and T swap roles.
+  void enqueue_step() {
+    const int X = CYCLE[cycle_pos & 7];
+    fw::StageArgs<float> a = base_args();
+    const int in_of[4] = {rA, rB, rC, rB};
+    const int out_of[4] = {rB, rC, rB, rT};
+    for (int s = 0; s < 4; ++s) {
+      a.win = set(in_of[s]); a.wm = set(rA); a.wout = set(out_of[s]); a.wt = set(rT);
+      for (int f = 0; f < 6; ++f) {
+        if (!slab[f].on) continue;
+        a.ain[f] = aset(f, in_of[s]); a.am[f] = aset(f, rA); a.aout[f] = aset(f, out_of[s]); a.at[f] = aset(f, rT);
+      }
+      a.a = RKA[s] * stept;
+      a.b = RKB[s] * stept;
+      a.stage = s;
+      const int v = (s % 2 == 0) ? X : (~X & 7);
+      const int rk = s == 0 ? 0 : (s == 3 ? 2 : 1);
+      fw::launch_stage_f32(a, v, rk, st);
+    }
+    fw::RecvArgs r{};
+    r.g = g; r.w = set(rT); r.npt = npt; r.idx = d_rec; r.tinv = tinv; r.seismo = d_seis; r.cap = cap;
+    r.ntime = d_ntime;
+    fw::launch_advance_record(r, st);
+    std::swap(rA, rT);
+    cycle_pos = (cycle_pos + 1) & 7;
+    ntime += 1;
+  }
+
+  fwant_status run(int nsteps) {
+    if (nsteps < 0) return fail(FWANT_ERR_INVALID_ARG, "nsteps < 0");
+    if (!have_coord || !have_metric || !have_media)
+      return fail(FWANT_ERR_STATE, "coordinates, metric and media must be set before fwant_run");
+    cudaSetDevice(cfg.device);
+    fwant_status rc = prepare_sources(ntime + nsteps);
+    if (rc != FWANT_OK) return rc;
+    if ((rc = prepare_receivers(ntime + nsteps)) != FWANT_OK) return rc;
+    cudaEventRecord(ev0, st);
+    int left = nsteps;
+    while (left > 0) {
+      if (cycle_pos == 0 && left >= 8) {
+        const int gi = rA == 0 ? 0 : 1;
+        if (!graph[gi]) {
+          const int save_ntime = ntime;
+          cudaGraph_t gr;
+          cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+          if (e != cudaSuccess) return cuda_fail(e, "begin capture");
+          for (int q = 0; q < 8; ++q) enqueue_step();
+          e = cudaStreamEndCapture(st, &gr);
+          if (e != cudaSuccess) return cuda_fail(e, "end capture");
+          ntime = save_ntime;
+          e = cudaGraphInstantiate(&graph[gi], gr, 0);
+          cudaGraphDestroy(gr);
+          if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
+        }
+        cudaError_t e = cudaGraphLaunch(graph[gi], st);
+        if (e != cudaSuccess) return cuda_fail(e, "graph launch");
+        ntime += 8;
+        left -= 8;
+      } else {
+        enqueue_step();
+        left -= 1;
+      }
+    }
+    cudaEventRecord(ev1, st);
+    cudaError_t e = cudaEventSynchronize(ev1);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "run");
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    last_ms = ms;
+    if (npt > 0) nsamp = std::max(nsamp, std::min(ntime / tinv, cap));
+    return FWANT_OK;
+  }
+};
+
+extern "C" {
+
+const char* fwant_version(void) { return "fwant_gb300 0.1 (sm_103a)"; }
+
+fwant_status fwant_create(const fwant_config* cfg, fwant_solver** out) {
+  if (!cfg || !out) return FWANT_ERR_INVALID_ARG;
+  *out = nullptr;
+  fwant_solver* s = new (std::nothrow) fwant_solver;
+  if (!s) return FWANT_ERR_OOM;
+  s->cfg = *cfg;
+  fwant_status rc = s->init();
+  if (rc != FWANT_OK) {
+    std::fprintf(stderr, "fwant_create: %s\n", s->err.c_str());
+    delete s;
+    return rc;
+  }
+  *out = s;
+  return FWANT_OK;
+}
+
+void fwant_destroy(fwant_solver* s) { delete s; }
+
+const char* fwant_last_error(const fwant_solver* s) { return s ? s->err.c_str() : "null handle"; }
+
+fwant_status fwant_set_coord(fwant_solver* s, const float* x, const float* y, const float* z) {
+  if (!s || !x || !y || !z) return FWANT_ERR_INVALID_ARG;
+  cudaSetDevice(s->cfg.device);
+  s->hx.assign(x, x + s->g.nx); s->hy.assign(y, y + s->g.ny); s->hz.assign(z, z + s->g.nz);
+  cudaMemcpy(s->d_x, x, s->g.nx * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(s->d_y, y, s->g.ny * 4, cudaMemcpyHostToDevice);
+  cudaError_t e = cudaMemcpy(s->d_z, z, s->g.nz * 4, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return s->cuda_fail(e, "set_coord");
+  s->have_coord = true;
+  s->src_dirty = true;
+  return FWANT_OK;
+}
+
+fwant_status fwant_set_metric(fwant_solver* s, const float* xsin, const float* xcot, const float* xi_x,
+                              const float* eta_y, const float* zeta_z) {
+  if (!s || !xsin || !xcot || !xi_x || !eta_y || !zeta_z) return FWANT_ERR_INVALID_ARG;
+  cudaSetDevice(s->cfg.device);
+  const auto& g = s->g;
+  s->hxsin.assign(xsin, xsin + g.nx); s->hxcot.assign(xcot, xcot + g.nx);
+  cudaMemcpy(s->d_xsin, xsin, g.nx * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(s->d_xcot, xcot, g.nx * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(s->d_xi, xi_x, g.nx * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(s->d_eta, eta_y, g.ny * 4, cudaMemcpyHostToDevice);
+  cudaError_t e = cudaMemcpy(s->d_zeta, zeta_z, g.nz * 4, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return s->cuda_fail(e, "set_metric");
+  s->have_metric = true;
+  s->src_dirty = true;
+  return FWANT_OK;
+}
+
+fwant_status fwant_compute_metric(fwant_solver* s) {
+  if (!s) return FWANT_ERR_INVALID_ARG;
+  if (!s->have_coord) return s->fail(FWANT_ERR_STATE, "fwant_compute_metric needs fwant_set_coord first");
+  cudaSetDevice(s->cfg.device);
+  const auto& g = s->g;
+  fw::launch_sincot_fp64(g.nx, s->d_x, s->d_xsin, s->d_xcot, s->st);
+  fw::launch_metric_fp64(g.nx, s->d_x, s->d_xi, g.i1, g.i2, s->st);
+  fw::launch_metric_fp64(g.ny, s->d_y, s->d_eta, g.j1, g.j2, s->st);
+  fw::launch_metric_fp64(g.nz, s->d_z, s->d_zeta, g.k1, g.k2, s->st);
+  cudaError_t e = cudaStreamSynchronize(s->st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return s->cuda_fail(e, "compute_metric");
+  s->hxsin.resize(g.nx); s->hxcot.resize(g.nx);
+  cudaMemcpy(s->hxsin.data(), s->d_xsin, g.nx * 4, cudaMemcpyDeviceToHost);
+  cudaMemcpy(s->hxcot.data(), s->d_xcot, g.nx * 4, cudaMemcpyDeviceToHost);
+  s->have_metric = true;
+  s->src_dirty = true;
+  return FWANT_OK;
+}
+
+fwant_status fwant_get_metric(fwant_solver* s, float* xsin, float* xcot, float* xi_x, float* eta_y,
+                              float* zeta_z) {
+  if (!s || !xsin || !xcot || !xi_x || !eta_y || !zeta_z) return FWANT_ERR_INVALID_ARG;
+  cudaSetDevice(s->cfg.device);
+  const auto& g = s->g;
+  cudaMemcpy(xsin, s->d_xsin, g.nx * 4, cudaMemcpyDeviceToHost);
+  cudaMemcpy(xcot, s->d_xcot, g.nx * 4, cudaMemcpyDeviceToHost);
+  cudaMemcpy(xi_x, s->d_xi, g.nx * 4, cudaMemcpyDeviceToHost);
+  cudaMemcpy(eta_y, s->d_eta, g.ny * 4, cudaMemcpyDeviceToHost);
+  cudaError_t e = cudaMemcpy(zeta_z, s->d_zeta, g.nz * 4, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return s->cuda_fail(e, "get_metric");
+  return FWANT_OK;
+}
+
+fwant_status fwant_set_media(fwant_solver* s, const float* lambda, const float* mu, const float* rho) {
+  if (!s || !lambda || !mu || !rho) return FWANT_ERR_INVALID_ARG;
+  cudaSetDevice(s->cfg.device);
+  const auto& g = s->g;
+  const size_t n = size_t(g.nx) * g.ny * g.nz;
+  for (size_t q = 0; q < n; ++q)
+    if (!(rho[q] > 0.0f)) return s->fail(FWANT_ERR_INVALID_ARG, "rho must be > 0 everywhere (ghosts included)");
+  s->h_rho.assign(rho, rho + n);
+  s->put3(s->lam, lambda);
+  s->put3(s->mu, mu);
+  cudaError_t e = s->put3(s->rho, rho);
+  if (e != cudaSuccess) return s->cuda_fail(e, "set_media");
+  s->have_media = true;
+  s->src_dirty = true;
+  return FWANT_OK;
+}
+
+fwant_status fwant_set_pml(fwant_solver* s, const int number[6], const float velocity[6], const float bmax[6],
+                           const float amax[6]) {
+  if (!s || !number || !velocity || !bmax || !amax) return FWANT_ERR_INVALID_ARG;
+  cudaSetDevice(s->cfg.device);
+  return s->set_pml(number, velocity, bmax, amax);
+}
+
+static bool check_idx(const fwant_solver* s, const int* indx, int num) {
+  for (int q = 0; q < num; ++q) {
+    const int i = indx[3 * q], j = indx[3 * q + 1], k = indx[3 * q + 2];
+    if (i < 1 || i > s->g.nx || j < 1 || j > s->g.ny || k < 1 || k > s->g.nz) return false;
+  }
+  return true;
+}
+
+fwant_status fwant_set_forces(fwant_solver* s, int num, int ntwin, const int* indx, const float* shift,
+                              const float* start_time, const float* stf_time, const float* stf_freq,
+                              const float* fx, const float* fy, const float* fz, int stf_id) {
+  if (!s || num < 0 || (num > 0 && (ntwin <= 0 || !indx || !shift || !start_time || !stf_time || !stf_freq || !fx ||
+                                    !fy || !fz)))
+    return FWANT_ERR_INVALID_ARG;
+  if (num > 0 && !check_idx(s, indx, num)) return s->fail(FWANT_ERR_INVALID_ARG, "force index outside the grid");
+  auto& F = s->forces;
+  F.num = num; F.ntwin = num > 0 ? ntwin : 0; F.stf_id = stf_id;
+  F.indx.assign(indx, indx + 3 * num);
+  F.shift.assign(shift, shift + 3 * num);
+  F.t0.assign(start_time, start_time + num);
+  F.stf_time.assign(stf_time, stf_time + F.ntwin);
+  F.stf_freq.assign(stf_freq, stf_freq + F.ntwin);
+  F.fx.assign(fx, fx + size_t(F.ntwin) * num);
+  F.fy.assign(fy, fy + size_t(F.ntwin) * num);
+  F.fz.assign(fz, fz + size_t(F.ntwin) * num);
+  s->src_dirty = true;
+  return FWANT_OK;
+}
+
+fwant_status fwant_set_moments(fwant_solver* s, int num, int ntwin, const int* indx, const float* shift,
+                               const float* start_time, const float* stf_time, const float* stf_freq,
+                               const float* mom, int stf_id) {
+  if (!s || num < 0 || (num > 0 && (ntwin <= 0 || !indx || !shift || !start_time || !stf_time || !stf_freq || !mom)))
+    return FWANT_ERR_INVALID_ARG;
+  if (num > 0 && !check_idx(s, indx, num)) return s->fail(FWANT_ERR_INVALID_ARG, "moment index outside the grid");
+  auto& M = s->moments;
+  M.num = num; M.ntwin = num > 0 ? ntwin : 0; M.stf_id = stf_id;
+  M.indx.assign(indx, indx + 3 * num);
+  M.shift.assign(shift, shift + 3 * num);
+  M.t0.assign(start_time, start_time + num);
+  M.stf_time.assign(stf_time, stf_time + M.ntwin);
+  M.stf_freq.assign(stf_freq, stf_freq + M.ntwin);
+  M.mom.assign(mom, mom + 6 * size_t(M.ntwin) * num);
+  s->src_dirty = true;
+  return FWANT_OK;
+}
+
+fwant_status fwant_set_receivers(fwant_solver* s, int num, const int* indx, int tinv) {
+  if (!s || num < 0 || (num > 0 && !indx)) return FWANT_ERR_INVALID_ARG;
+  for (int q = 0; q < num; ++q) {
+    const int i = indx[3 * q] - 1, j = indx[3 * q + 1] - 1, k = indx[3 * q + 2] - 1;
+    if (i < s->g.i1 || i > s->g.i2 || j < s->g.j1 || j > s->g.j2 || k < s->g.k1 || k > s->g.k2)
+      return s->fail(FWANT_ERR_INVALID_ARG, "receiver outside the interior");
+  }
+  cudaSetDevice(s->cfg.device);
+  s->drop_graphs();
+  s->npt = num;
+  s->tinv = tinv > 0 ? tinv : 1;
+  s->rec_idx.resize(3 * size_t(num));
+  for (int q = 0; q < 3 * num; ++q) s->rec_idx[q] = indx[q] - 1;
+  cudaFree(s->d_rec); s->d_rec = nullptr;
+  cudaFree(s->d_seis); s->d_seis = nullptr;
+  s->cap = 0; s->nsamp = 0;
+  return FWANT_OK;
+}
+
+fwant_status fwant_run(fwant_solver* s, int nsteps) {
+  if (!s) return FWANT_ERR_INVALID_ARG;
+  return s->run(nsteps);
+}
+
+int fwant_reference_steps(int nt) { return nt < 0 ? 0 : 8 * (nt / 8 + 1); }
+
+fwant_status fwant_get_ntime(fwant_solver* s, int* ntime) {
+  if (!s || !ntime) return FWANT_ERR_INVALID_ARG;
+  *ntime = s->ntime;
+  return FWANT_OK;
+}
+
+fwant_status fwant_get_seismo(fwant_solver* s, float* out, int max_samples, int* nsamp) {
+  if (!s || !nsamp || (max_samples > 0 && !out)) return FWANT_ERR_INVALID_ARG;
+  cudaSetDevice(s->cfg.device);
+  const int ns = std::min(s->nsamp, std::max(max_samples, 0));
+  *nsamp = ns;
+  if (ns == 0 || s->npt == 0) return FWANT_OK;
+  for (int f = 0; f < fw::NF; ++f) {
+    cudaError_t e = cudaMemcpy(out + size_t(f) * ns * s->npt, s->d_seis + size_t(f) * s->cap * s->npt,
+                               size_t(ns) * s->npt * 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return s->cuda_fail(e, "get_seismo");
+  }
+  return FWANT_OK;
+}
+
+fwant_status fwant_get_field(fwant_solver* s, int component, float* out) {
+  if (!s || !out || component < 0 || component >= fw::NF) return FWANT_ERR_INVALID_ARG;
+  cudaSetDevice(s->cfg.device);
+  cudaError_t e = s->get3(out, s->set(s->rA) + component * s->g.fstride);
+  if (e != cudaSuccess) return s->cuda_fail(e, "get_field");
+  return FWANT_OK;
+}
+
+fwant_status fwant_set_field(fwant_solver* s, int component, const float* in) {
+  if (!s || !in || component < 0 || component >= fw::NF) return FWANT_ERR_INVALID_ARG;
+  cudaSetDevice(s->cfg.device);
+  const auto& g = s->g;
+  std::vector<float> tmp(in, in + size_t(g.nx) * g.ny * g.nz);
+  for (int k = 0; k < g.nz; ++k)
+    for (int j = 0; j < g.ny; ++j)
+      for (int i = 0; i < g.nx; ++i)
+        if (i < g.i1 || i > g.i2 || j < g.j1 || j > g.j2 || k < g.k1 || k > g.k2)
+          tmp[size_t(i) + size_t(g.nx) * (size_t(j) + size_t(g.ny) * k)] = 0.0f;
+  cudaError_t e = s->put3(s->set(s->rA) + component * g.fstride, tmp.data());
+  if (e != cudaSuccess) return s->cuda_fail(e, "set_field");
+  return FWANT_OK;
+}
+
+fwant_status fwant_check(fwant_solver* s) {
+  if (!s) return FWANT_ERR_INVALID_ARG;
+  cudaSetDevice(s->cfg.device);
+  cudaMemsetAsync(s->d_maxbits, 0, sizeof(unsigned int), s->st);
+  fw::launch_maxabs(s->g, s->set(s->rA), s->d_maxbits, s->st);
+  unsigned int bits = 0;
+  cudaMemcpyAsync(&bits, s->d_maxbits, sizeof(bits), cudaMemcpyDeviceToHost, s->st);
+  cudaError_t e = cudaStreamSynchronize(s->st);
+  if (e != cudaSuccess) return s->cuda_fail(e, "check");
+  float v;
+  std::memcpy(&v, &bits, sizeof(v));
+  if (!(v < 3.4028234663852886e38f)) {  // huge(1.0), NaN and Inf all fail this test
+    char b[128];
+    std::snprintf(b, sizeof(b), "overflow: max |field| = %g at ntime %d", double(v), s->ntime);
+    return s->fail(FWANT_ERR_NUMERIC_OVERFLOW, b);
+  }
+  return FWANT_OK;
+}
+
+fwant_status fwant_last_run_ms(fwant_solver* s, double* ms) {
+  if (!s || !ms) return FWANT_ERR_INVALID_ARG;
+  *ms = s->last_ms;
+  return FWANT_OK;
+}
+
+}  // extern "C"

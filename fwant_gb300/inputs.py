@@ -1,0 +1,266 @@
+"""Seeded synthetic inputs in the reference's layouts.
+
+The reference's preprocessors write per-rank NetCDF files that the solver reads
+(coord, metric, media, source, station).  No input data ships with the reference, so
+the workloads are generated here with the same arithmetic the preprocessors use where
+it matters for the solver:
+
+* coordinates: seis3d_grid.F90:89-149 (uniform step or explicit list, degrees to
+  radians, ghosts extrapolated linearly), in FP32 like the reference;
+* sources: seis3d_source.F90:75-117 (nearest node, fractional shift, surface
+  sources pinned to k = nk2);
+* receivers: seis3d_station.F90:64-105 (nearest node; surface receivers on k = nk2);
+* media: values sampled at the nodes of a 1-D layered model (Vs = Vp/1.73, Gardner
+  density) with an optional seeded Gaussian-correlated perturbation.  The effective
+  medium averaging of seis3d_media is not applied (both the solver and the oracle read
+  the same node values).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+LENFD = 3
+R_EARTH_KM = 6371.0
+
+
+@dataclass
+class Model:
+    ni: int
+    nj: int
+    nk: int
+    stept: float
+    x: np.ndarray   # (nx,) colatitude, rad
+    y: np.ndarray   # (ny,) longitude, rad
+    z: np.ndarray   # (nz,) radius, m
+    lam: np.ndarray  # (nx, ny, nz) Fortran-ordered semantics (index [i,j,k])
+    mu: np.ndarray
+    rho: np.ndarray
+    pml_number: np.ndarray = field(default_factory=lambda: np.zeros(6, np.int32))
+    pml_velocity: np.ndarray = field(default_factory=lambda: np.zeros(6, np.float32))
+    pml_bmax: np.ndarray = field(default_factory=lambda: np.ones(6, np.float32))
+    pml_amax: np.ndarray = field(default_factory=lambda: np.zeros(6, np.float32))
+    free_surface: bool = True
+    # forces: 1-based Fortran indices (num,3), shifts (num,3), start times (num,),
+    # windows stf_time/stf_freq (ntwin,), amplitudes (num, ntwin)
+    force_indx: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), np.int32))
+    force_shift: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), np.float32))
+    force_t0: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    stf_time: np.ndarray = field(default_factory=lambda: np.zeros(1, np.float32))
+    stf_freq: np.ndarray = field(default_factory=lambda: np.zeros(1, np.float32))
+    fx: np.ndarray = field(default_factory=lambda: np.zeros((0, 1), np.float32))
+    fy: np.ndarray = field(default_factory=lambda: np.zeros((0, 1), np.float32))
+    fz: np.ndarray = field(default_factory=lambda: np.zeros((0, 1), np.float32))
+    stf_id: int = 200
+    recv_indx: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), np.int32))
+    recv_tinv: int = 1
+    name: str = ""
+
+    @property
+    def shape(self):
+        return (self.ni + 6, self.nj + 6, self.nk + 6)
+
+    @property
+    def npoints(self):
+        return self.ni * self.nj * self.nk
+
+
+def grid_coords(n: int, step: float | None, origin: float, values: np.ndarray | None, to_si: float,
+                degrees: bool, top_anchored: bool = False) -> np.ndarray:
+    """One axis of read_grid_coord (seis3d_grid.F90:89-149) for a single domain."""
+    nx = n + 2 * LENFD
+    g = np.zeros(nx, np.float32)
+    i1 = LENFD  # 0-based index of the first interior point
+    if values is None:
+        idx = np.arange(nx)
+        if top_anchored:  # gz(k) = (k - num_z + LenFD)*dh + rmax
+            g[:] = ((idx - (nx - 1) + LENFD).astype(np.float32) * np.float32(step) + np.float32(origin))
+        else:             # gx(i) = (i - ni1)*dh + x0
+            g[:] = ((idx - i1).astype(np.float32) * np.float32(step) + np.float32(origin))
+    else:
+        v = np.asarray(values, np.float32)
+        assert v.size == n
+        g[i1:i1 + n] = v
+    if degrees:
+        g = (g.astype(np.float64) / 180.0 * np.pi).astype(np.float32)
+    else:
+        g = (g * np.float32(to_si)).astype(np.float32)
+    i2 = i1 + n - 1
+    for q in range(1, LENFD + 1):
+        g[i1 - q] = np.float32(np.float32(g[i1 - q + 1] + g[i1]) - g[i1 + 1])
+        g[i2 + q] = np.float32(np.float32(g[i2 + q - 1] + g[i2]) - g[i2 - 1])
+    return g
+
+
+def stretched_depths_km(nk: int, top_km: float = 0.5, bottom_km: float = 2.0) -> np.ndarray:
+    """Radii list (km, bottom to top) with spacing growing geometrically from top_km at
+    the surface to bottom_km at the bottom (the `<z` list form of the grid input)."""
+    if nk < 2:
+        raise ValueError("nk >= 2")
+    ratio = (bottom_km / top_km) ** (1.0 / max(nk - 2, 1))
+    h = top_km * ratio ** np.arange(nk - 1)  # spacings from the top down
+    depth = np.concatenate([[0.0], np.cumsum(h)])  # depth of node from the top
+    r = R_EARTH_KM - depth[::-1]  # bottom to top
+    return r.astype(np.float32)
+
+
+def layered_media(x, y, z, seed: int, vp_top=5.8, vp_bottom=8.0, nlayers=4, perturb: float = 0.0,
+                  corr_km: float = 10.0):
+    """Node-sampled 1-D layered medium (Vp in km/s from vp_top to vp_bottom across
+    seeded interfaces), Vs = Vp/1.73, rho = 1.741 Vp^0.25 g/cm^3, optional Gaussian-
+    correlated relative perturbation of Vp and Vs scaled to max |dv| = perturb.
+    Returns lam, mu, rho (SI) with shape (nx, ny, nz)."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = x.size, y.size, z.size
+    ztop = float(z[nz - 1 - LENFD])
+    depth_km = (ztop - z.astype(np.float64)) / 1000.0
+    dmax = max(float(depth_km[LENFD]), 1e-3)
+    iface = np.sort(rng.uniform(0.05, 0.9, nlayers - 1)) * dmax
+    vps = np.linspace(vp_top, vp_bottom, nlayers)
+    layer = np.searchsorted(iface, depth_km, side="right")
+    vp1 = vps[np.clip(layer, 0, nlayers - 1)]  # (nz,)
+    vp = np.broadcast_to(vp1[None, None, :], (nx, ny, nz)).astype(np.float64).copy()
+    vs = vp / 1.73
+    if perturb > 0.0:
+        dv = gaussian_field((nx, ny, nz), x, y, z, corr_km, rng)
+        dv *= perturb / max(np.abs(dv).max(), 1e-30)
+        vp *= 1.0 + dv
+        vs *= 1.0 + dv
+    rho = 1.741 * vp ** 0.25 * 1000.0          # kg/m^3
+    vp_ms, vs_ms = vp * 1000.0, vs * 1000.0
+    mu = rho * vs_ms ** 2
+    lam = rho * vp_ms ** 2 - 2.0 * mu
+    return lam.astype(np.float32), mu.astype(np.float32), rho.astype(np.float32)
+
+
+def gaussian_field(shape, x, y, z, corr_km, rng):
+    """Zero-mean Gaussian random field with a Gaussian correlation of length corr_km,
+    filtered in the Fourier domain on the (roughly uniform) node spacing."""
+    nx, ny, nz = shape
+    r_top = float(z[-1 - LENFD])
+    dx = abs(float(x[LENFD + 1] - x[LENFD])) * r_top / 1000.0
+    dy = abs(float(y[LENFD + 1] - y[LENFD])) * r_top / 1000.0 * np.sin(float(x[nx // 2]))
+    dz = abs(float(np.mean(np.diff(z[LENFD:-LENFD])))) / 1000.0
+    noise = rng.standard_normal(shape)
+    kx = np.fft.fftfreq(nx, d=dx)[:, None, None]
+    ky = np.fft.fftfreq(ny, d=dy)[None, :, None]
+    kz = np.fft.rfftfreq(nz, d=dz)[None, None, :]
+    filt = np.exp(-(np.pi * corr_km) ** 2 * (kx ** 2 + ky ** 2 + kz ** 2) / 2.0)
+    f = np.fft.irfftn(np.fft.rfftn(noise) * filt, s=shape)
+    f -= f.mean()
+    return f / max(f.std(), 1e-30)
+
+
+def locate(coord: np.ndarray, v: float) -> int:
+    """minloc(abs(coord - v)) as a 1-based index (first minimum wins, like Fortran)."""
+    return int(np.argmin(np.abs(coord - np.float32(v)))) + 1
+
+
+def source_shift(coord: np.ndarray, i: int, v: float) -> float:
+    """Fractional offset of a source from its node (seis3d_source.F90:100-116)."""
+    c = coord
+    i0 = i - 1
+    if v > c[i0]:
+        return float(np.float32((np.float32(v) - c[i0]) / (c[i0 + 1] - c[i0])))
+    return float(np.float32((np.float32(v) - c[i0]) / (c[i0] - c[i0 - 1])))
+
+
+def make_model(ni, nj, nk, seed=0, dh_km=1.0, theta_c_deg=50.0, phi_c_deg=100.0, z_top_km=0.5,
+               z_bottom_km=2.0, npml=12, free_surface=True, nrecv=16, cfl=0.5, perturb=0.0,
+               source="surface", force=(0.0, 0.0, 1.0e15), fc=0.2, t0=7.5, name="") -> Model:
+    """A seeded model of the BASELINE workloads: 1 km horizontal spacing (in degrees at
+    the top radius), vertical spacing stretched from z_top_km to z_bottom_km, layered
+    medium, CFS-PML of npml cells on x1 x2 y1 y2 z1 (+z2 without a free surface), one
+    Ricker point force and nrecv seeded surface receivers."""
+    rng = np.random.default_rng(seed + 7919)
+    dh_deg = dh_km / R_EARTH_KM * 180.0 / np.pi
+    theta0 = theta_c_deg - dh_deg * (ni - 1) / 2.0
+    phi0 = phi_c_deg - dh_deg * (nj - 1) / 2.0
+    x = grid_coords(ni, dh_deg, theta0, None, 1.0, degrees=True)
+    y = grid_coords(nj, dh_deg, phi0, None, 1.0, degrees=True)
+    zl = stretched_depths_km(nk, z_top_km, z_bottom_km)
+    z = grid_coords(nk, None, 0.0, zl, 1000.0, degrees=False)
+    lam, mu, rho = layered_media(x, y, z, seed, perturb=perturb)
+    vpmax = float(np.sqrt((lam + 2 * mu) / rho)[LENFD:-LENFD, LENFD:-LENFD, LENFD:-LENFD].max())
+    r_top = float(z[-1 - LENFD])
+    hmin = min(float(np.min(np.diff(z[LENFD:-LENFD]))), dh_km * 1000.0 * float(np.sin(x[LENFD:-LENFD]).min()),
+               dh_km * 1000.0)
+    stept = cfl * hmin / vpmax
+    m = Model(ni, nj, nk, float(np.float32(stept)), x, y, z, lam, mu, rho, name=name)
+    m.free_surface = free_surface
+    faces = [npml, npml, npml, npml, npml, 0 if free_surface else npml]
+    m.pml_number = np.array(faces, np.int32)
+    m.pml_velocity = np.full(6, 8000.0, np.float32)
+    m.pml_bmax = np.full(6, 2.0, np.float32)
+    m.pml_amax = np.full(6, np.float32(np.pi * fc), np.float32)
+    nx, ny, nz = ni + 6, nj + 6, nk + 6
+    ic, jc = LENFD + ni // 2 + 1, LENFD + nj // 2 + 1  # 1-based centre node
+    if source == "surface":
+        kc = nk + LENFD  # nk2 (1-based)
+        shift = (0.0, 0.0, 0.0)
+    elif source == "buried":
+        kc = nk + LENFD - max(6, nk // 4)
+        # an off-node position to exercise the fractional shift
+        xs = float(x[ic - 1]) + 0.3 * float(x[ic] - x[ic - 1])
+        ys = float(y[jc - 1]) - 0.2 * float(y[jc - 1] - y[jc - 2])
+        zs = float(z[kc - 1]) + 0.25 * float(z[kc] - z[kc - 1])
+        ic, jc, kc = locate(x, xs), locate(y, ys), locate(z, zs)
+        shift = (source_shift(x, ic, xs), source_shift(y, jc, ys), source_shift(z, kc, zs))
+    else:
+        raise ValueError(source)
+    m.force_indx = np.array([[ic, jc, kc]], np.int32)
+    m.force_shift = np.array([shift], np.float32)
+    m.force_t0 = np.zeros(1, np.float32)
+    m.stf_time = np.array([t0], np.float32)
+    m.stf_freq = np.array([fc], np.float32)
+    m.fx = np.array([[force[0]]], np.float32)
+    m.fy = np.array([[force[1]]], np.float32)
+    m.fz = np.array([[force[2]]], np.float32)
+    m.stf_id = 200
+    # receivers on the surface away from the PML
+    lo_i, hi_i = LENFD + npml + 3, LENFD + ni - npml - 2
+    lo_j, hi_j = LENFD + npml + 3, LENFD + nj - npml - 2
+    if hi_i < lo_i:
+        lo_i, hi_i = LENFD + 1, LENFD + ni
+    if hi_j < lo_j:
+        lo_j, hi_j = LENFD + 1, LENFD + nj
+    ri = rng.integers(lo_i, hi_i + 1, nrecv)
+    rj = rng.integers(lo_j, hi_j + 1, nrecv)
+    rk = np.full(nrecv, nk + LENFD)
+    m.recv_indx = np.stack([ri, rj, rk], axis=1).astype(np.int32)
+    m.recv_tinv = 1
+    return m
+
+
+def config_c1(seed=0, **kw) -> Model:
+    """Config 1: 100x100x60, 1 km horizontal, 0.5-2 km vertical, layered Vp 5.8-8.0,
+    12-cell PML on 5 faces, free surface, vertical Ricker force (0.2 Hz) at the surface
+    centre, 16 seeded surface receivers, CFL 0.5 (flat top)."""
+    return make_model(100, 100, 60, seed=seed, name="C1 100x100x60", **kw)
+
+
+def config_c2(seed=0, component=2, **kw) -> Model:
+    """Config 2: 400x400x200 with a +/-5% Gaussian-correlated (10 km) Vp/Vs perturbation,
+    64 surface receivers; component selects the force direction (0 Fx, 1 Fy, 2 Fz)."""
+    f = [0.0, 0.0, 0.0]
+    f[component] = 1.0e15
+    return make_model(400, 400, 200, seed=seed, nrecv=64, perturb=0.05, force=tuple(f),
+                      name=f"C2 400x400x200 F{'xyz'[component]}", **kw)
+
+
+def attach(solver, m: Model, metric: dict | None = None):
+    """Feed a Model to a Solver (or any object with the same set-up methods)."""
+    solver.set_coord(m.x, m.y, m.z)
+    if metric is None:
+        solver.compute_metric()
+    else:
+        solver.set_metric(metric["xsin"], metric["xcot"], metric["xi_x"], metric["eta_y"], metric["zeta_z"])
+    solver.set_media(m.lam, m.mu, m.rho)
+    solver.set_pml(m.pml_number, m.pml_velocity, m.pml_bmax, m.pml_amax)
+    if m.force_indx.shape[0] > 0:
+        solver.set_forces(m.force_indx, m.force_shift, m.force_t0, m.stf_time, m.stf_freq, m.fx, m.fy, m.fz,
+                          m.stf_id)
+    if m.recv_indx.shape[0] > 0:
+        solver.set_receivers(m.recv_indx, m.recv_tinv)
+    return solver

@@ -1,0 +1,176 @@
+/*
+ * fwant_gb300 — C ABI of the GB300 forward solver for FWANT (seis3d_wave).
+ *
+ * The reference solver is the Fortran program `seis3d_wave_mpi`
+ * (code/srcF/seis3d_wave_8op_p3.F90).  It has no library API: its modules read
+ * per-rank NetCDF inputs into module globals and run the time loop.  Each entry point
+ * below replaces one of those import/run/export steps, named on its line as
+ * file:line of the reference (paths relative to the reference project root).
+ *
+ * Conventions
+ *  - Every call returns fwant_status; fwant_last_error() gives the message.  No
+ *    call aborts the process (the reference stops or calls MPI_ABORT instead).
+ *  - Arrays are plain host pointers.  Each call copies what it needs; the handle
+ *    keeps no caller pointer after it returns.
+ *  - 3-D arrays are Fortran-ordered (i fastest, then j, then k) and include the
+ *    LenFD = 3 ghost cells on every side: nx = ni+6, ny = nj+6, nz = nk+6
+ *    (code/srcF/mod_para.F90:79-82).  1-D coordinate and metric arrays have
+ *    nx, ny or nz entries.
+ *  - Grid indices (sources, receivers, snapshots) are the reference's 1-based
+ *    Fortran indices including ghosts: the first interior point is 4.
+ *  - Wavefield components are numbered in the receiver output order of
+ *    io_seismo_put (code/srcF/mod_io.F90:461-497):
+ *      0 Vx, 1 Vy, 2 Vz, 3 Txx, 4 Tyy, 5 Tzz, 6 Txy, 7 Txz, 8 Tyz.
+ *  - One host thread per handle.  Handles are independent and may live on
+ *    different devices.
+ */
+#ifndef FWANT_GB300_H
+#define FWANT_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum fwant_status {
+  FWANT_OK = 0,
+  FWANT_ERR_INVALID_ARG = 1,
+  FWANT_ERR_OOM = 2,
+  FWANT_ERR_CUDA = 3,
+  FWANT_ERR_NUMERIC_OVERFLOW = 4, /* macdrp_check found Inf/NaN/huge (mod_macdrp.F90:228-264) */
+  FWANT_ERR_TIMEOUT = 5,
+  FWANT_ERR_STATE = 6 /* call made in the wrong order (e.g. run before set_media) */
+} fwant_status;
+
+/* Storage kind of the wavefield registers (W, m, t) and the PML memory variables.
+ * Arithmetic is always FP32 for the first three; FP64 stores and computes in double
+ * (the FP64 run of the same solver used as the precision reference). */
+typedef enum fwant_storage {
+  FWANT_STORAGE_FP32 = 0,
+  FWANT_STORAGE_BF16 = 1,
+  FWANT_STORAGE_FP16 = 2,
+  FWANT_STORAGE_FP64 = 3
+} fwant_storage;
+
+/* Source time function ids of src_stf/src_svf (code/srcF/mod_src.F90:48-57). */
+enum {
+  FWANT_SVF_BELL = 100,
+  FWANT_SVF_TRIANGLE = 110,
+  FWANT_SVF_GAUSS = 120,
+  FWANT_STF_RICKER = 200,
+  FWANT_STF_GAUSS = 220,
+  FWANT_STF_BELL = 230,
+  FWANT_STF_STEP = 240,
+  FWANT_STF_DELTA = 250
+};
+
+typedef struct fwant_config {
+  int ni, nj, nk;      /* interior size: keys ni nj nk (code/srcF/mod_para.F90:75-77) */
+  double stept;        /* time step in s: key stept (code/srcF/mod_para.F90:84) */
+  int free_surface;    /* 1: top face k=nk2 is the traction-free surface (freenode) */
+  int src_surface;     /* 1: forces on the surface act as traction (-DSrcSurface) */
+  int storage;         /* fwant_storage */
+  int device;          /* CUDA device ordinal */
+} fwant_config;
+
+typedef struct fwant_solver fwant_solver;
+
+/* Library version string. */
+const char* fwant_version(void);
+
+/* Allocate a solver: replaces para_init + macdrp_init
+ * (code/srcF/mod_para.F90:70-88, code/srcF/mod_macdrp.F90:124-218). */
+fwant_status fwant_create(const fwant_config* cfg, fwant_solver** out);
+
+/* Release every device and host resource of the handle (macdrp_destroy,
+ * code/srcF/mod_macdrp.F90:219-227).  Accepts NULL. */
+void fwant_destroy(fwant_solver* s);
+
+/* Message of the last failing call on this handle ("" if none). */
+const char* fwant_last_error(const fwant_solver* s);
+
+/* Coordinates x=theta (rad), y=phi (rad), z=r (m), nx/ny/nz entries including the
+ * ghost cells: grid_coord_import (code/srcF/mod_grid.F90:85-94). */
+fwant_status fwant_set_coord(fwant_solver* s, const float* x, const float* y, const float* z);
+
+/* Metric arrays as stored in metric_mpi*.nc: grid_metric_import
+ * (code/srcF/mod_grid.F90:95-114).  xsin, xcot, xi_x have nx entries; eta_y ny; zeta_z nz. */
+fwant_status fwant_set_metric(fwant_solver* s, const float* xsin, const float* xcot,
+                              const float* xi_x, const float* eta_y, const float* zeta_z);
+
+/* Compute the metric from the coordinates on the device in FP64 and round to FP32:
+ * replaces the seis3d_metric preprocessor (code/srcF/seis3d_metric.F90:83-112). */
+fwant_status fwant_compute_metric(fwant_solver* s);
+
+/* Copy the metric currently in use back to the host (same shapes as fwant_set_metric). */
+fwant_status fwant_get_metric(fwant_solver* s, float* xsin, float* xcot, float* xi_x,
+                              float* eta_y, float* zeta_z);
+
+/* Lame parameters and density, (nx,ny,nz) each: media_import
+ * (code/srcF/mod_media.F90:76-96). */
+fwant_status fwant_set_media(fwant_solver* s, const float* lambda, const float* mu,
+                             const float* rho);
+
+/* CFS-PML on the faces x1 x2 y1 y2 z1 z2 (6 entries each): keys abs_number,
+ * abs_velocity, CFS_bmax, CFS_amax of abs_init (code/srcF/mod_abs_npml.F90:135-616).
+ * number[f] <= 0 disables face f.  A PML on z2 turns the free surface off
+ * (code/srcF/mod_abs_npml.F90:182-184).  Call after fwant_set_coord. */
+fwant_status fwant_set_pml(fwant_solver* s, const int number[6], const float velocity[6],
+                           const float bmax[6], const float amax[6]);
+
+/* Force sources as stored in source_mpi*.nc: src_import (code/srcF/mod_src.F90:148-202).
+ * indx, shift: 3 x num (column-major); start_time: num; stf_time, stf_freq: ntwin;
+ * fx, fy, fz: ntwin x num (column-major); stf_id: one of the FWANT_STF_* ids. */
+fwant_status fwant_set_forces(fwant_solver* s, int num, int ntwin, const int* indx,
+                              const float* shift, const float* start_time,
+                              const float* stf_time, const float* stf_freq, const float* fx,
+                              const float* fy, const float* fz, int stf_id);
+
+/* Moment-tensor sources: src_import (code/srcF/mod_src.F90:155-173).
+ * mom holds Mxx Myy Mzz Mxy Mxz Myz, each ntwin x num, one after the other. */
+fwant_status fwant_set_moments(fwant_solver* s, int num, int ntwin, const int* indx,
+                               const float* shift, const float* start_time,
+                               const float* stf_time, const float* stf_freq, const float* mom,
+                               int stf_id);
+
+/* Receivers at grid nodes, sampled every tinv steps: io_pt_import
+ * (code/srcF/mod_io.F90:160-176); indx is 3 x num (1-based). */
+fwant_status fwant_set_receivers(fwant_solver* s, int num, const int* indx, int tinv);
+
+/* Advance nsteps time steps of the 8-step F/B LDDRK4 cycle
+ * (code/srcF/seis3d_wave_8op_p3.F90:92-594).  Asynchronous device work is finished
+ * before the call returns. */
+fwant_status fwant_run(fwant_solver* s, int nsteps);
+
+/* Number of steps the reference executes for a configured nt: the exit test runs only
+ * at the start of each 8-step block (code/srcF/seis3d_wave_8op_p3.F90:92-95). */
+int fwant_reference_steps(int nt);
+
+/* Completed time steps (the reference's ntime). */
+fwant_status fwant_get_ntime(fwant_solver* s, int* ntime);
+
+/* Receiver seismograms recorded so far: out is [9][nsamp][num] (component, sample,
+ * receiver), i.e. per component the (num_pt, time) layout of seismo_mpi*.nc
+ * (code/srcF/mod_nfseis.F90:81-126).  Writes at most max_samples samples; *nsamp gets
+ * the number written. */
+fwant_status fwant_get_seismo(fwant_solver* s, float* out, int max_samples, int* nsamp);
+
+/* Whole component including ghosts, (nx,ny,nz): the data of a restart file
+ * (io_rest_export, code/srcF/mod_io.F90:342-405). */
+fwant_status fwant_get_field(fwant_solver* s, int component, float* out);
+
+/* Overwrite a component, (nx,ny,nz): io_rest_import (code/srcF/mod_io.F90:406-427).
+ * Only the interior is taken; ghosts stay zero. */
+fwant_status fwant_set_field(fwant_solver* s, int component, const float* in);
+
+/* Overflow check of the nine components: macdrp_check (code/srcF/mod_macdrp.F90:228-264).
+ * Returns FWANT_ERR_NUMERIC_OVERFLOW when a value is NaN, Inf or >= huge(1.0). */
+fwant_status fwant_check(fwant_solver* s);
+
+/* Device time of the last fwant_run call in milliseconds (CUDA events). */
+fwant_status fwant_last_run_ms(fwant_solver* s, double* ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FWANT_GB300_H */

@@ -1,0 +1,239 @@
+"""ORACLE — test infrastructure, never the product.
+
+ctypes binding of the CPU restatement in fwant_oracle.cpp.  `Oracle` has the same
+set-up methods as `fwant_gb300.Solver`, so a test feeds both from one Model.  Only the
+tests, `__graft_entry__.smoke()` and the `cpu_baseline` leg of `bench.py` use it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "fwant_oracle.cpp")
+LIB = os.path.join(HERE, "_build", "libfwant_oracle.so")
+COMPONENTS = ("Vx", "Vy", "Vz", "Txx", "Tyy", "Tzz", "Txy", "Txz", "Tyz")
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_fp = C.POINTER(C.c_float)
+_vp = C.c_void_p
+_SIGS = [
+    ("orc_create", _vp, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int]),
+    ("orc_destroy", None, [_vp]),
+    ("orc_set_threads", C.c_int, [C.c_int]),
+    ("orc_set_coord", None, [_vp, _dp, _dp, _dp]),
+    ("orc_set_metric", None, [_vp, _dp, _dp, _dp, _dp, _dp]),
+    ("orc_set_media", None, [_vp, _dp, _dp, _dp]),
+    ("orc_set_pml", C.c_int, [_vp, _ip, _dp, _dp, _dp]),
+    ("orc_set_srcsurface", None, [_vp, C.c_int]),
+    ("orc_set_forces", None, [_vp, C.c_int, C.c_int, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.c_int]),
+    ("orc_set_moments", None, [_vp, C.c_int, C.c_int, _ip, _dp, _dp, _dp, _dp, _dp, C.c_int]),
+    ("orc_set_receivers", None, [_vp, C.c_int, _ip, C.c_int]),
+    ("orc_run", C.c_int, [_vp, C.c_int]),
+    ("orc_ntime", C.c_int, [_vp]),
+    ("orc_freenode", C.c_int, [_vp]),
+    ("orc_get_field", None, [_vp, C.c_int, _dp]),
+    ("orc_set_field", None, [_vp, C.c_int, _dp]),
+    ("orc_get_pml_profile", None, [_vp, C.c_int, _dp, _dp, _dp]),
+    ("orc_get_seismo", C.c_int, [_vp, _dp, C.c_int]),
+    ("orc_last_error", C.c_char_p, [_vp]),
+    ("orc_stf", C.c_double, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double, C.c_int]),
+    ("orc_norm_delt", C.c_int, [C.c_double, C.c_double, C.c_double, _dp]),
+    ("orc_pml_R", C.c_double, [C.c_int]),
+    ("orc_metric", None, [C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, _fp, _fp, _fp, _fp, _fp]),
+    ("orc_op", C.c_double, [C.c_int, C.c_int, _dp, C.c_int]),
+]
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile the oracle (g++, OpenMP, no FP contraction)."""
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-o", LIB, SRC]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stderr}")
+    return LIB
+
+
+_LIB = None
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB):
+            build()
+        L = C.CDLL(LIB)
+        for name, res, args in _SIGS:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def _d(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(-1))
+
+
+def _p(a, t=C.c_double):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+def set_threads(n: int) -> int:
+    return lib().orc_set_threads(int(n))
+
+
+class Oracle:
+    """CPU restatement of seis3d_wave; dbl=True gives the FP64 (-DDataTypeDouble) solver."""
+
+    def __init__(self, ni, nj, nk, stept, free_surface=True, src_surface=True, dbl=False):
+        self._L = lib()
+        self._h = self._L.orc_create(int(ni), int(nj), int(nk), float(stept), int(bool(free_surface)), int(bool(dbl)))
+        self._L.orc_set_srcsurface(self._h, int(bool(src_surface)))
+        self.ni, self.nj, self.nk = int(ni), int(nj), int(nk)
+        self.nx, self.ny, self.nz = self.ni + 6, self.nj + 6, self.nk + 6
+        self.shape = (self.nx, self.ny, self.nz)
+        self.num_pt = 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.orc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _keep(self, *a):
+        self._refs = a
+
+    def set_coord(self, x, y, z):
+        a = [_d(x), _d(y), _d(z)]
+        self._L.orc_set_coord(self._h, *[_p(v) for v in a])
+        self.x, self.y, self.z = [np.asarray(v, np.float32) for v in (x, y, z)]
+
+    def set_metric(self, xsin, xcot, xi_x, eta_y, zeta_z):
+        a = [_d(v) for v in (xsin, xcot, xi_x, eta_y, zeta_z)]
+        self._L.orc_set_metric(self._h, *[_p(v) for v in a])
+
+    def compute_metric(self):
+        m = metric(self.x, self.y, self.z)
+        self.set_metric(m["xsin"], m["xcot"], m["xi_x"], m["eta_y"], m["zeta_z"])
+
+    def set_media(self, lam, mu, rho):
+        a = [_d(np.asarray(v, np.float32).reshape(-1, order="F")) for v in (lam, mu, rho)]
+        self._L.orc_set_media(self._h, *[_p(v) for v in a])
+
+    def set_pml(self, number, velocity, bmax, amax):
+        n = np.ascontiguousarray(np.asarray(number, np.int32).reshape(6))
+        a = [_d(np.asarray(v, np.float32)) for v in (velocity, bmax, amax)]
+        rc = self._L.orc_set_pml(self._h, _p(n, C.c_int), *[_p(v) for v in a])
+        if rc:
+            raise RuntimeError(self._L.orc_last_error(self._h).decode())
+
+    def set_forces(self, indx, shift, start_time, stf_time, stf_freq, fx, fy, fz, stf_id=200):
+        indx = np.ascontiguousarray(np.asarray(indx, np.int32).reshape(-1, 3))
+        num = indx.shape[0]
+        ntwin = np.asarray(stf_time).size
+        a = [_d(np.asarray(shift, np.float32).reshape(-1, 3)), _d(np.asarray(start_time, np.float32)),
+             _d(np.asarray(stf_time, np.float32)), _d(np.asarray(stf_freq, np.float32))]
+        f = [_d(np.asarray(q, np.float32).reshape(num, ntwin)) for q in (fx, fy, fz)]
+        self._L.orc_set_forces(self._h, num, ntwin, _p(indx, C.c_int), *[_p(v) for v in a], *[_p(v) for v in f],
+                               int(stf_id))
+
+    def set_moments(self, indx, shift, start_time, stf_time, stf_freq, mom, stf_id=200):
+        indx = np.ascontiguousarray(np.asarray(indx, np.int32).reshape(-1, 3))
+        num = indx.shape[0]
+        ntwin = np.asarray(stf_time).size
+        a = [_d(np.asarray(shift, np.float32).reshape(-1, 3)), _d(np.asarray(start_time, np.float32)),
+             _d(np.asarray(stf_time, np.float32)), _d(np.asarray(stf_freq, np.float32)),
+             _d(np.asarray(mom, np.float32).reshape(6, num, ntwin))]
+        self._L.orc_set_moments(self._h, num, ntwin, _p(indx, C.c_int), *[_p(v) for v in a], int(stf_id))
+
+    def set_receivers(self, indx, tinv=1):
+        indx = np.ascontiguousarray(np.asarray(indx, np.int32).reshape(-1, 3))
+        self.num_pt = indx.shape[0]
+        self._L.orc_set_receivers(self._h, self.num_pt, _p(indx, C.c_int), int(tinv))
+        self._rec = indx
+
+    def run(self, nsteps):
+        if self._L.orc_run(self._h, int(nsteps)):
+            raise RuntimeError(self._L.orc_last_error(self._h).decode())
+
+    @property
+    def ntime(self):
+        return self._L.orc_ntime(self._h)
+
+    @property
+    def free_surface(self):
+        return bool(self._L.orc_freenode(self._h))
+
+    def get_field(self, component):
+        c = COMPONENTS.index(component) if isinstance(component, str) else int(component)
+        out = np.zeros(self.nx * self.ny * self.nz)
+        self._L.orc_get_field(self._h, c, _p(out))
+        return out.reshape(self.shape, order="F")
+
+    def set_field(self, component, values):
+        c = COMPONENTS.index(component) if isinstance(component, str) else int(component)
+        a = _d(np.asarray(values).reshape(-1, order="F"))
+        self._L.orc_set_field(self._h, c, _p(a))
+
+    def pml_profile(self, axis):
+        n = (self.nx, self.ny, self.nz)[axis]
+        A, B, D = np.zeros(n), np.zeros(n), np.zeros(n)
+        self._L.orc_get_pml_profile(self._h, axis, _p(A), _p(B), _p(D))
+        return A, B, D
+
+    def get_seismo(self, max_samples=None):
+        if max_samples is None:
+            max_samples = self.ntime + 1
+        out = np.zeros(9 * max(max_samples, 1) * max(self.num_pt, 1))
+        n = self._L.orc_get_seismo(self._h, _p(out), int(max_samples))
+        return out[: 9 * n * self.num_pt].reshape(9, n, self.num_pt)
+
+
+def metric(x, y, z):
+    """seis3d_metric restated in SP (seis3d_metric.F90:83-112)."""
+    x, y, z = [np.ascontiguousarray(np.asarray(v, np.float32)) for v in (x, y, z)]
+    out = [np.zeros(x.size, np.float32), np.zeros(x.size, np.float32), np.zeros(x.size, np.float32),
+           np.zeros(y.size, np.float32), np.zeros(z.size, np.float32)]
+    lib().orc_metric(x.size, y.size, z.size, _p(x, C.c_float), _p(y, C.c_float), _p(z, C.c_float),
+                     *[_p(v, C.c_float) for v in out])
+    return dict(zip(("xsin", "xcot", "xi_x", "eta_y", "zeta_z"), out))
+
+
+def stf(t, t0, f0, stf_id=200, ntime=1, stept=0.01, dbl=False):
+    return lib().orc_stf(0, int(stf_id), t, t0, f0, int(ntime), stept, int(dbl))
+
+
+def svf(t, t0, f0, stf_id=200, ntime=1, stept=0.01, dbl=False):
+    return lib().orc_stf(1, int(stf_id), t, t0, f0, int(ntime), stept, int(dbl))
+
+
+def norm_delt(x0, y0, z0):
+    out = np.zeros(343)
+    if lib().orc_norm_delt(x0, y0, z0, _p(out)):
+        raise RuntimeError("cal_norm_delt is zero")
+    return out.reshape(7, 7, 7, order="F")  # [li, lj, lk]
+
+
+def pml_R(n):
+    return lib().orc_pml_R(int(n))
+
+
+def op(kind, fwd, f, i):
+    """kind 0 DRP/opt, 1 2-4, 2 2-2 one-sided operator on a 1-D array at 0-based i."""
+    a = _d(f)
+    return lib().orc_op(int(kind), int(bool(fwd)), _p(a), int(i))

@@ -1,0 +1,107 @@
+"""Parity of the CUDA solver with the oracle on seeded small models.
+
+Both sides get identical inputs (same coordinates, metric, media, sources), so every
+field is compared after each of the first eight steps (one full F/B cycle, i.e. all
+eight operator variants and all four RK stages) and after a longer run.  The CUDA
+kernels are built without FMA contraction and follow the reference's operand order, so
+the expected difference is zero; the assertion allows 1e-6 relative L2 per field.
+"""
+import numpy as np
+import pytest
+
+from helpers import feed, interior, rel_l2, small_model
+
+pytestmark = pytest.mark.gpu
+
+KINDS = ["surface", "buried", "nofree", "moment", "water"]
+
+
+def _pair(kind, oracle_mod, native_lib):
+    import fwant_gb300 as fw
+    m = small_model(kind)
+    met = oracle_mod.metric(m.x, m.y, m.z)
+    g = feed(fw.Solver(m.ni, m.nj, m.nk, m.stept, free_surface=m.free_surface), m, met, kind)
+    o = feed(oracle_mod.Oracle(m.ni, m.nj, m.nk, m.stept, free_surface=m.free_surface), m, met, kind)
+    return m, g, o
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_each_step_of_one_cycle(kind, oracle_mod, native_lib):
+    m, g, o = _pair(kind, oracle_mod, native_lib)
+    worst = 0.0
+    for step in range(1, 9):
+        g.run(1)
+        o.run(1)
+        for c in range(9):
+            a = interior(g.get_field(c))
+            b = interior(o.get_field(c))
+            if not np.any(b):
+                assert not np.any(a), f"{kind} step {step} comp {c}: expected zeros"
+                continue
+            e = rel_l2(a, b)
+            worst = max(worst, e)
+            assert e < 1e-6, f"{kind}: step {step} component {c} rel L2 {e:.3e}"
+    print(f"{kind}: worst rel L2 over 8 steps = {worst:.3e}")
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_long_run_fields_and_seismograms(kind, oracle_mod, native_lib):
+    m, g, o = _pair(kind, oracle_mod, native_lib)
+    # 75 steps: whole 8-step blocks through the CUDA graph plus an eager remainder
+    g.run(40)
+    g.run(35)
+    o.run(75)
+    assert g.ntime == o.ntime == 75
+    for c in range(9):
+        a, b = interior(g.get_field(c)), interior(o.get_field(c))
+        if np.any(b):
+            assert rel_l2(a, b) < 1e-5, f"{kind} component {c}"
+    sg, so = g.get_seismo(), o.get_seismo()
+    assert sg.shape == so.shape == (9, 75, m.recv_indx.shape[0])
+    for c in range(9):
+        if np.any(so[c]):
+            assert rel_l2(sg[c], so[c]) < 1e-5, f"{kind} seismogram component {c}"
+
+
+def test_run_in_pieces_equals_one_run(oracle_mod, native_lib):
+    import fwant_gb300 as fw
+    m = small_model("buried")
+    met = oracle_mod.metric(m.x, m.y, m.z)
+    a = feed(fw.Solver(m.ni, m.nj, m.nk, m.stept), m, met, "buried")
+    b = feed(fw.Solver(m.ni, m.nj, m.nk, m.stept), m, met, "buried")
+    a.run(27)
+    for n in (3, 8, 5, 11):
+        b.run(n)
+    for c in range(9):
+        assert np.array_equal(a.get_field(c), b.get_field(c))
+    assert np.array_equal(a.get_seismo(), b.get_seismo())
+
+
+def test_fp64_metric_matches_sp_metric(oracle_mod, native_lib):
+    """fwant_compute_metric (FP64 on the device) against seis3d_metric's SP arithmetic."""
+    import fwant_gb300 as fw
+    m = small_model("surface")
+    s = fw.Solver(m.ni, m.nj, m.nk, m.stept)
+    s.set_coord(m.x, m.y, m.z)
+    s.compute_metric()
+    got = s.get_metric()
+    ref = oracle_mod.metric(m.x, m.y, m.z)
+    for k in ref:
+        np.testing.assert_allclose(got[k], ref[k], rtol=2e-6, err_msg=k)
+
+
+def test_overflow_check_reports_nan(native_lib):
+    """macdrp_check: a NaN planted in the host-side initial state is reported as an error
+    status (no GPU fault: the value is uploaded as data)."""
+    import fwant_gb300 as fw
+    m = small_model("surface")
+    s = fw.Solver(m.ni, m.nj, m.nk, m.stept)
+    from fwant_gb300 import inputs
+    inputs.attach(s, m)
+    s.check()
+    f = np.zeros(s.shape, np.float32)
+    f[10, 10, 10] = np.nan
+    s.set_field("Vx", f)
+    with pytest.raises(fw.FwantError) as e:
+        s.check()
+    assert e.value.code == 4
