@@ -1,0 +1,328 @@
+#!/usr/bin/env python
+"""Benchmark of the forward-solver hot path (seis3d_wave time loop) on GB300.
+
+Workload (default, --config c2): 400x400x200 interior grid, 1 km horizontal spacing,
+0.5-2 km stretched vertical spacing, layered medium with a seeded +/-5% Gaussian-
+correlated (10 km) Vp/Vs perturbation, 12-cell CFS-PML on five faces, free surface,
+64 surface receivers, and three simulations (vertical/horizontal point forces Fx, Fy,
+Fz; Ricker 0.2 Hz) that together produce the strain Green's tensors.  One bench step =
+one LDDRK4 time step (four fused stage launches + the step-end kernel) of each of the
+three simulations.  Inputs are synthetic and seeded.  The register sets (9 components x
+4 x 37.5M points x 4 B per simulation) are far larger than L2, so no L2 flush is used.
+
+Metric: grid-point updates per second (interior points x steps / device time).
+
+--impl reference times the reference's algorithm on the host cores instead: the
+oracle (a restatement of the Fortran solver, which cannot be compiled here) with all
+available threads, one time step of one simulation per bench step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# Algorithmic DRAM bytes of the fused scheme per interior point per time step (FP32):
+# W ping-pong, RK registers m and t, medium (lambda, mu, rho):
+#   stage 1: read W 9 + medium 3, write W' 9 + t 9                = 30 floats
+#   stage 2, 3: read W 9 + medium 3 + m 9 + t 9, write W' 9 + t 9  = 48 floats each
+#   stage 4: read W 9 + medium 3 + t 9, write W 9                  = 30 floats
+BYTES_PT_STEP = 156 * 4
+# CFS-PML memory variables, per slab point per step: 6 variables x (18+30+30+18) floats
+BYTES_PML_PT_STEP = 6 * 16 * 4
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=32)
+    p.add_argument("--warmup", type=int, default=8)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--config", choices=["c2", "c1"], default="c2")
+    p.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max-reduction over ranks (gloo on CPU tensors; replicas only)."""
+
+    def __init__(self, world):
+        self.world = world
+        if world > 1:
+            import torch.distributed as td
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, v):
+        if self.world == 1:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per stage launch from the committed ncu summary (per interior point,
+    so that it scales to the benchmark grid), or None."""
+    path = os.path.join(ROOT, "profiles", "stage_kernel_c2.md")
+    if not os.path.exists(path):
+        return None
+    m = re.search(r"dram_bytes_per_point_per_launch:\s*([0-9.eE+-]+)", open(path).read())
+    return float(m.group(1)) if m else None
+
+
+def make_models(config, seed):
+    from fwant_gb300 import inputs
+    if config == "c1":
+        m = inputs.config_c1(seed=seed)
+        return [m], "C1: 100x100x60, FP32, 12-cell CFS-PML x5, free surface, Fz Ricker 0.2 Hz, 16 receivers"
+    base = inputs.config_c2(seed=seed, component=0)
+    models = []
+    for c in range(3):
+        m = inputs.Model(**{k: getattr(base, k) for k in base.__dataclass_fields__})
+        f = np.zeros((1, 1), np.float32)
+        m.fx, m.fy, m.fz = f.copy(), f.copy(), f.copy()
+        (m.fx, m.fy, m.fz)[c][0, 0] = np.float32(1.0e15)
+        models.append(m)
+    return models, ("C2: 400x400x200, FP32, +/-5% Gaussian-correlated Vp/Vs (10 km), 12-cell CFS-PML x5, "
+                    "free surface, 3 force components (Fx,Fy,Fz) x 64 surface receivers")
+
+
+def slab_points(m):
+    n = m.pml_number
+    tot = 0
+    tot += (n[0] + 1) * m.nj * m.nk if n[0] > 0 else 0
+    tot += (n[1] + 1) * m.nj * m.nk if n[1] > 0 else 0
+    tot += (n[2] + 1) * m.ni * m.nk if n[2] > 0 else 0
+    tot += (n[3] + 1) * m.ni * m.nk if n[3] > 0 else 0
+    tot += (n[4] + 1) * m.ni * m.nj if n[4] > 0 else 0
+    tot += (n[5] + 1) * m.ni * m.nj if n[5] > 0 else 0
+    return tot
+
+
+def cpu_sample(models, steps):
+    """The oracle on all host threads: `steps` time steps of the first simulation."""
+    from fwant_gb300 import inputs
+    from oracle import oracle as O
+    O.build()
+    threads = O.set_threads(os.cpu_count() or 1)
+    m = models[0]
+    o = O.Oracle(m.ni, m.nj, m.nk, m.stept)
+    inputs.attach(o, m, metric=O.metric(m.x, m.y, m.z))
+    o.run(1)  # first touch of every array
+    t0 = time.perf_counter()
+    o.run(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return m.npoints * steps / dt / 1e9, threads, dt
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    models, desc = make_models(args.config, seed=0)
+    from fwant_gb300 import inputs
+    from oracle import oracle as O
+    O.build()
+    threads = O.set_threads(os.cpu_count() or 1)
+    m = models[0]
+    o = O.Oracle(m.ni, m.nj, m.nk, m.stept)
+    inputs.attach(o, m, metric=O.metric(m.x, m.y, m.z))
+    o.run(max(args.warmup, 1))
+    t0 = time.perf_counter()
+    o.run(args.steps)
+    dt = time.perf_counter() - t0
+    v = m.npoints * args.steps / dt / 1e9
+    sample = (f"one time step of one of the three simulations ({m.ni}x{m.nj}x{m.nk}) per bench step, "
+              f"{args.steps} steps after {max(args.warmup, 1)} warm-up")
+    out = {
+        "impl": "reference", "metric": "grid-point updates per second", "value": v, "unit": "GPts/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": desc, "sample": sample, "l2": "inputs larger than L2 (no flush)"},
+        "cpu_baseline": {"value": v, "unit": "GPts/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "GPts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def run_ours(args, rank, world):
+    import fwant_gb300 as fw
+    from fwant_gb300 import inputs
+    dist = Dist(world)
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    fw.load_library()
+    models, desc = make_models(args.config, seed=rank)
+    sims = [inputs.attach(fw.Solver(m.ni, m.nj, m.nk, m.stept, device=dev), m) for m in models]
+    npts = sum(m.npoints for m in models)
+    # per-launch timing of the stage kernel (CUDA events around each launch, eager)
+    stage_ms, end_ms = sims[0].profile_stages(8)
+    for s in sims[1:]:
+        s.run(8)
+    warm = max(args.warmup, 3)
+    for s in sims:
+        s.run(warm)
+    clocks = Clocks(dev)
+    dist.barrier()
+    clocks.start()
+    t_host = time.perf_counter()
+    dev_ms = 0.0
+    for s in sims:
+        s.run(args.steps)  # whole 8-step blocks replay a CUDA graph; returns after device completion
+        dev_ms += s.last_run_ms()
+    t_host = time.perf_counter() - t_host
+    clk = clocks.stop()
+    dist.barrier()
+    dev_ms = dist.max(dev_ms)
+    value = world * npts * args.steps / (dev_ms * 1e-3) / 1e9
+
+    # roofline of the stage kernel
+    m0 = models[0]
+    algo_bytes_step = BYTES_PT_STEP * m0.npoints + BYTES_PML_PT_STEP * slab_points(m0)
+    launch_ms = float(np.mean(stage_ms))
+    achieved = algo_bytes_step / 4.0 / (launch_ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    tr = ncu_traffic()
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": peak_kind, "traffic": (tr * m0.npoints) if tr else None,
+            "stage_ms": stage_ms, "step_end_ms": end_ms,
+            "algorithmic_bytes_per_launch": algo_bytes_step / 4.0}
+
+    out = {
+        "metric": "grid-point updates per second", "value": value, "unit": "GPts/s", "n_gpus": world,
+        "steps": args.steps, "warmup": warm, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": desc, "points_per_step": npts, "l2": "inputs larger than L2 (no flush)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+        "host_wall_s": t_host, "roofline": roof, "clocks": clk,
+        "gpu_launches": args.steps * len(sims) * 5,
+    }
+    for s in sims:
+        s.close()
+
+    if not args.no_e2e:
+        # The whole job through the public API: create, upload the model from host arrays,
+        # run, read the seismograms back; host wall clock.
+        t0 = time.perf_counter()
+        h2d = d2h = 0
+        for m in models:
+            s = fw.Solver(m.ni, m.nj, m.nk, m.stept, device=dev)
+            inputs.attach(s, m)
+            s.run(args.steps)
+            sg = s.get_seismo()
+            s.close()
+            h2d += 3 * m.lam.nbytes + m.x.nbytes + m.y.nbytes + m.z.nbytes
+            d2h += sg.nbytes
+        t_e2e = dist.max(time.perf_counter() - t0)
+        out["e2e"] = {"value": world * npts * args.steps / t_e2e / 1e9, "unit": "GPts/s",
+                      "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps,
+                      "wall_s": t_e2e, "includes": "solver creation, model upload, run, seismogram download"}
+    if rank == 0 and not args.no_cpu_baseline:
+        v, thr, dt = cpu_sample(models, args.cpu_steps)
+        out["cpu_baseline"] = {"value": v, "unit": "GPts/s", "cores": thr, "kind": "port",
+                               "sample": f"{args.cpu_steps} time steps of one simulation "
+                                         f"({m0.ni}x{m0.nj}x{m0.nk}), {dt:.1f} s"}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    dist.close()
+    return 0
+
+
+def main():
+    args = parse_args()
+    rank, world, _ = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_ours(args, rank, world)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

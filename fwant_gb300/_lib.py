@@ -55,6 +55,7 @@ EXPORTS = [
     ("fwant_get_field", C.c_int, [_vp, C.c_int, _fp]),
     ("fwant_set_field", C.c_int, [_vp, C.c_int, _fp]),
     ("fwant_check", C.c_int, [_vp]),
+    ("fwant_profile_stages", C.c_int, [_vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("fwant_last_run_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
 ]
 
@@ -226,6 +227,13 @@ class Solver:
         v = C.c_double()
         self._chk(self._lib.fwant_last_run_ms(self._h, C.byref(v)))
         return v.value
+
+    def profile_stages(self, nsteps):
+        """Advance nsteps with per-launch CUDA events; returns (stage_ms[4], step_end_ms)."""
+        st = (C.c_double * 4)()
+        other = C.c_double()
+        self._chk(self._lib.fwant_profile_stages(self._h, int(nsteps), st, C.byref(other)))
+        return [st[i] for i in range(4)], other.value
 
     def get_seismo(self, max_samples=None):
         """Return array (9, nsamp, num_pt)."""

@@ -486,7 +486,7 @@ struct fwant_solver {
   // Register-set roles: A holds W at the step start (and is the RK "m" register), T is
   // the RK "t" accumulator; B and C are the stage outputs.  Stage 4 writes W(n+1) into
   // T in place, after which A and T swap roles.
-  void enqueue_step() {
+  void enqueue_step(cudaEvent_t* ev = nullptr) {
     const int X = CYCLE[cycle_pos & 7];
     fw::StageArgs<float> a = base_args();
     const int in_of[4] = {rA, rB, rC, rB};
@@ -502,12 +502,15 @@ struct fwant_solver {
       a.stage = s;
       const int v = (s % 2 == 0) ? X : (~X & 7);
       const int rk = s == 0 ? 0 : (s == 3 ? 2 : 1);
+      if (ev) cudaEventRecord(ev[s], st);
       fw::launch_stage_f32(a, v, rk, st);
     }
+    if (ev) cudaEventRecord(ev[4], st);
     fw::RecvArgs r{};
     r.g = g; r.w = set(rT); r.npt = npt; r.idx = d_rec; r.tinv = tinv; r.seismo = d_seis; r.cap = cap;
     r.ntime = d_ntime;
     fw::launch_advance_record(r, st);
+    if (ev) cudaEventRecord(ev[5], st);
     std::swap(rA, rT);
     cycle_pos = (cycle_pos + 1) & 7;
     ntime += 1;
@@ -555,6 +558,37 @@ struct fwant_solver {
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, ev0, ev1);
     last_ms = ms;
+    if (npt > 0) nsamp = std::max(nsamp, std::min(ntime / tinv, cap));
+    return FWANT_OK;
+  }
+
+  // Eager steps with CUDA events around every launch: average device time of the four
+  // stage launches (index = stage inside the step) and of the step-end kernel.
+  fwant_status profile(int nsteps, double* stage_ms, double* other_ms) {
+    if (nsteps <= 0) return fail(FWANT_ERR_INVALID_ARG, "nsteps <= 0");
+    if (!have_coord || !have_metric || !have_media)
+      return fail(FWANT_ERR_STATE, "coordinates, metric and media must be set before profiling");
+    cudaSetDevice(cfg.device);
+    fwant_status rc = prepare_sources(ntime + nsteps);
+    if (rc != FWANT_OK) return rc;
+    if ((rc = prepare_receivers(ntime + nsteps)) != FWANT_OK) return rc;
+    std::vector<cudaEvent_t> ev(size_t(6) * nsteps);
+    for (auto& e : ev) cudaEventCreate(&e);
+    for (int q = 0; q < nsteps; ++q) enqueue_step(&ev[size_t(6) * q]);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    double acc[5] = {0, 0, 0, 0, 0};
+    if (e == cudaSuccess)
+      for (int q = 0; q < nsteps; ++q)
+        for (int k = 0; k < 5; ++k) {
+          float ms = 0.0f;
+          cudaEventElapsedTime(&ms, ev[size_t(6) * q + k], ev[size_t(6) * q + k + 1]);
+          acc[k] += ms;
+        }
+    for (auto& x : ev) cudaEventDestroy(x);
+    if (e != cudaSuccess) return cuda_fail(e, "profile");
+    for (int k = 0; k < 4; ++k) stage_ms[k] = acc[k] / nsteps;
+    *other_ms = acc[4] / nsteps;
     if (npt > 0) nsamp = std::max(nsamp, std::min(ntime / tinv, cap));
     return FWANT_OK;
   }
@@ -805,6 +839,11 @@ fwant_status fwant_check(fwant_solver* s) {
     return s->fail(FWANT_ERR_NUMERIC_OVERFLOW, b);
   }
   return FWANT_OK;
+}
+
+fwant_status fwant_profile_stages(fwant_solver* s, int nsteps, double* stage_ms, double* other_ms) {
+  if (!s || !stage_ms || !other_ms) return FWANT_ERR_INVALID_ARG;
+  return s->profile(nsteps, stage_ms, other_ms);
 }
 
 fwant_status fwant_last_run_ms(fwant_solver* s, double* ms) {

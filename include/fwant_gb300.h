@@ -166,6 +166,12 @@ fwant_status fwant_set_field(fwant_solver* s, int component, const float* in);
  * Returns FWANT_ERR_NUMERIC_OVERFLOW when a value is NaN, Inf or >= huge(1.0). */
 fwant_status fwant_check(fwant_solver* s);
 
+/* Advance nsteps steps with one CUDA event pair around every launch (no graph) and
+ * report the average device time of each of the four stage launches (stage_ms[4],
+ * stage order inside the step) and of the step-end receiver/counter kernel.  Same
+ * results as fwant_run; used for per-kernel timing. */
+fwant_status fwant_profile_stages(fwant_solver* s, int nsteps, double* stage_ms, double* other_ms);
+
 /* Device time of the last fwant_run call in milliseconds (CUDA events). */
 fwant_status fwant_last_run_ms(fwant_solver* s, double* ms);
 

@@ -845,6 +845,33 @@ template <class T> struct Solver {
   }
 };
 
+// The same metric formula evaluated in double from the SP coordinates and rounded
+// once: the FP64 precomputation the GPU path performs.
+static void metric_dp(int nx, int ny, int nz, const float* x, const float* y, const float* z,
+                      float* xsin, float* xcot, float* xi_x, float* eta_y, float* zeta_z) {
+  const double coeF[5] = {-0.30874, -0.6326, 1.2330, -0.3334, 0.04168};
+  const double coeB[5] = {-0.04168, 0.3334, -1.2330, 0.6326, 0.30874};
+  for (int i = 0; i < nx; ++i) {
+    xsin[i] = float(std::sin(double(x[i])));
+    xcot[i] = float(1.0 / std::tan(double(x[i])));
+  }
+  auto one = [&](int n, const float* g, float* out) {
+    const int lo = LenFD, hi = n - 1 - LenFD;
+    for (int i = 0; i < n; ++i) {
+      const int ii = i < lo ? lo : (i > hi ? hi : i);
+      double sb = 0.0, sf = 0.0;
+      for (int q = 0; q < 5; ++q) {
+        sb += double(g[ii - 3 + q]) * coeB[q];
+        sf += double(g[ii - 1 + q]) * coeF[q];
+      }
+      out[i] = float(1.0 / ((sb + sf) * 0.5));
+    }
+  };
+  one(nx, x, xi_x);
+  one(ny, y, eta_y);
+  one(nz, z, zeta_z);
+}
+
 // seis3d_metric (seis3d_metric.F90:83-112): SP coordinates, DP sin/tan, SP metric.
 static void metric_sp(int nx, int ny, int nz, const float* x, const float* y, const float* z,
                       float* xsin, float* xcot, float* xi_x, float* eta_y, float* zeta_z) {
@@ -1082,6 +1109,11 @@ double orc_pml_R(int n) { return double(orc::cal_pml_R<float>(n)); }
 void orc_metric(int nx, int ny, int nz, const float* x, const float* y, const float* z, float* xsin,
                 float* xcot, float* xi_x, float* eta_y, float* zeta_z) {
   orc::metric_sp(nx, ny, nz, x, y, z, xsin, xcot, xi_x, eta_y, zeta_z);
+}
+
+void orc_metric_dp(int nx, int ny, int nz, const float* x, const float* y, const float* z, float* xsin,
+                   float* xcot, float* xi_x, float* eta_y, float* zeta_z) {
+  orc::metric_dp(nx, ny, nz, x, y, z, xsin, xcot, xi_x, eta_y, zeta_z);
 }
 
 // One-sided operator applied to a 1-D array at 0-based index i (known-answer tests).

@@ -45,6 +45,7 @@ _SIGS = [
     ("orc_norm_delt", C.c_int, [C.c_double, C.c_double, C.c_double, _dp]),
     ("orc_pml_R", C.c_double, [C.c_int]),
     ("orc_metric", None, [C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, _fp, _fp, _fp, _fp, _fp]),
+    ("orc_metric_dp", None, [C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, _fp, _fp, _fp, _fp, _fp]),
     ("orc_op", C.c_double, [C.c_int, C.c_int, _dp, C.c_int]),
 ]
 
@@ -204,13 +205,15 @@ class Oracle:
         return out[: 9 * n * self.num_pt].reshape(9, n, self.num_pt)
 
 
-def metric(x, y, z):
-    """seis3d_metric restated in SP (seis3d_metric.F90:83-112)."""
+def metric(x, y, z, dp=False):
+    """seis3d_metric restated in SP (seis3d_metric.F90:83-112); dp=True evaluates the same
+    formula in double from the SP coordinates (the FP64 precomputation)."""
     x, y, z = [np.ascontiguousarray(np.asarray(v, np.float32)) for v in (x, y, z)]
     out = [np.zeros(x.size, np.float32), np.zeros(x.size, np.float32), np.zeros(x.size, np.float32),
            np.zeros(y.size, np.float32), np.zeros(z.size, np.float32)]
-    lib().orc_metric(x.size, y.size, z.size, _p(x, C.c_float), _p(y, C.c_float), _p(z, C.c_float),
-                     *[_p(v, C.c_float) for v in out])
+    fn = lib().orc_metric_dp if dp else lib().orc_metric
+    fn(x.size, y.size, z.size, _p(x, C.c_float), _p(y, C.c_float), _p(z, C.c_float),
+       *[_p(v, C.c_float) for v in out])
     return dict(zip(("xsin", "xcot", "xi_x", "eta_y", "zeta_z"), out))
 
 

@@ -77,17 +77,23 @@ def test_run_in_pieces_equals_one_run(oracle_mod, native_lib):
     assert np.array_equal(a.get_seismo(), b.get_seismo())
 
 
-def test_fp64_metric_matches_sp_metric(oracle_mod, native_lib):
-    """fwant_compute_metric (FP64 on the device) against seis3d_metric's SP arithmetic."""
+def test_fp64_metric(oracle_mod, native_lib):
+    """fwant_compute_metric (FP64 on the device) against the same formula evaluated in
+    double on the host (1 ulp of FP32 allowed for summation order), and against
+    seis3d_metric's SP arithmetic, whose cancellation error on FP32 colatitudes near
+    0.87 rad with 1.6e-4 rad spacing reaches ~1e-3 relative."""
     import fwant_gb300 as fw
     m = small_model("surface")
     s = fw.Solver(m.ni, m.nj, m.nk, m.stept)
     s.set_coord(m.x, m.y, m.z)
     s.compute_metric()
     got = s.get_metric()
-    ref = oracle_mod.metric(m.x, m.y, m.z)
+    ref = oracle_mod.metric(m.x, m.y, m.z, dp=True)
     for k in ref:
-        np.testing.assert_allclose(got[k], ref[k], rtol=2e-6, err_msg=k)
+        np.testing.assert_allclose(got[k], ref[k], rtol=2.5e-7, err_msg=k)
+    sp = oracle_mod.metric(m.x, m.y, m.z)
+    for k in sp:
+        np.testing.assert_allclose(got[k], sp[k], rtol=2e-3, err_msg=k)
 
 
 def test_overflow_check_reports_nan(native_lib):
