@@ -52,6 +52,8 @@ def parse_args():
     p.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--grid", default=None, help="override the C2 interior size, e.g. 200x200x100 (profiling)")
+    p.add_argument("--sims", type=int, default=3, help="number of force components simulated (C2)")
     return p.parse_args()
 
 
@@ -157,25 +159,30 @@ def ncu_traffic():
     return float(m.group(1)) if m else None
 
 
-def make_models(config, seed):
+def make_models(config, seed, grid=None, sims=3):
     from fwant_gb300 import inputs
     if config == "c1":
         m = inputs.config_c1(seed=seed)
         return [m], "C1: 100x100x60, FP32, 12-cell CFS-PML x5, free surface, Fz Ricker 0.2 Hz, 16 receivers"
-    base = inputs.config_c2(seed=seed, component=0)
+    if grid:
+        ni, nj, nk = (int(v) for v in grid.lower().split("x"))
+        base = inputs.make_model(ni, nj, nk, seed=seed, nrecv=64, perturb=0.05, name=f"C2-physics {grid}")
+    else:
+        base = inputs.config_c2(seed=seed, component=0)
     models = []
-    for c in range(3):
+    for c in range(sims):
         m = inputs.Model(**{k: getattr(base, k) for k in base.__dataclass_fields__})
         f = np.zeros((1, 1), np.float32)
         m.fx, m.fy, m.fz = f.copy(), f.copy(), f.copy()
         (m.fx, m.fy, m.fz)[c][0, 0] = np.float32(1.0e15)
         models.append(m)
-    return models, ("C2: 400x400x200, FP32, +/-5% Gaussian-correlated Vp/Vs (10 km), 12-cell CFS-PML x5, "
-                    "free surface, 3 force components (Fx,Fy,Fz) x 64 surface receivers")
+    size = grid or "400x400x200"
+    return models, (f"C2: {size}, FP32, +/-5% Gaussian-correlated Vp/Vs (10 km), 12-cell CFS-PML x5, "
+                    f"free surface, {sims} force component(s) of (Fx,Fy,Fz) x 64 surface receivers")
 
 
 def slab_points(m):
-    n = m.pml_number
+    n = [int(v) for v in m.pml_number]
     tot = 0
     tot += (n[0] + 1) * m.nj * m.nk if n[0] > 0 else 0
     tot += (n[1] + 1) * m.nj * m.nk if n[1] > 0 else 0
@@ -206,7 +213,7 @@ def cpu_sample(models, steps):
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
-    models, desc = make_models(args.config, seed=0)
+    models, desc = make_models(args.config, seed=0, grid=args.grid, sims=args.sims)
     from fwant_gb300 import inputs
     from oracle import oracle as O
     O.build()
@@ -240,7 +247,7 @@ def run_ours(args, rank, world):
     dist = Dist(world)
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     fw.load_library()
-    models, desc = make_models(args.config, seed=rank)
+    models, desc = make_models(args.config, seed=rank, grid=args.grid, sims=args.sims)
     sims = [inputs.attach(fw.Solver(m.ni, m.nj, m.nk, m.stept, device=dev), m) for m in models]
     npts = sum(m.npoints for m in models)
     # per-launch timing of the stage kernel (CUDA events around each launch, eager)
@@ -266,7 +273,7 @@ def run_ours(args, rank, world):
 
     # roofline of the stage kernel
     m0 = models[0]
-    algo_bytes_step = BYTES_PT_STEP * m0.npoints + BYTES_PML_PT_STEP * slab_points(m0)
+    algo_bytes_step = BYTES_PT_STEP * int(m0.npoints) + BYTES_PML_PT_STEP * slab_points(m0)
     launch_ms = float(np.mean(stage_ms))
     achieved = algo_bytes_step / 4.0 / (launch_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
