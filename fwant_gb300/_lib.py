@@ -65,7 +65,7 @@ class FwantConfig(C.Structure):
         ("ni", C.c_int), ("nj", C.c_int), ("nk", C.c_int),
         ("stept", C.c_double),
         ("free_surface", C.c_int), ("src_surface", C.c_int),
-        ("storage", C.c_int), ("device", C.c_int),
+        ("storage", C.c_int), ("device", C.c_int), ("exact_arith", C.c_int),
     ]
 
 
@@ -120,10 +120,11 @@ def _ptr(a, t=C.c_float):
 class Solver:
     """One simulation on one GPU (the reference's per-rank solver state)."""
 
-    def __init__(self, ni, nj, nk, stept, free_surface=True, src_surface=True, storage=STORAGE_FP32, device=0):
+    def __init__(self, ni, nj, nk, stept, free_surface=True, src_surface=True, storage=STORAGE_FP32, device=0,
+                 exact_arith=False):
         self._lib = load_library()
         cfg = FwantConfig(int(ni), int(nj), int(nk), float(stept), int(bool(free_surface)),
-                          int(bool(src_surface)), int(storage), int(device))
+                          int(bool(src_surface)), int(storage), int(device), int(bool(exact_arith)))
         h = C.c_void_p()
         rc = self._lib.fwant_create(C.byref(cfg), C.byref(h))
         if rc != 0:

@@ -19,14 +19,17 @@ LIB = os.path.join(LIB_DIR, "libfwant_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-# -fmad=false: every product and sum rounds separately, as in the reference's FP32 source.
-CU_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler",
-            "-ffp-contract=off", "-Xptxas", "-O3"]
+CU_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+            "-Xptxas", "-O3"]
+# the reference-order units: every product and sum rounds separately, as in the
+# reference's FP32 source expressions
+EXACT_FLAGS = ["-fmad=false"]
 # -ffp-contract=off: host set-up arithmetic (PML profiles, source weights) must not
 # contract into FMAs on aarch64, where GCC would otherwise do so by default.
 CPP_FLAGS = ["-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
 
-SOURCES = ["stage.cu", "aux.cu", "solver.cpp"]
+SOURCES = ["stage_fast_rk0.cu", "stage_fast_rk1.cu", "stage_fast_rk2.cu", "stage_exact_rk0.cu",
+           "stage_exact_rk1.cu", "stage_exact_rk2.cu", "stage_dispatch.cu", "aux.cu", "solver.cpp"]
 
 
 def _nvcc() -> str:
@@ -73,6 +76,8 @@ def build(verbose: bool = False, force: bool = False, jobs: int | None = None) -
         objs.append(obj)
         if force or _stale(obj, [path] + hdrs):
             flags = CU_FLAGS + ARCH if src.endswith(".cu") else CPP_FLAGS
+            if "exact" in src:
+                flags = flags + EXACT_FLAGS
             jobs_todo.append([nvcc, *flags, "-I", CSRC, "-I", INCLUDE, "-c", path, "-o", obj])
     if jobs_todo:
         with ThreadPoolExecutor(max_workers=jobs or min(8, len(jobs_todo))) as ex:

@@ -60,7 +60,8 @@ struct Sources {
   const float* mom_M;     // [nmom][ntwin][6] Mxx Myy Mzz Mxy Mxz Myz
 };
 
-// Everything one RK-stage launch needs.
+// Everything one RK-stage launch needs.  S is the storage type of the wavefield
+// registers and PML memory variables; arithmetic is float (double for S = double).
 template <class S>
 struct StageArgs {
   Geom g;
@@ -78,9 +79,12 @@ struct StageArgs {
   const float* xsin;
   const float* xcot;
   const float* zc;
-  // PML profiles (A, B, D/B) per axis, 0-based Fortran index
-  const float* pA[3];
-  const float* pB[3];
+  const float* rzinv;  // 1/z (fast arithmetic)
+  const float* rsinv;  // 1/xsin (fast arithmetic)
+  // PML profile terms per axis, 0-based Fortran index: b1 = 1/B, b1 - 1, A + D, D (D = d/b)
+  const float* pb1[3];
+  const float* pb11[3];
+  const float* pad[3];
   const float* pD[3];
   Slab slab[6];
   const S* ain[6];
@@ -89,13 +93,19 @@ struct StageArgs {
   S* at[6];
   float a, b;     // rka*stept, rkb*stept
   int stage;      // 0..3 inside the step
+  int kc;         // planes per CTA along k
   const int* ntime;  // device step counter
   Sources src;
   int src_surface;
 };
 
-// Launchers (stage.cu).  variant bit 2 = x, bit 1 = y, bit 0 = z; 1 = forward operator.
-void launch_stage_f32(const StageArgs<float>& a, int variant, int rk, void* stream);
+// Stage launchers (stage_*.cu).  variant bit 2 = x, bit 1 = y, bit 0 = z; 1 = forward
+// operator.  rk: 0 = RK_beg, 1 = RK_inn, 2 = RK_fin.  exact = 1 selects the reference's
+// operand order with IEEE division and no FMA (bit-reproducible against FP32 CPU runs
+// of the same expressions); 0 the fast form (FMA, reciprocals).
+void launch_stage_f32(const StageArgs<float>& a, int variant, int rk, int exact, void* stream);
+int stage_planes_per_cta(const Geom& g, int sm_count);
+constexpr int STAGE_TX = 32, STAGE_TY = 8;
 
 struct RecvArgs {
   Geom g;

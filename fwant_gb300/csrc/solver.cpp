@@ -58,7 +58,9 @@ struct fwant_solver {
   // 1-D arrays, each with nx/ny/nz entries
   float *d_x = nullptr, *d_y = nullptr, *d_z = nullptr, *d_xsin = nullptr, *d_xcot = nullptr;
   float *d_xi = nullptr, *d_eta = nullptr, *d_zeta = nullptr;
-  float* d_prof = nullptr;  // A,B,D for x (nx each), y (ny), z (nz)
+  float* d_prof = nullptr;  // b1, b1-1, A+D, D for x (nx each), y (ny), z (nz)
+  float *d_rzinv = nullptr, *d_rsinv = nullptr;
+  int kc = 8;                // planes per CTA of the stage kernel
   std::vector<float> hx, hy, hz, hxsin, hxcot;
   bool have_coord = false, have_metric = false, have_media = false;
 
@@ -97,7 +99,7 @@ struct fwant_solver {
     free_sources();
     cudaFree(regs); cudaFree(lam); cudaFree(mu); cudaFree(rho);
     cudaFree(d_x); cudaFree(d_y); cudaFree(d_z); cudaFree(d_xsin); cudaFree(d_xcot);
-    cudaFree(d_xi); cudaFree(d_eta); cudaFree(d_zeta); cudaFree(d_prof);
+    cudaFree(d_xi); cudaFree(d_eta); cudaFree(d_zeta); cudaFree(d_prof); cudaFree(d_rzinv); cudaFree(d_rsinv);
     for (int f = 0; f < 6; ++f) cudaFree(aux[f]);
     cudaFree(d_rec); cudaFree(d_seis); cudaFree(d_ntime); cudaFree(d_maxbits);
     if (ev0) cudaEventDestroy(ev0);
@@ -156,6 +158,9 @@ struct fwant_solver {
     g.fstride = ((g.plane * g.nz + 63) / 64) * 64;
     g.i1 = 3; g.i2 = 3 + ni - 1; g.j1 = 3; g.j2 = 3 + nj - 1; g.k1 = 3; g.k2 = 3 + nk - 1;
     g.freesurf = cfg.free_surface ? 1 : 0;
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, cfg.device);
+    kc = fw::stage_planes_per_cta(g, nsm > 0 ? nsm : 152);
     if ((e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
     cudaEventCreate(&ev0);
     cudaEventCreate(&ev1);
@@ -165,10 +170,11 @@ struct fwant_solver {
     d_x = dalloc<float>(g.nx); d_y = dalloc<float>(g.ny); d_z = dalloc<float>(g.nz);
     d_xsin = dalloc<float>(g.nx); d_xcot = dalloc<float>(g.nx); d_xi = dalloc<float>(g.nx);
     d_eta = dalloc<float>(g.ny); d_zeta = dalloc<float>(g.nz);
-    d_prof = dalloc<float>(3 * size_t(g.nx + g.ny + g.nz));
+    d_prof = dalloc<float>(4 * size_t(g.nx + g.ny + g.nz));
+    d_rzinv = dalloc<float>(g.nz); d_rsinv = dalloc<float>(g.nx);
     d_ntime = dalloc<int>(1); d_maxbits = dalloc<unsigned int>(1);
     if (!regs || !lam || !mu || !rho || !d_x || !d_y || !d_z || !d_xsin || !d_xcot || !d_xi || !d_eta ||
-        !d_zeta || !d_prof || !d_ntime || !d_maxbits)
+        !d_zeta || !d_prof || !d_rzinv || !d_rsinv || !d_ntime || !d_maxbits)
       return fail(FWANT_ERR_OOM, "device allocation failed");
     cudaMemset(regs, 0, nreg * sizeof(float));
     cudaMemset(lam, 0, g.fstride * sizeof(float)); cudaMemset(mu, 0, g.fstride * sizeof(float));
@@ -184,20 +190,37 @@ struct fwant_solver {
     return FWANT_OK;
   }
 
+  // Per-index PML terms as the reference forms them at every point
+  // (mod_abs_npml.F90:1168-1172): b1 = 1/B, b1_1 = b1 - 1, ad = A + D; and D.
   cudaError_t upload_profiles() {
     float* p = d_prof;
     for (int a = 0; a < 3; ++a) {
       const size_t n = hA[a].size();
-      cudaMemcpy(p, hA[a].data(), n * 4, cudaMemcpyHostToDevice); p += n;
-      cudaMemcpy(p, hB[a].data(), n * 4, cudaMemcpyHostToDevice); p += n;
+      std::vector<float> b1(n), b11(n), ad(n);
+      for (size_t q = 0; q < n; ++q) {
+        b1[q] = 1.0f / hB[a][q];
+        b11[q] = b1[q] - 1.0f;
+        ad[q] = hA[a][q] + hD[a][q];
+      }
+      cudaMemcpy(p, b1.data(), n * 4, cudaMemcpyHostToDevice); p += n;
+      cudaMemcpy(p, b11.data(), n * 4, cudaMemcpyHostToDevice); p += n;
+      cudaMemcpy(p, ad.data(), n * 4, cudaMemcpyHostToDevice); p += n;
       cudaMemcpy(p, hD[a].data(), n * 4, cudaMemcpyHostToDevice); p += n;
     }
     return cudaGetLastError();
   }
   const float* prof(int axis, int which) const {
     const float* p = d_prof;
-    for (int a = 0; a < axis; ++a) p += 3 * hA[a].size();
+    for (int a = 0; a < axis; ++a) p += 4 * hA[a].size();
     return p + which * hA[axis].size();
+  }
+  // 1/z and 1/xsin for the fast arithmetic form
+  cudaError_t upload_reciprocals() {
+    std::vector<float> rz(g.nz), rs(g.nx);
+    for (int k = 0; k < g.nz; ++k) rz[k] = 1.0f / hz[k];
+    for (int i = 0; i < g.nx; ++i) rs[i] = 1.0f / hxsin[i];
+    cudaMemcpy(d_rzinv, rz.data(), g.nz * 4, cudaMemcpyHostToDevice);
+    return cudaMemcpy(d_rsinv, rs.data(), g.nx * 4, cudaMemcpyHostToDevice);
   }
 
   // Fortran (nx,ny,nz) host array -> padded device array
@@ -305,6 +328,7 @@ struct fwant_solver {
     if (!src_dirty && steps <= stf_cap_steps) return FWANT_OK;
     drop_graphs();
     free_sources();
+    if (upload_reciprocals() != cudaSuccess) return fail(FWANT_ERR_CUDA, "reciprocal tables");
     const int cap_steps = std::max(steps + 8, 1024);
     const int G = cap_steps * 4;
     const float incr[4] = {0.0f, RKA[0], RKA[1], RKA[2]};  // set_cur_time(ntime, firRKa(s))
@@ -474,7 +498,11 @@ struct fwant_solver {
     a.g = g;
     a.lam = lam; a.mu = mu; a.rho = rho;
     a.xi_x = d_xi; a.eta_y = d_eta; a.zeta_z = d_zeta; a.xsin = d_xsin; a.xcot = d_xcot; a.zc = d_z;
-    for (int ax = 0; ax < 3; ++ax) { a.pA[ax] = prof(ax, 0); a.pB[ax] = prof(ax, 1); a.pD[ax] = prof(ax, 2); }
+    a.rzinv = d_rzinv; a.rsinv = d_rsinv;
+    for (int ax = 0; ax < 3; ++ax) {
+      a.pb1[ax] = prof(ax, 0); a.pb11[ax] = prof(ax, 1); a.pad[ax] = prof(ax, 2); a.pD[ax] = prof(ax, 3);
+    }
+    a.kc = kc;
     for (int f = 0; f < 6; ++f) a.slab[f] = slab[f];
     a.ntime = d_ntime;
     a.src = S;
@@ -503,7 +531,7 @@ struct fwant_solver {
       const int v = (s % 2 == 0) ? X : (~X & 7);
       const int rk = s == 0 ? 0 : (s == 3 ? 2 : 1);
       if (ev) cudaEventRecord(ev[s], st);
-      fw::launch_stage_f32(a, v, rk, st);
+      fw::launch_stage_f32(a, v, rk, cfg.exact_arith, st);
     }
     if (ev) cudaEventRecord(ev[4], st);
     fw::RecvArgs r{};

@@ -1,0 +1,9 @@
+// Instantiation unit: reference-order (exact) arithmetic, RK kind 0 (RK_beg).
+// Compiled with -fmad=false; the kernel itself is in stage_impl.cuh.
+#include "stage_impl.cuh"
+
+namespace fw {
+void launch_stage_exact_rk0(const StageArgs<float>& a, int variant, cudaStream_t st) {
+  launch_rk_variant<true, 0>(a, variant, st);
+}
+}  // namespace fw

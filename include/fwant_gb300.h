@@ -70,6 +70,9 @@ typedef struct fwant_config {
   int src_surface;     /* 1: forces on the surface act as traction (-DSrcSurface) */
   int storage;         /* fwant_storage */
   int device;          /* CUDA device ordinal */
+  int exact_arith;     /* 1: the reference's FP32 operand order, IEEE division, no FMA
+                          (reproduces an FP32 CPU run of the same expressions bit for bit);
+                          0: fast form (FMA, precomputed reciprocals) */
 } fwant_config;
 
 typedef struct fwant_solver fwant_solver;

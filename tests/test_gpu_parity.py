@@ -1,10 +1,13 @@
 """Parity of the CUDA solver with the oracle on seeded small models.
 
-Both sides get identical inputs (same coordinates, metric, media, sources), so every
-field is compared after each of the first eight steps (one full F/B cycle, i.e. all
-eight operator variants and all four RK stages) and after a longer run.  The CUDA
-kernels are built without FMA contraction and follow the reference's operand order, so
-the expected difference is zero; the assertion allows 1e-6 relative L2 per field.
+Both sides get identical inputs (coordinates, metric, media, sources), so every field
+is compared.  Two arithmetic forms of the same kernel are checked:
+
+* exact_arith=True keeps the reference's FP32 operand order with IEEE division and no
+  FMA; it must agree with the oracle to within 1e-6 relative L2 per field (in practice
+  it is bit-identical);
+* the default fast form (FMA, precomputed reciprocals) must agree within 1e-5 relative
+  L2 after 75 steps (the benchmark spec tolerance for full runs: 1e-4 on seismograms).
 """
 import numpy as np
 import pytest
@@ -16,19 +19,21 @@ pytestmark = pytest.mark.gpu
 KINDS = ["surface", "buried", "nofree", "moment", "water"]
 
 
-def _pair(kind, oracle_mod, native_lib):
+def _pair(kind, oracle_mod, exact):
     import fwant_gb300 as fw
     m = small_model(kind)
     met = oracle_mod.metric(m.x, m.y, m.z)
-    g = feed(fw.Solver(m.ni, m.nj, m.nk, m.stept, free_surface=m.free_surface), m, met, kind)
+    g = feed(fw.Solver(m.ni, m.nj, m.nk, m.stept, free_surface=m.free_surface, exact_arith=exact), m, met, kind)
     o = feed(oracle_mod.Oracle(m.ni, m.nj, m.nk, m.stept, free_surface=m.free_surface), m, met, kind)
     return m, g, o
 
 
 @pytest.mark.parametrize("kind", KINDS)
-def test_each_step_of_one_cycle(kind, oracle_mod, native_lib):
-    m, g, o = _pair(kind, oracle_mod, native_lib)
+def test_exact_each_step_of_one_cycle(kind, oracle_mod, native_lib):
+    """All eight F/B variants and all four RK stages, one step at a time."""
+    m, g, o = _pair(kind, oracle_mod, True)
     worst = 0.0
+    nonzero = 0
     for step in range(1, 9):
         g.run(1)
         o.run(1)
@@ -38,29 +43,44 @@ def test_each_step_of_one_cycle(kind, oracle_mod, native_lib):
             if not np.any(b):
                 assert not np.any(a), f"{kind} step {step} comp {c}: expected zeros"
                 continue
+            nonzero += 1
             e = rel_l2(a, b)
             worst = max(worst, e)
             assert e < 1e-6, f"{kind}: step {step} component {c} rel L2 {e:.3e}"
+    assert nonzero > 0
     print(f"{kind}: worst rel L2 over 8 steps = {worst:.3e}")
 
 
+@pytest.mark.parametrize("exact", [True, False], ids=["exact", "fast"])
 @pytest.mark.parametrize("kind", KINDS)
-def test_long_run_fields_and_seismograms(kind, oracle_mod, native_lib):
-    m, g, o = _pair(kind, oracle_mod, native_lib)
+def test_long_run_fields_and_seismograms(kind, exact, oracle_mod, native_lib):
+    m, g, o = _pair(kind, oracle_mod, exact)
     # 75 steps: whole 8-step blocks through the CUDA graph plus an eager remainder
     g.run(40)
     g.run(35)
     o.run(75)
     assert g.ntime == o.ntime == 75
+    tol = 1e-6 if exact else 1e-5
     for c in range(9):
         a, b = interior(g.get_field(c)), interior(o.get_field(c))
         if np.any(b):
-            assert rel_l2(a, b) < 1e-5, f"{kind} component {c}"
+            assert rel_l2(a, b) < tol, f"{kind} component {c}: {rel_l2(a, b):.3e}"
     sg, so = g.get_seismo(), o.get_seismo()
     assert sg.shape == so.shape == (9, 75, m.recv_indx.shape[0])
     for c in range(9):
         if np.any(so[c]):
-            assert rel_l2(sg[c], so[c]) < 1e-5, f"{kind} seismogram component {c}"
+            assert rel_l2(sg[c], so[c]) < tol, f"{kind} seismogram component {c}: {rel_l2(sg[c], so[c]):.3e}"
+
+
+def test_exact_is_bitwise(oracle_mod, native_lib):
+    """The reference-order form reproduces the FP32 CPU restatement bit for bit."""
+    m, g, o = _pair("buried", oracle_mod, True)
+    g.run(16)
+    o.run(16)
+    for c in range(9):
+        a, b = g.get_field(c), o.get_field(c).astype(np.float32)
+        assert np.array_equal(interior(a), interior(b)), f"component {c}"
+    assert np.array_equal(g.get_seismo(), o.get_seismo().astype(np.float32))
 
 
 def test_run_in_pieces_equals_one_run(oracle_mod, native_lib):
@@ -75,6 +95,24 @@ def test_run_in_pieces_equals_one_run(oracle_mod, native_lib):
     for c in range(9):
         assert np.array_equal(a.get_field(c), b.get_field(c))
     assert np.array_equal(a.get_seismo(), b.get_seismo())
+
+
+@pytest.mark.parametrize("shape", [(33, 19, 21), (40, 9, 30), (64, 24, 9)])
+def test_ragged_tiles(shape, oracle_mod, native_lib):
+    """Grid sizes that are not multiples of the 32 x 8 tile or of the k chunk."""
+    import fwant_gb300 as fw
+    from fwant_gb300 import inputs
+    ni, nj, nk = shape
+    m = inputs.make_model(ni, nj, nk, seed=5, npml=3, nrecv=3, source="buried", fc=2.0, t0=0.6)
+    met = oracle_mod.metric(m.x, m.y, m.z)
+    g = inputs.attach(fw.Solver(ni, nj, nk, m.stept, exact_arith=True), m, metric=met)
+    o = inputs.attach(oracle_mod.Oracle(ni, nj, nk, m.stept), m, metric=met)
+    g.run(12)
+    o.run(12)
+    for c in range(9):
+        b = interior(o.get_field(c))
+        if np.any(b):
+            assert rel_l2(interior(g.get_field(c)), b) < 1e-6, (shape, c)
 
 
 def test_fp64_metric(oracle_mod, native_lib):
@@ -100,9 +138,9 @@ def test_overflow_check_reports_nan(native_lib):
     """macdrp_check: a NaN planted in the host-side initial state is reported as an error
     status (no GPU fault: the value is uploaded as data)."""
     import fwant_gb300 as fw
+    from fwant_gb300 import inputs
     m = small_model("surface")
     s = fw.Solver(m.ni, m.nj, m.nk, m.stept)
-    from fwant_gb300 import inputs
     inputs.attach(s, m)
     s.check()
     f = np.zeros(s.shape, np.float32)
