@@ -16,10 +16,11 @@ __global__ void advance_record_kernel(const RecvArgs a) {
     const int m = nn / a.tinv - 1;
     if (m < a.cap) {
       for (int e = threadIdx.x; e < a.npt * NF; e += blockDim.x) {
-        const int pt = e % a.npt, f = e / a.npt;
+        const int pt = e % a.npt, f = e / a.npt;  // f in the output order Vx Vy Vz Txx Tyy Tzz Txy Txz Tyz
+        const int fi = f < 3 ? f : (f == 3 ? TXX : (f == 4 ? TYY : (f == 5 ? TZZ : (f == 6 ? TXY : (f == 7 ? TXZ : TYZ)))));
         const int i = a.idx[3 * pt], j = a.idx[3 * pt + 1], k = a.idx[3 * pt + 2];
         const long long p = (long long)(i + PADL) + (long long)a.g.px * ((long long)j + (long long)a.g.ny * k);
-        a.seismo[((long long)f * a.cap + m) * a.npt + pt] = a.w[f * a.g.fstride + p];
+        a.seismo[((long long)f * a.cap + m) * a.npt + pt] = a.w[fi * a.g.fstride + p];
       }
     }
   }

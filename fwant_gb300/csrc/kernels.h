@@ -1,13 +1,19 @@
 // Internal interface between the host driver (solver.cpp) and the CUDA kernels.
 // Plain structs only: they are passed to kernels by value.
 #pragma once
+#include <cuda.h>
+
 #include <cstddef>
 #include <cstdint>
 
 namespace fw {
 
-constexpr int NF = 9;  // Vx Vy Vz Txx Tyy Tzz Txy Txz Tyz
-enum { VX = 0, VY, VZ, TXX, TYY, TZZ, TXY, TXZ, TYZ };
+constexpr int NF = 9;
+// Storage order of the nine components inside a register set.  The six components
+// differentiated along k come first so that one TMA box fetches exactly them.
+enum { VX = 0, VY, VZ, TZZ, TXZ, TYZ, TXX, TYY, TXY };
+// C-ABI component order (Vx Vy Vz Txx Tyy Tzz Txy Txz Tyz) -> storage index
+constexpr int ABI2INT[NF] = {VX, VY, VZ, TXX, TYY, TZZ, TXY, TXZ, TYZ};
 constexpr int LENFD = 3;
 constexpr int PADL = 29;  // physical column of Fortran index i is (i-1)+PADL: interior starts at 32
 
@@ -16,9 +22,9 @@ constexpr int PADL = 29;  // physical column of Fortran index i is (i-1)+PADL: i
 // (i + PADL) + px*(j + ny*k).
 struct Geom {
   int ni, nj, nk, nx, ny, nz;
-  int px;                 // row pitch in elements
+  int px;                 // row pitch in elements (multiple of 32)
   long long plane;        // px*ny
-  long long fstride;      // elements between components of one register set
+  long long fstride;      // elements between components of one register set (multiple of 64)
   int i1, i2, j1, j2, k1, k2;  // interior, inclusive
   int freesurf;           // free surface on k = k2
 };
@@ -60,18 +66,23 @@ struct Sources {
   const float* mom_M;     // [nmom][ntwin][6] Mxx Myy Mzz Mxy Mxz Myz
 };
 
-// Everything one RK-stage launch needs.  S is the storage type of the wavefield
-// registers and PML memory variables; arithmetic is float (double for S = double).
-template <class S>
+// Stage-kernel tiling: a CTA owns TX x TY columns and marches along k.
+constexpr int STAGE_TX = 32, STAGE_TY = 8;
+// TMA boxes (x, y, 1 plane, components).  The halo'd tile starts 4 columns left of the
+// CTA's first column so that its x origin stays 16-byte aligned.
+constexpr int TILE_BX = STAGE_TX + 8, TILE_BY = STAGE_TY + 6;
+
+// Everything one RK-stage launch needs.
 struct StageArgs {
+  CUtensorMap tm_tile;  // stage input W: box TILE_BX x TILE_BY x 1 x 9
+  CUtensorMap tm_q;     // stage input W: box TX x TY x 1 x 6 (k-differentiated components)
+  CUtensorMap tm_m;     // RK register m: box TX x TY x 1 x 9
+  CUtensorMap tm_t;     // RK register t: box TX x TY x 1 x 9
+  CUtensorMap tm_med;   // lambda, mu, rho: box TX x TY x 1 x 3
   Geom g;
-  const S* win;   // stage input W (9 components)
-  const S* wm;    // step-start register m (stages 2,3)
-  S* wout;        // stage output W
-  S* wt;          // RK accumulator t
-  const float* lam;
-  const float* mu;
-  const float* rho;
+  const float* win;   // stage input W (9 components)
+  float* wout;        // stage output W
+  float* wt;          // RK accumulator t
   // 1-D metric, 0-based Fortran index, with ghosts
   const float* xi_x;
   const float* eta_y;
@@ -87,25 +98,26 @@ struct StageArgs {
   const float* pad[3];
   const float* pD[3];
   Slab slab[6];
-  const S* ain[6];
-  const S* am[6];
-  S* aout[6];
-  S* at[6];
+  const float* ain[6];
+  const float* am[6];
+  float* aout[6];
+  float* at[6];
   float a, b;     // rka*stept, rkb*stept
   int stage;      // 0..3 inside the step
   int kc;         // planes per CTA along k
   const int* ntime;  // device step counter
+  int* err;          // device error word (bounded-wait timeouts)
   Sources src;
-  int src_surface;
 };
 
 // Stage launchers (stage_*.cu).  variant bit 2 = x, bit 1 = y, bit 0 = z; 1 = forward
 // operator.  rk: 0 = RK_beg, 1 = RK_inn, 2 = RK_fin.  exact = 1 selects the reference's
 // operand order with IEEE division and no FMA (bit-reproducible against FP32 CPU runs
 // of the same expressions); 0 the fast form (FMA, reciprocals).
-void launch_stage_f32(const StageArgs<float>& a, int variant, int rk, int exact, void* stream);
+int launch_stage_f32(const StageArgs& a, int variant, int rk, int exact, void* stream);
 int stage_planes_per_cta(const Geom& g, int sm_count);
-constexpr int STAGE_TX = 32, STAGE_TY = 8;
+size_t stage_smem_bytes();
+int stage_configure();  // set the dynamic shared-memory attribute of every instantiation
 
 struct RecvArgs {
   Geom g;
@@ -113,7 +125,7 @@ struct RecvArgs {
   int npt;
   const int* idx;     // [npt][3] 0-based
   int tinv;
-  float* seismo;      // [9][cap][npt]
+  float* seismo;      // [9][cap][npt], C-ABI component order
   int cap;
   int* ntime;
 };
@@ -122,5 +134,8 @@ void launch_advance_record(const RecvArgs& a, void* stream);
 void launch_metric_fp64(int n, const float* coord, float* metric_out, int lo, int hi, void* stream);
 void launch_sincot_fp64(int n, const float* x, float* xsin, float* xcot, void* stream);
 void launch_maxabs(const Geom& g, const float* w, unsigned int* out_bits, void* stream);
+
+// device error codes written to StageArgs::err
+enum { DEVERR_NONE = 0, DEVERR_TMA_TIMEOUT = 1 };
 
 }  // namespace fw

@@ -53,8 +53,13 @@ struct fwant_solver {
   // four register sets of nine components each (W ping-pong, m, t; see run_step)
   float* regs = nullptr;
   int rA = 0, rB = 1, rC = 2, rT = 3;
+  float* med = nullptr;  // lambda, mu, rho, fstride apart (one TMA tensor)
   float *lam = nullptr, *mu = nullptr, *rho = nullptr;
   std::vector<float> h_rho;
+  int* d_err = nullptr;  // device error word of the stage kernel (bounded waits)
+  // TMA descriptors: per register set the halo'd tile, the z-queue plane and the point
+  // box; one for the medium
+  CUtensorMap tm_tile[4], tm_q[4], tm_pt[4], tm_med;
   // 1-D arrays, each with nx/ny/nz entries
   float *d_x = nullptr, *d_y = nullptr, *d_z = nullptr, *d_xsin = nullptr, *d_xcot = nullptr;
   float *d_xi = nullptr, *d_eta = nullptr, *d_zeta = nullptr;
@@ -97,7 +102,7 @@ struct fwant_solver {
     cudaSetDevice(cfg.device);
     drop_graphs();
     free_sources();
-    cudaFree(regs); cudaFree(lam); cudaFree(mu); cudaFree(rho);
+    cudaFree(regs); cudaFree(med); cudaFree(d_err);
     cudaFree(d_x); cudaFree(d_y); cudaFree(d_z); cudaFree(d_xsin); cudaFree(d_xcot);
     cudaFree(d_xi); cudaFree(d_eta); cudaFree(d_zeta); cudaFree(d_prof); cudaFree(d_rzinv); cudaFree(d_rsinv);
     for (int f = 0; f < 6; ++f) cudaFree(aux[f]);
@@ -166,20 +171,25 @@ struct fwant_solver {
     cudaEventCreate(&ev1);
     const size_t nreg = size_t(4) * fw::NF * g.fstride;
     regs = dalloc<float>(nreg);
-    lam = dalloc<float>(g.fstride); mu = dalloc<float>(g.fstride); rho = dalloc<float>(g.fstride);
+    med = dalloc<float>(3 * size_t(g.fstride));
+    lam = med; mu = med + g.fstride; rho = med + 2 * g.fstride;
+    d_err = dalloc<int>(1);
     d_x = dalloc<float>(g.nx); d_y = dalloc<float>(g.ny); d_z = dalloc<float>(g.nz);
     d_xsin = dalloc<float>(g.nx); d_xcot = dalloc<float>(g.nx); d_xi = dalloc<float>(g.nx);
     d_eta = dalloc<float>(g.ny); d_zeta = dalloc<float>(g.nz);
     d_prof = dalloc<float>(4 * size_t(g.nx + g.ny + g.nz));
     d_rzinv = dalloc<float>(g.nz); d_rsinv = dalloc<float>(g.nx);
     d_ntime = dalloc<int>(1); d_maxbits = dalloc<unsigned int>(1);
-    if (!regs || !lam || !mu || !rho || !d_x || !d_y || !d_z || !d_xsin || !d_xcot || !d_xi || !d_eta ||
+    if (!regs || !med || !d_err || !d_x || !d_y || !d_z || !d_xsin || !d_xcot || !d_xi || !d_eta ||
         !d_zeta || !d_prof || !d_rzinv || !d_rsinv || !d_ntime || !d_maxbits)
       return fail(FWANT_ERR_OOM, "device allocation failed");
     cudaMemset(regs, 0, nreg * sizeof(float));
-    cudaMemset(lam, 0, g.fstride * sizeof(float)); cudaMemset(mu, 0, g.fstride * sizeof(float));
-    cudaMemset(rho, 0, g.fstride * sizeof(float));
+    cudaMemset(med, 0, 3 * g.fstride * sizeof(float));
     cudaMemset(d_ntime, 0, sizeof(int));
+    cudaMemset(d_err, 0, sizeof(int));
+    fwant_status rc = make_tensor_maps();
+    if (rc != FWANT_OK) return rc;
+    if (int ce = fw::stage_configure()) return cuda_fail(cudaError_t(ce), "stage kernel configuration");
     for (int a = 0; a < 3; ++a) {
       const int n = a == 0 ? g.nx : a == 1 ? g.ny : g.nz;
       hA[a].assign(n, 0.0f); hB[a].assign(n, 1.0f); hD[a].assign(n, 0.0f);
@@ -214,6 +224,37 @@ struct fwant_solver {
     for (int a = 0; a < axis; ++a) p += 4 * hA[a].size();
     return p + which * hA[axis].size();
   }
+  // TMA descriptors over the padded layout: 4-D tensors (x: px, y: ny, z: nz,
+  // component) with the component stride fstride.  Out-of-range box elements read 0.
+  fwant_status make_tensor_maps() {
+    using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || !fn || q != cudaDriverEntryPointSuccess)
+      return fail(FWANT_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+    EncodeFn encode = reinterpret_cast<EncodeFn>(fn);
+    auto make = [&](CUtensorMap* m, float* base, int ncomp, cuuint32_t bx, cuuint32_t by, cuuint32_t bc) {
+      const cuuint64_t dims[4] = {cuuint64_t(g.px), cuuint64_t(g.ny), cuuint64_t(g.nz), cuuint64_t(ncomp)};
+      const cuuint64_t strides[3] = {cuuint64_t(g.px) * 4, cuuint64_t(g.plane) * 4, cuuint64_t(g.fstride) * 4};
+      const cuuint32_t box[4] = {bx, by, 1, bc};
+      const cuuint32_t es[4] = {1, 1, 1, 1};
+      return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    };
+    for (int r = 0; r < 4; ++r) {
+      if (make(&tm_tile[r], set(r), fw::NF, fw::TILE_BX, fw::TILE_BY, fw::NF) != CUDA_SUCCESS ||
+          make(&tm_q[r], set(r), fw::NF, fw::STAGE_TX, fw::STAGE_TY, 6) != CUDA_SUCCESS ||
+          make(&tm_pt[r], set(r), fw::NF, fw::STAGE_TX, fw::STAGE_TY, fw::NF) != CUDA_SUCCESS)
+        return fail(FWANT_ERR_CUDA, "tensor map encoding failed");
+    }
+    if (make(&tm_med, med, 3, fw::STAGE_TX, fw::STAGE_TY, 3) != CUDA_SUCCESS)
+      return fail(FWANT_ERR_CUDA, "tensor map encoding failed");
+    return FWANT_OK;
+  }
+
   // 1/z and 1/xsin for the fast arithmetic form
   cudaError_t upload_reciprocals() {
     std::vector<float> rz(g.nz), rs(g.nx);
@@ -493,10 +534,11 @@ struct fwant_solver {
     return FWANT_OK;
   }
 
-  fw::StageArgs<float> base_args() const {
-    fw::StageArgs<float> a{};
+  fw::StageArgs base_args() const {
+    fw::StageArgs a{};
     a.g = g;
-    a.lam = lam; a.mu = mu; a.rho = rho;
+    a.tm_med = tm_med;
+    a.err = d_err;
     a.xi_x = d_xi; a.eta_y = d_eta; a.zeta_z = d_zeta; a.xsin = d_xsin; a.xcot = d_xcot; a.zc = d_z;
     a.rzinv = d_rzinv; a.rsinv = d_rsinv;
     for (int ax = 0; ax < 3; ++ax) {
@@ -506,7 +548,6 @@ struct fwant_solver {
     for (int f = 0; f < 6; ++f) a.slab[f] = slab[f];
     a.ntime = d_ntime;
     a.src = S;
-    a.src_surface = cfg.src_surface;
     return a;
   }
 
@@ -514,13 +555,15 @@ struct fwant_solver {
   // Register-set roles: A holds W at the step start (and is the RK "m" register), T is
   // the RK "t" accumulator; B and C are the stage outputs.  Stage 4 writes W(n+1) into
   // T in place, after which A and T swap roles.
-  void enqueue_step(cudaEvent_t* ev = nullptr) {
+  int enqueue_step(cudaEvent_t* ev = nullptr) {
     const int X = CYCLE[cycle_pos & 7];
-    fw::StageArgs<float> a = base_args();
+    fw::StageArgs a = base_args();
     const int in_of[4] = {rA, rB, rC, rB};
     const int out_of[4] = {rB, rC, rB, rT};
+    int lerr = 0;
     for (int s = 0; s < 4; ++s) {
-      a.win = set(in_of[s]); a.wm = set(rA); a.wout = set(out_of[s]); a.wt = set(rT);
+      a.win = set(in_of[s]); a.wout = set(out_of[s]); a.wt = set(rT);
+      a.tm_tile = tm_tile[in_of[s]]; a.tm_q = tm_q[in_of[s]]; a.tm_m = tm_pt[rA]; a.tm_t = tm_pt[rT];
       for (int f = 0; f < 6; ++f) {
         if (!slab[f].on) continue;
         a.ain[f] = aset(f, in_of[s]); a.am[f] = aset(f, rA); a.aout[f] = aset(f, out_of[s]); a.at[f] = aset(f, rT);
@@ -531,7 +574,8 @@ struct fwant_solver {
       const int v = (s % 2 == 0) ? X : (~X & 7);
       const int rk = s == 0 ? 0 : (s == 3 ? 2 : 1);
       if (ev) cudaEventRecord(ev[s], st);
-      fw::launch_stage_f32(a, v, rk, cfg.exact_arith, st);
+      const int le = fw::launch_stage_f32(a, v, rk, cfg.exact_arith, st);
+      if (le && !lerr) lerr = le;
     }
     if (ev) cudaEventRecord(ev[4], st);
     fw::RecvArgs r{};
@@ -542,6 +586,18 @@ struct fwant_solver {
     std::swap(rA, rT);
     cycle_pos = (cycle_pos + 1) & 7;
     ntime += 1;
+    return lerr;
+  }
+
+  // device error word written by the stage kernel's bounded waits
+  fwant_status check_device_error() {
+    int h = 0;
+    cudaMemcpy(&h, d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (h == fw::DEVERR_TMA_TIMEOUT) {
+      cudaMemset(d_err, 0, sizeof(int));
+      return fail(FWANT_ERR_TIMEOUT, "stage kernel: TMA copy did not complete within the wait bound");
+    }
+    return FWANT_OK;
   }
 
   fwant_status run(int nsteps) {
@@ -562,8 +618,10 @@ struct fwant_solver {
           cudaGraph_t gr;
           cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
           if (e != cudaSuccess) return cuda_fail(e, "begin capture");
-          for (int q = 0; q < 8; ++q) enqueue_step();
+          int lerr = 0;
+          for (int q = 0; q < 8; ++q) lerr |= enqueue_step();
           e = cudaStreamEndCapture(st, &gr);
+          if (e == cudaSuccess && lerr) e = cudaError_t(lerr);
           if (e != cudaSuccess) return cuda_fail(e, "end capture");
           ntime = save_ntime;
           e = cudaGraphInstantiate(&graph[gi], gr, 0);
@@ -575,7 +633,8 @@ struct fwant_solver {
         ntime += 8;
         left -= 8;
       } else {
-        enqueue_step();
+        const int le = enqueue_step();
+        if (le) return cuda_fail(cudaError_t(le), "stage launch");
         left -= 1;
       }
     }
@@ -583,6 +642,7 @@ struct fwant_solver {
     cudaError_t e = cudaEventSynchronize(ev1);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "run");
+    if ((rc = check_device_error()) != FWANT_OK) return rc;
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, ev0, ev1);
     last_ms = ms;
@@ -602,7 +662,8 @@ struct fwant_solver {
     if ((rc = prepare_receivers(ntime + nsteps)) != FWANT_OK) return rc;
     std::vector<cudaEvent_t> ev(size_t(6) * nsteps);
     for (auto& e : ev) cudaEventCreate(&e);
-    for (int q = 0; q < nsteps; ++q) enqueue_step(&ev[size_t(6) * q]);
+    int lerr = 0;
+    for (int q = 0; q < nsteps; ++q) lerr |= enqueue_step(&ev[size_t(6) * q]);
     cudaError_t e = cudaStreamSynchronize(st);
     if (e == cudaSuccess) e = cudaGetLastError();
     double acc[5] = {0, 0, 0, 0, 0};
@@ -614,7 +675,9 @@ struct fwant_solver {
           acc[k] += ms;
         }
     for (auto& x : ev) cudaEventDestroy(x);
+    if (e == cudaSuccess && lerr) e = cudaError_t(lerr);
     if (e != cudaSuccess) return cuda_fail(e, "profile");
+    if ((rc = check_device_error()) != FWANT_OK) return rc;
     for (int k = 0; k < 4; ++k) stage_ms[k] = acc[k] / nsteps;
     *other_ms = acc[4] / nsteps;
     if (npt > 0) nsamp = std::max(nsamp, std::min(ntime / tinv, cap));
@@ -830,7 +893,7 @@ fwant_status fwant_get_seismo(fwant_solver* s, float* out, int max_samples, int*
 fwant_status fwant_get_field(fwant_solver* s, int component, float* out) {
   if (!s || !out || component < 0 || component >= fw::NF) return FWANT_ERR_INVALID_ARG;
   cudaSetDevice(s->cfg.device);
-  cudaError_t e = s->get3(out, s->set(s->rA) + component * s->g.fstride);
+  cudaError_t e = s->get3(out, s->set(s->rA) + fw::ABI2INT[component] * s->g.fstride);
   if (e != cudaSuccess) return s->cuda_fail(e, "get_field");
   return FWANT_OK;
 }
@@ -845,7 +908,7 @@ fwant_status fwant_set_field(fwant_solver* s, int component, const float* in) {
       for (int i = 0; i < g.nx; ++i)
         if (i < g.i1 || i > g.i2 || j < g.j1 || j > g.j2 || k < g.k1 || k > g.k2)
           tmp[size_t(i) + size_t(g.nx) * (size_t(j) + size_t(g.ny) * k)] = 0.0f;
-  cudaError_t e = s->put3(s->set(s->rA) + component * g.fstride, tmp.data());
+  cudaError_t e = s->put3(s->set(s->rA) + fw::ABI2INT[component] * g.fstride, tmp.data());
   if (e != cudaSuccess) return s->cuda_fail(e, "set_field");
   return FWANT_OK;
 }

@@ -2,27 +2,46 @@
 #include <cuda_runtime.h>
 
 #include "kernels.h"
+#include "stage_impl.cuh"
 
 namespace fw {
 
-void launch_stage_fast_rk0(const StageArgs<float>&, int, cudaStream_t);
-void launch_stage_fast_rk1(const StageArgs<float>&, int, cudaStream_t);
-void launch_stage_fast_rk2(const StageArgs<float>&, int, cudaStream_t);
-void launch_stage_exact_rk0(const StageArgs<float>&, int, cudaStream_t);
-void launch_stage_exact_rk1(const StageArgs<float>&, int, cudaStream_t);
-void launch_stage_exact_rk2(const StageArgs<float>&, int, cudaStream_t);
+int launch_stage_fast_rk0(const StageArgs&, int, cudaStream_t);
+int launch_stage_fast_rk1(const StageArgs&, int, cudaStream_t);
+int launch_stage_fast_rk2(const StageArgs&, int, cudaStream_t);
+int launch_stage_exact_rk0(const StageArgs&, int, cudaStream_t);
+int launch_stage_exact_rk1(const StageArgs&, int, cudaStream_t);
+int launch_stage_exact_rk2(const StageArgs&, int, cudaStream_t);
 
-void launch_stage_f32(const StageArgs<float>& a, int variant, int rk, int exact, void* stream) {
+int launch_stage_f32(const StageArgs& a, int variant, int rk, int exact, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   if (exact) {
-    if (rk == 0) launch_stage_exact_rk0(a, variant, st);
-    else if (rk == 1) launch_stage_exact_rk1(a, variant, st);
-    else launch_stage_exact_rk2(a, variant, st);
-  } else {
-    if (rk == 0) launch_stage_fast_rk0(a, variant, st);
-    else if (rk == 1) launch_stage_fast_rk1(a, variant, st);
-    else launch_stage_fast_rk2(a, variant, st);
+    if (rk == 0) return launch_stage_exact_rk0(a, variant, st);
+    if (rk == 1) return launch_stage_exact_rk1(a, variant, st);
+    return launch_stage_exact_rk2(a, variant, st);
   }
+  if (rk == 0) return launch_stage_fast_rk0(a, variant, st);
+  if (rk == 1) return launch_stage_fast_rk1(a, variant, st);
+  return launch_stage_fast_rk2(a, variant, st);
+}
+
+size_t stage_smem_bytes() { return SMEM_BYTES; }
+
+int configure_stage_fast_rk0();
+int configure_stage_fast_rk1();
+int configure_stage_fast_rk2();
+int configure_stage_exact_rk0();
+int configure_stage_exact_rk1();
+int configure_stage_exact_rk2();
+
+int stage_configure() {
+  int e = configure_stage_fast_rk0();
+  if (!e) e = configure_stage_fast_rk1();
+  if (!e) e = configure_stage_fast_rk2();
+  if (!e) e = configure_stage_exact_rk0();
+  if (!e) e = configure_stage_exact_rk1();
+  if (!e) e = configure_stage_exact_rk2();
+  return e;
 }
 
 // Planes per CTA: long enough that the z-halo re-load (4 planes per chunk) stays small,

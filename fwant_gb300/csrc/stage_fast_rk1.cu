@@ -1,9 +1,10 @@
-// Instantiation unit: fast arithmetic, RK kind 1 (RK_inn).
-// Compiled with FMA contraction; the kernel itself is in stage_impl.cuh.
+// Instantiation unit of the stage kernel (stage_impl.cuh): fast arithmetic, compiled with FMA contraction; RK kind 1
+// (0 RK_beg, 1 RK_inn, 2 RK_fin).
 #include "stage_impl.cuh"
 
 namespace fw {
-void launch_stage_fast_rk1(const StageArgs<float>& a, int variant, cudaStream_t st) {
-  launch_rk_variant<false, 1>(a, variant, st);
+int launch_stage_fast_rk1(const StageArgs& a, int variant, cudaStream_t st) {
+  return launch_rk_variant<false, 1>(a, variant, st);
 }
+int configure_stage_fast_rk1() { return configure_rk<false, 1>(); }
 }  // namespace fw

@@ -1,9 +1,10 @@
-// Instantiation unit: fast arithmetic, RK kind 2 (RK_fin).
-// Compiled with FMA contraction; the kernel itself is in stage_impl.cuh.
+// Instantiation unit of the stage kernel (stage_impl.cuh): fast arithmetic, compiled with FMA contraction; RK kind 2
+// (0 RK_beg, 1 RK_inn, 2 RK_fin).
 #include "stage_impl.cuh"
 
 namespace fw {
-void launch_stage_fast_rk2(const StageArgs<float>& a, int variant, cudaStream_t st) {
-  launch_rk_variant<false, 2>(a, variant, st);
+int launch_stage_fast_rk2(const StageArgs& a, int variant, cudaStream_t st) {
+  return launch_rk_variant<false, 2>(a, variant, st);
 }
+int configure_stage_fast_rk2() { return configure_rk<false, 2>(); }
 }  // namespace fw
