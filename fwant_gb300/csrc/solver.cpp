@@ -242,7 +242,7 @@ struct fwant_solver {
       const cuuint32_t box[4] = {bx, by, 1, bc};
       const cuuint32_t es[4] = {1, 1, 1, 1};
       return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     };
     for (int r = 0; r < 4; ++r) {
       if (make(&tm_tile[r], set(r), fw::NF, fw::TILE_BX, fw::TILE_BY, fw::NF) != CUDA_SUCCESS ||

@@ -91,6 +91,41 @@ __device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(bar)
       : "memory");
 }
+// Same with an L2 cache policy (createpolicy) attached.
+__device__ __forceinline__ void tma_load_4d_hint(uint32_t dst, const CUtensorMap* map, int x, int y, int z, int w,
+                                                 uint32_t bar, uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1, {%2, %3, "
+      "%4, %5}], [%6], %7;" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(bar), "l"(policy)
+      : "memory");
+}
+// L2 policies: streams with no reuse inside the launch are marked evict-first so that the
+// stage input planes, which neighbouring tiles and later planes re-read, stay in L2.
+__device__ __forceinline__ uint64_t policy_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t policy_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ void st_stream(float* p, float v, uint64_t policy) {
+  asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(v), "l"(policy) : "memory");
+}
+__device__ __forceinline__ float ld_stream(const float* p, uint64_t policy) {
+  float v;
+  asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(policy));
+  return v;
+}
+// read of a location this thread writes back afterwards (not the non-coherent path)
+__device__ __forceinline__ float ld_rw_stream(const float* p, uint64_t policy) {
+  float v;
+  asm volatile("ld.global.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(policy) : "memory");
+  return v;
+}
 
 // ---- one-sided operators ------------------------------------------------------------
 // DRP/opt MacCormack operators (mod_macdrp.h:69-103) on values at offsets -3..+3 of c.
@@ -164,16 +199,19 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
   }
   __syncthreads();
 
+  const uint64_t pol_stream = policy_evict_first();
+  const uint64_t pol_keep = policy_evict_last();
   auto issue = [&](int kp, int b) {
     const uint32_t base = smem_u32(smem + b * BUF_BYTES);
     const uint32_t bar = bar0 + 8 * b;
     fence_proxy_async();
     mbar_expect_tx(bar, TX_BYTES);
     tma_load_4d(base, &A.tm_tile, i0 - HX + PADL, j0 - HY, kp, 0, bar);
-    tma_load_4d(base + OFF_Q, &A.tm_q, i0 + PADL, j0, kp + LEAD, 0, bar);
-    tma_load_4d(base + OFF_MED, &A.tm_med, i0 + PADL, j0, kp, 0, bar);
-    if (RK == 1) tma_load_4d(base + OFF_M, &A.tm_m, i0 + PADL, j0, kp, 0, bar);
-    if (RK >= 1) tma_load_4d(base + OFF_T, &A.tm_t, i0 + PADL, j0, kp, 0, bar);
+    // plane kp+LEAD comes back as the tile of a later iteration: keep it in L2
+    tma_load_4d_hint(base + OFF_Q, &A.tm_q, i0 + PADL, j0, kp + LEAD, 0, bar, pol_keep);
+    tma_load_4d_hint(base + OFF_MED, &A.tm_med, i0 + PADL, j0, kp, 0, bar, pol_stream);
+    if (RK == 1) tma_load_4d_hint(base + OFF_M, &A.tm_m, i0 + PADL, j0, kp, 0, bar, pol_stream);
+    if (RK >= 1) tma_load_4d_hint(base + OFF_T, &A.tm_t, i0 + PADL, j0, kp, 0, bar, pol_stream);
   };
   if (tid == 0) issue(kb, 0);
 
@@ -388,7 +426,7 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
         const float* __restrict__ ai = A.ain[sidx] + qa;
         float av[6], h[6];
 #pragma unroll
-        for (int v = 0; v < 6; ++v) av[v] = __ldg(ai + v * vs);
+        for (int v = 0; v < 6; ++v) av[v] = ld_stream(ai + v * vs, pol_stream);
         hVx = hVx + (b1_1 * d[0] - b1 * av[0]) * rrho; h[0] = Dv * d[0] - ad * av[0];
         hVy = hVy + (b1_1 * d[1] - b1 * av[1]) * rrho; h[1] = Dv * d[1] - ad * av[1];
         hVz = hVz + (b1_1 * d[2] - b1 * av[2]) * rrho; h[2] = Dv * d[2] - ad * av[2];
@@ -434,13 +472,13 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
 #pragma unroll
         for (int v = 0; v < 6; ++v) {
           if (RK == 0) {
-            ao[v * vs] = av[v] + A.a * h[v];
-            at[v * vs] = av[v] + A.b * h[v];
+            st_stream(ao + v * vs, av[v] + A.a * h[v], pol_stream);
+            st_stream(at + v * vs, av[v] + A.b * h[v], pol_stream);
           } else if (RK == 1) {
-            ao[v * vs] = __ldg(A.am[sidx] + qa + v * vs) + A.a * h[v];
-            at[v * vs] = at[v * vs] + A.b * h[v];
+            st_stream(ao + v * vs, ld_stream(A.am[sidx] + qa + v * vs, pol_stream) + A.a * h[v], pol_stream);
+            st_stream(at + v * vs, ld_rw_stream(at + v * vs, pol_stream) + A.b * h[v], pol_stream);
           } else {
-            at[v * vs] = at[v * vs] + A.b * h[v];
+            st_stream(at + v * vs, ld_rw_stream(at + v * vs, pol_stream) + A.b * h[v], pol_stream);
           }
         }
       }
@@ -488,13 +526,13 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
           // the tile holds the stored input; on the surface the imaged components were
           // patched in shared memory, so read those three from global memory there
           const float m = (top && (f == TZZ || f == TXZ || f == TYZ)) ? __ldg(W + o) : tile[f][r0][c0];
-          A.wout[o] = m + A.a * hh[f];
-          A.wt[o] = m + A.b * hh[f];
+          st_stream(A.wout + o, m + A.a * hh[f], pol_stream);
+          st_stream(A.wt + o, m + A.b * hh[f], pol_stream);
         } else if (RK == 1) {
-          A.wout[o] = mbuf[f][ty][tx] + A.a * hh[f];
-          A.wt[o] = tbuf[f][ty][tx] + A.b * hh[f];
+          st_stream(A.wout + o, mbuf[f][ty][tx] + A.a * hh[f], pol_stream);
+          st_stream(A.wt + o, tbuf[f][ty][tx] + A.b * hh[f], pol_stream);
         } else {
-          A.wt[o] = tbuf[f][ty][tx] + A.b * hh[f];
+          st_stream(A.wt + o, tbuf[f][ty][tx] + A.b * hh[f], pol_stream);
         }
       }
     }
