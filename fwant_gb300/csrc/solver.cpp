@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -166,6 +167,10 @@ struct fwant_solver {
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, cfg.device);
     kc = fw::stage_planes_per_cta(g, nsm > 0 ? nsm : 152);
+    if (const char* env = std::getenv("FWANT_PLANES_PER_CTA")) {  // tuning override
+      const int v = std::atoi(env);
+      if (v >= 1) kc = v;
+    }
     if ((e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
     cudaEventCreate(&ev0);
     cudaEventCreate(&ev1);
