@@ -54,6 +54,7 @@ EXPORTS = [
     ("fwant_get_seismo", C.c_int, [_vp, _fp, C.c_int, _ip]),
     ("fwant_get_field", C.c_int, [_vp, C.c_int, _fp]),
     ("fwant_set_field", C.c_int, [_vp, C.c_int, _fp]),
+    ("fwant_get_snapshot", C.c_int, [_vp, _ip, _ip, _ip, C.c_int, _ip, _fp]),
     ("fwant_check", C.c_int, [_vp]),
     ("fwant_profile_stages", C.c_int, [_vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("fwant_last_run_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
@@ -256,6 +257,22 @@ class Solver:
         c = COMPONENTS.index(component) if isinstance(component, str) else int(component)
         a = _fortran3(values, self.shape)
         self._chk(self._lib.fwant_set_field(self._h, c, _ptr(a)))
+
+    @staticmethod
+    def _snap_args(subs, subc, subt, comps):
+        comps = [COMPONENTS.index(c) if isinstance(c, str) else int(c) for c in comps]
+        a = [np.ascontiguousarray(np.asarray(v, dtype=np.int32).reshape(3)) for v in (subs, subc, subt)]
+        cm = np.ascontiguousarray(np.asarray(comps, dtype=np.int32))
+        out = np.zeros(int(np.prod(a[1], dtype=np.int64)) * len(comps), np.float32)
+        return a, cm, out
+
+    def get_snapshot(self, subs, subc, subt, comps=("Vx", "Vy", "Vz")):
+        """Strided sub-volume (1-based subs with ghosts, counts, strides) of the current
+        wavefield; returns array (ncomp, nI, nJ, nK) indexed [c, i, j, k]."""
+        (s0, c0, t0), cm, out = self._snap_args(subs, subc, subt, comps)
+        self._chk(self._lib.fwant_get_snapshot(self._h, _ptr(s0, C.c_int), _ptr(c0, C.c_int), _ptr(t0, C.c_int),
+                                               len(cm), _ptr(cm, C.c_int), _ptr(out)))
+        return out.reshape(len(cm), int(c0[2]), int(c0[1]), int(c0[0])).transpose(0, 3, 2, 1)
 
     def check(self):
         """macdrp_check: raises FwantError(NUMERIC_OVERFLOW) on NaN/Inf/huge."""

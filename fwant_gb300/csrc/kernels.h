@@ -131,6 +131,18 @@ struct RecvArgs {
 };
 void launch_advance_record(const RecvArgs& a, void* stream);
 
+// Strided sub-volume of one register set (snapshot frame).  start is 0-based (Fortran
+// index minus one); comp holds storage indices; out is [ncomp][cnt2][cnt1][cnt0].
+struct SnapArgs {
+  Geom g;
+  const float* w;
+  int start[3], cnt[3], stride[3];
+  int ncomp;
+  int comp[NF];
+  float* out;
+};
+void launch_pack_snapshot(const SnapArgs& a, void* stream);
+
 void launch_metric_fp64(int n, const float* coord, float* metric_out, int lo, int hi, void* stream);
 void launch_sincot_fp64(int n, const float* x, float* xsin, float* xcot, void* stream);
 void launch_maxabs(const Geom& g, const float* w, unsigned int* out_bits, void* stream);

@@ -1,0 +1,34 @@
+// Strided sub-volume extraction of the wavefield: the data of one snapshot frame of
+// io_wave_export (mod_io.F90:505-645), packed on the device into a staging buffer and
+// copied to the host.
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+
+namespace fw {
+
+__global__ void pack_snapshot_kernel(const SnapArgs a) {
+  const long long n = (long long)a.cnt[0] * a.cnt[1] * a.cnt[2];
+  const long long tot = n * a.ncomp;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
+    const int c = int(e / n);
+    long long r = e - (long long)c * n;
+    const int ii = int(r % a.cnt[0]);
+    r /= a.cnt[0];
+    const int jj = int(r % a.cnt[1]);
+    const int kk = int(r / a.cnt[1]);
+    const int i = a.start[0] + ii * a.stride[0], j = a.start[1] + jj * a.stride[1], k = a.start[2] + kk * a.stride[2];
+    const long long p = (long long)(i + PADL) + (long long)a.g.px * ((long long)j + (long long)a.g.ny * k);
+    a.out[e] = a.w[a.comp[c] * a.g.fstride + p];
+  }
+}
+
+void launch_pack_snapshot(const SnapArgs& a, void* stream) {
+  const long long tot = (long long)a.cnt[0] * a.cnt[1] * a.cnt[2] * a.ncomp;
+  long long blocks = (tot + 255) / 256;
+  if (blocks > 152LL * 16) blocks = 152LL * 16;
+  if (blocks < 1) blocks = 1;
+  pack_snapshot_kernel<<<int(blocks), 256, 0, (cudaStream_t)stream>>>(a);
+}
+
+}  // namespace fw

@@ -94,6 +94,8 @@ struct fwant_solver {
   int* d_ntime = nullptr;
   int ntime = 0, cycle_pos = 0;
   unsigned int* d_maxbits = nullptr;
+  float* d_snap = nullptr;  // staging buffer of fwant_get_snapshot (grown on demand)
+  size_t snap_cap = 0;
 
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one per (rA,rT) assignment
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -107,7 +109,7 @@ struct fwant_solver {
     cudaFree(d_x); cudaFree(d_y); cudaFree(d_z); cudaFree(d_xsin); cudaFree(d_xcot);
     cudaFree(d_xi); cudaFree(d_eta); cudaFree(d_zeta); cudaFree(d_prof); cudaFree(d_rzinv); cudaFree(d_rsinv);
     for (int f = 0; f < 6; ++f) cudaFree(aux[f]);
-    cudaFree(d_rec); cudaFree(d_seis); cudaFree(d_ntime); cudaFree(d_maxbits);
+    cudaFree(d_rec); cudaFree(d_seis); cudaFree(d_ntime); cudaFree(d_maxbits); cudaFree(d_snap);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (st) cudaStreamDestroy(st);
@@ -594,6 +596,31 @@ struct fwant_solver {
     return lerr;
   }
 
+  // Validate a snapshot request (io_snap_read/corr_indx, mod_io.F90:180-300: the
+  // sub-volume lies in the interior) and fill the pack-kernel arguments; n = floats out.
+  fwant_status snap_setup(const int* subs, const int* subc, const int* subt, int ncomp, const int* comps,
+                          fw::SnapArgs& a, size_t& n) {
+    if (!subs || !subc || !subt || !comps || ncomp < 1 || ncomp > fw::NF)
+      return fail(FWANT_ERR_INVALID_ARG, "snapshot: bad arguments");
+    a = fw::SnapArgs{};
+    a.g = g;
+    a.w = set(rA);
+    const int lo[3] = {g.i1, g.j1, g.k1}, hi[3] = {g.i2, g.j2, g.k2};
+    for (int d = 0; d < 3; ++d) {
+      if (subc[d] < 1 || subt[d] < 1) return fail(FWANT_ERR_INVALID_ARG, "snapshot: counts and strides must be >= 1");
+      const int s0 = subs[d] - 1, e0 = s0 + subt[d] * (subc[d] - 1);
+      if (s0 < lo[d] || e0 > hi[d]) return fail(FWANT_ERR_INVALID_ARG, "snapshot: sub-volume outside the interior");
+      a.start[d] = s0; a.cnt[d] = subc[d]; a.stride[d] = subt[d];
+    }
+    for (int c = 0; c < ncomp; ++c) {
+      if (comps[c] < 0 || comps[c] >= fw::NF) return fail(FWANT_ERR_INVALID_ARG, "snapshot: bad component id");
+      a.comp[c] = fw::ABI2INT[comps[c]];
+    }
+    a.ncomp = ncomp;
+    n = size_t(subc[0]) * subc[1] * subc[2] * ncomp;
+    return FWANT_OK;
+  }
+
   // device error word written by the stage kernel's bounded waits
   fwant_status check_device_error() {
     int h = 0;
@@ -915,6 +942,29 @@ fwant_status fwant_set_field(fwant_solver* s, int component, const float* in) {
           tmp[size_t(i) + size_t(g.nx) * (size_t(j) + size_t(g.ny) * k)] = 0.0f;
   cudaError_t e = s->put3(s->set(s->rA) + fw::ABI2INT[component] * g.fstride, tmp.data());
   if (e != cudaSuccess) return s->cuda_fail(e, "set_field");
+  return FWANT_OK;
+}
+
+fwant_status fwant_get_snapshot(fwant_solver* s, const int subs[3], const int subc[3], const int subt[3], int ncomp,
+                                const int* comps, float* out) {
+  if (!s || !out) return FWANT_ERR_INVALID_ARG;
+  cudaSetDevice(s->cfg.device);
+  fw::SnapArgs a;
+  size_t n = 0;
+  fwant_status rc = s->snap_setup(subs, subc, subt, ncomp, comps, a, n);
+  if (rc != FWANT_OK) return rc;
+  if (n > s->snap_cap) {
+    cudaFree(s->d_snap);
+    s->d_snap = dalloc<float>(n);
+    s->snap_cap = s->d_snap ? n : 0;
+    if (!s->d_snap) return s->fail(FWANT_ERR_OOM, "snapshot staging buffer");
+  }
+  a.out = s->d_snap;
+  fw::launch_pack_snapshot(a, s->st);
+  cudaError_t e = cudaMemcpyAsync(out, s->d_snap, n * sizeof(float), cudaMemcpyDeviceToHost, s->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return s->cuda_fail(e, "get_snapshot");
   return FWANT_OK;
 }
 

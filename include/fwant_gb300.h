@@ -165,6 +165,17 @@ fwant_status fwant_get_field(fwant_solver* s, int component, float* out);
  * Only the interior is taken; ghosts stay zero. */
 fwant_status fwant_set_field(fwant_solver* s, int component, const float* in);
 
+/* Strided sub-volume of the current wavefield: the data one frame of the vel_/sgt_
+ * snapshot files holds (io_wave_export, code/srcF/mod_io.F90:505-645).  subs: first point
+ * (1-based Fortran indices with ghosts; the interior starts at 4), subc: points per axis,
+ * subt: stride per axis (snap_NNN subs/subc/subt, code/srcF/mod_io.F90:180-205; the
+ * sub-volume must lie in the interior).  comps: ncomp component ids (0..8, receiver order;
+ * the reference writes Vx Vy Vz or Txx Tyy Tzz Txy Txz Tyz).  out receives
+ * [ncomp][subc[2]][subc[1]][subc[0]] floats, i fastest: per component the (I,J,K) layout of
+ * one NetCDF snapshot frame (code/srcF/mod_nfseis.F90:131-203). */
+fwant_status fwant_get_snapshot(fwant_solver* s, const int subs[3], const int subc[3], const int subt[3],
+                                int ncomp, const int* comps, float* out);
+
 /* Overflow check of the nine components: macdrp_check (code/srcF/mod_macdrp.F90:228-264).
  * Returns FWANT_ERR_NUMERIC_OVERFLOW when a value is NaN, Inf or >= huge(1.0). */
 fwant_status fwant_check(fwant_solver* s);
