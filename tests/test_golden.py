@@ -1,0 +1,59 @@
+"""The oracle and the CUDA path against the committed golden fixtures
+(tests/golden/make_golden.py).  Tolerance 1e-6 relative: the fixtures were written on
+x86-64; host libm differences (expf, logf, sin) on another CPU stay far below it."""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import feed, interior, rel_l2, small_model
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+KINDS = ["surface", "buried", "nofree", "moment", "water"]
+
+
+def load(kind):
+    return np.load(os.path.join(HERE, "golden", f"oracle_{kind}_16steps.npz"))
+
+
+def check(sim, ref, kind):
+    sg = sim.get_seismo()
+    assert sg.shape == ref["seismo"].shape
+    for c in range(9):
+        if np.any(ref["seismo"][c]):
+            assert rel_l2(sg[c], ref["seismo"][c]) < 1e-6, (kind, "seismo", c)
+    vz = interior(sim.get_field(2))
+    assert rel_l2(vz, ref["vz"]) < 1e-6, (kind, "Vz")
+    for c in range(9):
+        f = interior(sim.get_field(c)).astype(np.float64)
+        s, s2, mx = ref["checksums"][c]
+        assert (f * f).sum() == pytest.approx(s2, rel=2e-6, abs=1e-30), (kind, c)
+        assert np.abs(f).max() == pytest.approx(mx, rel=1e-6, abs=1e-30), (kind, c)
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_oracle_reproduces_golden(kind, oracle_mod):
+    m = small_model(kind)
+    met = oracle_mod.metric(m.x, m.y, m.z)
+    o = feed(oracle_mod.Oracle(m.ni, m.nj, m.nk, m.stept, free_surface=m.free_surface), m, met, kind)
+    o.run(16)
+    check(o, load(kind), kind)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("exact", [True, False], ids=["exact", "fast"])
+@pytest.mark.parametrize("kind", KINDS)
+def test_cuda_matches_golden(kind, exact, oracle_mod, native_lib):
+    import fwant_gb300 as fw
+    m = small_model(kind)
+    met = oracle_mod.metric(m.x, m.y, m.z)
+    g = feed(fw.Solver(m.ni, m.nj, m.nk, m.stept, free_surface=m.free_surface, exact_arith=exact), m, met, kind)
+    g.run(16)
+    ref = load(kind)
+    if exact:
+        check(g, ref, kind)
+    else:
+        sg = g.get_seismo()
+        for c in range(9):
+            if np.any(ref["seismo"][c]):
+                assert rel_l2(sg[c], ref["seismo"][c]) < 1e-5, (kind, c)
