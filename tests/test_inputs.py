@@ -10,7 +10,8 @@ def test_grid_ghosts_extrapolate_linearly():
     g = inputs.grid_coords(10, 0.01, 45.0, None, 1.0, degrees=True)
     assert g.dtype == np.float32 and g.size == 16
     d = np.diff(g.astype(np.float64))
-    assert np.allclose(d, d[5], rtol=1e-4)
+    # FP32 colatitudes near 0.79 rad resolve a 1.7e-4 rad spacing only to ~1e-3
+    assert np.allclose(d, d[5], rtol=2e-3)
     assert g[3] == pytest.approx(np.deg2rad(45.0), rel=1e-7)
 
 
