@@ -53,7 +53,8 @@ def test_cuda_matches_golden(kind, exact, oracle_mod, native_lib):
     if exact:
         check(g, ref, kind)
     else:
+        # velocities and stresses as two groups: on the free surface Tzz, Txz and Tyz are
+        # rounding noise around zero, so their own relative error means nothing
         sg = g.get_seismo()
-        for c in range(9):
-            if np.any(ref["seismo"][c]):
-                assert rel_l2(sg[c], ref["seismo"][c]) < 1e-5, (kind, c)
+        for grp in (slice(0, 3), slice(3, 9)):
+            assert rel_l2(sg[grp], ref["seismo"][grp]) < 1e-5, (kind, grp)
