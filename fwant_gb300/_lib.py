@@ -55,6 +55,7 @@ EXPORTS = [
     ("fwant_get_field", C.c_int, [_vp, C.c_int, _fp]),
     ("fwant_set_field", C.c_int, [_vp, C.c_int, _fp]),
     ("fwant_get_snapshot", C.c_int, [_vp, _ip, _ip, _ip, C.c_int, _ip, _fp]),
+    ("fwant_get_snapshot_noalloc", C.c_int, [_vp, _ip, _ip, _ip, C.c_int, _ip, _fp]),
     ("fwant_check", C.c_int, [_vp]),
     ("fwant_profile_stages", C.c_int, [_vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("fwant_last_run_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
@@ -272,6 +273,14 @@ class Solver:
         (s0, c0, t0), cm, out = self._snap_args(subs, subc, subt, comps)
         self._chk(self._lib.fwant_get_snapshot(self._h, _ptr(s0, C.c_int), _ptr(c0, C.c_int), _ptr(t0, C.c_int),
                                                len(cm), _ptr(cm, C.c_int), _ptr(out)))
+        return out.reshape(len(cm), int(c0[2]), int(c0[1]), int(c0[0])).transpose(0, 3, 2, 1)
+
+    def get_snapshot_noalloc(self, subs, subc, subt, comps=("Vx", "Vy", "Vz")):
+        """get_snapshot through the entry point that allocates no device memory (staging in
+        a fixed 16 MiB device array shared by all calls on the device)."""
+        (s0, c0, t0), cm, out = self._snap_args(subs, subc, subt, comps)
+        self._chk(self._lib.fwant_get_snapshot_noalloc(self._h, _ptr(s0, C.c_int), _ptr(c0, C.c_int),
+                                                       _ptr(t0, C.c_int), len(cm), _ptr(cm, C.c_int), _ptr(out)))
         return out.reshape(len(cm), int(c0[2]), int(c0[1]), int(c0[0])).transpose(0, 3, 2, 1)
 
     def check(self):

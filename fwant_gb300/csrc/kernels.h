@@ -142,6 +142,9 @@ struct SnapArgs {
   float* out;
 };
 void launch_pack_snapshot(const SnapArgs& a, void* stream);
+// Fixed staging array of fwant_get_snapshot_noalloc (floats) and its per-device address.
+constexpr long long SNAPSHOT_NOALLOC_MAX = 4LL << 20;
+int snapshot_noalloc_staging(int device, float** ptr);
 
 void launch_metric_fp64(int n, const float* coord, float* metric_out, int lo, int hi, void* stream);
 void launch_sincot_fp64(int n, const float* x, float* xsin, float* xcot, void* stream);

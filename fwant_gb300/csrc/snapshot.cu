@@ -3,6 +3,8 @@
 // copied to the host.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "kernels.h"
 
 namespace fw {
@@ -29,6 +31,31 @@ void launch_pack_snapshot(const SnapArgs& a, void* stream) {
   if (blocks > 152LL * 16) blocks = 152LL * 16;
   if (blocks < 1) blocks = 1;
   pack_snapshot_kernel<<<int(blocks), 256, 0, (cudaStream_t)stream>>>(a);
+}
+
+// Staging buffer of fwant_get_snapshot_noalloc, for callers that must not allocate
+// device memory.  It is a module-scope device array, so it exists on every device that
+// loads this library, for as long as the library stays loaded; every call on a device
+// shares it.  The pack kernel writes every element that is copied out, so nothing in it
+// needs clearing between calls.
+static __device__ __align__(256) float g_snapshot_staging[SNAPSHOT_NOALLOC_MAX];
+
+// Device address of the staging array on `device`, resolved once per device (with that
+// device current, which the caller guarantees) and cached.
+static std::mutex g_staging_mutex;
+static float* g_staging_ptr[64] = {};
+
+int snapshot_noalloc_staging(int device, float** ptr) {
+  if (device < 0 || device >= 64) return int(cudaErrorInvalidDevice);
+  std::lock_guard<std::mutex> lock(g_staging_mutex);
+  if (!g_staging_ptr[device]) {
+    float* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_snapshot_staging);
+    if (e != cudaSuccess) return int(e);
+    g_staging_ptr[device] = p;
+  }
+  *ptr = g_staging_ptr[device];
+  return 0;
 }
 
 }  // namespace fw

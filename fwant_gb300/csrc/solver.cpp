@@ -968,6 +968,33 @@ fwant_status fwant_get_snapshot(fwant_solver* s, const int subs[3], const int su
   return FWANT_OK;
 }
 
+fwant_status fwant_get_snapshot_noalloc(fwant_solver* s, const int subs[3], const int subc[3], const int subt[3],
+                                        int ncomp, const int* comps, float* out) {
+  if (!s || !out) return FWANT_ERR_INVALID_ARG;
+  cudaError_t e = cudaSetDevice(s->cfg.device);
+  if (e != cudaSuccess) return s->cuda_fail(e, "get_snapshot_noalloc");
+  fw::SnapArgs a;
+  size_t n = 0;
+  fwant_status rc = s->snap_setup(subs, subc, subt, ncomp, comps, a, n);
+  if (rc != FWANT_OK) return rc;
+  if (n > size_t(fw::SNAPSHOT_NOALLOC_MAX)) {
+    char b[160];
+    std::snprintf(b, sizeof(b), "get_snapshot_noalloc: %zu values requested, the fixed staging buffer holds %lld",
+                  n, fw::SNAPSHOT_NOALLOC_MAX);
+    return s->fail(FWANT_ERR_INVALID_ARG, b);
+  }
+  float* staging = nullptr;
+  if (int ge = fw::snapshot_noalloc_staging(s->cfg.device, &staging))
+    return s->cuda_fail(cudaError_t(ge), "get_snapshot_noalloc: staging address");
+  a.out = staging;
+  fw::launch_pack_snapshot(a, s->st);
+  e = cudaMemcpyAsync(out, staging, n * sizeof(float), cudaMemcpyDeviceToHost, s->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return s->cuda_fail(e, "get_snapshot_noalloc");
+  return FWANT_OK;
+}
+
 fwant_status fwant_check(fwant_solver* s) {
   if (!s) return FWANT_ERR_INVALID_ARG;
   cudaSetDevice(s->cfg.device);

@@ -176,6 +176,26 @@ fwant_status fwant_set_field(fwant_solver* s, int component, const float* in);
 fwant_status fwant_get_snapshot(fwant_solver* s, const int subs[3], const int subc[3], const int subt[3],
                                 int ncomp, const int* comps, float* out);
 
+/* fwant_get_snapshot without any device allocation.  No counterpart in the reference.
+ *
+ * For callers that must not allocate device memory at this point: code running while a
+ * CUDA graph is being captured (an allocation would break the capture), monitoring or
+ * output hooks that run in the middle of a long solve on a GPU whose memory is fully
+ * committed to the wavefield registers (an allocation could fail with out-of-memory
+ * partway through a run), and host programs that route every device allocation through
+ * their own budgeted pool and forbid hidden library allocations.
+ *
+ * Same arguments and output as fwant_get_snapshot.  The values are staged in a fixed
+ * device array of 4,194,304 floats (16 MiB) that the library holds on every GPU it is
+ * loaded on until the process exits; a request for more values (ncomp * subc[0] *
+ * subc[1] * subc[2]) is rejected with FWANT_ERR_INVALID_ARG, so large volumes are read in
+ * pieces (e.g. k-ranges).  The first call on a device resolves that array's device
+ * address; make it before any stream capture.  All calls on one device share the array:
+ * each call overwrites every value it returns, but calls that overlap on the GPU (other
+ * threads or handles on the same device) race with each other. */
+fwant_status fwant_get_snapshot_noalloc(fwant_solver* s, const int subs[3], const int subc[3], const int subt[3],
+                                        int ncomp, const int* comps, float* out);
+
 /* Overflow check of the nine components: macdrp_check (code/srcF/mod_macdrp.F90:228-264).
  * Returns FWANT_ERR_NUMERIC_OVERFLOW when a value is NaN, Inf or >= huge(1.0). */
 fwant_status fwant_check(fwant_solver* s);
