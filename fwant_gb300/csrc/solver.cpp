@@ -243,21 +243,33 @@ struct fwant_solver {
     if (e != cudaSuccess || !fn || q != cudaDriverEntryPointSuccess)
       return fail(FWANT_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
     EncodeFn encode = reinterpret_cast<EncodeFn>(fn);
-    auto make = [&](CUtensorMap* m, float* base, int ncomp, cuuint32_t bx, cuuint32_t by, cuuint32_t bc) {
+    // The halo'd tile's rows (160 B) start 16 B before a 128 B line: without promotion a
+    // miss fetches only the 32 B sectors the row covers.  Override for tuning:
+    // FWANT_TILE_L2_PROMOTION = 0, 64, 128 or 256.
+    CUtensorMapL2promotion tile_promo = CU_TENSOR_MAP_L2_PROMOTION_NONE;
+    if (const char* env = std::getenv("FWANT_TILE_L2_PROMOTION")) {
+      const int v = std::atoi(env);
+      tile_promo = v == 64 ? CU_TENSOR_MAP_L2_PROMOTION_L2_64B
+                 : v == 128 ? CU_TENSOR_MAP_L2_PROMOTION_L2_128B
+                 : v == 256 ? CU_TENSOR_MAP_L2_PROMOTION_L2_256B : CU_TENSOR_MAP_L2_PROMOTION_NONE;
+    }
+    auto make = [&](CUtensorMap* m, float* base, int ncomp, cuuint32_t bx, cuuint32_t by, cuuint32_t bc,
+                    CUtensorMapL2promotion promo) {
       const cuuint64_t dims[4] = {cuuint64_t(g.px), cuuint64_t(g.ny), cuuint64_t(g.nz), cuuint64_t(ncomp)};
       const cuuint64_t strides[3] = {cuuint64_t(g.px) * 4, cuuint64_t(g.plane) * 4, cuuint64_t(g.fstride) * 4};
       const cuuint32_t box[4] = {bx, by, 1, bc};
       const cuuint32_t es[4] = {1, 1, 1, 1};
       return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                    CU_TENSOR_MAP_SWIZZLE_NONE, promo, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     };
+    const CUtensorMapL2promotion line = CU_TENSOR_MAP_L2_PROMOTION_L2_128B;  // line-aligned boxes
     for (int r = 0; r < 4; ++r) {
-      if (make(&tm_tile[r], set(r), fw::NF, fw::TILE_BX, fw::TILE_BY, fw::NF) != CUDA_SUCCESS ||
-          make(&tm_q[r], set(r), fw::NF, fw::STAGE_TX, fw::STAGE_TY, 6) != CUDA_SUCCESS ||
-          make(&tm_pt[r], set(r), fw::NF, fw::STAGE_TX, fw::STAGE_TY, fw::NF) != CUDA_SUCCESS)
+      if (make(&tm_tile[r], set(r), fw::NF, fw::TILE_BX, fw::TILE_BY, fw::NF, tile_promo) != CUDA_SUCCESS ||
+          make(&tm_q[r], set(r), fw::NF, fw::STAGE_TX, fw::STAGE_TY, 6, line) != CUDA_SUCCESS ||
+          make(&tm_pt[r], set(r), fw::NF, fw::STAGE_TX, fw::STAGE_TY, fw::NF, line) != CUDA_SUCCESS)
         return fail(FWANT_ERR_CUDA, "tensor map encoding failed");
     }
-    if (make(&tm_med, med, 3, fw::STAGE_TX, fw::STAGE_TY, 3) != CUDA_SUCCESS)
+    if (make(&tm_med, med, 3, fw::STAGE_TX, fw::STAGE_TY, 3, line) != CUDA_SUCCESS)
       return fail(FWANT_ERR_CUDA, "tensor map encoding failed");
     return FWANT_OK;
   }
