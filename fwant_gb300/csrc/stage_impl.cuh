@@ -249,10 +249,41 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
   const float c = act ? __ldg(A.xcot + i) : 0.0f;
   const float rs = act ? __ldg(A.rsinv + i) : 0.0f;
 
+  // Does this CTA's block of points touch any smoothed source box?  (tested once here
+  // instead of per point and plane)
+  bool cta_src = false;
+  for (int n = 0; n < S.nforce && !cta_src; ++n)
+    cta_src = S.force_c[3 * n] + 3 >= i0 && S.force_c[3 * n] - 3 <= i0 + TX - 1 && S.force_c[3 * n + 1] + 3 >= j0 &&
+              S.force_c[3 * n + 1] - 3 <= j0 + TY - 1 && S.force_c[3 * n + 2] + 3 >= kb && S.force_c[3 * n + 2] - 3 <= ke;
+  for (int n = 0; n < S.nmom && !cta_src; ++n)
+    cta_src = S.mom_c[3 * n] + 3 >= i0 && S.mom_c[3 * n] - 3 <= i0 + TX - 1 && S.mom_c[3 * n + 1] + 3 >= j0 &&
+              S.mom_c[3 * n + 1] - 3 <= j0 + TY - 1 && S.mom_c[3 * n + 2] + 3 >= kb && S.mom_c[3 * n + 2] - 3 <= ke;
+
+  // Prefetch into L1 the PML memory variables of this point on plane kp (their global
+  // loads then hit L1 instead of exposing DRAM latency inside the compute).
+  auto prefetch_pml = [&](int kp) {
+    if (!act) return;
+#pragma unroll 1
+    for (int sidx = 0; sidx < 6; ++sidx) {
+      const Slab& sl = A.slab[sidx];
+      if (!sl.on || i < sl.i1 || i > sl.i2 || j < sl.j1 || j > sl.j2 || kp < sl.k1 || kp > sl.k2) continue;
+      const long long qa =
+          (long long)(i - sl.i1) + (long long)sl.sx * ((long long)(j - sl.j1) + (long long)sl.sy * (kp - sl.k1));
+#pragma unroll
+      for (int v = 0; v < 6; ++v) {
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(A.ain[sidx] + qa + v * sl.vstride));
+        if (RK >= 1) asm volatile("prefetch.global.L1 [%0];" ::"l"(A.at[sidx] + qa + v * sl.vstride));
+        if (RK == 1) asm volatile("prefetch.global.L1 [%0];" ::"l"(A.am[sidx] + qa + v * sl.vstride));
+      }
+    }
+  };
+  prefetch_pml(kb);
+
   int it = 0;
   for (int k = kb; k <= ke; ++k, ++it) {
     const int cur = it & 1;
     if (tid == 0 && k < ke) issue(k + 1, cur ^ 1);
+    if (k < ke) prefetch_pml(k + 1);
     const bool ok = mbar_wait(bar0 + 8 * cur, (it >> 1) & 1);
     unsigned char* buf = smem + cur * BUF_BYTES;
     float(*tile)[TBY][TBX] = reinterpret_cast<float(*)[TBY][TBX]>(buf);
@@ -485,7 +516,7 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
 
       // ---- moment tensors (src_stress, mod_src.F90:207-273)
 #pragma unroll 1
-      for (int n = 0; n < S.nmom; ++n) {
+      for (int n = 0; cta_src && n < S.nmom; ++n) {
         const int li = i - S.mom_c[3 * n], lj = j - S.mom_c[3 * n + 1], lk = k - S.mom_c[3 * n + 2];
         if (li < -3 || li > 3 || lj < -3 || lj > 3 || lk < -3 || lk > 3) continue;
         const int e = n * 343 + (li + 3) + 7 * ((lj + 3) + 7 * (lk + 3));
@@ -501,7 +532,7 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
       }
       // ---- body forces (src_force, mod_src.F90:275-345)
 #pragma unroll 1
-      for (int n = 0; n < S.nforce; ++n) {
+      for (int n = 0; cta_src && n < S.nforce; ++n) {
         const int li = i - S.force_c[3 * n], lj = j - S.force_c[3 * n + 1], lk = k - S.force_c[3 * n + 2];
         if (li < -3 || li > 3 || lj < -3 || lj > 3 || lk < -3 || lk > 3) continue;
         const int e = n * 343 + (li + 3) + 7 * ((lj + 3) + 7 * (lk + 3));
