@@ -259,16 +259,31 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
     cta_src = S.mom_c[3 * n] + 3 >= i0 && S.mom_c[3 * n] - 3 <= i0 + TX - 1 && S.mom_c[3 * n + 1] + 3 >= j0 &&
               S.mom_c[3 * n + 1] - 3 <= j0 + TY - 1 && S.mom_c[3 * n + 2] + 3 >= kb && S.mom_c[3 * n + 2] - 3 <= ke;
 
+  // PML slabs holding this column: the x and y slabs span every plane, so their
+  // membership is fixed per thread (bits 0-3: x1 x2 y1 y2); the z slabs (bits 4, 5) are
+  // tested per plane, uniformly across the CTA.
+  unsigned xymask = 0;
+  if (act)
+#pragma unroll
+    for (int sidx = 0; sidx < 4; ++sidx) {
+      const Slab& sl = A.slab[sidx];
+      if (sl.on && i >= sl.i1 && i <= sl.i2 && j >= sl.j1 && j <= sl.j2) xymask |= 1u << sidx;
+    }
+  auto slab_mask = [&](int kp) -> unsigned {
+    unsigned m = act ? xymask : 0u;
+    if (act && A.slab[4].on && kp >= A.slab[4].k1 && kp <= A.slab[4].k2) m |= 16u;
+    if (act && A.slab[5].on && kp >= A.slab[5].k1 && kp <= A.slab[5].k2) m |= 32u;
+    return m;
+  };
+
   // Prefetch into L1 the PML memory variables of this point on plane kp (their global
   // loads then hit L1 instead of exposing DRAM latency inside the compute).
   auto prefetch_pml = [&](int kp) {
-    if (!act) return;
 #pragma unroll 1
-    for (int sidx = 0; sidx < 6; ++sidx) {
+    for (unsigned mk = slab_mask(kp); mk; mk &= mk - 1) {
+      const int sidx = __ffs(mk) - 1;
       const Slab& sl = A.slab[sidx];
-      if (!sl.on || i < sl.i1 || i > sl.i2 || j < sl.j1 || j > sl.j2 || kp < sl.k1 || kp > sl.k2) continue;
-      const long long qa =
-          (long long)(i - sl.i1) + (long long)sl.sx * ((long long)(j - sl.j1) + (long long)sl.sy * (kp - sl.k1));
+      const int qa = (i - sl.i1) + sl.sx * ((j - sl.j1) + sl.sy * (kp - sl.k1));
 #pragma unroll
       for (int v = 0; v < 6; ++v) {
         asm volatile("prefetch.global.L1 [%0];" ::"l"(A.ain[sidx] + qa + v * sl.vstride));
@@ -308,12 +323,14 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
     }
 
     if (ok && act) {
-      // advance the z queue with plane k+LEAD
+      // advance the z queue with plane k+LEAD (the image applies on and above the surface)
+      const bool img = fsurf && k + LEAD >= g.k2;
 #pragma unroll
       for (int f = 0; f < 6; ++f) {
         q[f][0] = q[f][1]; q[f][1] = q[f][2]; q[f][2] = q[f][3]; q[f][3] = q[f][4];
-        q[f][4] = qval(f, qs[f][ty][tx], k + LEAD);
+        q[f][4] = img ? qval(f, qs[f][ty][tx], k + LEAD) : qs[f][ty][tx];
       }
+      const unsigned pmask = slab_mask(k);
       const int p = col + k * plane;
       const float lam = med[0][ty][tx], miu = med[1][ty][tx], rhov = med[2][ty][tx];
       const float ze = __ldg(A.zeta_z + k);
@@ -386,13 +403,15 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
         hTxz = 2.0f * miu * E13;
         hTyz = 2.0f * miu * E23;
         // PML terms (mod_abs_npml.F90:1179-1301, 1523-1645, 1867-1983)
-        dx_[0] = (DxTxx + 2.0f * Txz) / r; dx_[1] = (DxTxy + Tyz) / r; dx_[2] = (DxTxz - Txx + Tzz) / r;
-        dx_[3] = (DxVx + Vz) / r; dx_[4] = DxVy / r; dx_[5] = (DxVz - Vx) / r;
-        dy_[0] = (DyTxy / xs + (Txx - Tyy) * c + Txz) / r;
-        dy_[1] = (DyTyy / xs + 2.0f * Txy * c + 2.0f * Tyz) / r;
-        dy_[2] = (DyTyz / xs + Txz * c + (Tzz - Tyy)) / r;
-        dy_[3] = (DyVx / xs - Vy * c) / r; dy_[4] = (DyVy / xs + Vx * c + Vz) / r; dy_[5] = (DyVz / xs - Vy) / r;
-        dz_[0] = DzTxz; dz_[1] = DzTyz; dz_[2] = DzTzz; dz_[3] = DzVx; dz_[4] = DzVy; dz_[5] = DzVz;
+        if (pmask) {
+          dx_[0] = (DxTxx + 2.0f * Txz) / r; dx_[1] = (DxTxy + Tyz) / r; dx_[2] = (DxTxz - Txx + Tzz) / r;
+          dx_[3] = (DxVx + Vz) / r; dx_[4] = DxVy / r; dx_[5] = (DxVz - Vx) / r;
+          dy_[0] = (DyTxy / xs + (Txx - Tyy) * c + Txz) / r;
+          dy_[1] = (DyTyy / xs + 2.0f * Txy * c + 2.0f * Tyz) / r;
+          dy_[2] = (DyTyz / xs + Txz * c + (Tzz - Tyy)) / r;
+          dy_[3] = (DyVx / xs - Vy * c) / r; dy_[4] = (DyVy / xs + Vx * c + Vz) / r; dy_[5] = (DyVz / xs - Vy) / r;
+          dz_[0] = DzTxz; dz_[1] = DzTyz; dz_[2] = DzTzz; dz_[3] = DzVx; dz_[4] = DzVy; dz_[5] = DzVz;
+        }
       } else {
         // same equations with the metric folded into one factor per axis
         const float rr = __ldg(A.rzinv + k);
@@ -427,13 +446,15 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
         hTxy = 2.0f * miu * E12;
         hTxz = 2.0f * miu * E13;
         hTyz = 2.0f * miu * E23;
-        dx_[0] = gxTxx + 2.0f * Txz * rr; dx_[1] = gxTxy + Tyz * rr; dx_[2] = gxTxz + (Tzz - Txx) * rr;
-        dx_[3] = gxVx + Vz * rr; dx_[4] = gxVy; dx_[5] = gxVz - Vx * rr;
-        dy_[0] = gyTxy + ((Txx - Tyy) * c + Txz) * rr;
-        dy_[1] = gyTyy + (2.0f * Txy * c + 2.0f * Tyz) * rr;
-        dy_[2] = gyTyz + (Txz * c + (Tzz - Tyy)) * rr;
-        dy_[3] = gyVx - Vy * c * rr; dy_[4] = gyVy + (Vx * c + Vz) * rr; dy_[5] = gyVz - Vy * rr;
-        dz_[0] = gzTxz; dz_[1] = gzTyz; dz_[2] = gzTzz; dz_[3] = gzVx; dz_[4] = gzVy; dz_[5] = gzVz;
+        if (pmask) {
+          dx_[0] = gxTxx + 2.0f * Txz * rr; dx_[1] = gxTxy + Tyz * rr; dx_[2] = gxTxz + (Tzz - Txx) * rr;
+          dx_[3] = gxVx + Vz * rr; dx_[4] = gxVy; dx_[5] = gxVz - Vx * rr;
+          dy_[0] = gyTxy + ((Txx - Tyy) * c + Txz) * rr;
+          dy_[1] = gyTyy + (2.0f * Txy * c + 2.0f * Tyz) * rr;
+          dy_[2] = gyTyz + (Txz * c + (Tzz - Tyy)) * rr;
+          dy_[3] = gyVx - Vy * c * rr; dy_[4] = gyVy + (Vx * c + Vz) * rr; dy_[5] = gyVz - Vy * rr;
+          dz_[0] = gzTxz; dz_[1] = gzTyz; dz_[2] = gzTzz; dz_[3] = gzVx; dz_[4] = gzVy; dz_[5] = gzVz;
+        }
       }
 
       // ---- CFS-PML slabs in the reference's order x1 x2 y1 y2 z1 z2 (additive at corners)
@@ -441,9 +462,9 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
       const float tc11 = tc13 + 2.0f * tc66;
       const float tc12 = tc13, tc22 = tc11, tc23 = tc13, tc33 = tc11, tc44 = tc66, tc55 = tc66;
 #pragma unroll 1
-      for (int sidx = 0; sidx < 6; ++sidx) {
+      for (unsigned mk = pmask; mk; mk &= mk - 1) {
+        const int sidx = __ffs(mk) - 1;
         const Slab& sl = A.slab[sidx];
-        if (!sl.on || i < sl.i1 || i > sl.i2 || j < sl.j1 || j > sl.j2 || k < sl.k1 || k > sl.k2) continue;
         const int axis = sidx >> 1;
         const int ia = axis == 0 ? i : (axis == 1 ? j : k);
         const float b1 = __ldg(A.pb1[axis] + ia), b1_1 = __ldg(A.pb11[axis] + ia);
@@ -451,8 +472,7 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
         float d[6];
 #pragma unroll
         for (int v = 0; v < 6; ++v) d[v] = axis == 0 ? dx_[v] : (axis == 1 ? dy_[v] : dz_[v]);
-        const long long qa =
-            (long long)(i - sl.i1) + (long long)sl.sx * ((long long)(j - sl.j1) + (long long)sl.sy * (k - sl.k1));
+        const int qa = (i - sl.i1) + sl.sx * ((j - sl.j1) + sl.sy * (k - sl.k1));
         const long long vs = sl.vstride;
         const float* __restrict__ ai = A.ain[sidx] + qa;
         float av[6], h[6];
