@@ -149,13 +149,13 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """DRAM bytes per stage launch from the committed ncu summary (per interior point,
-    so that it scales to the benchmark grid), or None."""
+def ncu_traffic_ratio():
+    """Measured DRAM bytes over algorithmic bytes of the stage kernel, from the committed
+    ncu summary (captured on a smaller grid of the same kernel), or None."""
     path = os.path.join(ROOT, "profiles", "stage_kernel_c2.md")
     if not os.path.exists(path):
         return None
-    m = re.search(r"dram_bytes_per_point_per_launch:\s*([0-9.eE+-]+)", open(path).read())
+    m = re.search(r"dram_traffic_over_algorithmic:\s*([0-9.eE+-]+)", open(path).read())
     return float(m.group(1)) if m else None
 
 
@@ -277,9 +277,11 @@ def run_ours(args, rank, world):
     launch_ms = float(np.mean(stage_ms))
     achieved = algo_bytes_step / 4.0 / (launch_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
-    tr = ncu_traffic()
+    tr = ncu_traffic_ratio()
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "peak_source": peak_kind, "traffic": (tr * m0.npoints) if tr else None,
+            "peak_source": peak_kind, "traffic": (tr * algo_bytes_step / 4.0) if tr else None,
+            "traffic_note": "bytes per launch: ncu DRAM/algorithmic ratio (profiles/stage_kernel_c2.md) x "
+                            "algorithmic bytes of this launch",
             "stage_ms": stage_ms, "step_end_ms": end_ms,
             "algorithmic_bytes_per_launch": algo_bytes_step / 4.0}
 
