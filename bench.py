@@ -37,7 +37,15 @@ sys.path.insert(0, ROOT)
 #   stage 1: read W 9 + medium 3, write W' 9 + t 9                = 30 floats
 #   stage 2, 3: read W 9 + medium 3 + m 9 + t 9, write W' 9 + t 9  = 48 floats each
 #   stage 4: read W 9 + medium 3 + t 9, write W 9                  = 30 floats
-BYTES_PT_STEP = 156 * 4
+# Of the 156 values, 12 are the medium (always FP32) and 144 are wavefield registers,
+# which --storage bf16/fp16 holds in 2 bytes.
+FIELD_VALUES_PT_STEP, MEDIUM_VALUES_PT_STEP = 144, 12
+BYTES_PT_STEP = (FIELD_VALUES_PT_STEP + MEDIUM_VALUES_PT_STEP) * 4
+STORAGE_BYTES = {"fp32": 4, "bf16": 2, "fp16": 2}
+
+
+def bytes_pt_step(storage):
+    return FIELD_VALUES_PT_STEP * STORAGE_BYTES[storage] + MEDIUM_VALUES_PT_STEP * 4
 # CFS-PML memory variables, per slab point per step: 6 variables x (18+30+30+18) floats
 BYTES_PML_PT_STEP = 6 * 16 * 4
 
@@ -54,6 +62,8 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--grid", default=None, help="override the C2 interior size, e.g. 200x200x100 (profiling)")
     p.add_argument("--sims", type=int, default=3, help="number of force components simulated (C2)")
+    p.add_argument("--storage", choices=["fp32", "bf16", "fp16"], default="fp32",
+                   help="storage of the wavefield registers (arithmetic stays FP32)")
     return p.parse_args()
 
 
@@ -248,7 +258,16 @@ def run_ours(args, rank, world):
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     fw.load_library()
     models, desc = make_models(args.config, seed=rank, grid=args.grid, sims=args.sims)
-    sims = [inputs.attach(fw.Solver(m.ni, m.nj, m.nk, m.stept, device=dev), m) for m in models]
+    storage = {"fp32": fw.STORAGE_FP32, "bf16": fw.STORAGE_BF16, "fp16": fw.STORAGE_FP16}[args.storage]
+
+    def make_solver(m):
+        s = fw.Solver(m.ni, m.nj, m.nk, m.stept, device=dev, storage=storage)
+        if args.storage == "fp16":
+            # a 1e15 N surface force on 1 km cells peaks near 50 m/s and 1.2e9 Pa at the source
+            s.set_storage_scale(2.0 ** 9, 2.0 ** -15)
+        return s
+
+    sims = [inputs.attach(make_solver(m), m) for m in models]
     npts = sum(m.npoints for m in models)
     # per-launch timing of the stage kernel (CUDA events around each launch, eager)
     stage_ms, end_ms = sims[0].profile_stages(8)
@@ -267,17 +286,23 @@ def run_ours(args, rank, world):
         dev_ms += s.last_run_ms()
     t_host = time.perf_counter() - t_host
     clk = clocks.stop()
+    finite = True
+    for s in sims:
+        try:
+            s.check()
+        except fw.FwantError:
+            finite = False
     dist.barrier()
     dev_ms = dist.max(dev_ms)
     value = world * npts * args.steps / (dev_ms * 1e-3) / 1e9
 
     # roofline of the stage kernel
     m0 = models[0]
-    algo_bytes_step = BYTES_PT_STEP * int(m0.npoints) + BYTES_PML_PT_STEP * slab_points(m0)
+    algo_bytes_step = bytes_pt_step(args.storage) * int(m0.npoints) + BYTES_PML_PT_STEP * slab_points(m0)
     launch_ms = float(np.mean(stage_ms))
     achieved = algo_bytes_step / 4.0 / (launch_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
-    tr = ncu_traffic_ratio()
+    tr = ncu_traffic_ratio() if args.storage == "fp32" else None
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "peak_source": peak_kind, "traffic": (tr * algo_bytes_step / 4.0) if tr else None,
             "traffic_note": "bytes per launch: ncu DRAM/algorithmic ratio (profiles/stage_kernel_c2.md) x "
@@ -290,6 +315,7 @@ def run_ours(args, rank, world):
         "steps": args.steps, "warmup": warm, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": desc, "points_per_step": npts, "l2": "inputs larger than L2 (no flush)",
+                   "storage": args.storage, "fields_finite_after_run": finite,
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
         "host_wall_s": t_host, "roofline": roof, "clocks": clk,
         "gpu_launches": args.steps * len(sims) * 5,
@@ -303,7 +329,7 @@ def run_ours(args, rank, world):
         t0 = time.perf_counter()
         h2d = d2h = 0
         for m in models:
-            s = fw.Solver(m.ni, m.nj, m.nk, m.stept, device=dev)
+            s = make_solver(m)
             inputs.attach(s, m)
             s.run(args.steps)
             sg = s.get_seismo()

@@ -56,6 +56,8 @@ EXPORTS = [
     ("fwant_set_field", C.c_int, [_vp, C.c_int, _fp]),
     ("fwant_get_snapshot", C.c_int, [_vp, _ip, _ip, _ip, C.c_int, _ip, _fp]),
     ("fwant_get_snapshot_noalloc", C.c_int, [_vp, _ip, _ip, _ip, C.c_int, _ip, _fp]),
+    ("fwant_set_storage_scale", C.c_int, [_vp, C.c_float, C.c_float]),
+    ("fwant_max_abs", C.c_int, [_vp, _fp]),
     ("fwant_check", C.c_int, [_vp]),
     ("fwant_profile_stages", C.c_int, [_vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("fwant_last_run_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
@@ -282,6 +284,16 @@ class Solver:
         self._chk(self._lib.fwant_get_snapshot_noalloc(self._h, _ptr(s0, C.c_int), _ptr(c0, C.c_int),
                                                        _ptr(t0, C.c_int), len(cm), _ptr(cm, C.c_int), _ptr(out)))
         return out.reshape(len(cm), int(c0[2]), int(c0[1]), int(c0[0])).transpose(0, 3, 2, 1)
+
+    def set_storage_scale(self, velocity_scale, stress_scale):
+        """Power-of-two scales of 2-byte storage (stored value = physical value * scale)."""
+        self._chk(self._lib.fwant_set_storage_scale(self._h, float(velocity_scale), float(stress_scale)))
+
+    def max_abs(self):
+        """Per-component max |value| (receiver order Vx Vy Vz Txx Tyy Tzz Txy Txz Tyz)."""
+        out = np.zeros(9, np.float32)
+        self._chk(self._lib.fwant_max_abs(self._h, _ptr(out)))
+        return out
 
     def check(self):
         """macdrp_check: raises FwantError(NUMERIC_OVERFLOW) on NaN/Inf/huge."""

@@ -29,7 +29,9 @@ EXACT_FLAGS = ["-fmad=false"]
 CPP_FLAGS = ["-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
 
 SOURCES = ["stage_fast_rk0.cu", "stage_fast_rk1.cu", "stage_fast_rk2.cu", "stage_exact_rk0.cu",
-           "stage_exact_rk1.cu", "stage_exact_rk2.cu", "stage_dispatch.cu", "aux.cu", "snapshot.cu", "solver.cpp"]
+           "stage_exact_rk1.cu", "stage_exact_rk2.cu", "stage_bf16_rk0.cu", "stage_bf16_rk1.cu",
+           "stage_bf16_rk2.cu", "stage_fp16_rk0.cu", "stage_fp16_rk1.cu", "stage_fp16_rk2.cu",
+           "stage_dispatch.cu", "aux.cu", "snapshot.cu", "solver.cpp"]
 
 
 def _nvcc() -> str:

@@ -1,8 +1,12 @@
 // Small kernels around the stage kernel: receiver sampling with the step counter,
 // the FP64 metric, and the overflow check.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <math.h>
+
 #include "kernels.h"
+#include "storage.cuh"
 
 namespace fw {
 
@@ -20,7 +24,7 @@ __global__ void advance_record_kernel(const RecvArgs a) {
         const int fi = f < 3 ? f : (f == 3 ? TXX : (f == 4 ? TYY : (f == 5 ? TZZ : (f == 6 ? TXY : (f == 7 ? TXZ : TYZ)))));
         const int i = a.idx[3 * pt], j = a.idx[3 * pt + 1], k = a.idx[3 * pt + 2];
         const long long p = (long long)(i + PADL) + (long long)a.g.px * ((long long)j + (long long)a.g.ny * k);
-        a.seismo[((long long)f * a.cap + m) * a.npt + pt] = a.w[fi * a.g.fstride + p];
+        a.seismo[((long long)f * a.cap + m) * a.npt + pt] = load_component(a.w, a.storage, a.g.fstride, fi, p, a.isv, a.ist);
       }
     }
   }
@@ -66,12 +70,15 @@ void launch_sincot_fp64(int n, const float* x, float* xsin, float* xcot, void* s
   sincot_kernel<<<(n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(n, x, xsin, xcot);
 }
 
-// macdrp_check (mod_macdrp.F90:228-264): maximum of |value| over the interior of the
-// nine components.  The bit pattern of a non-negative float orders like the value,
-// and NaN (0x7fc00000 after fabs) orders above Inf, so an atomicMax on the bits
-// yields max|v| with NaN and Inf detectable on the host.
-__global__ void maxabs_kernel(const Geom g, const float* __restrict__ w, unsigned int* out) {
-  unsigned int best = 0;
+// macdrp_check (mod_macdrp.F90:228-264): maximum of |value| over the interior of each
+// of the nine components.  The bit pattern of a non-negative float orders like the value,
+// and NaN (0x7fc00000 after fabs) orders above Inf, so an atomicMax on the bits yields
+// max|v| with NaN and Inf detectable on the host.
+__global__ void maxabs_kernel(const Geom g, const void* __restrict__ w, int storage, float isv, float ist,
+                              unsigned int* out) {
+  unsigned int best[NF];
+#pragma unroll
+  for (int f = 0; f < NF; ++f) best[f] = 0;
   const long long tot = (long long)g.ni * g.nj * g.nk;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
     const int i = g.i1 + int(e % g.ni);
@@ -81,20 +88,47 @@ __global__ void maxabs_kernel(const Geom g, const float* __restrict__ w, unsigne
     const long long p = (long long)(i + PADL) + (long long)g.px * ((long long)j + (long long)g.ny * k);
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
-      const unsigned int b = __float_as_uint(fabsf(w[f * g.fstride + p]));
-      best = b > best ? b : best;
+      const unsigned int b = __float_as_uint(fabsf(load_component(w, storage, g.fstride, f, p, isv, ist)));
+      best[f] = b > best[f] ? b : best[f];
     }
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned int v = __shfl_xor_sync(0xffffffffu, best, o);
-    best = v > best ? v : best;
+  for (int f = 0; f < NF; ++f) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned int v = __shfl_xor_sync(0xffffffffu, best[f], o);
+      best[f] = v > best[f] ? v : best[f];
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(out + f, best[f]);
   }
-  if ((threadIdx.x & 31) == 0) atomicMax(out, best);
 }
 
-void launch_maxabs(const Geom& g, const float* w, unsigned int* out_bits, void* stream) {
-  maxabs_kernel<<<152 * 4, 256, 0, (cudaStream_t)stream>>>(g, w, out_bits);
+void launch_maxabs(const Geom& g, const void* w, int storage, float isv, float ist, unsigned int* out_bits,
+                   void* stream) {
+  maxabs_kernel<<<152 * 4, 256, 0, (cudaStream_t)stream>>>(g, w, storage, isv, ist, out_bits);
+}
+
+// One component between its storage type and FP32 over the whole padded array.
+__global__ void convert_kernel(long long n, const void* __restrict__ src, int src_st, float scale, void* __restrict__ dst,
+                               int dst_st) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    float v;
+    if (src_st == ST_F32) v = static_cast<const float*>(src)[e];
+    else if (src_st == ST_BF16) v = __bfloat162float(static_cast<const __nv_bfloat16*>(src)[e]);
+    else v = __half2float(static_cast<const __half*>(src)[e]);
+    v = v * scale;
+    if (dst_st == ST_F32) static_cast<float*>(dst)[e] = v;
+    else if (dst_st == ST_BF16) static_cast<__nv_bfloat16*>(dst)[e] = __float2bfloat16_rn(v);
+    else static_cast<__half*>(dst)[e] = __float2half_rn(v);
+  }
+}
+
+void launch_convert_to_f32(const Geom& g, const void* src, int storage, float inv_scale, float* dst, void* stream) {
+  convert_kernel<<<152 * 8, 256, 0, (cudaStream_t)stream>>>(g.plane * g.nz, src, storage, inv_scale, dst, ST_F32);
+}
+
+void launch_convert_from_f32(const Geom& g, const float* src, int storage, float scale, void* dst, void* stream) {
+  convert_kernel<<<152 * 8, 256, 0, (cudaStream_t)stream>>>(g.plane * g.nz, src, ST_F32, scale, dst, storage);
 }
 
 }  // namespace fw

@@ -68,9 +68,15 @@ struct Sources {
 
 // Stage-kernel tiling: a CTA owns TX x TY columns and marches along k.
 constexpr int STAGE_TX = 32, STAGE_TY = 8;
-// TMA boxes (x, y, 1 plane, components).  The halo'd tile starts 4 columns left of the
-// CTA's first column so that its x origin stays 16-byte aligned.
-constexpr int TILE_BX = STAGE_TX + 8, TILE_BY = STAGE_TY + 6;
+// TMA boxes (x, y, 1 plane, components).  The halo'd tile starts tile_halo_x columns left
+// of the CTA's first column so that its x origin stays 16-byte aligned: 4 columns for
+// 4-byte storage, 8 for 2-byte storage.
+constexpr int tile_halo_x(int elem_bytes) { return elem_bytes >= 4 ? 4 : 8; }
+constexpr int tile_box_x(int elem_bytes) { return STAGE_TX + 2 * tile_halo_x(elem_bytes); }
+constexpr int TILE_BY = STAGE_TY + 6;
+// wavefield storage kinds inside the kernels
+enum { ST_F32 = 0, ST_BF16 = 1, ST_F16 = 2 };
+constexpr int storage_bytes(int st) { return st == ST_F32 ? 4 : 2; }
 
 // Everything one RK-stage launch needs.
 struct StageArgs {
@@ -80,9 +86,11 @@ struct StageArgs {
   CUtensorMap tm_t;     // RK register t: box TX x TY x 1 x 9
   CUtensorMap tm_med;   // lambda, mu, rho: box TX x TY x 1 x 3
   Geom g;
-  const float* win;   // stage input W (9 components)
-  float* wout;        // stage output W
-  float* wt;          // RK accumulator t
+  const void* win;    // stage input W (9 components, storage type)
+  void* wout;         // stage output W
+  void* wt;           // RK accumulator t
+  // BF16/FP16 storage holds value * scale: velocities (sv) and stresses (st); 1/scale too
+  float sv, st, isv, ist;
   // 1-D metric, 0-based Fortran index, with ghosts
   const float* xi_x;
   const float* eta_y;
@@ -114,14 +122,16 @@ struct StageArgs {
 // operator.  rk: 0 = RK_beg, 1 = RK_inn, 2 = RK_fin.  exact = 1 selects the reference's
 // operand order with IEEE division and no FMA (bit-reproducible against FP32 CPU runs
 // of the same expressions); 0 the fast form (FMA, reciprocals).
-int launch_stage_f32(const StageArgs& a, int variant, int rk, int exact, void* stream);
+// storage: ST_F32 / ST_BF16 / ST_F16 (the exact form exists for ST_F32 only).
+int launch_stage(const StageArgs& a, int variant, int rk, int exact, int storage, void* stream);
 int stage_planes_per_cta(const Geom& g, int sm_count);
-size_t stage_smem_bytes();
 int stage_configure();  // set the dynamic shared-memory attribute of every instantiation
 
 struct RecvArgs {
   Geom g;
-  const float* w;     // register set holding the step's result
+  const void* w;      // register set holding the step's result (storage type)
+  int storage;        // ST_*; stored values are multiplied by isv / ist on reading
+  float isv, ist;
   int npt;
   const int* idx;     // [npt][3] 0-based
   int tinv;
@@ -135,7 +145,9 @@ void launch_advance_record(const RecvArgs& a, void* stream);
 // index minus one); comp holds storage indices; out is [ncomp][cnt2][cnt1][cnt0].
 struct SnapArgs {
   Geom g;
-  const float* w;
+  const void* w;
+  int storage;
+  float isv, ist;
   int start[3], cnt[3], stride[3];
   int ncomp;
   int comp[NF];
@@ -148,7 +160,12 @@ int snapshot_noalloc_staging(int device, float** ptr);
 
 void launch_metric_fp64(int n, const float* coord, float* metric_out, int lo, int hi, void* stream);
 void launch_sincot_fp64(int n, const float* x, float* xsin, float* xcot, void* stream);
-void launch_maxabs(const Geom& g, const float* w, unsigned int* out_bits, void* stream);
+// max |value| of each of the nine components (storage order) into out_bits[9]
+void launch_maxabs(const Geom& g, const void* w, int storage, float isv, float ist, unsigned int* out_bits,
+                   void* stream);
+// one component between storage type and FP32 (padded layout, scale applied)
+void launch_convert_to_f32(const Geom& g, const void* src, int storage, float inv_scale, float* dst, void* stream);
+void launch_convert_from_f32(const Geom& g, const float* src, int storage, float scale, void* dst, void* stream);
 
 // device error codes written to StageArgs::err
 enum { DEVERR_NONE = 0, DEVERR_TMA_TIMEOUT = 1 };

@@ -6,6 +6,7 @@
 #include <mutex>
 
 #include "kernels.h"
+#include "storage.cuh"
 
 namespace fw {
 
@@ -21,7 +22,7 @@ __global__ void pack_snapshot_kernel(const SnapArgs a) {
     const int kk = int(r / a.cnt[1]);
     const int i = a.start[0] + ii * a.stride[0], j = a.start[1] + jj * a.stride[1], k = a.start[2] + kk * a.stride[2];
     const long long p = (long long)(i + PADL) + (long long)a.g.px * ((long long)j + (long long)a.g.ny * k);
-    a.out[e] = a.w[a.comp[c] * a.g.fstride + p];
+    a.out[e] = load_component(a.w, a.storage, a.g.fstride, a.comp[c], p, a.isv, a.ist);
   }
 }
 

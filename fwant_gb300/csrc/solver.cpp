@@ -52,7 +52,11 @@ struct fwant_solver {
   std::string err;
 
   // four register sets of nine components each (W ping-pong, m, t; see run_step)
-  float* regs = nullptr;
+  char* regs = nullptr;       // storage type given by `stor` (esz bytes per element)
+  int stor = fw::ST_F32, esz = 4;
+  // BF16/FP16 registers hold value * scale (velocities sv, stresses st)
+  float sv = 1.0f, sc_t = 1.0f;
+  float* d_conv = nullptr;    // FP32 staging for field import/export of 2-byte storage
   int rA = 0, rB = 1, rC = 2, rT = 3;
   float* med = nullptr;  // lambda, mu, rho, fstride apart (one TMA tensor)
   float *lam = nullptr, *mu = nullptr, *rho = nullptr;
@@ -109,7 +113,7 @@ struct fwant_solver {
     cudaFree(d_x); cudaFree(d_y); cudaFree(d_z); cudaFree(d_xsin); cudaFree(d_xcot);
     cudaFree(d_xi); cudaFree(d_eta); cudaFree(d_zeta); cudaFree(d_prof); cudaFree(d_rzinv); cudaFree(d_rsinv);
     for (int f = 0; f < 6; ++f) cudaFree(aux[f]);
-    cudaFree(d_rec); cudaFree(d_seis); cudaFree(d_ntime); cudaFree(d_maxbits); cudaFree(d_snap);
+    cudaFree(d_rec); cudaFree(d_seis); cudaFree(d_ntime); cudaFree(d_maxbits); cudaFree(d_snap); cudaFree(d_conv);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (st) cudaStreamDestroy(st);
@@ -147,15 +151,21 @@ struct fwant_solver {
   long long off(int i, int j, int k) const {
     return (long long)(i + fw::PADL) + (long long)g.px * ((long long)j + (long long)g.ny * k);
   }
-  float* set(int r) const { return regs + (long long)r * fw::NF * g.fstride; }
+  void* set(int r) const { return regs + (long long)r * fw::NF * g.fstride * esz; }
+  void* comp(int r, int f) const { return static_cast<char*>(set(r)) + (long long)f * g.fstride * esz; }
   float* aset(int f, int r) const { return aux[f] + (long long)r * aux_set[f]; }
 
   fwant_status init() {
     const int ni = cfg.ni, nj = cfg.nj, nk = cfg.nk;
     if (ni < 8 || nj < 8 || nk < 8) return fail(FWANT_ERR_INVALID_ARG, "ni, nj, nk must be >= 8");
     if (!(cfg.stept > 0.0)) return fail(FWANT_ERR_INVALID_ARG, "stept must be > 0");
-    if (cfg.storage != FWANT_STORAGE_FP32)
-      return fail(FWANT_ERR_INVALID_ARG, "only FWANT_STORAGE_FP32 is available in this build");
+    if (cfg.storage == FWANT_STORAGE_FP32) stor = fw::ST_F32;
+    else if (cfg.storage == FWANT_STORAGE_BF16) stor = fw::ST_BF16;
+    else if (cfg.storage == FWANT_STORAGE_FP16) stor = fw::ST_F16;
+    else return fail(FWANT_ERR_INVALID_ARG, "storage must be FP32, BF16 or FP16 (FP64 runs on the CPU solver)");
+    if (stor != fw::ST_F32 && cfg.exact_arith)
+      return fail(FWANT_ERR_INVALID_ARG, "exact_arith needs FP32 storage");
+    esz = fw::storage_bytes(stor);
     cudaError_t e = cudaSetDevice(cfg.device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
     stept = float(cfg.stept);
@@ -177,7 +187,7 @@ struct fwant_solver {
     cudaEventCreate(&ev0);
     cudaEventCreate(&ev1);
     const size_t nreg = size_t(4) * fw::NF * g.fstride;
-    regs = dalloc<float>(nreg);
+    regs = dalloc<char>(nreg * esz);
     med = dalloc<float>(3 * size_t(g.fstride));
     lam = med; mu = med + g.fstride; rho = med + 2 * g.fstride;
     d_err = dalloc<int>(1);
@@ -186,11 +196,11 @@ struct fwant_solver {
     d_eta = dalloc<float>(g.ny); d_zeta = dalloc<float>(g.nz);
     d_prof = dalloc<float>(4 * size_t(g.nx + g.ny + g.nz));
     d_rzinv = dalloc<float>(g.nz); d_rsinv = dalloc<float>(g.nx);
-    d_ntime = dalloc<int>(1); d_maxbits = dalloc<unsigned int>(1);
+    d_ntime = dalloc<int>(1); d_maxbits = dalloc<unsigned int>(fw::NF);
     if (!regs || !med || !d_err || !d_x || !d_y || !d_z || !d_xsin || !d_xcot || !d_xi || !d_eta ||
         !d_zeta || !d_prof || !d_rzinv || !d_rsinv || !d_ntime || !d_maxbits)
       return fail(FWANT_ERR_OOM, "device allocation failed");
-    cudaMemset(regs, 0, nreg * sizeof(float));
+    cudaMemset(regs, 0, nreg * esz);
     cudaMemset(med, 0, 3 * g.fstride * sizeof(float));
     cudaMemset(d_ntime, 0, sizeof(int));
     cudaMemset(d_err, 0, sizeof(int));
@@ -253,23 +263,28 @@ struct fwant_solver {
                  : v == 128 ? CU_TENSOR_MAP_L2_PROMOTION_L2_128B
                  : v == 256 ? CU_TENSOR_MAP_L2_PROMOTION_L2_256B : CU_TENSOR_MAP_L2_PROMOTION_NONE;
     }
-    auto make = [&](CUtensorMap* m, float* base, int ncomp, cuuint32_t bx, cuuint32_t by, cuuint32_t bc,
+    const CUtensorMapDataType wtype = stor == fw::ST_F32    ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                      : stor == fw::ST_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                                                            : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+    auto make = [&](CUtensorMap* m, void* base, CUtensorMapDataType dt, int es, int ncomp, cuuint32_t bx,
+                    cuuint32_t by, cuuint32_t bc,
                     CUtensorMapL2promotion promo) {
       const cuuint64_t dims[4] = {cuuint64_t(g.px), cuuint64_t(g.ny), cuuint64_t(g.nz), cuuint64_t(ncomp)};
-      const cuuint64_t strides[3] = {cuuint64_t(g.px) * 4, cuuint64_t(g.plane) * 4, cuuint64_t(g.fstride) * 4};
+      const cuuint64_t strides[3] = {cuuint64_t(g.px) * es, cuuint64_t(g.plane) * es, cuuint64_t(g.fstride) * es};
       const cuuint32_t box[4] = {bx, by, 1, bc};
-      const cuuint32_t es[4] = {1, 1, 1, 1};
-      return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+      const cuuint32_t el[4] = {1, 1, 1, 1};
+      return encode(m, dt, 4, base, dims, strides, box, el, CU_TENSOR_MAP_INTERLEAVE_NONE,
                     CU_TENSOR_MAP_SWIZZLE_NONE, promo, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     };
     const CUtensorMapL2promotion line = CU_TENSOR_MAP_L2_PROMOTION_L2_128B;  // line-aligned boxes
     for (int r = 0; r < 4; ++r) {
-      if (make(&tm_tile[r], set(r), fw::NF, fw::TILE_BX, fw::TILE_BY, fw::NF, tile_promo) != CUDA_SUCCESS ||
-          make(&tm_q[r], set(r), fw::NF, fw::STAGE_TX, fw::STAGE_TY, 6, line) != CUDA_SUCCESS ||
-          make(&tm_pt[r], set(r), fw::NF, fw::STAGE_TX, fw::STAGE_TY, fw::NF, line) != CUDA_SUCCESS)
+      if (make(&tm_tile[r], set(r), wtype, esz, fw::NF, fw::tile_box_x(esz), fw::TILE_BY, fw::NF, tile_promo) !=
+              CUDA_SUCCESS ||
+          make(&tm_q[r], set(r), wtype, esz, fw::NF, fw::STAGE_TX, fw::STAGE_TY, 6, line) != CUDA_SUCCESS ||
+          make(&tm_pt[r], set(r), wtype, esz, fw::NF, fw::STAGE_TX, fw::STAGE_TY, fw::NF, line) != CUDA_SUCCESS)
         return fail(FWANT_ERR_CUDA, "tensor map encoding failed");
     }
-    if (make(&tm_med, med, 3, fw::STAGE_TX, fw::STAGE_TY, 3, line) != CUDA_SUCCESS)
+    if (make(&tm_med, med, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, 3, fw::STAGE_TX, fw::STAGE_TY, 3, line) != CUDA_SUCCESS)
       return fail(FWANT_ERR_CUDA, "tensor map encoding failed");
     return FWANT_OK;
   }
@@ -558,6 +573,7 @@ struct fwant_solver {
     a.g = g;
     a.tm_med = tm_med;
     a.err = d_err;
+    a.sv = sv; a.st = sc_t; a.isv = 1.0f / sv; a.ist = 1.0f / sc_t;
     a.xi_x = d_xi; a.eta_y = d_eta; a.zeta_z = d_zeta; a.xsin = d_xsin; a.xcot = d_xcot; a.zc = d_z;
     a.rzinv = d_rzinv; a.rsinv = d_rsinv;
     for (int ax = 0; ax < 3; ++ax) {
@@ -593,12 +609,13 @@ struct fwant_solver {
       const int v = (s % 2 == 0) ? X : (~X & 7);
       const int rk = s == 0 ? 0 : (s == 3 ? 2 : 1);
       if (ev) cudaEventRecord(ev[s], st);
-      const int le = fw::launch_stage_f32(a, v, rk, cfg.exact_arith, st);
+      const int le = fw::launch_stage(a, v, rk, cfg.exact_arith, stor, st);
       if (le && !lerr) lerr = le;
     }
     if (ev) cudaEventRecord(ev[4], st);
     fw::RecvArgs r{};
     r.g = g; r.w = set(rT); r.npt = npt; r.idx = d_rec; r.tinv = tinv; r.seismo = d_seis; r.cap = cap;
+    r.storage = stor; r.isv = 1.0f / sv; r.ist = 1.0f / sc_t;
     r.ntime = d_ntime;
     fw::launch_advance_record(r, st);
     if (ev) cudaEventRecord(ev[5], st);
@@ -617,6 +634,7 @@ struct fwant_solver {
     a = fw::SnapArgs{};
     a.g = g;
     a.w = set(rA);
+    a.storage = stor; a.isv = 1.0f / sv; a.ist = 1.0f / sc_t;
     const int lo[3] = {g.i1, g.j1, g.k1}, hi[3] = {g.i2, g.j2, g.k2};
     for (int d = 0; d < 3; ++d) {
       if (subc[d] < 1 || subt[d] < 1) return fail(FWANT_ERR_INVALID_ARG, "snapshot: counts and strides must be >= 1");
@@ -934,10 +952,28 @@ fwant_status fwant_get_seismo(fwant_solver* s, float* out, int max_samples, int*
   return FWANT_OK;
 }
 
+// FP32 staging array for converting one component of 2-byte storage
+static fwant_status conv_buffer(fwant_solver* s) {
+  if (s->d_conv) return FWANT_OK;
+  s->d_conv = dalloc<float>(s->g.fstride);
+  if (!s->d_conv) return s->fail(FWANT_ERR_OOM, "conversion buffer");
+  cudaMemset(s->d_conv, 0, s->g.fstride * sizeof(float));
+  return FWANT_OK;
+}
+
 fwant_status fwant_get_field(fwant_solver* s, int component, float* out) {
   if (!s || !out || component < 0 || component >= fw::NF) return FWANT_ERR_INVALID_ARG;
   cudaSetDevice(s->cfg.device);
-  cudaError_t e = s->get3(out, s->set(s->rA) + fw::ABI2INT[component] * s->g.fstride);
+  const int f = fw::ABI2INT[component];
+  const float* src = static_cast<const float*>(s->comp(s->rA, f));
+  if (s->stor != fw::ST_F32) {
+    fwant_status rc = conv_buffer(s);
+    if (rc != FWANT_OK) return rc;
+    fw::launch_convert_to_f32(s->g, s->comp(s->rA, f), s->stor, 1.0f / (f < 3 ? s->sv : s->sc_t), s->d_conv, s->st);
+    cudaStreamSynchronize(s->st);
+    src = s->d_conv;
+  }
+  cudaError_t e = s->get3(out, src);
   if (e != cudaSuccess) return s->cuda_fail(e, "get_field");
   return FWANT_OK;
 }
@@ -952,8 +988,45 @@ fwant_status fwant_set_field(fwant_solver* s, int component, const float* in) {
       for (int i = 0; i < g.nx; ++i)
         if (i < g.i1 || i > g.i2 || j < g.j1 || j > g.j2 || k < g.k1 || k > g.k2)
           tmp[size_t(i) + size_t(g.nx) * (size_t(j) + size_t(g.ny) * k)] = 0.0f;
-  cudaError_t e = s->put3(s->set(s->rA) + fw::ABI2INT[component] * g.fstride, tmp.data());
+  const int f = fw::ABI2INT[component];
+  cudaError_t e;
+  if (s->stor == fw::ST_F32) {
+    e = s->put3(static_cast<float*>(s->comp(s->rA, f)), tmp.data());
+  } else {
+    fwant_status rc = conv_buffer(s);
+    if (rc != FWANT_OK) return rc;
+    e = s->put3(s->d_conv, tmp.data());
+    fw::launch_convert_from_f32(s->g, s->d_conv, s->stor, f < 3 ? s->sv : s->sc_t, s->comp(s->rA, f), s->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+  }
   if (e != cudaSuccess) return s->cuda_fail(e, "set_field");
+  return FWANT_OK;
+}
+
+fwant_status fwant_set_storage_scale(fwant_solver* s, float velocity_scale, float stress_scale) {
+  if (!s || !(velocity_scale > 0.0f) || !(stress_scale > 0.0f) || !std::isfinite(velocity_scale) ||
+      !std::isfinite(stress_scale))
+    return FWANT_ERR_INVALID_ARG;
+  int ev = 0, et = 0;
+  if (std::frexp(velocity_scale, &ev) != 0.5f || std::frexp(stress_scale, &et) != 0.5f)
+    return s->fail(FWANT_ERR_INVALID_ARG, "storage scales must be powers of two");
+  if (s->ntime != 0) return s->fail(FWANT_ERR_STATE, "storage scales must be set before the first step");
+  s->sv = velocity_scale;
+  s->sc_t = stress_scale;
+  s->drop_graphs();
+  return FWANT_OK;
+}
+
+fwant_status fwant_max_abs(fwant_solver* s, float out[9]) {
+  if (!s || !out) return FWANT_ERR_INVALID_ARG;
+  cudaSetDevice(s->cfg.device);
+  cudaMemsetAsync(s->d_maxbits, 0, fw::NF * sizeof(unsigned int), s->st);
+  fw::launch_maxabs(s->g, s->set(s->rA), s->stor, 1.0f / s->sv, 1.0f / s->sc_t, s->d_maxbits, s->st);
+  unsigned int bits[fw::NF];
+  cudaMemcpyAsync(bits, s->d_maxbits, sizeof(bits), cudaMemcpyDeviceToHost, s->st);
+  cudaError_t e = cudaStreamSynchronize(s->st);
+  if (e != cudaSuccess) return s->cuda_fail(e, "max_abs");
+  for (int c = 0; c < fw::NF; ++c) std::memcpy(&out[c], &bits[fw::ABI2INT[c]], sizeof(float));
   return FWANT_OK;
 }
 
@@ -1009,19 +1082,16 @@ fwant_status fwant_get_snapshot_noalloc(fwant_solver* s, const int subs[3], cons
 
 fwant_status fwant_check(fwant_solver* s) {
   if (!s) return FWANT_ERR_INVALID_ARG;
-  cudaSetDevice(s->cfg.device);
-  cudaMemsetAsync(s->d_maxbits, 0, sizeof(unsigned int), s->st);
-  fw::launch_maxabs(s->g, s->set(s->rA), s->d_maxbits, s->st);
-  unsigned int bits = 0;
-  cudaMemcpyAsync(&bits, s->d_maxbits, sizeof(bits), cudaMemcpyDeviceToHost, s->st);
-  cudaError_t e = cudaStreamSynchronize(s->st);
-  if (e != cudaSuccess) return s->cuda_fail(e, "check");
-  float v;
-  std::memcpy(&v, &bits, sizeof(v));
-  if (!(v < 3.4028234663852886e38f)) {  // huge(1.0), NaN and Inf all fail this test
-    char b[128];
-    std::snprintf(b, sizeof(b), "overflow: max |field| = %g at ntime %d", double(v), s->ntime);
-    return s->fail(FWANT_ERR_NUMERIC_OVERFLOW, b);
+  float m[fw::NF];
+  fwant_status rc = fwant_max_abs(s, m);
+  if (rc != FWANT_OK) return rc;
+  static const char* const names[fw::NF] = {"Vx", "Vy", "Vz", "Txx", "Tyy", "Tzz", "Txy", "Txz", "Tyz"};
+  for (int c = 0; c < fw::NF; ++c) {
+    if (!(m[c] < 3.4028234663852886e38f)) {  // huge(1.0), NaN and Inf all fail this test
+      char b[128];
+      std::snprintf(b, sizeof(b), "overflow: max |%s| = %g at ntime %d", names[c], double(m[c]), s->ntime);
+      return s->fail(FWANT_ERR_NUMERIC_OVERFLOW, b);
+    }
   }
   return FWANT_OK;
 }

@@ -2,46 +2,43 @@
 #include <cuda_runtime.h>
 
 #include "kernels.h"
-#include "stage_impl.cuh"
 
 namespace fw {
 
-int launch_stage_fast_rk0(const StageArgs&, int, cudaStream_t);
-int launch_stage_fast_rk1(const StageArgs&, int, cudaStream_t);
-int launch_stage_fast_rk2(const StageArgs&, int, cudaStream_t);
-int launch_stage_exact_rk0(const StageArgs&, int, cudaStream_t);
-int launch_stage_exact_rk1(const StageArgs&, int, cudaStream_t);
-int launch_stage_exact_rk2(const StageArgs&, int, cudaStream_t);
+#define FW_DECL(mode)                                                 \
+  int launch_stage_##mode##_rk0(const StageArgs&, int, cudaStream_t); \
+  int launch_stage_##mode##_rk1(const StageArgs&, int, cudaStream_t); \
+  int launch_stage_##mode##_rk2(const StageArgs&, int, cudaStream_t); \
+  int configure_stage_##mode##_rk0();                                 \
+  int configure_stage_##mode##_rk1();                                 \
+  int configure_stage_##mode##_rk2();
+FW_DECL(fast)
+FW_DECL(exact)
+FW_DECL(bf16)
+FW_DECL(fp16)
+#undef FW_DECL
 
-int launch_stage_f32(const StageArgs& a, int variant, int rk, int exact, void* stream) {
+int launch_stage(const StageArgs& a, int variant, int rk, int exact, int storage, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
-  if (exact) {
-    if (rk == 0) return launch_stage_exact_rk0(a, variant, st);
-    if (rk == 1) return launch_stage_exact_rk1(a, variant, st);
-    return launch_stage_exact_rk2(a, variant, st);
-  }
-  if (rk == 0) return launch_stage_fast_rk0(a, variant, st);
-  if (rk == 1) return launch_stage_fast_rk1(a, variant, st);
-  return launch_stage_fast_rk2(a, variant, st);
+#define FW_RK(mode)                                                    \
+  return rk == 0 ? launch_stage_##mode##_rk0(a, variant, st)           \
+                 : (rk == 1 ? launch_stage_##mode##_rk1(a, variant, st) \
+                            : launch_stage_##mode##_rk2(a, variant, st));
+  if (storage == ST_BF16) { FW_RK(bf16) }
+  if (storage == ST_F16) { FW_RK(fp16) }
+  if (exact) { FW_RK(exact) }
+  FW_RK(fast)
+#undef FW_RK
 }
 
-size_t stage_smem_bytes() { return SMEM_BYTES; }
-
-int configure_stage_fast_rk0();
-int configure_stage_fast_rk1();
-int configure_stage_fast_rk2();
-int configure_stage_exact_rk0();
-int configure_stage_exact_rk1();
-int configure_stage_exact_rk2();
-
 int stage_configure() {
-  int e = configure_stage_fast_rk0();
-  if (!e) e = configure_stage_fast_rk1();
-  if (!e) e = configure_stage_fast_rk2();
-  if (!e) e = configure_stage_exact_rk0();
-  if (!e) e = configure_stage_exact_rk1();
-  if (!e) e = configure_stage_exact_rk2();
-  return e;
+  int (*const fns[])() = {configure_stage_fast_rk0, configure_stage_fast_rk1, configure_stage_fast_rk2,
+                          configure_stage_exact_rk0, configure_stage_exact_rk1, configure_stage_exact_rk2,
+                          configure_stage_bf16_rk0, configure_stage_bf16_rk1, configure_stage_bf16_rk2,
+                          configure_stage_fp16_rk0, configure_stage_fp16_rk1, configure_stage_fp16_rk2};
+  for (auto fn : fns)
+    if (int e = fn()) return e;
+  return 0;
 }
 
 // Planes per CTA.  Short chunks keep the CTAs that share halo rows marching through the

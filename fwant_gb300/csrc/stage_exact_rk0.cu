@@ -1,10 +1,10 @@
-// Instantiation unit of the stage kernel (stage_impl.cuh): reference-order (exact) arithmetic, compiled with -fmad=false; RK kind 0
-// (0 RK_beg, 1 RK_inn, 2 RK_fin).
+// Instantiation unit of the stage kernel (stage_impl.cuh): reference-order (exact) arithmetic, FP32 storage, compiled with -fmad=false;
+// RK kind 0 (0 RK_beg, 1 RK_inn, 2 RK_fin).
 #include "stage_impl.cuh"
 
 namespace fw {
 int launch_stage_exact_rk0(const StageArgs& a, int variant, cudaStream_t st) {
-  return launch_rk_variant<true, 0>(a, variant, st);
+  return launch_rk_variant<float, true, 0>(a, variant, st);
 }
-int configure_stage_exact_rk0() { return configure_rk<true, 0>(); }
+int configure_stage_exact_rk0() { return configure_rk<float, true, 0>(); }
 }  // namespace fw

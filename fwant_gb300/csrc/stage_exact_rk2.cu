@@ -1,10 +1,10 @@
-// Instantiation unit of the stage kernel (stage_impl.cuh): reference-order (exact) arithmetic, compiled with -fmad=false; RK kind 2
-// (0 RK_beg, 1 RK_inn, 2 RK_fin).
+// Instantiation unit of the stage kernel (stage_impl.cuh): reference-order (exact) arithmetic, FP32 storage, compiled with -fmad=false;
+// RK kind 2 (0 RK_beg, 1 RK_inn, 2 RK_fin).
 #include "stage_impl.cuh"
 
 namespace fw {
 int launch_stage_exact_rk2(const StageArgs& a, int variant, cudaStream_t st) {
-  return launch_rk_variant<true, 2>(a, variant, st);
+  return launch_rk_variant<float, true, 2>(a, variant, st);
 }
-int configure_stage_exact_rk2() { return configure_rk<true, 2>(); }
+int configure_stage_exact_rk2() { return configure_rk<float, true, 2>(); }
 }  // namespace fw

@@ -1,0 +1,10 @@
+// Instantiation unit of the stage kernel (stage_impl.cuh): fast arithmetic, FP16 storage (FP32 arithmetic);
+// RK kind 0 (0 RK_beg, 1 RK_inn, 2 RK_fin).
+#include "stage_impl.cuh"
+
+namespace fw {
+int launch_stage_fp16_rk0(const StageArgs& a, int variant, cudaStream_t st) {
+  return launch_rk_variant<__half, false, 0>(a, variant, st);
+}
+int configure_stage_fp16_rk0() { return configure_rk<__half, false, 0>(); }
+}  // namespace fw

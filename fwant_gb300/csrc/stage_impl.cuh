@@ -24,27 +24,53 @@
 // for the copy still in flight and returns.
 #pragma once
 #include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
+
+#include <type_traits>
 
 #include "kernels.h"
 
 namespace fw {
 
 constexpr int TX = STAGE_TX, TY = STAGE_TY;
-constexpr int TBX = TILE_BX, TBY = TILE_BY;
-constexpr int HX = 4, HY = 3;  // position of the CTA's first column/row inside the tile box
-// shared-memory layout of one pipeline buffer (byte offsets, 128-byte aligned)
-constexpr int SZ_TILE = NF * TBY * TBX * 4;
-constexpr int OFF_Q = ((SZ_TILE + 127) / 128) * 128;
-constexpr int SZ_Q = 6 * TY * TX * 4;
-constexpr int OFF_MED = OFF_Q + SZ_Q;
-constexpr int SZ_MED = 3 * TY * TX * 4;
-constexpr int OFF_M = OFF_MED + SZ_MED;
-constexpr int SZ_PT = NF * TY * TX * 4;
-constexpr int OFF_T = OFF_M + SZ_PT;
-constexpr int BUF_BYTES = ((OFF_T + SZ_PT + 1023) / 1024) * 1024;
-constexpr int SMEM_BYTES = 2 * BUF_BYTES + 64;
+constexpr int TBY = TILE_BY;
+constexpr int HY = 3;  // row of the CTA's first row inside the tile box
 constexpr int WAIT_SPINS = 1 << 22;
+
+// Shared-memory layout of one pipeline buffer for storage type S (byte offsets,
+// 128-byte aligned).  The tile box starts HX columns left of the CTA's first column so
+// that its x origin stays 16-byte aligned (4 columns of 4 bytes, 8 columns of 2 bytes).
+template <class S>
+struct Lay {
+  static constexpr int ES = sizeof(S);
+  static constexpr int HX = tile_halo_x(ES);
+  static constexpr int TBX = tile_box_x(ES);
+  static constexpr int SZ_TILE = NF * TBY * TBX * ES;
+  static constexpr int OFF_Q = ((SZ_TILE + 127) / 128) * 128;
+  static constexpr int SZ_Q = 6 * TY * TX * ES;
+  static constexpr int OFF_MED = OFF_Q + SZ_Q;
+  static constexpr int SZ_MED = 3 * TY * TX * 4;  // the medium stays FP32
+  static constexpr int OFF_M = OFF_MED + SZ_MED;
+  static constexpr int SZ_PT = NF * TY * TX * ES;
+  static constexpr int OFF_T = OFF_M + SZ_PT;
+  static constexpr int BUF_BYTES = ((OFF_T + SZ_PT + 1023) / 1024) * 1024;
+  static constexpr int SMEM_BYTES = 2 * BUF_BYTES + 64;
+};
+
+// Storage conversions.  BF16/FP16 registers hold value * scale (a power of two per
+// component group, so scaling is exact); arithmetic is FP32.
+template <class S> __device__ __forceinline__ float to_f(S v);
+template <> __device__ __forceinline__ float to_f<float>(float v) { return v; }
+template <> __device__ __forceinline__ float to_f<__nv_bfloat16>(__nv_bfloat16 v) { return __bfloat162float(v); }
+template <> __device__ __forceinline__ float to_f<__half>(__half v) { return __half2float(v); }
+template <class S> __device__ __forceinline__ S from_f(float v);
+template <> __device__ __forceinline__ float from_f<float>(float v) { return v; }
+template <> __device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
+template <> __device__ __forceinline__ __half from_f<__half>(float v) { return __float2half_rn(v); }
+template <class S>
+constexpr bool is_f32_v = std::is_same<S, float>::value;
 
 #define MCA_1 (-0.30874f)
 #define MCA0 (-0.6326f)
@@ -127,6 +153,24 @@ __device__ __forceinline__ float ld_rw_stream(const float* p, uint64_t policy) {
   return v;
 }
 
+// streaming store of one register element in its storage type
+template <class S>
+__device__ __forceinline__ void st_stream_s(S* p, S v, uint64_t policy);
+template <>
+__device__ __forceinline__ void st_stream_s<float>(float* p, float v, uint64_t policy) {
+  st_stream(p, v, policy);
+}
+template <>
+__device__ __forceinline__ void st_stream_s<__nv_bfloat16>(__nv_bfloat16* p, __nv_bfloat16 v, uint64_t policy) {
+  asm volatile("st.global.L2::cache_hint.b16 [%0], %1, %2;" ::"l"(p), "h"(__bfloat16_as_ushort(v)), "l"(policy)
+               : "memory");
+}
+template <>
+__device__ __forceinline__ void st_stream_s<__half>(__half* p, __half v, uint64_t policy) {
+  asm volatile("st.global.L2::cache_hint.b16 [%0], %1, %2;" ::"l"(p), "h"(__half_as_ushort(v)), "l"(policy)
+               : "memory");
+}
+
 // ---- one-sided operators ------------------------------------------------------------
 // DRP/opt MacCormack operators (mod_macdrp.h:69-103) on values at offsets -3..+3 of c.
 template <int F>
@@ -135,6 +179,19 @@ __device__ __forceinline__ float dop(const float* c, int s) {
     return MCA_1 * c[-s] + MCA0 * c[0] + MCA1 * c[s] + MCA2 * c[2 * s] + MCA3 * c[3 * s];
   else
     return -MCA3 * c[-3 * s] - MCA2 * c[-2 * s] - MCA1 * c[-s] - MCA0 * c[0] - MCA_1 * c[s];
+}
+// Same operator on stored values (converted to FP32 element by element).
+template <int F, class S>
+__device__ __forceinline__ float dopS(const S* c, int s) {
+  if constexpr (is_f32_v<S>) {
+    return dop<F>(c, s);
+  } else if (F) {
+    return MCA_1 * to_f(c[-s]) + MCA0 * to_f(c[0]) + MCA1 * to_f(c[s]) + MCA2 * to_f(c[2 * s]) +
+           MCA3 * to_f(c[3 * s]);
+  } else {
+    return -MCA3 * to_f(c[-3 * s]) - MCA2 * to_f(c[-2 * s]) - MCA1 * to_f(c[-s]) - MCA0 * to_f(c[0]) -
+           MCA_1 * to_f(c[s]);
+  }
 }
 // Same operator on a five-entry z queue (F: planes -1..+3, B: planes -3..+1).
 template <int F>
@@ -167,8 +224,13 @@ __device__ __forceinline__ float surf_val(const Sources& S, const float* tab, in
   return v;
 }
 
-template <bool EXACT, int FX, int FY, int FZ, int RK>
+template <class S, bool EXACT, int FX, int FY, int FZ, int RK>
 __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant__ StageArgs A) {
+  static_assert(!EXACT || is_f32_v<S>, "the reference-order form exists for FP32 storage only");
+  using L = Lay<S>;
+  constexpr int TBX = L::TBX, HX = L::HX;
+  constexpr int BUF_BYTES = L::BUF_BYTES, OFF_Q = L::OFF_Q, OFF_MED = L::OFF_MED, OFF_M = L::OFF_M,
+                OFF_T = L::OFF_T;
   extern __shared__ __align__(1024) unsigned char smem[];
   const Geom& g = A.g;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
@@ -181,15 +243,30 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
   const int px = g.px, plane = int(g.plane);
   const long long fs = g.fstride;
   const int col = (i + PADL) + px * j;
-  const float* __restrict__ W = A.win;
+  const S* __restrict__ W = static_cast<const S*>(A.win);
+  S* __restrict__ Wout = static_cast<S*>(A.wout);
+  S* __restrict__ Wt = static_cast<S*>(A.wt);
+  // stored -> physical value of component f, and back (BF16/FP16 registers are scaled)
+  auto dec = [&](S v, int f) -> float {
+    if constexpr (is_f32_v<S>) return to_f(v);
+    else return to_f(v) * (f < 3 ? A.isv : A.ist);
+  };
+  auto enc = [&](float v, int f) -> S {
+    if constexpr (is_f32_v<S>) return from_f<S>(v);
+    else return from_f<S>(v * (f < 3 ? A.sv : A.st));
+  };
+  auto unscale = [&](float v, int f) -> float {
+    if constexpr (is_f32_v<S>) return v;
+    else return v * (f < 3 ? A.isv : A.ist);
+  };
   const int gst = __ldg(A.ntime) * 4 + A.stage;
   const bool fsurf = g.freesurf != 0;
-  const Sources& S = A.src;
+  const Sources& Src = A.src;
 
   constexpr int LEAD = FZ ? 3 : 1;   // planes ahead of k in the z operator
   constexpr int TRAIL = FZ ? 1 : 3;  // planes behind k
   constexpr uint32_t TX_BYTES =
-      SZ_TILE + SZ_Q + SZ_MED + (RK == 1 ? SZ_PT : 0) + (RK >= 1 ? SZ_PT : 0);
+      L::SZ_TILE + L::SZ_Q + L::SZ_MED + (RK == 1 ? L::SZ_PT : 0) + (RK >= 1 ? L::SZ_PT : 0);
 
   const uint32_t bar0 = smem_u32(smem + 2 * BUF_BYTES);
   if (tid == 0) {
@@ -218,16 +295,16 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
   // T*Src of this column (read on the top planes only)
   float tsx = 0.0f, tsy = 0.0f, tsz = 0.0f;
   if (fsurf && act && ke >= g.k2 - 3) {
-    tsx = surf_val(S, S.disp, gst, 0, i, j);
-    tsy = surf_val(S, S.disp, gst, 1, i, j);
-    tsz = surf_val(S, S.disp, gst, 2, i, j);
+    tsx = surf_val(Src, Src.disp, gst, 0, i, j);
+    tsy = surf_val(Src, Src.disp, gst, 1, i, j);
+    tsz = surf_val(Src, Src.disp, gst, 2, i, j);
   }
   // value pushed into the z queue for component qf (0..5 = storage index) at plane kk
   auto qval = [&](int qf, float raw, int kk) -> float {
     if (qf >= TZZ && fsurf && kk >= g.k2) {  // free_timg image (mod_macdrp.F90:3414-3436)
       const float ts = qf == TZZ ? tsz : (qf == TXZ ? tsx : tsy);
       if (kk == g.k2) return ts;
-      return 2.0f * ts - __ldg(W + qf * fs + col + (2 * g.k2 - kk) * plane);
+      return 2.0f * ts - dec(W[qf * fs + col + (2 * g.k2 - kk) * plane], qf);
     }
     return raw;
   };
@@ -239,7 +316,7 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
 #pragma unroll
     for (int d = 1; d < 5; ++d) {
       const int kk = kb - TRAIL + d - 1;
-      q[f][d] = act ? qval(f, __ldg(W + f * fs + col + kk * plane), kk) : 0.0f;
+      q[f][d] = act ? qval(f, dec(W[f * fs + col + kk * plane], f), kk) : 0.0f;
     }
   }
 
@@ -252,12 +329,12 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
   // Does this CTA's block of points touch any smoothed source box?  (tested once here
   // instead of per point and plane)
   bool cta_src = false;
-  for (int n = 0; n < S.nforce && !cta_src; ++n)
-    cta_src = S.force_c[3 * n] + 3 >= i0 && S.force_c[3 * n] - 3 <= i0 + TX - 1 && S.force_c[3 * n + 1] + 3 >= j0 &&
-              S.force_c[3 * n + 1] - 3 <= j0 + TY - 1 && S.force_c[3 * n + 2] + 3 >= kb && S.force_c[3 * n + 2] - 3 <= ke;
-  for (int n = 0; n < S.nmom && !cta_src; ++n)
-    cta_src = S.mom_c[3 * n] + 3 >= i0 && S.mom_c[3 * n] - 3 <= i0 + TX - 1 && S.mom_c[3 * n + 1] + 3 >= j0 &&
-              S.mom_c[3 * n + 1] - 3 <= j0 + TY - 1 && S.mom_c[3 * n + 2] + 3 >= kb && S.mom_c[3 * n + 2] - 3 <= ke;
+  for (int n = 0; n < Src.nforce && !cta_src; ++n)
+    cta_src = Src.force_c[3 * n] + 3 >= i0 && Src.force_c[3 * n] - 3 <= i0 + TX - 1 && Src.force_c[3 * n + 1] + 3 >= j0 &&
+              Src.force_c[3 * n + 1] - 3 <= j0 + TY - 1 && Src.force_c[3 * n + 2] + 3 >= kb && Src.force_c[3 * n + 2] - 3 <= ke;
+  for (int n = 0; n < Src.nmom && !cta_src; ++n)
+    cta_src = Src.mom_c[3 * n] + 3 >= i0 && Src.mom_c[3 * n] - 3 <= i0 + TX - 1 && Src.mom_c[3 * n + 1] + 3 >= j0 &&
+              Src.mom_c[3 * n + 1] - 3 <= j0 + TY - 1 && Src.mom_c[3 * n + 2] + 3 >= kb && Src.mom_c[3 * n + 2] - 3 <= ke;
 
   // PML slabs holding this column: the x and y slabs span every plane, so their
   // membership is fixed per thread (bits 0-3: x1 x2 y1 y2); the z slabs (bits 4, 5) are
@@ -301,11 +378,11 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
     if (k < ke) prefetch_pml(k + 1);
     const bool ok = mbar_wait(bar0 + 8 * cur, (it >> 1) & 1);
     unsigned char* buf = smem + cur * BUF_BYTES;
-    float(*tile)[TBY][TBX] = reinterpret_cast<float(*)[TBY][TBX]>(buf);
-    const float(*qs)[TY][TX] = reinterpret_cast<const float(*)[TY][TX]>(buf + OFF_Q);
+    S(*tile)[TBY][TBX] = reinterpret_cast<S(*)[TBY][TBX]>(buf);
+    const S(*qs)[TY][TX] = reinterpret_cast<const S(*)[TY][TX]>(buf + OFF_Q);
     const float(*med)[TY][TX] = reinterpret_cast<const float(*)[TY][TX]>(buf + OFF_MED);
-    const float(*mbuf)[TY][TX] = reinterpret_cast<const float(*)[TY][TX]>(buf + OFF_M);
-    const float(*tbuf)[TY][TX] = reinterpret_cast<const float(*)[TY][TX]>(buf + OFF_T);
+    const S(*mbuf)[TY][TX] = reinterpret_cast<const S(*)[TY][TX]>(buf + OFF_M);
+    const S(*tbuf)[TY][TX] = reinterpret_cast<const S(*)[TY][TX]>(buf + OFF_T);
     const bool top = fsurf && k == g.k2;
     if (top) {
       // the imaged stress components read T*Src on the free surface (interior columns)
@@ -314,9 +391,9 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
           const int r = e / TBX, cc = e % TBX;
           const int ii = i0 - HX + cc, jj = j0 - HY + r;
           if (ii >= g.i1 && ii <= g.i2 && jj >= g.j1 && jj <= g.j2) {
-            tile[TXZ][r][cc] = surf_val(S, S.disp, gst, 0, ii, jj);
-            tile[TYZ][r][cc] = surf_val(S, S.disp, gst, 1, ii, jj);
-            tile[TZZ][r][cc] = surf_val(S, S.disp, gst, 2, ii, jj);
+            tile[TXZ][r][cc] = enc(surf_val(Src, Src.disp, gst, 0, ii, jj), TXZ);
+            tile[TYZ][r][cc] = enc(surf_val(Src, Src.disp, gst, 1, ii, jj), TYZ);
+            tile[TZZ][r][cc] = enc(surf_val(Src, Src.disp, gst, 2, ii, jj), TZZ);
           }
         }
       __syncthreads();
@@ -328,7 +405,7 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
 #pragma unroll
       for (int f = 0; f < 6; ++f) {
         q[f][0] = q[f][1]; q[f][1] = q[f][2]; q[f][2] = q[f][3]; q[f][3] = q[f][4];
-        q[f][4] = img ? qval(f, qs[f][ty][tx], k + LEAD) : qs[f][ty][tx];
+        q[f][4] = img ? qval(f, dec(qs[f][ty][tx], f), k + LEAD) : dec(qs[f][ty][tx], f);
       }
       const unsigned pmask = slab_mask(k);
       const int p = col + k * plane;
@@ -336,18 +413,18 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
       const float ze = __ldg(A.zeta_z + k);
       const int r0 = ty + HY, c0 = tx + HX;
       // stencil sums along x (tile rows), y (tile columns), z (queue)
-      const float sxTxx = dop<FX>(&tile[TXX][r0][c0], 1);
-      const float sxTxy = dop<FX>(&tile[TXY][r0][c0], 1);
-      const float sxTxz = dop<FX>(&tile[TXZ][r0][c0], 1);
-      const float sxVx = dop<FX>(&tile[VX][r0][c0], 1);
-      const float sxVy = dop<FX>(&tile[VY][r0][c0], 1);
-      const float sxVz = dop<FX>(&tile[VZ][r0][c0], 1);
-      const float syTyy = dop<FY>(&tile[TYY][r0][c0], TBX);
-      const float syTxy = dop<FY>(&tile[TXY][r0][c0], TBX);
-      const float syTyz = dop<FY>(&tile[TYZ][r0][c0], TBX);
-      const float syVx = dop<FY>(&tile[VX][r0][c0], TBX);
-      const float syVy = dop<FY>(&tile[VY][r0][c0], TBX);
-      const float syVz = dop<FY>(&tile[VZ][r0][c0], TBX);
+      const float sxTxx = unscale(dopS<FX>(&tile[TXX][r0][c0], 1), TXX);
+      const float sxTxy = unscale(dopS<FX>(&tile[TXY][r0][c0], 1), TXY);
+      const float sxTxz = unscale(dopS<FX>(&tile[TXZ][r0][c0], 1), TXZ);
+      const float sxVx = unscale(dopS<FX>(&tile[VX][r0][c0], 1), VX);
+      const float sxVy = unscale(dopS<FX>(&tile[VY][r0][c0], 1), VY);
+      const float sxVz = unscale(dopS<FX>(&tile[VZ][r0][c0], 1), VZ);
+      const float syTyy = unscale(dopS<FY>(&tile[TYY][r0][c0], TBX), TYY);
+      const float syTxy = unscale(dopS<FY>(&tile[TXY][r0][c0], TBX), TXY);
+      const float syTyz = unscale(dopS<FY>(&tile[TYZ][r0][c0], TBX), TYZ);
+      const float syVx = unscale(dopS<FY>(&tile[VX][r0][c0], TBX), VX);
+      const float syVy = unscale(dopS<FY>(&tile[VY][r0][c0], TBX), VY);
+      const float syVz = unscale(dopS<FY>(&tile[VZ][r0][c0], TBX), VZ);
       const float szTzz = dopq<FZ>(q[TZZ]);
       const float szTxz = dopq<FZ>(q[TXZ]);
       const float szTyz = dopq<FZ>(q[TYZ]);
@@ -361,7 +438,8 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
       }
       const float Vx = q[VX][TRAIL], Vy = q[VY][TRAIL], Vz = q[VZ][TRAIL];
       const float Tzz = q[TZZ][TRAIL], Txz = q[TXZ][TRAIL], Tyz = q[TYZ][TRAIL];
-      const float Txx = tile[TXX][r0][c0], Tyy = tile[TYY][r0][c0], Txy = tile[TXY][r0][c0];
+      const float Txx = dec(tile[TXX][r0][c0], TXX), Tyy = dec(tile[TYY][r0][c0], TYY);
+      const float Txy = dec(tile[TXY][r0][c0], TXY);
       const bool water = miu <= 1.0e-20f;
 
       float hVx, hVy, hVz, hTxx, hTyy, hTzz, hTxy, hTxz, hTyz;
@@ -392,9 +470,9 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
         float E13 = (DxVz / r + DzVx - Vx / r) / 2.0f;
         float E23 = (DyVz / r / xs + DzVy - Vy / r) / 2.0f;
         if (top) {
-          E33 = -(lam / lam2mu * (E11 + E22)) + surf_val(S, S.rate, gst, 2, i, j) / lam2mu;
-          E13 = surf_val(S, S.rate, gst, 0, i, j) / miu / 2.0f;
-          E23 = surf_val(S, S.rate, gst, 1, i, j) / miu / 2.0f;
+          E33 = -(lam / lam2mu * (E11 + E22)) + surf_val(Src, Src.rate, gst, 2, i, j) / lam2mu;
+          E13 = surf_val(Src, Src.rate, gst, 0, i, j) / miu / 2.0f;
+          E23 = surf_val(Src, Src.rate, gst, 1, i, j) / miu / 2.0f;
         }
         hTxx = lam2mu * E11 + lam * (E22 + E33);
         hTyy = lam2mu * E22 + lam * (E11 + E33);
@@ -436,9 +514,9 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
         float E13 = 0.5f * (gxVz + gzVx - Vx * rr);
         float E23 = 0.5f * (gyVz + gzVy - Vy * rr);
         if (top) {
-          E33 = (surf_val(S, S.rate, gst, 2, i, j) - lam * (E11 + E22)) / lam2mu;
-          E13 = 0.5f * surf_val(S, S.rate, gst, 0, i, j) / miu;
-          E23 = 0.5f * surf_val(S, S.rate, gst, 1, i, j) / miu;
+          E33 = (surf_val(Src, Src.rate, gst, 2, i, j) - lam * (E11 + E22)) / lam2mu;
+          E13 = 0.5f * surf_val(Src, Src.rate, gst, 0, i, j) / miu;
+          E23 = 0.5f * surf_val(Src, Src.rate, gst, 1, i, j) / miu;
         }
         hTxx = lam2mu * E11 + lam * (E22 + E33);
         hTyy = lam2mu * E22 + lam * (E11 + E33);
@@ -536,31 +614,31 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
 
       // ---- moment tensors (src_stress, mod_src.F90:207-273)
 #pragma unroll 1
-      for (int n = 0; cta_src && n < S.nmom; ++n) {
-        const int li = i - S.mom_c[3 * n], lj = j - S.mom_c[3 * n + 1], lk = k - S.mom_c[3 * n + 2];
+      for (int n = 0; cta_src && n < Src.nmom; ++n) {
+        const int li = i - Src.mom_c[3 * n], lj = j - Src.mom_c[3 * n + 1], lk = k - Src.mom_c[3 * n + 2];
         if (li < -3 || li > 3 || lj < -3 || lj > 3 || lk < -3 || lk > 3) continue;
         const int e = n * 343 + (li + 3) + 7 * ((lj + 3) + 7 * (lk + 3));
-        if (!S.mom_on[e]) continue;
-        const float dd = S.mom_d[e], vol = S.mom_vol[e];
-        for (int m = 0; m < S.ntwin_m; ++m) {
-          const float rate = S.mrate[(long long)gst * S.nw_m + n * S.ntwin_m + m];
+        if (!Src.mom_on[e]) continue;
+        const float dd = Src.mom_d[e], vol = Src.mom_vol[e];
+        for (int m = 0; m < Src.ntwin_m; ++m) {
+          const float rate = Src.mrate[(long long)gst * Src.nw_m + n * Src.ntwin_m + m];
           const float V = dd * rate / vol;
-          const float* M = S.mom_M + 6 * (n * S.ntwin_m + m);
+          const float* M = Src.mom_M + 6 * (n * Src.ntwin_m + m);
           hTxx = hTxx - M[0] * V; hTyy = hTyy - M[1] * V; hTzz = hTzz - M[2] * V;
           hTxy = hTxy - M[3] * V; hTxz = hTxz - M[4] * V; hTyz = hTyz - M[5] * V;
         }
       }
       // ---- body forces (src_force, mod_src.F90:275-345)
 #pragma unroll 1
-      for (int n = 0; cta_src && n < S.nforce; ++n) {
-        const int li = i - S.force_c[3 * n], lj = j - S.force_c[3 * n + 1], lk = k - S.force_c[3 * n + 2];
+      for (int n = 0; cta_src && n < Src.nforce; ++n) {
+        const int li = i - Src.force_c[3 * n], lj = j - Src.force_c[3 * n + 1], lk = k - Src.force_c[3 * n + 2];
         if (li < -3 || li > 3 || lj < -3 || lj > 3 || lk < -3 || lk > 3) continue;
         const int e = n * 343 + (li + 3) + 7 * ((lj + 3) + 7 * (lk + 3));
-        if (!S.force_on[e]) continue;
-        const float V = S.force_wt[e];
-        for (int m = 0; m < S.ntwin_f; ++m) {
-          const float disp = S.disp[(long long)gst * S.nw_f + n * S.ntwin_f + m];
-          const float* F = S.force_F + 3 * (n * S.ntwin_f + m);
+        if (!Src.force_on[e]) continue;
+        const float V = Src.force_wt[e];
+        for (int m = 0; m < Src.ntwin_f; ++m) {
+          const float disp = Src.disp[(long long)gst * Src.nw_f + n * Src.ntwin_f + m];
+          const float* F = Src.force_F + 3 * (n * Src.ntwin_f + m);
           const float fx0 = F[0] * disp, fy0 = F[1] * disp, fz0 = F[2] * disp;
           hVx = hVx + fx0 * V; hVy = hVy + fy0 * V; hVz = hVz + fz0 * V;
         }
@@ -576,14 +654,14 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
         if (RK == 0) {
           // the tile holds the stored input; on the surface the imaged components were
           // patched in shared memory, so read those three from global memory there
-          const float m = (top && (f == TZZ || f == TXZ || f == TYZ)) ? __ldg(W + o) : tile[f][r0][c0];
-          st_stream(A.wout + o, m + A.a * hh[f], pol_stream);
-          st_stream(A.wt + o, m + A.b * hh[f], pol_stream);
+          const float m = dec((top && (f == TZZ || f == TXZ || f == TYZ)) ? W[o] : tile[f][r0][c0], f);
+          st_stream_s(Wout + o, enc(m + A.a * hh[f], f), pol_stream);
+          st_stream_s(Wt + o, enc(m + A.b * hh[f], f), pol_stream);
         } else if (RK == 1) {
-          st_stream(A.wout + o, mbuf[f][ty][tx] + A.a * hh[f], pol_stream);
-          st_stream(A.wt + o, tbuf[f][ty][tx] + A.b * hh[f], pol_stream);
+          st_stream_s(Wout + o, enc(dec(mbuf[f][ty][tx], f) + A.a * hh[f], f), pol_stream);
+          st_stream_s(Wt + o, enc(dec(tbuf[f][ty][tx], f) + A.b * hh[f], f), pol_stream);
         } else {
-          st_stream(A.wt + o, tbuf[f][ty][tx] + A.b * hh[f], pol_stream);
+          st_stream_s(Wt + o, enc(dec(tbuf[f][ty][tx], f) + A.b * hh[f], f), pol_stream);
         }
       }
     }
@@ -598,39 +676,39 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
   }
 }
 
-template <bool EXACT, int FX, int FY, int FZ, int RK>
+template <class S, bool EXACT, int FX, int FY, int FZ, int RK>
 static int launch_one(const StageArgs& a, const dim3& grid, cudaStream_t st) {
-  stage_kernel<EXACT, FX, FY, FZ, RK><<<grid, dim3(TX, TY, 1), SMEM_BYTES, st>>>(a);
+  stage_kernel<S, EXACT, FX, FY, FZ, RK><<<grid, dim3(TX, TY, 1), Lay<S>::SMEM_BYTES, st>>>(a);
   return int(cudaGetLastError());
 }
 
 // Opt every instantiation of one (EXACT, RK) pair into the dynamic shared memory it
 // needs; called once per device before any launch or stream capture.
-template <bool EXACT, int RK>
+template <class S, bool EXACT, int RK>
 static int configure_rk() {
   cudaError_t e = cudaSuccess;
-#define FW_CFG(FX, FY, FZ)                                                                                   \
-  if (e == cudaSuccess)                                                                                      \
-    e = cudaFuncSetAttribute(stage_kernel<EXACT, FX, FY, FZ, RK>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                             SMEM_BYTES);
+#define FW_CFG(FX, FY, FZ)                                                                                      \
+  if (e == cudaSuccess)                                                                                         \
+    e = cudaFuncSetAttribute(stage_kernel<S, EXACT, FX, FY, FZ, RK>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                             Lay<S>::SMEM_BYTES);
   FW_CFG(0, 0, 0) FW_CFG(0, 0, 1) FW_CFG(0, 1, 0) FW_CFG(0, 1, 1)
   FW_CFG(1, 0, 0) FW_CFG(1, 0, 1) FW_CFG(1, 1, 0) FW_CFG(1, 1, 1)
 #undef FW_CFG
   return int(e);
 }
 
-template <bool EXACT, int RK>
+template <class S, bool EXACT, int RK>
 static int launch_rk_variant(const StageArgs& a, int variant, cudaStream_t st) {
   const dim3 grid((a.g.ni + TX - 1) / TX, (a.g.nj + TY - 1) / TY, (a.g.nk + a.kc - 1) / a.kc);
   switch (variant) {
-    case 0: return launch_one<EXACT, 0, 0, 0, RK>(a, grid, st);
-    case 1: return launch_one<EXACT, 0, 0, 1, RK>(a, grid, st);
-    case 2: return launch_one<EXACT, 0, 1, 0, RK>(a, grid, st);
-    case 3: return launch_one<EXACT, 0, 1, 1, RK>(a, grid, st);
-    case 4: return launch_one<EXACT, 1, 0, 0, RK>(a, grid, st);
-    case 5: return launch_one<EXACT, 1, 0, 1, RK>(a, grid, st);
-    case 6: return launch_one<EXACT, 1, 1, 0, RK>(a, grid, st);
-    default: return launch_one<EXACT, 1, 1, 1, RK>(a, grid, st);
+    case 0: return launch_one<S, EXACT, 0, 0, 0, RK>(a, grid, st);
+    case 1: return launch_one<S, EXACT, 0, 0, 1, RK>(a, grid, st);
+    case 2: return launch_one<S, EXACT, 0, 1, 0, RK>(a, grid, st);
+    case 3: return launch_one<S, EXACT, 0, 1, 1, RK>(a, grid, st);
+    case 4: return launch_one<S, EXACT, 1, 0, 0, RK>(a, grid, st);
+    case 5: return launch_one<S, EXACT, 1, 0, 1, RK>(a, grid, st);
+    case 6: return launch_one<S, EXACT, 1, 1, 0, RK>(a, grid, st);
+    default: return launch_one<S, EXACT, 1, 1, 1, RK>(a, grid, st);
   }
 }
 

@@ -41,9 +41,11 @@ typedef enum fwant_status {
   FWANT_ERR_STATE = 6 /* call made in the wrong order (e.g. run before set_media) */
 } fwant_status;
 
-/* Storage kind of the wavefield registers (W, m, t) and the PML memory variables.
- * Arithmetic is always FP32 for the first three; FP64 stores and computes in double
- * (the FP64 run of the same solver used as the precision reference). */
+/* Storage kind of the wavefield registers (W and the RK registers m, t).  Arithmetic is
+ * FP32 for all three; the PML memory variables and the medium stay FP32.  BF16/FP16 store
+ * value * scale (fwant_set_storage_scale) and round to nearest even on every store.
+ * FP64 is reserved: the solver rejects it (FWANT_ERR_INVALID_ARG); the double-precision
+ * run used as the precision reference is the CPU restatement compiled for double. */
 typedef enum fwant_storage {
   FWANT_STORAGE_FP32 = 0,
   FWANT_STORAGE_BF16 = 1,
@@ -195,6 +197,18 @@ fwant_status fwant_get_snapshot(fwant_solver* s, const int subs[3], const int su
  * threads or handles on the same device) race with each other. */
 fwant_status fwant_get_snapshot_noalloc(fwant_solver* s, const int subs[3], const int subc[3], const int subt[3],
                                         int ncomp, const int* comps, float* out);
+
+/* Scale factors of 2-byte storage: velocities are stored as v * velocity_scale and stresses
+ * as t * stress_scale, and divided back on every load, so that FP16's range (6.1e-5 to
+ * 65504 normal) can be centred on the field's magnitudes.  Both must be powers of two
+ * (scaling is then exact) and set before the first time step; default 1, 1.  Ignored
+ * for FP32 storage.  No counterpart in the reference (it stores FP32 only). */
+fwant_status fwant_set_storage_scale(fwant_solver* s, float velocity_scale, float stress_scale);
+
+/* Largest |value| of each of the nine components over the whole register set, in receiver
+ * order (Vx Vy Vz Txx Tyy Tzz Txy Txz Tyz), physical units; NaN propagates.  The reduction
+ * macdrp_check (code/srcF/mod_macdrp.F90:228-264) makes, reported per component. */
+fwant_status fwant_max_abs(fwant_solver* s, float out[9]);
 
 /* Overflow check of the nine components: macdrp_check (code/srcF/mod_macdrp.F90:228-264).
  * Returns FWANT_ERR_NUMERIC_OVERFLOW when a value is NaN, Inf or >= huge(1.0). */

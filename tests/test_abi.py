@@ -47,3 +47,19 @@ def test_create_rejects_bad_config(native_lib):
     with pytest.raises(fw.FwantError) as e:
         fw.Solver(4, 20, 20, 0.01)
     assert e.value.code in (1, 3)  # INVALID_ARG (or CUDA_ERROR where no device exists)
+    # the configuration is validated before any device call
+    for kw in (dict(storage=fw.STORAGE_FP64), dict(storage=7), dict(storage=fw.STORAGE_BF16, exact_arith=True),
+               dict(storage=fw.STORAGE_FP16, exact_arith=True)):
+        with pytest.raises(fw.FwantError) as e:
+            fw.Solver(20, 20, 20, 0.01, **kw)
+        assert e.value.code == 1, kw
+
+
+def test_null_handles_are_rejected(native_lib):
+    import ctypes as C
+    import numpy as np
+    out = np.zeros(9, np.float32)
+    p = out.ctypes.data_as(C.POINTER(C.c_float))
+    assert native_lib.fwant_max_abs(None, p) == 1
+    assert native_lib.fwant_set_storage_scale(None, 1.0, 1.0) == 1
+    assert native_lib.fwant_check(None) == 1
