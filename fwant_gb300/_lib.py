@@ -56,6 +56,20 @@ EXPORTS = [
     ("fwant_set_field", C.c_int, [_vp, C.c_int, _fp]),
     ("fwant_get_snapshot", C.c_int, [_vp, _ip, _ip, _ip, C.c_int, _ip, _fp]),
     ("fwant_get_snapshot_noalloc", C.c_int, [_vp, _ip, _ip, _ip, C.c_int, _ip, _fp]),
+    ("fwant_set_sgt_record", C.c_int, [_vp, _ip, _ip, _ip, C.c_int, C.c_int]),
+    ("fwant_get_sgt", C.c_int, [_vp, _fp, C.c_int, _ip]),
+    ("fwant_sgtker_create", C.c_int, [C.c_longlong, C.c_int, C.c_double, C.c_int, C.POINTER(_vp)]),
+    ("fwant_sgtker_destroy", None, [_vp]),
+    ("fwant_sgtker_last_error", C.c_char_p, [_vp]),
+    ("fwant_sgtker_set_media", C.c_int, [_vp, _fp, _fp]),
+    ("fwant_sgtker_set_sgt", C.c_int, [_vp, C.c_int, _fp]),
+    ("fwant_sgtker_take_sgt", C.c_int, [_vp, C.c_int, _vp]),
+    ("fwant_sgtker_scatter", C.c_int, [_vp, C.c_int, C.c_int, C.c_int]),
+    ("fwant_sgtker_get_scatter", C.c_int, [_vp, C.c_int, C.POINTER(C.c_double)]),
+    ("fwant_sgtker_kernel", C.c_int, [_vp, C.c_int, _fp, _fp, C.c_int, C.c_int, C.c_double,
+                                      C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                      C.POINTER(C.c_double)]),
+    ("fwant_sgtker_last_scatter_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
     ("fwant_set_storage_scale", C.c_int, [_vp, C.c_float, C.c_float]),
     ("fwant_max_abs", C.c_int, [_vp, _fp]),
     ("fwant_check", C.c_int, [_vp]),
@@ -285,6 +299,26 @@ class Solver:
                                                        _ptr(t0, C.c_int), len(cm), _ptr(cm, C.c_int), _ptr(out)))
         return out.reshape(len(cm), int(c0[2]), int(c0[1]), int(c0[0])).transpose(0, 3, 2, 1)
 
+    def set_sgt_record(self, subs, subc, subt, tinv, max_frames):
+        """Keep sgt_ snapshot frames (six stresses of a strided sub-volume every tinv steps)
+        in device memory; subs 1-based with ghosts as in get_snapshot."""
+        a = [np.ascontiguousarray(np.asarray(v, dtype=np.int32).reshape(3)) for v in (subs, subc, subt)]
+        self._sgt_cnt = tuple(int(v) for v in a[1])
+        self._chk(self._lib.fwant_set_sgt_record(self._h, *[_ptr(v, C.c_int) for v in a], int(tinv),
+                                                 int(max_frames)))
+
+    def get_sgt(self, max_frames=None):
+        """Recorded frames as (6, nframes, npts) float32 (Txx Tyy Tzz Txy Txz Tyz; points i
+        fastest over the sub-volume counts)."""
+        npts = int(np.prod(self._sgt_cnt))
+        if max_frames is None:
+            max_frames = self.ntime
+        out = np.zeros(6 * max(int(max_frames), 1) * npts, np.float32)
+        nf = C.c_int()
+        self._chk(self._lib.fwant_get_sgt(self._h, _ptr(out), int(max_frames), C.byref(nf)))
+        n = nf.value
+        return out[: 6 * n * npts].reshape(6, n, npts)
+
     def set_storage_scale(self, velocity_scale, stress_scale):
         """Power-of-two scales of 2-byte storage (stored value = physical value * scale)."""
         self._chk(self._lib.fwant_set_storage_scale(self._h, float(velocity_scale), float(stress_scale)))
@@ -298,6 +332,69 @@ class Solver:
     def check(self):
         """macdrp_check: raises FwantError(NUMERIC_OVERFLOW) on NaN/Inf/huge."""
         self._chk(self._lib.fwant_check(self._h))
+
+
+class SgtKernel:
+    """Sensitivity-kernel accumulation of one block of npts kernel points
+    (SI_ker_sta.F90: stress2strain, sgt2scatter3, scatter2kernel) on the GPU, FP64 sums.
+    which: 0/1/2 = receiver station X/Y/Z force SGT, 3 = source station SGT."""
+
+    def __init__(self, npts, knt, kdt, device=0):
+        self._lib = load_library()
+        h = C.c_void_p()
+        rc = self._lib.fwant_sgtker_create(int(npts), int(knt), float(kdt), int(device), C.byref(h))
+        if rc != 0:
+            raise FwantError(rc, "fwant_sgtker_create failed")
+        self._h = h
+        self.npts, self.knt, self.kdt = int(npts), int(knt), float(kdt)
+
+    def _chk(self, rc):
+        if rc != 0:
+            raise FwantError(rc, self._lib.fwant_sgtker_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.fwant_sgtker_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_media(self, lam, mu):
+        a, b = _f32(lam, self.npts), _f32(mu, self.npts)
+        self._chk(self._lib.fwant_sgtker_set_media(self._h, _ptr(a), _ptr(b)))
+
+    def set_sgt(self, which, stress):
+        a = _f32(stress, 6 * self.knt * self.npts)
+        self._chk(self._lib.fwant_sgtker_set_sgt(self._h, int(which), _ptr(a)))
+
+    def take_sgt(self, which, solver):
+        self._chk(self._lib.fwant_sgtker_take_sgt(self._h, int(which), solver._h))
+
+    def scatter(self, flags, nt1=1, nt2=None):
+        nt2 = self.knt if nt2 is None else int(nt2)
+        self._chk(self._lib.fwant_sgtker_scatter(self._h, int(flags), int(nt1), nt2))
+
+    def get_scatter(self, slot):
+        out = np.zeros(self.knt * self.npts, np.float64)
+        self._chk(self._lib.fwant_sgtker_get_scatter(self._h, int(slot), _ptr(out, C.c_double)))
+        return out.reshape(self.knt, self.npts)
+
+    def kernel(self, ncmp, v, u, nt1, nt2, sgt_m0):
+        """(phase_Vp, amplitude_Vp, phase_Vs, amplitude_Vs) as float64 arrays of npts."""
+        v_, u_ = _f32(v, self.knt), _f32(u, self.knt)
+        outs = [np.zeros(self.npts, np.float64) for _ in range(4)]
+        self._chk(self._lib.fwant_sgtker_kernel(self._h, int(ncmp), _ptr(v_), _ptr(u_), int(nt1), int(nt2),
+                                                float(sgt_m0), *[_ptr(o, C.c_double) for o in outs]))
+        return tuple(outs)
+
+    def last_scatter_ms(self):
+        ms = C.c_double()
+        self._chk(self._lib.fwant_sgtker_last_scatter_ms(self._h, C.byref(ms)))
+        return ms.value
 
 
 def reference_steps(nt: int) -> int:

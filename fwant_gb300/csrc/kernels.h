@@ -158,6 +158,49 @@ void launch_pack_snapshot(const SnapArgs& a, void* stream);
 constexpr long long SNAPSHOT_NOALLOC_MAX = 4LL << 20;
 int snapshot_noalloc_staging(int device, float** ptr);
 
+// Strain-Green's-tensor recording: the six stresses of a strided sub-volume after every
+// step whose counter is a multiple of tinv (frame ntime/tinv - 1), into
+// out[6][max_frames][npts] (Txx Tyy Tzz Txy Txz Tyz, points i fastest).
+struct SgtRecArgs {
+  Geom g;
+  const void* w;
+  int storage;
+  float isv, ist;
+  int start[3], cnt[3], stride[3];
+  int tinv, max_frames;
+  long long npts;
+  const int* ntime;
+  float* out;
+};
+void launch_record_sgt(const SgtRecArgs& a, void* stream);
+
+// Sensitivity-kernel accumulation (sgtker.cu).  Strains of the receiver-side SGTs
+// (X, Y, Z force) and of the source-side SGT are formed from FP32 stresses in FP32
+// (stress2strain); the time convolutions and window integrals accumulate in FP64.
+struct ScatterArgs {
+  long long npts;
+  int knt;               // frames per series
+  int nt1, nt2;          // 1-based output range
+  double dt;
+  const float* lam;      // [npts]
+  const float* mu;       // [npts]
+  const float* rsgt[3];  // receiver SGT per force component, [6][knt][npts] stresses (null: skipped)
+  const float* ssgt;     // source SGT, [6][knt][npts]
+  double* out;           // [6][knt][npts]: X -> (0, 3), Y -> (1, 5), Z -> (2, 4)
+};
+int launch_sgt_scatter(const ScatterArgs& a, int sm_count, void* stream);
+struct KernelArgs {
+  long long npts;
+  int knt, nt1, nt2;
+  const double* ka;      // [knt][npts]
+  const double* kb;
+  const double* wv;      // [knt] trapezoid weight x V(n) (1-based n at index n-1)
+  const double* wu;      // [knt] trapezoid weight x U(n)
+  double v0, u0;         // normalisations: trapezoid integral of V^2 (U^2) x SGT_M0
+  double* kap; double* kaq; double* kbp; double* kbq;  // [npts]
+};
+void launch_scatter_kernel(const KernelArgs& a, void* stream);
+
 void launch_metric_fp64(int n, const float* coord, float* metric_out, int lo, int hi, void* stream);
 void launch_sincot_fp64(int n, const float* x, float* xsin, float* xcot, void* stream);
 // max |value| of each of the nine components (storage order) into out_bits[9]

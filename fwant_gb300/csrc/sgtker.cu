@@ -1,0 +1,162 @@
+// Sensitivity-kernel accumulation on the device: the strain Green's tensor convolution
+// of sgt2scatter3 (SI_ker_sta.F90:1257-1337) with the strains of stress2strain
+// (SI_ker_sta.F90:1185-1211), and the window integrals of scatter2kernel
+// (SI_ker_sta.F90:1375-1431).
+//
+// Strains are formed from the FP32 stresses with the reference's FP32 expressions
+// (round-to-nearest intrinsics: no contraction, IEEE division).  Products of two strains
+// are exact in FP64 and every sum runs in FP64 in a fixed order (ascending lag m, then the
+// six components Exx Eyy Ezz Exy Exz Eyz), so the results do not depend on the launch shape.
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+
+namespace fw {
+
+namespace {
+
+constexpr int SC_THREADS = 256;  // outputs n per CTA
+constexpr int SC_MCHUNK = 512;   // lags m staged per pass
+// per time index: trace (FP64) + six strains (FP64, shear components doubled on the receiver side)
+constexpr int SC_VALS = 7;
+
+struct Compliance {
+  float e1, e2, e3;
+};
+
+__device__ __forceinline__ Compliance compliance(float lam, float miu) {
+  // E1 = (lam+miu)/(miu*(3 lam+2 miu)), E2 = -lam/(2 miu (3 lam+2 miu)), E3 = 1/miu
+  const float s = __fadd_rn(__fmul_rn(3.0f, lam), __fmul_rn(2.0f, miu));
+  Compliance c;
+  c.e1 = __fdiv_rn(__fadd_rn(lam, miu), __fmul_rn(miu, s));
+  c.e2 = -__fdiv_rn(lam, __fmul_rn(__fmul_rn(2.0f, miu), s));
+  c.e3 = __fdiv_rn(1.0f, miu);
+  return c;
+}
+
+// Strains of one time index from the six stresses (Txx Tyy Tzz Txy Txz Tyz); FP32 as in
+// stress2strain.  Writes the FP64 trace and the six strains, shear scaled by `shear`.
+__device__ __forceinline__ void strain_at(const float* __restrict__ sgt, long long cstride, long long o,
+                                          const Compliance& c, double shear, double* dst, int ld) {
+  const float txx = sgt[o], tyy = sgt[o + cstride], tzz = sgt[o + 2 * cstride];
+  const float txy = sgt[o + 3 * cstride], txz = sgt[o + 4 * cstride], tyz = sgt[o + 5 * cstride];
+  const float e0 = __fmul_rn(c.e2, __fadd_rn(__fadd_rn(txx, tyy), tzz));
+  const float d = __fsub_rn(c.e2, c.e1);
+  const float h = __fmul_rn(0.5f, c.e3);
+  const float exx = __fsub_rn(e0, __fmul_rn(d, txx));
+  const float eyy = __fsub_rn(e0, __fmul_rn(d, tyy));
+  const float ezz = __fsub_rn(e0, __fmul_rn(d, tzz));
+  dst[0] = ((double)exx + (double)eyy) + (double)ezz;
+  dst[ld] = exx;
+  dst[2 * ld] = eyy;
+  dst[3 * ld] = ezz;
+  dst[4 * ld] = shear * (double)__fmul_rn(h, txy);
+  dst[5 * ld] = shear * (double)__fmul_rn(h, txz);
+  dst[6 * ld] = shear * (double)__fmul_rn(h, tyz);
+}
+
+// grid: x = point, y = receiver force component (0 X, 1 Y, 2 Z), z = chunk of outputs.
+// Output n (1-based) of thread t is nt1 + z*SC_THREADS + t.
+__global__ void __launch_bounds__(SC_THREADS) sgt_scatter_kernel(const ScatterArgs a) {
+  extern __shared__ double sm[];
+  const int comp = blockIdx.y;
+  const float* __restrict__ rs = comp == 0 ? a.rsgt[0] : (comp == 1 ? a.rsgt[1] : a.rsgt[2]);
+  if (!rs) return;
+  const long long p = blockIdx.x;
+  const int n_lo = a.nt1 + blockIdx.z * SC_THREADS;
+  const int n_hi = min(a.nt2, n_lo + SC_THREADS - 1);
+  const int n = n_lo + threadIdx.x;
+  const long long cs = (long long)a.knt * a.npts;  // stride between stress components
+  const Compliance cm = compliance(a.lam[p], a.mu[p]);
+
+  // R chunk: lags [m0, m0+SC_MCHUNK), ld = SC_MCHUNK; S window: indices n - m for the
+  // CTA's outputs and the chunk's lags, ld = SC_THREADS + SC_MCHUNK.
+  constexpr int LDR = SC_MCHUNK, LDS = SC_THREADS + SC_MCHUNK;
+  double* R = sm;
+  double* Sw = sm + SC_VALS * LDR;
+
+  double x1 = 0.0, x2 = 0.0;
+  for (int m0 = 1; m0 <= n_hi - 1; m0 += SC_MCHUNK) {
+    const int m1 = min(m0 + SC_MCHUNK, n_hi);  // exclusive
+    // S indices needed: [max(1, n_lo - m1 + 1), n_hi - m0]
+    const int s_lo = max(1, n_lo - m1 + 1);
+    const int s_hi = n_hi - m0;
+    __syncthreads();
+    for (int m = m0 + threadIdx.x; m < m1; m += SC_THREADS)
+      strain_at(rs, cs, (long long)(m - 1) * a.npts + p, cm, 2.0, R + (m - m0), LDR);
+    for (int s = s_lo + threadIdx.x; s <= s_hi; s += SC_THREADS)
+      strain_at(a.ssgt, cs, (long long)(s - 1) * a.npts + p, cm, 1.0, Sw + (s - s_lo), LDS);
+    __syncthreads();
+    if (n <= n_hi) {
+      const int mend = min(m1, n);  // m < n
+      for (int m = m0; m < mend; ++m) {
+        const double* r = R + (m - m0);
+        const double* q = Sw + (n - m - s_lo);
+        x1 = fma(r[0], q[0], x1);
+        x2 = fma(r[LDR], q[LDS], x2);
+        x2 = fma(r[2 * LDR], q[2 * LDS], x2);
+        x2 = fma(r[3 * LDR], q[3 * LDS], x2);
+        x2 = fma(r[4 * LDR], q[4 * LDS], x2);
+        x2 = fma(r[5 * LDR], q[5 * LDS], x2);
+        x2 = fma(r[6 * LDR], q[6 * LDS], x2);
+      }
+    }
+  }
+  if (n > n_hi) return;
+  const double lam = a.lam[p], mu = a.mu[p];
+  const double ka = (x1 * a.dt) * (2.0 * (lam + 2.0 * mu));
+  const double kb = ((x2 - x1) * a.dt) * (4.0 * mu);
+  // X -> (Exx, Exy), Y -> (Eyy, Eyz), Z -> (Ezz, Exz); component slots Exx Eyy Ezz Exy Exz Eyz
+  const int slot_a = comp, slot_b = comp == 0 ? 3 : (comp == 1 ? 5 : 4);
+  const long long o = (long long)(n - 1) * a.npts + p;
+  a.out[(long long)slot_a * cs + o] = ka;
+  a.out[(long long)slot_b * cs + o] = kb;
+}
+
+// scatter2kernel: trapezoid integrals of the two series against V and U, per point.
+__global__ void window_integral_kernel(const KernelArgs a) {
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= a.npts) return;
+  const double* ka = a.ka + p;
+  const double* kb = a.kb + p;
+  const long long ld = a.npts;
+  double sap = 0.0, saq = 0.0, sbp = 0.0, sbq = 0.0;
+  // trapezoid: both end points (weights carry the 1/2), then the interior in order
+  auto add = [&](int n) {
+    const double va = ka[(long long)(n - 1) * ld], vb = kb[(long long)(n - 1) * ld];
+    const double wv = a.wv[n - 1], wu = a.wu[n - 1];
+    sap = fma(wv, va, sap);
+    saq = fma(wu, va, saq);
+    sbp = fma(wv, vb, sbp);
+    sbq = fma(wu, vb, sbq);
+  };
+  add(a.nt1);
+  add(a.nt2);
+  for (int n = a.nt1 + 1; n < a.nt2; ++n) add(n);
+  a.kap[p] = sap / a.v0;
+  a.kaq[p] = saq / a.u0;
+  a.kbp[p] = sbp / a.v0;
+  a.kbq[p] = sbq / a.u0;
+}
+
+}  // namespace
+
+int launch_sgt_scatter(const ScatterArgs& a, int /*sm_count*/, void* stream) {
+  const size_t smem = sizeof(double) * SC_VALS * (SC_MCHUNK + SC_THREADS + SC_MCHUNK);
+  const cudaError_t e =
+      cudaFuncSetAttribute(sgt_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e != cudaSuccess) return int(e);
+  const int nout = a.nt2 - a.nt1 + 1;
+  if (a.npts <= 0 || nout <= 0) return 0;
+  dim3 grid((unsigned)a.npts, 3, (unsigned)((nout + SC_THREADS - 1) / SC_THREADS));
+  sgt_scatter_kernel<<<grid, SC_THREADS, smem, (cudaStream_t)stream>>>(a);
+  return int(cudaGetLastError());
+}
+
+void launch_scatter_kernel(const KernelArgs& a, void* stream) {
+  const long long blocks = (a.npts + 255) / 256;
+  if (blocks < 1) return;
+  window_integral_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(a);
+}
+
+}  // namespace fw

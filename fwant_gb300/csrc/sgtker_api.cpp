@@ -1,0 +1,259 @@
+// Host side of the sensitivity-kernel accumulation: one fwant_sgtker holds the strain
+// Green's tensors of one block of kernel points (the receiver station's X/Y/Z force
+// simulations and the source station's simulation, as the sgt_ snapshot files that
+// SI_ker_sta.F90 reads at :411-622), the media of those points, the scattering series
+// and the window kernels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/fwant_gb300.h"
+#include "kernels.h"
+
+namespace fw {
+int solver_sgt_view(fwant_solver* s, const float** data, long long* npts, int* max_frames, int* nframes,
+                    int* device);
+}
+
+struct fwant_sgtker {
+  long long npts = 0;
+  int knt = 0;
+  double kdt = 0.0;
+  int device = 0;
+  cudaStream_t st = nullptr;
+  float* lam = nullptr;
+  float* mu = nullptr;
+  float* sgt[4] = {nullptr, nullptr, nullptr, nullptr};  // X, Y, Z receiver SGT; source SGT
+  double* series = nullptr;                              // [6][knt][npts]
+  int scatter_nt1 = 0, scatter_nt2 = 0, scatter_flags = 0;
+  double* wts = nullptr;                                 // wv[knt], wu[knt]
+  double* kout = nullptr;                                // 4 x [npts]
+  bool have_media = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0.0;
+  std::string err;
+
+  ~fwant_sgtker() {
+    cudaSetDevice(device);
+    cudaFree(lam); cudaFree(mu);
+    for (float* p : sgt) cudaFree(p);
+    cudaFree(series); cudaFree(wts); cudaFree(kout);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (st) cudaStreamDestroy(st);
+  }
+  fwant_status fail(fwant_status c, const std::string& m) {
+    err = m;
+    return c;
+  }
+  fwant_status cuda_fail(cudaError_t e, const char* where) {
+    err = std::string(where) + ": " + cudaGetErrorString(e);
+    return FWANT_ERR_CUDA;
+  }
+  size_t series_len() const { return size_t(knt) * size_t(npts); }
+  template <class T>
+  fwant_status alloc(T** p, size_t n, const char* what) {
+    if (*p) return FWANT_OK;
+    void* q = nullptr;
+    if (cudaMalloc(&q, n * sizeof(T)) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(FWANT_ERR_OOM, std::string("out of device memory: ") + what);
+    }
+    *p = static_cast<T*>(q);
+    return FWANT_OK;
+  }
+};
+
+extern "C" {
+
+fwant_status fwant_sgtker_create(long long npts, int knt, double kdt, int device, fwant_sgtker** out) {
+  if (!out) return FWANT_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (npts < 1 || npts > 0x7fffffffLL || knt < 2 || !(kdt > 0.0)) return FWANT_ERR_INVALID_ARG;
+  auto* k = new fwant_sgtker();
+  k->npts = npts;
+  k->knt = knt;
+  k->kdt = kdt;
+  k->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&k->st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&k->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&k->ev1);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    delete k;
+    return FWANT_ERR_CUDA;
+  }
+  *out = k;
+  return FWANT_OK;
+}
+
+void fwant_sgtker_destroy(fwant_sgtker* k) { delete k; }
+
+const char* fwant_sgtker_last_error(fwant_sgtker* k) { return k ? k->err.c_str() : "null handle"; }
+
+fwant_status fwant_sgtker_set_media(fwant_sgtker* k, const float* lam, const float* mu) {
+  if (!k || !lam || !mu) return FWANT_ERR_INVALID_ARG;
+  for (long long p = 0; p < k->npts; ++p)
+    if (!(mu[p] > 0.0f) || !(lam[p] + mu[p] > 0.0f))
+      return k->fail(FWANT_ERR_INVALID_ARG, "sgtker media: mu must be > 0 at every kernel point (stress2strain)");
+  cudaSetDevice(k->device);
+  fwant_status rc;
+  if ((rc = k->alloc(&k->lam, size_t(k->npts), "lambda")) != FWANT_OK) return rc;
+  if ((rc = k->alloc(&k->mu, size_t(k->npts), "mu")) != FWANT_OK) return rc;
+  cudaError_t e = cudaMemcpy(k->lam, lam, size_t(k->npts) * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(k->mu, mu, size_t(k->npts) * sizeof(float), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return k->cuda_fail(e, "sgtker_set_media");
+  k->have_media = true;
+  return FWANT_OK;
+}
+
+fwant_status fwant_sgtker_set_sgt(fwant_sgtker* k, int which, const float* stress) {
+  if (!k || !stress || which < 0 || which > 3) return FWANT_ERR_INVALID_ARG;
+  cudaSetDevice(k->device);
+  fwant_status rc = k->alloc(&k->sgt[which], 6 * k->series_len(), "sgt");
+  if (rc != FWANT_OK) return rc;
+  cudaError_t e = cudaMemcpy(k->sgt[which], stress, 6 * k->series_len() * sizeof(float), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return k->cuda_fail(e, "sgtker_set_sgt");
+  return FWANT_OK;
+}
+
+fwant_status fwant_sgtker_take_sgt(fwant_sgtker* k, int which, fwant_solver* s) {
+  if (!k || !s || which < 0 || which > 3) return FWANT_ERR_INVALID_ARG;
+  const float* src = nullptr;
+  long long npts = 0;
+  int maxf = 0, nf = 0, dev = -1;
+  if (fw::solver_sgt_view(s, &src, &npts, &maxf, &nf, &dev))
+    return k->fail(FWANT_ERR_STATE, "sgtker_take_sgt: the solver records no SGT");
+  if (dev != k->device) return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_take_sgt: solver on another device");
+  if (npts != k->npts) return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_take_sgt: point count differs");
+  if (nf < k->knt) {
+    char b[128];
+    std::snprintf(b, sizeof(b), "sgtker_take_sgt: the solver has recorded %d frames, %d needed", nf, k->knt);
+    return k->fail(FWANT_ERR_STATE, b);
+  }
+  cudaSetDevice(k->device);
+  fwant_status rc = k->alloc(&k->sgt[which], 6 * k->series_len(), "sgt");
+  if (rc != FWANT_OK) return rc;
+  cudaError_t e = cudaSuccess;
+  for (int c = 0; c < 6 && e == cudaSuccess; ++c)
+    e = cudaMemcpyAsync(k->sgt[which] + size_t(c) * k->series_len(), src + size_t(c) * size_t(maxf) * size_t(npts),
+                        k->series_len() * sizeof(float), cudaMemcpyDeviceToDevice, k->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(k->st);
+  if (e != cudaSuccess) return k->cuda_fail(e, "sgtker_take_sgt");
+  return FWANT_OK;
+}
+
+fwant_status fwant_sgtker_scatter(fwant_sgtker* k, int flags, int nt1, int nt2) {
+  if (!k) return FWANT_ERR_INVALID_ARG;
+  if ((flags & 7) == 0 || (flags & ~7)) return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_scatter: flags must be 1..7");
+  if (nt1 < 1 || nt2 > k->knt || nt1 > nt2) return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_scatter: bad nt1/nt2");
+  if (!k->have_media) return k->fail(FWANT_ERR_STATE, "sgtker_scatter: media not set");
+  if (!k->sgt[3]) return k->fail(FWANT_ERR_STATE, "sgtker_scatter: source SGT not set");
+  for (int c = 0; c < 3; ++c)
+    if ((flags >> c & 1) && !k->sgt[c]) return k->fail(FWANT_ERR_STATE, "sgtker_scatter: receiver SGT not set");
+  cudaSetDevice(k->device);
+  fwant_status rc = k->alloc(&k->series, 6 * k->series_len(), "scatter series");
+  if (rc != FWANT_OK) return rc;
+  cudaMemsetAsync(k->series, 0, 6 * k->series_len() * sizeof(double), k->st);
+  fw::ScatterArgs a{};
+  a.npts = k->npts;
+  a.knt = k->knt;
+  a.nt1 = nt1;
+  a.nt2 = nt2;
+  a.dt = k->kdt;
+  a.lam = k->lam;
+  a.mu = k->mu;
+  for (int c = 0; c < 3; ++c) a.rsgt[c] = (flags >> c & 1) ? k->sgt[c] : nullptr;
+  a.ssgt = k->sgt[3];
+  a.out = k->series;
+  cudaEventRecord(k->ev0, k->st);
+  int le = fw::launch_sgt_scatter(a, 0, k->st);
+  cudaEventRecord(k->ev1, k->st);
+  cudaError_t e = le ? cudaError_t(le) : cudaStreamSynchronize(k->st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return k->cuda_fail(e, "sgtker_scatter");
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, k->ev0, k->ev1);
+  k->last_ms = ms;
+  k->scatter_nt1 = nt1;
+  k->scatter_nt2 = nt2;
+  k->scatter_flags = flags;
+  return FWANT_OK;
+}
+
+fwant_status fwant_sgtker_get_scatter(fwant_sgtker* k, int slot, double* out) {
+  if (!k || !out || slot < 0 || slot > 5) return FWANT_ERR_INVALID_ARG;
+  if (!k->series) return k->fail(FWANT_ERR_STATE, "sgtker_get_scatter: no scatter computed");
+  cudaSetDevice(k->device);
+  cudaError_t e = cudaMemcpy(out, k->series + size_t(slot) * k->series_len(), k->series_len() * sizeof(double),
+                             cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return k->cuda_fail(e, "sgtker_get_scatter");
+  return FWANT_OK;
+}
+
+fwant_status fwant_sgtker_kernel(fwant_sgtker* k, int ncmp, const float* v, const float* u, int nt1, int nt2,
+                                 double sgt_m0, double* kap, double* kaq, double* kbp, double* kbq) {
+  if (!k || !v || !u || !kap || !kaq || !kbp || !kbq) return FWANT_ERR_INVALID_ARG;
+  if (ncmp < 1 || ncmp > 3) return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_kernel: ncmp must be 1, 2 or 3");
+  if (!k->series || !(k->scatter_flags >> (ncmp - 1) & 1))
+    return k->fail(FWANT_ERR_STATE, "sgtker_kernel: scatter of this component not computed");
+  if (nt1 < k->scatter_nt1 || nt2 > k->scatter_nt2 || nt1 > nt2)
+    return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_kernel: window outside the scatter range");
+  // normalisation (SI_ker_sta.F90:1397-1402): trapezoid integral of V^2 and U^2 times SGT_M0
+  const double dt = k->kdt;
+  const double v1 = v[nt1 - 1], v2 = v[nt2 - 1], u1 = u[nt1 - 1], u2 = u[nt2 - 1];
+  double v0 = (0.5 * v1 * v1 + 0.5 * v2 * v2) * dt, u0 = (0.5 * u1 * u1 + 0.5 * u2 * u2) * dt;
+  for (int n = nt1 + 1; n <= nt2 - 1; ++n) {
+    const double vn = v[n - 1], un = u[n - 1];
+    v0 += vn * vn * dt;
+    u0 += un * un * dt;
+  }
+  v0 *= sgt_m0;
+  u0 *= sgt_m0;
+  if (!(v0 != 0.0) || !(u0 != 0.0)) return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_kernel: zero normalisation");
+  std::vector<double> w(2 * size_t(k->knt), 0.0);
+  for (int n = nt1; n <= nt2; ++n) {
+    const double wt = (n == nt1 || n == nt2) ? 0.5 * dt : dt;
+    w[n - 1] = wt * double(v[n - 1]);
+    w[k->knt + n - 1] = wt * double(u[n - 1]);
+  }
+  cudaSetDevice(k->device);
+  fwant_status rc = k->alloc(&k->wts, 2 * size_t(k->knt), "weights");
+  if (rc == FWANT_OK) rc = k->alloc(&k->kout, 4 * size_t(k->npts), "kernels");
+  if (rc != FWANT_OK) return rc;
+  cudaError_t e = cudaMemcpyAsync(k->wts, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, k->st);
+  static const int slot_a[3] = {0, 1, 2}, slot_b[3] = {3, 5, 4};
+  fw::KernelArgs a{};
+  a.npts = k->npts;
+  a.knt = k->knt;
+  a.nt1 = nt1;
+  a.nt2 = nt2;
+  a.ka = k->series + size_t(slot_a[ncmp - 1]) * k->series_len();
+  a.kb = k->series + size_t(slot_b[ncmp - 1]) * k->series_len();
+  a.wv = k->wts;
+  a.wu = k->wts + k->knt;
+  a.v0 = v0;
+  a.u0 = u0;
+  const size_t np = size_t(k->npts);
+  a.kap = k->kout; a.kaq = k->kout + np; a.kbp = k->kout + 2 * np; a.kbq = k->kout + 3 * np;
+  fw::launch_scatter_kernel(a, k->st);
+  double* dst[4] = {kap, kaq, kbp, kbq};
+  for (int q = 0; q < 4 && e == cudaSuccess; ++q)
+    e = cudaMemcpyAsync(dst[q], k->kout + q * np, np * sizeof(double), cudaMemcpyDeviceToHost, k->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(k->st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return k->cuda_fail(e, "sgtker_kernel");
+  return FWANT_OK;
+}
+
+fwant_status fwant_sgtker_last_scatter_ms(fwant_sgtker* k, double* ms) {
+  if (!k || !ms) return FWANT_ERR_INVALID_ARG;
+  *ms = k->last_ms;
+  return FWANT_OK;
+}
+
+}  // extern "C"

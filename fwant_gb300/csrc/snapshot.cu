@@ -34,6 +34,37 @@ void launch_pack_snapshot(const SnapArgs& a, void* stream) {
   pack_snapshot_kernel<<<int(blocks), 256, 0, (cudaStream_t)stream>>>(a);
 }
 
+// Stress components of an SGT frame in storage order: Txx Tyy Tzz Txy Txz Tyz.
+__constant__ int kSgtComp[6] = {6, 7, 3, 8, 4, 5};
+
+__global__ void record_sgt_kernel(const SgtRecArgs a) {
+  const int nt = *a.ntime;
+  if (nt <= 0 || nt % a.tinv != 0) return;
+  const int frame = nt / a.tinv - 1;
+  if (frame >= a.max_frames) return;
+  const long long tot = a.npts * 6;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
+    const int c = int(e / a.npts);
+    long long r = e - (long long)c * a.npts;
+    const long long pt = r;
+    const int ii = int(r % a.cnt[0]);
+    r /= a.cnt[0];
+    const int jj = int(r % a.cnt[1]);
+    const int kk = int(r / a.cnt[1]);
+    const int i = a.start[0] + ii * a.stride[0], j = a.start[1] + jj * a.stride[1], k = a.start[2] + kk * a.stride[2];
+    const long long p = (long long)(i + PADL) + (long long)a.g.px * ((long long)j + (long long)a.g.ny * k);
+    a.out[((long long)c * a.max_frames + frame) * a.npts + pt] =
+        load_component(a.w, a.storage, a.g.fstride, kSgtComp[c], p, a.isv, a.ist);
+  }
+}
+
+void launch_record_sgt(const SgtRecArgs& a, void* stream) {
+  long long blocks = (a.npts * 6 + 255) / 256;
+  if (blocks > 152LL * 8) blocks = 152LL * 8;
+  if (blocks < 1) blocks = 1;
+  record_sgt_kernel<<<int(blocks), 256, 0, (cudaStream_t)stream>>>(a);
+}
+
 // Staging buffer of fwant_get_snapshot_noalloc, for callers that must not allocate
 // device memory.  It is a module-scope device array, so it exists on every device that
 // loads this library, for as long as the library stays loaded; every call on a device

@@ -100,6 +100,10 @@ struct fwant_solver {
   unsigned int* d_maxbits = nullptr;
   float* d_snap = nullptr;  // staging buffer of fwant_get_snapshot (grown on demand)
   size_t snap_cap = 0;
+  // strain Green's tensor recording: sgt_ snapshot frames kept on the device
+  float* d_sgt = nullptr;
+  fw::SgtRecArgs sgt{};
+  bool sgt_on = false;
 
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one per (rA,rT) assignment
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -113,7 +117,7 @@ struct fwant_solver {
     cudaFree(d_x); cudaFree(d_y); cudaFree(d_z); cudaFree(d_xsin); cudaFree(d_xcot);
     cudaFree(d_xi); cudaFree(d_eta); cudaFree(d_zeta); cudaFree(d_prof); cudaFree(d_rzinv); cudaFree(d_rsinv);
     for (int f = 0; f < 6; ++f) cudaFree(aux[f]);
-    cudaFree(d_rec); cudaFree(d_seis); cudaFree(d_ntime); cudaFree(d_maxbits); cudaFree(d_snap); cudaFree(d_conv);
+    cudaFree(d_rec); cudaFree(d_seis); cudaFree(d_ntime); cudaFree(d_maxbits); cudaFree(d_snap); cudaFree(d_conv); cudaFree(d_sgt);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (st) cudaStreamDestroy(st);
@@ -618,6 +622,11 @@ struct fwant_solver {
     r.storage = stor; r.isv = 1.0f / sv; r.ist = 1.0f / sc_t;
     r.ntime = d_ntime;
     fw::launch_advance_record(r, st);
+    if (sgt_on) {
+      fw::SgtRecArgs q = sgt;
+      q.w = set(rT);
+      fw::launch_record_sgt(q, st);
+    }
     if (ev) cudaEventRecord(ev[5], st);
     std::swap(rA, rT);
     cycle_pos = (cycle_pos + 1) & 7;
@@ -1079,6 +1088,71 @@ fwant_status fwant_get_snapshot_noalloc(fwant_solver* s, const int subs[3], cons
   if (e != cudaSuccess) return s->cuda_fail(e, "get_snapshot_noalloc");
   return FWANT_OK;
 }
+
+fwant_status fwant_set_sgt_record(fwant_solver* s, const int subs[3], const int subc[3], const int subt[3], int tinv,
+                                  int max_frames) {
+  if (!s) return FWANT_ERR_INVALID_ARG;
+  if (tinv < 1 || max_frames < 1) return s->fail(FWANT_ERR_INVALID_ARG, "sgt record: tinv and max_frames must be >= 1");
+  if (s->ntime != 0) return s->fail(FWANT_ERR_STATE, "sgt record: set before the first time step");
+  cudaSetDevice(s->cfg.device);
+  static const int comps[1] = {3};
+  fw::SnapArgs a;
+  size_t n = 0;
+  fwant_status rc = s->snap_setup(subs, subc, subt, 1, comps, a, n);
+  if (rc != FWANT_OK) return rc;
+  const size_t total = n * 6 * size_t(max_frames);
+  cudaFree(s->d_sgt);
+  s->d_sgt = dalloc<float>(total);
+  s->sgt_on = false;
+  if (!s->d_sgt) return s->fail(FWANT_ERR_OOM, "sgt record buffer");
+  cudaMemset(s->d_sgt, 0, total * sizeof(float));
+  fw::SgtRecArgs& r = s->sgt;
+  r = fw::SgtRecArgs{};
+  r.g = s->g;
+  r.storage = s->stor;
+  r.isv = 1.0f / s->sv; r.ist = 1.0f / s->sc_t;
+  for (int d = 0; d < 3; ++d) { r.start[d] = a.start[d]; r.cnt[d] = a.cnt[d]; r.stride[d] = a.stride[d]; }
+  r.tinv = tinv;
+  r.max_frames = max_frames;
+  r.npts = (long long)n;
+  r.ntime = s->d_ntime;
+  r.out = s->d_sgt;
+  s->sgt_on = true;
+  s->drop_graphs();
+  return FWANT_OK;
+}
+
+fwant_status fwant_get_sgt(fwant_solver* s, float* out, int max_frames, int* nframes) {
+  if (!s || !out || !nframes || max_frames < 0) return FWANT_ERR_INVALID_ARG;
+  if (!s->sgt_on) return s->fail(FWANT_ERR_STATE, "get_sgt: no sgt record configured");
+  cudaSetDevice(s->cfg.device);
+  const int have = std::min(s->ntime / s->sgt.tinv, s->sgt.max_frames);
+  const int nf = std::min(have, max_frames);
+  const size_t npts = size_t(s->sgt.npts);
+  cudaError_t e = cudaSuccess;
+  for (int c = 0; c < 6 && e == cudaSuccess && nf > 0; ++c)
+    e = cudaMemcpy(out + size_t(c) * nf * npts, s->d_sgt + size_t(c) * s->sgt.max_frames * npts,
+                   size_t(nf) * npts * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return s->cuda_fail(e, "get_sgt");
+  *nframes = nf;
+  return FWANT_OK;
+}
+
+extern "C++" {
+namespace fw {
+// Device view of a solver's SGT record for the sensitivity-kernel object.
+int solver_sgt_view(fwant_solver* s, const float** data, long long* npts, int* max_frames, int* nframes,
+                    int* device) {
+  if (!s || !s->sgt_on) return 1;
+  *data = s->d_sgt;
+  *npts = s->sgt.npts;
+  *max_frames = s->sgt.max_frames;
+  *nframes = std::min(s->ntime / s->sgt.tinv, s->sgt.max_frames);
+  *device = s->cfg.device;
+  return 0;
+}
+}  // namespace fw
+}  // extern "C++"
 
 fwant_status fwant_check(fwant_solver* s) {
   if (!s) return FWANT_ERR_INVALID_ARG;

@@ -198,6 +198,62 @@ fwant_status fwant_get_snapshot(fwant_solver* s, const int subs[3], const int su
 fwant_status fwant_get_snapshot_noalloc(fwant_solver* s, const int subs[3], const int subc[3], const int subt[3],
                                         int ncomp, const int* comps, float* out);
 
+/* Record the strain Green's tensor on the device: the six stresses (Txx Tyy Tzz Txy Txz
+ * Tyz) of a strided sub-volume after every step whose counter is a multiple of tinv, i.e.
+ * the frames of the sgt_ snapshot files (io_wave_export, code/srcF/mod_io.F90:505-560,
+ * snap_NNN with a "T" variable list, :180-205), kept in device memory instead of files.
+ * subs/subc/subt as in fwant_get_snapshot; frame f (0-based) is taken at ntime =
+ * (f+1)*tinv; at most max_frames frames are kept.  Set before the first time step. */
+fwant_status fwant_set_sgt_record(fwant_solver* s, const int subs[3], const int subc[3], const int subt[3], int tinv,
+                                  int max_frames);
+
+/* Recorded SGT frames: out is [6][nframes][subc[2]][subc[1]][subc[0]] (component, frame,
+ * point with i fastest): per component the (I,J,K,time) layout of one sgt_ file variable.
+ * Copies at most max_frames frames; *nframes gets the number copied. */
+fwant_status fwant_get_sgt(fwant_solver* s, float* out, int max_frames, int* nframes);
+
+/* ---- Sensitivity-kernel accumulation (code/srcF.kernel/SI_ker_sta.F90) ----
+ * One fwant_sgtker holds one block of npts kernel points: the strain Green's tensors of
+ * the receiver station's three force simulations (which = 0 X, 1 Y, 2 Z) and of the
+ * source station (which = 3), each as knt frames of the six stresses
+ * ([6][knt][npts], Txx Tyy Tzz Txy Txz Tyz), frame n at time n*kdt
+ * (kdt = sub_gtinv*stept, SI_ker_sta.F90:274), and lambda, mu at the points.
+ * Strains are formed in FP32 exactly as stress2strain (SI_ker_sta.F90:1185-1211); the
+ * convolutions and window integrals accumulate in FP64 on the device. */
+typedef struct fwant_sgtker fwant_sgtker;
+fwant_status fwant_sgtker_create(long long npts, int knt, double kdt, int device, fwant_sgtker** out);
+void fwant_sgtker_destroy(fwant_sgtker* k);
+const char* fwant_sgtker_last_error(fwant_sgtker* k);
+/* lambda, mu at the npts kernel points (the media file read with the block's
+ * bsubs/bsubc/bsubt); mu must be > 0 everywhere (stress2strain divides by it). */
+fwant_status fwant_sgtker_set_media(fwant_sgtker* k, const float* lam, const float* mu);
+/* SGT of one simulation from host memory ([6][knt][npts] FP32 stresses). */
+fwant_status fwant_sgtker_set_sgt(fwant_sgtker* k, int which, const float* stress);
+/* SGT of one simulation from a solver's device record (fwant_set_sgt_record with npts
+ * points and at least knt recorded frames; device-to-device copy of the first knt). */
+fwant_status fwant_sgtker_take_sgt(fwant_sgtker* k, int which, fwant_solver* s);
+/* sgt2scatter3 (SI_ker_sta.F90:1257-1337) for the force components in flags (bit 0 X,
+ * bit 1 Y, bit 2 Z; the reference's flag_udx/y/z), outputs n = nt1..nt2 (1-based):
+ *   x1(n) = dt sum_{m=1}^{n-1} tr E_R(m) tr E_S(n-m)
+ *   x2(n) = dt sum_{m=1}^{n-1} E_R(m) : E_S(n-m)   (shear terms doubled)
+ *   Ka(n) = x1 * 2 (lambda + 2 mu),  Kb(n) = (x2 - x1) * 4 mu
+ * into the series slots of the reference's in-place outputs: X -> (0 Exx, 3 Exy),
+ * Y -> (1 Eyy, 5 Eyz), Z -> (2 Ezz, 4 Exz).  Slots of components not computed hold 0. */
+fwant_status fwant_sgtker_scatter(fwant_sgtker* k, int flags, int nt1, int nt2);
+/* One series slot (0..5: Exx Eyy Ezz Exy Exz Eyz positions), [knt][npts] FP64. */
+fwant_status fwant_sgtker_get_scatter(fwant_sgtker* k, int slot, double* out);
+/* scatter2kernel (SI_ker_sta.F90:1375-1431) for component ncmp (1 X, 2 Y, 3 Z: the
+ * reference's ncmp 1..3, no rotation): trapezoid integrals over frames nt1..nt2 of
+ * V(n) Ka(n), U(n) Ka(n), V(n) Kb(n), U(n) Kb(n), each divided by the trapezoid integral
+ * of V^2 (or U^2) times sgt_m0.  v, u: [knt] receiver velocity and displacement
+ * (already filtered); outputs [npts] FP64: phase_Vp, amplitude_Vp, phase_Vs,
+ * amplitude_Vs of the kernel file. */
+fwant_status fwant_sgtker_kernel(fwant_sgtker* k, int ncmp, const float* v, const float* u, int nt1, int nt2,
+                                 double sgt_m0, double* kap, double* kaq, double* kbp, double* kbq);
+/* Device time of the last fwant_sgtker_scatter in milliseconds.  No counterpart in the
+ * reference. */
+fwant_status fwant_sgtker_last_scatter_ms(fwant_sgtker* k, double* ms);
+
 /* Scale factors of 2-byte storage: velocities are stored as v * velocity_scale and stresses
  * as t * stress_scale, and divided back on every load, so that FP16's range (6.1e-5 to
  * 65504 normal) can be centred on the field's magnitudes.  Both must be powers of two

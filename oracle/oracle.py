@@ -1,6 +1,7 @@
 """ORACLE — test infrastructure, never the product.
 
-ctypes binding of the CPU restatement in fwant_oracle.cpp.  `Oracle` has the same
+ctypes binding of the CPU restatements in fwant_oracle.cpp (the forward solver) and
+sgtker_oracle.cpp (the sensitivity-kernel accumulation).  `Oracle` has the same
 set-up methods as `fwant_gb300.Solver`, so a test feeds both from one Model.  Only the
 tests, `__graft_entry__.smoke()` and the `cpu_baseline` leg of `bench.py` use it.
 """
@@ -13,7 +14,7 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SRC = os.path.join(HERE, "fwant_oracle.cpp")
+SRCS = [os.path.join(HERE, "fwant_oracle.cpp"), os.path.join(HERE, "sgtker_oracle.cpp")]
 LIB = os.path.join(HERE, "_build", "libfwant_oracle.so")
 COMPONENTS = ("Vx", "Vy", "Vz", "Txx", "Tyy", "Tzz", "Txy", "Txz", "Tyz")
 
@@ -47,15 +48,20 @@ _SIGS = [
     ("orc_metric", None, [C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, _fp, _fp, _fp, _fp, _fp]),
     ("orc_metric_dp", None, [C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, _fp, _fp, _fp, _fp, _fp]),
     ("orc_op", C.c_double, [C.c_int, C.c_int, _dp, C.c_int]),
+    ("orc_stress2strain", None, [C.c_longlong, C.c_int, _fp, _fp, _fp, _fp]),
+    ("orc_sgt2scatter3", None, [C.c_longlong, C.c_int, C.c_int, C.c_int, C.c_double, _fp, _fp, _fp, _fp, _fp, _fp,
+                                C.c_int, _dp]),
+    ("orc_scatter2kernel", None, [C.c_longlong, C.c_int, C.c_int, C.c_int, C.c_double, _fp, _fp, _dp, _dp,
+                                  C.c_double, C.c_int, _dp, _dp, _dp, _dp]),
 ]
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
     """Compile the oracle (g++, OpenMP, no FP contraction)."""
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(s) for s in SRCS):
         return LIB
-    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-o", LIB, SRC]
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-o", LIB, *SRCS]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -91,6 +97,51 @@ def _p(a, t=C.c_double):
 
 def set_threads(n: int) -> int:
     return lib().orc_set_threads(int(n))
+
+
+def _f(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1))
+
+
+def stress2strain(lam, mu, stress):
+    """stress: (6, knt, npts) Txx Tyy Tzz Txy Txz Tyz -> strains of the same shape (FP32)."""
+    st = np.asarray(stress, np.float32)
+    _, knt, npts = st.shape
+    out = np.zeros(st.size, np.float32)
+    lam_, mu_, s_ = _f(lam), _f(mu), _f(st)
+    lib().orc_stress2strain(npts, knt, _p(lam_, C.c_float), _p(mu_, C.c_float), _p(s_, C.c_float),
+                            _p(out, C.c_float))
+    return out.reshape(st.shape)
+
+
+def sgt2scatter3(lam, mu, rsgt, ssgt, dt, nt1=None, nt2=None, mode=1):
+    """rsgt: [X, Y, Z] receiver SGT stresses (6, knt, npts) or None; ssgt the source SGT.
+    mode 0: the reference's FP32 arithmetic; mode 1: FP64 accumulation.  Returns
+    (6, knt, npts) float64 series (slots X -> 0, 3; Y -> 1, 5; Z -> 2, 4)."""
+    s = _f(ssgt)
+    _, knt, npts = np.asarray(ssgt).shape
+    nt1 = 1 if nt1 is None else int(nt1)
+    nt2 = knt if nt2 is None else int(nt2)
+    rs = [None if r is None else _f(r) for r in rsgt]
+    out = np.zeros(6 * knt * npts, np.float64)
+    lam_, mu_ = _f(lam), _f(mu)
+    ptrs = [None if r is None else _p(r, C.c_float) for r in rs]
+    lib().orc_sgt2scatter3(npts, knt, nt1, nt2, float(dt), _p(lam_, C.c_float), _p(mu_, C.c_float), *ptrs,
+                           _p(s, C.c_float), int(mode), _p(out))
+    return out.reshape(6, knt, npts)
+
+
+def scatter2kernel(v, u, ka, kb, dt, nt1, nt2, sgt_m0, mode=1):
+    """Window kernels (phase_Vp, amplitude_Vp, phase_Vs, amplitude_Vs) of series ka, kb
+    ((knt, npts) float64) against V and U over frames nt1..nt2 (1-based)."""
+    ka_ = np.ascontiguousarray(ka, np.float64)
+    kb_ = np.ascontiguousarray(kb, np.float64)
+    knt, npts = ka_.shape
+    v_, u_ = _f(v), _f(u)
+    outs = [np.zeros(npts, np.float64) for _ in range(4)]
+    lib().orc_scatter2kernel(npts, knt, int(nt1), int(nt2), float(dt), _p(v_, C.c_float), _p(u_, C.c_float),
+                             _p(ka_), _p(kb_), float(sgt_m0), int(mode), *[_p(o) for o in outs])
+    return tuple(outs)
 
 
 class Oracle:
