@@ -6,9 +6,10 @@ Workload (default, --config c2): 400x400x200 interior grid, 1 km horizontal spac
 correlated (10 km) Vp/Vs perturbation, 12-cell CFS-PML on five faces, free surface,
 64 surface receivers, and three simulations (vertical/horizontal point forces Fx, Fy,
 Fz; Ricker 0.2 Hz) that together produce the strain Green's tensors.  One bench step =
-one LDDRK4 time step (four fused stage launches + the step-end kernel) of each of the
-three simulations.  Inputs are synthetic and seeded.  The register sets (9 components x
-4 x 37.5M points x 4 B per simulation) are far larger than L2, so no L2 flush is used.
+one LDDRK4 time step of the three simulations stepped as a batch: four fused stage
+launches, each covering all three, plus each simulation's step-end kernel.  Inputs are
+synthetic and seeded.  The register sets (9 components x 4 x 32M points x 4 B per
+simulation) are far larger than L2, so no L2 flush is used.
 
 Metric: grid-point updates per second (interior points x steps / device time).
 
@@ -56,7 +57,7 @@ def parse_args():
     p.add_argument("--steps", type=int, default=32)
     p.add_argument("--warmup", type=int, default=8)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--config", choices=["c2", "c1"], default="c2")
+    p.add_argument("--config", choices=["c2", "c1", "c3"], default="c2")
     p.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -174,6 +175,10 @@ def make_models(config, seed, grid=None, sims=3):
     if config == "c1":
         m = inputs.config_c1(seed=seed)
         return [m], "C1: 100x100x60, FP32, 12-cell CFS-PML x5, free surface, Fz Ricker 0.2 Hz, 16 receivers"
+    if config == "c3":
+        ms = inputs.config_c3(seed=seed)
+        return ms, (f"C3: {len(ms)} virtual sources of seeded sizes (horizontal 160-320, depth 80-160 cells), "
+                    "C2 physics, one vertical surface force and 16 receivers each, stepped as one batch")
     if grid:
         ni, nj, nk = (int(v) for v in grid.lower().split("x"))
         base = inputs.make_model(ni, nj, nk, seed=seed, nrecv=64, perturb=0.05, name=f"C2-physics {grid}")
@@ -270,20 +275,18 @@ def run_ours(args, rank, world):
     sims = [inputs.attach(make_solver(m), m) for m in models]
     npts = sum(m.npoints for m in models)
     # per-launch timing of the stage kernel (CUDA events around each launch, eager)
-    stage_ms, end_ms = sims[0].profile_stages(8)
-    for s in sims[1:]:
-        s.run(8)
+    # the simulations step together: each RK stage of all of them is one launch
+    batch = fw.Batch(sims)
+    # per-launch timing of the stage kernel (CUDA events around each launch, eager)
+    stage_ms, end_ms = batch.profile_stages(8)
     warm = max(args.warmup, 3)
-    for s in sims:
-        s.run(warm)
+    batch.run(warm)
     clocks = Clocks(dev)
     dist.barrier()
     clocks.start()
     t_host = time.perf_counter()
-    dev_ms = 0.0
-    for s in sims:
-        s.run(args.steps)  # whole 8-step blocks replay a CUDA graph; returns after device completion
-        dev_ms += s.last_run_ms()
+    batch.run(args.steps)  # whole 8-step blocks replay a CUDA graph; returns after device completion
+    dev_ms = batch.last_run_ms()
     t_host = time.perf_counter() - t_host
     clk = clocks.stop()
     finite = True
@@ -296,9 +299,10 @@ def run_ours(args, rank, world):
     dev_ms = dist.max(dev_ms)
     value = world * npts * args.steps / (dev_ms * 1e-3) / 1e9
 
-    # roofline of the stage kernel
+    # roofline of the stage kernel: one launch covers one stage of every simulation
     m0 = models[0]
-    algo_bytes_step = bytes_pt_step(args.storage) * int(m0.npoints) + BYTES_PML_PT_STEP * slab_points(m0)
+    algo_bytes_step = sum(bytes_pt_step(args.storage) * int(m.npoints) + BYTES_PML_PT_STEP * slab_points(m)
+                          for m in models)
     launch_ms = float(np.mean(stage_ms))
     achieved = algo_bytes_step / 4.0 / (launch_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
@@ -318,8 +322,20 @@ def run_ours(args, rank, world):
                    "storage": args.storage, "fields_finite_after_run": finite,
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
         "host_wall_s": t_host, "roofline": roof, "clocks": clk,
-        "gpu_launches": args.steps * len(sims) * 5,
+        # per step: four batched stage launches per group of up to 18 simulations, and the
+        # step-end (receivers + step counter) kernel of every simulation
+        "gpu_launches": args.steps * (4 * ((len(sims) + 17) // 18) + len(sims)),
     }
+    if args.config == "c3":
+        # the same simulations launched one at a time (one simulation per stage launch)
+        single_ms = 0.0
+        for s in sims:
+            s.run(8)
+            s.run(args.steps)
+            single_ms += s.last_run_ms()
+        out["config"]["single_launch_value"] = npts * args.steps / (single_ms * 1e-3) / 1e9
+        out["config"]["single_launch_ms_per_step"] = single_ms / args.steps
+    batch.close()
     for s in sims:
         s.close()
 
@@ -328,14 +344,20 @@ def run_ours(args, rank, world):
         # run, read the seismograms back; host wall clock.
         t0 = time.perf_counter()
         h2d = d2h = 0
+        esims = []
         for m in models:
             s = make_solver(m)
             inputs.attach(s, m)
-            s.run(args.steps)
-            sg = s.get_seismo()
-            s.close()
+            esims.append(s)
             h2d += 3 * m.lam.nbytes + m.x.nbytes + m.y.nbytes + m.z.nbytes
+        eb = fw.Batch(esims)
+        eb.run(args.steps)
+        for s in esims:
+            sg = s.get_seismo()
             d2h += sg.nbytes
+        eb.close()
+        for s in esims:
+            s.close()
         t_e2e = dist.max(time.perf_counter() - t0)
         out["e2e"] = {"value": world * npts * args.steps / t_e2e / 1e9, "unit": "GPts/s",
                       "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps,

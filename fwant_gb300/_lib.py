@@ -70,6 +70,15 @@ EXPORTS = [
                                       C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                       C.POINTER(C.c_double)]),
     ("fwant_sgtker_last_scatter_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
+    ("fwant_set_planes_per_cta", C.c_int, [_vp, C.c_int]),
+    ("fwant_get_planes_per_cta", C.c_int, [_vp, _ip]),
+    ("fwant_batch_create", C.c_int, [C.POINTER(_vp), C.c_int, C.POINTER(_vp)]),
+    ("fwant_batch_destroy", None, [_vp]),
+    ("fwant_batch_last_error", C.c_char_p, [_vp]),
+    ("fwant_batch_set_ctas", C.c_int, [_vp, C.c_int]),
+    ("fwant_batch_run", C.c_int, [_vp, C.c_int]),
+    ("fwant_batch_last_run_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
+    ("fwant_batch_profile_stages", C.c_int, [_vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("fwant_set_storage_scale", C.c_int, [_vp, C.c_float, C.c_float]),
     ("fwant_max_abs", C.c_int, [_vp, _fp]),
     ("fwant_check", C.c_int, [_vp]),
@@ -319,6 +328,16 @@ class Solver:
         n = nf.value
         return out[: 6 * n * npts].reshape(6, n, npts)
 
+    @property
+    def planes_per_cta(self):
+        v = C.c_int()
+        self._chk(self._lib.fwant_get_planes_per_cta(self._h, C.byref(v)))
+        return v.value
+
+    @planes_per_cta.setter
+    def planes_per_cta(self, planes):
+        self._chk(self._lib.fwant_set_planes_per_cta(self._h, int(planes)))
+
     def set_storage_scale(self, velocity_scale, stress_scale):
         """Power-of-two scales of 2-byte storage (stored value = physical value * scale)."""
         self._chk(self._lib.fwant_set_storage_scale(self._h, float(velocity_scale), float(stress_scale)))
@@ -332,6 +351,53 @@ class Solver:
     def check(self):
         """macdrp_check: raises FwantError(NUMERIC_OVERFLOW) on NaN/Inf/huge."""
         self._chk(self._lib.fwant_check(self._h))
+
+
+class Batch:
+    """Solvers stepped together: one launch per RK stage for up to 18 members."""
+
+    def __init__(self, solvers):
+        self._lib = load_library()
+        self.solvers = list(solvers)
+        arr = (_vp * len(self.solvers))(*[s._h.value for s in self.solvers])
+        h = C.c_void_p()
+        rc = self._lib.fwant_batch_create(arr, len(self.solvers), C.byref(h))
+        if rc != 0:
+            raise FwantError(rc, "fwant_batch_create failed")
+        self._h = h
+
+    def _chk(self, rc):
+        if rc != 0:
+            raise FwantError(rc, self._lib.fwant_batch_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.fwant_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_ctas(self, ctas):
+        self._chk(self._lib.fwant_batch_set_ctas(self._h, int(ctas)))
+
+    def run(self, nsteps):
+        self._chk(self._lib.fwant_batch_run(self._h, int(nsteps)))
+
+    def last_run_ms(self):
+        ms = C.c_double()
+        self._chk(self._lib.fwant_batch_last_run_ms(self._h, C.byref(ms)))
+        return ms.value
+
+    def profile_stages(self, nsteps):
+        """(average ms of each of the four stage launches, ms of the step-end kernels)."""
+        st = (C.c_double * 4)()
+        other = C.c_double()
+        self._chk(self._lib.fwant_batch_profile_stages(self._h, int(nsteps), st, C.byref(other)))
+        return list(st), other.value
 
 
 class SgtKernel:

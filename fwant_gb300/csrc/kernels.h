@@ -118,12 +118,26 @@ struct StageArgs {
   Sources src;
 };
 
+// Batched launch: one stage of up to BATCH_PER_LAUNCH simulations in one grid, their
+// arguments (tensor maps included) held in the kernel's parameter space (the 32 KB
+// parameter limit bounds the count); larger batches use one launch per group.
+constexpr int MAX_BATCH = 64;
+constexpr int BATCH_PER_LAUNCH = 18;
+struct BatchArgs {
+  StageArgs sims[BATCH_PER_LAUNCH];
+  int nsims, total;                  // simulations, work items
+  int off[BATCH_PER_LAUNCH + 1];     // first work item of each simulation
+  int tiles_x[BATCH_PER_LAUNCH], tiles_y[BATCH_PER_LAUNCH];
+};
+static_assert(sizeof(BatchArgs) <= 32764, "kernel parameter space");
+
 // Stage launchers (stage_*.cu).  variant bit 2 = x, bit 1 = y, bit 0 = z; 1 = forward
 // operator.  rk: 0 = RK_beg, 1 = RK_inn, 2 = RK_fin.  exact = 1 selects the reference's
 // operand order with IEEE division and no FMA (bit-reproducible against FP32 CPU runs
 // of the same expressions); 0 the fast form (FMA, reciprocals).
 // storage: ST_F32 / ST_BF16 / ST_F16 (the exact form exists for ST_F32 only).
 int launch_stage(const StageArgs& a, int variant, int rk, int exact, int storage, void* stream);
+int launch_stage_batch(const BatchArgs& b, int variant, int rk, int exact, int storage, int ctas, void* stream);
 int stage_planes_per_cta(const Geom& g, int sm_count);
 int stage_configure();  // set the dynamic shared-memory attribute of every instantiation
 

@@ -594,43 +594,87 @@ struct fwant_solver {
   // Register-set roles: A holds W at the step start (and is the RK "m" register), T is
   // the RK "t" accumulator; B and C are the stage outputs.  Stage 4 writes W(n+1) into
   // T in place, after which A and T swap roles.
-  int enqueue_step(cudaEvent_t* ev = nullptr) {
-    const int X = CYCLE[cycle_pos & 7];
+  // Arguments of stage s (0..3) of a step that starts with W in register set ra (the
+  // other of sets 0 and 3 is the accumulator T).
+  fw::StageArgs stage_args(int s, int ra) const {
+    const int rt = 3 - ra;
     fw::StageArgs a = base_args();
-    const int in_of[4] = {rA, rB, rC, rB};
-    const int out_of[4] = {rB, rC, rB, rT};
-    int lerr = 0;
-    for (int s = 0; s < 4; ++s) {
-      a.win = set(in_of[s]); a.wout = set(out_of[s]); a.wt = set(rT);
-      a.tm_tile = tm_tile[in_of[s]]; a.tm_q = tm_q[in_of[s]]; a.tm_m = tm_pt[rA]; a.tm_t = tm_pt[rT];
-      for (int f = 0; f < 6; ++f) {
-        if (!slab[f].on) continue;
-        a.ain[f] = aset(f, in_of[s]); a.am[f] = aset(f, rA); a.aout[f] = aset(f, out_of[s]); a.at[f] = aset(f, rT);
-      }
-      a.a = RKA[s] * stept;
-      a.b = RKB[s] * stept;
-      a.stage = s;
-      const int v = (s % 2 == 0) ? X : (~X & 7);
-      const int rk = s == 0 ? 0 : (s == 3 ? 2 : 1);
-      if (ev) cudaEventRecord(ev[s], st);
-      const int le = fw::launch_stage(a, v, rk, cfg.exact_arith, stor, st);
-      if (le && !lerr) lerr = le;
+    const int in_of[4] = {ra, rB, rC, rB};
+    const int out_of[4] = {rB, rC, rB, rt};
+    a.win = set(in_of[s]); a.wout = set(out_of[s]); a.wt = set(rt);
+    a.tm_tile = tm_tile[in_of[s]]; a.tm_q = tm_q[in_of[s]]; a.tm_m = tm_pt[ra]; a.tm_t = tm_pt[rt];
+    for (int f = 0; f < 6; ++f) {
+      if (!slab[f].on) continue;
+      a.ain[f] = aset(f, in_of[s]); a.am[f] = aset(f, ra); a.aout[f] = aset(f, out_of[s]); a.at[f] = aset(f, rt);
     }
-    if (ev) cudaEventRecord(ev[4], st);
+    a.a = RKA[s] * stept;
+    a.b = RKB[s] * stept;
+    a.stage = s;
+    return a;
+  }
+  static int stage_variant(int cpos, int s) {
+    const int X = CYCLE[cpos & 7];
+    return (s % 2 == 0) ? X : (~X & 7);
+  }
+  static int stage_rk(int s) { return s == 0 ? 0 : (s == 3 ? 2 : 1); }
+
+  // Step-end work of one simulation: receivers, step counter, SGT frame.
+  fw::RecvArgs recv_args(int rt) const {
     fw::RecvArgs r{};
-    r.g = g; r.w = set(rT); r.npt = npt; r.idx = d_rec; r.tinv = tinv; r.seismo = d_seis; r.cap = cap;
+    r.g = g; r.w = set(rt); r.npt = npt; r.idx = d_rec; r.tinv = tinv; r.seismo = d_seis; r.cap = cap;
     r.storage = stor; r.isv = 1.0f / sv; r.ist = 1.0f / sc_t;
     r.ntime = d_ntime;
-    fw::launch_advance_record(r, st);
-    if (sgt_on) {
-      fw::SgtRecArgs q = sgt;
-      q.w = set(rT);
-      fw::launch_record_sgt(q, st);
+    return r;
+  }
+  fw::SgtRecArgs sgt_args(int rt) const {
+    fw::SgtRecArgs q = sgt;
+    q.w = set(rt);
+    return q;
+  }
+  void enqueue_step_end(cudaStream_t stream) const {
+    fw::launch_advance_record(recv_args(rT), stream);
+    if (sgt_on) fw::launch_record_sgt(sgt_args(rT), stream);
+  }
+  // Bytes of every launch argument of a step for both register-role assignments: equal
+  // signatures mean a captured graph of this simulation's launches is still valid.
+  void append_signature(std::vector<unsigned char>& sig) const {
+    auto put = [&](const void* p, size_t n) {
+      const auto* c = static_cast<const unsigned char*>(p);
+      sig.insert(sig.end(), c, c + n);
+    };
+    for (int ra : {0, 3}) {
+      for (int s = 0; s < 4; ++s) {
+        const fw::StageArgs a = stage_args(s, ra);
+        put(&a, sizeof(a));
+      }
+      const fw::RecvArgs r = recv_args(3 - ra);
+      put(&r, sizeof(r));
+      if (sgt_on) {
+        const fw::SgtRecArgs q = sgt_args(3 - ra);
+        put(&q, sizeof(q));
+      }
     }
-    if (ev) cudaEventRecord(ev[5], st);
+    put(&kc, sizeof(kc));
+  }
+  void finish_step_host() {
     std::swap(rA, rT);
     cycle_pos = (cycle_pos + 1) & 7;
     ntime += 1;
+  }
+
+  // One time step: four fused stage launches and the step-end kernels.
+  int enqueue_step(cudaEvent_t* ev = nullptr) {
+    int lerr = 0;
+    for (int s = 0; s < 4; ++s) {
+      const fw::StageArgs a = stage_args(s, rA);
+      if (ev) cudaEventRecord(ev[s], st);
+      const int le = fw::launch_stage(a, stage_variant(cycle_pos, s), stage_rk(s), cfg.exact_arith, stor, st);
+      if (le && !lerr) lerr = le;
+    }
+    if (ev) cudaEventRecord(ev[4], st);
+    enqueue_step_end(st);
+    if (ev) cudaEventRecord(ev[5], st);
+    finish_step_host();
     return lerr;
   }
 
@@ -1178,6 +1222,292 @@ fwant_status fwant_profile_stages(fwant_solver* s, int nsteps, double* stage_ms,
 fwant_status fwant_last_run_ms(fwant_solver* s, double* ms) {
   if (!s || !ms) return FWANT_ERR_INVALID_ARG;
   *ms = s->last_ms;
+  return FWANT_OK;
+}
+
+fwant_status fwant_set_planes_per_cta(fwant_solver* s, int planes) {
+  if (!s || planes < 1 || planes > 4096) return FWANT_ERR_INVALID_ARG;
+  s->kc = planes;
+  s->drop_graphs();
+  return FWANT_OK;
+}
+
+fwant_status fwant_get_planes_per_cta(fwant_solver* s, int* planes) {
+  if (!s || !planes) return FWANT_ERR_INVALID_ARG;
+  *planes = s->kc;
+  return FWANT_OK;
+}
+
+}  // extern "C"
+
+// ---- batches of simulations stepped together -------------------------------------------
+// Each stage of up to BATCH_PER_LAUNCH members runs in one launch (stage_batch_kernel);
+// the members' step-end kernels follow.  Members advance in lockstep, so they share the
+// F/B variant of every stage and the register-role assignment.
+struct fwant_batch {
+  std::vector<fwant_solver*> sims;
+  int device = 0;
+  int ctas = 0;                              // persistent CTAs per launch (0: 2 per SM)
+  int sm_count = 152;
+  cudaStream_t st = nullptr;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  std::vector<unsigned char> graph_sig;      // launch arguments the graphs were captured with
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0.0;
+  std::string err;
+
+  ~fwant_batch() {
+    cudaSetDevice(device);
+    drop_graphs();
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (st) cudaStreamDestroy(st);
+  }
+  fwant_status fail(fwant_status c, const std::string& m) {
+    err = m;
+    return c;
+  }
+  fwant_status cuda_fail(cudaError_t e, const char* where) {
+    err = std::string(where) + ": " + cudaGetErrorString(e);
+    return FWANT_ERR_CUDA;
+  }
+  void drop_graphs() {
+    for (auto& ge : graph)
+      if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
+  }
+  int n() const { return int(sims.size()); }
+
+  // Arguments of stage s for members [first, first+count) (count <= BATCH_PER_LAUNCH).
+  void batch_args(fw::BatchArgs& b, int first, int count, int ra, int s) const {
+    b.nsims = count;
+    int off = 0;
+    for (int q = 0; q < count; ++q) {
+      const fwant_solver* m = sims[first + q];
+      const fw::Geom& g = m->g;
+      const int tx = (g.ni + fw::STAGE_TX - 1) / fw::STAGE_TX, ty = (g.nj + fw::STAGE_TY - 1) / fw::STAGE_TY;
+      const int tz = (g.nk + m->kc - 1) / m->kc;
+      b.sims[q] = m->stage_args(s, ra);
+      b.off[q] = off;
+      b.tiles_x[q] = tx;
+      b.tiles_y[q] = ty;
+      off += tx * ty * tz;
+    }
+    b.off[count] = off;
+    b.total = off;
+  }
+
+  // ev (optional, 6 events): recorded before each stage, after the stages and after the
+  // step-end kernels.
+  int enqueue_step(cudaEvent_t* ev = nullptr) {
+    fwant_solver* s0 = sims[0];
+    int lerr = 0;
+    static thread_local fw::BatchArgs b;  // 30 KB: kept off the stack
+    for (int s = 0; s < 4; ++s) {
+      if (ev) cudaEventRecord(ev[s], st);
+      for (int first = 0; first < n(); first += fw::BATCH_PER_LAUNCH) {
+        const int count = std::min(fw::BATCH_PER_LAUNCH, n() - first);
+        batch_args(b, first, count, s0->rA, s);
+        const int nct = ctas > 0 ? std::min(b.total, ctas) : b.total;
+        const int le = fw::launch_stage_batch(b, fwant_solver::stage_variant(s0->cycle_pos, s),
+                                              fwant_solver::stage_rk(s), s0->cfg.exact_arith, s0->stor,
+                                              std::max(1, nct), st);
+        if (le && !lerr) lerr = le;
+      }
+    }
+    if (ev) cudaEventRecord(ev[4], st);
+    for (fwant_solver* m : sims) m->enqueue_step_end(st);
+    if (ev) cudaEventRecord(ev[5], st);
+    for (fwant_solver* m : sims) m->finish_step_host();
+    return lerr;
+  }
+
+  fwant_status prepare(int nsteps) {
+    fwant_solver* s0 = sims[0];
+    for (fwant_solver* m : sims) {
+      if (m->ntime != s0->ntime || m->cycle_pos != s0->cycle_pos || m->rA != s0->rA)
+        return fail(FWANT_ERR_STATE, "batch members must be at the same time step");
+      if (!m->have_coord || !m->have_metric || !m->have_media)
+        return fail(FWANT_ERR_STATE, "coordinates, metric and media must be set for every member");
+      fwant_status rc = m->prepare_sources(m->ntime + nsteps);
+      if (rc == FWANT_OK) rc = m->prepare_receivers(m->ntime + nsteps);
+      if (rc != FWANT_OK) return fail(rc, "member: " + m->err);
+    }
+    return FWANT_OK;
+  }
+  fwant_status finish() {
+    for (fwant_solver* m : sims) {
+      fwant_status rc = m->check_device_error();
+      if (rc != FWANT_OK) return fail(rc, "member: " + m->err);
+      if (m->npt > 0) m->nsamp = std::max(m->nsamp, std::min(m->ntime / m->tinv, m->cap));
+    }
+    return FWANT_OK;
+  }
+
+  // Eager steps with events around every stage: average device time per stage launch
+  // group and of the step-end kernels.
+  fwant_status profile(int nsteps, double* stage_ms, double* other_ms) {
+    if (nsteps <= 0) return fail(FWANT_ERR_INVALID_ARG, "nsteps <= 0");
+    cudaSetDevice(device);
+    fwant_status rc = prepare(nsteps);
+    if (rc != FWANT_OK) return rc;
+    std::vector<cudaEvent_t> ev(size_t(6) * nsteps);
+    for (auto& x : ev) cudaEventCreate(&x);
+    int lerr = 0;
+    for (int q = 0; q < nsteps; ++q) lerr |= enqueue_step(&ev[size_t(6) * q]);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    double acc[5] = {0, 0, 0, 0, 0};
+    if (e == cudaSuccess)
+      for (int q = 0; q < nsteps; ++q)
+        for (int k = 0; k < 5; ++k) {
+          float ms = 0.0f;
+          cudaEventElapsedTime(&ms, ev[size_t(6) * q + k], ev[size_t(6) * q + k + 1]);
+          acc[k] += ms;
+        }
+    for (auto& x : ev) cudaEventDestroy(x);
+    if (e == cudaSuccess && lerr) e = cudaError_t(lerr);
+    if (e != cudaSuccess) return cuda_fail(e, "batch profile");
+    if ((rc = finish()) != FWANT_OK) return rc;
+    for (int k = 0; k < 4; ++k) stage_ms[k] = acc[k] / nsteps;
+    *other_ms = acc[4] / nsteps;
+    return FWANT_OK;
+  }
+
+  // Capture the graph of an 8-step block that starts with W in register set ra.
+  fwant_status capture(int gi) {
+    std::vector<int> save_nt, save_ra, save_cp;
+    for (fwant_solver* m : sims) {
+      save_nt.push_back(m->ntime); save_ra.push_back(m->rA); save_cp.push_back(m->cycle_pos);
+      m->rA = gi == 0 ? 0 : 3; m->rT = 3 - m->rA; m->cycle_pos = 0;
+    }
+    cudaGraph_t gr;
+    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    int lerr = 0;
+    if (e == cudaSuccess) {
+      for (int q = 0; q < 8; ++q) lerr |= enqueue_step();
+      e = cudaStreamEndCapture(st, &gr);
+    }
+    if (e == cudaSuccess && lerr) e = cudaError_t(lerr);
+    for (int q = 0; q < n(); ++q) {
+      sims[q]->ntime = save_nt[q]; sims[q]->rA = save_ra[q]; sims[q]->rT = 3 - save_ra[q];
+      sims[q]->cycle_pos = save_cp[q];
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "graph capture");
+    e = cudaGraphInstantiate(&graph[gi], gr, 0);
+    cudaGraphDestroy(gr);
+    if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
+    return FWANT_OK;
+  }
+
+  fwant_status run(int nsteps) {
+    if (nsteps < 0) return fail(FWANT_ERR_INVALID_ARG, "nsteps < 0");
+    cudaSetDevice(device);
+    fwant_solver* s0 = sims[0];
+    fwant_status rc = prepare(nsteps);
+    if (rc != FWANT_OK) return rc;
+    // graphs hold the launch arguments: keep them only while those are unchanged (source
+    // tables and receiver buffers may have been reallocated above)
+    std::vector<unsigned char> sig;
+    for (const fwant_solver* m : sims) m->append_signature(sig);
+    sig.insert(sig.end(), reinterpret_cast<const unsigned char*>(&ctas),
+               reinterpret_cast<const unsigned char*>(&ctas) + sizeof(ctas));
+    if (sig != graph_sig) {
+      drop_graphs();
+      graph_sig = sig;
+    }
+    // the graph that the 8-step blocks of this call will use, built before timing starts
+    const int pre = (8 - s0->cycle_pos) & 7;
+    if (nsteps - pre >= 8) {
+      const int gi = ((s0->rA == 0 ? 0 : 1) ^ (pre & 1));
+      if (!graph[gi] && (rc = capture(gi)) != FWANT_OK) return rc;
+    }
+    cudaError_t e = cudaSuccess;
+    cudaEventRecord(ev0, st);
+    int left = nsteps;
+    while (left > 0) {
+      if (s0->cycle_pos == 0 && left >= 8) {
+        const int gi = s0->rA == 0 ? 0 : 1;
+        if (!graph[gi] && (rc = capture(gi)) != FWANT_OK) return rc;
+        e = cudaGraphLaunch(graph[gi], st);
+        if (e != cudaSuccess) return cuda_fail(e, "graph launch");
+        for (int q = 0; q < 8; ++q)
+          for (fwant_solver* m : sims) m->finish_step_host();
+        left -= 8;
+      } else {
+        const int le = enqueue_step();
+        if (le) return cuda_fail(cudaError_t(le), "batch stage launch");
+        left -= 1;
+      }
+    }
+    cudaEventRecord(ev1, st);
+    e = cudaEventSynchronize(ev1);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "batch run");
+    if ((rc = finish()) != FWANT_OK) return rc;
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    last_ms = ms;
+    return FWANT_OK;
+  }
+};
+
+extern "C" {
+
+fwant_status fwant_batch_create(fwant_solver* const* sims, int n, fwant_batch** out) {
+  if (!out) return FWANT_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (!sims || n < 1 || n > fw::MAX_BATCH) return FWANT_ERR_INVALID_ARG;
+  for (int q = 0; q < n; ++q) {
+    if (!sims[q]) return FWANT_ERR_INVALID_ARG;
+    for (int r = 0; r < q; ++r)
+      if (sims[r] == sims[q]) return FWANT_ERR_INVALID_ARG;
+    if (sims[q]->cfg.device != sims[0]->cfg.device || sims[q]->stor != sims[0]->stor ||
+        sims[q]->cfg.exact_arith != sims[0]->cfg.exact_arith)
+      return FWANT_ERR_INVALID_ARG;
+  }
+  auto* b = new fwant_batch();
+  b->sims.assign(sims, sims + n);
+  b->device = sims[0]->cfg.device;
+  cudaError_t e = cudaSetDevice(b->device);
+  int nsm = 0;
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, b->device);
+  if (nsm > 0) b->sm_count = nsm;
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    delete b;
+    return FWANT_ERR_CUDA;
+  }
+  *out = b;
+  return FWANT_OK;
+}
+
+void fwant_batch_destroy(fwant_batch* b) { delete b; }
+
+const char* fwant_batch_last_error(fwant_batch* b) { return b ? b->err.c_str() : "null handle"; }
+
+fwant_status fwant_batch_set_ctas(fwant_batch* b, int ctas) {
+  if (!b || ctas < 0) return FWANT_ERR_INVALID_ARG;
+  b->ctas = ctas;
+  b->drop_graphs();
+  return FWANT_OK;
+}
+
+fwant_status fwant_batch_run(fwant_batch* b, int nsteps) {
+  if (!b) return FWANT_ERR_INVALID_ARG;
+  return b->run(nsteps);
+}
+
+fwant_status fwant_batch_profile_stages(fwant_batch* b, int nsteps, double* stage_ms, double* other_ms) {
+  if (!b || !stage_ms || !other_ms) return FWANT_ERR_INVALID_ARG;
+  return b->profile(nsteps, stage_ms, other_ms);
+}
+
+fwant_status fwant_batch_last_run_ms(fwant_batch* b, double* ms) {
+  if (!b || !ms) return FWANT_ERR_INVALID_ARG;
+  *ms = b->last_ms;
   return FWANT_OK;
 }
 

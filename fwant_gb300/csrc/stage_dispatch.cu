@@ -5,12 +5,15 @@
 
 namespace fw {
 
-#define FW_DECL(mode)                                                 \
-  int launch_stage_##mode##_rk0(const StageArgs&, int, cudaStream_t); \
-  int launch_stage_##mode##_rk1(const StageArgs&, int, cudaStream_t); \
-  int launch_stage_##mode##_rk2(const StageArgs&, int, cudaStream_t); \
-  int configure_stage_##mode##_rk0();                                 \
-  int configure_stage_##mode##_rk1();                                 \
+#define FW_DECL(mode)                                                            \
+  int launch_stage_##mode##_rk0(const StageArgs&, int, cudaStream_t);            \
+  int launch_stage_##mode##_rk1(const StageArgs&, int, cudaStream_t);            \
+  int launch_stage_##mode##_rk2(const StageArgs&, int, cudaStream_t);            \
+  int launch_stage_batch_##mode##_rk0(const BatchArgs&, int, int, cudaStream_t); \
+  int launch_stage_batch_##mode##_rk1(const BatchArgs&, int, int, cudaStream_t); \
+  int launch_stage_batch_##mode##_rk2(const BatchArgs&, int, int, cudaStream_t); \
+  int configure_stage_##mode##_rk0();                                            \
+  int configure_stage_##mode##_rk1();                                            \
   int configure_stage_##mode##_rk2();
 FW_DECL(fast)
 FW_DECL(exact)
@@ -24,6 +27,19 @@ int launch_stage(const StageArgs& a, int variant, int rk, int exact, int storage
   return rk == 0 ? launch_stage_##mode##_rk0(a, variant, st)           \
                  : (rk == 1 ? launch_stage_##mode##_rk1(a, variant, st) \
                             : launch_stage_##mode##_rk2(a, variant, st));
+  if (storage == ST_BF16) { FW_RK(bf16) }
+  if (storage == ST_F16) { FW_RK(fp16) }
+  if (exact) { FW_RK(exact) }
+  FW_RK(fast)
+#undef FW_RK
+}
+
+int launch_stage_batch(const BatchArgs& b, int variant, int rk, int exact, int storage, int ctas, void* stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+#define FW_RK(mode)                                                                  \
+  return rk == 0 ? launch_stage_batch_##mode##_rk0(b, variant, ctas, st)             \
+                 : (rk == 1 ? launch_stage_batch_##mode##_rk1(b, variant, ctas, st)  \
+                            : launch_stage_batch_##mode##_rk2(b, variant, ctas, st));
   if (storage == ST_BF16) { FW_RK(bf16) }
   if (storage == ST_F16) { FW_RK(fp16) }
   if (exact) { FW_RK(exact) }

@@ -6,5 +6,8 @@ namespace fw {
 int launch_stage_exact_rk1(const StageArgs& a, int variant, cudaStream_t st) {
   return launch_rk_variant<float, true, 1>(a, variant, st);
 }
+int launch_stage_batch_exact_rk1(const BatchArgs& b, int variant, int ctas, cudaStream_t st) {
+  return launch_batch_rk_variant<float, true, 1>(b, variant, ctas, st);
+}
 int configure_stage_exact_rk1() { return configure_rk<float, true, 1>(); }
 }  // namespace fw

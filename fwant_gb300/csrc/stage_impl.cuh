@@ -103,6 +103,9 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     if (mbar_try(bar, parity)) return true;
   return false;
 }
+__device__ __forceinline__ void mbar_inval(uint32_t bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
+}
 __device__ __forceinline__ void fence_barrier_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
@@ -224,21 +227,24 @@ __device__ __forceinline__ float surf_val(const Sources& S, const float* tab, in
   return v;
 }
 
+// One CTA's work: columns [bx*TX, +TX) x [by*TY, +TY) of the interior, planes
+// [bz*kc, +kc).  Returns false when a bounded wait gave up (error word set).  The
+// mbarriers are initialised on entry and invalidated on a normal exit, so a persistent
+// CTA can run several work items in turn.
 template <class S, bool EXACT, int FX, int FY, int FZ, int RK>
-__global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant__ StageArgs A) {
+__device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, int bz, unsigned char* smem) {
   static_assert(!EXACT || is_f32_v<S>, "the reference-order form exists for FP32 storage only");
   using L = Lay<S>;
   constexpr int TBX = L::TBX, HX = L::HX;
   constexpr int BUF_BYTES = L::BUF_BYTES, OFF_Q = L::OFF_Q, OFF_MED = L::OFF_MED, OFF_M = L::OFF_M,
                 OFF_T = L::OFF_T;
-  extern __shared__ __align__(1024) unsigned char smem[];
   const Geom& g = A.g;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
-  const int i0 = g.i1 + blockIdx.x * TX, j0 = g.j1 + blockIdx.y * TY;
+  const int i0 = g.i1 + bx * TX, j0 = g.j1 + by * TY;
   const int i = i0 + tx, j = j0 + ty;
   const bool act = i <= g.i2 && j <= g.j2;  // interior point owned by this thread
-  const int kb = g.k1 + blockIdx.z * A.kc;
-  if (kb > g.k2) return;
+  const int kb = g.k1 + bz * A.kc;
+  if (kb > g.k2) return true;
   const int ke = min(kb + A.kc - 1, g.k2);
   const int px = g.px, plane = int(g.plane);
   const long long fs = g.fstride;
@@ -671,14 +677,49 @@ __global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant_
         atomicExch(A.err, DEVERR_TMA_TIMEOUT);
         if (k < ke) mbar_wait(bar0 + 8 * (cur ^ 1), ((it + 1) >> 1) & 1);  // copy still in flight
       }
-      return;
+      return false;
     }
+  }
+  // every issued copy has been waited for (the last plane issues none)
+  if (tid == 0) {
+    mbar_inval(bar0);
+    mbar_inval(bar0 + 8);
+  }
+  return true;
+}
+
+template <class S, bool EXACT, int FX, int FY, int FZ, int RK>
+__global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant__ StageArgs A) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  stage_body<S, EXACT, FX, FY, FZ, RK>(A, blockIdx.x, blockIdx.y, blockIdx.z, smem);
+}
+
+// Launch over a batch of simulations: the work items (tiles x k-chunks) of all
+// simulations are numbered simulation after simulation, x fastest, and CTA b runs items
+// b, b + gridDim.x, ... (one item each when the grid covers them all).
+template <class S, bool EXACT, int FX, int FY, int FZ, int RK>
+__global__ void __launch_bounds__(TX* TY, 2) stage_batch_kernel(const __grid_constant__ BatchArgs B) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  for (int item = blockIdx.x; item < B.total; item += gridDim.x) {
+    int s = 0;
+    while (item >= B.off[s + 1]) ++s;
+    const int local = item - B.off[s];
+    const int bx = local % B.tiles_x[s], r = local / B.tiles_x[s];
+    const int by = r % B.tiles_y[s], bz = r / B.tiles_y[s];
+    if (!stage_body<S, EXACT, FX, FY, FZ, RK>(B.sims[s], bx, by, bz, smem)) return;
+    __syncthreads();  // the next item re-initialises the barriers and reuses the buffers
   }
 }
 
 template <class S, bool EXACT, int FX, int FY, int FZ, int RK>
 static int launch_one(const StageArgs& a, const dim3& grid, cudaStream_t st) {
   stage_kernel<S, EXACT, FX, FY, FZ, RK><<<grid, dim3(TX, TY, 1), Lay<S>::SMEM_BYTES, st>>>(a);
+  return int(cudaGetLastError());
+}
+
+template <class S, bool EXACT, int FX, int FY, int FZ, int RK>
+static int launch_batch_one(const BatchArgs& b, int ctas, cudaStream_t st) {
+  stage_batch_kernel<S, EXACT, FX, FY, FZ, RK><<<ctas, dim3(TX, TY, 1), Lay<S>::SMEM_BYTES, st>>>(b);
   return int(cudaGetLastError());
 }
 
@@ -691,6 +732,13 @@ static int configure_rk() {
   if (e == cudaSuccess)                                                                                         \
     e = cudaFuncSetAttribute(stage_kernel<S, EXACT, FX, FY, FZ, RK>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                              Lay<S>::SMEM_BYTES);
+  FW_CFG(0, 0, 0) FW_CFG(0, 0, 1) FW_CFG(0, 1, 0) FW_CFG(0, 1, 1)
+  FW_CFG(1, 0, 0) FW_CFG(1, 0, 1) FW_CFG(1, 1, 0) FW_CFG(1, 1, 1)
+#undef FW_CFG
+#define FW_CFG(FX, FY, FZ)                                                                              \
+  if (e == cudaSuccess)                                                                                 \
+    e = cudaFuncSetAttribute(stage_batch_kernel<S, EXACT, FX, FY, FZ, RK>,                              \
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, Lay<S>::SMEM_BYTES);
   FW_CFG(0, 0, 0) FW_CFG(0, 0, 1) FW_CFG(0, 1, 0) FW_CFG(0, 1, 1)
   FW_CFG(1, 0, 0) FW_CFG(1, 0, 1) FW_CFG(1, 1, 0) FW_CFG(1, 1, 1)
 #undef FW_CFG
@@ -709,6 +757,20 @@ static int launch_rk_variant(const StageArgs& a, int variant, cudaStream_t st) {
     case 5: return launch_one<S, EXACT, 1, 0, 1, RK>(a, grid, st);
     case 6: return launch_one<S, EXACT, 1, 1, 0, RK>(a, grid, st);
     default: return launch_one<S, EXACT, 1, 1, 1, RK>(a, grid, st);
+  }
+}
+
+template <class S, bool EXACT, int RK>
+static int launch_batch_rk_variant(const BatchArgs& b, int variant, int ctas, cudaStream_t st) {
+  switch (variant) {
+    case 0: return launch_batch_one<S, EXACT, 0, 0, 0, RK>(b, ctas, st);
+    case 1: return launch_batch_one<S, EXACT, 0, 0, 1, RK>(b, ctas, st);
+    case 2: return launch_batch_one<S, EXACT, 0, 1, 0, RK>(b, ctas, st);
+    case 3: return launch_batch_one<S, EXACT, 0, 1, 1, RK>(b, ctas, st);
+    case 4: return launch_batch_one<S, EXACT, 1, 0, 0, RK>(b, ctas, st);
+    case 5: return launch_batch_one<S, EXACT, 1, 0, 1, RK>(b, ctas, st);
+    case 6: return launch_batch_one<S, EXACT, 1, 1, 0, RK>(b, ctas, st);
+    default: return launch_batch_one<S, EXACT, 1, 1, 1, RK>(b, ctas, st);
   }
 }
 

@@ -249,6 +249,42 @@ def config_c2(seed=0, component=2, **kw) -> Model:
                       name=f"C2 400x400x200 F{'xyz'[component]}", **kw)
 
 
+C4_STATIONS = ((-40, 0), (40, 0))  # (di, dj) of stations A and B from the surface centre, 1 km cells
+
+
+def config_c4(seed=0, station=0, **kw) -> Model:
+    """Config 4 (precision study): 256x256x128 with the C2 physics (+/-5% perturbation),
+    a vertical surface force at station A (station=0) or B (station=1), 80 km apart on the
+    surface; receivers: A, B, then 16 seeded surface receivers.  The two simulations are
+    the source-side and receiver-side strain Green's tensors of the station pair."""
+    m = make_model(256, 256, 128, seed=seed, nrecv=16, perturb=0.05, name=f"C4 256x256x128 station {'AB'[station]}",
+                   **kw)
+    ic, jc = LENFD + m.ni // 2 + 1, LENFD + m.nj // 2 + 1
+    kc = m.nk + LENFD
+    st = [(ic + di, jc + dj, kc) for di, dj in C4_STATIONS]
+    m.force_indx = np.array([st[station]], np.int32)
+    m.recv_indx = np.concatenate([np.array(st, np.int32), m.recv_indx]).astype(np.int32)
+    return m
+
+
+def config_c3(seed=0, count=32, **kw) -> list:
+    """Config 3: `count` virtual sources of seeded uneven sizes (horizontal 160-320 cells,
+    depth 80-160 cells), the C2 physics (+/-5% perturbation), one vertical surface force
+    at a seeded station each, 16 surface receivers."""
+    rng = np.random.default_rng(seed + 104729)
+    out = []
+    for n in range(count):
+        ni, nj = (int(v) for v in rng.integers(160, 321, 2))
+        nk = int(rng.integers(80, 161))
+        m = make_model(ni, nj, nk, seed=seed * 1000 + n, nrecv=16, perturb=0.05,
+                       name=f"C3 #{n} {ni}x{nj}x{nk}", **kw)
+        di = int(rng.integers(-ni // 4, ni // 4 + 1))
+        dj = int(rng.integers(-nj // 4, nj // 4 + 1))
+        m.force_indx = np.array([[LENFD + ni // 2 + 1 + di, LENFD + nj // 2 + 1 + dj, nk + LENFD]], np.int32)
+        out.append(m)
+    return out
+
+
 def attach(solver, m: Model, metric: dict | None = None):
     """Feed a Model to a Solver (or any object with the same set-up methods)."""
     solver.set_coord(m.x, m.y, m.z)

@@ -279,6 +279,35 @@ fwant_status fwant_profile_stages(fwant_solver* s, int nsteps, double* stage_ms,
 /* Device time of the last fwant_run call in milliseconds (CUDA events). */
 fwant_status fwant_last_run_ms(fwant_solver* s, double* ms);
 
+/* Planes along k that one CTA of the stage kernel marches through (default chosen from
+ * the grid size; a tuning knob of the autotuner).  No counterpart in the reference. */
+fwant_status fwant_set_planes_per_cta(fwant_solver* s, int planes);
+fwant_status fwant_get_planes_per_cta(fwant_solver* s, int* planes);
+
+/* ---- Batches: many simulations stepped together ----
+ * No counterpart in the reference, which runs one virtual source per job.  A batch steps
+ * n solvers (same device, storage and arithmetic form; sizes, media, sources and
+ * receivers may all differ) in lockstep: each RK stage of up to 18 members is one launch
+ * whose CTAs walk the work items (tiles x k-chunks) of every member, and whole 8-step
+ * blocks replay a CUDA graph.  Results are those of fwant_run on each member: bit for bit
+ * with exact_arith, to FP32 rounding in the fast form (multiply-add contraction may differ
+ * between the batched and the single-simulation kernels).
+ * Members must be at the same time step when fwant_batch_run is called and must not run
+ * on their own while the batch runs; they stay usable on their own (fwant_get_seismo,
+ * fwant_run, ...) between batch runs.  n <= 64; the batch does not own the solvers. */
+typedef struct fwant_batch fwant_batch;
+fwant_status fwant_batch_create(fwant_solver* const* sims, int n, fwant_batch** out);
+void fwant_batch_destroy(fwant_batch* b);
+const char* fwant_batch_last_error(fwant_batch* b);
+/* CTAs per stage launch: 0 (default) = one CTA per work item; a smaller count makes the
+ * launch persistent, each CTA walking items ctas apart. */
+fwant_status fwant_batch_set_ctas(fwant_batch* b, int ctas);
+fwant_status fwant_batch_run(fwant_batch* b, int nsteps);
+fwant_status fwant_batch_last_run_ms(fwant_batch* b, double* ms);
+/* fwant_profile_stages for a batch: eager steps with events around each stage's launches
+ * (stage_ms[4]: all members' launches of that stage) and the step-end kernels. */
+fwant_status fwant_batch_profile_stages(fwant_batch* b, int nsteps, double* stage_ms, double* other_ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -847,15 +847,16 @@ template <class T> struct Solver {
 
 // The same metric formula evaluated in double from the SP coordinates and rounded
 // once: the FP64 precomputation the GPU path performs.
+template <class O>
 static void metric_dp(int nx, int ny, int nz, const float* x, const float* y, const float* z,
-                      float* xsin, float* xcot, float* xi_x, float* eta_y, float* zeta_z) {
+                      O* xsin, O* xcot, O* xi_x, O* eta_y, O* zeta_z) {
   const double coeF[5] = {-0.30874, -0.6326, 1.2330, -0.3334, 0.04168};
   const double coeB[5] = {-0.04168, 0.3334, -1.2330, 0.6326, 0.30874};
   for (int i = 0; i < nx; ++i) {
-    xsin[i] = float(std::sin(double(x[i])));
-    xcot[i] = float(1.0 / std::tan(double(x[i])));
+    xsin[i] = O(std::sin(double(x[i])));
+    xcot[i] = O(1.0 / std::tan(double(x[i])));
   }
-  auto one = [&](int n, const float* g, float* out) {
+  auto one = [&](int n, const float* g, O* out) {
     const int lo = LenFD, hi = n - 1 - LenFD;
     for (int i = 0; i < n; ++i) {
       const int ii = i < lo ? lo : (i > hi ? hi : i);
@@ -864,7 +865,7 @@ static void metric_dp(int nx, int ny, int nz, const float* x, const float* y, co
         sb += double(g[ii - 3 + q]) * coeB[q];
         sf += double(g[ii - 1 + q]) * coeF[q];
       }
-      out[i] = float(1.0 / ((sb + sf) * 0.5));
+      out[i] = O(1.0 / ((sb + sf) * 0.5));
     }
   };
   one(nx, x, xi_x);
@@ -1113,6 +1114,12 @@ void orc_metric(int nx, int ny, int nz, const float* x, const float* y, const fl
 
 void orc_metric_dp(int nx, int ny, int nz, const float* x, const float* y, const float* z, float* xsin,
                    float* xcot, float* xi_x, float* eta_y, float* zeta_z) {
+  orc::metric_dp(nx, ny, nz, x, y, z, xsin, xcot, xi_x, eta_y, zeta_z);
+}
+
+// The FP64 metric without rounding to FP32 (the metric of the double-precision run).
+void orc_metric_dd(int nx, int ny, int nz, const float* x, const float* y, const float* z, double* xsin,
+                   double* xcot, double* xi_x, double* eta_y, double* zeta_z) {
   orc::metric_dp(nx, ny, nz, x, y, z, xsin, xcot, xi_x, eta_y, zeta_z);
 }
 

@@ -48,6 +48,7 @@ _SIGS = [
     ("orc_metric", None, [C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, _fp, _fp, _fp, _fp, _fp]),
     ("orc_metric_dp", None, [C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, _fp, _fp, _fp, _fp, _fp]),
     ("orc_op", C.c_double, [C.c_int, C.c_int, _dp, C.c_int]),
+    ("orc_metric_dd", None, [C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, _dp, _dp, _dp, _dp, _dp]),
     ("orc_stress2strain", None, [C.c_longlong, C.c_int, _fp, _fp, _fp, _fp]),
     ("orc_sgt2scatter3", None, [C.c_longlong, C.c_int, C.c_int, C.c_int, C.c_double, _fp, _fp, _fp, _fp, _fp, _fp,
                                 C.c_int, _dp]),
@@ -256,10 +257,16 @@ class Oracle:
         return out[: 9 * n * self.num_pt].reshape(9, n, self.num_pt)
 
 
-def metric(x, y, z, dp=False):
+def metric(x, y, z, dp=False, full=False):
     """seis3d_metric restated in SP (seis3d_metric.F90:83-112); dp=True evaluates the same
-    formula in double from the SP coordinates (the FP64 precomputation)."""
+    formula in double from the SP coordinates (the FP64 precomputation); full=True also
+    keeps the double results (the metric of the FP64 run) instead of rounding to FP32."""
     x, y, z = [np.ascontiguousarray(np.asarray(v, np.float32)) for v in (x, y, z)]
+    if full:
+        out = [np.zeros(x.size), np.zeros(x.size), np.zeros(x.size), np.zeros(y.size), np.zeros(z.size)]
+        lib().orc_metric_dd(x.size, y.size, z.size, _p(x, C.c_float), _p(y, C.c_float), _p(z, C.c_float),
+                            *[_p(v) for v in out])
+        return dict(zip(("xsin", "xcot", "xi_x", "eta_y", "zeta_z"), out))
     out = [np.zeros(x.size, np.float32), np.zeros(x.size, np.float32), np.zeros(x.size, np.float32),
            np.zeros(y.size, np.float32), np.zeros(z.size, np.float32)]
     fn = lib().orc_metric_dp if dp else lib().orc_metric
