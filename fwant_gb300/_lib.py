@@ -70,6 +70,8 @@ EXPORTS = [
                                       C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                       C.POINTER(C.c_double)]),
     ("fwant_sgtker_last_scatter_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
+    ("fwant_autotune", C.c_int, [_vp, C.c_int, _ip]),
+    ("fwant_batch_autotune", C.c_int, [_vp, C.c_int, _ip]),
     ("fwant_set_planes_per_cta", C.c_int, [_vp, C.c_int]),
     ("fwant_get_planes_per_cta", C.c_int, [_vp, _ip]),
     ("fwant_batch_create", C.c_int, [C.POINTER(_vp), C.c_int, C.POINTER(_vp)]),
@@ -80,6 +82,17 @@ EXPORTS = [
     ("fwant_batch_last_run_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
     ("fwant_batch_profile_stages", C.c_int, [_vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("fwant_set_storage_scale", C.c_int, [_vp, C.c_float, C.c_float]),
+    # surrogate kernels (include/fwant_surrogate.h): device pointers, a stream, cudaError_t
+    ("fwant_nn_conv3d_fwd", C.c_int, [_vp, _vp, _vp, _vp] + [C.c_int] * 7 + [_vp]),
+    ("fwant_nn_conv3d_bwd", C.c_int, [_vp] * 6 + [C.c_int] * 7 + [_vp]),
+    ("fwant_nn_linear_fwd", C.c_int, [_vp] * 4 + [C.c_int] * 3 + [_vp]),
+    ("fwant_nn_linear_bwd", C.c_int, [_vp] * 6 + [C.c_int] * 3 + [_vp]),
+    ("fwant_nn_lrelu_fwd", C.c_int, [_vp, C.c_longlong, C.c_float, _vp]),
+    ("fwant_nn_lrelu_bwd", C.c_int, [_vp, _vp, C.c_longlong, C.c_float, _vp]),
+    ("fwant_nn_mse", C.c_int, [_vp] * 5 + [C.c_longlong, _vp]),
+    ("fwant_nn_adam", C.c_int, [_vp] * 5 + [C.c_longlong] + [C.c_float] * 5 + [C.c_int, _vp]),
+    ("fwant_nn_to_bf16", C.c_int, [_vp, _vp, C.c_longlong, _vp]),
+    ("fwant_nn_axpby", C.c_int, [_vp, _vp, C.c_float, _vp, C.c_longlong, _vp]),
     ("fwant_max_abs", C.c_int, [_vp, _fp]),
     ("fwant_check", C.c_int, [_vp]),
     ("fwant_profile_stages", C.c_int, [_vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
@@ -328,6 +341,12 @@ class Solver:
         n = nf.value
         return out[: 6 * n * npts].reshape(6, n, npts)
 
+    def autotune(self, trial_steps=4):
+        """Pick the fastest planes-per-CTA (before the first step); returns it."""
+        v = C.c_int()
+        self._chk(self._lib.fwant_autotune(self._h, int(trial_steps), C.byref(v)))
+        return v.value
+
     @property
     def planes_per_cta(self):
         v = C.c_int()
@@ -383,6 +402,12 @@ class Batch:
 
     def set_ctas(self, ctas):
         self._chk(self._lib.fwant_batch_set_ctas(self._h, int(ctas)))
+
+    def autotune(self, trial_steps=4):
+        """Tune every member and the CTA schedule (before the first step); returns ctas."""
+        v = C.c_int()
+        self._chk(self._lib.fwant_batch_autotune(self._h, int(trial_steps), C.byref(v)))
+        return v.value
 
     def run(self, nsteps):
         self._chk(self._lib.fwant_batch_run(self._h, int(nsteps)))

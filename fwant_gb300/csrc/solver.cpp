@@ -8,6 +8,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -765,6 +767,21 @@ struct fwant_solver {
     return FWANT_OK;
   }
 
+  // Back to the state before the first step (zero wavefield, memory variables, records),
+  // keeping the model, sources and receivers.
+  cudaError_t reset_state() {
+    cudaError_t e = cudaMemsetAsync(regs, 0, size_t(4) * fw::NF * g.fstride * esz, st);
+    for (int f = 0; f < 6 && e == cudaSuccess; ++f)
+      if (aux[f]) e = cudaMemsetAsync(aux[f], 0, size_t(4) * aux_set[f] * sizeof(float), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_ntime, 0, sizeof(int), st);
+    if (e == cudaSuccess && d_seis) e = cudaMemsetAsync(d_seis, 0, size_t(fw::NF) * cap * npt * sizeof(float), st);
+    if (e == cudaSuccess && sgt_on)
+      e = cudaMemsetAsync(d_sgt, 0, size_t(6) * sgt.max_frames * sgt.npts * sizeof(float), st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    ntime = 0; cycle_pos = 0; rA = 0; rT = 3; nsamp = 0;
+    return e;
+  }
+
   // Eager steps with CUDA events around every launch: average device time of the four
   // stage launches (index = stage inside the step) and of the step-end kernel.
   fwant_status profile(int nsteps, double* stage_ms, double* other_ms) {
@@ -1225,6 +1242,71 @@ fwant_status fwant_last_run_ms(fwant_solver* s, double* ms) {
   return FWANT_OK;
 }
 
+// ---- autotuning -------------------------------------------------------------------------
+// Candidates are timed with CUDA events on eager steps (fwant_profile_stages) from the
+// initial state, which is restored afterwards; results are cached per process by the
+// shape of the problem.
+namespace {
+struct TuneKey {
+  int ni, nj, nk, storage, exact, device;
+  int pml[6];
+  bool operator<(const TuneKey& o) const { return std::memcmp(this, &o, sizeof(TuneKey)) < 0; }
+};
+std::mutex g_tune_mutex;
+std::map<TuneKey, int> g_tune_cache;
+
+TuneKey tune_key(const fwant_solver* s) {
+  TuneKey k;
+  std::memset(&k, 0, sizeof(k));
+  k.ni = s->cfg.ni; k.nj = s->cfg.nj; k.nk = s->cfg.nk; k.storage = s->stor; k.exact = s->cfg.exact_arith;
+  k.device = s->cfg.device;
+  for (int f = 0; f < 6; ++f) k.pml[f] = s->slab[f].on ? (s->slab[f].i2 - s->slab[f].i1 + 1) * 1000000 +
+                                                          (s->slab[f].j2 - s->slab[f].j1 + 1) * 1000 +
+                                                          (s->slab[f].k2 - s->slab[f].k1 + 1) : 0;
+  return k;
+}
+}  // namespace
+
+fwant_status fwant_autotune(fwant_solver* s, int trial_steps, int* planes_out) {
+  if (!s || trial_steps < 1) return FWANT_ERR_INVALID_ARG;
+  if (s->ntime != 0) return s->fail(FWANT_ERR_STATE, "autotune: call before the first time step");
+  const TuneKey key = tune_key(s);
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      s->kc = it->second;
+      s->drop_graphs();
+      if (planes_out) *planes_out = s->kc;
+      return FWANT_OK;
+    }
+  }
+  const int cand[] = {4, 6, 8, 12, 16, 24, 32, 48, 64, 96, 128};
+  double best = 1e30;
+  int best_kc = s->kc;
+  for (int kc : cand) {
+    if (kc > s->cfg.nk && kc != cand[0]) break;
+    s->kc = kc;
+    s->drop_graphs();
+    double st[4], other;
+    fwant_status rc = s->profile(1, st, &other);  // first touch of this configuration
+    if (rc == FWANT_OK) rc = s->profile(trial_steps, st, &other);
+    cudaError_t e = s->reset_state();
+    if (rc != FWANT_OK) return rc;
+    if (e != cudaSuccess) return s->cuda_fail(e, "autotune reset");
+    const double t = st[0] + st[1] + st[2] + st[3];
+    if (t < best) { best = t; best_kc = kc; }
+  }
+  s->kc = best_kc;
+  s->drop_graphs();
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tune_cache[key] = best_kc;
+  }
+  if (planes_out) *planes_out = best_kc;
+  return FWANT_OK;
+}
+
 fwant_status fwant_set_planes_per_cta(fwant_solver* s, int planes) {
   if (!s || planes < 1 || planes > 4096) return FWANT_ERR_INVALID_ARG;
   s->kc = planes;
@@ -1498,6 +1580,38 @@ fwant_status fwant_batch_set_ctas(fwant_batch* b, int ctas) {
 fwant_status fwant_batch_run(fwant_batch* b, int nsteps) {
   if (!b) return FWANT_ERR_INVALID_ARG;
   return b->run(nsteps);
+}
+
+fwant_status fwant_batch_autotune(fwant_batch* b, int trial_steps, int* ctas_out) {
+  if (!b || trial_steps < 1) return FWANT_ERR_INVALID_ARG;
+  for (fwant_solver* m : b->sims)
+    if (m->ntime != 0) return b->fail(FWANT_ERR_STATE, "batch autotune: call before the first time step");
+  for (fwant_solver* m : b->sims) {
+    fwant_status rc = fwant_autotune(m, trial_steps, nullptr);
+    if (rc != FWANT_OK) return b->fail(rc, "member autotune: " + m->err);
+  }
+  // CTA schedule: one CTA per work item, or persistent grids of 1, 2 and 4 CTAs per SM
+  const int cand[] = {0, b->sm_count, 2 * b->sm_count, 4 * b->sm_count};
+  double best = 1e30;
+  int best_ctas = 0;
+  for (int c : cand) {
+    b->ctas = c;
+    b->drop_graphs();
+    double st[4], other;
+    fwant_status rc = b->profile(1, st, &other);
+    if (rc == FWANT_OK) rc = b->profile(trial_steps, st, &other);
+    cudaError_t e = cudaSuccess;
+    for (fwant_solver* m : b->sims)
+      if (e == cudaSuccess) e = m->reset_state();
+    if (rc != FWANT_OK) return rc;
+    if (e != cudaSuccess) return b->cuda_fail(e, "batch autotune reset");
+    const double t = st[0] + st[1] + st[2] + st[3];
+    if (t < best) { best = t; best_ctas = c; }
+  }
+  b->ctas = best_ctas;
+  b->drop_graphs();
+  if (ctas_out) *ctas_out = best_ctas;
+  return FWANT_OK;
 }
 
 fwant_status fwant_batch_profile_stages(fwant_batch* b, int nsteps, double* stage_ms, double* other_ms) {

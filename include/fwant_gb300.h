@@ -284,6 +284,13 @@ fwant_status fwant_last_run_ms(fwant_solver* s, double* ms);
 fwant_status fwant_set_planes_per_cta(fwant_solver* s, int planes);
 fwant_status fwant_get_planes_per_cta(fwant_solver* s, int* planes);
 
+/* Autotuner: times every planes-per-CTA candidate (4 ... 128, up to nk) over trial_steps
+ * eager steps with CUDA events, keeps the fastest and returns it in *planes (may be NULL).
+ * Call before the first time step: the trial steps run from the initial state, which is
+ * restored afterwards (wavefield, memory variables, receiver and SGT records).  Results
+ * are cached per process by problem shape.  No counterpart in the reference. */
+fwant_status fwant_autotune(fwant_solver* s, int trial_steps, int* planes);
+
 /* ---- Batches: many simulations stepped together ----
  * No counterpart in the reference, which runs one virtual source per job.  A batch steps
  * n solvers (same device, storage and arithmetic form; sizes, media, sources and
@@ -304,6 +311,10 @@ const char* fwant_batch_last_error(fwant_batch* b);
 fwant_status fwant_batch_set_ctas(fwant_batch* b, int ctas);
 fwant_status fwant_batch_run(fwant_batch* b, int nsteps);
 fwant_status fwant_batch_last_run_ms(fwant_batch* b, double* ms);
+/* Autotune every member (fwant_autotune), then the CTA schedule of the batched launch
+ * (one CTA per work item, or persistent grids of 1, 2 or 4 CTAs per SM); the chosen CTA
+ * count (0 = one per work item) goes to *ctas (may be NULL).  Before the first step. */
+fwant_status fwant_batch_autotune(fwant_batch* b, int trial_steps, int* ctas);
 /* fwant_profile_stages for a batch: eager steps with events around each stage's launches
  * (stage_ms[4]: all members' launches of that stage) and the step-end kernels. */
 fwant_status fwant_batch_profile_stages(fwant_batch* b, int nsteps, double* stage_ms, double* other_ms);

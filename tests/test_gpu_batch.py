@@ -101,3 +101,31 @@ def test_batch_rules(oracle_mod, native_lib):
     c = fw.Solver(m.ni, m.nj, m.nk, m.stept, exact_arith=False)
     with pytest.raises(fw.FwantError):
         fw.Batch([b, c])   # different arithmetic form
+
+
+def test_autotune_keeps_results(oracle_mod, native_lib):
+    """Tuning runs trial steps and restores the initial state: a tuned solver then gives
+    the results of an untuned one bit for bit (planes per CTA only move work between
+    CTAs), and a tuned batch those of its members run alone."""
+    import fwant_gb300 as fw
+    pairs = _members(oracle_mod, False)[:3]
+    tuned, plain = pairs[0]
+    kc = tuned.autotune(2)
+    assert kc >= 4 and tuned.ntime == 0 and tuned.planes_per_cta == kc
+    for s in (tuned, plain):
+        s.run(20)
+    for c in range(9):
+        np.testing.assert_array_equal(tuned.get_field(c), plain.get_field(c))
+    np.testing.assert_array_equal(tuned.get_seismo(), plain.get_seismo())
+    members = [p[0] for p in pairs[1:]]
+    alone = [p[1] for p in pairs[1:]]
+    b = fw.Batch(members)
+    ctas = b.autotune(2)
+    assert ctas >= 0 and all(m.ntime == 0 for m in members)
+    b.run(12)
+    for m, a in zip(members, alone):
+        a.run(12)
+        assert rel_l2(m.get_field("Vz"), a.get_field("Vz")) < 1e-6
+    with pytest.raises(fw.FwantError) as e:
+        tuned.autotune(2)   # after the first step
+    assert e.value.code == 6
