@@ -57,7 +57,8 @@ def parse_args():
     p.add_argument("--steps", type=int, default=32)
     p.add_argument("--warmup", type=int, default=8)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--config", choices=["c2", "c1", "c3"], default="c2")
+    p.add_argument("--config", choices=["c2", "c1", "c3", "c5"], default="c2",
+                   help="c5: train the waveform surrogate on 512 FD solves and screen 64 held-out models")
     p.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -256,9 +257,34 @@ def run_reference(args, rank, world):
     return 0
 
 
+def run_surrogate(args, rank):
+    """Config 5: the surrogate's screening speedup over FD solves at 1% waveform error."""
+    from fwant_gb300 import surrogate
+    if rank != 0:
+        return 0
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    t0 = time.perf_counter()
+    r = surrogate.run_c5(device=dev)
+    wall = time.perf_counter() - t0
+    out = {
+        "metric": "surrogate screening speedup over FD solves at 1% waveform error", "value": r["speedup"],
+        "unit": "x", "n_gpus": 1, "steps": r["n_test"], "warmup": 0, "higher_is_better": True,
+        "scaling": "replicas only", "vs_baseline": None, "dtype": "bf16 weights, f32 accumulation",
+        "data": "synthetic (seeded)",
+        "config": {"workload": f"C5: {r['n_train'] + r['n_val']} FD solves at {r['grid']} with +/-5% Vs "
+                               f"perturbations ({r['corr_km']} km correlation) train an ensemble of {r['ensemble']} "
+                               f"networks; {r['n_test']} held-out models screened"},
+        "surrogate": r, "wall_s": wall,
+    }
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_ours(args, rank, world):
     import fwant_gb300 as fw
     from fwant_gb300 import inputs
+    if args.config == "c5":
+        return run_surrogate(args, rank)
     dist = Dist(world)
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     fw.load_library()

@@ -93,6 +93,8 @@ EXPORTS = [
     ("fwant_nn_adam", C.c_int, [_vp] * 5 + [C.c_longlong] + [C.c_float] * 5 + [C.c_int, _vp]),
     ("fwant_nn_to_bf16", C.c_int, [_vp, _vp, C.c_longlong, _vp]),
     ("fwant_nn_axpby", C.c_int, [_vp, _vp, C.c_float, _vp, C.c_longlong, _vp]),
+    ("fwant_nn_basis_fwd", C.c_int, [_vp, _vp, _vp] + [C.c_int] * 4 + [_vp]),
+    ("fwant_nn_basis_bwd", C.c_int, [_vp, _vp, _vp] + [C.c_int] * 4 + [_vp]),
     ("fwant_max_abs", C.c_int, [_vp, _fp]),
     ("fwant_check", C.c_int, [_vp]),
     ("fwant_profile_stages", C.c_int, [_vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),

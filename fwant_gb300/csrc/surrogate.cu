@@ -331,6 +331,37 @@ __global__ void axpby_kernel(const float* a, const float* b, float s, float* y, 
     y[e] = a[e] + s * b[e];
 }
 
+// out[b][g][t] = sum_k coef[b][g][k] basis[g][k][t]
+__global__ void basis_fwd_kernel(const float* __restrict__ coef, const float* __restrict__ basis,
+                                 float* __restrict__ out, int B, int G, int K, int T) {
+  const long long n = (long long)B * G * T;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const int t = int(e % T);
+    const long long bg = e / T;
+    const int g = int(bg % G);
+    const float* c = coef + bg * K;
+    const float* bs = basis + (long long)g * K * T + t;
+    float acc = 0.0f;
+    for (int k = 0; k < K; ++k) acc = fmaf(c[k], bs[(long long)k * T], acc);
+    out[e] = acc;
+  }
+}
+// dcoef[b][g][k] = sum_t dout[b][g][t] basis[g][k][t]
+__global__ void basis_bwd_kernel(const float* __restrict__ dout, const float* __restrict__ basis,
+                                 float* __restrict__ dcoef, int B, int G, int K, int T) {
+  const long long n = (long long)B * G * K;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const int k = int(e % K);
+    const long long bg = e / K;
+    const int g = int(bg % G);
+    const float* d = dout + bg * T;
+    const float* bs = basis + ((long long)g * K + k) * T;
+    float acc = 0.0f;
+    for (int t = 0; t < T; ++t) acc = fmaf(d[t], bs[t], acc);
+    dcoef[e] = acc;
+  }
+}
+
 ConvDims dims(int B, int Ci, int D, int H, int W, int Co, int s) {
   ConvDims c{B, Ci, D, H, W, Co, s, (D - 1) / s + 1, (H - 1) / s + 1, (W - 1) / s + 1};
   return c;
@@ -412,6 +443,17 @@ int fwant_nn_adam(float* w, uint16_t* w16, const float* g, float* m, float* v, l
 
 int fwant_nn_to_bf16(const float* w, uint16_t* w16, long long n, void* stream) {
   to_bf16_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(w, w16, n);
+  return int(cudaGetLastError());
+}
+
+int fwant_nn_basis_fwd(const float* coef, const float* basis, float* out, int B, int G, int K, int T, void* stream) {
+  basis_fwd_kernel<<<grid_for((long long)B * G * T, 256), 256, 0, (cudaStream_t)stream>>>(coef, basis, out, B, G, K, T);
+  return int(cudaGetLastError());
+}
+
+int fwant_nn_basis_bwd(const float* dout, const float* basis, float* dcoef, int B, int G, int K, int T, void* stream) {
+  basis_bwd_kernel<<<grid_for((long long)B * G * K, 256), 256, 0, (cudaStream_t)stream>>>(dout, basis, dcoef, B, G, K,
+                                                                                        T);
   return int(cudaGetLastError());
 }
 

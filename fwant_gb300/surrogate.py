@@ -43,9 +43,14 @@ class Net:
     """The surrogate network on one GPU.  convs: [(cin, cout, stride)], dense: [(in, out)],
     in_shape: (C, D, H, W) of one input sample."""
 
-    def __init__(self, in_shape, convs, dense, seed=0, device="cuda"):
+    def __init__(self, in_shape, convs, dense, seed=0, device="cuda", basis=None):
         import torch
         self.torch = torch
+        # optional fixed output basis (G, K, T): the dense output is G*K coefficients
+        self.basis = basis
+        if basis is not None:
+            self.G, self.K, self.T = (int(v) for v in basis.shape)
+            assert dense[-1][1] == self.G * self.K
         self.L = _lib()
         self.in_shape = tuple(int(v) for v in in_shape)
         self.convs = [tuple(int(v) for v in c) for c in convs]
@@ -155,6 +160,10 @@ class Net:
             outs.append(y)
             h = y
         self._outs = outs
+        if self.basis is not None:
+            out = self._buf("basis_out", (B, self.G * self.T))
+            _ok(self.L.fwant_nn_basis_fwd(_p(h), _p(self.basis), _p(out), B, self.G, self.K, self.T, st), "basis fwd")
+            h = out
         return h
 
     def backward(self, dy):
@@ -163,6 +172,10 @@ class Net:
         st = self._stream()
         nc = len(self.convs)
         dy = dy.contiguous()
+        if self.basis is not None:
+            dc = self._buf("basis_dcoef", (B, self.G * self.K))
+            _ok(self.L.fwant_nn_basis_bwd(_p(dy), _p(self.basis), _p(dc), B, self.G, self.K, self.T, st), "basis bwd")
+            dy = dc
         for n in reversed(range(len(self.dense))):
             din, dout = self.dense[n]
             hin = self._outs[nc + n - 1].reshape(B, -1) if n > 0 else self._outs[nc - 1].reshape(B, -1)
@@ -291,19 +304,46 @@ def features(dv, energy, f=4):
     return np.stack([pool_volume(dv, f) * 20.0, energy]).astype(np.float32)
 
 
-def c5_net(in_shape, nout, seed):
+def waveform_basis(u_ref, dt, fc, scale, windows=8):
+    """Fixed output basis of the network: for every trace g of the reference gather
+    u_ref (G, T) (sampling interval dt s), the trace and its first two time derivatives
+    (scaled by 1/(2 pi fc) per derivative, i.e. to the trace's own magnitude) under
+    `windows` raised-cosine windows that sum to one.  A coefficient vector then expresses
+    a windowed amplitude change and time shift (to second order) of the reference wave
+    trains.  Returns (G, 3 * windows, T) float32, divided by `scale`."""
+    u = np.asarray(u_ref, np.float64)
+    G, T = u.shape
+    d1 = np.gradient(u, dt, axis=1) / (2 * np.pi * fc)
+    d2 = np.gradient(d1, dt, axis=1) / (2 * np.pi * fc)
+    hop = (T - 1) / (windows - 1)
+    t = np.arange(T)
+    win = np.zeros((windows, T))
+    for w in range(windows):
+        x = (t - w * hop) / hop
+        win[w] = np.where(np.abs(x) < 1.0, np.cos(0.5 * np.pi * x) ** 2, 0.0)
+    out = np.zeros((G, 3 * windows, T))
+    for j, d in enumerate((u, d1, d2)):
+        out[:, j * windows:(j + 1) * windows, :] = win[None, :, :] * d[:, None, :]
+    return (out / scale).astype(np.float32)
+
+
+def c5_net(in_shape, nout, seed, basis=None):
+    """The surrogate network for inputs of in_shape; with a basis (G, K, T) its dense head
+    emits G*K coefficients and the output is their basis expansion (nout = G*T)."""
     d, h, w = in_shape[1:]
     flat = 32 * ((((d - 1) // 2 + 1) - 1) // 2 + 1) * ((((h - 1) // 2 + 1) - 1) // 2 + 1) * \
         ((((w - 1) // 2 + 1) - 1) // 2 + 1)
-    return Net(in_shape, [(in_shape[0], 16, 1), (16, 32, 2), (32, 32, 2)], [(flat, 256), (256, nout)], seed=seed)
+    head = nout if basis is None else int(basis.shape[0] * basis.shape[1])
+    return Net(in_shape, [(in_shape[0], 16, 1), (16, 32, 2), (32, 32, 2)], [(flat, 256), (256, head)], seed=seed,
+               basis=basis)
 
 
 class Ensemble:
     """K networks trained from different initial weights on the same data; the spread of
     their predictions estimates the error of the mean."""
 
-    def __init__(self, in_shape, nout, k=4, seed=0):
-        self.nets = [c5_net(in_shape, nout, seed + 7919 * q) for q in range(k)]
+    def __init__(self, in_shape, nout, k=4, seed=0, basis=None):
+        self.nets = [c5_net(in_shape, nout, seed + 7919 * q, basis=basis) for q in range(k)]
 
     def fit(self, x, t, epochs=200, batch=32, lr=1e-3, lr_end=1e-4, wd=1e-4, seed=0):
         """x (N, C, D, H, W), t (N, out): CUDA tensors.  Returns the final epoch losses."""
@@ -365,7 +405,7 @@ def rel_err(a, b):
 
 
 def run_c5(n_train=512, n_val=64, n_test=64, nt=800, grid=(128, 128, 64), nrecv=64, k=4, epochs=200, tol=0.01,
-           seed=0, device=0, fc=0.2, t0=7.5, log=None):
+           seed=0, device=0, fc=0.2, t0=7.5, corr_km=25.0, windows=8, use_basis=False, log=None):
     """Train the surrogate ensemble on n_train seeded FD solves (the last n_val of them held
     back to calibrate the error estimate), then screen n_test held-out seeds: a candidate
     whose estimated error exceeds tol falls back to the FD solve.  Returns a dict of errors
@@ -378,16 +418,24 @@ def run_c5(n_train=512, n_val=64, n_test=64, nt=800, grid=(128, 128, 64), nrecv=
     u_ref, _ = simulate([ref], nt, device=device)
     energy = reference_energy(ref, nt, device=device)
     t0 = time.perf_counter()
-    x_tr, u_tr, t_fd = generate(ref, list(range(n_train)), nt, energy, device=device)
-    x_te, u_te, t_fd_te = generate(ref, list(range(100_000, 100_000 + n_test)), nt, energy, device=device)
+    x_tr, u_tr, t_fd = generate(ref, list(range(n_train)), nt, energy, device=device, corr_km=corr_km)
+    x_te, u_te, t_fd_te = generate(ref, list(range(100_000, 100_000 + n_test)), nt, energy, device=device,
+                                   corr_km=corr_km)
     say(f"data: {n_train + n_test} FD solves in {time.perf_counter() - t0:.1f} s, {t_fd:.2f} ms per solve")
+    # gathers trace-major: (n, 3, nrecv, nsamp), trace g = component * nrecv + receiver
+    u_ref, u_tr, u_te = (np.ascontiguousarray(a.transpose(0, 1, 3, 2)) for a in (u_ref, u_tr, u_te))
     scale = float(np.sqrt(np.mean(u_ref.astype(np.float64) ** 2)))
     dev = torch.device("cuda", device)
     tgt = ((u_tr - u_ref) / scale).reshape(n_train, -1).astype(np.float32)
     X = torch.tensor(x_tr, device=dev)
     T = torch.tensor(tgt, device=dev)
     fit_n = n_train - n_val
-    ens = Ensemble(tuple(x_tr.shape[1:]), tgt.shape[1], k=k, seed=seed)
+    basis = None
+    if use_basis:
+        g = u_ref.reshape(-1, u_ref.shape[-1])
+        basis = torch.tensor(waveform_basis(g, ref.recv_tinv * float(np.float32(ref.stept)), fc, scale, windows),
+                             device=dev)
+    ens = Ensemble(tuple(x_tr.shape[1:]), tgt.shape[1], k=k, seed=seed, basis=basis)
     t1 = time.perf_counter()
     losses = ens.fit(X[:fit_n], T[:fit_n], epochs=epochs, seed=seed)
     torch.cuda.synchronize()
@@ -420,8 +468,16 @@ def run_c5(n_train=512, n_val=64, n_test=64, nt=800, grid=(128, 128, 64), nrecv=
     accept = est <= tol
     final = np.where(accept, err, 0.0)  # fallbacks are the FD solve itself
     cost = n_test * t_nn + (~accept).sum() * t_fd_te
+    screening = {}
+    for tq in sorted({tol, 0.01, 0.02, 0.05}):
+        acc = est <= tq
+        screening[f"{tq:g}"] = {
+            "accepted": int(acc.sum()), "accepted_err_max": float(err[acc].max()) if acc.any() else None,
+            "speedup": float(n_test * t_fd_te / (n_test * t_nn + (~acc).sum() * t_fd_te))}
     return {
+        "screening": screening,
         "grid": list(grid), "nt": nt, "nrecv": nrecv, "n_train": fit_n, "n_val": n_val, "n_test": n_test,
+        "corr_km": corr_km, "basis_windows": windows if use_basis else None,
         "ensemble": k, "epochs": epochs, "params_per_net": ens.nets[0].nparams,
         "fd_ms_per_solve": t_fd_te, "surrogate_ms_per_candidate": t_nn, "train_s": t_train,
         "baseline_err_median": float(np.median(base)), "baseline_err_max": float(base.max()),

@@ -63,6 +63,11 @@ int fwant_nn_adam(float* w, uint16_t* w16, const float* g, float* m, float* v, l
 /* w16 = round-to-nearest-even BF16 of w. */
 int fwant_nn_to_bf16(const float* w, uint16_t* w16, long long n, void* stream);
 
+/* Fixed waveform basis: out[b][g][t] = sum_k coef[b][g][k] basis[g][k][t] (G groups of
+ * K basis traces of T samples), and its backward dcoef[b][g][k] = sum_t dout basis. */
+int fwant_nn_basis_fwd(const float* coef, const float* basis, float* out, int B, int G, int K, int T, void* stream);
+int fwant_nn_basis_bwd(const float* dout, const float* basis, float* dcoef, int B, int G, int K, int T, void* stream);
+
 /* y = a + s * b, elementwise. */
 int fwant_nn_axpby(const float* a, const float* b, float s, float* y, long long n, void* stream);
 

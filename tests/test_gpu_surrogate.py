@@ -103,7 +103,27 @@ def test_surrogate_beats_reference_waveforms(native_lib):
     without the network).  Small configuration of the 128x128x64 workload."""
     from fwant_gb300 import surrogate
     r = surrogate.run_c5(n_train=96, n_val=16, n_test=16, nt=240, grid=(40, 40, 24), nrecv=12, k=2, epochs=60,
-                         fc=0.5, t0=2.5)
+                         fc=0.5, t0=2.5, use_basis=True)
     print(r)
     assert r["baseline_err_median"] > 0.005  # the perturbations change the waveforms
     assert r["surrogate_err_median"] < 0.7 * r["baseline_err_median"]
+
+
+def test_basis_layer_matches_numpy(native_lib):
+    import torch
+
+    from fwant_gb300 import surrogate
+    rng = np.random.default_rng(9)
+    B, G, K, T = 3, 5, 7, 11
+    coef = rng.normal(size=(B, G, K)).astype(np.float32)
+    basis = rng.normal(size=(G, K, T)).astype(np.float32)
+    dout = rng.normal(size=(B, G, T)).astype(np.float32)
+    c, bs, d = (torch.tensor(a, device="cuda") for a in (coef, basis, dout))
+    out = torch.zeros((B, G, T), device="cuda")
+    dc = torch.zeros((B, G, K), device="cuda")
+    L = surrogate._lib()
+    assert L.fwant_nn_basis_fwd(surrogate._p(c), surrogate._p(bs), surrogate._p(out), B, G, K, T, None) == 0
+    assert L.fwant_nn_basis_bwd(surrogate._p(d), surrogate._p(bs), surrogate._p(dc), B, G, K, T, None) == 0
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(out.cpu().numpy(), np.einsum("bgk,gkt->bgt", coef, basis), rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(dc.cpu().numpy(), np.einsum("bgt,gkt->bgk", dout, basis), rtol=1e-5, atol=1e-5)
