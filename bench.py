@@ -164,7 +164,7 @@ def peaks():
 def ncu_traffic_ratio():
     """Measured DRAM bytes over algorithmic bytes of the stage kernel, from the committed
     ncu summary (captured on a smaller grid of the same kernel), or None."""
-    path = os.path.join(ROOT, "profiles", "stage_kernel_c2.md")
+    path = os.path.join(ROOT, "profiles", "stage_batch_kernel_c2.md")
     if not os.path.exists(path):
         return None
     m = re.search(r"dram_traffic_over_algorithmic:\s*([0-9.eE+-]+)", open(path).read())
@@ -335,7 +335,7 @@ def run_ours(args, rank, world):
     tr = ncu_traffic_ratio() if args.storage == "fp32" else None
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "peak_source": peak_kind, "traffic": (tr * algo_bytes_step / 4.0) if tr else None,
-            "traffic_note": "bytes per launch: ncu DRAM/algorithmic ratio (profiles/stage_kernel_c2.md) x "
+            "traffic_note": "bytes per launch: ncu DRAM/algorithmic ratio (profiles/stage_batch_kernel_c2.md) x "
                             "algorithmic bytes of this launch",
             "stage_ms": stage_ms, "step_end_ms": end_ms,
             "algorithmic_bytes_per_launch": algo_bytes_step / 4.0}
