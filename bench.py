@@ -348,9 +348,9 @@ def run_ours(args, rank, world):
                    "storage": args.storage, "fields_finite_after_run": finite,
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
         "host_wall_s": t_host, "roofline": roof, "clocks": clk,
-        # per step: four batched stage launches per group of up to 18 simulations, and the
-        # step-end (receivers + step counter) kernel of every simulation
-        "gpu_launches": args.steps * (4 * ((len(sims) + 17) // 18) + len(sims)),
+        # per step: per group of up to 16 simulations four stages x (interior launch + boundary
+        # launch), and the step-end (receivers + step counter) kernel of every simulation
+        "gpu_launches": args.steps * (8 * ((len(sims) + 15) // 16) + len(sims)),
     }
     if args.config == "c3":
         # the same simulations launched one at a time (one simulation per stage launch)

@@ -375,7 +375,7 @@ class Solver:
 
 
 class Batch:
-    """Solvers stepped together: one launch per RK stage for up to 18 members."""
+    """Solvers stepped together: one launch per RK stage for up to 16 members."""
 
     def __init__(self, solvers):
         self._lib = load_library()

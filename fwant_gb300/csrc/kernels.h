@@ -85,10 +85,13 @@ struct StageArgs {
   CUtensorMap tm_m;     // RK register m: box TX x TY x 1 x 9
   CUtensorMap tm_t;     // RK register t: box TX x TY x 1 x 9
   CUtensorMap tm_med;   // lambda, mu, rho: box TX x TY x 1 x 3
+  CUtensorMap tm_tile_lo;  // stage input W, lean form: box TILE_BX x TILE_BY x 1 x 3 (Vx Vy Vz)
+  CUtensorMap tm_tile_hi;  // stage input W, lean form: box TILE_BX x TILE_BY x 1 x 5 (Txz .. Txy)
   Geom g;
   const void* win;    // stage input W (9 components, storage type)
   void* wout;         // stage output W
   void* wt;           // RK accumulator t
+  const void* wm;     // RK register m (W at the step start)
   // BF16/FP16 storage holds value * scale: velocities (sv) and stresses (st); 1/scale too
   float sv, st, isv, ist;
   // 1-D metric, 0-based Fortran index, with ghosts
@@ -122,12 +125,12 @@ struct StageArgs {
 // arguments (tensor maps included) held in the kernel's parameter space (the 32 KB
 // parameter limit bounds the count); larger batches use one launch per group.
 constexpr int MAX_BATCH = 64;
-constexpr int BATCH_PER_LAUNCH = 18;
+constexpr int BATCH_PER_LAUNCH = 16;
 struct BatchArgs {
   StageArgs sims[BATCH_PER_LAUNCH];
-  int nsims, total;                  // simulations, work items
-  int off[BATCH_PER_LAUNCH + 1];     // first work item of each simulation
-  int tiles_x[BATCH_PER_LAUNCH], tiles_y[BATCH_PER_LAUNCH];
+  const int* items[BATCH_PER_LAUNCH];  // per simulation: work items, bx | by << 10 | bz << 20
+  int nsims, total;                    // simulations, work items
+  int off[BATCH_PER_LAUNCH + 1];       // first work item of each simulation
 };
 static_assert(sizeof(BatchArgs) <= 32764, "kernel parameter space");
 
@@ -136,8 +139,14 @@ static_assert(sizeof(BatchArgs) <= 32764, "kernel parameter space");
 // operand order with IEEE division and no FMA (bit-reproducible against FP32 CPU runs
 // of the same expressions); 0 the fast form (FMA, reciprocals).
 // storage: ST_F32 / ST_BF16 / ST_F16 (the exact form exists for ST_F32 only).
-int launch_stage(const StageArgs& a, int variant, int rk, int exact, int storage, void* stream);
-int launch_stage_batch(const BatchArgs& b, int variant, int rk, int exact, int storage, int ctas, void* stream);
+// lean = 1: the interior-only form (items without PML points, sources or free surface).
+int launch_stage_batch(const BatchArgs& b, int variant, int rk, int exact, int storage, int lean, int ctas,
+                       void* stream);
+// Work items of one simulation split into the lean (interior) list and the full list.
+// force_c / mom_c: 0-based source centres (3 per source).
+void stage_items(const Geom& g, int kc, const Slab slab[6], const int* force_c, int nforce, const int* mom_c,
+                 int nmom, int* lean, int* nlean, int* full, int* nfull);
+long long stage_item_count(const Geom& g, int kc);
 int stage_planes_per_cta(const Geom& g, int sm_count);
 int stage_configure();  // set the dynamic shared-memory attribute of every instantiation
 

@@ -66,7 +66,7 @@ struct fwant_solver {
   int* d_err = nullptr;  // device error word of the stage kernel (bounded waits)
   // TMA descriptors: per register set the halo'd tile, the z-queue plane and the point
   // box; one for the medium
-  CUtensorMap tm_tile[4], tm_q[4], tm_pt[4], tm_med;
+  CUtensorMap tm_tile[4], tm_q[4], tm_pt[4], tm_med, tm_tile_lo[4], tm_tile_hi[4];
   // 1-D arrays, each with nx/ny/nz entries
   float *d_x = nullptr, *d_y = nullptr, *d_z = nullptr, *d_xsin = nullptr, *d_xcot = nullptr;
   float *d_xi = nullptr, *d_eta = nullptr, *d_zeta = nullptr;
@@ -102,6 +102,16 @@ struct fwant_solver {
   unsigned int* d_maxbits = nullptr;
   float* d_snap = nullptr;  // staging buffer of fwant_get_snapshot (grown on demand)
   size_t snap_cap = 0;
+  // work items of the stage launches: lean (interior) items first, then the full ones
+  int* d_items = nullptr;
+  int n_lean = 0, n_full = 0;
+  // RK kinds (bit 0 beg, 1 inn, 2 fin) whose interior items use the lean form.  Measured
+  // on C2 (stage ms, full form -> split): beg 2.93 -> 2.66, fin 3.11 -> 3.08, inn 4.08 ->
+  // 4.23 (the inn stage moves the most bytes and is DRAM-bound either way; the split only
+  // adds a second launch and its tail).
+  int lean_mask = 5;
+  std::vector<int> h_items;
+  std::vector<int> h_force_c, h_mom_c;  // 0-based source centres (item classification)
   // strain Green's tensor recording: sgt_ snapshot frames kept on the device
   float* d_sgt = nullptr;
   fw::SgtRecArgs sgt{};
@@ -119,7 +129,7 @@ struct fwant_solver {
     cudaFree(d_x); cudaFree(d_y); cudaFree(d_z); cudaFree(d_xsin); cudaFree(d_xcot);
     cudaFree(d_xi); cudaFree(d_eta); cudaFree(d_zeta); cudaFree(d_prof); cudaFree(d_rzinv); cudaFree(d_rsinv);
     for (int f = 0; f < 6; ++f) cudaFree(aux[f]);
-    cudaFree(d_rec); cudaFree(d_seis); cudaFree(d_ntime); cudaFree(d_maxbits); cudaFree(d_snap); cudaFree(d_conv); cudaFree(d_sgt);
+    cudaFree(d_rec); cudaFree(d_seis); cudaFree(d_ntime); cudaFree(d_maxbits); cudaFree(d_snap); cudaFree(d_conv); cudaFree(d_sgt); cudaFree(d_items);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (st) cudaStreamDestroy(st);
@@ -164,6 +174,9 @@ struct fwant_solver {
   fwant_status init() {
     const int ni = cfg.ni, nj = cfg.nj, nk = cfg.nk;
     if (ni < 8 || nj < 8 || nk < 8) return fail(FWANT_ERR_INVALID_ARG, "ni, nj, nk must be >= 8");
+    // work items pack the tile indices in 10 + 10 + 11 bits
+    if (ni > 1024 * fw::STAGE_TX || nj > 1024 * fw::STAGE_TY || nk > 2047 * 4)
+      return fail(FWANT_ERR_INVALID_ARG, "grid too large: ni <= 32768, nj <= 8192, nk <= 8188");
     if (!(cfg.stept > 0.0)) return fail(FWANT_ERR_INVALID_ARG, "stept must be > 0");
     if (cfg.storage == FWANT_STORAGE_FP32) stor = fw::ST_F32;
     else if (cfg.storage == FWANT_STORAGE_BF16) stor = fw::ST_BF16;
@@ -185,9 +198,13 @@ struct fwant_solver {
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, cfg.device);
     kc = fw::stage_planes_per_cta(g, nsm > 0 ? nsm : 152);
+    if (const char* env = std::getenv("FWANT_LEAN_STAGES")) {  // tuning override
+      const int v = std::atoi(env);
+      if (v >= 0 && v <= 7) lean_mask = v;
+    }
     if (const char* env = std::getenv("FWANT_PLANES_PER_CTA")) {  // tuning override
       const int v = std::atoi(env);
-      if (v >= 1) kc = v;
+      if (v >= 1 && (nk + v - 1) / v <= 2047) kc = v;
     }
     if ((e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
     cudaEventCreate(&ev0);
@@ -287,7 +304,11 @@ struct fwant_solver {
       if (make(&tm_tile[r], set(r), wtype, esz, fw::NF, fw::tile_box_x(esz), fw::TILE_BY, fw::NF, tile_promo) !=
               CUDA_SUCCESS ||
           make(&tm_q[r], set(r), wtype, esz, fw::NF, fw::STAGE_TX, fw::STAGE_TY, 6, line) != CUDA_SUCCESS ||
-          make(&tm_pt[r], set(r), wtype, esz, fw::NF, fw::STAGE_TX, fw::STAGE_TY, fw::NF, line) != CUDA_SUCCESS)
+          make(&tm_pt[r], set(r), wtype, esz, fw::NF, fw::STAGE_TX, fw::STAGE_TY, fw::NF, line) != CUDA_SUCCESS ||
+          make(&tm_tile_lo[r], set(r), wtype, esz, fw::NF, fw::tile_box_x(esz), fw::TILE_BY, 3, tile_promo) !=
+              CUDA_SUCCESS ||
+          make(&tm_tile_hi[r], set(r), wtype, esz, fw::NF, fw::tile_box_x(esz), fw::TILE_BY, 5, tile_promo) !=
+              CUDA_SUCCESS)
         return fail(FWANT_ERR_CUDA, "tensor map encoding failed");
     }
     if (make(&tm_med, med, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, 3, fw::STAGE_TX, fw::STAGE_TY, 3, line) != CUDA_SUCCESS)
@@ -538,6 +559,8 @@ struct fwant_solver {
     S.disp = upload(disp); S.rate = upload(rate); S.mrate = upload(mrate);
     S.nsurf = int(surf_w.size());
     S.surf_ij = upload(surf_ij); S.surf_q = upload(surf_q); S.surf_w = upload(surf_w);
+    h_force_c = fc;
+    h_mom_c = mc;
     S.nforce = F.num; S.ntwin_f = F.ntwin;
     S.force_c = upload(fc); S.force_wt = upload(fwt); S.force_on = upload(fon); S.force_F = upload(fF);
     S.nmom = Mo.num; S.ntwin_m = Mo.ntwin;
@@ -596,6 +619,47 @@ struct fwant_solver {
   // Register-set roles: A holds W at the step start (and is the RK "m" register), T is
   // the RK "t" accumulator; B and C are the stage outputs.  Stage 4 writes W(n+1) into
   // T in place, after which A and T swap roles.
+  // Work-item lists of the stage launches for the current k-chunk, PML and sources
+  // (rebuilt, and the graphs dropped, when they change).
+  fwant_status ensure_items() {
+    const long long n = fw::stage_item_count(g, kc);
+    std::vector<int> lean(static_cast<size_t>(n)), full(static_cast<size_t>(n));
+    int nl = 0, nf = 0;
+    fw::stage_items(g, kc, slab, h_force_c.data(), int(h_force_c.size() / 3), h_mom_c.data(),
+                    int(h_mom_c.size() / 3), lean.data(), &nl, full.data(), &nf);
+    // lean items, full items, then every item in launch order (x fastest, then y, k)
+    std::vector<int> all(lean.begin(), lean.begin() + nl);
+    all.insert(all.end(), full.begin(), full.begin() + nf);
+    {
+      const int nbx = (g.ni + fw::STAGE_TX - 1) / fw::STAGE_TX, nby = (g.nj + fw::STAGE_TY - 1) / fw::STAGE_TY;
+      for (int bz = 0; bz * kc < g.nk; ++bz)
+        for (int by = 0; by < nby; ++by)
+          for (int bx = 0; bx < nbx; ++bx) all.push_back(bx | (by << 10) | (bz << 20));
+    }
+    if (d_items && nl == n_lean && all == h_items) return FWANT_OK;
+    cudaFree(d_items);
+    d_items = dalloc<int>(all.size());
+    if (!d_items) return fail(FWANT_ERR_OOM, "work items");
+    cudaError_t e = cudaMemcpy(d_items, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "work items");
+    h_items = std::move(all);
+    n_lean = nl;
+    n_full = nf;
+    drop_graphs();
+    return FWANT_OK;
+  }
+  // Items of one launch of RK kind rk: lean = 1 the interior items, lean = 0 the others,
+  // or all items in launch order when the lean form is off for rk.
+  bool lean_on(int rk) const { return (lean_mask >> rk & 1) != 0; }
+  const int* items(bool lean, int rk) const {
+    if (!lean_on(rk)) return d_items + n_lean + n_full;
+    return d_items + (lean ? 0 : n_lean);
+  }
+  int item_count(bool lean, int rk) const {
+    if (!lean_on(rk)) return lean ? 0 : n_lean + n_full;
+    return lean ? n_lean : n_full;
+  }
+
   // Arguments of stage s (0..3) of a step that starts with W in register set ra (the
   // other of sets 0 and 3 is the accumulator T).
   fw::StageArgs stage_args(int s, int ra) const {
@@ -603,8 +667,9 @@ struct fwant_solver {
     fw::StageArgs a = base_args();
     const int in_of[4] = {ra, rB, rC, rB};
     const int out_of[4] = {rB, rC, rB, rt};
-    a.win = set(in_of[s]); a.wout = set(out_of[s]); a.wt = set(rt);
+    a.win = set(in_of[s]); a.wout = set(out_of[s]); a.wt = set(rt); a.wm = set(ra);
     a.tm_tile = tm_tile[in_of[s]]; a.tm_q = tm_q[in_of[s]]; a.tm_m = tm_pt[ra]; a.tm_t = tm_pt[rt];
+    a.tm_tile_lo = tm_tile_lo[in_of[s]]; a.tm_tile_hi = tm_tile_hi[in_of[s]];
     for (int f = 0; f < 6; ++f) {
       if (!slab[f].on) continue;
       a.ain[f] = aset(f, in_of[s]); a.am[f] = aset(f, ra); a.aout[f] = aset(f, out_of[s]); a.at[f] = aset(f, rt);
@@ -657,6 +722,10 @@ struct fwant_solver {
       }
     }
     put(&kc, sizeof(kc));
+    put(&d_items, sizeof(d_items));
+    put(&n_lean, sizeof(n_lean));
+    put(&n_full, sizeof(n_full));
+    put(&lean_mask, sizeof(lean_mask));
   }
   void finish_step_host() {
     std::swap(rA, rT);
@@ -664,14 +733,26 @@ struct fwant_solver {
     ntime += 1;
   }
 
-  // One time step: four fused stage launches and the step-end kernels.
+  // One time step: per RK stage the lean launch over the interior items and the full
+  // launch over the others, then the step-end kernels.
   int enqueue_step(cudaEvent_t* ev = nullptr) {
     int lerr = 0;
+    static thread_local fw::BatchArgs b;  // 30 KB: kept off the stack
     for (int s = 0; s < 4; ++s) {
-      const fw::StageArgs a = stage_args(s, rA);
       if (ev) cudaEventRecord(ev[s], st);
-      const int le = fw::launch_stage(a, stage_variant(cycle_pos, s), stage_rk(s), cfg.exact_arith, stor, st);
-      if (le && !lerr) lerr = le;
+      b.sims[0] = stage_args(s, rA);
+      b.nsims = 1;
+      for (int lean = 1; lean >= 0; --lean) {
+        const int cnt = item_count(lean, stage_rk(s));
+        if (cnt == 0) continue;
+        b.items[0] = items(lean, stage_rk(s));
+        b.off[0] = 0;
+        b.off[1] = cnt;
+        b.total = cnt;
+        const int le = fw::launch_stage_batch(b, stage_variant(cycle_pos, s), stage_rk(s), cfg.exact_arith, stor,
+                                              lean, cnt, st);
+        if (le && !lerr) lerr = le;
+      }
     }
     if (ev) cudaEventRecord(ev[4], st);
     enqueue_step_end(st);
@@ -725,6 +806,7 @@ struct fwant_solver {
     fwant_status rc = prepare_sources(ntime + nsteps);
     if (rc != FWANT_OK) return rc;
     if ((rc = prepare_receivers(ntime + nsteps)) != FWANT_OK) return rc;
+    if ((rc = ensure_items()) != FWANT_OK) return rc;
     cudaEventRecord(ev0, st);
     int left = nsteps;
     while (left > 0) {
@@ -792,6 +874,7 @@ struct fwant_solver {
     fwant_status rc = prepare_sources(ntime + nsteps);
     if (rc != FWANT_OK) return rc;
     if ((rc = prepare_receivers(ntime + nsteps)) != FWANT_OK) return rc;
+    if ((rc = ensure_items()) != FWANT_OK) return rc;
     std::vector<cudaEvent_t> ev(size_t(6) * nsteps);
     for (auto& e : ev) cudaEventCreate(&e);
     int lerr = 0;
@@ -1309,6 +1392,8 @@ fwant_status fwant_autotune(fwant_solver* s, int trial_steps, int* planes_out) {
 
 fwant_status fwant_set_planes_per_cta(fwant_solver* s, int planes) {
   if (!s || planes < 1 || planes > 4096) return FWANT_ERR_INVALID_ARG;
+  if ((s->cfg.nk + planes - 1) / planes > 2047)
+    return s->fail(FWANT_ERR_INVALID_ARG, "planes per CTA: at most 2047 k-chunks");
   s->kc = planes;
   s->drop_graphs();
   return FWANT_OK;
@@ -1359,20 +1444,18 @@ struct fwant_batch {
   }
   int n() const { return int(sims.size()); }
 
-  // Arguments of stage s for members [first, first+count) (count <= BATCH_PER_LAUNCH).
-  void batch_args(fw::BatchArgs& b, int first, int count, int ra, int s) const {
+  // Arguments of stage s for members [first, first+count) (count <= BATCH_PER_LAUNCH),
+  // lean or full items.
+  void batch_args(fw::BatchArgs& b, int first, int count, int ra, int s, bool lean) const {
     b.nsims = count;
     int off = 0;
+    const int rk = fwant_solver::stage_rk(s);
     for (int q = 0; q < count; ++q) {
       const fwant_solver* m = sims[first + q];
-      const fw::Geom& g = m->g;
-      const int tx = (g.ni + fw::STAGE_TX - 1) / fw::STAGE_TX, ty = (g.nj + fw::STAGE_TY - 1) / fw::STAGE_TY;
-      const int tz = (g.nk + m->kc - 1) / m->kc;
       b.sims[q] = m->stage_args(s, ra);
+      b.items[q] = m->items(lean, rk);
       b.off[q] = off;
-      b.tiles_x[q] = tx;
-      b.tiles_y[q] = ty;
-      off += tx * ty * tz;
+      off += m->item_count(lean, rk);
     }
     b.off[count] = off;
     b.total = off;
@@ -1388,12 +1471,15 @@ struct fwant_batch {
       if (ev) cudaEventRecord(ev[s], st);
       for (int first = 0; first < n(); first += fw::BATCH_PER_LAUNCH) {
         const int count = std::min(fw::BATCH_PER_LAUNCH, n() - first);
-        batch_args(b, first, count, s0->rA, s);
-        const int nct = ctas > 0 ? std::min(b.total, ctas) : b.total;
-        const int le = fw::launch_stage_batch(b, fwant_solver::stage_variant(s0->cycle_pos, s),
-                                              fwant_solver::stage_rk(s), s0->cfg.exact_arith, s0->stor,
-                                              std::max(1, nct), st);
-        if (le && !lerr) lerr = le;
+        for (int lean = 1; lean >= 0; --lean) {
+          batch_args(b, first, count, s0->rA, s, lean != 0);
+          if (b.total == 0) continue;
+          const int nct = ctas > 0 ? std::min(b.total, ctas) : b.total;
+          const int le = fw::launch_stage_batch(b, fwant_solver::stage_variant(s0->cycle_pos, s),
+                                                fwant_solver::stage_rk(s), s0->cfg.exact_arith, s0->stor, lean,
+                                                std::max(1, nct), st);
+          if (le && !lerr) lerr = le;
+        }
       }
     }
     if (ev) cudaEventRecord(ev[4], st);
@@ -1412,6 +1498,7 @@ struct fwant_batch {
         return fail(FWANT_ERR_STATE, "coordinates, metric and media must be set for every member");
       fwant_status rc = m->prepare_sources(m->ntime + nsteps);
       if (rc == FWANT_OK) rc = m->prepare_receivers(m->ntime + nsteps);
+      if (rc == FWANT_OK) rc = m->ensure_items();
       if (rc != FWANT_OK) return fail(rc, "member: " + m->err);
     }
     return FWANT_OK;

@@ -1,19 +1,18 @@
 // Selection of the stage-kernel instantiation and of the k-chunk length.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "kernels.h"
 
 namespace fw {
 
-#define FW_DECL(mode)                                                            \
-  int launch_stage_##mode##_rk0(const StageArgs&, int, cudaStream_t);            \
-  int launch_stage_##mode##_rk1(const StageArgs&, int, cudaStream_t);            \
-  int launch_stage_##mode##_rk2(const StageArgs&, int, cudaStream_t);            \
-  int launch_stage_batch_##mode##_rk0(const BatchArgs&, int, int, cudaStream_t); \
-  int launch_stage_batch_##mode##_rk1(const BatchArgs&, int, int, cudaStream_t); \
-  int launch_stage_batch_##mode##_rk2(const BatchArgs&, int, int, cudaStream_t); \
-  int configure_stage_##mode##_rk0();                                            \
-  int configure_stage_##mode##_rk1();                                            \
+#define FW_DECL(mode)                                                                       \
+  int launch_stage_batch_##mode##_rk0(const BatchArgs&, int, int, int, cudaStream_t);       \
+  int launch_stage_batch_##mode##_rk1(const BatchArgs&, int, int, int, cudaStream_t);       \
+  int launch_stage_batch_##mode##_rk2(const BatchArgs&, int, int, int, cudaStream_t);       \
+  int configure_stage_##mode##_rk0();                                                       \
+  int configure_stage_##mode##_rk1();                                                       \
   int configure_stage_##mode##_rk2();
 FW_DECL(fast)
 FW_DECL(exact)
@@ -21,25 +20,13 @@ FW_DECL(bf16)
 FW_DECL(fp16)
 #undef FW_DECL
 
-int launch_stage(const StageArgs& a, int variant, int rk, int exact, int storage, void* stream) {
+int launch_stage_batch(const BatchArgs& b, int variant, int rk, int exact, int storage, int lean, int ctas,
+                       void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
-#define FW_RK(mode)                                                    \
-  return rk == 0 ? launch_stage_##mode##_rk0(a, variant, st)           \
-                 : (rk == 1 ? launch_stage_##mode##_rk1(a, variant, st) \
-                            : launch_stage_##mode##_rk2(a, variant, st));
-  if (storage == ST_BF16) { FW_RK(bf16) }
-  if (storage == ST_F16) { FW_RK(fp16) }
-  if (exact) { FW_RK(exact) }
-  FW_RK(fast)
-#undef FW_RK
-}
-
-int launch_stage_batch(const BatchArgs& b, int variant, int rk, int exact, int storage, int ctas, void* stream) {
-  cudaStream_t st = (cudaStream_t)stream;
-#define FW_RK(mode)                                                                  \
-  return rk == 0 ? launch_stage_batch_##mode##_rk0(b, variant, ctas, st)             \
-                 : (rk == 1 ? launch_stage_batch_##mode##_rk1(b, variant, ctas, st)  \
-                            : launch_stage_batch_##mode##_rk2(b, variant, ctas, st));
+#define FW_RK(mode)                                                                         \
+  return rk == 0 ? launch_stage_batch_##mode##_rk0(b, variant, lean, ctas, st)              \
+                 : (rk == 1 ? launch_stage_batch_##mode##_rk1(b, variant, lean, ctas, st)   \
+                            : launch_stage_batch_##mode##_rk2(b, variant, lean, ctas, st));
   if (storage == ST_BF16) { FW_RK(bf16) }
   if (storage == ST_F16) { FW_RK(fp16) }
   if (exact) { FW_RK(exact) }
@@ -55,6 +42,49 @@ int stage_configure() {
   for (auto fn : fns)
     if (int e = fn()) return e;
   return 0;
+}
+
+long long stage_item_count(const Geom& g, int kc) {
+  return (long long)((g.ni + STAGE_TX - 1) / STAGE_TX) * ((g.nj + STAGE_TY - 1) / STAGE_TY) * ((g.nk + kc - 1) / kc);
+}
+
+// An item is lean when none of its points lies in a PML slab, within reach (3 points) of
+// a smoothed source box, or within four planes of a free surface (images, VLOW rows,
+// T*Src): exactly the code the lean form compiles out.
+void stage_items(const Geom& g, int kc, const Slab slab[6], const int* force_c, int nforce, const int* mom_c,
+                 int nmom, int* lean, int* nlean, int* full, int* nfull) {
+  const int nbx = (g.ni + STAGE_TX - 1) / STAGE_TX, nby = (g.nj + STAGE_TY - 1) / STAGE_TY;
+  const int nbz = (g.nk + kc - 1) / kc;
+  auto overlap = [](int a0, int a1, int b0, int b1) { return a0 <= b1 && b0 <= a1; };
+  int nl = 0, nf = 0;
+  for (int bz = 0; bz < nbz; ++bz)
+    for (int by = 0; by < nby; ++by)
+      for (int bx = 0; bx < nbx; ++bx) {
+        const int i0 = g.i1 + bx * STAGE_TX, i1 = std::min(i0 + STAGE_TX - 1, g.i2);
+        const int j0 = g.j1 + by * STAGE_TY, j1 = std::min(j0 + STAGE_TY - 1, g.j2);
+        const int k0 = g.k1 + bz * kc, k1 = std::min(k0 + kc - 1, g.k2);
+        bool is_lean = !(g.freesurf && k1 > g.k2 - 4);
+        for (int f = 0; f < 6 && is_lean; ++f) {
+          const Slab& s = slab[f];
+          if (s.on && overlap(i0, i1, s.i1, s.i2) && overlap(j0, j1, s.j1, s.j2) && overlap(k0, k1, s.k1, s.k2))
+            is_lean = false;
+        }
+        for (int n = 0; n < nforce && is_lean; ++n)
+          if (overlap(i0, i1, force_c[3 * n] - 3, force_c[3 * n] + 3) &&
+              overlap(j0, j1, force_c[3 * n + 1] - 3, force_c[3 * n + 1] + 3) &&
+              overlap(k0, k1, force_c[3 * n + 2] - 3, force_c[3 * n + 2] + 3))
+            is_lean = false;
+        for (int n = 0; n < nmom && is_lean; ++n)
+          if (overlap(i0, i1, mom_c[3 * n] - 3, mom_c[3 * n] + 3) &&
+              overlap(j0, j1, mom_c[3 * n + 1] - 3, mom_c[3 * n + 1] + 3) &&
+              overlap(k0, k1, mom_c[3 * n + 2] - 3, mom_c[3 * n + 2] + 3))
+            is_lean = false;
+        const int packed = bx | (by << 10) | (bz << 20);
+        if (is_lean) lean[nl++] = packed;
+        else full[nf++] = packed;
+      }
+  *nlean = nl;
+  *nfull = nf;
 }
 
 // Planes per CTA.  Short chunks keep the CTAs that share halo rows marching through the

@@ -3,11 +3,8 @@
 #include "stage_impl.cuh"
 
 namespace fw {
-int launch_stage_fast_rk1(const StageArgs& a, int variant, cudaStream_t st) {
-  return launch_rk_variant<float, false, 1>(a, variant, st);
-}
-int launch_stage_batch_fast_rk1(const BatchArgs& b, int variant, int ctas, cudaStream_t st) {
-  return launch_batch_rk_variant<float, false, 1>(b, variant, ctas, st);
+int launch_stage_batch_fast_rk1(const BatchArgs& b, int variant, int lean, int ctas, cudaStream_t st) {
+  return launch_batch_rk_variant<float, false, 1>(b, variant, lean, ctas, st);
 }
 int configure_stage_fast_rk1() { return configure_rk<float, false, 1>(); }
 }  // namespace fw

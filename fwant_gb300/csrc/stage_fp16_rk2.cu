@@ -3,11 +3,8 @@
 #include "stage_impl.cuh"
 
 namespace fw {
-int launch_stage_fp16_rk2(const StageArgs& a, int variant, cudaStream_t st) {
-  return launch_rk_variant<__half, false, 2>(a, variant, st);
-}
-int launch_stage_batch_fp16_rk2(const BatchArgs& b, int variant, int ctas, cudaStream_t st) {
-  return launch_batch_rk_variant<__half, false, 2>(b, variant, ctas, st);
+int launch_stage_batch_fp16_rk2(const BatchArgs& b, int variant, int lean, int ctas, cudaStream_t st) {
+  return launch_batch_rk_variant<__half, false, 2>(b, variant, lean, ctas, st);
 }
 int configure_stage_fp16_rk2() { return configure_rk<__half, false, 2>(); }
 }  // namespace fw

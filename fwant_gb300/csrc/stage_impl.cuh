@@ -57,6 +57,22 @@ struct Lay {
   static constexpr int OFF_T = OFF_M + SZ_PT;
   static constexpr int BUF_BYTES = ((OFF_T + SZ_PT + 1023) / 1024) * 1024;
   static constexpr int SMEM_BYTES = 2 * BUF_BYTES + 64;
+  // Interior-only (lean) form: the tile holds the eight x/y-differentiated components
+  // (Tzz comes from the z queue) as two boxes, components 0-2 and 4-8, each starting on a
+  // 128-byte boundary; the RK registers m and t of the current plane are staged in one
+  // buffer after the two pipeline buffers.
+  static constexpr int SZ_PLANE = TBY * TBX * ES;
+  static constexpr int OFF_HI_L = ((3 * SZ_PLANE + 127) / 128) * 128;
+  static constexpr int SZ_TILE_L = OFF_HI_L + 5 * SZ_PLANE;
+  static constexpr int OFF_Q_L = ((SZ_TILE_L + 127) / 128) * 128;
+  static constexpr int OFF_MED_L = OFF_Q_L + SZ_Q;
+  static constexpr int BUF_BYTES_LEAN = ((OFF_MED_L + SZ_MED + 127) / 128) * 128;
+  static constexpr int OFF_MT_L = 2 * BUF_BYTES_LEAN;
+  template <int RK>
+  static constexpr int SZ_MT_L = RK == 1 ? 2 * SZ_PT : (RK == 2 ? SZ_PT : 0);
+  static int smem_bytes(bool lean, int rk) {
+    return lean ? OFF_MT_L + (rk == 1 ? 2 * SZ_PT : (rk == 2 ? SZ_PT : 0)) + 64 : SMEM_BYTES;
+  }
 };
 
 // Storage conversions.  BF16/FP16 registers hold value * scale (a power of two per
@@ -231,13 +247,18 @@ __device__ __forceinline__ float surf_val(const Sources& S, const float* tab, in
 // [bz*kc, +kc).  Returns false when a bounded wait gave up (error word set).  The
 // mbarriers are initialised on entry and invalidated on a normal exit, so a persistent
 // CTA can run several work items in turn.
-template <class S, bool EXACT, int FX, int FY, int FZ, int RK>
+// LEAN: the item holds no PML slab point, no source box and no plane within 4 of a free
+// surface (the host classifies the items); that code is compiled out, and the RK
+// registers m and t are read from global memory instead of being staged, so that the
+// lean form fits three CTAs per SM (registers and shared memory).
+template <class S, bool EXACT, int FX, int FY, int FZ, int RK, bool LEAN>
 __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, int bz, unsigned char* smem) {
   static_assert(!EXACT || is_f32_v<S>, "the reference-order form exists for FP32 storage only");
   using L = Lay<S>;
   constexpr int TBX = L::TBX, HX = L::HX;
-  constexpr int BUF_BYTES = L::BUF_BYTES, OFF_Q = L::OFF_Q, OFF_MED = L::OFF_MED, OFF_M = L::OFF_M,
-                OFF_T = L::OFF_T;
+  constexpr int BUF_BYTES = LEAN ? L::BUF_BYTES_LEAN : L::BUF_BYTES, OFF_Q = LEAN ? L::OFF_Q_L : L::OFF_Q,
+                OFF_MED = LEAN ? L::OFF_MED_L : L::OFF_MED, OFF_M = L::OFF_M, OFF_T = L::OFF_T;
+  constexpr int OFF_BAR = LEAN ? L::OFF_MT_L + L::template SZ_MT_L<RK> : 2 * L::BUF_BYTES;
   const Geom& g = A.g;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
   const int i0 = g.i1 + bx * TX, j0 = g.j1 + by * TY;
@@ -266,18 +287,21 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
     else return v * (f < 3 ? A.isv : A.ist);
   };
   const int gst = __ldg(A.ntime) * 4 + A.stage;
-  const bool fsurf = g.freesurf != 0;
+  const bool fsurf = !LEAN && g.freesurf != 0;
   const Sources& Src = A.src;
 
   constexpr int LEAD = FZ ? 3 : 1;   // planes ahead of k in the z operator
   constexpr int TRAIL = FZ ? 1 : 3;  // planes behind k
-  constexpr uint32_t TX_BYTES =
-      L::SZ_TILE + L::SZ_Q + L::SZ_MED + (RK == 1 ? L::SZ_PT : 0) + (RK >= 1 ? L::SZ_PT : 0);
+  constexpr uint32_t TX_BYTES = (LEAN ? 8 * L::SZ_PLANE : L::SZ_TILE) + L::SZ_Q + L::SZ_MED +
+                                 (!LEAN && RK == 1 ? L::SZ_PT : 0) + (!LEAN && RK >= 1 ? L::SZ_PT : 0);
+  constexpr uint32_t MT_BYTES = L::template SZ_MT_L<RK>;  // lean: m and t of one plane
 
-  const uint32_t bar0 = smem_u32(smem + 2 * BUF_BYTES);
+  const uint32_t bar0 = smem_u32(smem + OFF_BAR);
+  const uint32_t bar_mt = bar0 + 16;
   if (tid == 0) {
     mbar_init(bar0, 1);
     mbar_init(bar0 + 8, 1);
+    if (LEAN && RK >= 1) mbar_init(bar_mt, 1);
     fence_barrier_init();
   }
   __syncthreads();
@@ -289,14 +313,27 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
     const uint32_t bar = bar0 + 8 * b;
     fence_proxy_async();
     mbar_expect_tx(bar, TX_BYTES);
-    tma_load_4d(base, &A.tm_tile, i0 - HX + PADL, j0 - HY, kp, 0, bar);
+    if (LEAN) {
+      tma_load_4d(base, &A.tm_tile_lo, i0 - HX + PADL, j0 - HY, kp, 0, bar);
+      tma_load_4d(base + L::OFF_HI_L, &A.tm_tile_hi, i0 - HX + PADL, j0 - HY, kp, 4, bar);
+    } else {
+      tma_load_4d(base, &A.tm_tile, i0 - HX + PADL, j0 - HY, kp, 0, bar);
+    }
     // plane kp+LEAD comes back as the tile of a later iteration: keep it in L2
     tma_load_4d_hint(base + OFF_Q, &A.tm_q, i0 + PADL, j0, kp + LEAD, 0, bar, pol_keep);
     tma_load_4d_hint(base + OFF_MED, &A.tm_med, i0 + PADL, j0, kp, 0, bar, pol_stream);
-    if (RK == 1) tma_load_4d_hint(base + OFF_M, &A.tm_m, i0 + PADL, j0, kp, 0, bar, pol_stream);
-    if (RK >= 1) tma_load_4d_hint(base + OFF_T, &A.tm_t, i0 + PADL, j0, kp, 0, bar, pol_stream);
+    if (!LEAN && RK == 1) tma_load_4d_hint(base + OFF_M, &A.tm_m, i0 + PADL, j0, kp, 0, bar, pol_stream);
+    if (!LEAN && RK >= 1) tma_load_4d_hint(base + OFF_T, &A.tm_t, i0 + PADL, j0, kp, 0, bar, pol_stream);
   };
   if (tid == 0) issue(kb, 0);
+  // lean form: m and t of plane kp into the single RK buffer
+  auto issue_mt = [&](int kp) {
+    const uint32_t base = smem_u32(smem + L::OFF_MT_L);
+    fence_proxy_async();
+    mbar_expect_tx(bar_mt, MT_BYTES);
+    if (RK == 1) tma_load_4d_hint(base, &A.tm_m, i0 + PADL, j0, kp, 0, bar_mt, pol_stream);
+    tma_load_4d_hint(base + (RK == 1 ? L::SZ_PT : 0), &A.tm_t, i0 + PADL, j0, kp, 0, bar_mt, pol_stream);
+  };
 
   // T*Src of this column (read on the top planes only)
   float tsx = 0.0f, tsy = 0.0f, tsz = 0.0f;
@@ -335,10 +372,10 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
   // Does this CTA's block of points touch any smoothed source box?  (tested once here
   // instead of per point and plane)
   bool cta_src = false;
-  for (int n = 0; n < Src.nforce && !cta_src; ++n)
+  for (int n = 0; !LEAN && n < Src.nforce && !cta_src; ++n)
     cta_src = Src.force_c[3 * n] + 3 >= i0 && Src.force_c[3 * n] - 3 <= i0 + TX - 1 && Src.force_c[3 * n + 1] + 3 >= j0 &&
               Src.force_c[3 * n + 1] - 3 <= j0 + TY - 1 && Src.force_c[3 * n + 2] + 3 >= kb && Src.force_c[3 * n + 2] - 3 <= ke;
-  for (int n = 0; n < Src.nmom && !cta_src; ++n)
+  for (int n = 0; !LEAN && n < Src.nmom && !cta_src; ++n)
     cta_src = Src.mom_c[3 * n] + 3 >= i0 && Src.mom_c[3 * n] - 3 <= i0 + TX - 1 && Src.mom_c[3 * n + 1] + 3 >= j0 &&
               Src.mom_c[3 * n + 1] - 3 <= j0 + TY - 1 && Src.mom_c[3 * n + 2] + 3 >= kb && Src.mom_c[3 * n + 2] - 3 <= ke;
 
@@ -346,13 +383,14 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
   // membership is fixed per thread (bits 0-3: x1 x2 y1 y2); the z slabs (bits 4, 5) are
   // tested per plane, uniformly across the CTA.
   unsigned xymask = 0;
-  if (act)
+  if (!LEAN && act)
 #pragma unroll
     for (int sidx = 0; sidx < 4; ++sidx) {
       const Slab& sl = A.slab[sidx];
       if (sl.on && i >= sl.i1 && i <= sl.i2 && j >= sl.j1 && j <= sl.j2) xymask |= 1u << sidx;
     }
   auto slab_mask = [&](int kp) -> unsigned {
+    if (LEAN) return 0u;
     unsigned m = act ? xymask : 0u;
     if (act && A.slab[4].on && kp >= A.slab[4].k1 && kp <= A.slab[4].k2) m |= 16u;
     if (act && A.slab[5].on && kp >= A.slab[5].k1 && kp <= A.slab[5].k2) m |= 32u;
@@ -375,20 +413,29 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
       }
     }
   };
-  prefetch_pml(kb);
+  if (!LEAN) prefetch_pml(kb);
 
   int it = 0;
   for (int k = kb; k <= ke; ++k, ++it) {
     const int cur = it & 1;
+    // (every thread finished the previous plane, so the RK buffer is free)
+    if (LEAN && RK >= 1 && tid == 0) issue_mt(k);
     if (tid == 0 && k < ke) issue(k + 1, cur ^ 1);
-    if (k < ke) prefetch_pml(k + 1);
+    if (!LEAN && k < ke) prefetch_pml(k + 1);
     const bool ok = mbar_wait(bar0 + 8 * cur, (it >> 1) & 1);
     unsigned char* buf = smem + cur * BUF_BYTES;
-    S(*tile)[TBY][TBX] = reinterpret_cast<S(*)[TBY][TBX]>(buf);
+    // component f of the halo'd tile (the lean tile has no Tzz)
+    auto tl = [&](int f) -> S(*)[TBX] {
+      if constexpr (LEAN)
+        return reinterpret_cast<S(*)[TBX]>(buf + (f < 3 ? f * L::SZ_PLANE : L::OFF_HI_L + (f - 4) * L::SZ_PLANE));
+      else
+        return reinterpret_cast<S(*)[TBX]>(buf + f * L::SZ_PLANE);
+    };
     const S(*qs)[TY][TX] = reinterpret_cast<const S(*)[TY][TX]>(buf + OFF_Q);
     const float(*med)[TY][TX] = reinterpret_cast<const float(*)[TY][TX]>(buf + OFF_MED);
-    const S(*mbuf)[TY][TX] = reinterpret_cast<const S(*)[TY][TX]>(buf + OFF_M);
-    const S(*tbuf)[TY][TX] = reinterpret_cast<const S(*)[TY][TX]>(buf + OFF_T);
+    const S(*mbuf)[TY][TX] = reinterpret_cast<const S(*)[TY][TX]>(LEAN ? smem + L::OFF_MT_L : buf + OFF_M);
+    const S(*tbuf)[TY][TX] = reinterpret_cast<const S(*)[TY][TX]>(
+        LEAN ? smem + L::OFF_MT_L + (RK == 1 ? L::SZ_PT : 0) : buf + OFF_T);
     const bool top = fsurf && k == g.k2;
     if (top) {
       // the imaged stress components read T*Src on the free surface (interior columns)
@@ -397,14 +444,15 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
           const int r = e / TBX, cc = e % TBX;
           const int ii = i0 - HX + cc, jj = j0 - HY + r;
           if (ii >= g.i1 && ii <= g.i2 && jj >= g.j1 && jj <= g.j2) {
-            tile[TXZ][r][cc] = enc(surf_val(Src, Src.disp, gst, 0, ii, jj), TXZ);
-            tile[TYZ][r][cc] = enc(surf_val(Src, Src.disp, gst, 1, ii, jj), TYZ);
-            tile[TZZ][r][cc] = enc(surf_val(Src, Src.disp, gst, 2, ii, jj), TZZ);
+            tl(TXZ)[r][cc] = enc(surf_val(Src, Src.disp, gst, 0, ii, jj), TXZ);
+            tl(TYZ)[r][cc] = enc(surf_val(Src, Src.disp, gst, 1, ii, jj), TYZ);
+            tl(TZZ)[r][cc] = enc(surf_val(Src, Src.disp, gst, 2, ii, jj), TZZ);
           }
         }
       __syncthreads();
     }
 
+    bool ok_mt = true;
     if (ok && act) {
       // advance the z queue with plane k+LEAD (the image applies on and above the surface)
       const bool img = fsurf && k + LEAD >= g.k2;
@@ -419,18 +467,18 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
       const float ze = __ldg(A.zeta_z + k);
       const int r0 = ty + HY, c0 = tx + HX;
       // stencil sums along x (tile rows), y (tile columns), z (queue)
-      const float sxTxx = unscale(dopS<FX>(&tile[TXX][r0][c0], 1), TXX);
-      const float sxTxy = unscale(dopS<FX>(&tile[TXY][r0][c0], 1), TXY);
-      const float sxTxz = unscale(dopS<FX>(&tile[TXZ][r0][c0], 1), TXZ);
-      const float sxVx = unscale(dopS<FX>(&tile[VX][r0][c0], 1), VX);
-      const float sxVy = unscale(dopS<FX>(&tile[VY][r0][c0], 1), VY);
-      const float sxVz = unscale(dopS<FX>(&tile[VZ][r0][c0], 1), VZ);
-      const float syTyy = unscale(dopS<FY>(&tile[TYY][r0][c0], TBX), TYY);
-      const float syTxy = unscale(dopS<FY>(&tile[TXY][r0][c0], TBX), TXY);
-      const float syTyz = unscale(dopS<FY>(&tile[TYZ][r0][c0], TBX), TYZ);
-      const float syVx = unscale(dopS<FY>(&tile[VX][r0][c0], TBX), VX);
-      const float syVy = unscale(dopS<FY>(&tile[VY][r0][c0], TBX), VY);
-      const float syVz = unscale(dopS<FY>(&tile[VZ][r0][c0], TBX), VZ);
+      const float sxTxx = unscale(dopS<FX>(&tl(TXX)[r0][c0], 1), TXX);
+      const float sxTxy = unscale(dopS<FX>(&tl(TXY)[r0][c0], 1), TXY);
+      const float sxTxz = unscale(dopS<FX>(&tl(TXZ)[r0][c0], 1), TXZ);
+      const float sxVx = unscale(dopS<FX>(&tl(VX)[r0][c0], 1), VX);
+      const float sxVy = unscale(dopS<FX>(&tl(VY)[r0][c0], 1), VY);
+      const float sxVz = unscale(dopS<FX>(&tl(VZ)[r0][c0], 1), VZ);
+      const float syTyy = unscale(dopS<FY>(&tl(TYY)[r0][c0], TBX), TYY);
+      const float syTxy = unscale(dopS<FY>(&tl(TXY)[r0][c0], TBX), TXY);
+      const float syTyz = unscale(dopS<FY>(&tl(TYZ)[r0][c0], TBX), TYZ);
+      const float syVx = unscale(dopS<FY>(&tl(VX)[r0][c0], TBX), VX);
+      const float syVy = unscale(dopS<FY>(&tl(VY)[r0][c0], TBX), VY);
+      const float syVz = unscale(dopS<FY>(&tl(VZ)[r0][c0], TBX), VZ);
       const float szTzz = dopq<FZ>(q[TZZ]);
       const float szTxz = dopq<FZ>(q[TXZ]);
       const float szTyz = dopq<FZ>(q[TYZ]);
@@ -444,8 +492,8 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
       }
       const float Vx = q[VX][TRAIL], Vy = q[VY][TRAIL], Vz = q[VZ][TRAIL];
       const float Tzz = q[TZZ][TRAIL], Txz = q[TXZ][TRAIL], Tyz = q[TYZ][TRAIL];
-      const float Txx = dec(tile[TXX][r0][c0], TXX), Tyy = dec(tile[TYY][r0][c0], TYY);
-      const float Txy = dec(tile[TXY][r0][c0], TXY);
+      const float Txx = dec(tl(TXX)[r0][c0], TXX), Tyy = dec(tl(TYY)[r0][c0], TYY);
+      const float Txy = dec(tl(TXY)[r0][c0], TXY);
       const bool water = miu <= 1.0e-20f;
 
       float hVx, hVy, hVz, hTxx, hTyy, hTzz, hTxy, hTxz, hTyz;
@@ -651,16 +699,18 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
       }
 
       // ---- RK update (mod_macdrp.F90:291-393); m of stage 1 is the stored input value
+      if (LEAN && RK >= 1) ok_mt = mbar_wait(bar_mt, it & 1);
       float hh[NF];
       hh[VX] = hVx; hh[VY] = hVy; hh[VZ] = hVz; hh[TZZ] = hTzz; hh[TXZ] = hTxz; hh[TYZ] = hTyz;
       hh[TXX] = hTxx; hh[TYY] = hTyy; hh[TXY] = hTxy;
 #pragma unroll
-      for (int f = 0; f < NF; ++f) {
+      for (int f = 0; f < NF && ok_mt; ++f) {
         const long long o = f * fs + p;
         if (RK == 0) {
           // the tile holds the stored input; on the surface the imaged components were
           // patched in shared memory, so read those three from global memory there
-          const float m = dec((top && (f == TZZ || f == TXZ || f == TYZ)) ? W[o] : tile[f][r0][c0], f);
+          const float m = (LEAN && f == TZZ) ? q[TZZ][TRAIL]
+                          : dec((top && (f == TZZ || f == TXZ || f == TYZ)) ? W[o] : tl(f)[r0][c0], f);
           st_stream_s(Wout + o, enc(m + A.a * hh[f], f), pol_stream);
           st_stream_s(Wt + o, enc(m + A.b * hh[f], f), pol_stream);
         } else if (RK == 1) {
@@ -672,10 +722,11 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
       }
     }
     // all threads agree on a timeout before leaving the pipeline
-    if (__syncthreads_or(!ok)) {
+    if (__syncthreads_or(!ok || !ok_mt)) {
       if (tid == 0) {
         atomicExch(A.err, DEVERR_TMA_TIMEOUT);
-        if (k < ke) mbar_wait(bar0 + 8 * (cur ^ 1), ((it + 1) >> 1) & 1);  // copy still in flight
+        if (k < ke) mbar_wait(bar0 + 8 * (cur ^ 1), ((it + 1) >> 1) & 1);  // copies still in flight
+        if (LEAN && RK >= 1) mbar_wait(bar_mt, it & 1);
       }
       return false;
     }
@@ -684,94 +735,71 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
   if (tid == 0) {
     mbar_inval(bar0);
     mbar_inval(bar0 + 8);
+    if (LEAN && RK >= 1) mbar_inval(bar_mt);
   }
   return true;
 }
 
-template <class S, bool EXACT, int FX, int FY, int FZ, int RK>
-__global__ void __launch_bounds__(TX* TY, 2) stage_kernel(const __grid_constant__ StageArgs A) {
-  extern __shared__ __align__(1024) unsigned char smem[];
-  stage_body<S, EXACT, FX, FY, FZ, RK>(A, blockIdx.x, blockIdx.y, blockIdx.z, smem);
-}
-
-// Launch over a batch of simulations: the work items (tiles x k-chunks) of all
-// simulations are numbered simulation after simulation, x fastest, and CTA b runs items
-// b, b + gridDim.x, ... (one item each when the grid covers them all).
-template <class S, bool EXACT, int FX, int FY, int FZ, int RK>
-__global__ void __launch_bounds__(TX* TY, 2) stage_batch_kernel(const __grid_constant__ BatchArgs B) {
+// Launch over a batch of simulations: the work items (tile x k-chunk, packed as
+// bx | by << 10 | bz << 20) of all simulations are numbered simulation after simulation,
+// and CTA b runs items b, b + gridDim.x, ... (one item each when the grid covers them
+// all).  Lean launches get the interior items, full launches the others.
+template <class S, bool EXACT, int FX, int FY, int FZ, int RK, bool LEAN>
+__global__ void __launch_bounds__(TX* TY, LEAN ? 3 : 2) stage_batch_kernel(const __grid_constant__ BatchArgs B) {
   extern __shared__ __align__(1024) unsigned char smem[];
   for (int item = blockIdx.x; item < B.total; item += gridDim.x) {
     int s = 0;
     while (item >= B.off[s + 1]) ++s;
-    const int local = item - B.off[s];
-    const int bx = local % B.tiles_x[s], r = local / B.tiles_x[s];
-    const int by = r % B.tiles_y[s], bz = r / B.tiles_y[s];
-    if (!stage_body<S, EXACT, FX, FY, FZ, RK>(B.sims[s], bx, by, bz, smem)) return;
+    const int packed = B.items[s][item - B.off[s]];
+    const int bx = packed & 1023, by = (packed >> 10) & 1023, bz = packed >> 20;
+    if (!stage_body<S, EXACT, FX, FY, FZ, RK, LEAN>(B.sims[s], bx, by, bz, smem)) return;
     __syncthreads();  // the next item re-initialises the barriers and reuses the buffers
   }
 }
 
-template <class S, bool EXACT, int FX, int FY, int FZ, int RK>
-static int launch_one(const StageArgs& a, const dim3& grid, cudaStream_t st) {
-  stage_kernel<S, EXACT, FX, FY, FZ, RK><<<grid, dim3(TX, TY, 1), Lay<S>::SMEM_BYTES, st>>>(a);
-  return int(cudaGetLastError());
-}
-
-template <class S, bool EXACT, int FX, int FY, int FZ, int RK>
+template <class S, bool EXACT, int FX, int FY, int FZ, int RK, bool LEAN>
 static int launch_batch_one(const BatchArgs& b, int ctas, cudaStream_t st) {
-  stage_batch_kernel<S, EXACT, FX, FY, FZ, RK><<<ctas, dim3(TX, TY, 1), Lay<S>::SMEM_BYTES, st>>>(b);
+  stage_batch_kernel<S, EXACT, FX, FY, FZ, RK, LEAN>
+      <<<ctas, dim3(TX, TY, 1), Lay<S>::smem_bytes(LEAN, RK), st>>>(b);
   return int(cudaGetLastError());
 }
 
-// Opt every instantiation of one (EXACT, RK) pair into the dynamic shared memory it
+// Opt every instantiation of one (storage, form, RK) into the dynamic shared memory it
 // needs; called once per device before any launch or stream capture.
 template <class S, bool EXACT, int RK>
 static int configure_rk() {
   cudaError_t e = cudaSuccess;
-#define FW_CFG(FX, FY, FZ)                                                                                      \
-  if (e == cudaSuccess)                                                                                         \
-    e = cudaFuncSetAttribute(stage_kernel<S, EXACT, FX, FY, FZ, RK>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                             Lay<S>::SMEM_BYTES);
-  FW_CFG(0, 0, 0) FW_CFG(0, 0, 1) FW_CFG(0, 1, 0) FW_CFG(0, 1, 1)
-  FW_CFG(1, 0, 0) FW_CFG(1, 0, 1) FW_CFG(1, 1, 0) FW_CFG(1, 1, 1)
-#undef FW_CFG
-#define FW_CFG(FX, FY, FZ)                                                                              \
-  if (e == cudaSuccess)                                                                                 \
-    e = cudaFuncSetAttribute(stage_batch_kernel<S, EXACT, FX, FY, FZ, RK>,                              \
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, Lay<S>::SMEM_BYTES);
+#define FW_CFG(FX, FY, FZ)                                                                           \
+  if (e == cudaSuccess)                                                                              \
+    e = cudaFuncSetAttribute(stage_batch_kernel<S, EXACT, FX, FY, FZ, RK, false>,                    \
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, Lay<S>::smem_bytes(false, RK)); \
+  if (e == cudaSuccess)                                                                              \
+    e = cudaFuncSetAttribute(stage_batch_kernel<S, EXACT, FX, FY, FZ, RK, true>,                     \
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, Lay<S>::smem_bytes(true, RK));
   FW_CFG(0, 0, 0) FW_CFG(0, 0, 1) FW_CFG(0, 1, 0) FW_CFG(0, 1, 1)
   FW_CFG(1, 0, 0) FW_CFG(1, 0, 1) FW_CFG(1, 1, 0) FW_CFG(1, 1, 1)
 #undef FW_CFG
   return int(e);
 }
 
-template <class S, bool EXACT, int RK>
-static int launch_rk_variant(const StageArgs& a, int variant, cudaStream_t st) {
-  const dim3 grid((a.g.ni + TX - 1) / TX, (a.g.nj + TY - 1) / TY, (a.g.nk + a.kc - 1) / a.kc);
+template <class S, bool EXACT, int RK, bool LEAN>
+static int launch_batch_lean(const BatchArgs& b, int variant, int ctas, cudaStream_t st) {
   switch (variant) {
-    case 0: return launch_one<S, EXACT, 0, 0, 0, RK>(a, grid, st);
-    case 1: return launch_one<S, EXACT, 0, 0, 1, RK>(a, grid, st);
-    case 2: return launch_one<S, EXACT, 0, 1, 0, RK>(a, grid, st);
-    case 3: return launch_one<S, EXACT, 0, 1, 1, RK>(a, grid, st);
-    case 4: return launch_one<S, EXACT, 1, 0, 0, RK>(a, grid, st);
-    case 5: return launch_one<S, EXACT, 1, 0, 1, RK>(a, grid, st);
-    case 6: return launch_one<S, EXACT, 1, 1, 0, RK>(a, grid, st);
-    default: return launch_one<S, EXACT, 1, 1, 1, RK>(a, grid, st);
+    case 0: return launch_batch_one<S, EXACT, 0, 0, 0, RK, LEAN>(b, ctas, st);
+    case 1: return launch_batch_one<S, EXACT, 0, 0, 1, RK, LEAN>(b, ctas, st);
+    case 2: return launch_batch_one<S, EXACT, 0, 1, 0, RK, LEAN>(b, ctas, st);
+    case 3: return launch_batch_one<S, EXACT, 0, 1, 1, RK, LEAN>(b, ctas, st);
+    case 4: return launch_batch_one<S, EXACT, 1, 0, 0, RK, LEAN>(b, ctas, st);
+    case 5: return launch_batch_one<S, EXACT, 1, 0, 1, RK, LEAN>(b, ctas, st);
+    case 6: return launch_batch_one<S, EXACT, 1, 1, 0, RK, LEAN>(b, ctas, st);
+    default: return launch_batch_one<S, EXACT, 1, 1, 1, RK, LEAN>(b, ctas, st);
   }
 }
 
 template <class S, bool EXACT, int RK>
-static int launch_batch_rk_variant(const BatchArgs& b, int variant, int ctas, cudaStream_t st) {
-  switch (variant) {
-    case 0: return launch_batch_one<S, EXACT, 0, 0, 0, RK>(b, ctas, st);
-    case 1: return launch_batch_one<S, EXACT, 0, 0, 1, RK>(b, ctas, st);
-    case 2: return launch_batch_one<S, EXACT, 0, 1, 0, RK>(b, ctas, st);
-    case 3: return launch_batch_one<S, EXACT, 0, 1, 1, RK>(b, ctas, st);
-    case 4: return launch_batch_one<S, EXACT, 1, 0, 0, RK>(b, ctas, st);
-    case 5: return launch_batch_one<S, EXACT, 1, 0, 1, RK>(b, ctas, st);
-    case 6: return launch_batch_one<S, EXACT, 1, 1, 0, RK>(b, ctas, st);
-    default: return launch_batch_one<S, EXACT, 1, 1, 1, RK>(b, ctas, st);
-  }
+static int launch_batch_rk_variant(const BatchArgs& b, int variant, int lean, int ctas, cudaStream_t st) {
+  return lean ? launch_batch_lean<S, EXACT, RK, true>(b, variant, ctas, st)
+              : launch_batch_lean<S, EXACT, RK, false>(b, variant, ctas, st);
 }
 
 }  // namespace fw

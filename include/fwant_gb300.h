@@ -294,7 +294,7 @@ fwant_status fwant_autotune(fwant_solver* s, int trial_steps, int* planes);
 /* ---- Batches: many simulations stepped together ----
  * No counterpart in the reference, which runs one virtual source per job.  A batch steps
  * n solvers (same device, storage and arithmetic form; sizes, media, sources and
- * receivers may all differ) in lockstep: each RK stage of up to 18 members is one launch
+ * receivers may all differ) in lockstep: each RK stage of up to 16 members is one launch
  * whose CTAs walk the work items (tiles x k-chunks) of every member, and whole 8-step
  * blocks replay a CUDA graph.  Results are those of fwant_run on each member: bit for bit
  * with exact_arith, to FP32 rounding in the fast form (multiply-add contraction may differ
