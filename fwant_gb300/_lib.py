@@ -56,6 +56,8 @@ EXPORTS = [
     ("fwant_set_field", C.c_int, [_vp, C.c_int, _fp]),
     ("fwant_get_snapshot", C.c_int, [_vp, _ip, _ip, _ip, C.c_int, _ip, _fp]),
     ("fwant_get_snapshot_noalloc", C.c_int, [_vp, _ip, _ip, _ip, C.c_int, _ip, _fp]),
+    ("fwant_save_checkpoint", C.c_int, [_vp, C.c_char_p]),
+    ("fwant_load_checkpoint", C.c_int, [_vp, C.c_char_p]),
     ("fwant_set_sgt_record", C.c_int, [_vp, _ip, _ip, _ip, C.c_int, C.c_int]),
     ("fwant_get_sgt", C.c_int, [_vp, _fp, C.c_int, _ip]),
     ("fwant_sgtker_create", C.c_int, [C.c_longlong, C.c_int, C.c_double, C.c_int, C.POINTER(_vp)]),
@@ -322,6 +324,12 @@ class Solver:
         self._chk(self._lib.fwant_get_snapshot_noalloc(self._h, _ptr(s0, C.c_int), _ptr(c0, C.c_int),
                                                        _ptr(t0, C.c_int), len(cm), _ptr(cm, C.c_int), _ptr(out)))
         return out.reshape(len(cm), int(c0[2]), int(c0[1]), int(c0[0])).transpose(0, 3, 2, 1)
+
+    def save_checkpoint(self, path):
+        self._chk(self._lib.fwant_save_checkpoint(self._h, os.fsencode(path)))
+
+    def load_checkpoint(self, path):
+        self._chk(self._lib.fwant_load_checkpoint(self._h, os.fsencode(path)))
 
     def set_sgt_record(self, subs, subc, subt, tinv, max_frames):
         """Keep sgt_ snapshot frames (six stresses of a strided sub-volume every tinv steps)

@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstdint>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -1230,6 +1231,142 @@ fwant_status fwant_get_snapshot_noalloc(fwant_solver* s, const int subs[3], cons
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) return s->cuda_fail(e, "get_snapshot_noalloc");
+  return FWANT_OK;
+}
+
+// ---- checkpoint / resume -----------------------------------------------------------------
+// File: a fixed header (magic, version, the configuration the state belongs to, counters,
+// section sizes, FNV-1a 64 checksum of the payload) followed by the payload: the
+// wavefield register set holding W (padded layout, storage type), the PML memory variables
+// of that set per active slab, the recorded seismogram samples and the recorded SGT frames.
+namespace {
+constexpr char CKPT_MAGIC[8] = {'F', 'W', 'A', 'N', 'T', 'C', 'K', '1'};
+struct CkptHeader {
+  char magic[8];
+  uint32_t version;
+  int32_t ni, nj, nk, px, storage, freesurf;
+  int64_t fstride;
+  int32_t ntime, cycle_pos;
+  float sv, st;
+  int32_t slab_on[6];
+  int64_t aux_set[6];
+  int32_t npt, tinv, nsamp;
+  int32_t sgt_on, sgt_frames, sgt_max_frames;
+  int64_t sgt_npts;
+  uint64_t payload_bytes;
+  uint64_t checksum;
+};
+uint64_t fnv1a(const unsigned char* p, size_t n, uint64_t h) {
+  for (size_t i = 0; i < n; ++i) {
+    h ^= p[i];
+    h *= 1099511628211ULL;
+  }
+  return h;
+}
+}  // namespace
+
+fwant_status fwant_save_checkpoint(fwant_solver* s, const char* path) {
+  if (!s || !path) return FWANT_ERR_INVALID_ARG;
+  cudaSetDevice(s->cfg.device);
+  CkptHeader h;
+  std::memset(&h, 0, sizeof(h));
+  std::memcpy(h.magic, CKPT_MAGIC, 8);
+  h.version = 1;
+  h.ni = s->g.ni; h.nj = s->g.nj; h.nk = s->g.nk; h.px = s->g.px; h.storage = s->stor; h.freesurf = s->g.freesurf;
+  h.fstride = s->g.fstride;
+  h.ntime = s->ntime; h.cycle_pos = s->cycle_pos;
+  h.sv = s->sv; h.st = s->sc_t;
+  for (int f = 0; f < 6; ++f) { h.slab_on[f] = s->slab[f].on; h.aux_set[f] = s->slab[f].on ? s->aux_set[f] : 0; }
+  h.npt = s->npt; h.tinv = s->tinv; h.nsamp = s->npt > 0 ? std::min(s->nsamp, s->cap) : 0;
+  h.sgt_on = s->sgt_on;
+  h.sgt_frames = s->sgt_on ? std::min(s->ntime / s->sgt.tinv, s->sgt.max_frames) : 0;
+  h.sgt_max_frames = s->sgt_on ? s->sgt.max_frames : 0;
+  h.sgt_npts = s->sgt_on ? s->sgt.npts : 0;
+  // payload
+  std::vector<unsigned char> pay;
+  auto append_dev = [&](const void* d, size_t bytes) -> cudaError_t {
+    const size_t o = pay.size();
+    pay.resize(o + bytes);
+    return bytes ? cudaMemcpy(pay.data() + o, d, bytes, cudaMemcpyDeviceToHost) : cudaSuccess;
+  };
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = append_dev(s->set(s->rA), size_t(fw::NF) * s->g.fstride * s->esz);
+  for (int f = 0; f < 6 && e == cudaSuccess; ++f)
+    if (h.slab_on[f]) e = append_dev(s->aset(f, s->rA), size_t(h.aux_set[f]) * sizeof(float));
+  for (int c = 0; c < fw::NF && e == cudaSuccess; ++c)
+    e = append_dev(s->d_seis + size_t(c) * s->cap * s->npt, size_t(h.nsamp) * s->npt * sizeof(float));
+  for (int c = 0; c < 6 && e == cudaSuccess && h.sgt_on; ++c)
+    e = append_dev(s->d_sgt + size_t(c) * h.sgt_max_frames * h.sgt_npts, size_t(h.sgt_frames) * h.sgt_npts * 4);
+  if (e != cudaSuccess) return s->cuda_fail(e, "save_checkpoint");
+  h.payload_bytes = pay.size();
+  h.checksum = fnv1a(pay.data(), pay.size(), 1469598103934665603ULL);
+  FILE* fp = std::fopen(path, "wb");
+  if (!fp) return s->fail(FWANT_ERR_INVALID_ARG, std::string("save_checkpoint: cannot open ") + path);
+  const bool ok = std::fwrite(&h, sizeof(h), 1, fp) == 1 && std::fwrite(pay.data(), 1, pay.size(), fp) == pay.size();
+  if (std::fclose(fp) != 0 || !ok) return s->fail(FWANT_ERR_INVALID_ARG, "save_checkpoint: write failed");
+  return FWANT_OK;
+}
+
+fwant_status fwant_load_checkpoint(fwant_solver* s, const char* path) {
+  if (!s || !path) return FWANT_ERR_INVALID_ARG;
+  cudaSetDevice(s->cfg.device);
+  FILE* fp = std::fopen(path, "rb");
+  if (!fp) return s->fail(FWANT_ERR_INVALID_ARG, std::string("load_checkpoint: cannot open ") + path);
+  CkptHeader h;
+  std::vector<unsigned char> pay;
+  bool ok = std::fread(&h, sizeof(h), 1, fp) == 1 && std::memcmp(h.magic, CKPT_MAGIC, 8) == 0 && h.version == 1 &&
+            h.payload_bytes < (uint64_t(1) << 44);
+  if (ok) {
+    pay.resize(size_t(h.payload_bytes));
+    ok = std::fread(pay.data(), 1, pay.size(), fp) == pay.size();
+  }
+  std::fclose(fp);
+  if (!ok) return s->fail(FWANT_ERR_INVALID_ARG, "load_checkpoint: not a checkpoint file or truncated");
+  if (fnv1a(pay.data(), pay.size(), 1469598103934665603ULL) != h.checksum)
+    return s->fail(FWANT_ERR_INVALID_ARG, "load_checkpoint: checksum mismatch (corrupt file)");
+  // the state must belong to this solver's configuration
+  bool same = h.ni == s->g.ni && h.nj == s->g.nj && h.nk == s->g.nk && h.px == s->g.px && h.storage == s->stor &&
+              h.freesurf == s->g.freesurf && h.fstride == s->g.fstride && h.npt == s->npt && h.tinv == s->tinv &&
+              h.sgt_on == int(s->sgt_on) && h.cycle_pos >= 0 && h.cycle_pos < 8 && h.ntime >= 0 &&
+              h.cycle_pos == (h.ntime & 7);
+  for (int f = 0; f < 6; ++f)
+    same = same && h.slab_on[f] == s->slab[f].on && (!h.slab_on[f] || h.aux_set[f] == s->aux_set[f]);
+  if (h.sgt_on) same = same && h.sgt_npts == s->sgt.npts && h.sgt_max_frames == s->sgt.max_frames;
+  if (!same) return s->fail(FWANT_ERR_STATE, "load_checkpoint: the file belongs to another configuration");
+  size_t need = size_t(fw::NF) * h.fstride * s->esz;
+  for (int f = 0; f < 6; ++f) need += size_t(h.aux_set[f]) * sizeof(float);
+  need += size_t(fw::NF) * h.nsamp * h.npt * sizeof(float) + size_t(6) * h.sgt_frames * h.sgt_npts * 4;
+  if (need != pay.size()) return s->fail(FWANT_ERR_INVALID_ARG, "load_checkpoint: section sizes disagree");
+  if (h.npt > 0) {
+    fwant_status rc = s->prepare_receivers(h.nsamp * h.tinv);
+    if (rc != FWANT_OK) return rc;
+  }
+  // W into set 0 (roles A = 0, T = 3), memory variables likewise
+  size_t o = 0;
+  auto put_dev = [&](void* d, size_t bytes) -> cudaError_t {
+    const cudaError_t e = bytes ? cudaMemcpy(d, pay.data() + o, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
+    o += bytes;
+    return e;
+  };
+  s->drop_graphs();
+  s->rA = 0; s->rT = 3;
+  cudaError_t e = put_dev(s->set(0), size_t(fw::NF) * h.fstride * s->esz);
+  for (int f = 0; f < 6 && e == cudaSuccess; ++f)
+    if (h.slab_on[f]) e = put_dev(s->aset(f, 0), size_t(h.aux_set[f]) * sizeof(float));
+  if (e == cudaSuccess && s->d_seis)
+    e = cudaMemset(s->d_seis, 0, size_t(fw::NF) * s->cap * s->npt * sizeof(float));
+  for (int c = 0; c < fw::NF && e == cudaSuccess; ++c)
+    e = put_dev(s->d_seis + size_t(c) * s->cap * s->npt, size_t(h.nsamp) * h.npt * sizeof(float));
+  if (e == cudaSuccess && h.sgt_on) e = cudaMemset(s->d_sgt, 0, size_t(6) * h.sgt_max_frames * h.sgt_npts * 4);
+  for (int c = 0; c < 6 && e == cudaSuccess && h.sgt_on; ++c)
+    e = put_dev(s->d_sgt + size_t(c) * h.sgt_max_frames * h.sgt_npts, size_t(h.sgt_frames) * h.sgt_npts * 4);
+  if (e == cudaSuccess) e = cudaMemcpy(s->d_ntime, &h.ntime, sizeof(int), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return s->cuda_fail(e, "load_checkpoint");
+  s->ntime = h.ntime;
+  s->cycle_pos = h.cycle_pos;
+  s->nsamp = h.nsamp;
+  s->sv = h.sv;
+  s->sc_t = h.st;
   return FWANT_OK;
 }
 

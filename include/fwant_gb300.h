@@ -167,6 +167,18 @@ fwant_status fwant_get_field(fwant_solver* s, int component, float* out);
  * Only the interior is taken; ghosts stay zero. */
 fwant_status fwant_set_field(fwant_solver* s, int component, const float* in);
 
+/* Checkpoint of the complete time-stepping state to a file: the wavefield, the CFS-PML
+ * memory variables (which the reference's restart files leave out, so its restarts are
+ * inexact inside the PML: io_rest_export, code/srcF/mod_io.F90:342-405), the step
+ * counters, the recorded seismograms and SGT frames; with a checksum.  The model
+ * (coordinates, metric, media, PML profile, sources, receivers) is not stored: load into a
+ * solver set up with the same inputs (io_rest_import, code/srcF/mod_io.F90:406-427).
+ * Loading checks the file (FWANT_ERR_INVALID_ARG: unreadable, truncated or corrupt) and
+ * the configuration (FWANT_ERR_STATE: another grid, storage, PML, receiver or SGT setup);
+ * a resumed run then gives the results of the uninterrupted run bit for bit. */
+fwant_status fwant_save_checkpoint(fwant_solver* s, const char* path);
+fwant_status fwant_load_checkpoint(fwant_solver* s, const char* path);
+
 /* Strided sub-volume of the current wavefield: the data one frame of the vel_/sgt_
  * snapshot files holds (io_wave_export, code/srcF/mod_io.F90:505-645).  subs: first point
  * (1-based Fortran indices with ghosts; the interior starts at 4), subc: points per axis,
