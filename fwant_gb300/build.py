@@ -34,6 +34,10 @@ SOURCES = ["stage_fast_rk0.cu", "stage_fast_rk1.cu", "stage_fast_rk2.cu", "stage
            "stage_dispatch.cu", "aux.cu", "snapshot.cu", "sgtker.cu", "surrogate.cu", "solver.cpp", "sgtker_api.cpp"]
 
 
+EXE = os.path.join(HERE, "bin", "fwant_wave")
+EXE_SOURCES = ["fwant_wave.cpp", "netcdf3.cpp", "conf.cpp"]
+
+
 def _nvcc() -> str:
     for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
         if cand and (os.path.sep not in cand or os.path.exists(cand)):
@@ -86,6 +90,12 @@ def build(verbose: bool = False, force: bool = False, jobs: int | None = None) -
             list(ex.map(lambda c: _run(c, verbose), jobs_todo))
     if force or jobs_todo or _stale(LIB, objs):
         _run([nvcc, "-shared", *ARCH, "-o", LIB, *objs, "-lcudart"], verbose)
+    # the solver-stage program (SeisFD3D.conf + NetCDF files in and out) over the C ABI
+    exe_src = [os.path.join(CSRC, f) for f in EXE_SOURCES]
+    if force or _stale(EXE, exe_src + hdrs + [LIB]):
+        os.makedirs(os.path.dirname(EXE), exist_ok=True)
+        _run(["g++", "-O2", "-std=c++17", "-Wall", "-I", CSRC, "-I", INCLUDE, *exe_src, "-o", EXE, "-L", LIB_DIR,
+              "-lfwant_gb300", "-Wl,-rpath,$ORIGIN/../lib"], verbose)
     return LIB
 
 

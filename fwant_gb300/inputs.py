@@ -300,3 +300,128 @@ def attach(solver, m: Model, metric: dict | None = None):
     if m.recv_indx.shape[0] > 0:
         solver.set_receivers(m.recv_indx, m.recv_tinv)
     return solver
+
+
+# ---- the reference's input files -----------------------------------------------------------
+SUFFIX = "mpi000000"
+
+
+def write_inputs(m: Model, root: str, metric: dict | None = None):
+    """Write a Model as the reference's one-rank input files (NetCDF classic, the schemas
+    of seis3d_grid/metric/media/source/station): coord_, metric_, media_, source_ and
+    station_mpi000000.nc in `root`.  The metric defaults to the FP64 formula rounded to
+    FP32 (seis3d_metric.F90:83-112 computed in double)."""
+    import os
+
+    from scipy.io import netcdf_file
+    os.makedirs(root, exist_ok=True)
+    f32 = np.float32
+
+    def grid_file(name, arrays):
+        with netcdf_file(os.path.join(root, f"{name}_{SUFFIX}.nc"), "w", version=1) as f:
+            f.createDimension("I", m.x.size)
+            f.createDimension("J", m.y.size)
+            f.createDimension("K", m.z.size)
+            for var, dim, a in arrays:
+                v = f.createVariable(var, "f4", (dim,))
+                v[:] = np.asarray(a, f32)
+
+    grid_file("coord", [("x", "I", m.x), ("y", "J", m.y), ("z", "K", m.z)])
+    if metric is None:
+        metric = metric_fp64(m.x, m.y, m.z)
+    grid_file("metric", [("xsin", "I", metric["xsin"]), ("xcot", "I", metric["xcot"]), ("xi_x", "I", metric["xi_x"]),
+                         ("eta_y", "J", metric["eta_y"]), ("zeta_z", "K", metric["zeta_z"])])
+    with netcdf_file(os.path.join(root, f"media_{SUFFIX}.nc"), "w", version=1) as f:
+        f.createDimension("I", m.x.size)
+        f.createDimension("J", m.y.size)
+        f.createDimension("K", m.z.size)
+        for var, a in (("lambda", m.lam), ("mu", m.mu), ("rho", m.rho)):
+            v = f.createVariable(var, "f4", ("K", "J", "I"))
+            v[:] = np.asarray(a, f32).transpose(2, 1, 0)
+    nf = int(m.force_indx.shape[0])
+    with netcdf_file(os.path.join(root, f"source_{SUFFIX}.nc"), "w", version=1) as f:
+        f.createDimension("geo_dimension", 3)
+        f.number_of_force = np.int32(nf)
+        f.number_of_moment = np.int32(0)
+        if nf > 0:
+            ntw = int(np.asarray(m.stf_time).size)
+            f.createDimension("force_point", nf)
+            f.createDimension("force_time_window", ntw)
+            for var, a in (("Fx", m.fx), ("Fy", m.fy), ("Fz", m.fz)):  # Fortran (ntwin, num)
+                v = f.createVariable(var, "f4", ("force_point", "force_time_window"))
+                v[:] = np.asarray(a, f32).reshape(nf, ntw)
+            v = f.createVariable("force_indx", "i4", ("force_point", "geo_dimension"))
+            v[:] = np.asarray(m.force_indx, np.int32)
+            v = f.createVariable("force_axis", "f4", ("force_point", "geo_dimension"))
+            v[:] = np.zeros((nf, 3), f32)
+            v = f.createVariable("force_shift", "f4", ("force_point", "geo_dimension"))
+            v[:] = np.asarray(m.force_shift, f32)
+            v = f.createVariable("force_start_time", "f4", ("force_point",))
+            v[:] = np.asarray(m.force_t0, f32)
+            v = f.createVariable("force_stf_time", "f4", ("force_time_window",))
+            v[:] = np.asarray(m.stf_time, f32)
+            v = f.createVariable("force_stf_freq", "f4", ("force_time_window",))
+            v[:] = np.asarray(m.stf_freq, f32)
+            f.force_stf_id = np.int32(m.stf_id)
+            f.force_stf_type = b"ricker" if m.stf_id == 200 else b"stf"
+    npt = int(m.recv_indx.shape[0])
+    with netcdf_file(os.path.join(root, f"station_{SUFFIX}.nc"), "w", version=1) as f:
+        f.createDimension("num_pt", None)
+        f.createDimension("geo_dim", 3)
+        f.createDimension("twoelem", 2)
+        for var, typ, a in (("indx", "i4", m.recv_indx), ("gindx", "i4", m.recv_indx),
+                            ("coord", "f4", np.zeros((npt, 3))), ("grid", "f4", m.recv_indx)):
+            v = f.createVariable(var, typ, ("num_pt", "geo_dim"))
+            v[:npt] = np.asarray(a).astype(typ)
+        v = f.createVariable("id", "i4", ("num_pt", "twoelem"))
+        v[:npt] = np.stack([np.arange(1, npt + 1), np.ones(npt, int)], axis=1).astype(np.int32)
+        f.tinv = np.int32(m.recv_tinv)
+        f.title = b"station"
+
+
+def metric_fp64(x, y, z):
+    """seis3d_metric (seis3d_metric.F90:83-112) evaluated in double from the FP32
+    coordinates and rounded to FP32: sin/cot of theta and the inverse of the mean of the
+    forward and backward MacCormack derivatives of each coordinate (edges copied into the
+    ghosts)."""
+    coe_f = np.array([-0.30874, -0.6326, 1.2330, -0.3334, 0.04168])
+    coe_b = np.array([-0.04168, 0.3334, -1.2330, 0.6326, 0.30874])
+
+    def one(g):
+        g = np.asarray(g, np.float32).astype(np.float64)
+        n = g.size
+        out = np.zeros(n)
+        for i in range(n):
+            ii = min(max(i, LENFD), n - 1 - LENFD)
+            sb = sum(g[ii - 3 + q] * coe_b[q] for q in range(5))
+            sf = sum(g[ii - 1 + q] * coe_f[q] for q in range(5))
+            out[i] = 1.0 / ((sb + sf) * 0.5)
+        return out.astype(np.float32)
+
+    xs = np.asarray(x, np.float32).astype(np.float64)
+    return {"xsin": np.sin(xs).astype(np.float32), "xcot": (1.0 / np.tan(xs)).astype(np.float32),
+            "xi_x": one(x), "eta_y": one(y), "zeta_z": one(z)}
+
+
+def write_conf(path: str, m: Model, nt: int, roots: dict, snaps=(), checkpoint_tinv=0, run_from_checkpoint=0):
+    """A SeisFD3D.conf for `m` with the keys the solver reads (para_init, io_init,
+    abs_init, io_snap_read).  roots: GRID_ROOT MEDIA_ROOT SOURCE_ROOT STATION_ROOT
+    OUTPUT_ROOT CHECKPOINT_ROOT.  snaps: (subs, subc, subt, tinv, tcnt, "V"|"T"|"TV") with
+    the reference's interior-relative indices (-1: first point / to the end, -2: surface)."""
+    n = [int(v) for v in m.pml_number]
+    lines = [f"ni = {m.ni}", f"nj = {m.nj}", f"nk = {m.nk}", f"nt = {int(nt)}", f"stept = {float(m.stept)!r}",
+             "dims = 1 1 1", "# PML: x1 x2 y1 y2 z1 z2",
+             "abs_number = " + " ".join(str(v) for v in n),
+             "abs_velocity = " + " ".join(repr(float(v)) for v in m.pml_velocity),
+             "CFS_bmax = " + " ".join(repr(float(v)) for v in m.pml_bmax),
+             "CFS_amax = " + " ".join(repr(float(v)) for v in m.pml_amax)]
+    for k in ("GRID_ROOT", "MEDIA_ROOT", "SOURCE_ROOT", "STATION_ROOT", "OUTPUT_ROOT", "CHECKPOINT_ROOT"):
+        if k in roots:
+            lines.append(f"{k} = {roots[k]}")
+    lines += [f"checkpoint_tinv = {int(checkpoint_tinv)}", f"run_from_checkpoint = {int(run_from_checkpoint)}",
+              f"number_of_snap = {len(snaps)}"]
+    for q, (subs, subc, subt, tinv, tcnt, var) in enumerate(snaps, start=1):
+        cols = " ".join(str(int(v)) for v in (*subs, *subc, *subt, tinv, tcnt))
+        lines.append(f"snap_{q:03d} = {cols} {var}   # subs subc subt tinv tcnt")
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
