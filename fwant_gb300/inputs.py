@@ -147,7 +147,7 @@ def gaussian_field(shape, x, y, z, corr_km, rng):
     ky = np.fft.fftfreq(ny, d=dy)[None, :, None]
     kz = np.fft.rfftfreq(nz, d=dz)[None, None, :]
     filt = np.exp(-(np.pi * corr_km) ** 2 * (kx ** 2 + ky ** 2 + kz ** 2) / 2.0)
-    f = np.fft.irfftn(np.fft.rfftn(noise) * filt, s=shape)
+    f = np.fft.irfftn(np.fft.rfftn(noise) * filt, s=shape, axes=(0, 1, 2))
     f -= f.mean()
     return f / max(f.std(), 1e-30)
 
