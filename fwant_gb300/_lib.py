@@ -72,6 +72,11 @@ EXPORTS = [
                                       C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                       C.POINTER(C.c_double)]),
     ("fwant_sgtker_last_scatter_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
+    ("fwant_sgtker_rotate", C.c_int, [_vp, C.POINTER(C.c_double)]),
+    ("fwant_sgtker_kernel_filtered", C.c_int, [_vp, C.c_int, _fp, _fp, C.c_int, C.c_int, C.c_double, C.c_int,
+                                               C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                               C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                               C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("fwant_autotune", C.c_int, [_vp, C.c_int, _ip]),
     ("fwant_batch_autotune", C.c_int, [_vp, C.c_int, _ip]),
     ("fwant_set_planes_per_cta", C.c_int, [_vp, C.c_int]),
@@ -83,6 +88,7 @@ EXPORTS = [
     ("fwant_batch_run", C.c_int, [_vp, C.c_int]),
     ("fwant_batch_last_run_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
     ("fwant_batch_profile_stages", C.c_int, [_vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("fwant_batch_launches_per_step", C.c_int, [_vp, C.POINTER(C.c_int)]),
     ("fwant_set_storage_scale", C.c_int, [_vp, C.c_float, C.c_float]),
     # surrogate kernels (include/fwant_surrogate.h): device pointers, a stream, cudaError_t
     ("fwant_nn_conv3d_fwd", C.c_int, [_vp, _vp, _vp, _vp] + [C.c_int] * 7 + [_vp]),
@@ -434,6 +440,12 @@ class Batch:
         self._chk(self._lib.fwant_batch_profile_stages(self._h, int(nsteps), st, C.byref(other)))
         return list(st), other.value
 
+    def launches_per_step(self):
+        """Kernels one step launches (counted by the last step enqueued)."""
+        v = C.c_int()
+        self._chk(self._lib.fwant_batch_launches_per_step(self._h, C.byref(v)))
+        return v.value
+
 
 class SgtKernel:
     """Sensitivity-kernel accumulation of one block of npts kernel points
@@ -484,13 +496,27 @@ class SgtKernel:
         self._chk(self._lib.fwant_sgtker_get_scatter(self._h, int(slot), _ptr(out, C.c_double)))
         return out.reshape(self.knt, self.npts)
 
-    def kernel(self, ncmp, v, u, nt1, nt2, sgt_m0):
-        """(phase_Vp, amplitude_Vp, phase_Vs, amplitude_Vs) as float64 arrays of npts."""
+    def kernel(self, ncmp, v, u, nt1, nt2, sgt_m0, filt=None):
+        """(phase_Vp, amplitude_Vp, phase_Vs, amplitude_Vs) as float64 arrays of npts.
+        filt: None or (mode, b, a) with mode 1 (one pass) or 2 (forward-backward)."""
         v_, u_ = _f32(v, self.knt), _f32(u, self.knt)
         outs = [np.zeros(self.npts, np.float64) for _ in range(4)]
-        self._chk(self._lib.fwant_sgtker_kernel(self._h, int(ncmp), _ptr(v_), _ptr(u_), int(nt1), int(nt2),
-                                                float(sgt_m0), *[_ptr(o, C.c_double) for o in outs]))
+        if filt is None:
+            self._chk(self._lib.fwant_sgtker_kernel(self._h, int(ncmp), _ptr(v_), _ptr(u_), int(nt1), int(nt2),
+                                                    float(sgt_m0), *[_ptr(o, C.c_double) for o in outs]))
+        else:
+            mode, b, a = filt
+            b_ = np.ascontiguousarray(b, np.float64)
+            a_ = np.ascontiguousarray(a, np.float64)
+            self._chk(self._lib.fwant_sgtker_kernel_filtered(
+                self._h, int(ncmp), _ptr(v_), _ptr(u_), int(nt1), int(nt2), float(sgt_m0), int(mode), int(b_.size),
+                _ptr(b_, C.c_double), _ptr(a_, C.c_double), *[_ptr(o, C.c_double) for o in outs]))
         return tuple(outs)
+
+    def rotate(self, rot):
+        """Rotate the three force components' series by the 3x3 matrix rot (rot[d, c])."""
+        r = np.ascontiguousarray(np.asarray(rot, np.float64).reshape(3, 3).T.reshape(-1))  # column-major
+        self._chk(self._lib.fwant_sgtker_rotate(self._h, _ptr(r, C.c_double)))
 
     def last_scatter_ms(self):
         ms = C.c_double()

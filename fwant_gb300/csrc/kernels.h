@@ -223,6 +223,22 @@ struct KernelArgs {
   double* kap; double* kaq; double* kbp; double* kbq;  // [npts]
 };
 void launch_scatter_kernel(const KernelArgs& a, void* stream);
+// IIR filtering of npts series of knt samples ([knt][npts] FP64) as scatter_filter (mode 1)
+// or scatter_filtfilt (mode 2) of SI_ker_sta.F90:1433-1558; nod1 coefficients b[], a[];
+// scratch holds (knt + 6 (nod1-1)) x npts doubles.
+struct IirArgs {
+  long long npts;
+  int knt, mode, nod1;
+  double b[16], a[16];
+  const double* in;
+  double* out;
+  double* scratch;
+};
+constexpr int IIR_MAX_COEF = 16;
+void launch_iir(const IirArgs& a, void* stream);
+// Rotation of the three force components of the series: slots (0,1,2) and (3,5,4),
+// new_c = sum_d rot[d + 3c] old_d (rot column-major, SI_ker_sta.F90:1339-1373).
+void launch_rotate_series(double* series, long long slot_len, const double rot[9], void* stream);
 
 void launch_metric_fp64(int n, const float* coord, float* metric_out, int lo, int hi, void* stream);
 void launch_sincot_fp64(int n, const float* x, float* xsin, float* xcot, void* stream);

@@ -139,7 +139,83 @@ __global__ void window_integral_kernel(const KernelArgs a) {
   a.kbq[p] = sbq / a.u0;
 }
 
+// One thread per point.  The padded series (NFACT = 3 NOD values reflected about the end
+// samples, or zeros in front for the one-pass filter) is generated on the fly; the forward
+// pass stores its output in scratch ([NEL][npts]), the backward pass of filtfilt reads it
+// in reverse and writes only the unpadded range.  Operands in the reference's order, no
+// contraction: y(n) = ((b1 x(n) + b2 x(n-1) - a2 y(n-1)) + ...) / a1.
+__global__ void iir_kernel(const IirArgs A) {
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= A.npts) return;
+  const int nod = A.nod1 - 1, nfact = 3 * nod, nt = A.knt, nel = nt + 2 * nfact;
+  const long long ld = A.npts;
+  const double* in = A.in + p;
+  auto x_at = [&](int n) -> double {  // 1-based padded input
+    if (n <= nfact) {
+      if (A.mode == 1) return 0.0;
+      return __dsub_rn(__dmul_rn(2.0, in[0]), in[(long long)(nfact + 1 - n) * ld]);
+    }
+    if (n <= nfact + nt) return in[(long long)(n - nfact - 1) * ld];
+    const int m = n - nfact - nt;
+    return __dsub_rn(__dmul_rn(2.0, in[(long long)(nt - 1) * ld]), in[(long long)(nt - 1 - m) * ld]);
+  };
+  double xs[IIR_MAX_COEF], ys[IIR_MAX_COEF];  // x(n-1..n-nod), y(n-1..n-nod)
+  for (int m = 0; m < IIR_MAX_COEF; ++m) xs[m] = ys[m] = 0.0;
+  double* scr = A.scratch + p;
+  double* out = A.out + p;
+  auto step = [&](double x, int n) -> double {
+    double y = __dmul_rn(A.b[0], x);
+    const int mm = min(nod + 1, n);
+    for (int m = 2; m <= mm; ++m) y = __dsub_rn(__dadd_rn(y, __dmul_rn(A.b[m - 1], xs[m - 2])), __dmul_rn(A.a[m - 1], ys[m - 2]));
+    y = __ddiv_rn(y, A.a[0]);
+    for (int m = nod - 1; m > 0; --m) { xs[m] = xs[m - 1]; ys[m] = ys[m - 1]; }
+    xs[0] = x;
+    ys[0] = y;
+    return y;
+  };
+  for (int n = 1; n <= nel; ++n) {
+    const double y = step(x_at(n), n);
+    if (A.mode == 1) {
+      if (n > nfact && n <= nfact + nt) out[(long long)(n - nfact - 1) * ld] = y;
+    } else {
+      scr[(long long)(n - 1) * ld] = y;
+    }
+  }
+  if (A.mode != 2) return;
+  for (int m = 0; m < IIR_MAX_COEF; ++m) xs[m] = ys[m] = 0.0;
+  for (int m = 1; m <= nel; ++m) {
+    const double y = step(scr[(long long)(nel - m) * ld], m);
+    const int n = nel + 1 - m;  // position in the final (reversed) series
+    if (n > nfact && n <= nfact + nt) out[(long long)(n - nfact - 1) * ld] = y;
+  }
+}
+
+__global__ void rotate_series_kernel(double* s, long long len, const double r0, const double r1, const double r2,
+                                     const double r3, const double r4, const double r5, const double r6,
+                                     const double r7, const double r8) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= len) return;
+  const double rot[9] = {r0, r1, r2, r3, r4, r5, r6, r7, r8};
+  const int slots[2][3] = {{0, 1, 2}, {3, 5, 4}};
+  for (int g = 0; g < 2; ++g) {
+    double v[3];
+    for (int d = 0; d < 3; ++d) v[d] = s[slots[g][d] * len + e];
+    for (int c = 0; c < 3; ++c)
+      s[slots[g][c] * len + e] =
+          __dadd_rn(__dadd_rn(__dmul_rn(v[0], rot[3 * c]), __dmul_rn(v[1], rot[3 * c + 1])), __dmul_rn(v[2], rot[3 * c + 2]));
+  }
+}
+
 }  // namespace
+
+void launch_iir(const IirArgs& a, void* stream) {
+  iir_kernel<<<(unsigned)((a.npts + 127) / 128), 128, 0, (cudaStream_t)stream>>>(a);
+}
+
+void launch_rotate_series(double* series, long long slot_len, const double rot[9], void* stream) {
+  rotate_series_kernel<<<(unsigned)((slot_len + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      series, slot_len, rot[0], rot[1], rot[2], rot[3], rot[4], rot[5], rot[6], rot[7], rot[8]);
+}
 
 int launch_sgt_scatter(const ScatterArgs& a, int /*sm_count*/, void* stream) {
   const size_t smem = sizeof(double) * SC_VALS * (SC_MCHUNK + SC_THREADS + SC_MCHUNK);

@@ -31,6 +31,9 @@ struct fwant_sgtker {
   int scatter_nt1 = 0, scatter_nt2 = 0, scatter_flags = 0;
   double* wts = nullptr;                                 // wv[knt], wu[knt]
   double* kout = nullptr;                                // 4 x [npts]
+  double* filtered = nullptr;                            // 2 x [knt][npts]: filtered Ka, Kb
+  double* iir_scratch = nullptr;                         // [knt + 6 nod][npts]
+  size_t iir_scratch_len = 0;
   bool have_media = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;
@@ -40,7 +43,7 @@ struct fwant_sgtker {
     cudaSetDevice(device);
     cudaFree(lam); cudaFree(mu);
     for (float* p : sgt) cudaFree(p);
-    cudaFree(series); cudaFree(wts); cudaFree(kout);
+    cudaFree(series); cudaFree(wts); cudaFree(kout); cudaFree(filtered); cudaFree(iir_scratch);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (st) cudaStreamDestroy(st);
@@ -195,20 +198,114 @@ fwant_status fwant_sgtker_get_scatter(fwant_sgtker* k, int slot, double* out) {
   return FWANT_OK;
 }
 
+namespace {
+// filter / filtfilt of SI_ker_sta.F90:1491-1558 on one host series (the synthetic V or U),
+// in double, operands in the reference's order
+std::vector<double> host_iir(const float* w0, int nt, int mode, int nod1, const double* b, const double* a) {
+  const int nod = nod1 - 1, nfact = 3 * nod, nel = nt + 2 * nfact;
+  std::vector<double> x(nel + 1), y(nel + 1), w(nel + 1);
+  for (int n = 1; n <= nt; ++n) x[nfact + n] = w0[n - 1];
+  for (int n = 1; n <= nfact; ++n) {
+    x[n] = mode == 1 ? 0.0 : 2.0 * x[nfact + 1] - x[2 * nfact + 1 - (n - 1)];
+    x[nel - nfact + n] = 2.0 * x[nel - nfact] - x[nel - nfact - n];
+  }
+  auto filter = [&](const std::vector<double>& in, std::vector<double>& out) {
+    for (int n = 1; n <= nel; ++n) {
+      double yy = b[0] * in[n];
+      for (int m = 2; m <= std::min(nod + 1, n); ++m) yy = (yy + b[m - 1] * in[n - m + 1]) - a[m - 1] * out[n - m + 1];
+      out[n] = yy / a[0];
+    }
+  };
+  filter(x, y);
+  if (mode == 2) {
+    for (int n = 1; n <= nel; ++n) w[n] = y[nel + 1 - n];
+    filter(w, x);
+    for (int n = 1; n <= nel; ++n) y[n] = x[nel + 1 - n];
+  }
+  return std::vector<double>(y.begin() + nfact + 1, y.begin() + nfact + 1 + nt);
+}
+}  // namespace
+
+fwant_status fwant_sgtker_rotate(fwant_sgtker* k, const double rot[9]) {
+  if (!k || !rot) return FWANT_ERR_INVALID_ARG;
+  if (!k->series || (k->scatter_flags & 7) != 7)
+    return k->fail(FWANT_ERR_STATE, "sgtker_rotate: the scatter of all three components is needed");
+  cudaSetDevice(k->device);
+  fw::launch_rotate_series(k->series, (long long)k->series_len(), rot, k->st);
+  cudaError_t e = cudaStreamSynchronize(k->st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return k->cuda_fail(e, "sgtker_rotate");
+  return FWANT_OK;
+}
+
+fwant_status fwant_sgtker_kernel_filtered(fwant_sgtker* k, int ncmp, const float* v, const float* u, int nt1,
+                                          int nt2, double sgt_m0, int mode, int nod1, const double* b,
+                                          const double* a, double* kap, double* kaq, double* kbp, double* kbq);
+
 fwant_status fwant_sgtker_kernel(fwant_sgtker* k, int ncmp, const float* v, const float* u, int nt1, int nt2,
                                  double sgt_m0, double* kap, double* kaq, double* kbp, double* kbq) {
+  return fwant_sgtker_kernel_filtered(k, ncmp, v, u, nt1, nt2, sgt_m0, 0, 0, nullptr, nullptr, kap, kaq, kbp, kbq);
+}
+
+fwant_status fwant_sgtker_kernel_filtered(fwant_sgtker* k, int ncmp, const float* v, const float* u, int nt1,
+                                          int nt2, double sgt_m0, int mode, int nod1, const double* b,
+                                          const double* a, double* kap, double* kaq, double* kbp, double* kbq) {
   if (!k || !v || !u || !kap || !kaq || !kbp || !kbq) return FWANT_ERR_INVALID_ARG;
+  if (mode < 0 || mode > 2) return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_kernel: filter mode must be 0, 1 or 2");
+  if (mode != 0 && (!b || !a || nod1 < 1 || nod1 > fw::IIR_MAX_COEF || !(a[0] != 0.0)))
+    return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_kernel: filter needs 1..16 coefficients with a[0] != 0");
+  // the reflected padding of 3 (order) samples at each end lies inside the series
+  if (mode != 0 && k->knt <= 3 * (nod1 - 1))
+    return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_kernel: series shorter than the filter padding");
   if (ncmp < 1 || ncmp > 3) return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_kernel: ncmp must be 1, 2 or 3");
   if (!k->series || !(k->scatter_flags >> (ncmp - 1) & 1))
     return k->fail(FWANT_ERR_STATE, "sgtker_kernel: scatter of this component not computed");
   if (nt1 < k->scatter_nt1 || nt2 > k->scatter_nt2 || nt1 > nt2)
     return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_kernel: window outside the scatter range");
+  // filtering of the synthetics (syn_filter / syn_filtfilt) and of the two series
+  // (scatter_filter / scatter_filtfilt), SI_ker_sta.F90:756-773
+  static const int slot_a[3] = {0, 1, 2}, slot_b[3] = {3, 5, 4};
+  const double* ser_a = k->series + size_t(slot_a[ncmp - 1]) * k->series_len();
+  const double* ser_b = k->series + size_t(slot_b[ncmp - 1]) * k->series_len();
+  std::vector<double> vd(k->knt), ud(k->knt);
+  if (mode != 0) {
+    const std::vector<double> fv = host_iir(v, k->knt, mode, nod1, b, a), fu = host_iir(u, k->knt, mode, nod1, b, a);
+    vd = fv;
+    ud = fu;
+    cudaSetDevice(k->device);
+    const size_t nel = size_t(k->knt) + 6 * size_t(nod1 - 1);
+    fwant_status rc = k->alloc(&k->filtered, 2 * k->series_len(), "filtered series");
+    if (rc != FWANT_OK) return rc;
+    if (k->iir_scratch_len < nel * size_t(k->npts)) {
+      cudaFree(k->iir_scratch);
+      k->iir_scratch = nullptr;
+      k->iir_scratch_len = 0;
+      if ((rc = k->alloc(&k->iir_scratch, nel * size_t(k->npts), "filter scratch")) != FWANT_OK) return rc;
+      k->iir_scratch_len = nel * size_t(k->npts);
+    }
+    fw::IirArgs ia{};
+    ia.npts = k->npts;
+    ia.knt = k->knt;
+    ia.mode = mode;
+    ia.nod1 = nod1;
+    for (int q = 0; q < nod1; ++q) { ia.b[q] = b[q]; ia.a[q] = a[q]; }
+    ia.scratch = k->iir_scratch;
+    for (int s = 0; s < 2; ++s) {
+      ia.in = s == 0 ? ser_a : ser_b;
+      ia.out = k->filtered + size_t(s) * k->series_len();
+      fw::launch_iir(ia, k->st);
+    }
+    ser_a = k->filtered;
+    ser_b = k->filtered + k->series_len();
+  } else {
+    for (int n = 0; n < k->knt; ++n) { vd[n] = v[n]; ud[n] = u[n]; }
+  }
   // normalisation (SI_ker_sta.F90:1397-1402): trapezoid integral of V^2 and U^2 times SGT_M0
   const double dt = k->kdt;
-  const double v1 = v[nt1 - 1], v2 = v[nt2 - 1], u1 = u[nt1 - 1], u2 = u[nt2 - 1];
+  const double v1 = vd[nt1 - 1], v2 = vd[nt2 - 1], u1 = ud[nt1 - 1], u2 = ud[nt2 - 1];
   double v0 = (0.5 * v1 * v1 + 0.5 * v2 * v2) * dt, u0 = (0.5 * u1 * u1 + 0.5 * u2 * u2) * dt;
   for (int n = nt1 + 1; n <= nt2 - 1; ++n) {
-    const double vn = v[n - 1], un = u[n - 1];
+    const double vn = vd[n - 1], un = ud[n - 1];
     v0 += vn * vn * dt;
     u0 += un * un * dt;
   }
@@ -218,29 +315,28 @@ fwant_status fwant_sgtker_kernel(fwant_sgtker* k, int ncmp, const float* v, cons
   std::vector<double> w(2 * size_t(k->knt), 0.0);
   for (int n = nt1; n <= nt2; ++n) {
     const double wt = (n == nt1 || n == nt2) ? 0.5 * dt : dt;
-    w[n - 1] = wt * double(v[n - 1]);
-    w[k->knt + n - 1] = wt * double(u[n - 1]);
+    w[n - 1] = wt * vd[n - 1];
+    w[k->knt + n - 1] = wt * ud[n - 1];
   }
   cudaSetDevice(k->device);
   fwant_status rc = k->alloc(&k->wts, 2 * size_t(k->knt), "weights");
   if (rc == FWANT_OK) rc = k->alloc(&k->kout, 4 * size_t(k->npts), "kernels");
   if (rc != FWANT_OK) return rc;
   cudaError_t e = cudaMemcpyAsync(k->wts, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, k->st);
-  static const int slot_a[3] = {0, 1, 2}, slot_b[3] = {3, 5, 4};
-  fw::KernelArgs a{};
-  a.npts = k->npts;
-  a.knt = k->knt;
-  a.nt1 = nt1;
-  a.nt2 = nt2;
-  a.ka = k->series + size_t(slot_a[ncmp - 1]) * k->series_len();
-  a.kb = k->series + size_t(slot_b[ncmp - 1]) * k->series_len();
-  a.wv = k->wts;
-  a.wu = k->wts + k->knt;
-  a.v0 = v0;
-  a.u0 = u0;
+  fw::KernelArgs ka{};
+  ka.npts = k->npts;
+  ka.knt = k->knt;
+  ka.nt1 = nt1;
+  ka.nt2 = nt2;
+  ka.ka = ser_a;
+  ka.kb = ser_b;
+  ka.wv = k->wts;
+  ka.wu = k->wts + k->knt;
+  ka.v0 = v0;
+  ka.u0 = u0;
   const size_t np = size_t(k->npts);
-  a.kap = k->kout; a.kaq = k->kout + np; a.kbp = k->kout + 2 * np; a.kbq = k->kout + 3 * np;
-  fw::launch_scatter_kernel(a, k->st);
+  ka.kap = k->kout; ka.kaq = k->kout + np; ka.kbp = k->kout + 2 * np; ka.kbq = k->kout + 3 * np;
+  fw::launch_scatter_kernel(ka, k->st);
   double* dst[4] = {kap, kaq, kbp, kbq};
   for (int q = 0; q < 4 && e == cudaSuccess; ++q)
     e = cudaMemcpyAsync(dst[q], k->kout + q * np, np * sizeof(double), cudaMemcpyDeviceToHost, k->st);

@@ -699,9 +699,11 @@ struct fwant_solver {
     q.w = set(rt);
     return q;
   }
-  void enqueue_step_end(cudaStream_t stream) const {
+  // Returns the number of kernels launched.
+  int enqueue_step_end(cudaStream_t stream) const {
     fw::launch_advance_record(recv_args(rT), stream);
     if (sgt_on) fw::launch_record_sgt(sgt_args(rT), stream);
+    return sgt_on ? 2 : 1;
   }
   // Bytes of every launch argument of a step for both register-role assignments: equal
   // signatures mean a captured graph of this simulation's launches is still valid.
@@ -1558,6 +1560,7 @@ struct fwant_batch {
   std::vector<unsigned char> graph_sig;      // launch arguments the graphs were captured with
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;
+  int launches_per_step = 0;                 // kernels of the last enqueued step
   std::string err;
 
   ~fwant_batch() {
@@ -1602,7 +1605,7 @@ struct fwant_batch {
   // step-end kernels.
   int enqueue_step(cudaEvent_t* ev = nullptr) {
     fwant_solver* s0 = sims[0];
-    int lerr = 0;
+    int lerr = 0, nlaunch = 0;
     static thread_local fw::BatchArgs b;  // 30 KB: kept off the stack
     for (int s = 0; s < 4; ++s) {
       if (ev) cudaEventRecord(ev[s], st);
@@ -1616,11 +1619,13 @@ struct fwant_batch {
                                                 fwant_solver::stage_rk(s), s0->cfg.exact_arith, s0->stor, lean,
                                                 std::max(1, nct), st);
           if (le && !lerr) lerr = le;
+          ++nlaunch;
         }
       }
     }
     if (ev) cudaEventRecord(ev[4], st);
-    for (fwant_solver* m : sims) m->enqueue_step_end(st);
+    for (fwant_solver* m : sims) nlaunch += m->enqueue_step_end(st);
+    launches_per_step = nlaunch;
     if (ev) cudaEventRecord(ev[5], st);
     for (fwant_solver* m : sims) m->finish_step_host();
     return lerr;
@@ -1846,6 +1851,12 @@ fwant_status fwant_batch_profile_stages(fwant_batch* b, int nsteps, double* stag
 fwant_status fwant_batch_last_run_ms(fwant_batch* b, double* ms) {
   if (!b || !ms) return FWANT_ERR_INVALID_ARG;
   *ms = b->last_ms;
+  return FWANT_OK;
+}
+
+fwant_status fwant_batch_launches_per_step(fwant_batch* b, int* n) {
+  if (!b || !n) return FWANT_ERR_INVALID_ARG;
+  *n = b->launches_per_step;
   return FWANT_OK;
 }
 

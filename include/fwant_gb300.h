@@ -262,6 +262,20 @@ fwant_status fwant_sgtker_get_scatter(fwant_sgtker* k, int slot, double* out);
  * amplitude_Vs of the kernel file. */
 fwant_status fwant_sgtker_kernel(fwant_sgtker* k, int ncmp, const float* v, const float* u, int nt1, int nt2,
                                  double sgt_m0, double* kap, double* kaq, double* kbp, double* kbq);
+/* scatter_rotate + syn_rotate (SI_ker_sta.F90:1339-1373, used for the reference's ncmp 4-6):
+ * replace the series of the three force components by their rotation, for Ka (slots 0 1 2)
+ * and Kb (slots 3 5 4): new_c = sum_d old_d rot(d,c), rot column-major 3x3 (rot_mat).
+ * Needs the scatter of all three components; rotate the synthetics the same way before
+ * passing them to fwant_sgtker_kernel. */
+fwant_status fwant_sgtker_rotate(fwant_sgtker* k, const double rot[9]);
+/* fwant_sgtker_kernel with the pick's band filter applied first (SI_ker_sta.F90:756-773):
+ * mode 0 none, 1 one-pass IIR (scatter_filter / syn_filter, zero padding in front), 2
+ * zero-phase forward-backward IIR (scatter_filtfilt / syn_filtfilt, 3(nod1-1) samples
+ * reflected about each end); b[nod1], a[nod1] the coefficients of the filter file
+ * (nod1 <= 16).  The series are filtered on the device in FP64, V and U on the host. */
+fwant_status fwant_sgtker_kernel_filtered(fwant_sgtker* k, int ncmp, const float* v, const float* u, int nt1,
+                                          int nt2, double sgt_m0, int mode, int nod1, const double* b,
+                                          const double* a, double* kap, double* kaq, double* kbp, double* kbq);
 /* Device time of the last fwant_sgtker_scatter in milliseconds.  No counterpart in the
  * reference. */
 fwant_status fwant_sgtker_last_scatter_ms(fwant_sgtker* k, double* ms);
@@ -330,6 +344,9 @@ fwant_status fwant_batch_autotune(fwant_batch* b, int trial_steps, int* ctas);
 /* fwant_profile_stages for a batch: eager steps with events around each stage's launches
  * (stage_ms[4]: all members' launches of that stage) and the step-end kernels. */
 fwant_status fwant_batch_profile_stages(fwant_batch* b, int nsteps, double* stage_ms, double* other_ms);
+/* Kernels one step of the batch launches (stage launches of the interior-only and full
+ * forms, step-end kernels), as counted by the last step enqueued; 0 before the first. */
+fwant_status fwant_batch_launches_per_step(fwant_batch* b, int* n);
 
 #ifdef __cplusplus
 }

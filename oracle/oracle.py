@@ -48,12 +48,15 @@ _SIGS = [
     ("orc_metric", None, [C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, _fp, _fp, _fp, _fp, _fp]),
     ("orc_metric_dp", None, [C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, _fp, _fp, _fp, _fp, _fp]),
     ("orc_op", C.c_double, [C.c_int, C.c_int, _dp, C.c_int]),
+    ("orc_iir", None, [_dp, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]),
     ("orc_metric_dd", None, [C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, _dp, _dp, _dp, _dp, _dp]),
     ("orc_stress2strain", None, [C.c_longlong, C.c_int, _fp, _fp, _fp, _fp]),
     ("orc_sgt2scatter3", None, [C.c_longlong, C.c_int, C.c_int, C.c_int, C.c_double, _fp, _fp, _fp, _fp, _fp, _fp,
                                 C.c_int, _dp]),
     ("orc_scatter2kernel", None, [C.c_longlong, C.c_int, C.c_int, C.c_int, C.c_double, _fp, _fp, _dp, _dp,
                                   C.c_double, C.c_int, _dp, _dp, _dp, _dp]),
+    ("orc_scatter2kernel_dv", None, [C.c_longlong, C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp, _dp, _dp,
+                                     C.c_double, _dp, _dp, _dp, _dp]),
 ]
 
 
@@ -132,6 +135,21 @@ def sgt2scatter3(lam, mu, rsgt, ssgt, dt, nt1=None, nt2=None, mode=1):
     return out.reshape(6, knt, npts)
 
 
+def iir(series, b, a, mode):
+    """filter (mode 1) / filtfilt (mode 2) of SI_ker_sta along axis 0 of a (nt, ...) array."""
+    s = np.asarray(series, np.float64)
+    nt = s.shape[0]
+    flat = s.reshape(nt, -1)
+    out = np.zeros_like(flat)
+    b_, a_ = _d(b), _d(a)
+    for q in range(flat.shape[1]):
+        col = np.ascontiguousarray(flat[:, q])
+        o = np.zeros(nt)
+        lib().orc_iir(_p(col), nt, int(mode), b_.size, _p(b_), _p(a_), _p(o))
+        out[:, q] = o
+    return out.reshape(s.shape)
+
+
 def scatter2kernel(v, u, ka, kb, dt, nt1, nt2, sgt_m0, mode=1):
     """Window kernels (phase_Vp, amplitude_Vp, phase_Vs, amplitude_Vs) of series ka, kb
     ((knt, npts) float64) against V and U over frames nt1..nt2 (1-based)."""
@@ -142,6 +160,20 @@ def scatter2kernel(v, u, ka, kb, dt, nt1, nt2, sgt_m0, mode=1):
     outs = [np.zeros(npts, np.float64) for _ in range(4)]
     lib().orc_scatter2kernel(npts, knt, int(nt1), int(nt2), float(dt), _p(v_, C.c_float), _p(u_, C.c_float),
                              _p(ka_), _p(kb_), float(sgt_m0), int(mode), *[_p(o) for o in outs])
+    return tuple(outs)
+
+
+def scatter2kernel_filtered(v, u, ka, kb, dt, nt1, nt2, sgt_m0, b, a, mode):
+    """scatter2kernel after filtering (mode 1 filter, mode 2 filtfilt) of the synthetics V,
+    U and of the two series ka, kb along time (SI_ker_sta.F90:756-773), FP64 throughout."""
+    fv = _d(iir(np.asarray(v, np.float32).astype(np.float64), b, a, mode))
+    fu = _d(iir(np.asarray(u, np.float32).astype(np.float64), b, a, mode))
+    fa = _d(iir(ka, b, a, mode))
+    fb = _d(iir(kb, b, a, mode))
+    knt, npts = np.asarray(ka).shape
+    outs = [np.zeros(npts, np.float64) for _ in range(4)]
+    lib().orc_scatter2kernel_dv(npts, knt, int(nt1), int(nt2), float(dt), _p(fv), _p(fu), _p(fa), _p(fb),
+                                float(sgt_m0), *[_p(o) for o in outs])
     return tuple(outs)
 
 

@@ -129,6 +129,45 @@ void orc_sgt2scatter3(long long npts, int knt, int nt1, int nt2, double dt, cons
   }
 }
 
+// FP64 accumulation of scatter2kernel (SI_ker_sta.F90:1375-1431): trapezoid weights
+// times the synthetic, one fma per frame in the order nt1, nt2, nt1+1 .. nt2-1.
+extern "C++" {
+template <typename T>
+static void scatter2kernel_fp64(long long npts, int nt1, int nt2, double dt, const T* v, const T* u, const double* ka,
+                                const double* kb, double sgt_m0, double* kap, double* kaq, double* kbp, double* kbq) {
+  const double v1 = v[nt1 - 1], v2 = v[nt2 - 1], u1 = u[nt1 - 1], u2 = u[nt2 - 1];
+  double v0 = (0.5 * v1 * v1 + 0.5 * v2 * v2) * dt, u0 = (0.5 * u1 * u1 + 0.5 * u2 * u2) * dt;
+  for (int n = nt1 + 1; n <= nt2 - 1; ++n) {
+    const double vn = v[n - 1], un = u[n - 1];
+    v0 += vn * vn * dt;
+    u0 += un * un * dt;
+  }
+  v0 *= sgt_m0;
+  u0 *= sgt_m0;
+  auto wv = [&](int n) { return ((n == nt1 || n == nt2) ? 0.5 * dt : dt) * double(v[n - 1]); };
+  auto wu = [&](int n) { return ((n == nt1 || n == nt2) ? 0.5 * dt : dt) * double(u[n - 1]); };
+#pragma omp parallel for schedule(static)
+  for (long long p = 0; p < npts; ++p) {
+    double sap = 0.0, saq = 0.0, sbp = 0.0, sbq = 0.0;
+    auto add = [&](int n) {
+      const double a = ka[size_t(n - 1) * size_t(npts) + size_t(p)];
+      const double b = kb[size_t(n - 1) * size_t(npts) + size_t(p)];
+      sap = std::fma(wv(n), a, sap);
+      saq = std::fma(wu(n), a, saq);
+      sbp = std::fma(wv(n), b, sbp);
+      sbq = std::fma(wu(n), b, sbq);
+    };
+    add(nt1);
+    add(nt2);
+    for (int n = nt1 + 1; n < nt2; ++n) add(n);
+    kap[p] = sap / v0;
+    kaq[p] = saq / u0;
+    kbp[p] = sbp / v0;
+    kbq[p] = sbq / u0;
+  }
+}
+}  // extern "C++"
+
 // scatter2kernel over frames nt1..nt2 (1-based) of the series ka, kb ([knt][npts]).
 void orc_scatter2kernel(long long npts, int knt, int nt1, int nt2, double dt, const float* v, const float* u,
                         const double* ka, const double* kb, double sgt_m0, int mode, double* kap, double* kaq,
@@ -166,36 +205,49 @@ void orc_scatter2kernel(long long npts, int knt, int nt1, int nt2, double dt, co
     }
     return;
   }
-  const double v1 = v[nt1 - 1], v2 = v[nt2 - 1], u1 = u[nt1 - 1], u2 = u[nt2 - 1];
-  double v0 = (0.5 * v1 * v1 + 0.5 * v2 * v2) * dt, u0 = (0.5 * u1 * u1 + 0.5 * u2 * u2) * dt;
-  for (int n = nt1 + 1; n <= nt2 - 1; ++n) {
-    const double vn = v[n - 1], un = u[n - 1];
-    v0 += vn * vn * dt;
-    u0 += un * un * dt;
+  scatter2kernel_fp64(npts, nt1, nt2, dt, v, u, ka, kb, sgt_m0, kap, kaq, kbp, kbq);
+}
+
+// scatter2kernel with the synthetics already in double (after filter / filtfilt), FP64
+// accumulation as in mode 1 of orc_scatter2kernel.
+void orc_scatter2kernel_dv(long long npts, int knt, int nt1, int nt2, double dt, const double* v, const double* u,
+                           const double* ka, const double* kb, double sgt_m0, double* kap, double* kaq, double* kbp,
+                           double* kbq) {
+  (void)knt;
+  scatter2kernel_fp64(npts, nt1, nt2, dt, v, u, ka, kb, sgt_m0, kap, kaq, kbp, kbq);
+}
+
+// filter (mode 1) / filtfilt (mode 2) of SI_ker_sta.F90:1433-1558 on one series of nt
+// samples, double arithmetic in the reference's operand order, padding of NFACT = 3 NOD
+// samples at each end (zeros in front for the one-pass filter, reflections otherwise).
+void orc_iir(const double* w0, int nt, int mode, int nod1, const double* b, const double* a, double* out) {
+  const int nod = nod1 - 1, nfact = 3 * nod, nel = nt + 2 * nfact;
+  double* x = new double[nel + 1];
+  double* y = new double[nel + 1];
+  double* w = new double[nel + 1];
+  for (int n = 1; n <= nt; ++n) x[nfact + n] = w0[n - 1];
+  for (int n = 1; n <= nfact; ++n) {
+    x[n] = mode == 1 ? 0.0 : 2.0 * x[nfact + 1] - x[2 * nfact + 1 - (n - 1)];
+    x[nel - nfact + n] = 2.0 * x[nel - nfact] - x[nel - nfact - n];
   }
-  v0 *= sgt_m0;
-  u0 *= sgt_m0;
-  auto wv = [&](int n) { return ((n == nt1 || n == nt2) ? 0.5 * dt : dt) * double(v[n - 1]); };
-  auto wu = [&](int n) { return ((n == nt1 || n == nt2) ? 0.5 * dt : dt) * double(u[n - 1]); };
-#pragma omp parallel for schedule(static)
-  for (long long p = 0; p < npts; ++p) {
-    double sap = 0.0, saq = 0.0, sbp = 0.0, sbq = 0.0;
-    auto add = [&](int n) {
-      const double a = ka[size_t(n - 1) * size_t(npts) + size_t(p)];
-      const double b = kb[size_t(n - 1) * size_t(npts) + size_t(p)];
-      sap = std::fma(wv(n), a, sap);
-      saq = std::fma(wu(n), a, saq);
-      sbp = std::fma(wv(n), b, sbp);
-      sbq = std::fma(wu(n), b, sbq);
-    };
-    add(nt1);
-    add(nt2);
-    for (int n = nt1 + 1; n < nt2; ++n) add(n);
-    kap[p] = sap / v0;
-    kaq[p] = saq / u0;
-    kbp[p] = sbp / v0;
-    kbq[p] = sbq / u0;
+  auto filter = [&](const double* in, double* o) {
+    for (int n = 1; n <= nel; ++n) {
+      double yy = b[0] * in[n];
+      const int mm = nod + 1 < n ? nod + 1 : n;
+      for (int m = 2; m <= mm; ++m) yy = (yy + b[m - 1] * in[n - m + 1]) - a[m - 1] * o[n - m + 1];
+      o[n] = yy / a[0];
+    }
+  };
+  filter(x, y);
+  if (mode == 2) {
+    for (int n = 1; n <= nel; ++n) w[n] = y[nel + 1 - n];
+    filter(w, x);
+    for (int n = 1; n <= nel; ++n) y[n] = x[nel + 1 - n];
   }
+  for (int n = 1; n <= nt; ++n) out[n - 1] = y[nfact + n];
+  delete[] x;
+  delete[] y;
+  delete[] w;
 }
 
 }  // extern "C"

@@ -172,3 +172,80 @@ def test_recorded_sgt_equals_snapshots_and_feeds_the_kernel(oracle_mod, native_l
     with pytest.raises(fw.FwantError) as e:
         short.take_sgt(0, sims[0][0])
     assert e.value.code == 6
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_filtered_kernels_bitwise(mode, oracle_mod, native_lib):
+    """Filtering of the synthetics and of the two series before the window integral
+    (SI_ker_sta.F90:756-773; filter / filtfilt :1433-1558): the device filter of every
+    point's series and the host filter of V, U equal the restatement bit for bit."""
+    import fwant_gb300 as fw
+    signal = pytest.importorskip("scipy.signal")
+    b, a = signal.butter(3, [0.04, 0.3], btype="band")  # 7 coefficients: 18 padding samples
+    rng = np.random.default_rng(40 + mode)
+    npts, knt, dt, nt1, nt2 = 131, 300, 0.1, 21, 280  # 131 points: a partial block of 128
+    lam, mu = _media(rng, npts)
+    r = [_series(rng, npts, knt) for _ in range(3)]
+    s = _series(rng, npts, knt)
+    k = fw.SgtKernel(npts, knt, dt)
+    k.set_media(lam, mu)
+    for c in range(3):
+        k.set_sgt(c, r[c])
+    k.set_sgt(3, s)
+    k.scatter(7)
+    scat = oracle_mod.sgt2scatter3(lam, mu, r, s, dt, mode=1)
+    v = rng.normal(size=knt).astype(np.float32)
+    u = np.cumsum(v).astype(np.float32) * np.float32(dt)
+    for ncmp, (sa, sb) in ((1, (0, 3)), (2, (1, 5)), (3, (2, 4))):
+        got = k.kernel(ncmp, v, u, nt1, nt2, 1.0e16, filt=(mode, b, a))
+        want = oracle_mod.scatter2kernel_filtered(v, u, scat[sa], scat[sb], dt, nt1, nt2, 1.0e16, b, a, mode)
+        for g, w in zip(got, want):
+            np.testing.assert_array_equal(g, w)
+        plain = k.kernel(ncmp, v, u, nt1, nt2, 1.0e16)
+        assert not np.allclose(plain[0], got[0], rtol=1e-3, atol=0.0)  # the filter changed the kernel
+    # the unfiltered series are kept: a plain call after a filtered one is unchanged
+    np.testing.assert_array_equal(k.kernel(1, v, u, nt1, nt2, 1.0e16)[0],
+                                  oracle_mod.scatter2kernel(v, u, scat[0], scat[3], dt, nt1, nt2, 1.0e16, mode=1)[0])
+    for bad in ((3, b, a), (1, np.ones(17), np.ones(17)), (1, b, np.r_[0.0, a[1:]])):
+        with pytest.raises(fw.FwantError) as e:
+            k.kernel(1, v, u, nt1, nt2, 1.0e16, filt=bad)
+        assert e.value.code == 1
+    short = fw.SgtKernel(npts, 18, dt)  # 18 frames: not more than the 18 padding samples
+    short.set_media(lam, mu)
+    for c in range(4):
+        short.set_sgt(c if c < 3 else 3, np.ascontiguousarray((r[c] if c < 3 else s)[:, :18]))
+    short.scatter(1)
+    with pytest.raises(fw.FwantError) as e:
+        short.kernel(1, v[:18], u[:18], 1, 18, 1.0e16, filt=(mode, b, a))
+    assert e.value.code == 1
+
+
+def test_rotation_of_the_force_components(oracle_mod, native_lib):
+    """scatter_rotate (SI_ker_sta.F90:1357-1373): the three force components' series mixed
+    by the rotation matrix, rot(d, c) weighting component d into c, summed in order."""
+    import fwant_gb300 as fw
+    rng = np.random.default_rng(77)
+    npts, knt, dt = 40, 90, 0.2
+    lam, mu = _media(rng, npts)
+    r = [_series(rng, npts, knt) for _ in range(3)]
+    s = _series(rng, npts, knt)
+    k = fw.SgtKernel(npts, knt, dt)
+    k.set_media(lam, mu)
+    for c in range(3):
+        k.set_sgt(c, r[c])
+    k.set_sgt(3, s)
+    k.scatter(3)
+    with pytest.raises(fw.FwantError) as e:
+        k.rotate(np.eye(3))  # Z not computed
+    assert e.value.code == 6
+    k.scatter(7)
+    th = 0.7
+    rot = np.array([[np.cos(th), np.sin(th), 0.0], [-np.sin(th), np.cos(th), 0.0], [0.0, 0.0, 1.0]])
+    rot = rot @ np.array([[1.0, 0.0, 0.0], [0.0, np.cos(0.3), -np.sin(0.3)], [0.0, np.sin(0.3), np.cos(0.3)]])
+    before = [k.get_scatter(q) for q in range(6)]
+    k.rotate(rot)
+    for group in ((0, 1, 2), (3, 5, 4)):
+        v = [before[q] for q in group]
+        for c in range(3):
+            want = (v[0] * rot[0, c] + v[1] * rot[1, c]) + v[2] * rot[2, c]
+            np.testing.assert_array_equal(k.get_scatter(group[c]), want)

@@ -143,3 +143,29 @@ def test_scatter2kernel_trapezoid(nt1, nt2, oracle_mod):
                                     kb.astype(np.float32).astype(np.float64), dt, nt1, nt2, m0, mode=0)
     for g, ww in zip(ref, want):
         assert np.linalg.norm(g - ww) / np.linalg.norm(ww) < 1e-5
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_iir_against_lfilter(mode, oracle_mod):
+    """filter/filtfilt restated against scipy.signal.lfilter on the reference's padded
+    series (zero initial conditions; scipy's own filtfilt pads differently).  The restatement
+    evaluates the difference equation in direct form I as the reference does, lfilter in
+    transposed direct form II: the order-8 band-pass's poles near the unit circle amplify
+    their different roundings to ~1e-11 of the signal, hence the tolerance."""
+    signal = pytest.importorskip("scipy.signal")
+    b, a = signal.butter(4, [0.05, 0.2], btype="band")
+    rng = np.random.default_rng(mode)
+    nt = 180
+    x = rng.normal(size=(nt, 3))
+    got = oracle_mod.iir(x, b, a, mode)
+    nod = b.size - 1
+    nf = 3 * nod
+    for q in range(3):
+        w = x[:, q]
+        left = np.zeros(nf) if mode == 1 else 2 * w[0] - w[nf:0:-1]
+        right = 2 * w[-1] - w[-2:-nf - 2:-1]
+        xp = np.concatenate([left, w, right])
+        y = signal.lfilter(b, a, xp)
+        if mode == 2:
+            y = signal.lfilter(b, a, y[::-1])[::-1]
+        np.testing.assert_allclose(got[:, q], y[nf:nf + nt], rtol=0, atol=1e-9 * np.abs(y).max())
