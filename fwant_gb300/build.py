@@ -36,6 +36,8 @@ SOURCES = ["stage_fast_rk0.cu", "stage_fast_rk1.cu", "stage_fast_rk2.cu", "stage
 
 EXE = os.path.join(HERE, "bin", "fwant_wave")
 EXE_SOURCES = ["fwant_wave.cpp", "netcdf3.cpp", "conf.cpp"]
+KER_EXE = os.path.join(HERE, "bin", "fwant_ker")
+KER_SOURCES = ["fwant_ker.cpp", "netcdf3.cpp", "conf.cpp"]
 
 
 def _nvcc() -> str:
@@ -90,12 +92,14 @@ def build(verbose: bool = False, force: bool = False, jobs: int | None = None) -
             list(ex.map(lambda c: _run(c, verbose), jobs_todo))
     if force or jobs_todo or _stale(LIB, objs):
         _run([nvcc, "-shared", *ARCH, "-o", LIB, *objs, "-lcudart"], verbose)
-    # the solver-stage program (SeisFD3D.conf + NetCDF files in and out) over the C ABI
-    exe_src = [os.path.join(CSRC, f) for f in EXE_SOURCES]
-    if force or _stale(EXE, exe_src + hdrs + [LIB]):
-        os.makedirs(os.path.dirname(EXE), exist_ok=True)
-        _run(["g++", "-O2", "-std=c++17", "-Wall", "-I", CSRC, "-I", INCLUDE, *exe_src, "-o", EXE, "-L", LIB_DIR,
-              "-lfwant_gb300", "-Wl,-rpath,$ORIGIN/../lib"], verbose)
+    # the programs over the C ABI: the solver stage (SeisFD3D.conf + NetCDF files in and
+    # out) and the sensitivity-kernel stage (TomoKernel.conf, sgt_ files in, kernel files out)
+    for exe, srcs in ((EXE, EXE_SOURCES), (KER_EXE, KER_SOURCES)):
+        exe_src = [os.path.join(CSRC, f) for f in srcs]
+        if force or _stale(exe, exe_src + hdrs + [LIB]):
+            os.makedirs(os.path.dirname(exe), exist_ok=True)
+            _run(["g++", "-O2", "-std=c++17", "-Wall", "-ffp-contract=off", "-I", CSRC, "-I", INCLUDE, *exe_src,
+                  "-o", exe, "-L", LIB_DIR, "-lfwant_gb300", "-Wl,-rpath,$ORIGIN/../lib"], verbose)
     return LIB
 
 

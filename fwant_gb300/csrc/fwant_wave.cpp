@@ -25,10 +25,11 @@
 #include "../../include/fwant_gb300.h"
 #include "conf.h"
 #include "netcdf3.h"
+#include "seisfd_conf.h"
 
 namespace {
 
-const char* const SUFFIX = "mpi000000";
+const char* const SUFFIX = seisfd::MPI_SUFFIX;
 const char* const COMP[9] = {"Vx", "Vy", "Vz", "Txx", "Tyy", "Tzz", "Txy", "Txz", "Tyz"};
 
 [[noreturn]] void die(const std::string& msg) {
@@ -40,18 +41,9 @@ void check(fwant_status rc, fwant_solver* s, const char* what) {
   if (rc != FWANT_OK) die(std::string(what) + ": " + (s ? fwant_last_error(s) : "error"));
 }
 
-std::string pad(int v, int width) {
-  char b[32];
-  std::snprintf(b, sizeof(b), "%0*d", width, v);
-  return b;
-}
+using seisfd::pad;
 
-struct Snap {
-  int id;                        // 1-based snap_NNN number
-  int subs[3], subc[3], subt[3];  // subs: 1-based with ghosts
-  int gsubs[3], gsube[3];        // interior-relative, as the reference's attributes
-  int tinv, tcnt;
-  bool vel, sgt;
+struct Snap : seisfd::SnapDef {
   std::vector<float> vbuf, tbuf;  // frames of the current file
   std::vector<float> times;
   int frames() const { return int(times.size()); }
@@ -114,16 +106,14 @@ void write_snap_file(const std::string& root, const Snap& sp, bool vel, float st
       std::memcpy(&d[size_t(f) * n], &buf[(size_t(f) * nc + c) * n], n * sizeof(float));
     w.add_var_f(vel ? vnames[c] : tnames[c], {T, K, J, I}, d.data(), d.size());
   }
-  const std::string path = root + "/" + (vel ? "vel_" : "sgt_") + pad(sp.id, 3) + "_" + SUFFIX + "_n" +
-                           pad(sp.file_no(ntime_last), 5) + ".nc";
+  const std::string path = seisfd::snap_file(root, vel ? "vel_" : "sgt_", sp.id, sp.file_no(ntime_last));
   std::string err;
   if (!w.write(path, &err)) die(err);
 }
 
 // frames of a partly written snapshot group back from its file (resume)
 void reload_snap_file(const std::string& root, Snap& sp, bool vel, int ntime) {
-  const std::string path = root + "/" + (vel ? "vel_" : "sgt_") + pad(sp.id, 3) + "_" + SUFFIX + "_n" +
-                           pad(sp.file_no(ntime), 5) + ".nc";
+  const std::string path = seisfd::snap_file(root, vel ? "vel_" : "sgt_", sp.id, sp.file_no(ntime));
   nc3::Reader r;
   std::string err;
   if (!r.open(path, &err)) die("resume: " + err);
@@ -314,32 +304,14 @@ int main(int argc, char** argv) {
   }
   // snapshots (io_snap_read / corr_indx / io_snap_locate, code/srcF/mod_io.F90:180-262)
   std::vector<Snap> snaps;
-  const int nsnap = cf.has("number_of_snap") ? need_i("number_of_snap", 2) : 0;
-  const int last[3] = {ni, nj, nk};
-  for (int n = 1; n <= nsnap; ++n) {
-    const std::string key = "snap_" + pad(n, 3);
-    Snap sp{};
-    sp.id = n;
-    for (int d = 0; d < 3; ++d) {
-      int s0 = need_i(key, d + 2), c0 = need_i(key, d + 5), t0 = need_i(key, d + 8);
-      if (s0 == -1) s0 = 1;                    // first interior point
-      if (d == 2 && s0 == -2) s0 = nk;         // the free surface
-      if (t0 < 1) die(key + ": stride must be >= 1");
-      if (c0 == -1) c0 = (last[d] - s0) / t0 + 1;
-      sp.gsubs[d] = s0;
-      sp.subc[d] = c0;
-      sp.subt[d] = t0;
-      sp.gsube[d] = s0 + t0 * (c0 - 1);
-      sp.subs[d] = s0 + 3;                     // 1-based with ghosts
+  try {
+    for (const seisfd::SnapDef& d : seisfd::read_snaps(cf, ni, nj, nk)) {
+      Snap sp;
+      static_cast<seisfd::SnapDef&>(sp) = d;
+      snaps.push_back(sp);
     }
-    sp.tinv = need_i(key, 11);
-    sp.tcnt = need_i(key, 12);
-    std::string var;
-    if (!cf.get(key, 13, &var)) die(key + ": variable list (V, T or TV) missing");
-    sp.vel = var.find('V') != std::string::npos;
-    sp.sgt = var.find('T') != std::string::npos;
-    if (sp.tinv < 1 || sp.tcnt < 1) die(key + ": tinv and tcnt must be >= 1");
-    snaps.push_back(sp);
+  } catch (const std::exception& e) {
+    die(conf_path + ": " + e.what());
   }
 
   const int total = fwant_reference_steps(nt);

@@ -240,6 +240,106 @@ bool Reader::read(const std::string& name, std::vector<int>* out, std::string* e
   return true;
 }
 
+namespace {
+// Element offsets of a hyperslab: calls row(file_offset_of_first, slab_index_of_first) for
+// every run along the last dimension (count elements stride apart).
+template <typename F>
+bool for_rows(const Reader& r, const Var& v, uint64_t numrecs, uint64_t recsize, const std::vector<uint64_t>& start,
+              const std::vector<uint64_t>& cnt, const std::vector<uint64_t>& stride, std::string* err, F row) {
+  const size_t nd = v.dims.size();
+  if (nd == 0 || start.size() != nd || cnt.size() != nd || stride.size() != nd) {
+    *err = "variable " + v.name + ": slab rank differs from the variable's";
+    return false;
+  }
+  const int sz = type_size(v.type);
+  std::vector<uint64_t> len(nd), pitch(nd);
+  for (size_t d = 0; d < nd; ++d) {
+    len[d] = r.dims[v.dims[d]].len == 0 ? numrecs : r.dims[v.dims[d]].len;
+    if (cnt[d] == 0) return true;
+    if (stride[d] == 0 || start[d] + (cnt[d] - 1) * stride[d] >= len[d]) {
+      *err = "variable " + v.name + ": slab outside dimension " + r.dims[v.dims[d]].name;
+      return false;
+    }
+  }
+  // byte pitch of each dimension
+  uint64_t p = uint64_t(sz);
+  for (size_t d = nd; d-- > 0;) {
+    pitch[d] = p;
+    if (!(d == 0 && v.record)) p *= len[d];
+  }
+  if (v.record) pitch[0] = recsize;
+  std::vector<uint64_t> idx(nd - 1, 0);
+  uint64_t slab = 0;
+  for (;;) {
+    uint64_t off = v.begin + start[nd - 1] * pitch[nd - 1];
+    for (size_t d = 0; d + 1 < nd; ++d) off += (start[d] + idx[d] * stride[d]) * pitch[d];
+    if (!row(off, slab)) return false;
+    slab += cnt[nd - 1];
+    size_t d = nd - 1;
+    while (d > 0) {
+      --d;
+      if (++idx[d] < cnt[d]) break;
+      idx[d] = 0;
+      if (d == 0) return true;
+    }
+    if (nd == 1) return true;
+  }
+}
+}  // namespace
+
+bool Reader::read_slab(const std::string& name, const std::vector<uint64_t>& start, const std::vector<uint64_t>& cnt,
+                       const std::vector<uint64_t>& stride, std::vector<float>* out, std::string* err) const {
+  const Var* v = var(name);
+  if (!v) { *err = "no variable " + name; return false; }
+  uint64_t total = 1;
+  for (uint64_t c : cnt) total *= c;
+  out->assign(size_t(total), 0.0f);
+  if (total == 0) return true;
+  const int sz = type_size(v->type);
+  const uint64_t n = cnt.back(), st = stride.back(), span = (n - 1) * st + 1;
+  std::vector<unsigned char> buf(size_t(span * sz));
+  return for_rows(*this, *v, numrecs_, recsize_, start, cnt, stride, err, [&](uint64_t off, uint64_t slab) {
+    if (std::fseek(fp_, long(off), SEEK_SET) != 0 || std::fread(buf.data(), 1, buf.size(), fp_) != buf.size()) {
+      *err = "truncated data of variable " + v->name;
+      return false;
+    }
+    for (uint64_t e = 0; e < n; ++e) (*out)[size_t(slab + e)] = float(decode(&buf[size_t(e * st * sz)], v->type));
+    return true;
+  });
+}
+
+bool update_slab(const std::string& path, const std::string& name, const std::vector<uint64_t>& start,
+                 const std::vector<uint64_t>& cnt, const std::vector<uint64_t>& stride, const float* data,
+                 std::string* err) {
+  Reader r;
+  if (!r.open(path, err)) return false;
+  const Var* v = r.var(name);
+  if (!v) { *err = path + ": no variable " + name; return false; }
+  if (v->type != NC_FLOAT || v->record) { *err = path + ": " + name + " is not a fixed-size float variable"; return false; }
+  FILE* f = std::fopen(path.c_str(), "r+b");
+  if (!f) { *err = "cannot open " + path + " for writing"; return false; }
+  const uint64_t n = cnt.empty() ? 0 : cnt.back(), st = stride.empty() ? 1 : stride.back(), span = n ? (n - 1) * st + 1 : 0;
+  std::vector<unsigned char> buf(size_t(span * 4)), one;
+  const bool ok = for_rows(r, *v, r.numrecs_, r.recsize_, start, cnt, stride, err, [&](uint64_t off, uint64_t slab) {
+    if (std::fseek(f, long(off), SEEK_SET) != 0 || std::fread(buf.data(), 1, buf.size(), f) != buf.size()) {
+      *err = path + ": truncated data of variable " + name;
+      return false;
+    }
+    for (uint64_t e = 0; e < n; ++e) {
+      one.clear();
+      encode(one, double(data[slab + e]), NC_FLOAT);
+      std::memcpy(&buf[size_t(e * st * 4)], one.data(), 4);
+    }
+    if (std::fseek(f, long(off), SEEK_SET) != 0 || std::fwrite(buf.data(), 1, buf.size(), f) != buf.size()) {
+      *err = path + ": write failed";
+      return false;
+    }
+    return true;
+  });
+  if (std::fclose(f) != 0 && ok) { *err = path + ": write failed"; return false; }
+  return ok;
+}
+
 // ---- writer ------------------------------------------------------------------------------
 int Writer::add_dim(const std::string& name, uint64_t len) {
   dims_.push_back(Dim{name, len});

@@ -54,12 +54,19 @@ class Reader {
   bool read(const std::string& name, std::vector<double>* out, std::string* err) const;
   bool read(const std::string& name, std::vector<float>* out, std::string* err) const;
   bool read(const std::string& name, std::vector<int>* out, std::string* err) const;
+  // strided hyperslab (per dimension, slowest first: 0-based start, count, stride >= 1; for
+  // a record variable the first dimension counts records) converted to float, slab
+  // elements in file order (last dimension fastest) -- nf90_get_var with start/count/stride
+  bool read_slab(const std::string& name, const std::vector<uint64_t>& start, const std::vector<uint64_t>& count,
+                 const std::vector<uint64_t>& stride, std::vector<float>* out, std::string* err) const;
   std::vector<Dim> dims;
   std::vector<Att> gatts;
   std::vector<Var> vars;
 
  private:
   bool read_raw(const Var& v, std::vector<double>* out, std::string* err) const;
+  friend bool update_slab(const std::string&, const std::string&, const std::vector<uint64_t>&,
+                          const std::vector<uint64_t>&, const std::vector<uint64_t>&, const float*, std::string*);
   FILE* fp_ = nullptr;
   uint64_t numrecs_ = 0, recsize_ = 0;
 };
@@ -83,5 +90,12 @@ class Writer {
   std::vector<std::vector<unsigned char>> data_;  // big-endian element bytes, file order
   uint64_t numrecs_ = 0;
 };
+
+// Writes a strided hyperslab of a fixed-size NC_FLOAT variable of an existing file in
+// place (nf90_put_var with start/count/stride on a file opened for writing); data in slab
+// file order.  The rest of the file is left as it is.
+bool update_slab(const std::string& path, const std::string& name, const std::vector<uint64_t>& start,
+                 const std::vector<uint64_t>& count, const std::vector<uint64_t>& stride, const float* data,
+                 std::string* err);
 
 }  // namespace nc3

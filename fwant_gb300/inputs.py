@@ -425,3 +425,70 @@ def write_conf(path: str, m: Model, nt: int, roots: dict, snaps=(), checkpoint_t
         lines.append(f"snap_{q:03d} = {cols} {var}   # subs subc subt tinv tcnt")
     with open(path, "w") as f:
         f.write("\n".join(lines) + "\n")
+
+
+# ---- inputs of the sensitivity-kernel program (SI_ker_sta) ---------------------------------
+
+def _f32text(v) -> str:
+    """The shortest text that reads back as the same float32 value."""
+    return repr(float(np.float32(v)))
+
+
+def write_tomo_conf(path: str, main_conf: str, snap_id: int, roots: dict, knt: int, sgt_m0: float,
+                    sub_start=(1, 1, 1), sub_count=(-1, -1, -1), sub_stride=(1, 1, 1), block_from=(1, 1, 1),
+                    block_size=(-1, -1, -1), first_run=True, max_pick=4, filter_files=()):
+    """TomoKernel.conf with the keys init_kernel and init_filter read
+    (code/srcF.kernel/SI_ker_sta.F90:1047-1112).  roots: SGT_ROOT SGT_STAX SGT_STAY SGT_STAZ
+    EVENT_ROOT EVENT_OUTD.  filter_files: one file name (or "none") per frequency band."""
+    def row(key, vals):
+        return f"{key} = " + " ".join(str(int(v)) for v in vals)
+    lines = [f"MAIN_CONF = {main_conf}", f"snap_id = {int(snap_id)}",
+             f"first_run = {'.true.' if first_run else '.false.'}",
+             row("sub_start", sub_start), row("sub_count", sub_count), row("sub_stride", sub_stride),
+             row("block_from", block_from), row("block_size", block_size),
+             f"SGT_TIMEDIM_SIZE = {int(knt)}", f"SGT_M0 = {_f32text(sgt_m0)}"]
+    for k in ("SGT_ROOT", "SGT_STAX", "SGT_STAY", "SGT_STAZ", "EVENT_ROOT", "EVENT_OUTD"):
+        lines.append(f"{k} = {roots[k]}")
+    lines += [f"maximum_of_pick_per_component = {int(max_pick)}", f"number_of_freqband = {len(filter_files)}",
+              "<filter_file>"] + [str(f) for f in filter_files]
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def write_filter_file(path: str, b, a):
+    """A filter file: NOD1, then NOD1 lines of a and b in F20.16 (init_filter).  Returns the
+    (b, a) coefficients as they read back."""
+    b = np.asarray(b, np.float64)
+    a = np.asarray(a, np.float64)
+    rows = [f"{x:20.16f}{y:20.16f}" for x, y in zip(a, b)]
+    if any(len(r) != 40 for r in rows):
+        raise ValueError("coefficient does not fit F20.16")
+    with open(path, "w") as f:
+        f.write(f"{b.size}\n" + "\n".join(rows) + "\n")
+    return np.array([float(r[20:]) for r in rows]), np.array([float(r[:20]) for r in rows])
+
+
+def write_synthetic(path: str, t, v, u):
+    """A synthetic file: one line of T V U per sample (init_synthetic)."""
+    with open(path, "w") as f:
+        for row in zip(t, v, u):
+            f.write(" ".join(_f32text(x) for x in row) + "\n")
+
+
+def write_event_list(path: str, events):
+    """An event list: per event the header line (name, six pick counts, rot_mat column by
+    column), three synthetic file names and the pick lines of components 1..6 (band,
+    P1 | P2 | N, t1, t2, output directory).  events: dicts with name, picks (six lists of
+    (band, filt, t1, t2, dir)), rot (3x3, rot[d, c]) and syn (three file names)."""
+    lines = []
+    for e in events:
+        picks = e["picks"]
+        rot = np.asarray(e["rot"], np.float32).reshape(3, 3)
+        head = [e["name"]] + [str(len(p)) for p in picks] + [_f32text(x) for x in rot.flatten(order="F")]
+        lines.append(" ".join(head))
+        lines += list(e["syn"])
+        for comp in picks:
+            for band, filt, t1, t2, d in comp:
+                lines.append(f"{int(band)} {filt} {_f32text(t1)} {_f32text(t2)} {d}")
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")

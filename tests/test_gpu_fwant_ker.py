@@ -1,0 +1,238 @@
+"""`fwant_ker`, the station sensitivity-kernel program (SI_ker_sta) on the GPU, end to end
+through files: four `fwant_wave` runs write the sgt_ snapshot series of a station's three
+force components and of an event; `fwant_ker` reads them block by block with the
+reference's TomoKernel.conf, filter files, station and event lists, and writes one kernel
+file per pick.  Every kernel file equals the restatement's pipeline on the same SGTs
+(stress2strain + sgt2scatter3 in FP64 accumulation, the component rotation, the pick's
+filter and window) bit for bit after the cast to float32; the points outside the kernel
+selection stay zero, a pick outside the time range writes no file, and a second run that
+starts at a later block over the first run's files (first_run false) rewrites them
+unchanged."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from helpers import LENFD, small_model
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+WAVE = os.path.join(ROOT, "fwant_gb300", "bin", "fwant_wave")
+KER = os.path.join(ROOT, "fwant_gb300", "bin", "fwant_ker")
+NT = 40                                  # 48 steps executed: 24 frames at tinv 2
+SNAP = ((3, 4, 5), (6, 5, 4), (2, 2, 2), 2, 5, "T")
+KNT = 20                                 # frames used: files n00001-n00004
+SUB = dict(sub_start=(2, 1, 1), sub_count=(-1, 4, -1), sub_stride=(2, 1, 1), block_size=(2, 3, -1))
+M0 = 1.0e15
+
+
+def _read(path):
+    from scipy.io import netcdf_file
+    with netcdf_file(path, "r", mmap=False) as f:
+        return {k: np.array(v[:]) for k, v in f.variables.items()}, dict(f._attributes)
+
+
+def _wave_run(tmp, m, out_dir):
+    from fwant_gb300 import inputs
+    os.makedirs(tmp, exist_ok=True)
+    os.makedirs(out_dir, exist_ok=True)
+    inputs.write_inputs(m, tmp)
+    roots = {k: tmp for k in ("GRID_ROOT", "MEDIA_ROOT", "SOURCE_ROOT", "STATION_ROOT")}
+    roots["OUTPUT_ROOT"] = out_dir
+    conf = os.path.join(tmp, "SeisFD3D.conf")
+    inputs.write_conf(conf, m, NT, roots, snaps=[SNAP])
+    r = subprocess.run([WAVE, conf], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return conf
+
+
+def _sgt_series(out_dir):
+    """(6, KNT, K, J, I) stresses of the snapshot series from its files."""
+    frames = []
+    n = 1
+    while sum(f.shape[1] for f in frames) < KNT:
+        v, _ = _read(os.path.join(out_dir, f"sgt_001_mpi000000_n{n:05d}.nc"))
+        frames.append(np.stack([v[c] for c in ("Txx", "Tyy", "Tzz", "Txy", "Txz", "Tyz")]))
+        n += 1
+    return np.concatenate(frames, axis=1)[:, :KNT]
+
+
+def _window(t, t1, t2, kdt):
+    """Pick window (SI_ker_sta.F90:676-704) over the synthetic's times t; the range is
+    kdt .. knt kdt.  None when the pick is skipped."""
+    knt = t.size
+    tmin, tmax = kdt, np.float32(knt) * kdt
+    if t1 > tmax or t2 < tmin:
+        return None
+    nt1 = 1 if t1 <= tmin else int(np.flatnonzero(t <= t1)[np.argmax(t[t <= t1])]) + 1
+    nt2 = knt if t2 >= tmax else int(np.flatnonzero(t >= t2)[np.argmin(t[t >= t2])]) + 1
+    return nt1, nt2
+
+
+@pytest.fixture(scope="module")
+def runs(tmp_path_factory, native_lib):
+    signal = pytest.importorskip("scipy.signal")
+    from fwant_gb300 import inputs
+    tmp = str(tmp_path_factory.mktemp("ker"))
+    sgt_root, evt_root = os.path.join(tmp, "SGT"), os.path.join(tmp, "EVT")
+    # the station's three force runs and the event run share grid and medium
+    for c, name in enumerate(("FX", "FY", "FZ")):
+        m = small_model("surface")
+        for q, f in enumerate((m.fx, m.fy, m.fz)):
+            f[:] = np.float32(1.0e15) if q == c else np.float32(0.0)
+        _wave_run(os.path.join(tmp, "run_" + name), m, os.path.join(sgt_root, "STA", name))
+    main = _wave_run(os.path.join(tmp, "run_ev"), small_model("buried"), os.path.join(evt_root, "EV1", "OUT"))
+    os.symlink(os.path.join(evt_root, "EV1"), os.path.join(evt_root, "EV2"))  # a second event, same SGTs
+    m = small_model("surface")
+    kdt = np.float32(SNAP[3]) * np.float32(m.stept)
+    t = np.float32(np.arange(1, KNT + 1)) * kdt
+    rng = np.random.default_rng(12)
+    syn = []
+    for c in range(4):
+        v = rng.normal(size=KNT).astype(np.float32)
+        u = (np.cumsum(v) * kdt).astype(np.float32)
+        p = os.path.join(tmp, f"syn{c}.txt")
+        inputs.write_synthetic(p, t, v, u)
+        syn.append((p, v, u))
+    b, a = signal.butter(2, [0.15, 0.45], btype="band")
+    fb, fa = inputs.write_filter_file(os.path.join(tmp, "bp1.txt"), b, a)
+    kd = lambda name: os.path.join(tmp, "kernels", name)  # noqa: E731
+    picks1 = [[(1, "P2", 2.5 * kdt, 15.2 * kdt, kd("A"))],
+              [(1, "N", 100 * kdt, 200 * kdt, kd("F"))],                       # after the series: skipped
+              [(2, "N", 0.5 * kdt, 30 * kdt, kd("B")), (1, "P1", 3 * kdt, 16 * kdt, kd("C"))],
+              [(2, "N", 1.5 * kdt, 12 * kdt, kd("D"))],
+              [],
+              [(1, "P2", 4 * kdt, 19 * kdt, kd("E"))]]
+    picks2 = [[], [(2, "N", 2 * kdt, 18 * kdt, kd("G"))], [], [], [], []]
+    th = 0.6
+    rot = np.array([[np.cos(th), -np.sin(th), 0.0], [np.sin(th), np.cos(th), 0.0], [0.0, 0.0, 1.0]])
+    events = [dict(name="EV1", picks=picks1, rot=rot, syn=[s[0] for s in syn[:3]]),
+              dict(name="EV2", picks=picks2, rot=np.eye(3), syn=[syn[3][0], syn[3][0], syn[3][0]])]
+    for e in events:
+        for comp in e["picks"]:
+            for p in comp:
+                os.makedirs(p[4], exist_ok=True)
+    evt = os.path.join(tmp, "evt.lst")
+    inputs.write_event_list(evt, events)
+    sta = os.path.join(tmp, "sta.lst")
+    with open(sta, "w") as f:
+        f.write(f"# station  event list\nSTA {evt}\n")
+    kroots = dict(SGT_ROOT=sgt_root, SGT_STAX="FX", SGT_STAY="FY", SGT_STAZ="FZ", EVENT_ROOT=evt_root,
+                  EVENT_OUTD="OUT")
+    conf = os.path.join(tmp, "TomoKernel.conf")
+    inputs.write_tomo_conf(conf, main, 1, kroots, KNT, M0, filter_files=[os.path.join(tmp, "bp1.txt"), "none"], **SUB)
+    r = subprocess.run([KER, conf], input=f"{sta}\n0 0 0\n", capture_output=True, text=True, cwd=tmp)
+    assert r.returncode == 0, r.stderr
+    assert "t1>Tmax" in r.stderr
+    return dict(tmp=tmp, m=m, kdt=kdt, t=t, syn=syn, filt=(fb, fa), events=events, conf=conf, sta=sta,
+                sgt_root=sgt_root, evt_root=evt_root, kd=kd, stdout=r.stdout)
+
+
+def _expected(R, oracle_mod):
+    """Kernels of every pick over all selected points, float32, in file (K, J, I) layout."""
+    m, kdt, t = R["m"], R["kdt"], R["t"]
+    subs, subc, subt = SNAP[0], SNAP[1], SNAP[2]
+    # selected sample indices (0-based) per axis: start, stride, count of the kernel selection
+    sel = []
+    for d in range(3):
+        st, cnt, sd = SUB["sub_start"][d], SUB["sub_count"][d], SUB["sub_stride"][d]
+        n = (subc[d] - st) // sd + 1
+        if cnt != -1:
+            n = min(n, cnt)
+        sel.append(np.arange(st - 1, st - 1 + n * sd, sd))
+    si, sj, sk = sel
+    # media at those points (grid index with ghosts: first snapshot point + sample x stride)
+    gi = [LENFD + subs[d] - 1 + sel[d] * subt[d] for d in range(3)]
+    lam = m.lam[np.ix_(*gi)].transpose(2, 1, 0).reshape(-1)
+    mu = m.mu[np.ix_(*gi)].transpose(2, 1, 0).reshape(-1)
+
+    def block(series):  # (6, KNT, K, J, I) -> (6, KNT, points) with i fastest
+        return np.ascontiguousarray(series[:, :, sk][:, :, :, sj][:, :, :, :, si].reshape(6, KNT, -1))
+    rs = [block(_sgt_series(os.path.join(R["sgt_root"], "STA", c))) for c in ("FX", "FY", "FZ")]
+    ss = block(_sgt_series(os.path.join(R["evt_root"], "EV1", "OUT")))
+    dt = float(kdt)
+    m0 = float(np.float32(M0))
+    fb, fa = R["filt"]
+    out = {}
+    for e, syn in ((R["events"][0], R["syn"][:3]), (R["events"][1], [R["syn"][3]] * 3)):
+        rot_any = any(len(p) for p in e["picks"][3:])
+        ud = [len(e["picks"][c]) > 0 or rot_any for c in range(3)]
+        scat = oracle_mod.sgt2scatter3(lam, mu, [rs[c] if ud[c] else None for c in range(3)], ss, dt, mode=1)
+        V = [s[1].copy() for s in syn]
+        U = [s[2].copy() for s in syn]
+        rot = np.asarray(e["rot"], np.float32).reshape(3, 3)
+        for ncmp in range(1, 7):
+            if ncmp == 4 and rot_any:
+                for W in (V, U):
+                    w0, w1, w2 = W[0].copy(), W[1].copy(), W[2].copy()
+                    for c in range(3):
+                        W[c] = (w0 * rot[0, c] + w1 * rot[1, c]) + w2 * rot[2, c]
+                r64 = rot.astype(np.float64)
+                for grp in ((0, 1, 2), (3, 5, 4)):
+                    v = [scat[q].copy() for q in grp]
+                    for c in range(3):
+                        scat[grp[c]] = (v[0] * r64[0, c] + v[1] * r64[1, c]) + v[2] * r64[2, c]
+            comp = (ncmp - 1) % 3
+            sa, sb = ((0, 3), (1, 5), (2, 4))[comp]
+            for band, filt, t1, t2, d in e["picks"][ncmp - 1]:
+                w = _window(t, np.float32(t1), np.float32(t2), kdt)
+                if w is None:
+                    out[d] = None
+                    continue
+                if filt == "N":
+                    k = oracle_mod.scatter2kernel(V[comp], U[comp], scat[sa], scat[sb], dt, w[0], w[1], m0, mode=1)
+                else:
+                    k = oracle_mod.scatter2kernel_filtered(V[comp], U[comp], scat[sa], scat[sb], dt, w[0], w[1], m0,
+                                                           fb, fa, 1 if filt == "P1" else 2)
+                full = []
+                for q in range(4):
+                    a = np.zeros((subc[2], subc[1], subc[0]), np.float32)
+                    a[np.ix_(sk, sj, si)] = np.asarray(k[q], np.float64).astype(np.float32).reshape(
+                        sk.size, sj.size, si.size)
+                    full.append(a)
+                out[d] = full
+    return out
+
+
+NAMES = ("phase_Vp", "amplitude_Vp", "phase_Vs", "amplitude_Vs")
+
+
+def test_kernel_files_equal_the_restatement(runs, oracle_mod):
+    want = _expected(runs, oracle_mod)
+    assert len(want) == 7
+    for d, w in want.items():
+        path = os.path.join(d, "kernel_001_mpi000000_n00000.nc")
+        if w is None:
+            assert not os.path.exists(path)
+            continue
+        got, att = _read(path)
+        assert att["title"] == b"Finite frequency kernel"
+        for q, name in enumerate(NAMES):
+            assert got[name].shape == (SNAP[1][2], SNAP[1][1], SNAP[1][0])
+            np.testing.assert_array_equal(got[name], w[q], err_msg=f"{d}:{name}")
+            assert np.any(w[q])
+
+
+def test_resumed_blocks_rewrite_the_same_files(runs):
+    """first_run false and block_from (2, 1, 1): the later blocks are recomputed into the
+    existing files, which keep their content."""
+    from fwant_gb300 import inputs
+    before = {}
+    for d in ("A", "E", "G"):
+        before[d] = _read(os.path.join(runs["kd"](d), "kernel_001_mpi000000_n00000.nc"))[0]
+    conf = os.path.join(runs["tmp"], "TomoKernel_resume.conf")
+    kroots = dict(SGT_ROOT=runs["sgt_root"], SGT_STAX="FX", SGT_STAY="FY", SGT_STAZ="FZ",
+                  EVENT_ROOT=runs["evt_root"], EVENT_OUTD="OUT")
+    main = os.path.join(runs["tmp"], "run_ev", "SeisFD3D.conf")
+    inputs.write_tomo_conf(conf, main, 1, kroots, KNT, M0, first_run=False, block_from=(2, 1, 1),
+                           filter_files=[os.path.join(runs["tmp"], "bp1.txt"), "none"], **SUB)
+    r = subprocess.run([KER, conf], input=f"{runs['sta']}\n0 0 0\n", capture_output=True, text=True, cwd=runs["tmp"])
+    assert r.returncode == 0, r.stderr
+    for d, b in before.items():
+        got = _read(os.path.join(runs["kd"](d), "kernel_001_mpi000000_n00000.nc"))[0]
+        for name in NAMES:
+            np.testing.assert_array_equal(got[name], b[name])
+    shutil.rmtree(os.path.join(runs["tmp"], "kernels"), ignore_errors=True)
