@@ -57,8 +57,10 @@ def parse_args():
     p.add_argument("--steps", type=int, default=32)
     p.add_argument("--warmup", type=int, default=8)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--config", choices=["c2", "c1", "c3", "c5"], default="c2",
-                   help="c5: train the waveform surrogate on 512 FD solves and screen 64 held-out models")
+    p.add_argument("--config", choices=["c2", "c1", "c3", "c5", "lsqr"], default="c2",
+                   help="c5: train the waveform surrogate on 512 FD solves and screen 64 held-out models; "
+                        "lsqr: LSQR iterations of the damped, smoothed inversion (inv.LSQR) on a synthetic system")
+    p.add_argument("--lsqr-scale", type=float, default=1.0, help="fraction of the LSQR system's data rows (profiling)")
     p.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -257,6 +259,114 @@ def run_reference(args, rank, world):
     return 0
 
 
+def lsqr_system(scale=1.0, seed=0):
+    """A synthetic inversion system shaped like the reference's: 1.5M unknowns (3
+    components x 500k blocks + station and event terms), 25,000 measurements whose kernel
+    rows are 64 runs of 250 consecutive blocks (a localised sensitivity kernel in block
+    order), one damping row per unknown and first-difference smoothing rows along the block
+    order of each component.  Returns (row_ptr, col, val, rhs, ncol)."""
+    rng = np.random.default_rng(seed)
+    nblk, ncmp, nsta, nevt = 500_000, 3, 400, 2_000
+    nm = nblk * ncmp
+    ncol = nm + nsta + nevt
+    ndata = max(1, int(25_000 * scale))
+    runs, runlen = 64, 250
+    starts = rng.integers(0, nm - runlen, size=(ndata, runs))
+    starts.sort(axis=1)
+    kcols = (starts[:, :, None] + np.arange(runlen)[None, None, :]).reshape(ndata, -1)
+    sta = nm + rng.integers(0, nsta, size=ndata)
+    evt = nm + nsta + rng.integers(0, nevt, size=ndata)
+    dcols = np.concatenate([kcols, sta[:, None], evt[:, None]], axis=1)
+    nper = dcols.shape[1]
+    dvals = rng.normal(size=(ndata, nper)) * 1e-3
+    dvals[:, -2:] = rng.choice([-1.0, 1.0], size=(ndata, 2))
+    smo = np.arange(nm)
+    smo = smo[(smo + 1) % nblk != 0]  # first differences within each component
+    rp = np.concatenate([np.arange(ndata + 1, dtype=np.int64) * nper,
+                         ndata * nper + np.arange(1, ncol + 1, dtype=np.int64),
+                         ndata * nper + ncol + 2 * np.arange(1, smo.size + 1, dtype=np.int64)])
+    col = np.concatenate([dcols.reshape(-1), np.arange(ncol), np.stack([smo, smo + 1], axis=1).reshape(-1)])
+    val = np.concatenate([dvals.reshape(-1), np.full(ncol, 0.05), np.tile([-0.5, 0.5], smo.size)])
+    rhs = np.concatenate([rng.normal(size=ndata), np.zeros(ncol + smo.size)])
+    return rp, col.astype(np.int32), val.astype(np.float64), rhs, ncol
+
+
+def lsqr_bytes_per_iteration(nnz, nrow, ncol):
+    """Algorithmic bytes of one LSQR iteration: both products read every stored entry once
+    (8 B value + 4 B index, compressed rows and compressed columns) and their offsets; the
+    vector passes read and write u twice (product, normalisation), v twice, and x, w, sig
+    with v once more in the update.  Gathered vector reads are not counted (L2)."""
+    return 24 * nnz + 8 * (nrow + ncol) + 32 * nrow + 88 * ncol
+
+
+def run_lsqr(args, rank):
+    """The inversion's LSQR (fwant_lsqr_*) on the synthetic system: K iterations timed on
+    the device, the roofline of the iteration, the oracle's sequential LSQR on the host for
+    a bounded sample, and the end-to-end job through the public API (upload, solve,
+    solution read back)."""
+    import fwant_gb300 as fw
+    if rank != 0:
+        return 0
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    rp, col, val, rhs, ncol = lsqr_system(args.lsqr_scale)
+    nrow, nnz = rp.size - 1, int(rp[-1])
+    t0 = time.perf_counter()
+    L = fw.Lsqr(rp, col, val, rhs, ncol, device=dev)
+    create_s = time.perf_counter() - t0
+    warm = max(args.warmup, 3)
+    L.solve(0.0, 0.0, warm)
+    clocks = Clocks(dev)
+    clocks.start()
+    it = L.solve(0.0, 0.0, args.steps)
+    dev_ms = L.last_solve_ms()
+    clk = clocks.stop()
+    x, _ = L.solution()
+    finite = bool(np.all(np.isfinite(x)))
+    value = nnz * it / (dev_ms * 1e-3) / 1e9
+    per_it = lsqr_bytes_per_iteration(nnz, nrow, ncol)
+    achieved = per_it * it / (dev_ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    out = {
+        "metric": "LSQR matrix entries per second", "value": value, "unit": "Gentries/s", "n_gpus": 1,
+        "steps": it, "warmup": warm, "ms_per_step": dev_ms / it, "higher_is_better": True, "scaling": "replicas only",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": f"inversion system: {nrow} rows x {ncol} unknowns, {nnz} stored entries "
+                               f"({int(25_000 * args.lsqr_scale)} measurements x 16,002 entries, damping, smoothing)",
+                   "l2": "matrix larger than L2 (no flush)", "solution_finite": finite,
+                   "iteration": "one LSQR iteration (A v, A^T u, two normalisations, update, test) per step"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_iteration": per_it},
+        "clocks": clk, "create_s": create_s,
+        # per 32 iterations one graph of 7 kernels each, plus 5 start kernels
+        "gpu_launches": 5 + 7 * 32 * ((it + 31) // 32),
+    }
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        O.build()
+        k = 2
+        t1 = time.perf_counter()
+        O.lsqr(rp, col, val, rhs, ncol, atol=0.0, btol=0.0, maxit=k)
+        dt = time.perf_counter() - t1
+        out["cpu_baseline"] = {"value": nnz * k / dt / 1e9, "unit": "Gentries/s", "cores": 1, "kind": "port",
+                               "sample": f"{k} iterations of the sequential restatement on the same system, "
+                                         f"{dt:.1f} s (setup and |A|_F included)"}
+    if not args.no_e2e:
+        t1 = time.perf_counter()
+        L2 = fw.Lsqr(rp, col, val, rhs, ncol, device=dev)
+        it2 = L2.solve(0.0, 0.0, args.steps)
+        x2, e2 = L2.solution()
+        wall = time.perf_counter() - t1
+        L2.close()
+        out["e2e"] = {"value": nnz * it2 / wall / 1e9, "unit": "Gentries/s",
+                      "h2d_bytes_per_step": (rp.nbytes + col.nbytes + val.nbytes + rhs.nbytes) / it2,
+                      "d2h_bytes_per_step": (x2.nbytes + e2.nbytes) / it2, "wall_s": wall,
+                      "includes": "transpose on the host, upload, |A|_F, K iterations, solution and errors read back"}
+    L.close()
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_surrogate(args, rank):
     """Config 5: the surrogate's screening speedup over FD solves at 1% waveform error."""
     from fwant_gb300 import surrogate
@@ -285,6 +395,8 @@ def run_ours(args, rank, world):
     from fwant_gb300 import inputs
     if args.config == "c5":
         return run_surrogate(args, rank)
+    if args.config == "lsqr":
+        return run_lsqr(args, rank)
     dist = Dist(world)
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     fw.load_library()

@@ -107,6 +107,16 @@ EXPORTS = [
     ("fwant_check", C.c_int, [_vp]),
     ("fwant_profile_stages", C.c_int, [_vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("fwant_last_run_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
+    # LSQR inversion solver (include/fwant_lsqr.h)
+    ("fwant_lsqr_create", C.c_int, [C.c_longlong, C.c_longlong, C.POINTER(C.c_longlong), C.POINTER(C.c_int),
+                                    C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_void_p)]),
+    ("fwant_lsqr_destroy", None, [_vp]),
+    ("fwant_lsqr_last_error", C.c_char_p, [_vp]),
+    ("fwant_lsqr_solve", C.c_int, [_vp, C.c_double, C.c_double, C.c_longlong, C.POINTER(C.c_longlong)]),
+    ("fwant_lsqr_solution", C.c_int, [_vp, C.c_longlong, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("fwant_lsqr_info", C.c_int, [_vp, C.POINTER(C.c_double)]),
+    ("fwant_lsqr_multiply", C.c_int, [_vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("fwant_lsqr_last_solve_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
 ]
 
 
@@ -521,6 +531,72 @@ class SgtKernel:
     def last_scatter_ms(self):
         ms = C.c_double()
         self._chk(self._lib.fwant_sgtker_last_scatter_ms(self._h, C.byref(ms)))
+        return ms.value
+
+
+class Lsqr:
+    """LSQR on the GPU (inv.LSQR/mod_LSQR.f90: slsqr, lgtsol) for a compressed-row matrix
+    (row_ptr, col 0-based, val) and right-hand side b."""
+
+    def __init__(self, row_ptr, col, val, b, ncol, device=0):
+        self._lib = load_library()
+        rp = np.ascontiguousarray(row_ptr, np.int64)
+        ci = np.ascontiguousarray(col, np.int32)
+        va = np.ascontiguousarray(val, np.float64)
+        bb = np.ascontiguousarray(b, np.float64)
+        self.nrow, self.ncol = rp.size - 1, int(ncol)
+        if bb.size != self.nrow or ci.size != va.size or ci.size != int(rp[-1]):
+            raise ValueError("inconsistent compressed-row arrays")
+        h = C.c_void_p()
+        rc = self._lib.fwant_lsqr_create(self.nrow, self.ncol, rp.ctypes.data_as(C.POINTER(C.c_longlong)),
+                                         _ptr(ci, C.c_int), _ptr(va, C.c_double), _ptr(bb, C.c_double), int(device),
+                                         C.byref(h))
+        if rc != 0:
+            raise FwantError(rc, "fwant_lsqr_create failed")
+        self._h = h
+
+    def _chk(self, rc):
+        if rc != 0:
+            raise FwantError(rc, self._lib.fwant_lsqr_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.fwant_lsqr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, atol=1e-7, btol=1e-7, maxit=30000):
+        """Iterations run (the reference's defaults)."""
+        it = C.c_longlong()
+        self._chk(self._lib.fwant_lsqr_solve(self._h, float(atol), float(btol), int(maxit), C.byref(it)))
+        return it.value
+
+    def solution(self, nvar=None):
+        """(x, standard errors) of the first nvar unknowns (all by default)."""
+        n = self.ncol if nvar is None else int(nvar)
+        x, e = np.zeros(n), np.zeros(n)
+        self._chk(self._lib.fwant_lsqr_solution(self._h, n, _ptr(x, C.c_double), _ptr(e, C.c_double)))
+        return x, e
+
+    def info(self):
+        v = np.zeros(6)
+        self._chk(self._lib.fwant_lsqr_info(self._h, _ptr(v, C.c_double)))
+        return dict(zip(("anorm", "res2", "test1", "test2", "phibar", "xnorm"), v))
+
+    def multiply(self, x):
+        xx = np.ascontiguousarray(x, np.float64)
+        y = np.zeros(self.nrow)
+        self._chk(self._lib.fwant_lsqr_multiply(self._h, _ptr(xx, C.c_double), _ptr(y, C.c_double)))
+        return y
+
+    def last_solve_ms(self):
+        ms = C.c_double()
+        self._chk(self._lib.fwant_lsqr_last_solve_ms(self._h, C.byref(ms)))
         return ms.value
 
 

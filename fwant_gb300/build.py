@@ -31,13 +31,15 @@ CPP_FLAGS = ["-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-con
 SOURCES = ["stage_fast_rk0.cu", "stage_fast_rk1.cu", "stage_fast_rk2.cu", "stage_exact_rk0.cu",
            "stage_exact_rk1.cu", "stage_exact_rk2.cu", "stage_bf16_rk0.cu", "stage_bf16_rk1.cu",
            "stage_bf16_rk2.cu", "stage_fp16_rk0.cu", "stage_fp16_rk1.cu", "stage_fp16_rk2.cu",
-           "stage_dispatch.cu", "aux.cu", "snapshot.cu", "sgtker.cu", "surrogate.cu", "solver.cpp", "sgtker_api.cpp"]
+           "stage_dispatch.cu", "aux.cu", "snapshot.cu", "sgtker.cu", "surrogate.cu", "lsqr.cu", "solver.cpp", "sgtker_api.cpp"]
 
 
 EXE = os.path.join(HERE, "bin", "fwant_wave")
 EXE_SOURCES = ["fwant_wave.cpp", "netcdf3.cpp", "conf.cpp"]
 KER_EXE = os.path.join(HERE, "bin", "fwant_ker")
 KER_SOURCES = ["fwant_ker.cpp", "netcdf3.cpp", "conf.cpp"]
+LSQR_EXE = os.path.join(HERE, "bin", "fwant_lsqr")
+LSQR_SOURCES = ["fwant_lsqr.cpp"]
 
 
 def _nvcc() -> str:
@@ -93,8 +95,9 @@ def build(verbose: bool = False, force: bool = False, jobs: int | None = None) -
     if force or jobs_todo or _stale(LIB, objs):
         _run([nvcc, "-shared", *ARCH, "-o", LIB, *objs, "-lcudart"], verbose)
     # the programs over the C ABI: the solver stage (SeisFD3D.conf + NetCDF files in and
-    # out) and the sensitivity-kernel stage (TomoKernel.conf, sgt_ files in, kernel files out)
-    for exe, srcs in ((EXE, EXE_SOURCES), (KER_EXE, KER_SOURCES)):
+    # out), the sensitivity-kernel stage (TomoKernel.conf, sgt_ files in, kernel files out)
+    # and the inversion (data list, kernel rows, smoothing operator in; model files out)
+    for exe, srcs in ((EXE, EXE_SOURCES), (KER_EXE, KER_SOURCES), (LSQR_EXE, LSQR_SOURCES)):
         exe_src = [os.path.join(CSRC, f) for f in srcs]
         if force or _stale(exe, exe_src + hdrs + [LIB]):
             os.makedirs(os.path.dirname(exe), exist_ok=True)

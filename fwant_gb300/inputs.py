@@ -492,3 +492,35 @@ def write_event_list(path: str, events):
                 lines.append(f"{int(band)} {filt} {_f32text(t1)} {_f32text(t2)} {d}")
     with open(path, "w") as f:
         f.write("\n".join(lines) + "\n")
+
+
+# ---- inputs of the inversion (inv.LSQR solver_damp_smooth) ---------------------------------
+
+def write_kernel_row_file(path: str, nblk: int, idx, coef, ker0: float = 1.0):
+    """One measurement's kernel row for one component as the inversion reads it: Fortran
+    unformatted sequential records (4-byte length markers) of (num_blk, ker0), (ncoef) and
+    the ncoef pairs (1-based block index, single-precision coefficient)."""
+    import struct
+    idx = np.asarray(idx, np.int32)
+    coef = np.asarray(coef, np.float32)
+    pairs = np.empty(idx.size, dtype=[("i", "<i4"), ("c", "<f4")])
+    pairs["i"], pairs["c"] = idx, coef
+
+    def rec(payload: bytes) -> bytes:
+        return struct.pack("<i", len(payload)) + payload + struct.pack("<i", len(payload))
+    with open(path, "wb") as f:
+        f.write(rec(struct.pack("<if", int(nblk), float(ker0))))
+        f.write(rec(struct.pack("<i", idx.size)))
+        f.write(rec(pairs.tobytes()))
+
+
+def write_smoothing_file(path: str, nblk: int, rows):
+    """The smoothing operator: num_blk, number of rows, widest row, total entries; then per
+    row ncoef, its 1-based block indices and its coefficients.  rows: (idx, coef) pairs."""
+    nel = sum(len(r[0]) for r in rows)
+    nbd = max((len(r[0]) for r in rows), default=0)
+    lines = [f"{int(nblk)} {len(rows)} {nbd} {nel}"]
+    for idx, coef in rows:
+        lines.append(" ".join([str(len(idx))] + [str(int(i)) for i in idx] + [_f32text(c) for c in coef]))
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")

@@ -1,7 +1,8 @@
 """ORACLE — test infrastructure, never the product.
 
-ctypes binding of the CPU restatements in fwant_oracle.cpp (the forward solver) and
-sgtker_oracle.cpp (the sensitivity-kernel accumulation).  `Oracle` has the same
+ctypes binding of the CPU restatements in fwant_oracle.cpp (the forward solver),
+sgtker_oracle.cpp (the sensitivity-kernel accumulation) and lsqr_oracle.cpp (the LSQR
+inversion solver).  `Oracle` has the same
 set-up methods as `fwant_gb300.Solver`, so a test feeds both from one Model.  Only the
 tests, `__graft_entry__.smoke()` and the `cpu_baseline` leg of `bench.py` use it.
 """
@@ -14,7 +15,8 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SRCS = [os.path.join(HERE, "fwant_oracle.cpp"), os.path.join(HERE, "sgtker_oracle.cpp")]
+SRCS = [os.path.join(HERE, "fwant_oracle.cpp"), os.path.join(HERE, "sgtker_oracle.cpp"),
+        os.path.join(HERE, "lsqr_oracle.cpp")]
 LIB = os.path.join(HERE, "_build", "libfwant_oracle.so")
 COMPONENTS = ("Vx", "Vy", "Vz", "Txx", "Tyy", "Tzz", "Txy", "Txz", "Tyz")
 
@@ -55,6 +57,9 @@ _SIGS = [
                                 C.c_int, _dp]),
     ("orc_scatter2kernel", None, [C.c_longlong, C.c_int, C.c_int, C.c_int, C.c_double, _fp, _fp, _dp, _dp,
                                   C.c_double, C.c_int, _dp, _dp, _dp, _dp]),
+    ("orc_lsqr", C.c_longlong, [C.c_longlong, C.c_longlong, C.POINTER(C.c_longlong), _ip, _dp, _dp, C.c_double,
+                                 C.c_double, C.c_longlong, _dp, _dp, _dp, _ip]),
+    ("orc_lgtsol", None, [C.c_longlong, C.c_longlong, C.c_double, _dp, _dp]),
     ("orc_scatter2kernel_dv", None, [C.c_longlong, C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp, _dp, _dp,
                                      C.c_double, _dp, _dp, _dp, _dp]),
 ]
@@ -175,6 +180,27 @@ def scatter2kernel_filtered(v, u, ka, kb, dt, nt1, nt2, sgt_m0, b, a, mode):
     lib().orc_scatter2kernel_dv(npts, knt, int(nt1), int(nt2), float(dt), _p(fv), _p(fu), _p(fa), _p(fb),
                                 float(sgt_m0), *[_p(o) for o in outs])
     return tuple(outs)
+
+
+def lsqr(row_ptr, col, val, b, ncol, atol=1e-7, btol=1e-7, maxit=30000):
+    """slsqr + lgtsol of inv.LSQR/mod_LSQR.f90 on a compressed-row matrix (0-based).
+    Returns dict(x, serr, sig, itct, flag, anorm, res2, test1, test2, phibar, xnorm); serr
+    for all ncol unknowns."""
+    rp = np.ascontiguousarray(row_ptr, np.int64)
+    ci = np.ascontiguousarray(col, np.int32)
+    va = _d(val)
+    b_ = _d(b)
+    nrow = rp.size - 1
+    x = np.zeros(int(ncol))
+    sig = np.zeros(int(ncol))
+    info = np.zeros(6)
+    flag = C.c_int()
+    it = lib().orc_lsqr(nrow, int(ncol), rp.ctypes.data_as(C.POINTER(C.c_longlong)), _p(ci, C.c_int), _p(va), _p(b_),
+                        float(atol), float(btol), int(maxit), _p(x), _p(sig), _p(info), C.byref(flag))
+    serr = np.zeros(int(ncol))
+    lib().orc_lgtsol(nrow, int(ncol), float(info[1]), _p(sig), _p(serr))
+    return dict(x=x, serr=serr, sig=sig, itct=int(it), flag=flag.value, anorm=info[0], res2=info[1], test1=info[2],
+                test2=info[3], phibar=info[4], xnorm=info[5])
 
 
 class Oracle:
