@@ -4,8 +4,8 @@
 // Layout in HBM: A in compressed rows (row offsets int64, columns int32, values FP64) and
 // the same entries in compressed columns (built once on the host, rows ascending within a
 // column), so both products are gathers: A v over rows, A^T u over columns, with the rows
-// (columns) split by length into three classes handled one thread, eight lanes or a warp
-// per row, each summing its entries in a fixed order.  Vectors u (nrow) and v, w, x, sig
+// (columns) split by length into four classes handled one thread, eight lanes, a warp or a
+// block per row, each summing its entries in a fixed order.  Vectors u (nrow) and v, w, x, sig
 // (ncol) are FP64.
 //
 // One iteration is seven launches: rows (u = A v - alpha u, partial |u|^2), normalise u
@@ -63,21 +63,27 @@ __device__ double block_sum(double v, double* sh) {
   return t;
 }
 
-// Compressed rows (or columns) with their rows split by length into three classes, each
-// a list of row numbers: short rows (<= SHORT_ROW_MAX entries) one thread per row, medium rows
-// eight lanes per row, long rows (>= LONG_ROW_MIN) a warp per row with four independent
-// accumulators.  Row lengths of an inversion system are bimodal (measurement rows with
-// thousands of kernel entries, damping and smoothing rows with one or two), and a warp per
-// row would leave most lanes idle on a chain of dependent loads.
+// Compressed rows (or columns) with their rows split by length into four classes, each a
+// list of row numbers: short rows (<= SHORT_ROW_MAX entries) one thread per row, medium
+// rows eight lanes per row, long rows (>= LONG_ROW_MIN) a warp per row, very long rows
+// (>= BLOCK_ROW_MIN) a whole block per row; every lane keeps four independent accumulators.
+// Row lengths of an inversion system are bimodal (measurement rows with thousands of kernel
+// entries, damping and smoothing rows with one or two).  GB300 issues FP64 at a rate close
+// to its HBM rate for this product (one FMA per 12-byte entry), so the classes keep the
+// reduction's extra FP64 adds per row small against the row's FMAs: eight lanes up to 64
+// entries a lane, and a block per row only where a warp per row would leave the GPU with
+// fewer rows than warps.
 constexpr int SHORT_ROW_MAX = 4;
-constexpr int LONG_ROW_MIN = 96;
+constexpr int LONG_ROW_MIN = 512;
+constexpr int BLOCK_ROW_MIN = 4096;
+constexpr int NCLS = 4;
 
 struct Sparse {
   const long long* ptr;
   const int* idx;
   const double* val;
-  const int* cls[3];   // row numbers of the short, medium and long classes
-  long long ncls[3];
+  const int* cls[NCLS];  // row numbers of the short, medium, long and very long classes
+  long long ncls[NCLS];
 };
 
 // y = sum over row r's entries of val * in[idx] by W lanes (lane `sub` of the group takes
@@ -131,6 +137,16 @@ __global__ void __launch_bounds__(LS_THREADS) gather_kernel(const Sparse A, cons
   const double factor = which == 0 ? S->alpha : which == 1 ? S->beta : 0.0;
   const bool subtract = which != 2;
   double sq = 0.0;
+  // very long rows: a block per row (the loop is uniform over the block)
+  for (long long g = blockIdx.x; g < A.ncls[3]; g += gridDim.x) {
+    const int r = A.cls[3][g];
+    const double y = block_sum(row_dot<LS_THREADS>(A, r, threadIdx.x, in), sh);
+    if (threadIdx.x == 0) {
+      const double o = subtract ? __dsub_rn(y, __dmul_rn(out[r], factor)) : y;
+      out[r] = o;
+      sq = fma(o, o, sq);
+    }
+  }
   gather_class<32>(A, 2, in, out, factor, subtract, sq);
   gather_class<8>(A, 1, in, out, factor, subtract, sq);
   gather_class<1>(A, 0, in, out, factor, subtract, sq);
@@ -366,13 +382,13 @@ fwant_status fwant_lsqr_create(long long nrow, long long ncol, const long long* 
       }
   }
   // length classes of the rows and of the columns, each list ascending
-  auto classes = [](const long long* ptr, long long n, std::vector<int>& lst, long long cnt[3]) {
+  auto classes = [](const long long* ptr, long long n, std::vector<int>& lst, long long cnt[NCLS]) {
     lst.clear();
-    for (int c = 0; c < 3; ++c) {
+    for (int c = 0; c < NCLS; ++c) {
       cnt[c] = 0;
       for (long long r = 0; r < n; ++r) {
         const long long len = ptr[r + 1] - ptr[r];
-        const int k = len <= SHORT_ROW_MAX ? 0 : len >= LONG_ROW_MIN ? 2 : 1;
+        const int k = len <= SHORT_ROW_MAX ? 0 : len < LONG_ROW_MIN ? 1 : len < BLOCK_ROW_MIN ? 2 : 3;
         if (k == c) {
           lst.push_back(int(r));
           ++cnt[c];
@@ -381,7 +397,7 @@ fwant_status fwant_lsqr_create(long long nrow, long long ncol, const long long* 
     }
   };
   std::vector<int> rows_cls, cols_cls;
-  long long nrc[3], ncc[3];
+  long long nrc[NCLS], ncc[NCLS];
   classes(row_ptr, nrow, rows_cls, nrc);
   classes(cp.data(), ncol, cols_cls, ncc);
   fwant_status rc = FWANT_OK;
@@ -413,10 +429,17 @@ fwant_status fwant_lsqr_create(long long nrow, long long ncol, const long long* 
   if (e == cudaSuccess) e = cudaMemcpy(l->cls_rows, rows_cls.data(), nr * sizeof(int), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(l->cls_cols, cols_cls.data(), nc * sizeof(int), cudaMemcpyHostToDevice);
   {
-    l->A = Sparse{l->rp, l->ci, l->va, {l->cls_rows, l->cls_rows + nrc[0], l->cls_rows + nrc[0] + nrc[1]},
-                  {nrc[0], nrc[1], nrc[2]}};
-    l->At = Sparse{l->cp, l->ri, l->vt, {l->cls_cols, l->cls_cols + ncc[0], l->cls_cols + ncc[0] + ncc[1]},
-                   {ncc[0], ncc[1], ncc[2]}};
+    l->A = Sparse{l->rp, l->ci, l->va, {}, {}};
+    l->At = Sparse{l->cp, l->ri, l->vt, {}, {}};
+    long long ro = 0, co = 0;
+    for (int c = 0; c < NCLS; ++c) {
+      l->A.cls[c] = l->cls_rows + ro;
+      l->A.ncls[c] = nrc[c];
+      ro += nrc[c];
+      l->At.cls[c] = l->cls_cols + co;
+      l->At.ncls[c] = ncc[c];
+      co += ncc[c];
+    }
   }
   if (e == cudaSuccess) {
     // |A|_F once (slsqr :157-158)

@@ -37,23 +37,33 @@ def _inversion_system(ndata, nblk, seed, density=0.05, lam=0.2, eta=0.5):
     return G, b
 
 
-@pytest.mark.parametrize("ndata,nblk,k", [(200, 300, 5), (2000, 1500, 3), (2000, 1500, 40), (5000, 400, 60)])
-def test_fixed_iterations_match_restatement(ndata, nblk, k, oracle_mod, native_lib):
+# the last two systems put rows (columns) in the warp-per-row and block-per-row length
+# classes: 300 x 6000 at density 0.8 has rows of ~4800 entries, 3000 x 600 at density 0.3
+# columns of ~900.  tol = (x, relative to max |x|; standard errors; phibar) for k <= 5: the
+# restatement against itself on row-permuted input moves them by 1.3e-8, 1.4e-5 and 1.7e-9
+# on the first dense system (its early iterates are already sensitive to the summation
+# order), by 3e-11, 2.6e-9 and 6e-16 on the second, and by < 1e-14 on the sparse ones
+@pytest.mark.parametrize("ndata,nblk,k,density,tol", [
+    (200, 300, 5, 0.05, (1e-10, 1e-8, 1e-10)), (2000, 1500, 3, 0.05, (1e-10, 1e-8, 1e-10)),
+    (2000, 1500, 40, 0.05, None), (5000, 400, 60, 0.05, None),
+    (300, 6000, 5, 0.8, (2e-7, 2e-4, 3e-8)), (3000, 600, 5, 0.3, (1e-9, 5e-8, 1e-10))])
+def test_fixed_iterations_match_restatement(ndata, nblk, k, density, tol, oracle_mod, native_lib):
     import fwant_gb300 as fw
-    G, b = _inversion_system(ndata, nblk, ndata + k)
+    G, b = _inversion_system(ndata, nblk, ndata + k, density=density)
     ncol = G.shape[1]
     ref = oracle_mod.lsqr(G.indptr, G.indices, G.data, b, ncol, atol=0.0, btol=0.0, maxit=k)
     L = fw.Lsqr(G.indptr, G.indices, G.data, b, ncol)
     assert L.solve(0.0, 0.0, k) == k
     x, serr = L.solution()
     info = L.info()
-    assert info["anorm"] == pytest.approx(ref["anorm"], rel=1e-13)
+    # |A|_F: a blocked against a sequential FP64 sum of up to 1.5 M squares (sqrt(n) eps ~ 1e-13)
+    assert info["anorm"] == pytest.approx(ref["anorm"], rel=1e-11)
     # phibar is the residual norm of the device's own iterate
     assert info["phibar"] == pytest.approx(np.linalg.norm(b - G @ x), rel=1e-7)
-    if k <= 5:
-        np.testing.assert_allclose(x, ref["x"], rtol=0, atol=1e-10 * np.abs(ref["x"]).max())
-        np.testing.assert_allclose(serr, ref["serr"], rtol=1e-8)
-        assert info["phibar"] == pytest.approx(ref["phibar"], rel=1e-10)
+    if tol is not None:
+        np.testing.assert_allclose(x, ref["x"], rtol=0, atol=tol[0] * np.abs(ref["x"]).max())
+        np.testing.assert_allclose(serr, ref["serr"], rtol=tol[1])
+        assert info["phibar"] == pytest.approx(ref["phibar"], rel=tol[2])
     else:
         # mid-run, correct implementations differ by the rounding LSQR amplifies: on the
         # 2000 x 1500 system at iteration 40 scipy's LSQR against itself on permuted rows
