@@ -117,6 +117,20 @@ EXPORTS = [
     ("fwant_lsqr_info", C.c_int, [_vp, C.POINTER(C.c_double)]),
     ("fwant_lsqr_multiply", C.c_int, [_vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("fwant_lsqr_last_solve_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
+    # medium preprocessor (include/fwant_media.h)
+    ("fwant_media_create", C.c_int, [C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, C.c_float, C.POINTER(C.c_int), C.c_int,
+                                     C.POINTER(C.c_void_p)]),
+    ("fwant_media_destroy", None, [_vp]),
+    ("fwant_media_last_error", C.c_char_p, [_vp]),
+    ("fwant_media_set_cart1d", C.c_int, [_vp, C.c_int, _fp, _fp, _fp, _fp]),
+    ("fwant_media_set_layers", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int] + [_fp] * 10),
+    ("fwant_media_set_volume", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, C.c_float, _fp, _fp,
+                                         _fp]),
+    ("fwant_media_set_verpoly", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, C.c_float]
+     + [_fp] * 6),
+    ("fwant_media_eval", C.c_int, [_vp, _fp, _fp, _fp]),
+    ("fwant_media_stept_check", C.c_int, [_vp, _fp, C.POINTER(C.c_int), _fp, _fp]),
+    ("fwant_media_last_eval_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
 ]
 
 
@@ -597,6 +611,99 @@ class Lsqr:
     def last_solve_ms(self):
         ms = C.c_double()
         self._chk(self._lib.fwant_lsqr_last_solve_ms(self._h, C.byref(ms)))
+        return ms.value
+
+
+def _fo(a):
+    if a is None:
+        return None
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1, order="F"))
+
+
+class Media:
+    """The medium preprocessor on the GPU (seis3d_media: effmedia_eval, media_extend,
+    media_stept_check).  Grid x[ni+6], y[nj+6], z[nk+6] (radians, metres) with ghosts;
+    model arrays in Fortran index order (a[i, j, k], first index fastest)."""
+
+    INTERFACE, LAYERED, COMPOSITE = 2, 3, 4
+
+    def __init__(self, ni, nj, nk, x, y, z, ztopo, half_sample=(1, 1, 1), device=0):
+        self._lib = load_library()
+        self.shape = (ni + 6, nj + 6, nk + 6)
+        self._keep = []
+        hs = np.ascontiguousarray(half_sample, np.int32)
+        h = C.c_void_p()
+        g = [_fo(x), _fo(y), _fo(z)]
+        rc = self._lib.fwant_media_create(int(ni), int(nj), int(nk), *[_ptr(a) for a in g], float(ztopo),
+                                          _ptr(hs, C.c_int), int(device), C.byref(h))
+        if rc != 0:
+            raise FwantError(rc, "fwant_media_create failed")
+        self._h = h
+
+    def _chk(self, rc):
+        if rc != 0:
+            raise FwantError(rc, self._lib.fwant_media_last_error(self._h).decode())
+
+    def _fp(self, a):
+        a = _fo(a)
+        if a is None:
+            return None
+        self._keep.append(a)
+        return _ptr(a)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.fwant_media_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_cart1d(self, depth, vp, vs, rho):
+        self._chk(self._lib.fwant_media_set_cart1d(self._h, len(depth), *[self._fp(a) for a in (depth, vp, vs, rho)]))
+
+    def set_layers(self, kind, x, y, z, h, vp, vs, rho, vp_exp=None, vs_exp=None, rho_exp=None):
+        ni, nj, nk = np.shape(h)
+        self._chk(self._lib.fwant_media_set_layers(
+            self._h, int(kind), ni, nj, nk, *[self._fp(a) for a in (x, y, z, h, vp, vs, rho, vp_exp, vs_exp, rho_exp)]))
+
+    def set_volume(self, perturbed, x, y, rz, rz0, vp, vs, rho):
+        ni, nj, nk = np.shape(vp)
+        self._chk(self._lib.fwant_media_set_volume(self._h, int(perturbed), ni, nj, nk, self._fp(x), self._fp(y),
+                                                   self._fp(rz), float(rz0), self._fp(vp), self._fp(vs),
+                                                   self._fp(rho)))
+
+    def set_verpoly(self, perturbed, x, y, rz, rz0, vp_c, vs_c, rho_c, vp_exp, vs_exp, rho_exp):
+        ni, nj, nk, npoly = np.shape(vp_c)
+        self._chk(self._lib.fwant_media_set_verpoly(
+            self._h, int(perturbed), ni, nj, nk, npoly, self._fp(x), self._fp(y), self._fp(rz), float(rz0),
+            *[self._fp(a) for a in (vp_c, vs_c, rho_c, vp_exp, vs_exp, rho_exp)]))
+
+    def eval(self, copy=True):
+        """(lambda, mu, rho), each (ni+6, nj+6, nk+6) float32 with ghosts extended; with
+        copy=False the medium stays on the device (for stept_check) and None is returned."""
+        if not copy:
+            self._chk(self._lib.fwant_media_eval(self._h, None, None, None))
+            return None
+        n = int(np.prod(self.shape))
+        outs = [np.zeros(n, np.float32) for _ in range(3)]
+        self._chk(self._lib.fwant_media_eval(self._h, *[_ptr(o) for o in outs]))
+        return tuple(o.reshape(self.shape, order="F") for o in outs)
+
+    def stept_check(self):
+        """(dtmax, (i, j, k) 1-based local index, Vp, dL) of the last eval."""
+        dt, vp, dl = C.c_float(), C.c_float(), C.c_float()
+        ijk = np.zeros(3, np.int32)
+        self._chk(self._lib.fwant_media_stept_check(self._h, C.byref(dt), _ptr(ijk, C.c_int), C.byref(vp),
+                                                    C.byref(dl)))
+        return dt.value, tuple(int(v) for v in ijk), vp.value, dl.value
+
+    def last_eval_ms(self):
+        ms = C.c_double()
+        self._chk(self._lib.fwant_media_last_eval_ms(self._h, C.byref(ms)))
         return ms.value
 
 

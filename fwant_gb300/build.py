@@ -31,7 +31,9 @@ CPP_FLAGS = ["-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-con
 SOURCES = ["stage_fast_rk0.cu", "stage_fast_rk1.cu", "stage_fast_rk2.cu", "stage_exact_rk0.cu",
            "stage_exact_rk1.cu", "stage_exact_rk2.cu", "stage_bf16_rk0.cu", "stage_bf16_rk1.cu",
            "stage_bf16_rk2.cu", "stage_fp16_rk0.cu", "stage_fp16_rk1.cu", "stage_fp16_rk2.cu",
-           "stage_dispatch.cu", "aux.cu", "snapshot.cu", "sgtker.cu", "surrogate.cu", "lsqr.cu", "solver.cpp", "sgtker_api.cpp"]
+           "stage_dispatch.cu", "aux.cu", "snapshot.cu", "sgtker.cu", "surrogate.cu", "lsqr.cu", "media.cu", "solver.cpp", "sgtker_api.cpp"]
+# units whose FP32 expressions must round like the reference's source (no contraction)
+EXACT_SOURCES = {"media.cu"}
 
 
 EXE = os.path.join(HERE, "bin", "fwant_wave")
@@ -86,7 +88,7 @@ def build(verbose: bool = False, force: bool = False, jobs: int | None = None) -
         objs.append(obj)
         if force or _stale(obj, [path] + hdrs):
             flags = CU_FLAGS + ARCH if src.endswith(".cu") else CPP_FLAGS
-            if "exact" in src:
+            if "exact" in src or src in EXACT_SOURCES:
                 flags = flags + EXACT_FLAGS
             jobs_todo.append([nvcc, *flags, "-I", CSRC, "-I", INCLUDE, "-c", path, "-o", obj])
     if jobs_todo:

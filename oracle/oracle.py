@@ -1,8 +1,8 @@
 """ORACLE — test infrastructure, never the product.
 
 ctypes binding of the CPU restatements in fwant_oracle.cpp (the forward solver),
-sgtker_oracle.cpp (the sensitivity-kernel accumulation) and lsqr_oracle.cpp (the LSQR
-inversion solver).  `Oracle` has the same
+sgtker_oracle.cpp (the sensitivity-kernel accumulation), lsqr_oracle.cpp (the LSQR
+inversion solver) and media_oracle.cpp (the medium preprocessor).  `Oracle` has the same
 set-up methods as `fwant_gb300.Solver`, so a test feeds both from one Model.  Only the
 tests, `__graft_entry__.smoke()` and the `cpu_baseline` leg of `bench.py` use it.
 """
@@ -16,7 +16,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRCS = [os.path.join(HERE, "fwant_oracle.cpp"), os.path.join(HERE, "sgtker_oracle.cpp"),
-        os.path.join(HERE, "lsqr_oracle.cpp")]
+        os.path.join(HERE, "lsqr_oracle.cpp"), os.path.join(HERE, "media_oracle.cpp")]
 LIB = os.path.join(HERE, "_build", "libfwant_oracle.so")
 COMPONENTS = ("Vx", "Vy", "Vz", "Txx", "Tyy", "Tzz", "Txy", "Txz", "Tyz")
 
@@ -60,6 +60,17 @@ _SIGS = [
     ("orc_lsqr", C.c_longlong, [C.c_longlong, C.c_longlong, C.POINTER(C.c_longlong), _ip, _dp, _dp, C.c_double,
                                  C.c_double, C.c_longlong, _dp, _dp, _dp, _ip]),
     ("orc_lgtsol", None, [C.c_longlong, C.c_longlong, C.c_double, _dp, _dp]),
+    ("orc_media_create", _vp, [C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, C.c_float, _ip]),
+    ("orc_media_destroy", None, [_vp]),
+    ("orc_media_last_error", C.c_char_p, [_vp]),
+    ("orc_media_set_cart1d", None, [_vp, C.c_int, _fp, _fp, _fp, _fp]),
+    ("orc_media_set_layers", None, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, _fp, _fp, _fp, _fp, _fp,
+                                    _fp, _fp]),
+    ("orc_media_set_volume", None, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, C.c_float, _fp, _fp, _fp]),
+    ("orc_media_set_verpoly", None, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, C.c_float, _fp,
+                                     _fp, _fp, _fp, _fp, _fp]),
+    ("orc_media_eval", C.c_int, [_vp, _fp, _fp, _fp]),
+    ("orc_media_stept_check", None, [_vp, _fp, _fp, _fp, _fp, _ip, _fp, _fp]),
     ("orc_scatter2kernel_dv", None, [C.c_longlong, C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp, _dp, _dp,
                                      C.c_double, _dp, _dp, _dp, _dp]),
 ]
@@ -201,6 +212,76 @@ def lsqr(row_ptr, col, val, b, ncol, atol=1e-7, btol=1e-7, maxit=30000):
     lib().orc_lgtsol(nrow, int(ncol), float(info[1]), _p(sig), _p(serr))
     return dict(x=x, serr=serr, sig=sig, itct=int(it), flag=flag.value, anorm=info[0], res2=info[1], test1=info[2],
                 test2=info[3], phibar=info[4], xnorm=info[5])
+
+
+def _fo(a):
+    """float32 Fortran-order flattening, or NULL for None"""
+    if a is None:
+        return None
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1, order="F"))
+
+
+class MediaOracle:
+    """CPU restatement of seis3d_media's effmedia_eval, media_extend and media_stept_check,
+    with the same set-up methods as `fwant_gb300.Media` (arrays in Fortran index order:
+    a[i, j, k])."""
+
+    def __init__(self, ni, nj, nk, x, y, z, ztopo, half_sample=(1, 1, 1)):
+        self._L = lib()
+        self.shape = (ni + 6, nj + 6, nk + 6)
+        self._keep = [_fo(x), _fo(y), _fo(z)]
+        hs = np.ascontiguousarray(half_sample, np.int32)
+        self._h = self._L.orc_media_create(ni, nj, nk, *[_p(a, C.c_float) for a in self._keep], float(ztopo),
+                                           _p(hs, C.c_int))
+        self.result = None
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._L.orc_media_destroy(self._h)
+            self._h = None
+
+    def _fp(self, a):
+        a = _fo(a)
+        if a is None:
+            return None
+        self._keep.append(a)
+        return _p(a, C.c_float)
+
+    def set_cart1d(self, depth, vp, vs, rho):
+        self._L.orc_media_set_cart1d(self._h, len(depth), *[self._fp(a) for a in (depth, vp, vs, rho)])
+
+    def set_layers(self, kind, x, y, z, h, vp, vs, rho, vp_exp=None, vs_exp=None, rho_exp=None):
+        ni, nj, nk = np.shape(h)
+        self._L.orc_media_set_layers(self._h, int(kind), ni, nj, nk,
+                                     *[self._fp(a) for a in (x, y, z, h, vp, vs, rho, vp_exp, vs_exp, rho_exp)])
+
+    def set_volume(self, perturbed, x, y, rz, rz0, vp, vs, rho):
+        ni, nj, nk = np.shape(vp)
+        self._L.orc_media_set_volume(self._h, int(perturbed), ni, nj, nk, self._fp(x), self._fp(y), self._fp(rz),
+                                     float(rz0), self._fp(vp), self._fp(vs), self._fp(rho))
+
+    def set_verpoly(self, perturbed, x, y, rz, rz0, vp_c, vs_c, rho_c, vp_exp, vs_exp, rho_exp):
+        ni, nj, nk, npoly = np.shape(vp_c)
+        self._L.orc_media_set_verpoly(self._h, int(perturbed), ni, nj, nk, npoly, self._fp(x), self._fp(y),
+                                      self._fp(rz), float(rz0),
+                                      *[self._fp(a) for a in (vp_c, vs_c, rho_c, vp_exp, vs_exp, rho_exp)])
+
+    def eval(self):
+        """(lambda, mu, rho), each (ni+6, nj+6, nk+6) float32, ghosts extended."""
+        n = int(np.prod(self.shape))
+        outs = [np.zeros(n, np.float32) for _ in range(3)]
+        if self._L.orc_media_eval(self._h, *[_p(o, C.c_float) for o in outs]) != 0:
+            raise RuntimeError(self._L.orc_media_last_error(self._h).decode())
+        self.result = outs
+        return tuple(o.reshape(self.shape, order="F") for o in outs)
+
+    def stept_check(self):
+        """(dtmax, (i, j, k) 1-based local index, Vp, dL) of the last eval."""
+        dt, vp, dl = C.c_float(), C.c_float(), C.c_float()
+        ijk = np.zeros(3, np.int32)
+        self._L.orc_media_stept_check(self._h, *[_p(o, C.c_float) for o in self.result], C.byref(dt),
+                                      _p(ijk, C.c_int), C.byref(vp), C.byref(dl))
+        return dt.value, tuple(int(v) for v in ijk), vp.value, dl.value
 
 
 class Oracle:
