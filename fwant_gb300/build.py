@@ -42,6 +42,8 @@ KER_EXE = os.path.join(HERE, "bin", "fwant_ker")
 KER_SOURCES = ["fwant_ker.cpp", "netcdf3.cpp", "conf.cpp"]
 LSQR_EXE = os.path.join(HERE, "bin", "fwant_lsqr")
 LSQR_SOURCES = ["fwant_lsqr.cpp"]
+MEDIA_EXE = os.path.join(HERE, "bin", "fwant_media")
+MEDIA_SOURCES = ["fwant_media.cpp", "netcdf3.cpp", "conf.cpp"]
 
 
 def _nvcc() -> str:
@@ -98,8 +100,10 @@ def build(verbose: bool = False, force: bool = False, jobs: int | None = None) -
         _run([nvcc, "-shared", *ARCH, "-o", LIB, *objs, "-lcudart"], verbose)
     # the programs over the C ABI: the solver stage (SeisFD3D.conf + NetCDF files in and
     # out), the sensitivity-kernel stage (TomoKernel.conf, sgt_ files in, kernel files out)
-    # and the inversion (data list, kernel rows, smoothing operator in; model files out)
-    for exe, srcs in ((EXE, EXE_SOURCES), (KER_EXE, KER_SOURCES), (LSQR_EXE, LSQR_SOURCES)):
+    # the inversion (data list, kernel rows, smoothing operator in; model files out) and
+    # the medium preprocessor (media configuration and model files in; media file out)
+    for exe, srcs in ((EXE, EXE_SOURCES), (KER_EXE, KER_SOURCES), (LSQR_EXE, LSQR_SOURCES),
+                      (MEDIA_EXE, MEDIA_SOURCES)):
         exe_src = [os.path.join(CSRC, f) for f in srcs]
         if force or _stale(exe, exe_src + hdrs + [LIB]):
             os.makedirs(os.path.dirname(exe), exist_ok=True)

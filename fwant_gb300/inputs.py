@@ -524,3 +524,116 @@ def write_smoothing_file(path: str, nblk: int, rows):
         lines.append(" ".join([str(len(idx))] + [str(int(i)) for i in idx] + [_f32text(c) for c in coef]))
     with open(path, "w") as f:
         f.write("\n".join(lines) + "\n")
+
+
+# ---- inputs of the medium preprocessor (seis3d_media) ---------------------------------------
+
+def write_media_conf(path: str, background, perturbed=None, half_sample=(1, 1, 1)):
+    """The media configuration init_media reads (code/srcF/seis3d_media.F90:264-338):
+    background = (type, format, file name); perturbed likewise or None."""
+    lines = ["half_sample_point = " + " ".join(str(int(v)) for v in half_sample),
+             f"background_type = {background[0]}", f"background_format = {background[1]}",
+             f"background_filename = {background[2]}"]
+    if perturbed is None:
+        lines.append("perturbed_type = none")
+    else:
+        lines += [f"perturbed_type = {perturbed[0]}", f"perturbed_format = {perturbed[1]}",
+                  f"perturbed_filename = {perturbed[2]}"]
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def _units_lines(units):
+    return [f"distance2meter = {units[0]!r}", f"velocity2m/s = {units[1]!r}", f"density2kg/m^3 = {units[2]!r}"]
+
+
+def write_cart1d_file(path: str, z, rho, vp, vs, meaning="depth", units=(1.0, 1.0, 1.0)):
+    """An ascii cart1d model (layer1d_read :341-430): one record z rho Vp Vs per sample;
+    `meaning` axis, depth or thickness; units (distance, velocity, density) to SI."""
+    lines = [f"radial_sampling = {len(z)}"] + _units_lines(units) + [f"radial_meaning = {meaning}", "<anchor_data>"]
+    lines += [" ".join(_f32text(v) for v in row) for row in zip(z, rho, vp, vs)]
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def write_layer_file(path: str, kind: str, x_deg, y_deg, v, vp, vs, rho, meaning="depth", units=(1.0, 1.0, 1.0)):
+    """An ascii interface (kind "interface", v = interface heights (ni, nj, nk)) or layered
+    (kind "layered", v = depths or thicknesses per `meaning`) model (interface_read :433-532,
+    layered_read :535-643); vp, vs, rho (2, nk); x, y in degrees."""
+    v = np.asarray(v, np.float32)
+    ni, nj, nk = v.shape
+    key = "number_of_interface" if kind == "interface" else "number_of_layer"
+    lines = [f"{key} = {nk}"] + _units_lines(units) + [f"horizontal_sampling = {ni} {nj}"]
+    if kind != "interface":
+        lines.append(f"layer_meaning = {meaning}")
+    lines.append("<anchor_media>")
+    vp, vs, rho = (np.asarray(a, np.float32).reshape(2, nk, order="F") for a in (vp, vs, rho))
+    for k in range(nk):
+        lines.append(" ".join(_f32text(a[s, k]) for a in (vp, vs, rho) for s in range(2)))
+    lines.append("<anchor_interface>" if kind == "interface" else "<anchor_layer>")
+    for j in range(nj):
+        for i in range(ni):
+            lines.append(" ".join([_f32text(x_deg[i]), _f32text(y_deg[j])] + [_f32text(v[i, j, k]) for k in range(nk)]))
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def _nc_fortran(f, name, a, dims):
+    """a variable whose Fortran shape is a.shape, dimensions listed fastest first"""
+    a = np.asarray(a, np.float32)
+    v = f.createVariable(name, "f4", tuple(reversed(dims)))
+    v[:] = a.transpose(tuple(reversed(range(a.ndim))))
+
+
+def write_composite_nc(path: str, x_deg, y_deg, h, vp, vs, rho, vp_exp, vs_exp, rho_exp):
+    """A composite model (composite_read :646-702): thickness (ni, nj, nk), Vp, Vs, rho
+    (2, ni, nj, nk) and the exponents (nk)."""
+    from scipy.io import netcdf_file
+    h = np.asarray(h, np.float32)
+    ni, nj, nk = h.shape
+    with netcdf_file(path, "w", version=1) as f:
+        for d, n in (("theta", ni), ("phi", nj), ("layer", nk), ("side", 2)):
+            f.createDimension(d, n)
+        _nc_fortran(f, "theta", x_deg, ("theta",))
+        _nc_fortran(f, "phi", y_deg, ("phi",))
+        _nc_fortran(f, "thickness", h, ("theta", "phi", "layer"))
+        for name, a in (("Vp", vp), ("Vs", vs), ("rho", rho)):
+            _nc_fortran(f, name, a, ("side", "theta", "phi", "layer"))
+        for name, a in (("Vp_poly_d", vp_exp), ("Vs_poly_d", vs_exp), ("rho_poly_d", rho_exp)):
+            _nc_fortran(f, name, a, ("layer",))
+
+
+def write_volume_nc(path: str, x_deg, y_deg, rz, sealevel, vp, vs, rho):
+    """A volume model (volume_init / volume_read :705-779): depth2sealevel (nk), global
+    attribute sealevel, Vp, Vs, rho (ni, nj, nk)."""
+    from scipy.io import netcdf_file
+    vp = np.asarray(vp, np.float32)
+    ni, nj, nk = vp.shape
+    with netcdf_file(path, "w", version=1) as f:
+        for d, n in (("theta", ni), ("phi", nj), ("depth", nk)):
+            f.createDimension(d, n)
+        f.sealevel = np.float32(sealevel)
+        _nc_fortran(f, "theta", x_deg, ("theta",))
+        _nc_fortran(f, "phi", y_deg, ("phi",))
+        _nc_fortran(f, "depth2sealevel", rz, ("depth",))
+        for name, a in (("Vp", vp), ("Vs", vs), ("rho", rho)):
+            _nc_fortran(f, name, a, ("theta", "phi", "depth"))
+
+
+def write_verpoly_nc(path: str, x_deg, y_deg, rz, sealevel, vp_c, vs_c, rho_c, vp_exp, vs_exp, rho_exp):
+    """A verpoly model (verpoly_init / verpoly_read :782-850): depth2sealevel (ni, nj, nk),
+    coefficients (ni, nj, nk, npoly), exponents (npoly), global attribute sealevel."""
+    from scipy.io import netcdf_file
+    vp_c = np.asarray(vp_c, np.float32)
+    ni, nj, nk, npoly = vp_c.shape
+    with netcdf_file(path, "w", version=1) as f:
+        for d, n in (("theta", ni), ("phi", nj), ("depth", nk), ("polynomial", npoly)):
+            f.createDimension(d, n)
+        f.sealevel = np.float32(sealevel)
+        _nc_fortran(f, "theta", x_deg, ("theta",))
+        _nc_fortran(f, "phi", y_deg, ("phi",))
+        _nc_fortran(f, "depth2sealevel", rz, ("theta", "phi", "depth"))
+        for name, a in (("Vp_poly_c", vp_c), ("Vs_poly_c", vs_c), ("rho_poly_c", rho_c)):
+            _nc_fortran(f, name, a, ("theta", "phi", "depth", "polynomial"))
+        for name, a in (("Vp_poly_d", vp_exp), ("Vs_poly_d", vs_exp), ("rho_poly_d", rho_exp)):
+            _nc_fortran(f, name, a, ("polynomial",))
