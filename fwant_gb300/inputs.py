@@ -637,3 +637,56 @@ def write_verpoly_nc(path: str, x_deg, y_deg, rz, sealevel, vp_c, vs_c, rho_c, v
             _nc_fortran(f, name, a, ("theta", "phi", "depth", "polynomial"))
         for name, a in (("Vp_poly_d", vp_exp), ("Vs_poly_d", vs_exp), ("rho_poly_d", rho_exp)):
             _nc_fortran(f, name, a, ("polynomial",))
+
+
+def grid_c2(ni=400, nj=400, nk=200, dh_km=1.0, theta_c_deg=50.0, phi_c_deg=100.0, z_top_km=0.5, z_bottom_km=2.0):
+    """The grid (x, y, z with ghosts; radians and metres) of make_model for a size."""
+    dh_deg = dh_km / R_EARTH_KM * 180.0 / np.pi
+    x = grid_coords(ni, dh_deg, theta_c_deg - dh_deg * (ni - 1) / 2.0, None, 1.0, degrees=True)
+    y = grid_coords(nj, dh_deg, phi_c_deg - dh_deg * (nj - 1) / 2.0, None, 1.0, degrees=True)
+    z = grid_coords(nk, None, 0.0, stretched_depths_km(nk, z_top_km, z_bottom_km), 1000.0, degrees=False)
+    return x, y, z
+
+
+def media_models(x, y, z, seed=0, nlayers=4, vp_top=5.8, vp_bottom=8.0, perturb=0.05, corr_km=10.0,
+                 spacing_km=2.0):
+    """Seeded inputs of the medium preprocessor for a grid: a cart1d background of nlayers
+    constant-velocity layers (Vp from vp_top to vp_bottom km/s at seeded depths, each
+    interface a repeated depth; Vs = Vp / 1.73, Gardner density) and, for perturb > 0, a
+    volume perturbation of Vp and Vs (the same relative field, max |dv| = perturb, Gaussian
+    correlation corr_km) sampled every spacing_km over the grid.  Returns the set-up calls
+    of fwant_gb300.Media: [("set_cart1d", ...), ("set_volume", ...)]."""
+    rng = np.random.default_rng(seed)
+    f32 = np.float32
+    ztop = float(z[-1 - LENFD])
+    dmax = (ztop - float(z[0])) / 1000.0
+    iface = np.sort(rng.uniform(0.05, 0.9, nlayers - 1)) * dmax
+    vps = np.linspace(vp_top, vp_bottom, nlayers)
+    d = [0.0]
+    vp = [vps[0]]
+    for q, dz in enumerate(iface):
+        d += [dz, dz]
+        vp += [vps[q], vps[q + 1]]
+    d.append(dmax * 1.5)
+    vp.append(vps[-1])
+    d = (np.array(d) * 1000.0).astype(f32)
+    vp = (np.array(vp) * 1000.0).astype(f32)
+    calls = [("set_cart1d", (d, vp, (vp / f32(1.73)).astype(f32), (f32(1741.0) * (vp / f32(1000.0)) ** f32(0.25))))]
+    if perturb > 0.0:
+        r_km = ztop / 1000.0
+        span_x = (float(x[-1]) - float(x[0])) * r_km
+        span_y = (float(y[-1]) - float(y[0])) * r_km * np.sin(float(x[x.size // 2]))
+        mi, mj = int(span_x / spacing_km) + 3, int(span_y / spacing_km) + 3
+        mk = int(dmax * 1.2 / spacing_km) + 3
+        mx = np.linspace(float(x[0]), float(x[-1]), mi).astype(f32)
+        my = np.linspace(float(y[0]), float(y[-1]), mj).astype(f32)
+        rz = np.linspace(-1000.0, dmax * 1200.0, mk).astype(f32)
+        noise = rng.standard_normal((mi, mj, mk))
+        k = [np.fft.fftfreq(n, d=spacing_km) for n in (mi, mj)] + [np.fft.rfftfreq(mk, d=spacing_km)]
+        filt = np.exp(-(np.pi * corr_km) ** 2 * (k[0][:, None, None] ** 2 + k[1][None, :, None] ** 2
+                                                 + k[2][None, None, :] ** 2) / 2.0)
+        dv = np.fft.irfftn(np.fft.rfftn(noise) * filt, s=(mi, mj, mk), axes=(0, 1, 2))
+        dv = (dv - dv.mean()) * perturb / max(np.abs(dv - dv.mean()).max(), 1e-30)
+        dv = dv.astype(f32)
+        calls.append(("set_volume", (1, mx, my, rz, f32(ztop), dv, dv.copy(), np.zeros_like(dv))))
+    return calls

@@ -371,10 +371,7 @@ bool point(orc_media* m, int i, int j, int k, float* lam_out, float* mu_out, flo
             if (h <= SEIS_ZERO) continue;
             d = d + h;
             if (std::fabs(d - d0) <= dz2 / 5.0f) {
-              if (n == L.nk) {
-                m->err = "please increase the thickness of the lowest layer";
-                return false;
-              }
+              if (n == L.nk) return false;
               const int n1 = n;
               int n2 = L.nk;
               for (int mm = n + 1; mm <= L.nk; ++mm) {
@@ -415,7 +412,6 @@ bool point(orc_media* m, int i, int j, int k, float* lam_out, float* mu_out, flo
               }
               break;
             } else if (n == L.nk) {
-              m->err = "please increase the thickness of the lowest layer";
               return false;
             }
           }
@@ -668,12 +664,19 @@ void orc_media_set_verpoly(orc_media* m, int perturbed, int ni, int nj, int nk, 
 // effmedia_eval + media_extend; out arrays (nx, ny, nz), i fastest.  0 on success.
 int orc_media_eval(orc_media* m, float* lam, float* mu, float* rho) {
   const int nx = m->nx, ny = m->ny;
+  int bad = 0;
+  // points are independent: planes in parallel (OpenMP), each point's samples in order
+#pragma omp parallel for schedule(dynamic) reduction(| : bad)
   for (int k = LENFD; k < LENFD + m->nk; ++k)
     for (int j = LENFD; j < LENFD + m->nj; ++j)
       for (int i = LENFD; i < LENFD + m->ni; ++i) {
         const size_t p = (size_t(k) * ny + j) * nx + i;
-        if (!point(m, i, j, k, &lam[p], &mu[p], &rho[p])) return 1;
+        if (!point(m, i, j, k, &lam[p], &mu[p], &rho[p])) bad = 1;
       }
+  if (bad) {
+    m->err = "please increase the thickness of the lowest layer";
+    return 1;
+  }
   // extend_equal: each ghost takes the value of the nearest interior point (x, then y,
   // then z, as the reference's three passes leave it)
   for (float* w : {lam, mu, rho})
