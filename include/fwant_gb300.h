@@ -192,12 +192,11 @@ fwant_status fwant_get_snapshot(fwant_solver* s, const int subs[3], const int su
 
 /* fwant_get_snapshot without any device allocation.  No counterpart in the reference.
  *
- * For callers that must not allocate device memory at this point: code running while a
- * CUDA graph is being captured (an allocation would break the capture), monitoring or
- * output hooks that run in the middle of a long solve on a GPU whose memory is fully
- * committed to the wavefield registers (an allocation could fail with out-of-memory
- * partway through a run), and host programs that route every device allocation through
- * their own budgeted pool and forbid hidden library allocations.
+ * For callers that must not allocate device memory at this point: monitoring or output
+ * hooks that run in the middle of a long solve on a GPU whose memory is fully committed to
+ * the wavefield registers (an allocation could fail with out-of-memory partway through a
+ * run), and host programs that route every device allocation through their own budgeted
+ * pool and forbid hidden library allocations.
  *
  * Same arguments and output as fwant_get_snapshot.  The values are staged in a fixed
  * device array of 4,194,304 floats (16 MiB) that the library holds on every GPU it is

@@ -1,5 +1,5 @@
 """fwant_get_snapshot_noalloc: snapshot extraction for callers that must not allocate
-device memory (graph capture, a fully committed GPU, host programs with their own
+device memory (a GPU whose memory the wavefield fills, host programs with their own
 allocator).  Its output must equal fwant_get_snapshot's on two calls in a row: the
 second call, on a different sub-volume after more time steps, must not see anything left
 in the shared fixed staging array by the first.  This file is collected last so that a
