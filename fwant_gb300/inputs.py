@@ -110,7 +110,7 @@ def layered_media(x, y, z, seed: int, vp_top=5.8, vp_bottom=8.0, nlayers=4, pert
     """Node-sampled 1-D layered medium (Vp in km/s from vp_top to vp_bottom across
     seeded interfaces), Vs = Vp/1.73, rho = 1.741 Vp^0.25 g/cm^3, optional Gaussian-
     correlated relative perturbation of Vp and Vs scaled to max |dv| = perturb.
-    Returns lam, mu, rho (SI) with shape (nx, ny, nz)."""
+    Returns lam, mu, rho (SI) with shape (nx, ny, nz), Fortran-ordered."""
     rng = np.random.default_rng(seed)
     nx, ny, nz = x.size, y.size, z.size
     ztop = float(z[nz - 1 - LENFD])
@@ -131,7 +131,9 @@ def layered_media(x, y, z, seed: int, vp_top=5.8, vp_bottom=8.0, nlayers=4, pert
     vp_ms, vs_ms = vp * 1000.0, vs * 1000.0
     mu = rho * vs_ms ** 2
     lam = rho * vp_ms ** 2 - 2.0 * mu
-    return lam.astype(np.float32), mu.astype(np.float32), rho.astype(np.float32)
+    # stored in Fortran order (first index fastest), the layout of the reference's arrays
+    # and of the C ABI, so handing them to a solver needs no transposition
+    return tuple(np.asfortranarray(a, dtype=np.float32) for a in (lam, mu, rho))
 
 
 def gaussian_field(shape, x, y, z, corr_km, rng):
