@@ -123,6 +123,19 @@ __global__ void convert_kernel(long long n, const void* __restrict__ src, int sr
   }
 }
 
+// number of elements that are not > 0 (NaN included) into *count
+__global__ void count_nonpositive_kernel(long long n, const float* __restrict__ v, unsigned int* count) {
+  unsigned int c = 0;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+    c += !(v[e] > 0.0f);
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+}
+
+void launch_count_nonpositive(long long n, const float* v, unsigned int* count, void* stream) {
+  count_nonpositive_kernel<<<152 * 4, 256, 0, (cudaStream_t)stream>>>(n, v, count);
+}
+
 void launch_convert_to_f32(const Geom& g, const void* src, int storage, float inv_scale, float* dst, void* stream) {
   convert_kernel<<<152 * 8, 256, 0, (cudaStream_t)stream>>>(g.plane * g.nz, src, storage, inv_scale, dst, ST_F32);
 }

@@ -245,6 +245,8 @@ void launch_sincot_fp64(int n, const float* x, float* xsin, float* xcot, void* s
 // max |value| of each of the nine components (storage order) into out_bits[9]
 void launch_maxabs(const Geom& g, const void* w, int storage, float isv, float ist, unsigned int* out_bits,
                    void* stream);
+// count of the n values that are not > 0 (NaN included), added to *count
+void launch_count_nonpositive(long long n, const float* v, unsigned int* count, void* stream);
 // one component between storage type and FP32 (padded layout, scale applied)
 void launch_convert_to_f32(const Geom& g, const void* src, int storage, float inv_scale, float* dst, void* stream);
 void launch_convert_from_f32(const Geom& g, const float* src, int storage, float scale, void* dst, void* stream);

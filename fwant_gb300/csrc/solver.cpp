@@ -996,13 +996,39 @@ fwant_status fwant_set_media(fwant_solver* s, const float* lambda, const float* 
   cudaSetDevice(s->cfg.device);
   const auto& g = s->g;
   const size_t n = size_t(g.nx) * g.ny * g.nz;
-  for (size_t q = 0; q < n; ++q)
-    if (!(rho[q] > 0.0f)) return s->fail(FWANT_ERR_INVALID_ARG, "rho must be > 0 everywhere (ghosts included)");
-  s->h_rho.assign(rho, rho + n);
-  s->put3(s->lam, lambda);
-  s->put3(s->mu, mu);
-  cudaError_t e = s->put3(s->rho, rho);
+  // each array goes up contiguously into a staging buffer (one large copy), then into the
+  // padded layout on the device; rho is checked there before anything is overwritten
+  float* staging = nullptr;
+  cudaError_t e = cudaMalloc(&staging, n * sizeof(float) + 256);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return s->fail(FWANT_ERR_OOM, "set_media: no device memory for the staging buffer");
+  }
+  unsigned int* bad = reinterpret_cast<unsigned int*>(reinterpret_cast<char*>(staging) + ((n * sizeof(float) + 127) / 128) * 128);
+  unsigned int hbad = 0;
+  e = cudaMemcpy(staging, rho, n * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, sizeof(unsigned int), s->st);
+  if (e == cudaSuccess) {
+    fw::launch_count_nonpositive((long long)n, staging, bad, s->st);
+    e = cudaMemcpyAsync(&hbad, bad, sizeof(unsigned int), cudaMemcpyDeviceToHost, s->st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+  if (e == cudaSuccess && hbad) {
+    cudaFree(staging);
+    return s->fail(FWANT_ERR_INVALID_ARG, "rho must be > 0 everywhere (ghosts included)");
+  }
+  auto pad = [&](float* dst) {
+    return cudaMemcpy2D(dst + fw::PADL, size_t(g.px) * 4, staging, size_t(g.nx) * 4, size_t(g.nx) * 4,
+                        size_t(g.ny) * g.nz, cudaMemcpyDeviceToDevice);
+  };
+  if (e == cudaSuccess) e = pad(s->rho);
+  if (e == cudaSuccess) e = cudaMemcpy(staging, lambda, n * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = pad(s->lam);
+  if (e == cudaSuccess) e = cudaMemcpy(staging, mu, n * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = pad(s->mu);
+  cudaFree(staging);
   if (e != cudaSuccess) return s->cuda_fail(e, "set_media");
+  s->h_rho.assign(rho, rho + n);  // the source weights divide by rho at the source boxes
   s->have_media = true;
   s->src_dirty = true;
   return FWANT_OK;

@@ -151,6 +151,26 @@ def test_overflow_check_reports_nan(native_lib):
     assert e.value.code == 4
 
 
+def test_set_media_rejects_nonpositive_rho(native_lib):
+    """rho must be > 0 at every point, ghosts included (the solver divides by it); a zero
+    or NaN anywhere is refused with INVALID_ARG before the medium on the device changes,
+    and a valid medium is accepted afterwards."""
+    import fwant_gb300 as fw
+    from fwant_gb300 import inputs
+    m = small_model("surface")
+    s = fw.Solver(m.ni, m.nj, m.nk, m.stept)
+    inputs.attach(s, m)
+    for bad in (0.0, np.nan, -1.0):
+        rho = m.rho.copy()
+        rho[0, 5, 7] = bad  # a ghost point
+        with pytest.raises(fw.FwantError) as e:
+            s.set_media(m.lam, m.mu, rho)
+        assert e.value.code == 1
+    s.set_media(m.lam, m.mu, m.rho)
+    s.run(8)
+    s.check()
+
+
 def test_interior_items_bitwise(oracle_mod, native_lib):
     """A grid with interior work items (tiles away from the PML, the sources and the free
     surface run the lean form of the stage kernel): still bit-identical to the oracle in
