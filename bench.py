@@ -67,6 +67,9 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--grid", default=None, help="override the C2 interior size, e.g. 200x200x100 (profiling)")
     p.add_argument("--sims", type=int, default=3, help="number of force components simulated (C2)")
+    p.add_argument("--autotune", action="store_true",
+                   help="run the project's autotuner (planes per CTA of every member, the batch's CTA "
+                        "schedule) before timing; the end-to-end leg applies the tuned settings")
     p.add_argument("--storage", choices=["fp32", "bf16", "fp16"], default="fp32",
                    help="storage of the wavefield registers (arithmetic stays FP32)")
     return p.parse_args()
@@ -564,6 +567,12 @@ def run_ours(args, rank, world):
     # per-launch timing of the stage kernel (CUDA events around each launch, eager)
     # the simulations step together: each RK stage of all of them is one launch
     batch = fw.Batch(sims)
+    tuned = None
+    if args.autotune:
+        t_tune = time.perf_counter()
+        ctas = batch.autotune(4)
+        tuned = {"planes_per_cta": [s.planes_per_cta for s in sims], "ctas": ctas,
+                 "tune_s": time.perf_counter() - t_tune}
     # per-launch timing of the stage kernel (CUDA events around each launch, eager)
     stage_ms, end_ms = batch.profile_stages(8)
     launches = batch.launches_per_step()
@@ -609,7 +618,7 @@ def run_ours(args, rank, world):
         "config": {"workload": desc, "points_per_step": npts, "l2": "inputs larger than L2 (no flush)",
                    "storage": args.storage, "fields_finite_after_run": finite,
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
-        "host_wall_s": t_host, "roofline": roof, "clocks": clk,
+        "host_wall_s": t_host, "roofline": roof, "clocks": clk, "autotune": tuned,
         # per step, as the batch counts them: per group of up to 16 simulations and per stage
         # the interior-only launch (where that stage has one) and the full launch, and the
         # step-end (receivers + step counter) kernel of every simulation
@@ -637,9 +646,13 @@ def run_ours(args, rank, world):
         for m in models:
             s = make_solver(m)
             inputs.attach(s, m)
+            if tuned:
+                s.planes_per_cta = tuned["planes_per_cta"][len(esims)]
             esims.append(s)
             h2d += 3 * m.lam.nbytes + m.x.nbytes + m.y.nbytes + m.z.nbytes
         eb = fw.Batch(esims)
+        if tuned:
+            eb.set_ctas(tuned["ctas"])
         eb.run(args.steps)
         for s in esims:
             sg = s.get_seismo()
