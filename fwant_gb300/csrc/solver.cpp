@@ -1841,16 +1841,9 @@ fwant_status fwant_batch_autotune(fwant_batch* b, int trial_steps, int* ctas_out
   if (!b || trial_steps < 1) return FWANT_ERR_INVALID_ARG;
   for (fwant_solver* m : b->sims)
     if (m->ntime != 0) return b->fail(FWANT_ERR_STATE, "batch autotune: call before the first time step");
-  for (fwant_solver* m : b->sims) {
-    fwant_status rc = fwant_autotune(m, trial_steps, nullptr);
-    if (rc != FWANT_OK) return b->fail(rc, "member autotune: " + m->err);
-  }
-  // CTA schedule: one CTA per work item, or persistent grids of 1, 2 and 4 CTAs per SM
-  const int cand[] = {0, b->sm_count, 2 * b->sm_count, 4 * b->sm_count};
-  double best = 1e30;
-  int best_ctas = 0;
-  for (int c : cand) {
-    b->ctas = c;
+  // one timed trial of the batch as configured: the four stage times of trial_steps steps
+  // after one step of first touch, then every member back to its initial state
+  auto trial = [&](double* t) -> fwant_status {
     b->drop_graphs();
     double st[4], other;
     fwant_status rc = b->profile(1, st, &other);
@@ -1860,7 +1853,41 @@ fwant_status fwant_batch_autotune(fwant_batch* b, int trial_steps, int* ctas_out
       if (e == cudaSuccess) e = m->reset_state();
     if (rc != FWANT_OK) return rc;
     if (e != cudaSuccess) return b->cuda_fail(e, "batch autotune reset");
-    const double t = st[0] + st[1] + st[2] + st[3];
+    *t = st[0] + st[1] + st[2] + st[3];
+    return FWANT_OK;
+  };
+  // planes per CTA: one value for every member, timed on the batch itself (the members'
+  // items share each launch, so a member's fastest value alone is not the batch's)
+  int min_nk = b->sims[0]->cfg.nk;
+  for (fwant_solver* m : b->sims) min_nk = std::min(min_nk, m->cfg.nk);
+  const int kcand[] = {4, 6, 8, 12, 16, 24, 32};
+  double best_t = 1e30;
+  int best_kc = b->sims[0]->kc;
+  b->ctas = 0;
+  for (int kc : kcand) {
+    if (kc > min_nk && kc != kcand[0]) break;
+    for (fwant_solver* m : b->sims) {
+      m->kc = kc;
+      m->drop_graphs();
+    }
+    double t = 0.0;
+    fwant_status rc = trial(&t);
+    if (rc != FWANT_OK) return rc;
+    if (t < best_t) { best_t = t; best_kc = kc; }
+  }
+  for (fwant_solver* m : b->sims) {
+    m->kc = best_kc;
+    m->drop_graphs();
+  }
+  // CTA schedule: one CTA per work item, or persistent grids of 1, 2 and 4 CTAs per SM
+  const int cand[] = {0, b->sm_count, 2 * b->sm_count, 4 * b->sm_count};
+  double best = 1e30;
+  int best_ctas = 0;
+  for (int c : cand) {
+    b->ctas = c;
+    double t = 0.0;
+    fwant_status rc = trial(&t);
+    if (rc != FWANT_OK) return rc;
     if (t < best) { best = t; best_ctas = c; }
   }
   b->ctas = best_ctas;

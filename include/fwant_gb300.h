@@ -336,9 +336,10 @@ const char* fwant_batch_last_error(fwant_batch* b);
 fwant_status fwant_batch_set_ctas(fwant_batch* b, int ctas);
 fwant_status fwant_batch_run(fwant_batch* b, int nsteps);
 fwant_status fwant_batch_last_run_ms(fwant_batch* b, double* ms);
-/* Autotune every member (fwant_autotune), then the CTA schedule of the batched launch
- * (one CTA per work item, or persistent grids of 1, 2 or 4 CTAs per SM); the chosen CTA
- * count (0 = one per work item) goes to *ctas (may be NULL).  Before the first step. */
+/* Autotune the batch as it runs: one planes-per-CTA value for every member (4 ... 32,
+ * timed on the batched launches), then the CTA schedule (one CTA per work item, or
+ * persistent grids of 1, 2 or 4 CTAs per SM); the chosen CTA count (0 = one per work item)
+ * goes to *ctas (may be NULL).  Before the first step; the members' states are restored. */
 fwant_status fwant_batch_autotune(fwant_batch* b, int trial_steps, int* ctas);
 /* fwant_profile_stages for a batch: eager steps with events around each stage's launches
  * (stage_ms[4]: all members' launches of that stage) and the step-end kernels. */
