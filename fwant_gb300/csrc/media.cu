@@ -221,8 +221,254 @@ __device__ void verpoly(const DPoly& P, float x0, float y0, float z0, float dz2,
   }
 }
 
-// effmedia_eval at one interior point (0-based array indices); false on the lowest-layer
-// error
+// cart1d look-up of one depth (:916-966)
+__device__ __forceinline__ void cart1d_lookup(const DCart& c, float d0, float* Vp, float* Vs, float* Dp) {
+  auto set1 = [&](float p, float s, float r) {
+    Vp[0] = Vp[1] = p;
+    Vs[0] = Vs[1] = s;
+    Dp[0] = Dp[1] = r;
+  };
+  const float* d = c.d;
+  auto V = [&](int q, int s) {
+    Vp[s] = c.vp[q - 1];
+    Vs[s] = c.vs[q - 1];
+    Dp[s] = c.dp[q - 1];
+  };
+  int k1 = 1, k2 = c.nk;
+  if (fabsf(d[k1 - 1] - d0) < SEIS_ZERO || d0 < d[k1 - 1]) {
+    V(k1, 0);
+    V(k1, 1);
+  } else if (fabsf(d[k2 - 1] - d0) < SEIS_ZERO) {
+    if (fabsf(d[k2 - 2] - d[k2 - 1]) < SEIS_ZERO) {
+      V(k2 - 1, 0);
+      V(k2, 1);
+    } else {
+      V(k2, 0);
+      V(k2, 1);
+    }
+  } else if (d[k2 - 1] < d0) {
+    V(k2, 0);
+    V(k2, 1);
+  } else {
+    while (k2 - k1 > 1) {
+      const int k0 = (k2 - k1) / 2 + k1;
+      if (fabsf(d[k0 - 1] - d0) < SEIS_ZERO) {
+        k1 = k0;
+        k2 = k0;
+        break;
+      } else if (d[k0 - 1] > d0) {
+        k2 = k0;
+      } else {
+        k1 = k0;
+      }
+    }
+    if (k1 == k2) {
+      if (fabsf(d[k1 - 2] - d[k1 - 1]) < SEIS_ZERO) {
+        V(k1 - 1, 0);
+        V(k1, 1);
+      } else if (fabsf(d[k1] - d[k1 - 1]) < SEIS_ZERO) {
+        V(k1, 0);
+        V(k1 + 1, 1);
+      } else {
+        V(k1, 0);
+        V(k1, 1);
+      }
+    } else {
+      const float dd = d[k2 - 1], h = d[k2 - 1] - d[k1 - 1];
+      const float L1 = (dd - d0) / h, L2 = 1.0f - L1;
+      set1(c.vp[k1 - 1] * L1 + c.vp[k2 - 1] * L2, c.vs[k1 - 1] * L1 + c.vs[k2 - 1] * L2,
+           c.dp[k1 - 1] * L1 + c.dp[k2 - 1] * L2);
+    }
+  }
+}
+
+// background look-up of one sample (:870-1171); false on the lowest-layer error
+__device__ __forceinline__ bool bg_sample(const Args& a, float x0, float y0, float z0, float d0, float dz2, float* Vp,
+                                          float* Vs, float* Dp) {
+  auto set1 = [&](float p, float s, float r) {
+    Vp[0] = Vp[1] = p;
+    Vs[0] = Vs[1] = s;
+    Dp[0] = Dp[1] = r;
+  };
+  if (a.bkind == FWANT_MEDIA_CART1D) {
+    cart1d_lookup(a.c, d0, Vp, Vs, Dp);
+  } else if (a.bkind == FWANT_MEDIA_INTERFACE) {  // :968-1054
+    const DLayers& L = a.L;
+    const Cell2 c = cell2(L.x, L.ni, L.y, L.nj, x0, y0);
+    const size_t plane = size_t(L.ni) * L.nj;
+    auto pick = [&](int n1, int k1, int n2, int k2) {
+      const int p1 = (n1 - 1) + 2 * (k1 - 1), p2 = (n2 - 1) + 2 * (k2 - 1);
+      Vp[0] = L.vp[p1];
+      Vp[1] = L.vp[p2];
+      Vs[0] = L.vs[p1];
+      Vs[1] = L.vs[p2];
+      Dp[0] = L.dp[p1];
+      Dp[1] = L.dp[p2];
+    };
+    int n1 = 2, k1 = L.nk, n2 = 2, k2 = L.nk;
+    for (int n = L.nk; n >= 1; --n) {
+      const float z1 = at2(c, L.z, L.ni, plane * (n - 1));
+      const float h = n == L.nk ? 1.0e3f : at2(c, L.h, L.ni, plane * (n - 1));
+      if (h <= SEIS_ZERO && n > 1) continue;
+      if (h <= SEIS_ZERO && n == 1) {
+        if (L.vp[2 * (n - 1)] > SEIS_ZERO) n1 = k1 = n2 = k2 = 1;
+        pick(n1, k1, n2, k2);
+        break;
+      }
+      if (fabsf(z1 - z0) <= dz2 / 5.0f) {
+        k2 = n;
+        n2 = 2;
+        if (n == 1) {
+          k1 = n;
+          n1 = L.vp[2 * (n - 1)] > SEIS_ZERO ? 1 : 2;
+        }
+        for (int mm = n - 1; mm >= 1; --mm) {
+          if (at2(c, L.h, L.ni, plane * (mm - 1)) > SEIS_ZERO) {
+            k1 = mm + 1;
+            n1 = 1;
+            break;
+          } else if (mm == 1) {
+            if (L.vp[2 * (mm - 1)] > SEIS_ZERO) {
+              k1 = mm;
+              n1 = 1;
+            } else {
+              k1 = n;
+              n1 = 2;
+            }
+          }
+        }
+        pick(n1, k1, n2, k2);
+        break;
+      }
+      if (z0 < z1) {
+        const int q2 = 1 + 2 * (n - 1);
+        if (n == L.nk) {
+          set1(L.vp[q2], L.vs[q2], L.dp[q2]);
+        } else {
+          const int q1 = 2 * n;  // (1, n + 1)
+          const float L2 = (z1 - z0) / h, L1 = 1.0f - L2;
+          set1(L.vp[q2] * L1 + L.vp[q1] * L2, L.vs[q2] * L1 + L.vs[q1] * L2, L.dp[q2] * L1 + L.dp[q1] * L2);
+        }
+        break;
+      }
+      k1 = n;
+      k2 = n;
+      n1 = 2;
+      n2 = 2;
+      if (n == 1) {
+        if (L.vp[2 * (n - 1)] > SEIS_ZERO) n1 = k1 = n2 = k2 = 1;
+        pick(n1, k1, n2, k2);
+        break;
+      }
+    }
+  } else if (a.bkind == FWANT_MEDIA_LAYERED || a.bkind == FWANT_MEDIA_COMPOSITE) {  // :1055-1130
+    const DLayers& L = a.L;
+    const bool comp = a.bkind == FWANT_MEDIA_COMPOSITE;
+    const Cell2 c = cell2(L.x, L.ni, L.y, L.nj, x0, y0);
+    const size_t plane = size_t(L.ni) * L.nj;
+    float d = 0.0f;
+    for (int n = 1; n <= L.nk; ++n) {
+      const float h = at2(c, L.h, L.ni, plane * (n - 1));
+      if (h <= SEIS_ZERO) continue;
+      d = d + h;
+      if (fabsf(d - d0) <= dz2 / 5.0f) {
+        if (n == L.nk) return false;
+        const int n1 = n;
+        int n2 = L.nk;
+        for (int mm = n + 1; mm <= L.nk; ++mm)
+          if (at2(c, L.h, L.ni, plane * (mm - 1)) > SEIS_ZERO) {
+            n2 = mm;
+            break;
+          }
+        if (!comp) {
+          Vp[0] = L.vp[1 + 2 * (n1 - 1)];
+          Vp[1] = L.vp[2 * (n2 - 1)];
+          Vs[0] = L.vs[1 + 2 * (n1 - 1)];
+          Vs[1] = L.vs[2 * (n2 - 1)];
+          Dp[0] = L.dp[1 + 2 * (n1 - 1)];
+          Dp[1] = L.dp[2 * (n2 - 1)];
+        } else {
+          Vp[0] = at2c(c, L.vp, L.ni, L.nj, 1, n1);
+          Vs[0] = at2c(c, L.vs, L.ni, L.nj, 1, n1);
+          Dp[0] = at2c(c, L.dp, L.ni, L.nj, 1, n1);
+          Vp[1] = at2c(c, L.vp, L.ni, L.nj, 0, n2);
+          Vs[1] = at2c(c, L.vs, L.ni, L.nj, 0, n2);
+          Dp[1] = at2c(c, L.dp, L.ni, L.nj, 0, n2);
+        }
+        break;
+      } else if (d > d0) {
+        if (!comp) {
+          const float L1 = (d - d0) / h, L2 = 1.0f - L1;
+          const int q = 2 * (n - 1);
+          set1(L.vp[q] * L1 + L.vp[q + 1] * L2, L.vs[q] * L1 + L.vs[q + 1] * L2, L.dp[q] * L1 + L.dp[q + 1] * L2);
+        } else {
+          const float p1 = at2c(c, L.vp, L.ni, L.nj, 0, n), s1 = at2c(c, L.vs, L.ni, L.nj, 0, n);
+          const float r1 = at2c(c, L.dp, L.ni, L.nj, 0, n), p2 = at2c(c, L.vp, L.ni, L.nj, 1, n);
+          const float s2 = at2c(c, L.vs, L.ni, L.nj, 1, n), r2 = at2c(c, L.dp, L.ni, L.nj, 1, n);
+          const float t = d0 - (d - h);
+          const float ep = L.vpd[n - 1], es = L.vsd[n - 1], er = L.dpd[n - 1];
+          set1(p1 + (p2 - p1) / powf(h, ep) * powf(t, ep), s1 + (s2 - s1) / powf(h, es) * powf(t, es),
+               r1 + (r2 - r1) / powf(h, er) * powf(t, er));
+        }
+        break;
+      } else if (n == L.nk) {
+        return false;
+      }
+    }
+  } else if (a.bkind == FWANT_MEDIA_VOLUME) {  // :1131-1142
+    const Cell3 c = cell3(a.bv, x0, y0, z0);
+    set1(at3(c, a.bv, a.bv.vp), at3(c, a.bv, a.bv.vs), at3(c, a.bv, a.bv.dp));
+  } else if (a.bkind == FWANT_MEDIA_VERPOLY) {  // :1143-1171
+    verpoly(a.bp, x0, y0, z0, dz2, Vp, Vs, Dp);
+  }
+  return true;
+}
+
+// perturbation of one sample (:1173-1220)
+__device__ __forceinline__ void pt_sample(const Args& a, float x0, float y0, float z0, float dz2, float* Vp, float* Vs,
+                                          float* Dp) {
+  if (a.pkind == FWANT_MEDIA_VOLUME) {  // :1175-1190
+    const Cell3 c = cell3(a.pv, x0, y0, z0);
+    const float dVp = at3(c, a.pv, a.pv.vp), dVs = at3(c, a.pv, a.pv.vs), dDp = at3(c, a.pv, a.pv.dp);
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      Vp[s] = Vp[s] * (1.0f + dVp);
+      Vs[s] = Vs[s] * (1.0f + dVs);
+      Dp[s] = Dp[s] * (1.0f + dDp);
+    }
+  } else if (a.pkind == FWANT_MEDIA_VERPOLY) {  // :1192-1220
+    float dVp[2], dVs[2], dDp[2];
+    verpoly(a.pp, x0, y0, z0, dz2, dVp, dVs, dDp);
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      Vp[s] = Vp[s] * (1.0f + dVp[s]);
+      Vs[s] = Vs[s] * (1.0f + dVs[s]);
+      Dp[s] = Dp[s] * (1.0f + dDp[s]);
+    }
+  }
+}
+
+// Lame parameters of one sample, arithmetic rho and harmonic lambda, mu (:1222-1235)
+__device__ __forceinline__ void accumulate(const float* Vp, const float* Vs, const float* Dp, float& rho0, float& mu0,
+                                           float& lam0, bool& flag_water, int& nwater) {
+  float miu[2], la[2];
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    miu[s] = Dp[s] * Vs[s] * Vs[s];
+    la[s] = Vp[s] * Vp[s] * Dp[s] - 2.0f * miu[s];
+  }
+  rho0 = rho0 + 0.5f * (Dp[0] + Dp[1]);
+  if (miu[0] <= SEIS_ZERO || miu[1] <= SEIS_ZERO) {
+    flag_water = true;
+    nwater = nwater + 1;
+  } else {
+    mu0 = mu0 + 0.5f * (1.0f / miu[0] + 1.0f / miu[1]);
+  }
+  lam0 = lam0 + 0.5f * (1.0f / la[0] + 1.0f / la[1]);
+}
+
+// effmedia_eval at one interior point (0-based array indices), any half_sample_point;
+// false on the lowest-layer error
 __device__ bool eval_point(const Args& a, int i, int j, int k, float& lam_out, float& mu_out, float& rho_out) {
   const int NX = a.ng[0], NY = a.ng[1], NZ = a.ng[2];
   const int nsamp = max(2 * NX, 1) * max(2 * NY, 1) * max(2 * NZ, 1);
@@ -246,229 +492,9 @@ __device__ bool eval_point(const Args& a, int i, int j, int k, float& lam_out, f
       for (int mi = -NX; mi <= NX; ++mi) {
         if (NX != 0 && mi == 0) continue;
         const float x0 = mi < 0 ? float(mi) * dx1 + x[i] : mi > 0 ? float(mi) * dx2 + x[i] : x[i];
-        auto set1 = [&](float p, float s, float r) {
-          Vp[0] = Vp[1] = p;
-          Vs[0] = Vs[1] = s;
-          Dp[0] = Dp[1] = r;
-        };
-        // ---- background ----
-        if (a.bkind == FWANT_MEDIA_CART1D) {  // :916-966
-          const float* d = a.c.d;
-          auto V = [&](int q, int s) {
-            Vp[s] = a.c.vp[q - 1];
-            Vs[s] = a.c.vs[q - 1];
-            Dp[s] = a.c.dp[q - 1];
-          };
-          int k1 = 1, k2 = a.c.nk;
-          if (fabsf(d[k1 - 1] - d0) < SEIS_ZERO || d0 < d[k1 - 1]) {
-            V(k1, 0);
-            V(k1, 1);
-          } else if (fabsf(d[k2 - 1] - d0) < SEIS_ZERO) {
-            if (fabsf(d[k2 - 2] - d[k2 - 1]) < SEIS_ZERO) {
-              V(k2 - 1, 0);
-              V(k2, 1);
-            } else {
-              V(k2, 0);
-              V(k2, 1);
-            }
-          } else if (d[k2 - 1] < d0) {
-            V(k2, 0);
-            V(k2, 1);
-          } else {
-            while (k2 - k1 > 1) {
-              const int k0 = (k2 - k1) / 2 + k1;
-              if (fabsf(d[k0 - 1] - d0) < SEIS_ZERO) {
-                k1 = k0;
-                k2 = k0;
-                break;
-              } else if (d[k0 - 1] > d0) {
-                k2 = k0;
-              } else {
-                k1 = k0;
-              }
-            }
-            if (k1 == k2) {
-              if (fabsf(d[k1 - 2] - d[k1 - 1]) < SEIS_ZERO) {
-                V(k1 - 1, 0);
-                V(k1, 1);
-              } else if (fabsf(d[k1] - d[k1 - 1]) < SEIS_ZERO) {
-                V(k1, 0);
-                V(k1 + 1, 1);
-              } else {
-                V(k1, 0);
-                V(k1, 1);
-              }
-            } else {
-              const float dd = d[k2 - 1], h = d[k2 - 1] - d[k1 - 1];
-              const float L1 = (dd - d0) / h, L2 = 1.0f - L1;
-              set1(a.c.vp[k1 - 1] * L1 + a.c.vp[k2 - 1] * L2, a.c.vs[k1 - 1] * L1 + a.c.vs[k2 - 1] * L2,
-                   a.c.dp[k1 - 1] * L1 + a.c.dp[k2 - 1] * L2);
-            }
-          }
-        } else if (a.bkind == FWANT_MEDIA_INTERFACE) {  // :968-1054
-          const DLayers& L = a.L;
-          const Cell2 c = cell2(L.x, L.ni, L.y, L.nj, x0, y0);
-          const size_t plane = size_t(L.ni) * L.nj;
-          auto pick = [&](int n1, int k1, int n2, int k2) {
-            const int p1 = (n1 - 1) + 2 * (k1 - 1), p2 = (n2 - 1) + 2 * (k2 - 1);
-            Vp[0] = L.vp[p1];
-            Vp[1] = L.vp[p2];
-            Vs[0] = L.vs[p1];
-            Vs[1] = L.vs[p2];
-            Dp[0] = L.dp[p1];
-            Dp[1] = L.dp[p2];
-          };
-          int n1 = 2, k1 = L.nk, n2 = 2, k2 = L.nk;
-          for (int n = L.nk; n >= 1; --n) {
-            const float z1 = at2(c, L.z, L.ni, plane * (n - 1));
-            const float h = n == L.nk ? 1.0e3f : at2(c, L.h, L.ni, plane * (n - 1));
-            if (h <= SEIS_ZERO && n > 1) continue;
-            if (h <= SEIS_ZERO && n == 1) {
-              if (L.vp[2 * (n - 1)] > SEIS_ZERO) n1 = k1 = n2 = k2 = 1;
-              pick(n1, k1, n2, k2);
-              break;
-            }
-            if (fabsf(z1 - z0) <= dz2 / 5.0f) {
-              k2 = n;
-              n2 = 2;
-              if (n == 1) {
-                k1 = n;
-                n1 = L.vp[2 * (n - 1)] > SEIS_ZERO ? 1 : 2;
-              }
-              for (int mm = n - 1; mm >= 1; --mm) {
-                if (at2(c, L.h, L.ni, plane * (mm - 1)) > SEIS_ZERO) {
-                  k1 = mm + 1;
-                  n1 = 1;
-                  break;
-                } else if (mm == 1) {
-                  if (L.vp[2 * (mm - 1)] > SEIS_ZERO) {
-                    k1 = mm;
-                    n1 = 1;
-                  } else {
-                    k1 = n;
-                    n1 = 2;
-                  }
-                }
-              }
-              pick(n1, k1, n2, k2);
-              break;
-            }
-            if (z0 < z1) {
-              const int q2 = 1 + 2 * (n - 1);
-              if (n == L.nk) {
-                set1(L.vp[q2], L.vs[q2], L.dp[q2]);
-              } else {
-                const int q1 = 2 * n;  // (1, n + 1)
-                const float L2 = (z1 - z0) / h, L1 = 1.0f - L2;
-                set1(L.vp[q2] * L1 + L.vp[q1] * L2, L.vs[q2] * L1 + L.vs[q1] * L2, L.dp[q2] * L1 + L.dp[q1] * L2);
-              }
-              break;
-            }
-            k1 = n;
-            k2 = n;
-            n1 = 2;
-            n2 = 2;
-            if (n == 1) {
-              if (L.vp[2 * (n - 1)] > SEIS_ZERO) n1 = k1 = n2 = k2 = 1;
-              pick(n1, k1, n2, k2);
-              break;
-            }
-          }
-        } else if (a.bkind == FWANT_MEDIA_LAYERED || a.bkind == FWANT_MEDIA_COMPOSITE) {  // :1055-1130
-          const DLayers& L = a.L;
-          const bool comp = a.bkind == FWANT_MEDIA_COMPOSITE;
-          const Cell2 c = cell2(L.x, L.ni, L.y, L.nj, x0, y0);
-          const size_t plane = size_t(L.ni) * L.nj;
-          float d = 0.0f;
-          for (int n = 1; n <= L.nk; ++n) {
-            const float h = at2(c, L.h, L.ni, plane * (n - 1));
-            if (h <= SEIS_ZERO) continue;
-            d = d + h;
-            if (fabsf(d - d0) <= dz2 / 5.0f) {
-              if (n == L.nk) return false;
-              const int n1 = n;
-              int n2 = L.nk;
-              for (int mm = n + 1; mm <= L.nk; ++mm)
-                if (at2(c, L.h, L.ni, plane * (mm - 1)) > SEIS_ZERO) {
-                  n2 = mm;
-                  break;
-                }
-              if (!comp) {
-                Vp[0] = L.vp[1 + 2 * (n1 - 1)];
-                Vp[1] = L.vp[2 * (n2 - 1)];
-                Vs[0] = L.vs[1 + 2 * (n1 - 1)];
-                Vs[1] = L.vs[2 * (n2 - 1)];
-                Dp[0] = L.dp[1 + 2 * (n1 - 1)];
-                Dp[1] = L.dp[2 * (n2 - 1)];
-              } else {
-                Vp[0] = at2c(c, L.vp, L.ni, L.nj, 1, n1);
-                Vs[0] = at2c(c, L.vs, L.ni, L.nj, 1, n1);
-                Dp[0] = at2c(c, L.dp, L.ni, L.nj, 1, n1);
-                Vp[1] = at2c(c, L.vp, L.ni, L.nj, 0, n2);
-                Vs[1] = at2c(c, L.vs, L.ni, L.nj, 0, n2);
-                Dp[1] = at2c(c, L.dp, L.ni, L.nj, 0, n2);
-              }
-              break;
-            } else if (d > d0) {
-              if (!comp) {
-                const float L1 = (d - d0) / h, L2 = 1.0f - L1;
-                const int q = 2 * (n - 1);
-                set1(L.vp[q] * L1 + L.vp[q + 1] * L2, L.vs[q] * L1 + L.vs[q + 1] * L2, L.dp[q] * L1 + L.dp[q + 1] * L2);
-              } else {
-                const float p1 = at2c(c, L.vp, L.ni, L.nj, 0, n), s1 = at2c(c, L.vs, L.ni, L.nj, 0, n);
-                const float r1 = at2c(c, L.dp, L.ni, L.nj, 0, n), p2 = at2c(c, L.vp, L.ni, L.nj, 1, n);
-                const float s2 = at2c(c, L.vs, L.ni, L.nj, 1, n), r2 = at2c(c, L.dp, L.ni, L.nj, 1, n);
-                const float t = d0 - (d - h);
-                const float ep = L.vpd[n - 1], es = L.vsd[n - 1], er = L.dpd[n - 1];
-                set1(p1 + (p2 - p1) / powf(h, ep) * powf(t, ep), s1 + (s2 - s1) / powf(h, es) * powf(t, es),
-                     r1 + (r2 - r1) / powf(h, er) * powf(t, er));
-              }
-              break;
-            } else if (n == L.nk) {
-              return false;
-            }
-          }
-        } else if (a.bkind == FWANT_MEDIA_VOLUME) {  // :1131-1142
-          const Cell3 c = cell3(a.bv, x0, y0, z0);
-          set1(at3(c, a.bv, a.bv.vp), at3(c, a.bv, a.bv.vs), at3(c, a.bv, a.bv.dp));
-        } else if (a.bkind == FWANT_MEDIA_VERPOLY) {  // :1143-1171
-          verpoly(a.bp, x0, y0, z0, dz2, Vp, Vs, Dp);
-        }
-        // ---- perturbation ----
-        if (a.pkind == FWANT_MEDIA_VOLUME) {  // :1175-1190
-          const Cell3 c = cell3(a.pv, x0, y0, z0);
-          const float dVp = at3(c, a.pv, a.pv.vp), dVs = at3(c, a.pv, a.pv.vs), dDp = at3(c, a.pv, a.pv.dp);
-#pragma unroll
-          for (int s = 0; s < 2; ++s) {
-            Vp[s] = Vp[s] * (1.0f + dVp);
-            Vs[s] = Vs[s] * (1.0f + dVs);
-            Dp[s] = Dp[s] * (1.0f + dDp);
-          }
-        } else if (a.pkind == FWANT_MEDIA_VERPOLY) {  // :1192-1220
-          float dVp[2], dVs[2], dDp[2];
-          verpoly(a.pp, x0, y0, z0, dz2, dVp, dVs, dDp);
-#pragma unroll
-          for (int s = 0; s < 2; ++s) {
-            Vp[s] = Vp[s] * (1.0f + dVp[s]);
-            Vs[s] = Vs[s] * (1.0f + dVs[s]);
-            Dp[s] = Dp[s] * (1.0f + dDp[s]);
-          }
-        }
-        // ---- Lame parameters, arithmetic rho and harmonic lambda, mu :1222-1235 ----
-        float miu[2], la[2];
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
-          miu[s] = Dp[s] * Vs[s] * Vs[s];
-          la[s] = Vp[s] * Vp[s] * Dp[s] - 2.0f * miu[s];
-        }
-        rho0 = rho0 + 0.5f * (Dp[0] + Dp[1]);
-        if (miu[0] <= SEIS_ZERO || miu[1] <= SEIS_ZERO) {
-          flag_water = true;
-          nwater = nwater + 1;
-        } else {
-          mu0 = mu0 + 0.5f * (1.0f / miu[0] + 1.0f / miu[1]);
-        }
-        lam0 = lam0 + 0.5f * (1.0f / la[0] + 1.0f / la[1]);
+        if (!bg_sample(a, x0, y0, z0, d0, dz2, Vp, Vs, Dp)) return false;
+        pt_sample(a, x0, y0, z0, dz2, Vp, Vs, Dp);
+        accumulate(Vp, Vs, Dp, rho0, mu0, lam0, flag_water, nwater);
       }
     }
   }
@@ -479,6 +505,137 @@ __device__ bool eval_point(const Args& a, int i, int j, int k, float& lam_out, f
   return true;
 }
 
+// A located model axis of a volume: bracketing index and the two Lagrange weights.
+struct VolAxis {
+  int i1;
+  float l1, l2;
+};
+
+__device__ __forceinline__ VolAxis vaxis(const float* g, int n, float v) {
+  VolAxis r;
+  float v1;
+  locate(v, g, n, r.i1, v1);
+  lweights(g[r.i1 - 1], g[r.i1], v1, r.l1, r.l2);
+  return r;
+}
+
+// interp_3d at axes located separately (the same products and sums as at3)
+__device__ __forceinline__ float at3h(const VolAxis& cx, const VolAxis& cy, const VolAxis& cz, const DVol& V,
+                                      const float* f) {
+  const float lx[2] = {cx.l1, cx.l2}, ly[2] = {cy.l1, cy.l2}, lz[2] = {cz.l1, cz.l2};
+  float s = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+        s = s + lx[i] * ly[j] * lz[k] * f[(size_t(cz.i1 - 1 + k) * V.nj + (cy.i1 - 1 + j)) * V.ni + (cx.i1 - 1 + i)];
+  return s;
+}
+
+// eval_point for half_sample_point 0 or 1 on each axis (SX, SY, SZ = samples per axis, 1
+// or 2).  The look-ups that depend on one coordinate only are hoisted out of the sample
+// loops: a cart1d background depends on the depth alone, and a volume's bisections and
+// weights are separable by axis.  Every value is formed by the same operations as in
+// eval_point, so both paths give identical results.
+template <int SX, int SY, int SZ>
+__device__ bool eval_fast(const Args& a, int i, int j, int k, float& lam_out, float& mu_out, float& rho_out) {
+  constexpr int nsamp = SX * SY * SZ;
+  const float* x = a.x;
+  const float* y = a.y;
+  const float* z = a.z;
+  float xs[SX], ys[SY], zs[SZ], ds[SZ];
+  if constexpr (SX == 2) {
+    xs[0] = -1.0f * ((x[i] - x[i - 1]) / 2.0f / 2.0f) + x[i];
+    xs[1] = 1.0f * ((x[i + 1] - x[i]) / 2.0f / 2.0f) + x[i];
+  } else {
+    xs[0] = x[i];
+  }
+  if constexpr (SY == 2) {
+    ys[0] = -1.0f * ((y[j] - y[j - 1]) / 2.0f / 2.0f) + y[j];
+    ys[1] = 1.0f * ((y[j + 1] - y[j]) / 2.0f / 2.0f) + y[j];
+  } else {
+    ys[0] = y[j];
+  }
+  const float dz2 = (z[k + 1] - z[k]) / 2.0f / float(SZ);
+  if constexpr (SZ == 2) {
+    zs[0] = -1.0f * ((z[k] - z[k - 1]) / 2.0f / 2.0f) + z[k];
+    zs[1] = 1.0f * dz2 + z[k];
+  } else {
+    zs[0] = z[k];
+  }
+#pragma unroll
+  for (int q = 0; q < SZ; ++q) ds[q] = fmaxf(a.ztopo - zs[q], 0.0f);
+  const bool cart = a.bkind == FWANT_MEDIA_CART1D, bvol = a.bkind == FWANT_MEDIA_VOLUME;
+  const bool pvol = a.pkind == FWANT_MEDIA_VOLUME;
+  float cVp[SZ][2], cVs[SZ][2], cDp[SZ][2];
+  if (cart) {
+#pragma unroll
+    for (int q = 0; q < SZ; ++q) cart1d_lookup(a.c, ds[q], cVp[q], cVs[q], cDp[q]);
+  }
+  VolAxis bx[SX], by[SY], bz[SZ], px[SX], py[SY], pz[SZ];
+  if (bvol) {
+#pragma unroll
+    for (int q = 0; q < SX; ++q) bx[q] = vaxis(a.bv.x, a.bv.ni, xs[q]);
+#pragma unroll
+    for (int q = 0; q < SY; ++q) by[q] = vaxis(a.bv.y, a.bv.nj, ys[q]);
+#pragma unroll
+    for (int q = 0; q < SZ; ++q) bz[q] = vaxis(a.bv.rz, a.bv.nk, a.bv.rz0 - zs[q]);
+  }
+  if (pvol) {
+#pragma unroll
+    for (int q = 0; q < SX; ++q) px[q] = vaxis(a.pv.x, a.pv.ni, xs[q]);
+#pragma unroll
+    for (int q = 0; q < SY; ++q) py[q] = vaxis(a.pv.y, a.pv.nj, ys[q]);
+#pragma unroll
+    for (int q = 0; q < SZ; ++q) pz[q] = vaxis(a.pv.rz, a.pv.nk, a.pv.rz0 - zs[q]);
+  }
+  float rho0 = 0.0f, mu0 = 0.0f, lam0 = 0.0f;
+  bool flag_water = false;
+  int nwater = 0;
+  float Vp[2] = {0.0f, 0.0f}, Vs[2] = {0.0f, 0.0f}, Dp[2] = {0.0f, 0.0f};
+#pragma unroll
+  for (int mk = 0; mk < SZ; ++mk)
+#pragma unroll
+    for (int mj = 0; mj < SY; ++mj)
+#pragma unroll
+      for (int mi = 0; mi < SX; ++mi) {
+        if (cart) {
+          Vp[0] = cVp[mk][0]; Vp[1] = cVp[mk][1];
+          Vs[0] = cVs[mk][0]; Vs[1] = cVs[mk][1];
+          Dp[0] = cDp[mk][0]; Dp[1] = cDp[mk][1];
+        } else if (bvol) {
+          Vp[0] = Vp[1] = at3h(bx[mi], by[mj], bz[mk], a.bv, a.bv.vp);
+          Vs[0] = Vs[1] = at3h(bx[mi], by[mj], bz[mk], a.bv, a.bv.vs);
+          Dp[0] = Dp[1] = at3h(bx[mi], by[mj], bz[mk], a.bv, a.bv.dp);
+        } else if (!bg_sample(a, xs[mi], ys[mj], zs[mk], ds[mk], dz2, Vp, Vs, Dp)) {
+          return false;
+        }
+        if (pvol) {
+          const float dVp = at3h(px[mi], py[mj], pz[mk], a.pv, a.pv.vp);
+          const float dVs = at3h(px[mi], py[mj], pz[mk], a.pv, a.pv.vs);
+          const float dDp = at3h(px[mi], py[mj], pz[mk], a.pv, a.pv.dp);
+#pragma unroll
+          for (int s = 0; s < 2; ++s) {
+            Vp[s] = Vp[s] * (1.0f + dVp);
+            Vs[s] = Vs[s] * (1.0f + dVs);
+            Dp[s] = Dp[s] * (1.0f + dDp);
+          }
+        } else {
+          pt_sample(a, xs[mi], ys[mj], zs[mk], dz2, Vp, Vs, Dp);
+        }
+        accumulate(Vp, Vs, Dp, rho0, mu0, lam0, flag_water, nwater);
+      }
+  rho_out = rho0 / float(nsamp);
+  if (flag_water) mu_out = nwater >= nsamp / 2 ? 0.0f : float(nsamp - nwater) / mu0;
+  else mu_out = float(nsamp) / mu0;
+  lam_out = float(nsamp) / lam0;
+  return true;
+}
+
+// SX = 0: any half_sample_point (eval_point); else the hoisted form for 0 / 1 per axis
+template <int SX, int SY, int SZ>
 __global__ void __launch_bounds__(MD_THREADS) effmedia_kernel(const Args a) {
   const long long n = (long long)a.ni * a.nj * a.nk;
   for (long long p = (long long)blockIdx.x * MD_THREADS + threadIdx.x; p < n; p += (long long)gridDim.x * MD_THREADS) {
@@ -486,7 +643,10 @@ __global__ void __launch_bounds__(MD_THREADS) effmedia_kernel(const Args a) {
     const int j = int((p / a.ni) % a.nj) + LENFD;
     const int k = int(p / ((long long)a.ni * a.nj)) + LENFD;
     float l, m, r;
-    if (!eval_point(a, i, j, k, l, m, r)) {
+    bool ok;
+    if constexpr (SX == 0) ok = eval_point(a, i, j, k, l, m, r);
+    else ok = eval_fast<SX, SY, SZ>(a, i, j, k, l, m, r);
+    if (!ok) {
       atomicExch(a.err, 1);
       l = m = r = 0.0f;
     }
@@ -494,6 +654,22 @@ __global__ void __launch_bounds__(MD_THREADS) effmedia_kernel(const Args a) {
     a.lam[q] = l;
     a.mu[q] = m;
     a.rho[q] = r;
+  }
+}
+
+void launch_effmedia(const Args& a, int grid, cudaStream_t st) {
+  const int s0 = a.ng[0] + 1, s1 = a.ng[1] + 1, s2 = a.ng[2] + 1;
+  const int key = (s0 <= 2 && s1 <= 2 && s2 <= 2) ? (s0 - 1) * 4 + (s1 - 1) * 2 + (s2 - 1) : -1;
+  switch (key) {
+    case 0: effmedia_kernel<1, 1, 1><<<grid, MD_THREADS, 0, st>>>(a); break;
+    case 1: effmedia_kernel<1, 1, 2><<<grid, MD_THREADS, 0, st>>>(a); break;
+    case 2: effmedia_kernel<1, 2, 1><<<grid, MD_THREADS, 0, st>>>(a); break;
+    case 3: effmedia_kernel<1, 2, 2><<<grid, MD_THREADS, 0, st>>>(a); break;
+    case 4: effmedia_kernel<2, 1, 1><<<grid, MD_THREADS, 0, st>>>(a); break;
+    case 5: effmedia_kernel<2, 1, 2><<<grid, MD_THREADS, 0, st>>>(a); break;
+    case 6: effmedia_kernel<2, 2, 1><<<grid, MD_THREADS, 0, st>>>(a); break;
+    case 7: effmedia_kernel<2, 2, 2><<<grid, MD_THREADS, 0, st>>>(a); break;
+    default: effmedia_kernel<0, 0, 0><<<grid, MD_THREADS, 0, st>>>(a); break;
   }
 }
 
@@ -952,7 +1128,7 @@ fwant_status fwant_media_eval(fwant_media* m, float* lambda, float* mu, float* r
   const int g1 = int(std::min<long long>((ni3 + MD_THREADS - 1) / MD_THREADS, (long long)sms * 64));
   const int g2 = int(std::min<long long>((nx3 + MD_THREADS - 1) / MD_THREADS, (long long)sms * 32));
   cudaEventRecord(m->ev0, m->st);
-  effmedia_kernel<<<g1, MD_THREADS, 0, m->st>>>(m->a);
+  launch_effmedia(m->a, g1, m->st);
   extend_kernel<<<g2, MD_THREADS, 0, m->st>>>(m->a);
   cudaEventRecord(m->ev1, m->st);
   int herr = 0;
