@@ -57,10 +57,12 @@ def parse_args():
     p.add_argument("--steps", type=int, default=32)
     p.add_argument("--warmup", type=int, default=8)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--config", choices=["c2", "c1", "c3", "c5", "lsqr", "media"], default="c2",
+    p.add_argument("--config", choices=["c2", "c1", "c3", "c5", "lsqr", "media", "ker"], default="c2",
                    help="c5: train the waveform surrogate on 512 FD solves and screen 64 held-out models; "
                         "lsqr: LSQR iterations of the damped, smoothed inversion (inv.LSQR) on a synthetic system; "
-                        "media: the effective-medium preprocessor (seis3d_media) on the C2 grid")
+                        "media: the effective-medium preprocessor (seis3d_media) on the C2 grid; "
+                        "ker: the sensitivity-kernel accumulation (SI_ker_sta sgt2scatter3) of one SGT block")
+    p.add_argument("--ker-points", type=int, default=16384, help="kernel points of the --config ker block")
     p.add_argument("--lsqr-scale", type=float, default=1.0, help="fraction of the LSQR system's data rows (profiling)")
     p.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -282,6 +284,29 @@ def run_reference_lsqr(args):
                            f"inversion system, {nnz} stored entries", sample, 1, "f64")
 
 
+def run_reference_ker(args):
+    """the oracle's FP64-accumulation sgt2scatter3 with all host threads, each step a
+    sample of the block's points"""
+    from oracle import oracle as O
+    O.build()
+    threads = O.set_threads(os.cpu_count() or 1)
+    npts, knt = args.ker_points, 500
+    lam, mu, sgt = ker_block(npts, knt)
+    ns = min(npts, 1024)
+    sub = [a[:, :, :ns].copy() for a in sgt]
+    for _ in range(max(args.warmup, 1)):
+        O.sgt2scatter3(lam[:ns], mu[:ns], sub[:3], sub[3], 0.1, mode=1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.sgt2scatter3(lam[:ns], mu[:ns], sub[:3], sub[3], 0.1, mode=1)
+    dt = time.perf_counter() - t0
+    dfma = ns * 3 * 7 * knt * (knt - 1) / 2
+    sample = f"{ns} of the {npts} kernel points per step, {threads} threads"
+    return _reference_line(args, "sensitivity-kernel accumulation FP64 throughput", "TFLOP/s",
+                           2 * dfma * args.steps / dt / 1e12, dt, f"sgt2scatter3 of one SGT block ({npts} points)",
+                           sample, threads, "f64")
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -289,6 +314,8 @@ def run_reference(args, rank, world):
         return run_reference_media(args)
     if args.config == "lsqr":
         return run_reference_lsqr(args)
+    if args.config == "ker":
+        return run_reference_ker(args)
     models, desc = make_models(args.config, seed=0, grid=args.grid, sims=args.sims)
     from fwant_gb300 import inputs
     from oracle import oracle as O
@@ -517,6 +544,94 @@ def run_media(args, rank):
     return 0
 
 
+# GB300's FP64 FMA rate: no measured figure is available to the benchmark, so the nominal
+# dense FP64 rate stands as the denominator of the kernel-accumulation roofline
+FP64_NOMINAL_TFLOPS = 1.25
+
+
+def ker_block(npts, knt=500, seed=0):
+    rng = np.random.default_rng(seed)
+    lam = np.full(npts, 3.0e10, np.float32) * (1 + 0.05 * rng.random(npts, dtype=np.float32))
+    mu = np.full(npts, 2.5e10, np.float32) * (1 + 0.05 * rng.random(npts, dtype=np.float32))
+    sgt = [rng.standard_normal((6, knt, npts), dtype=np.float32) for _ in range(4)]
+    return lam, mu, sgt
+
+
+def run_ker(args, rank):
+    """The sensitivity-kernel accumulation (fwant_sgtker_*): sgt2scatter3 of the three
+    receiver force components against the source SGT for every point of one block (FP64
+    sums on the GPU), timed on the device; the oracle's FP64-accumulation form on a sample
+    of the points on the host; and the end-to-end job (upload the media and four SGT series,
+    scatter, window integrals of the three components, kernels read back)."""
+    import fwant_gb300 as fw
+    if rank != 0:
+        return 0
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    npts, knt, kdt = args.ker_points, 500, 0.1
+    lam, mu, sgt = ker_block(npts, knt)
+    # 7 FMA per lag for each of the 3 components, knt (knt - 1) / 2 lags per point
+    dfma = npts * 3 * 7 * knt * (knt - 1) / 2
+    K = fw.SgtKernel(npts, knt, kdt, device=dev)
+    K.set_media(lam, mu)
+    for w in range(4):
+        K.set_sgt(w, sgt[w])
+    warm = max(args.warmup, 3)
+    for _ in range(warm):
+        K.scatter(7)
+    clocks = Clocks(dev)
+    clocks.start()
+    ms = []
+    for _ in range(args.steps):
+        K.scatter(7)
+        ms.append(K.last_scatter_ms())
+    clk = clocks.stop()
+    K.close()
+    dev_ms = float(np.sum(ms))
+    tflops = 2 * dfma * args.steps / (dev_ms * 1e-3) / 1e12
+    out = {
+        "metric": "sensitivity-kernel accumulation FP64 throughput", "value": tflops, "unit": "TFLOP/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": warm, "ms_per_step": dev_ms / args.steps,
+        "higher_is_better": True, "scaling": "replicas only", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": f"sgt2scatter3 of one SGT block: {npts} kernel points x {knt} frames, receiver "
+                               f"X, Y, Z force SGTs against the source SGT (flags 7), FP64 sums",
+                   "step": "one fwant_sgtker_scatter over the block", "l2": "SGT series (786 MB) larger than L2"},
+        "roofline": {"bound": "fp64", "achieved": tflops, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                     "frac": tflops / FP64_NOMINAL_TFLOPS, "peak_source": "nominal GB300 dense FP64 rate",
+                     "traffic": None},
+        "clocks": clk, "gpu_launches": args.steps,
+    }
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        O.build()
+        threads = O.set_threads(os.cpu_count() or 1)
+        ns = min(npts, 2048)
+        sub = [a[:, :, :ns].copy() for a in sgt]
+        t1 = time.perf_counter()
+        O.sgt2scatter3(lam[:ns], mu[:ns], sub[:3], sub[3], kdt, mode=1)
+        dt = time.perf_counter() - t1
+        out["cpu_baseline"] = {"value": 2 * dfma * ns / npts / dt / 1e12, "unit": "TFLOP/s", "cores": threads,
+                               "kind": "port", "sample": f"{ns} of the {npts} points, same series, {dt:.1f} s"}
+    if not args.no_e2e:
+        v = np.sin(np.arange(knt, dtype=np.float32) * np.float32(0.05))
+        u = np.cos(np.arange(knt, dtype=np.float32) * np.float32(0.05))
+        t1 = time.perf_counter()
+        K2 = fw.SgtKernel(npts, knt, kdt, device=dev)
+        K2.set_media(lam, mu)
+        for w in range(4):
+            K2.set_sgt(w, sgt[w])
+        K2.scatter(7)
+        outs = K2.kernel(3, v, u, 50, 450, 1.0e15)
+        wall = time.perf_counter() - t1
+        K2.close()
+        out["e2e"] = {"value": 2 * dfma / wall / 1e12, "unit": "TFLOP/s",
+                      "h2d_bytes_per_step": lam.nbytes + mu.nbytes + sum(a.nbytes for a in sgt) + v.nbytes + u.nbytes,
+                      "d2h_bytes_per_step": sum(o.nbytes for o in outs), "wall_s": wall,
+                      "includes": "handle creation, media and SGT upload, one scatter, window integrals, kernels read back"}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_surrogate(args, rank):
     """Config 5: the surrogate's screening speedup over FD solves at 1% waveform error."""
     from fwant_gb300 import surrogate
@@ -549,6 +664,8 @@ def run_ours(args, rank, world):
         return run_lsqr(args, rank)
     if args.config == "media":
         return run_media(args, rank)
+    if args.config == "ker":
+        return run_ker(args, rank)
     dist = Dist(world)
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     fw.load_library()
