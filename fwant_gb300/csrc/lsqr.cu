@@ -87,12 +87,13 @@ struct Sparse {
 };
 
 // y = sum over row r's entries of val * in[idx] by W lanes (lane `sub` of the group takes
-// entries sub, sub + W, ...), combined in a fixed order
-template <int W>
+// entries sub, sub + W, ...), combined in a fixed order.  IT: entry-offset type, 32-bit
+// when every offset fits (fewer 64-bit integer instructions in the loop), else 64-bit.
+template <int W, typename IT>
 __device__ __forceinline__ double row_dot(const Sparse& A, int r, int sub, const double* __restrict__ in) {
-  const long long e0 = A.ptr[r], e1 = A.ptr[r + 1];
+  const IT e0 = IT(A.ptr[r]), e1 = IT(A.ptr[r + 1]);
   double y0 = 0.0, y1 = 0.0, y2 = 0.0, y3 = 0.0;
-  long long e = e0 + sub;
+  IT e = e0 + sub;
   for (; e + 3 * W < e1; e += 4 * W) {
     y0 = fma(A.val[e], in[A.idx[e]], y0);
     y1 = fma(A.val[e + W], in[A.idx[e + W]], y1);
@@ -105,7 +106,7 @@ __device__ __forceinline__ double row_dot(const Sparse& A, int r, int sub, const
 
 // One length class: groups of W lanes take the class's rows grid-stride; the group's first
 // lane writes out[r] (y, or y - out[r] * factor) and adds out[r]^2 to sq.
-template <int W>
+template <int W, typename IT>
 __device__ __forceinline__ void gather_class(const Sparse& A, int c, const double* __restrict__ in,
                                              double* __restrict__ out, double factor, bool subtract, double& sq) {
   const long long tid = (long long)blockIdx.x * LS_THREADS + threadIdx.x;
@@ -115,7 +116,7 @@ __device__ __forceinline__ void gather_class(const Sparse& A, int c, const doubl
   const unsigned mask = W == 32 ? 0xffffffffu : (((1u << W) - 1u) << (lane & ~(W - 1)));
   for (long long g = tid / W; g < A.ncls[c]; g += groups) {
     const int r = A.cls[c][g];
-    double y = row_dot<W>(A, r, sub, in);
+    double y = row_dot<W, IT>(A, r, sub, in);
     if (W > 1)
       for (int o = W / 2; o > 0; o >>= 1) y += __shfl_down_sync(mask, y, o, W);
     if (sub == 0) {
@@ -129,6 +130,7 @@ __device__ __forceinline__ void gather_class(const Sparse& A, int c, const doubl
 // out[r] = (A in)[r] for every row r, then out[r] = y - out[r] * factor (which 0: alpha,
 // u = A v - alpha u; which 1: beta, v = A^T u - beta v; which 2: out = A in), and the
 // block's sum of out[r]^2 into partial[blockIdx.x].
+template <typename IT>
 __global__ void __launch_bounds__(LS_THREADS) gather_kernel(const Sparse A, const double* __restrict__ in,
                                                             double* __restrict__ out, const Scal* __restrict__ S,
                                                             int which, int check_done, double* __restrict__ partial) {
@@ -140,18 +142,29 @@ __global__ void __launch_bounds__(LS_THREADS) gather_kernel(const Sparse A, cons
   // very long rows: a block per row (the loop is uniform over the block)
   for (long long g = blockIdx.x; g < A.ncls[3]; g += gridDim.x) {
     const int r = A.cls[3][g];
-    const double y = block_sum(row_dot<LS_THREADS>(A, r, threadIdx.x, in), sh);
+    const double y = block_sum(row_dot<LS_THREADS, IT>(A, r, threadIdx.x, in), sh);
     if (threadIdx.x == 0) {
       const double o = subtract ? __dsub_rn(y, __dmul_rn(out[r], factor)) : y;
       out[r] = o;
       sq = fma(o, o, sq);
     }
   }
-  gather_class<32>(A, 2, in, out, factor, subtract, sq);
-  gather_class<8>(A, 1, in, out, factor, subtract, sq);
-  gather_class<1>(A, 0, in, out, factor, subtract, sq);
+  gather_class<32, IT>(A, 2, in, out, factor, subtract, sq);
+  gather_class<8, IT>(A, 1, in, out, factor, subtract, sq);
+  gather_class<1, IT>(A, 0, in, out, factor, subtract, sq);
   const double t = block_sum(sq, sh);
   if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+// entry offsets up to this bound run the 32-bit form (e + 4 W stays below 2^31)
+constexpr long long I32_NNZ_MAX = 0x7fffffffLL - 8 * LS_THREADS;
+
+void launch_gather(const Sparse& A, long long nnz, const double* in, double* out, const Scal* S, int which,
+                   int check_done, double* partial, int nblk, cudaStream_t st) {
+  if (nnz <= I32_NNZ_MAX)
+    gather_kernel<int><<<nblk, LS_THREADS, 0, st>>>(A, in, out, S, which, check_done, partial);
+  else
+    gather_kernel<long long><<<nblk, LS_THREADS, 0, st>>>(A, in, out, S, which, check_done, partial);
 }
 
 // lnrliz: norm = sqrt(sum of the partials) (every block sums them in the same order), the
@@ -327,9 +340,9 @@ struct fwant_lsqr {
   }
   // one LSQR iteration (slsqr's loop body)
   void enqueue_iteration() {
-    gather_kernel<<<nblk, LS_THREADS, 0, st>>>(A, v, u, S, 0, 1, partial);
+    launch_gather(A, nnz, v, u, S, 0, 1, partial, nblk, st);
     normalise_kernel<<<nblk, LS_THREADS, 0, st>>>(u, nrow, partial, nblk, S, 0, 1);
-    gather_kernel<<<nblk, LS_THREADS, 0, st>>>(At, u, v, S, 1, 1, partial);
+    launch_gather(At, nnz, u, v, S, 1, 1, partial, nblk, st);
     normalise_kernel<<<nblk, LS_THREADS, 0, st>>>(v, ncol, partial, nblk, S, 1, 1);
     scalar_kernel<<<1, 1, 0, st>>>(S);
     update_kernel<<<nblk, LS_THREADS, 0, st>>>(x, w, v, sig, ncol, S, partial);
@@ -487,7 +500,7 @@ fwant_status fwant_lsqr_solve(fwant_lsqr* l, double atol, double btol, long long
   const int nb = l->nblk;
   sumsq_kernel<<<nb, LS_THREADS, 0, l->st>>>(l->u, l->nrow, l->partial);
   normalise_kernel<<<nb, LS_THREADS, 0, l->st>>>(l->u, l->nrow, l->partial, nb, l->S, 0, 0);
-  gather_kernel<<<nb, LS_THREADS, 0, l->st>>>(l->At, l->u, l->v, l->S, 2, 0, l->partial);
+  launch_gather(l->At, l->nnz, l->u, l->v, l->S, 2, 0, l->partial, nb, l->st);
   normalise_kernel<<<nb, LS_THREADS, 0, l->st>>>(l->v, l->ncol, l->partial, nb, l->S, 1, 0);
   start_kernel<<<nb, LS_THREADS, 0, l->st>>>(l->w, l->v, l->x, l->sig, l->ncol, l->S);
   e = cudaGetLastError();
@@ -556,7 +569,7 @@ fwant_status fwant_lsqr_multiply(fwant_lsqr* l, const double* x, double* y) {
   if (rc != FWANT_OK) return rc;
   cudaError_t e = cudaMemcpyAsync(l->tmp, x, size_t(l->ncol) * sizeof(double), cudaMemcpyHostToDevice, l->st);
   if (e == cudaSuccess) {
-    gather_kernel<<<l->nblk, LS_THREADS, 0, l->st>>>(l->A, l->tmp, yd, l->S, 2, 0, l->partial);
+    launch_gather(l->A, l->nnz, l->tmp, yd, l->S, 2, 0, l->partial, l->nblk, l->st);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(y, yd, size_t(l->nrow) * sizeof(double), cudaMemcpyDeviceToHost, l->st);
