@@ -63,7 +63,8 @@ def parse_args():
                         "media: the effective-medium preprocessor (seis3d_media) on the C2 grid; "
                         "ker: the sensitivity-kernel accumulation (SI_ker_sta sgt2scatter3) of one SGT block")
     p.add_argument("--ker-points", type=int, default=16384, help="kernel points of the --config ker block")
-    p.add_argument("--lsqr-scale", type=float, default=1.0, help="fraction of the LSQR system's data rows (profiling)")
+    p.add_argument("--lsqr-scale", type=float, default=1.0,
+                   help="fraction of the LSQR system's measurements and blocks (profiling)")
     p.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -349,9 +350,11 @@ def lsqr_system(scale=1.0, seed=0):
     components x 500k blocks + station and event terms), 25,000 measurements whose kernel
     rows are 64 runs of 250 consecutive blocks (a localised sensitivity kernel in block
     order), one damping row per unknown and first-difference smoothing rows along the block
-    order of each component.  Returns (row_ptr, col, val, rhs, ncol)."""
+    order of each component.  scale < 1 shrinks the measurements and the blocks together,
+    so rows and columns keep their lengths (profiling a smaller system of the same shape).
+    Returns (row_ptr, col, val, rhs, ncol)."""
     rng = np.random.default_rng(seed)
-    nblk, ncmp, nsta, nevt = 500_000, 3, 400, 2_000
+    nblk, ncmp, nsta, nevt = max(2_000, int(500_000 * scale)), 3, 400, 2_000
     nm = nblk * ncmp
     ncol = nm + nsta + nevt
     ndata = max(1, int(25_000 * scale))
