@@ -94,6 +94,27 @@ __device__ __forceinline__ double row_dot(const Sparse& A, int r, int sub, const
   const IT e0 = IT(A.ptr[r]), e1 = IT(A.ptr[r + 1]);
   double y0 = 0.0, y1 = 0.0, y2 = 0.0, y3 = 0.0;
   IT e = e0 + sub;
+  // two groups of four loaded before either is summed (more loads in flight); each
+  // accumulator still takes its entries in the same order as one group at a time
+  for (; e + 7 * W < e1; e += 8 * W) {
+    double a[8], x[8];
+    int c[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      a[q] = A.val[e + q * W];
+      c[q] = A.idx[e + q * W];
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) x[q] = in[c[q]];
+    y0 = fma(a[0], x[0], y0);
+    y1 = fma(a[1], x[1], y1);
+    y2 = fma(a[2], x[2], y2);
+    y3 = fma(a[3], x[3], y3);
+    y0 = fma(a[4], x[4], y0);
+    y1 = fma(a[5], x[5], y1);
+    y2 = fma(a[6], x[6], y2);
+    y3 = fma(a[7], x[7], y3);
+  }
   for (; e + 3 * W < e1; e += 4 * W) {
     y0 = fma(A.val[e], in[A.idx[e]], y0);
     y1 = fma(A.val[e + W], in[A.idx[e + W]], y1);
