@@ -85,6 +85,12 @@ def dist_env():
     return rank, world, local
 
 
+def replica_value(world, npts, steps, dev_ms_max):
+    """Whole-job rate of N replicas: every rank processed npts x steps points, the job took
+    the slowest rank's time (G points / s)."""
+    return world * npts * steps / (dev_ms_max * 1e-3) / 1e9
+
+
 class Dist:
     """Barrier and max-reduction over ranks (gloo on CPU tensors; replicas only)."""
 
@@ -714,7 +720,7 @@ def run_ours(args, rank, world):
             finite = False
     dist.barrier()
     dev_ms = dist.max(dev_ms)
-    value = world * npts * args.steps / (dev_ms * 1e-3) / 1e9
+    value = replica_value(world, npts, args.steps, dev_ms)
 
     # roofline of the stage kernel: one launch covers one stage of every simulation
     m0 = models[0]
