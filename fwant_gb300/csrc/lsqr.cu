@@ -24,7 +24,10 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
+#include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/fwant_lsqr.h"
@@ -384,8 +387,28 @@ fwant_status fwant_lsqr_create(long long nrow, long long ncol, const long long* 
     if (row_ptr[r + 1] < row_ptr[r]) return FWANT_ERR_INVALID_ARG;
   const long long nnz = row_ptr[nrow];
   if (nnz > 0 && (!col || !val)) return FWANT_ERR_INVALID_ARG;
-  for (long long e = 0; e < nnz; ++e)
-    if (col[e] < 0 || col[e] >= ncol) return FWANT_ERR_INVALID_ARG;
+  // host work in T threads, each over a contiguous range of rows holding about nnz / T
+  // entries (the column check, then the counting sort into compressed columns)
+  const int T = int(std::max(1u, std::min(16u, std::thread::hardware_concurrency())));
+  std::vector<long long> rb(size_t(T) + 1, nrow);
+  rb[0] = 0;
+  for (int t = 1; t < T; ++t)
+    rb[size_t(t)] = std::lower_bound(row_ptr, row_ptr + nrow + 1, nnz / T * t) - row_ptr;
+  auto parallel = [T](const std::function<void(int)>& body) {
+    std::vector<std::thread> th;
+    for (int t = 1; t < T; ++t) th.emplace_back(body, t);
+    body(0);
+    for (auto& x : th) x.join();
+  };
+  {
+    std::vector<char> bad_col(size_t(T), 0);
+    parallel([&](int t) {
+      for (long long e = row_ptr[rb[size_t(t)]]; e < row_ptr[rb[size_t(t) + 1]]; ++e)
+        if (col[e] < 0 || col[e] >= ncol) bad_col[size_t(t)] = 1;
+    });
+    for (char b : bad_col)
+      if (b) return FWANT_ERR_INVALID_ARG;
+  }
   auto* l = new fwant_lsqr();
   l->device = device;
   l->nrow = nrow;
@@ -400,21 +423,37 @@ fwant_status fwant_lsqr_create(long long nrow, long long ncol, const long long* 
     return bad(FWANT_ERR_CUDA);
   }
   l->nblk = LS_BLOCKS;
-  // compressed columns: counting sort by column, rows ascending within a column
+  // compressed columns: counting sort by column.  Thread t counts its rows' entries per
+  // column; a column's entries from thread t follow those of threads 0..t-1, so rows stay
+  // ascending within every column, whatever the thread count.
   std::vector<long long> cp(size_t(ncol) + 1, 0);
-  for (long long e = 0; e < nnz; ++e) ++cp[size_t(col[e]) + 1];
-  for (long long j = 0; j < ncol; ++j) cp[size_t(j) + 1] += cp[size_t(j)];
-  std::vector<int> ri(size_t(std::max(nnz, 1LL)));
-  std::vector<double> vt(size_t(std::max(nnz, 1LL)));
-  {
-    std::vector<long long> pos(cp.begin(), cp.end() - 1);
-    for (long long r = 0; r < nrow; ++r)
+  std::vector<std::vector<long long>> pos(static_cast<size_t>(T));
+  parallel([&](int t) {
+    std::vector<long long>& c = pos[size_t(t)];
+    c.assign(size_t(ncol), 0);
+    for (long long e = row_ptr[rb[size_t(t)]]; e < row_ptr[rb[size_t(t) + 1]]; ++e) ++c[size_t(col[e])];
+  });
+  for (long long j = 0; j < ncol; ++j) {
+    long long acc = cp[size_t(j)];
+    for (int t = 0; t < T; ++t) {
+      const long long c = pos[size_t(t)][size_t(j)];
+      pos[size_t(t)][size_t(j)] = acc;
+      acc += c;
+    }
+    cp[size_t(j) + 1] = acc;
+  }
+  std::unique_ptr<int[]> ri(new int[size_t(std::max(nnz, 1LL))]);
+  std::unique_ptr<double[]> vt(new double[size_t(std::max(nnz, 1LL))]);
+  parallel([&](int t) {
+    std::vector<long long>& c = pos[size_t(t)];
+    for (long long r = rb[size_t(t)]; r < rb[size_t(t) + 1]; ++r)
       for (long long e = row_ptr[r]; e < row_ptr[r + 1]; ++e) {
-        const long long p = pos[size_t(col[e])]++;
+        const long long p = c[size_t(col[e])]++;
         ri[size_t(p)] = int(r);
         vt[size_t(p)] = val[e];
       }
-  }
+  });
+  pos.clear();
   // length classes of the rows and of the columns, each list ascending
   auto classes = [](const long long* ptr, long long n, std::vector<int>& lst, long long cnt[NCLS]) {
     lst.clear();
@@ -457,8 +496,8 @@ fwant_status fwant_lsqr_create(long long nrow, long long ncol, const long long* 
   if (e == cudaSuccess) e = cudaMemcpy(l->cp, cp.data(), (nc + 1) * sizeof(long long), cudaMemcpyHostToDevice);
   if (e == cudaSuccess && ne) e = cudaMemcpy(l->ci, col, ne * sizeof(int), cudaMemcpyHostToDevice);
   if (e == cudaSuccess && ne) e = cudaMemcpy(l->va, val, ne * sizeof(double), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess && ne) e = cudaMemcpy(l->ri, ri.data(), ne * sizeof(int), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess && ne) e = cudaMemcpy(l->vt, vt.data(), ne * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && ne) e = cudaMemcpy(l->ri, ri.get(), ne * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && ne) e = cudaMemcpy(l->vt, vt.get(), ne * sizeof(double), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(l->b, rhs, nr * sizeof(double), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(l->cls_rows, rows_cls.data(), nr * sizeof(int), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(l->cls_cols, cols_cls.data(), nc * sizeof(int), cudaMemcpyHostToDevice);
