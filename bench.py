@@ -698,6 +698,7 @@ def run_ours(args, rank, world):
         t_tune = time.perf_counter()
         ctas = batch.autotune(4)
         tuned = {"planes_per_cta": [s.planes_per_cta for s in sims], "ctas": ctas,
+                 "lean_stages": sims[0].lean_stages,
                  "tune_s": time.perf_counter() - t_tune}
     # per-launch timing of the stage kernel (CUDA events around each launch, eager)
     stage_ms, end_ms = batch.profile_stages(8)
@@ -774,6 +775,7 @@ def run_ours(args, rank, world):
             inputs.attach(s, m)
             if tuned:
                 s.planes_per_cta = tuned["planes_per_cta"][len(esims)]
+                s.lean_stages = tuned["lean_stages"]
             esims.append(s)
             h2d += 3 * m.lam.nbytes + m.x.nbytes + m.y.nbytes + m.z.nbytes
         eb = fw.Batch(esims)

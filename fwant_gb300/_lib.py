@@ -81,6 +81,8 @@ EXPORTS = [
     ("fwant_batch_autotune", C.c_int, [_vp, C.c_int, _ip]),
     ("fwant_set_planes_per_cta", C.c_int, [_vp, C.c_int]),
     ("fwant_get_planes_per_cta", C.c_int, [_vp, _ip]),
+    ("fwant_set_lean_stages", C.c_int, [_vp, C.c_int]),
+    ("fwant_get_lean_stages", C.c_int, [_vp, _ip]),
     ("fwant_batch_create", C.c_int, [C.POINTER(_vp), C.c_int, C.POINTER(_vp)]),
     ("fwant_batch_destroy", None, [_vp]),
     ("fwant_batch_last_error", C.c_char_p, [_vp]),
@@ -396,6 +398,17 @@ class Solver:
     @planes_per_cta.setter
     def planes_per_cta(self, planes):
         self._chk(self._lib.fwant_set_planes_per_cta(self._h, int(planes)))
+
+    @property
+    def lean_stages(self):
+        """Bit mask of the RK stages split into interior-only and full launches."""
+        v = C.c_int()
+        self._chk(self._lib.fwant_get_lean_stages(self._h, C.byref(v)))
+        return v.value
+
+    @lean_stages.setter
+    def lean_stages(self, mask):
+        self._chk(self._lib.fwant_set_lean_stages(self._h, int(mask)))
 
     def set_storage_scale(self, velocity_scale, stress_scale):
         """Power-of-two scales of 2-byte storage (stored value = physical value * scale)."""

@@ -1570,6 +1570,19 @@ fwant_status fwant_get_planes_per_cta(fwant_solver* s, int* planes) {
   return FWANT_OK;
 }
 
+fwant_status fwant_set_lean_stages(fwant_solver* s, int mask) {
+  if (!s || (mask & ~5) != 0) return FWANT_ERR_INVALID_ARG;
+  s->lean_mask = mask;
+  s->drop_graphs();
+  return FWANT_OK;
+}
+
+fwant_status fwant_get_lean_stages(fwant_solver* s, int* mask) {
+  if (!s || !mask) return FWANT_ERR_INVALID_ARG;
+  *mask = s->lean_mask;
+  return FWANT_OK;
+}
+
 }  // extern "C"
 
 // ---- batches of simulations stepped together -------------------------------------------
@@ -1891,6 +1904,25 @@ fwant_status fwant_batch_autotune(fwant_batch* b, int trial_steps, int* ctas_out
     if (t < best) { best = t; best_ctas = c; }
   }
   b->ctas = best_ctas;
+  // interior-only launches for stages 1 and 4 (mask 5), for one of them, or none: on small
+  // grids most items touch a boundary and the extra launches can cost more than they save
+  const int masks[] = {5, 1, 4, 0};
+  int best_mask = b->sims[0]->lean_mask;
+  double best_m = 1e30;
+  for (int mk : masks) {
+    for (fwant_solver* m : b->sims) {
+      m->lean_mask = mk;
+      m->drop_graphs();
+    }
+    double t = 0.0;
+    fwant_status rc = trial(&t);
+    if (rc != FWANT_OK) return rc;
+    if (t < best_m) { best_m = t; best_mask = mk; }
+  }
+  for (fwant_solver* m : b->sims) {
+    m->lean_mask = best_mask;
+    m->drop_graphs();
+  }
   b->drop_graphs();
   if (ctas_out) *ctas_out = best_ctas;
   return FWANT_OK;

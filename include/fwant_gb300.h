@@ -308,6 +308,12 @@ fwant_status fwant_last_run_ms(fwant_solver* s, double* ms);
  * the grid size; a tuning knob of the autotuner).  No counterpart in the reference. */
 fwant_status fwant_set_planes_per_cta(fwant_solver* s, int planes);
 fwant_status fwant_get_planes_per_cta(fwant_solver* s, int* planes);
+/* Which RK stages split their work items into an interior-only launch and a full launch
+ * (bit 0: stage 1, bit 2: stage 4; default 5); 0 runs every stage as one full launch.
+ * No counterpart in the reference (a tuning knob of the stage kernel, set by
+ * fwant_batch_autotune). */
+fwant_status fwant_set_lean_stages(fwant_solver* s, int mask);
+fwant_status fwant_get_lean_stages(fwant_solver* s, int* mask);
 
 /* Autotuner: times every planes-per-CTA candidate (4 ... 128, up to nk) over trial_steps
  * eager steps with CUDA events, keeps the fastest and returns it in *planes (may be NULL).
@@ -338,8 +344,9 @@ fwant_status fwant_batch_run(fwant_batch* b, int nsteps);
 fwant_status fwant_batch_last_run_ms(fwant_batch* b, double* ms);
 /* Autotune the batch as it runs: one planes-per-CTA value for every member (4 ... 32,
  * timed on the batched launches), then the CTA schedule (one CTA per work item, or
- * persistent grids of 1, 2 or 4 CTAs per SM); the chosen CTA count (0 = one per work item)
- * goes to *ctas (may be NULL).  Before the first step; the members' states are restored. */
+ * persistent grids of 1, 2 or 4 CTAs per SM), then which stages split off an interior-only
+ * launch; the chosen CTA count (0 = one per work item) goes to *ctas (may be NULL).
+ * Before the first step; the members' states are restored. */
 fwant_status fwant_batch_autotune(fwant_batch* b, int trial_steps, int* ctas);
 /* fwant_profile_stages for a batch: eager steps with events around each stage's launches
  * (stage_ms[4]: all members' launches of that stage) and the step-end kernels. */
