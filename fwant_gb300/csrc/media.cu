@@ -838,7 +838,8 @@ struct fwant_media {
   std::vector<float> hx, hy, hz;  // grid on the host (model selection)
   cudaStream_t st = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  std::vector<void*> model_bufs;  // device arrays of the models
+  std::vector<void*> model_bufs[2];  // device arrays of the background (0) and perturbation (1)
+  int slot = 0;                      // the model being uploaded
   float *x = nullptr, *y = nullptr, *z = nullptr;
   float *lam = nullptr, *mu = nullptr, *rho = nullptr;
   double* trig = nullptr;  // ca[nx], sa[nx], cb[ny], sb[ny]
@@ -863,8 +864,19 @@ struct fwant_media {
     if (st) cudaStreamDestroy(st);
   }
   void free_models() {
-    for (void* p : model_bufs) cudaFree(p);
-    model_bufs.clear();
+    for (auto& v : model_bufs) {
+      for (void* p : v) cudaFree(p);
+      v.clear();
+    }
+  }
+  // A new background (s = 0) or perturbation (s = 1) replaces the previous one: its arrays
+  // are freed and the kind cleared until the new model is complete.
+  void begin_model(int s) {
+    for (void* p : model_bufs[s]) cudaFree(p);
+    model_bufs[s].clear();
+    if (s == 0) a.bkind = 0;
+    else a.pkind = 0;
+    slot = s;
   }
   fwant_status fail(fwant_status c, const std::string& m) {
     msg = m;
@@ -878,7 +890,7 @@ struct fwant_media {
       msg = std::string("out of device memory: ") + what;
       return nullptr;
     }
-    model_bufs.push_back(d);
+    model_bufs[slot].push_back(d);
     if (cudaMemcpy(d, h, n * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
       cudaGetLastError();
       msg = std::string("copy failed: ") + what;
@@ -986,6 +998,7 @@ fwant_status fwant_media_set_cart1d(fwant_media* m, int nk, const float* depth, 
   for (int k = 1; k < nk; ++k)
     if (!(depth[k] >= depth[k - 1])) return m->fail(FWANT_ERR_INVALID_ARG, "media_set_cart1d: depths must ascend");
   cudaSetDevice(m->device);
+  m->begin_model(0);
   DCart c;
   c.nk = nk;
   if (!(c.d = m->up(depth, nk, "cart1d")) || !(c.vp = m->up(vp, nk, "cart1d")) || !(c.vs = m->up(vs, nk, "cart1d")) ||
@@ -1008,6 +1021,7 @@ fwant_status fwant_media_set_layers(fwant_media* m, int kind, int ni, int nj, in
   if (kind == FWANT_MEDIA_COMPOSITE && (!vp_exp || !vs_exp || !rho_exp))
     return m->fail(FWANT_ERR_INVALID_ARG, "media_set_layers: composite needs the exponents");
   cudaSetDevice(m->device);
+  m->begin_model(0);
   const size_t n3 = size_t(ni) * nj * nk, nv = kind == FWANT_MEDIA_COMPOSITE ? 2 * n3 : size_t(2) * nk;
   DLayers L{};
   L.ni = ni;
@@ -1047,6 +1061,7 @@ fwant_status fwant_media_set_volume(fwant_media* m, int perturbed, int ni, int n
         for (int i = 0; i < vi; ++i)
           f[q][(size_t(k) * vj + j) * vi + i] = src[q][(size_t(k) * nj + (j1 - 1 + j)) * ni + (i1 - 1 + i)];
   }
+  m->begin_model(perturbed ? 1 : 0);
   DVol V{};
   V.ni = vi;
   V.nj = vj;
@@ -1093,6 +1108,7 @@ fwant_status fwant_media_set_verpoly(fwant_media* m, int perturbed, int ni, int 
           if (p == 0) r[d] = rz[s];
           for (int q = 0; q < 3; ++q) c[q][d] = src[q][s];
         }
+  m->begin_model(perturbed ? 1 : 0);
   DPoly P{};
   P.ni = vi;
   P.nj = vj;

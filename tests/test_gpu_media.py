@@ -72,6 +72,20 @@ def test_config_sized_grid(oracle_mod, native_lib):
     assert g.last_eval_ms() > 0
 
 
+def test_models_replace_earlier_ones(oracle_mod, native_lib):
+    """A second background or perturbation replaces the first (its device arrays freed):
+    the result equals a handle given only the later models"""
+    import fwant_gb300 as fw
+    from oracle import oracle as orc
+    x, y, z, zt = mc.grid(12, 10, 8, seed=6)
+    first = mc.case(mc.LAYERED, x, y, z, zt, seed=7, perturb=mc.VERPOLY)
+    second = mc.case(mc.VOLUME, x, y, z, zt, seed=8, perturb=mc.VOLUME)
+    g = mc.feed(fw.Media(12, 10, 8, x, y, z, zt), first + second)
+    o = mc.feed(orc.MediaOracle(12, 10, 8, x, y, z, zt), second)
+    for a, b in zip(g.eval(), o.eval()):
+        np.testing.assert_array_equal(a, b)
+
+
 def test_errors(oracle_mod, native_lib):
     import fwant_gb300 as fw
     from oracle import oracle as orc
