@@ -129,3 +129,20 @@ def test_autotune_keeps_results(oracle_mod, native_lib):
     with pytest.raises(fw.FwantError) as e:
         tuned.autotune(2)   # after the first step
     assert e.value.code == 6
+
+
+def test_lean_stage_split_keeps_results(oracle_mod, native_lib):
+    """Running every stage as one full launch (lean stages 0) instead of splitting stages 1
+    and 4 into interior-only and full launches moves work between kernels only: the same
+    fields bit for bit in the reference-order form.  Masks other than subsets of stages 1
+    and 4 are refused."""
+    import fwant_gb300 as fw
+    one, split = _members(oracle_mod, True)[0]
+    assert split.lean_stages == 5
+    one.lean_stages = 0
+    for s in (one, split):
+        s.run(16)
+    for c in range(9):
+        np.testing.assert_array_equal(one.get_field(c), split.get_field(c))
+    with pytest.raises(fw.FwantError):
+        one.lean_stages = 2
