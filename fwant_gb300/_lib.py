@@ -133,6 +133,9 @@ EXPORTS = [
     ("fwant_media_eval", C.c_int, [_vp, _fp, _fp, _fp]),
     ("fwant_media_stept_check", C.c_int, [_vp, _fp, C.POINTER(C.c_int), _fp, _fp]),
     ("fwant_media_last_eval_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
+    ("fwant_media_device_arrays", C.c_int, [_vp, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                            C.POINTER(C.c_void_p)]),
+    ("fwant_set_media_device", C.c_int, [_vp, _vp, _vp, _vp]),
 ]
 
 
@@ -718,6 +721,13 @@ class Media:
         ms = C.c_double()
         self._chk(self._lib.fwant_media_last_eval_ms(self._h, C.byref(ms)))
         return ms.value
+
+    def to_solver(self, solver):
+        """Hand the last evaluated medium to a solver on the same GPU, device to device
+        (fwant_media_device_arrays + fwant_set_media_device)."""
+        p = [C.c_void_p() for _ in range(3)]
+        self._chk(self._lib.fwant_media_device_arrays(self._h, *[C.byref(q) for q in p]))
+        solver._chk(self._lib.fwant_set_media_device(solver._h, *p))
 
 
 def reference_steps(nt: int) -> int:

@@ -1208,6 +1208,15 @@ fwant_status fwant_media_stept_check(fwant_media* m, float* dtmax, int ijk[3], f
   return FWANT_OK;
 }
 
+fwant_status fwant_media_device_arrays(fwant_media* m, const float** lambda, const float** mu, const float** rho) {
+  if (!m || !lambda || !mu || !rho) return FWANT_ERR_INVALID_ARG;
+  if (!m->evaluated) return m->fail(FWANT_ERR_STATE, "media_device_arrays: no evaluated medium");
+  *lambda = m->lam;
+  *mu = m->mu;
+  *rho = m->rho;
+  return FWANT_OK;
+}
+
 fwant_status fwant_media_last_eval_ms(fwant_media* m, double* ms) {
   if (!m || !ms) return FWANT_ERR_INVALID_ARG;
   *ms = m->last_ms;

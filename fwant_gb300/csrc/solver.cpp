@@ -63,7 +63,6 @@ struct fwant_solver {
   int rA = 0, rB = 1, rC = 2, rT = 3;
   float* med = nullptr;  // lambda, mu, rho, fstride apart (one TMA tensor)
   float *lam = nullptr, *mu = nullptr, *rho = nullptr;
-  std::vector<float> h_rho;
   int* d_err = nullptr;  // device error word of the stage kernel (bounded waits)
   // TMA descriptors: per register set the halo'd tile, the z-queue plane and the point
   // box; one for the medium
@@ -331,6 +330,23 @@ struct fwant_solver {
     return cudaMemcpy2D(dst + fw::PADL, size_t(g.px) * 4, src, size_t(g.nx) * 4, size_t(g.nx) * 4,
                         size_t(g.ny) * g.nz, cudaMemcpyHostToDevice);
   }
+  // rho of the 7^3 box around (si, sj, sk) from the device medium; entries outside the
+  // arrays stay 0 (the source weights use interior points only)
+  cudaError_t fetch_rho_box(int si, int sj, int sk, float* box) {
+    std::fill(box, box + 343, 0.0f);
+    const int i0 = std::max(si - 3, 0), i1 = std::min(si + 3, g.nx - 1);
+    if (i0 > i1) return cudaSuccess;
+    for (int lk = -3; lk <= 3; ++lk)
+      for (int lj = -3; lj <= 3; ++lj) {
+        const int j = sj + lj, k = sk + lk;
+        if (j < 0 || j >= g.ny || k < 0 || k >= g.nz) continue;
+        const float* src = rho + fw::PADL + i0 + size_t(g.px) * (size_t(j) + size_t(g.ny) * k);
+        const cudaError_t e = cudaMemcpy(box + (i0 - (si - 3)) + 7 * ((lj + 3) + 7 * (lk + 3)), src,
+                                         size_t(i1 - i0 + 1) * sizeof(float), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return e;
+      }
+    return cudaSuccess;
+  }
   cudaError_t get3(float* dst, const float* src) {
     return cudaMemcpy2D(dst, size_t(g.nx) * 4, src + fw::PADL, size_t(g.px) * 4, size_t(g.nx) * 4,
                         size_t(g.ny) * g.nz, cudaMemcpyDeviceToHost);
@@ -486,9 +502,13 @@ struct fwant_solver {
     std::vector<int> fc;
     std::vector<float> fwt, fF;
     std::vector<unsigned char> fon;
-    float nd[343];
+    float nd[343], rbox[343];
     for (int q = 0; q < F.num; ++q) {
       const int si = F.indx[3 * q] - 1, sj = F.indx[3 * q + 1] - 1, sk = F.indx[3 * q + 2] - 1;
+      {
+        const cudaError_t re = fetch_rho_box(si, sj, sk, rbox);
+        if (re != cudaSuccess) return cuda_fail(re, "source weights: rho");
+      }
       if (!fw::hm::norm_delt(nd, F.shift[3 * q], F.shift[3 * q + 1], F.shift[3 * q + 2]))
         return fail(FWANT_ERR_INVALID_ARG, "cal_norm_delt is zero");
       if (g.freesurf && sk + 3 > g.k2) {
@@ -508,8 +528,7 @@ struct fwant_solver {
             unsigned char on = 0;
             if (interior(i, j, k)) {
               float V = (X(i + 1) - X(i - 1)) * (Y(j + 1) - Y(j - 1)) * (Z(k + 1) - Z(k - 1)) / 8.0f * (Z(k) * Z(k)) * hxsin[i];
-              const size_t pf = size_t(i) + size_t(g.nx) * (size_t(j) + size_t(g.ny) * k);
-              V = 1.0f / (V * h_rho[pf]) * d;
+              V = 1.0f / (V * rbox[(li + 3) + 7 * ((lj + 3) + 7 * (lk + 3))]) * d;
               on = 1;
               wv = V;
               if (g.freesurf && k == g.k2) {
@@ -991,25 +1010,32 @@ fwant_status fwant_get_metric(fwant_solver* s, float* xsin, float* xcot, float* 
   return FWANT_OK;
 }
 
-fwant_status fwant_set_media(fwant_solver* s, const float* lambda, const float* mu, const float* rho) {
+// Medium from host arrays (through a device staging buffer, one large copy each) or from
+// device arrays; rho is checked on the device before anything is overwritten, then each
+// array goes into the padded layout.
+static fwant_status load_media(fwant_solver* s, const float* lambda, const float* mu, const float* rho,
+                               bool on_device) {
   if (!s || !lambda || !mu || !rho) return FWANT_ERR_INVALID_ARG;
   cudaSetDevice(s->cfg.device);
   const auto& g = s->g;
   const size_t n = size_t(g.nx) * g.ny * g.nz;
-  // each array goes up contiguously into a staging buffer (one large copy), then into the
-  // padded layout on the device; rho is checked there before anything is overwritten
   float* staging = nullptr;
-  cudaError_t e = cudaMalloc(&staging, n * sizeof(float) + 256);
+  const size_t bytes = on_device ? 256 : n * sizeof(float) + 256;
+  cudaError_t e = cudaMalloc(&staging, bytes);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return s->fail(FWANT_ERR_OOM, "set_media: no device memory for the staging buffer");
   }
-  unsigned int* bad = reinterpret_cast<unsigned int*>(reinterpret_cast<char*>(staging) + ((n * sizeof(float) + 127) / 128) * 128);
+  unsigned int* bad = reinterpret_cast<unsigned int*>(reinterpret_cast<char*>(staging) + bytes - 128);
   unsigned int hbad = 0;
-  e = cudaMemcpy(staging, rho, n * sizeof(float), cudaMemcpyHostToDevice);
+  const float* drho = rho;
+  if (!on_device) {
+    e = cudaMemcpy(staging, rho, n * sizeof(float), cudaMemcpyHostToDevice);
+    drho = staging;
+  }
   if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, sizeof(unsigned int), s->st);
   if (e == cudaSuccess) {
-    fw::launch_count_nonpositive((long long)n, staging, bad, s->st);
+    fw::launch_count_nonpositive((long long)n, drho, bad, s->st);
     e = cudaMemcpyAsync(&hbad, bad, sizeof(unsigned int), cudaMemcpyDeviceToHost, s->st);
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
@@ -1017,21 +1043,34 @@ fwant_status fwant_set_media(fwant_solver* s, const float* lambda, const float* 
     cudaFree(staging);
     return s->fail(FWANT_ERR_INVALID_ARG, "rho must be > 0 everywhere (ghosts included)");
   }
-  auto pad = [&](float* dst) {
-    return cudaMemcpy2D(dst + fw::PADL, size_t(g.px) * 4, staging, size_t(g.nx) * 4, size_t(g.nx) * 4,
+  auto pad = [&](float* dst, const float* src) {
+    return cudaMemcpy2D(dst + fw::PADL, size_t(g.px) * 4, src, size_t(g.nx) * 4, size_t(g.nx) * 4,
                         size_t(g.ny) * g.nz, cudaMemcpyDeviceToDevice);
   };
-  if (e == cudaSuccess) e = pad(s->rho);
-  if (e == cudaSuccess) e = cudaMemcpy(staging, lambda, n * sizeof(float), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = pad(s->lam);
-  if (e == cudaSuccess) e = cudaMemcpy(staging, mu, n * sizeof(float), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = pad(s->mu);
+  if (on_device) {
+    if (e == cudaSuccess) e = pad(s->rho, rho);
+    if (e == cudaSuccess) e = pad(s->lam, lambda);
+    if (e == cudaSuccess) e = pad(s->mu, mu);
+  } else {
+    if (e == cudaSuccess) e = pad(s->rho, staging);
+    if (e == cudaSuccess) e = cudaMemcpy(staging, lambda, n * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = pad(s->lam, staging);
+    if (e == cudaSuccess) e = cudaMemcpy(staging, mu, n * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = pad(s->mu, staging);
+  }
   cudaFree(staging);
   if (e != cudaSuccess) return s->cuda_fail(e, "set_media");
-  s->h_rho.assign(rho, rho + n);  // the source weights divide by rho at the source boxes
   s->have_media = true;
   s->src_dirty = true;
   return FWANT_OK;
+}
+
+fwant_status fwant_set_media(fwant_solver* s, const float* lambda, const float* mu, const float* rho) {
+  return load_media(s, lambda, mu, rho, false);
+}
+
+fwant_status fwant_set_media_device(fwant_solver* s, const float* d_lambda, const float* d_mu, const float* d_rho) {
+  return load_media(s, d_lambda, d_mu, d_rho, true);
 }
 
 fwant_status fwant_set_pml(fwant_solver* s, const int number[6], const float velocity[6], const float bmax[6],

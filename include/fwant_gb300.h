@@ -114,6 +114,12 @@ fwant_status fwant_get_metric(fwant_solver* s, float* xsin, float* xcot, float* 
  * (code/srcF/mod_media.F90:76-96). */
 fwant_status fwant_set_media(fwant_solver* s, const float* lambda, const float* mu,
                              const float* rho);
+/* fwant_set_media from arrays already in device memory on the solver's GPU (the same
+ * (nx,ny,nz) Fortran-ordered float arrays), e.g. fwant_media_device_arrays of the medium
+ * preprocessor: the medium goes from preprocessing to the solver without a round trip
+ * through the host.  No counterpart in the reference (its stages exchange files). */
+fwant_status fwant_set_media_device(fwant_solver* s, const float* d_lambda, const float* d_mu,
+                                    const float* d_rho);
 
 /* CFS-PML on the faces x1 x2 y1 y2 z1 z2 (6 entries each): keys abs_number,
  * abs_velocity, CFS_bmax, CFS_amax of abs_init (code/srcF/mod_abs_npml.F90:135-616).

@@ -91,6 +91,11 @@ fwant_status fwant_media_eval(fwant_media* m, float* lambda, float* mu, float* r
  * there. */
 fwant_status fwant_media_stept_check(fwant_media* m, float* dtmax, int ijk[3], float* vp, float* dl);
 
+/* Device addresses of the last evaluated lambda, mu and rho ((ni+6, nj+6, nk+6) floats each,
+ * Fortran order), valid until the next fwant_media_eval or fwant_media_destroy; hand them
+ * to fwant_set_media_device of a solver on the same GPU. */
+fwant_status fwant_media_device_arrays(fwant_media* m, const float** lambda, const float** mu, const float** rho);
+
 /* device time (ms) of the last fwant_media_eval's kernels */
 fwant_status fwant_media_last_eval_ms(fwant_media* m, double* ms);
 

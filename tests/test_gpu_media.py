@@ -86,6 +86,30 @@ def test_models_replace_earlier_ones(oracle_mod, native_lib):
         np.testing.assert_array_equal(a, b)
 
 
+def test_device_handoff_to_solver(oracle_mod, native_lib):
+    """The evaluated medium handed to a solver device to device (fwant_media_device_arrays
+    + fwant_set_media_device) gives the solver the same medium as the host arrays through
+    fwant_set_media: identical fields after 16 steps"""
+    import fwant_gb300 as fw
+    from fwant_gb300 import inputs
+
+    from helpers import small_model
+    m = small_model("buried")
+    zt = float(m.z[3 + m.nk - 1])
+    M = mc.feed(fw.Media(m.ni, m.nj, m.nk, m.x, m.y, m.z, zt), mc.case(mc.CART1D, m.x, m.y, m.z, zt, seed=2,
+                                                                      perturb=mc.VOLUME))
+    lam, mu, rho = M.eval()
+    a = inputs.attach(fw.Solver(m.ni, m.nj, m.nk, m.stept), m)
+    b = inputs.attach(fw.Solver(m.ni, m.nj, m.nk, m.stept), m)
+    M.to_solver(a)
+    b.set_media(lam, mu, rho)
+    for s in (a, b):
+        s.run(16)
+    for c in range(9):
+        np.testing.assert_array_equal(a.get_field(c), b.get_field(c))
+    assert np.any(a.get_field("Vz"))
+
+
 def test_errors(oracle_mod, native_lib):
     import fwant_gb300 as fw
     from oracle import oracle as orc
