@@ -693,6 +693,12 @@ struct StArgs {
   int ni, nj, nk, nx, ny;
   const float *z, *lam, *mu, *rho;
   const double *ca, *sa, *cb, *sb;  // cos / sin of x - pi/2 and of y, per grid index
+  // FP32 screen: the same cos / sin and their differences to the next and previous grid
+  // index (formed in double on the host), and the z differences
+  const float *fca, *fsa, *dcap, *dcam, *dsap, *dsam;   // [nx]
+  const float *fcb, *fsb, *dcbp, *dcbm, *dsbp, *dsbm;   // [ny]
+  const float *dzp, *dzm;                               // [nz]
+  const unsigned* screen_min;  // bits of the screen's minimum (pass 2)
 };
 
 __device__ __forceinline__ void gpoint(const StArgs& s, int i, int j, int k, double* g) {
@@ -737,6 +743,62 @@ __device__ float point_dt(const StArgs& s, int i, int j, int k, float& vp, float
   return 1.3f / vp * dl;
 }
 
+// The same quantity in FP32 from neighbour offsets relative to the point (each a product of
+// a few accurately rounded factors, so no large coordinates cancel): within about 1e-6 of
+// the exact value, used only to find the points that can hold the minimum.
+__device__ float point_dt32(const StArgs& s, int i, int j, int k) {
+  const size_t p = (size_t(k) * s.ny + j) * s.nx + i;
+  const float vp = sqrtf((s.lam[p] + 2.0f * s.mu[p]) / s.rho[p]);
+  const float zk = s.z[k], ca = s.fca[i], sa = s.fsa[i], cb = s.fcb[j], sb = s.fsb[j];
+  float ax[2][3], by[2][3], cz[2][3];
+  const float dca[2] = {s.dcam[i], s.dcap[i]}, dsa[2] = {s.dsam[i], s.dsap[i]};
+  const float dcb[2] = {s.dcbm[j], s.dcbp[j]}, dsb[2] = {s.dsbm[j], s.dsbp[j]};
+  const float dz[2] = {s.dzm[k], s.dzp[k]};
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    ax[q][0] = zk * dca[q] * cb;
+    ax[q][1] = zk * dca[q] * sb;
+    ax[q][2] = zk * dsa[q];
+    by[q][0] = zk * ca * dcb[q];
+    by[q][1] = zk * ca * dsb[q];
+    by[q][2] = 0.0f;
+    cz[q][0] = dz[q] * ca * cb;
+    cz[q][1] = dz[q] * ca * sb;
+    cz[q][2] = dz[q] * sa;
+  }
+  float dmin = 0.0f;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const float* a = ax[q & 1];
+    const float* b = by[(q >> 1) & 1];
+    const float* c = cz[(q >> 2) & 1];
+    const float u0 = b[0] - a[0], u1 = b[1] - a[1], u2 = b[2] - a[2];
+    const float v0 = c[0] - a[0], v1 = c[1] - a[1], v2 = c[2] - a[2];
+    const float p0 = u1 * v2 - u2 * v1, p1 = u2 * v0 - u0 * v2, p2 = u0 * v1 - u1 * v0;
+    const float d = fabsf(p0 * a[0] + p1 * a[1] + p2 * a[2]) / sqrtf(p0 * p0 + p1 * p1 + p2 * p2);
+    dmin = q == 0 ? d : fminf(dmin, d);
+  }
+  return 1.3f / vp * dmin;
+}
+
+// pass 1: the screen's minimum over interior points (NaN excluded) as float bits
+__global__ void __launch_bounds__(MD_THREADS) stept_screen_kernel(const StArgs s, unsigned* out) {
+  const long long n = (long long)s.ni * s.nj * s.nk;
+  float best = INFINITY;
+  for (long long p = (long long)blockIdx.x * MD_THREADS + threadIdx.x; p < n; p += (long long)gridDim.x * MD_THREADS) {
+    const int i = int(p % s.ni) + LENFD, j = int((p / s.ni) % s.nj) + LENFD, k = int(p / ((long long)s.ni * s.nj)) + LENFD;
+    const float v = point_dt32(s, i, j, k);
+    if (v < best) best = v;
+  }
+  for (int o = 16; o > 0; o >>= 1) best = fminf(best, __shfl_down_sync(0xffffffffu, best, o));
+  // non-negative floats order like their bit patterns
+  if ((threadIdx.x & 31) == 0 && best < INFINITY) atomicMin(out, __float_as_uint(fmaxf(best, 0.0f)));
+}
+
+// a point can hold the exact minimum only if its screen value is within this factor of the
+// screen's minimum (the screen's error is about 1e-6 relative)
+constexpr float SCREEN_MARGIN = 1.0e-3f;
+
 // (value, interior point number) minimum; NaN counts as no candidate, as `dtlocal < dtmax`
 // is false for it in the reference
 __device__ __forceinline__ bool better(float v, long long p, float bv, long long bp) {
@@ -749,8 +811,11 @@ __global__ void __launch_bounds__(MD_THREADS) stept_kernel(const StArgs s, float
   const long long n = (long long)s.ni * s.nj * s.nk;
   float bv = 1.0e10f;
   long long bp = n;  // none
+  const unsigned sm = *s.screen_min;
+  const float thr = sm == 0xffffffffu ? INFINITY : __uint_as_float(sm) * (1.0f + SCREEN_MARGIN);
   for (long long p = (long long)blockIdx.x * MD_THREADS + threadIdx.x; p < n; p += (long long)gridDim.x * MD_THREADS) {
     const int i = int(p % s.ni) + LENFD, j = int((p / s.ni) % s.nj) + LENFD, k = int(p / ((long long)s.ni * s.nj)) + LENFD;
+    if (!(point_dt32(s, i, j, k) <= thr)) continue;  // cannot hold the minimum
     float vp, dl;
     const float v = point_dt(s, i, j, k, vp, dl);
     if (better(v, p, bv, bp)) {
@@ -843,6 +908,8 @@ struct fwant_media {
   float *x = nullptr, *y = nullptr, *z = nullptr;
   float *lam = nullptr, *mu = nullptr, *rho = nullptr;
   double* trig = nullptr;  // ca[nx], sa[nx], cb[ny], sb[ny]
+  float* screen = nullptr;  // FP32 screen tables: 6 x nx, 6 x ny, 2 x nz
+  unsigned* smin = nullptr;
   int* err = nullptr;
   float* pv = nullptr;
   long long* pp = nullptr;
@@ -856,7 +923,8 @@ struct fwant_media {
   ~fwant_media() {
     cudaSetDevice(device);
     free_models();
-    for (void* p : {(void*)x, (void*)y, (void*)z, (void*)lam, (void*)mu, (void*)rho, (void*)trig, (void*)err,
+    for (void* p : {(void*)x, (void*)y, (void*)z, (void*)lam, (void*)mu, (void*)rho, (void*)trig, (void*)screen,
+                    (void*)smin, (void*)err,
                     (void*)pv, (void*)pp, (void*)res, (void*)ip})
       cudaFree(p);
     if (ev0) cudaEventDestroy(ev0);
@@ -940,6 +1008,39 @@ fwant_status fwant_media_create(int ni, int nj, int nk, const float* x, const fl
     trig[2 * m->nx + j] = std::cos(ang);
     trig[2 * m->nx + m->ny + j] = std::sin(ang);
   }
+  // FP32 screen of the time-step check: cos / sin and their differences to the next and
+  // previous index (differences formed in double), z differences
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  std::vector<float> scr(size_t(6) * nx + size_t(6) * ny + size_t(2) * nz, 0.0f);
+  {
+    float* f = scr.data();
+    const double* ca = trig.data();
+    const double* sa = ca + nx;
+    const double* cb = sa + nx;
+    const double* sb = cb + ny;
+    for (int i = 0; i < nx; ++i) {
+      f[i] = float(ca[i]);
+      f[nx + i] = float(sa[i]);
+      f[2 * nx + i] = i + 1 < nx ? float(ca[i + 1] - ca[i]) : 0.0f;
+      f[3 * nx + i] = i > 0 ? float(ca[i - 1] - ca[i]) : 0.0f;
+      f[4 * nx + i] = i + 1 < nx ? float(sa[i + 1] - sa[i]) : 0.0f;
+      f[5 * nx + i] = i > 0 ? float(sa[i - 1] - sa[i]) : 0.0f;
+    }
+    float* g = f + 6 * nx;
+    for (int j = 0; j < ny; ++j) {
+      g[j] = float(cb[j]);
+      g[ny + j] = float(sb[j]);
+      g[2 * ny + j] = j + 1 < ny ? float(cb[j + 1] - cb[j]) : 0.0f;
+      g[3 * ny + j] = j > 0 ? float(cb[j - 1] - cb[j]) : 0.0f;
+      g[4 * ny + j] = j + 1 < ny ? float(sb[j + 1] - sb[j]) : 0.0f;
+      g[5 * ny + j] = j > 0 ? float(sb[j - 1] - sb[j]) : 0.0f;
+    }
+    float* h = g + 6 * ny;
+    for (int k = 0; k < nz; ++k) {
+      h[k] = k + 1 < nz ? float(double(z[k + 1]) - double(z[k])) : 0.0f;
+      h[nz + k] = k > 0 ? float(double(z[k - 1]) - double(z[k])) : 0.0f;
+    }
+  }
   const size_t n3 = size_t(npts);
   cudaError_t e = cudaStreamCreateWithFlags(&m->st, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&m->ev0);
@@ -948,6 +1049,8 @@ fwant_status fwant_media_create(int ni, int nj, int nk, const float* x, const fl
   if (e == cudaSuccess) e = cudaMalloc(&m->y, m->ny * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&m->z, m->nz * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&m->trig, trig.size() * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&m->screen, scr.size() * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&m->smin, sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMalloc(&m->lam, n3 * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&m->mu, n3 * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&m->rho, n3 * sizeof(float));
@@ -960,6 +1063,7 @@ fwant_status fwant_media_create(int ni, int nj, int nk, const float* x, const fl
   if (e == cudaSuccess) e = cudaMemcpy(m->y, y, m->ny * sizeof(float), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(m->z, z, m->nz * sizeof(float), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(m->trig, trig.data(), trig.size() * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(m->screen, scr.data(), scr.size() * sizeof(float), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     const fwant_status rc = e == cudaErrorMemoryAllocation ? FWANT_ERR_OOM : FWANT_ERR_CUDA;
     cudaGetLastError();
@@ -1183,6 +1287,20 @@ fwant_status fwant_media_stept_check(fwant_media* m, float* dtmax, int ijk[3], f
   s.sa = m->trig + m->nx;
   s.cb = m->trig + 2 * m->nx;
   s.sb = m->trig + 2 * m->nx + m->ny;
+  {
+    const float* f = m->screen;
+    const int nx = m->nx, ny = m->ny;
+    s.fca = f; s.fsa = f + nx; s.dcap = f + 2 * nx; s.dcam = f + 3 * nx; s.dsap = f + 4 * nx; s.dsam = f + 5 * nx;
+    const float* g = f + 6 * nx;
+    s.fcb = g; s.fsb = g + ny; s.dcbp = g + 2 * ny; s.dcbm = g + 3 * ny; s.dsbp = g + 4 * ny; s.dsbm = g + 5 * ny;
+    s.dzp = g + 6 * ny;
+    s.dzm = g + 6 * ny + m->nz;
+    s.screen_min = m->smin;
+  }
+  // pass 1: FP32 screen for the minimum; pass 2: the exact FP64 check on the points that can
+  // hold it, reduced over (value, point number)
+  cudaMemsetAsync(m->smin, 0xff, sizeof(unsigned), m->st);
+  stept_screen_kernel<<<ST_BLOCKS, MD_THREADS, 0, m->st>>>(s, m->smin);
   stept_kernel<<<ST_BLOCKS, MD_THREADS, 0, m->st>>>(s, m->pv, m->pp);
   stept_final_kernel<<<1, 32, 0, m->st>>>(s, m->pv, m->pp, ST_BLOCKS, m->res, m->ip);
   float r[3];

@@ -86,6 +86,21 @@ def test_models_replace_earlier_ones(oracle_mod, native_lib):
         np.testing.assert_array_equal(a, b)
 
 
+def test_stept_check_ties_and_screen(oracle_mod, native_lib):
+    """A homogeneous medium on a uniform-in-angle grid gives many points the same or nearly
+    the same limit: the FP32 screen keeps every candidate and the exact pass returns the
+    reference's first minimum in loop order"""
+    import fwant_gb300 as fw
+    from oracle import oracle as orc
+    x, y, z, zt = mc.grid(20, 16, 10, seed=9)
+    d = np.array([0.0, 1e6], np.float32)
+    calls = [("set_cart1d", (d, np.full(2, 6000.0, np.float32), np.full(2, 3400.0, np.float32),
+                             np.full(2, 2700.0, np.float32)))]
+    g = mc.feed(fw.Media(20, 16, 10, x, y, z, zt), calls)
+    o = mc.feed(orc.MediaOracle(20, 16, 10, x, y, z, zt), calls)
+    _compare(g, o, True)
+
+
 def test_device_handoff_to_solver(oracle_mod, native_lib):
     """The evaluated medium handed to a solver device to device (fwant_media_device_arrays
     + fwant_set_media_device) gives the solver the same medium as the host arrays through
