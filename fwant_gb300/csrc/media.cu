@@ -636,7 +636,7 @@ __device__ bool eval_fast(const Args& a, int i, int j, int k, float& lam_out, fl
 
 // SX = 0: any half_sample_point (eval_point); else the hoisted form for 0 / 1 per axis
 template <int SX, int SY, int SZ>
-__global__ void __launch_bounds__(MD_THREADS) effmedia_kernel(const Args a) {
+__global__ void __launch_bounds__(MD_THREADS, SX == 0 ? 2 : 3) effmedia_kernel(const Args a) {
   const long long n = (long long)a.ni * a.nj * a.nk;
   for (long long p = (long long)blockIdx.x * MD_THREADS + threadIdx.x; p < n; p += (long long)gridDim.x * MD_THREADS) {
     const int i = int(p % a.ni) + LENFD;
