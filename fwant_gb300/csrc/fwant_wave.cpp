@@ -13,10 +13,13 @@
 //
 // Also: --nc-copy IN OUT re-writes a NetCDF file through this program's reader and
 // writer; --nc-dump FILE prints its header and per-variable sums (format checks).
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <ctime>
+#include <fstream>
 #include <map>
 #include <numeric>
 #include <string>
@@ -174,6 +177,80 @@ int nc_tool(int argc, char** argv) {
 
 }  // namespace
 
+// seismo_mpi000000.nc with the samples recorded up to ntime: dims num_pt,
+// time(unlimited); time(time); components (time, num_pt) (io_seismo_put's file)
+void write_seismo(const std::string& out_root, fwant_solver* s, int ntime, int pt_tinv, int num_pt, float fstept) {
+  int nsamp = ntime / pt_tinv;
+  std::vector<float> seis(size_t(9) * nsamp * num_pt);
+  check(fwant_get_seismo(s, seis.data(), nsamp, &nsamp), s, "seismograms");
+  nc3::Writer w;
+  const int P = w.add_dim("num_pt", num_pt), T = w.add_dim("time", 0);
+  w.set_numrecs(nsamp);
+  w.add_gatt_text("title", "seismograms");
+  std::vector<double> t(nsamp);
+  for (int m = 0; m < nsamp; ++m) t[m] = double(float((m + 1) * pt_tinv) * fstept);  // t = ntime*stept
+  w.add_var("time", nc3::NC_FLOAT, {T}, t);
+  for (int c = 0; c < 9; ++c)
+    w.add_var_f(COMP[c], {T, P}, seis.data() + size_t(c) * nsamp * num_pt, size_t(nsamp) * num_pt);
+  std::string err;
+  if (!w.write(out_root + "/seismo_" + SUFFIX + ".nc", &err)) die(err);
+}
+
+// The run-time log (swmpi_time_init / _write / _end, code/srcF/mod_mpi.F90:331-405): a
+// header, then one line per step with its wall time, the hours passed and the hours left.
+// Steps run in graph-replayed chunks between output events, so each step of a chunk is
+// logged with the chunk's average time.
+class StepLog {
+ public:
+  StepLog(const std::string& path, int ntime) : path_(path), n0_(ntime) {
+    if (path_.empty()) return;
+    t0_ = t1_ = now();
+    std::FILE* f = std::fopen(path_.c_str(), ntime == 0 ? "w" : "a");
+    if (!f) die("cannot open the run-time log " + path_);
+    if (ntime == 0) std::fprintf(f, " # seis3d_wave run time log\n");
+    else std::fprintf(f, "\n # seis3d_wave restart from ntime= %d\n", ntime);
+    std::fprintf(f, "\n the program begins from %s\n\n each step uses time\n", stamp().c_str());
+    std::fclose(f);
+  }
+  void steps(int from, int to, int total) {
+    if (path_.empty() || to <= from) return;
+    const double t2 = now(), per = (t2 - t1_) / double(to - from);
+    std::FILE* f = std::fopen(path_.c_str(), "a");
+    if (!f) return;
+    for (int n = from + 1; n <= to; ++n) {
+      const double passed = (t1_ + per * (n - from) - t0_) / 3600.0;
+      const double left = passed / double(n - n0_) * double(total - n0_) - passed;
+      std::fprintf(f, "%6d step uses%12.5G s,  %12.5G hours passed and%12.5G hours left\n", n, per, passed, left);
+    }
+    std::fclose(f);
+    t1_ = t2;
+  }
+  void end() {
+    if (path_.empty()) return;
+    const double sec = now() - t0_;
+    const int d = int(sec / 86400.0), h = int((sec - d * 86400.0) / 3600.0), m = int((sec - d * 86400.0 - h * 3600.0) / 60.0);
+    std::FILE* f = std::fopen(path_.c_str(), "a");
+    if (!f) return;
+    std::fprintf(f, " ------------------------------------\n the program\n   finish at %s\n the total run time is\n"
+                 "%10d       day%10d      hour%10d    minute\n", stamp().c_str(), d, h, m);
+    std::fclose(f);
+  }
+
+ private:
+  static double now() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+  }
+  static std::string stamp() {
+    const std::time_t t = std::time(nullptr);
+    char b[64];
+    std::strftime(b, sizeof(b), "%Y%m%d,%H/%M/%S", std::localtime(&t));
+    return b;
+  }
+  std::string path_;
+  int n0_ = 0;
+  double t0_ = 0.0, t1_ = 0.0;
+};
+
 int main(int argc, char** argv) {
   if (argc >= 2 && std::strncmp(argv[1], "--nc-", 5) == 0) return nc_tool(argc, argv);
   std::string conf_path = "SeisFD3D.conf";
@@ -219,6 +296,11 @@ int main(int argc, char** argv) {
   if (cf.has("CHECKPOINT_ROOT")) ckpt_root = need_s("CHECKPOINT_ROOT");
   if (cf.has("checkpoint_tinv")) ckpt_tinv = need_i("checkpoint_tinv", 2);
   if (cf.has("run_from_checkpoint")) from_ckpt = need_i("run_from_checkpoint", 2);
+  // io_init (code/srcF/mod_io.F90:98-106): the urgent-checkpoint control file and the
+  // per-step run-time log, both optional here
+  std::string urgent_path, log_path;
+  if (cf.has("urgent_checkpoint")) urgent_path = need_s("urgent_checkpoint");
+  if (cf.has("fnm_log")) log_path = need_s("fnm_log");
   // abs_init keys (code/srcF/mod_abs_npml.F90:157-178), columns x1 x2 y1 y2 z1 z2
   int pml_n[6];
   float pml_v[6], pml_b[6], pml_a[6];
@@ -328,12 +410,19 @@ int main(int argc, char** argv) {
   }
   std::string prev_ckpt;
   const float fstept = float(stept);
-  while (ntime < total) {
-    // next step at which something is written
-    int next = total;
+  StepLog steplog(log_path, ntime);
+  int nt_dyn_rest = 0, nt_dyn_sync = 0;
+  int total_now = total;
+  while (ntime < total_now) {
+    // next step at which something is written or read
+    int next = total_now;
     for (const Snap& sp : snaps) next = std::min(next, (ntime / sp.tinv + 1) * sp.tinv);
     if (ckpt_tinv > 0) next = std::min(next, (ntime / ckpt_tinv + 1) * ckpt_tinv);
+    if (!urgent_path.empty()) next = std::min(next, (ntime / 10 + 1) * 10);
+    if (nt_dyn_rest > ntime) next = std::min(next, nt_dyn_rest);
+    if (nt_dyn_sync > ntime) next = std::min(next, nt_dyn_sync);
     check(fwant_run(s, next - ntime), s, "run");
+    steplog.steps(ntime, next, total_now);
     ntime = next;
     for (Snap& sp : snaps) {
       if (ntime % sp.tinv != 0) continue;
@@ -358,7 +447,25 @@ int main(int argc, char** argv) {
         sp.vbuf.clear(); sp.tbuf.clear(); sp.times.clear();
       }
     }
-    if (ckpt_tinv > 0 && ntime % ckpt_tinv == 0 && ntime < total) {
+    // the urgent-checkpoint file, re-read every 10 steps (io_rest_export :350-362): a
+    // checkpoint step, a sync step and a new nt (taken when it lies ahead)
+    if (!urgent_path.empty() && ntime % 10 == 0) {
+      std::ifstream uf(urgent_path);
+      int r = 0, y = 0, nw = 0;
+      if (!uf || !(uf >> r >> y >> nw)) die("io_rest_export: error when open " + urgent_path);
+      nt_dyn_rest = r;
+      nt_dyn_sync = y;
+      if (nw > ntime) {
+        std::printf("reset nt to %d step\n", nw);
+        total_now = fwant_reference_steps(nw);
+      }
+    }
+    const bool rest_now = (ckpt_tinv > 0 && ntime % ckpt_tinv == 0) || ntime == nt_dyn_rest;
+    if ((rest_now || ntime == nt_dyn_sync) && ntime < total_now && num_pt > 0) {
+      // nf90_sync: the seismograms so far are on disk
+      write_seismo(out_root, s, ntime, pt_tinv, num_pt, fstept);
+    }
+    if (rest_now && ntime < total_now) {
       // partly filled snapshot groups go to their files so that a resume can read them back
       for (Snap& sp : snaps) {
         if (sp.vel) write_snap_file(out_root, sp, true, fstept, ntime);
@@ -374,22 +481,8 @@ int main(int argc, char** argv) {
     if (sp.vel) write_snap_file(out_root, sp, true, fstept, ntime);
     if (sp.sgt) write_snap_file(out_root, sp, false, fstept, ntime);
   }
-  // seismograms: dims num_pt, time(unlimited); time(time); components (time, num_pt)
-  if (num_pt > 0) {
-    int nsamp = ntime / pt_tinv;
-    std::vector<float> seis(size_t(9) * nsamp * num_pt);
-    check(fwant_get_seismo(s, seis.data(), nsamp, &nsamp), s, "seismograms");
-    nc3::Writer w;
-    const int P = w.add_dim("num_pt", num_pt), T = w.add_dim("time", 0);
-    w.set_numrecs(nsamp);
-    w.add_gatt_text("title", "seismograms");
-    std::vector<double> t(nsamp);
-    for (int m = 0; m < nsamp; ++m) t[m] = double(float((m + 1) * pt_tinv) * fstept);  // t = ntime*stept
-    w.add_var("time", nc3::NC_FLOAT, {T}, t);
-    for (int c = 0; c < 9; ++c)
-      w.add_var_f(COMP[c], {T, P}, seis.data() + size_t(c) * nsamp * num_pt, size_t(nsamp) * num_pt);
-    if (!w.write(out_root + "/seismo_" + SUFFIX + ".nc", &err)) die(err);
-  }
+  if (num_pt > 0) write_seismo(out_root, s, ntime, pt_tinv, num_pt, fstept);
+  steplog.end();
   double ms = 0.0;
   fwant_last_run_ms(s, &ms);
   std::printf("fwant_wave: %d steps of %dx%dx%d, %d receivers, %zu snapshot series\n", ntime, ni, nj, nk, num_pt,

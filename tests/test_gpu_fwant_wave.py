@@ -144,3 +144,43 @@ def test_resume_writes_the_uninterrupted_files(native_lib, tmp_path):
         for k in a:
             np.testing.assert_array_equal(a[k], b[k], err_msg=f"{f}:{k}")
     shutil.rmtree(str(tmp_path), ignore_errors=True)
+
+
+def test_urgent_checkpoint_file_and_step_log(native_lib, tmp_path):
+    """The urgent-checkpoint control file (re-read every 10 steps: checkpoint step, sync
+    step, new nt) and the per-step run-time log (fnm_log).  A run configured for nt = 30
+    whose control file asks for nt = 44 and a checkpoint at step 20 runs 48 steps (whole
+    8-step blocks past nt = 44), writes that checkpoint, and its seismograms equal a run
+    configured for nt = 44 from the start; a missing control file stops the run."""
+    base = os.path.join(str(tmp_path), "base")
+    dyn = os.path.join(str(tmp_path), "dyn")
+    os.makedirs(base)
+    os.makedirs(dyn)
+    from fwant_gb300 import inputs
+    m = small_model("surface")
+    _, conf_b, roots_b = _prepare(base)
+    inputs.write_conf(conf_b, m, 44, roots_b, snaps=SNAPS)
+    _run(conf_b)
+    _, conf_d, roots_d = _prepare(dyn)
+    urgent = os.path.join(dyn, "urgent.txt")
+    log = os.path.join(dyn, "run.log")
+    with open(urgent, "w") as f:
+        f.write("20 0 44\n")
+    with open(conf_d, "a") as f:
+        f.write(f"urgent_checkpoint = {urgent}\nfnm_log = {log}\n")
+    r = _run(conf_d)
+    assert "reset nt to 44" in r.stdout
+    assert sorted(os.listdir(roots_d["CHECKPOINT_ROOT"])) == ["rest_t00020_mpi000000.ckpt"]
+    a, _ = _read(os.path.join(roots_b["OUTPUT_ROOT"], "seismo_mpi000000.nc"))
+    b, _ = _read(os.path.join(roots_d["OUTPUT_ROOT"], "seismo_mpi000000.nc"))
+    assert a["Vz"].shape[0] == b["Vz"].shape[0] == 48
+    for k in a:
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    lines = open(log).read().splitlines()
+    steps = [ln for ln in lines if "step uses" in ln and ln.split()[0].isdigit()]
+    assert len(steps) == 48 and steps[-1].split()[0] == "48"
+    assert lines[0].strip() == "# seis3d_wave run time log" and "the total run time is" in open(log).read()
+    os.remove(urgent)
+    r = subprocess.run([EXE, conf_d], capture_output=True, text=True)
+    assert r.returncode != 0 and "urgent" in r.stderr
+    shutil.rmtree(str(tmp_path), ignore_errors=True)
