@@ -82,6 +82,7 @@ EXPORTS = [
     ("fwant_set_planes_per_cta", C.c_int, [_vp, C.c_int]),
     ("fwant_get_planes_per_cta", C.c_int, [_vp, _ip]),
     ("fwant_set_lean_stages", C.c_int, [_vp, C.c_int]),
+    ("fwant_check_wait_timeout", C.c_int, [_vp, C.c_int]),
     ("fwant_get_lean_stages", C.c_int, [_vp, _ip]),
     ("fwant_batch_create", C.c_int, [C.POINTER(_vp), C.c_int, C.POINTER(_vp)]),
     ("fwant_batch_destroy", None, [_vp]),
@@ -401,6 +402,10 @@ class Solver:
     @planes_per_cta.setter
     def planes_per_cta(self, planes):
         self._chk(self._lib.fwant_set_planes_per_cta(self._h, int(planes)))
+
+    def check_wait_timeout(self, spins=1000):
+        """Run the bounded-wait deadline check; raises FwantError (TIMEOUT) as designed."""
+        self._chk(self._lib.fwant_check_wait_timeout(self._h, int(spins)))
 
     @property
     def lean_stages(self):

@@ -251,6 +251,10 @@ void launch_count_nonpositive(long long n, const float* v, unsigned int* count, 
 void launch_convert_to_f32(const Geom& g, const void* src, int storage, float inv_scale, float* dst, void* stream);
 void launch_convert_from_f32(const Geom& g, const float* src, int storage, float scale, void* dst, void* stream);
 
+// a bounded wait on a barrier nothing completes: after `spins` polls it writes
+// DEVERR_TMA_TIMEOUT to *err (the stage kernel's expired-wait path)
+void launch_wait_timeout_probe(int spins, int* err, void* stream);
+
 // device error codes written to StageArgs::err
 enum { DEVERR_NONE = 0, DEVERR_TMA_TIMEOUT = 1 };
 

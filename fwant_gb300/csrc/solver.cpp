@@ -1609,6 +1609,16 @@ fwant_status fwant_get_planes_per_cta(fwant_solver* s, int* planes) {
   return FWANT_OK;
 }
 
+fwant_status fwant_check_wait_timeout(fwant_solver* s, int spins) {
+  if (!s || spins < 1 || spins > (1 << 20)) return FWANT_ERR_INVALID_ARG;
+  cudaSetDevice(s->cfg.device);
+  fw::launch_wait_timeout_probe(spins, s->d_err, s->st);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+  if (e != cudaSuccess) return s->cuda_fail(e, "wait timeout check");
+  return s->check_device_error();
+}
+
 fwant_status fwant_set_lean_stages(fwant_solver* s, int mask) {
   if (!s || (mask & ~5) != 0) return FWANT_ERR_INVALID_ARG;
   s->lean_mask = mask;

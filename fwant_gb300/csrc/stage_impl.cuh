@@ -114,8 +114,8 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
   return ok != 0;
 }
 // Bounded wait: false after WAIT_SPINS unsuccessful polls.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (int n = 0; n < WAIT_SPINS; ++n)
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int spins = WAIT_SPINS) {
+  for (int n = 0; n < spins; ++n)
     if (mbar_try(bar, parity)) return true;
   return false;
 }

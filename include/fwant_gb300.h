@@ -319,6 +319,11 @@ fwant_status fwant_get_planes_per_cta(fwant_solver* s, int* planes);
  * No counterpart in the reference (a tuning knob of the stage kernel, set by
  * fwant_batch_autotune). */
 fwant_status fwant_set_lean_stages(fwant_solver* s, int mask);
+/* Deadline check of the stage kernel's bounded waits, without a fault: a one-thread kernel
+ * waits on a barrier phase that nothing completes, gives up after `spins` polls (1 ..
+ * 2^20) and reports through the solver's device error word, so the call returns
+ * FWANT_ERR_TIMEOUT and the solver stays usable.  No counterpart in the reference. */
+fwant_status fwant_check_wait_timeout(fwant_solver* s, int spins);
 fwant_status fwant_get_lean_stages(fwant_solver* s, int* mask);
 
 /* Autotuner: times every planes-per-CTA candidate (4 ... 128, up to nk) over trial_steps

@@ -151,6 +151,22 @@ def test_overflow_check_reports_nan(native_lib):
     assert e.value.code == 4
 
 
+def test_wait_deadline_reports_timeout(native_lib):
+    """A bounded wait that runs out (a barrier phase nothing completes, 1000 polls) is
+    reported as FWANT_ERR_TIMEOUT through the solver's device error word, and the solver
+    then steps normally: the deadline path of the stage kernel, exercised without a fault."""
+    import fwant_gb300 as fw
+    from fwant_gb300 import inputs
+    m = small_model("surface")
+    s = inputs.attach(fw.Solver(m.ni, m.nj, m.nk, m.stept), m)
+    with pytest.raises(fw.FwantError) as e:
+        s.check_wait_timeout(1000)
+    assert e.value.code == 5
+    s.run(8)
+    s.check()
+    assert np.any(s.get_field("Vz"))
+
+
 def test_set_media_rejects_nonpositive_rho(native_lib):
     """rho must be > 0 at every point, ghosts included (the solver divides by it); a zero
     or NaN anywhere is refused with INVALID_ARG before the medium on the device changes,
