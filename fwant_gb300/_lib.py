@@ -43,6 +43,7 @@ EXPORTS = [
     ("fwant_set_metric", C.c_int, [_vp, _fp, _fp, _fp, _fp, _fp]),
     ("fwant_compute_metric", C.c_int, [_vp]),
     ("fwant_get_metric", C.c_int, [_vp, _fp, _fp, _fp, _fp, _fp]),
+    ("fwant_metric_arrays", C.c_int, [C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, C.c_int, _fp, _fp, _fp, _fp, _fp]),
     ("fwant_set_media", C.c_int, [_vp, _fp, _fp, _fp]),
     ("fwant_set_pml", C.c_int, [_vp, _ip, _fp, _fp, _fp]),
     ("fwant_set_forces", C.c_int, [_vp, C.c_int, C.c_int, _ip, _fp, _fp, _fp, _fp, _fp, _fp, _fp, C.c_int]),
@@ -733,6 +734,20 @@ class Media:
         p = [C.c_void_p() for _ in range(3)]
         self._chk(self._lib.fwant_media_device_arrays(self._h, *[C.byref(q) for q in p]))
         solver._chk(self._lib.fwant_set_media_device(solver._h, *p))
+
+
+def metric(x, y, z, device: int = 0) -> dict:
+    """The metric of a grid without a solver (fwant_metric_arrays: seis3d_metric in FP64
+    on the device, rounded to FP32): x, y, z with their ghosts in, the arrays of
+    metric_mpi*.nc out."""
+    x, y, z = (np.ascontiguousarray(np.asarray(a, np.float32)) for a in (x, y, z))
+    out = [np.zeros(x.size, np.float32), np.zeros(x.size, np.float32), np.zeros(x.size, np.float32),
+           np.zeros(y.size, np.float32), np.zeros(z.size, np.float32)]
+    code = load_library().fwant_metric_arrays(x.size - 6, y.size - 6, z.size - 6, _ptr(x), _ptr(y), _ptr(z),
+                                              int(device), *[_ptr(v) for v in out])
+    if code != 0:
+        raise FwantError(code, "fwant_metric_arrays failed")
+    return dict(zip(("xsin", "xcot", "xi_x", "eta_y", "zeta_z"), out))
 
 
 def reference_steps(nt: int) -> int:

@@ -44,6 +44,8 @@ LSQR_EXE = os.path.join(HERE, "bin", "fwant_lsqr")
 LSQR_SOURCES = ["fwant_lsqr.cpp"]
 MEDIA_EXE = os.path.join(HERE, "bin", "fwant_media")
 MEDIA_SOURCES = ["fwant_media.cpp", "netcdf3.cpp", "conf.cpp"]
+PREP_EXE = os.path.join(HERE, "bin", "fwant_prep")
+PREP_SOURCES = ["fwant_prep.cpp", "netcdf3.cpp", "conf.cpp"]
 
 
 def _nvcc() -> str:
@@ -100,10 +102,12 @@ def build(verbose: bool = False, force: bool = False, jobs: int | None = None) -
         _run([nvcc, "-shared", *ARCH, "-o", LIB, *objs, "-lcudart"], verbose)
     # the programs over the C ABI: the solver stage (SeisFD3D.conf + NetCDF files in and
     # out), the sensitivity-kernel stage (TomoKernel.conf, sgt_ files in, kernel files out)
-    # the inversion (data list, kernel rows, smoothing operator in; model files out) and
-    # the medium preprocessor (media configuration and model files in; media file out)
+    # the inversion (data list, kernel rows, smoothing operator in; model files out), the
+    # medium preprocessor (media configuration and model files in; media file out) and the
+    # grid, metric, source and station preprocessors (configuration in; coord_, metric_,
+    # source_ and station_ files out)
     for exe, srcs in ((EXE, EXE_SOURCES), (KER_EXE, KER_SOURCES), (LSQR_EXE, LSQR_SOURCES),
-                      (MEDIA_EXE, MEDIA_SOURCES)):
+                      (MEDIA_EXE, MEDIA_SOURCES), (PREP_EXE, PREP_SOURCES)):
         exe_src = [os.path.join(CSRC, f) for f in srcs]
         if force or _stale(exe, exe_src + hdrs + [LIB]):
             os.makedirs(os.path.dirname(exe), exist_ok=True)

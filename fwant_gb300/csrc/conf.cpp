@@ -4,6 +4,7 @@
 #include <cstdlib>
 #include <fstream>
 #include <sstream>
+#include <stdexcept>
 
 namespace conf {
 
@@ -62,6 +63,92 @@ bool File::get_double(const std::string& key, int gcol, double* out) const {
   if (end == s.c_str() || *end != '\0') return false;
   *out = v;
   return true;
+}
+
+namespace {
+std::string fortran_exponent(std::string s) {
+  for (char& c : s)
+    if (c == 'd' || c == 'D') c = 'e';
+  return s;
+}
+}  // namespace
+
+float to_float(const std::string& word, const std::string& where) {
+  const std::string s = fortran_exponent(word);
+  char* end = nullptr;
+  const float f = std::strtof(s.c_str(), &end);
+  if (end == s.c_str() || *end != '\0') throw std::runtime_error(where + ": not a number: " + word);
+  return f;
+}
+
+double to_double(const std::string& word, const std::string& where) {
+  const std::string s = fortran_exponent(word);
+  char* end = nullptr;
+  const double d = std::strtod(s.c_str(), &end);
+  if (end == s.c_str() || *end != '\0') throw std::runtime_error(where + ": not a number: " + word);
+  return d;
+}
+
+Text::Text(const std::string& path) : path_(path) {
+  std::string err;
+  if (!cf_.load(path, &err)) throw std::runtime_error(err);
+  std::ifstream in(path);
+  for (std::string l; std::getline(in, l);) raw_.push_back(l);
+}
+
+int Text::get_int(const std::string& key, int col) const {
+  int v;
+  if (!cf_.get_int(key, col, &v)) throw std::runtime_error(path_ + ": key " + key + " missing");
+  return v;
+}
+
+double Text::get_double(const std::string& key, int col) const {
+  double v;
+  if (!cf_.get_double(key, col, &v)) throw std::runtime_error(path_ + ": key " + key + " missing");
+  return v;
+}
+
+std::string Text::get(const std::string& key, int col) const {
+  std::string v;
+  if (!cf_.get(key, col, &v)) throw std::runtime_error(path_ + ": key " + key + " missing");
+  return v;
+}
+
+void Text::seek(const std::string& anchor) {
+  for (size_t q = 0; q < raw_.size(); ++q) {
+    std::string l = raw_[q];
+    const size_t h = l.find('#');
+    if (h != std::string::npos) l.resize(h);
+    for (char& c : l)
+      if (c == '=' || c == '\t' || c == '|' || c == '\r') c = ' ';
+    std::istringstream w(l);
+    std::string first;
+    if (w >> first && first == anchor) {
+      line_ = q + 1;
+      return;
+    }
+  }
+  throw std::runtime_error(path_ + ": no " + anchor + " line");
+}
+
+std::vector<std::string> Text::words(size_t n) {
+  std::vector<std::string> v;
+  while (v.size() < n) {
+    if (line_ >= raw_.size()) throw std::runtime_error(path_ + ": file ends inside a record");
+    std::string l = raw_[line_++];
+    for (char& c : l)
+      if (c == ',' || c == '\t' || c == '\r') c = ' ';
+    std::istringstream w(l);
+    for (std::string t; v.size() < n && w >> t;) v.push_back(t);
+  }
+  return v;
+}
+
+std::vector<float> Text::record(size_t n) {
+  std::vector<float> v;
+  v.reserve(n);
+  for (const std::string& t : words(n)) v.push_back(to_float(t, path_));
+  return v;
 }
 
 }  // namespace conf

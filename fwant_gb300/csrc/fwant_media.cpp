@@ -43,74 +43,8 @@ void check(fwant_status rc, fwant_media* m, const char* what) {
   if (rc != FWANT_OK) die(std::string(what) + ": " + (m ? fwant_media_last_error(m) : "failed"));
 }
 
-// An ascii model file: keys through string_conf semantics, and the numbers after an anchor
-// line read record by record as Fortran list-directed reads do (a record takes as many
-// lines as its values need; the rest of its last line is skipped).
-class TextModel {
- public:
-  explicit TextModel(const std::string& path) : path_(path) {
-    std::string err;
-    if (!cf_.load(path, &err)) die(err);
-    std::ifstream in(path);
-    for (std::string l; std::getline(in, l);) raw_.push_back(l);
-  }
-  int get_int(const std::string& key, int col) const {
-    int v;
-    if (!cf_.get_int(key, col, &v)) die(path_ + ": key " + key + " missing");
-    return v;
-  }
-  double get_double(const std::string& key, int col) const {
-    double v;
-    if (!cf_.get_double(key, col, &v)) die(path_ + ": key " + key + " missing");
-    return v;
-  }
-  std::string get(const std::string& key, int col) const {
-    std::string v;
-    if (!cf_.get(key, col, &v)) die(path_ + ": key " + key + " missing");
-    return v;
-  }
-  // position after the first line whose first word is the anchor
-  void seek(const std::string& anchor) {
-    for (size_t q = 0; q < raw_.size(); ++q) {
-      std::string l = raw_[q];
-      const size_t h = l.find('#');
-      if (h != std::string::npos) l.resize(h);
-      for (char& c : l)
-        if (c == '=' || c == '\t' || c == '|' || c == '\r') c = ' ';
-      std::istringstream w(l);
-      std::string first;
-      if (w >> first && first == anchor) {
-        line_ = q + 1;
-        return;
-      }
-    }
-    die(path_ + ": no " + anchor + " line");
-  }
-  // one list-directed record of n single-precision values
-  std::vector<float> record(size_t n) {
-    std::vector<float> v;
-    while (v.size() < n) {
-      if (line_ >= raw_.size()) die(path_ + ": file ends inside a record");
-      std::string l = raw_[line_++];
-      for (char& c : l)
-        if (c == ',' || c == '\t' || c == '\r') c = ' ';
-      std::istringstream w(l);
-      for (std::string t; v.size() < n && w >> t;) {
-        char* end = nullptr;
-        const float f = std::strtof(t.c_str(), &end);
-        if (end == t.c_str() || *end != '\0') die(path_ + ": not a number: " + t);
-        v.push_back(f);
-      }
-    }
-    return v;
-  }
-
- private:
-  std::string path_;
-  conf::File cf_;
-  std::vector<std::string> raw_;
-  size_t line_ = 0;
-};
+// ascii model files: string_conf keys and list-directed records after anchor lines
+using TextModel = conf::Text;
 
 // real(SP) array times a real(DP) factor, stored back in SP (L%Vp = L%Vp * v2ms)
 void scale(std::vector<float>& a, double f) {
@@ -357,7 +291,7 @@ void read_model(fwant_media* m, const std::string& type, const std::string& form
 
 }  // namespace
 
-int main(int argc, char** argv) {
+static int run(int argc, char** argv) {
   std::string conf_path = "SeisFD3D.conf";
   int device = 0;
   for (int a = 1; a < argc; ++a) {
@@ -455,4 +389,12 @@ int main(int argc, char** argv) {
   std::printf("effective media on the GPU: %.3f ms\n", ms);
   fwant_media_destroy(m);
   return 0;
+}
+
+int main(int argc, char** argv) {
+  try {
+    return run(argc, argv);
+  } catch (const std::exception& e) {
+    die(e.what());
+  }
 }

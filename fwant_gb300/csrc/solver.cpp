@@ -996,6 +996,41 @@ fwant_status fwant_compute_metric(fwant_solver* s) {
   return FWANT_OK;
 }
 
+fwant_status fwant_metric_arrays(int ni, int nj, int nk, const float* x, const float* y, const float* z, int device,
+                                 float* xsin, float* xcot, float* xi_x, float* eta_y, float* zeta_z) {
+  if (ni < 2 || nj < 2 || nk < 2 || !x || !y || !z || !xsin || !xcot || !xi_x || !eta_y || !zeta_z)
+    return FWANT_ERR_INVALID_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return FWANT_ERR_CUDA;
+  const int nx = ni + 6, ny = nj + 6, nz = nk + 6;
+  // one buffer: x, y, z, then xsin, xcot, xi_x, eta_y, zeta_z
+  const size_t n = size_t(3) * nx + 2 * size_t(ny) + 2 * size_t(nz) + 2 * size_t(nx);
+  float* d = nullptr;
+  cudaStream_t st = nullptr;
+  cudaError_t e = cudaMalloc(&d, n * sizeof(float));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  float *dx = d, *dy = dx + nx, *dz = dy + ny, *dsin = dz + nz, *dcot = dsin + nx, *dxi = dcot + nx,
+        *deta = dxi + nx, *dzeta = deta + ny;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x, nx * sizeof(float), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dy, y, ny * sizeof(float), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dz, z, nz * sizeof(float), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    fw::launch_sincot_fp64(nx, dx, dsin, dcot, st);
+    fw::launch_metric_fp64(nx, dx, dxi, 3, 3 + ni - 1, st);
+    fw::launch_metric_fp64(ny, dy, deta, 3, 3 + nj - 1, st);
+    fw::launch_metric_fp64(nz, dz, dzeta, 3, 3 + nk - 1, st);
+    e = cudaGetLastError();
+  }
+  const std::pair<float*, std::pair<const float*, int>> outs[] = {
+      {xsin, {dsin, nx}}, {xcot, {dcot, nx}}, {xi_x, {dxi, nx}}, {eta_y, {deta, ny}}, {zeta_z, {dzeta, nz}}};
+  for (const auto& o : outs)
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(o.first, o.second.first, o.second.second * sizeof(float), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (st) cudaStreamDestroy(st);
+  if (d) cudaFree(d);
+  return e == cudaSuccess ? FWANT_OK : FWANT_ERR_CUDA;
+}
+
 fwant_status fwant_get_metric(fwant_solver* s, float* xsin, float* xcot, float* xi_x, float* eta_y,
                               float* zeta_z) {
   if (!s || !xsin || !xcot || !xi_x || !eta_y || !zeta_z) return FWANT_ERR_INVALID_ARG;

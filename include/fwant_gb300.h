@@ -106,6 +106,14 @@ fwant_status fwant_set_metric(fwant_solver* s, const float* xsin, const float* x
  * replaces the seis3d_metric preprocessor (code/srcF/seis3d_metric.F90:83-112). */
 fwant_status fwant_compute_metric(fwant_solver* s);
 
+/* The metric of a grid without a solver: the seis3d_metric program
+ * (code/srcF/seis3d_metric.F90:83-112; the fwant_prep program's metric stage) on the device in
+ * FP64, rounded to FP32, the same values as fwant_compute_metric.  x[ni+6], y[nj+6], z[nk+6]
+ * include the ghosts; xsin, xcot, xi_x have ni+6 entries, eta_y nj+6, zeta_z nk+6. */
+fwant_status fwant_metric_arrays(int ni, int nj, int nk, const float* x, const float* y, const float* z,
+                                 int device, float* xsin, float* xcot, float* xi_x, float* eta_y,
+                                 float* zeta_z);
+
 /* Copy the metric currently in use back to the host (same shapes as fwant_set_metric). */
 fwant_status fwant_get_metric(fwant_solver* s, float* xsin, float* xcot, float* xi_x,
                               float* eta_y, float* zeta_z);
