@@ -172,3 +172,24 @@ def test_prep_rejects_bad_setups(grid_dir):
                   f"GRID_ROOT = {grid_dir}"])
     r = run("grid", path, ok=False)
     assert r.returncode != 0 and "dims must be 1 1 1" in r.stderr
+
+
+def test_angle2moment_known_answers(grid_dir):
+    """Aki & Richards' double couples: a vertical strike-slip fault striking north has only
+    M12 = M0 (Mxy = -M0 in theta, phi, r); a thrust on a 45-degree plane striking north has
+    M22 = -M0 and M33 = +M0.  Checked on the restatement and through the program's file."""
+    from oracle import prep_oracle as P
+    tiny = 1e-12
+    ss = P.angle2moment(0.0, 90.0, 0.0)
+    assert float(ss[3]) == -1.0 and all(abs(float(ss[c])) < tiny for c in (0, 1, 2, 4, 5))
+    th = P.angle2moment(0.0, 45.0, 90.0)
+    assert float(th[1]) == -1.0 and float(th[2]) == 1.0
+    assert all(abs(float(th[c])) < tiny for c in (0, 3, 4, 5))
+    x, y, z = _coords(grid_dir)
+    deg = lambda a: float(np.degrees(np.float64(a)))
+    mo = [(deg(x[8]), deg(y[8]), 6371000.0 - 2000.0, 0.0, 2.0, 0.0, 90.0, 0.0),
+          (deg(x[9]), deg(y[9]), 6371000.0 - 2000.0, 0.0, 3.0, 0.0, 45.0, 90.0)]
+    source_conf(grid_dir, 6370000.0, [], 0, mo, 1, "angle")
+    run("source", main_conf(grid_dir))
+    v, _, _ = read(os.path.join(grid_dir, "source_mpi000000.nc"))
+    assert v["Mxy"][0, 0] == -2.0 and v["Myy"][1, 0] == -3.0 and v["Mzz"][1, 0] == 3.0
