@@ -121,6 +121,15 @@ EXPORTS = [
     ("fwant_lsqr_info", C.c_int, [_vp, C.POINTER(C.c_double)]),
     ("fwant_lsqr_multiply", C.c_int, [_vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("fwant_lsqr_last_solve_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
+    # kernel assembly onto inversion blocks (include/fwant_assm.h)
+    ("fwant_assm_create", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _fp, C.POINTER(C.c_int),
+                                    C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_void_p)]),
+    ("fwant_assm_destroy", None, [_vp]),
+    ("fwant_assm_last_error", C.c_char_p, [_vp]),
+    ("fwant_assm_project", C.c_int, [_vp, C.c_int, C.POINTER(_fp), _fp]),
+    ("fwant_assm_project_device", C.c_int, [_vp, C.c_int, C.POINTER(C.c_void_p), _fp]),
+    ("fwant_assm_sums", C.c_int, [_vp, _fp]),
+    ("fwant_assm_last_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
     # medium preprocessor (include/fwant_media.h)
     ("fwant_media_create", C.c_int, [C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, C.c_float, C.POINTER(C.c_int), C.c_int,
                                      C.POINTER(C.c_void_p)]),
@@ -748,6 +757,72 @@ def metric(x, y, z, device: int = 0) -> dict:
     if code != 0:
         raise FwantError(code, "fwant_metric_arrays failed")
     return dict(zip(("xsin", "xcot", "xi_x", "eta_y", "zeta_z"), out))
+
+
+class Assm:
+    """Kernel assembly onto inversion blocks on the GPU (SI_ker2assm's projection): the
+    block file's volume (max_pix, num_blk), num_of_pix (num_blk) and indx_of_pix
+    (3, max_pix, num_blk) in Fortran index order over a kernel volume of shape (ki, kj, kk)."""
+
+    def __init__(self, shape, volume, num_of_pix, indx_of_pix, device=0):
+        self._lib = load_library()
+        ki, kj, kk = (int(v) for v in shape)
+        self.shape = (ki, kj, kk)
+        vol = np.asarray(volume, np.float32)
+        max_pix, num_blk = vol.shape
+        self.num_blk = num_blk
+        v = _fo(vol)
+        npx = np.ascontiguousarray(np.asarray(num_of_pix, np.int32).reshape(num_blk))
+        px = np.ascontiguousarray(np.asarray(indx_of_pix, np.int32).reshape(3, max_pix, num_blk).reshape(-1, order="F"))
+        h = C.c_void_p()
+        rc = self._lib.fwant_assm_create(ki, kj, kk, num_blk, max_pix, _ptr(v), _ptr(npx, C.c_int), _ptr(px, C.c_int),
+                                         int(device), C.byref(h))
+        if rc != 0:
+            msg = self._lib.fwant_assm_last_error(h).decode() if h.value else "fwant_assm_create failed"
+            if h.value:
+                self._lib.fwant_assm_destroy(h)
+            raise FwantError(rc, msg)
+        self._h = h
+
+    def _chk(self, rc):
+        if rc != 0:
+            raise FwantError(rc, self._lib.fwant_assm_last_error(self._h).decode())
+
+    def project(self, kernels):
+        """kernels: 1-4 arrays of shape (ki, kj, kk); returns B (nq, num_blk)."""
+        ks = [_fortran3(k, self.shape) for k in kernels]
+        arr = (_fp * len(ks))(*[_ptr(k) for k in ks])
+        out = np.zeros((len(ks), self.num_blk), np.float32)
+        self._chk(self._lib.fwant_assm_project(self._h, len(ks), arr, _ptr(out)))
+        return out
+
+    def project_device(self, pointers):
+        """Device addresses of 1-4 kernel volumes (Fortran order) on the handle's GPU."""
+        arr = (C.c_void_p * len(pointers))(*[int(p) for p in pointers])
+        out = np.zeros((len(pointers), self.num_blk), np.float32)
+        self._chk(self._lib.fwant_assm_project_device(self._h, len(pointers), arr, _ptr(out)))
+        return out
+
+    def sums(self):
+        out = np.zeros((4, self.num_blk), np.float32)
+        self._chk(self._lib.fwant_assm_sums(self._h, _ptr(out)))
+        return out
+
+    def last_ms(self):
+        ms = C.c_double()
+        self._chk(self._lib.fwant_assm_last_ms(self._h, C.byref(ms)))
+        return ms.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.fwant_assm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def reference_steps(nt: int) -> int:

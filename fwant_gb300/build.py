@@ -31,7 +31,7 @@ CPP_FLAGS = ["-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-con
 SOURCES = ["stage_fast_rk0.cu", "stage_fast_rk1.cu", "stage_fast_rk2.cu", "stage_exact_rk0.cu",
            "stage_exact_rk1.cu", "stage_exact_rk2.cu", "stage_bf16_rk0.cu", "stage_bf16_rk1.cu",
            "stage_bf16_rk2.cu", "stage_fp16_rk0.cu", "stage_fp16_rk1.cu", "stage_fp16_rk2.cu",
-           "stage_dispatch.cu", "waits.cu", "aux.cu", "snapshot.cu", "sgtker.cu", "surrogate.cu", "lsqr.cu", "media.cu", "solver.cpp", "sgtker_api.cpp"]
+           "stage_dispatch.cu", "waits.cu", "aux.cu", "snapshot.cu", "sgtker.cu", "surrogate.cu", "lsqr.cu", "media.cu", "assm.cu", "solver.cpp", "sgtker_api.cpp"]
 # units whose FP32 expressions must round like the reference's source (no contraction)
 EXACT_SOURCES = {"media.cu"}
 
@@ -46,6 +46,8 @@ MEDIA_EXE = os.path.join(HERE, "bin", "fwant_media")
 MEDIA_SOURCES = ["fwant_media.cpp", "netcdf3.cpp", "conf.cpp"]
 PREP_EXE = os.path.join(HERE, "bin", "fwant_prep")
 PREP_SOURCES = ["fwant_prep.cpp", "netcdf3.cpp", "conf.cpp"]
+ASSM_EXE = os.path.join(HERE, "bin", "fwant_assm")
+ASSM_SOURCES = ["fwant_assm.cpp", "netcdf3.cpp", "conf.cpp"]
 
 
 def _nvcc() -> str:
@@ -105,9 +107,10 @@ def build(verbose: bool = False, force: bool = False, jobs: int | None = None) -
     # the inversion (data list, kernel rows, smoothing operator in; model files out), the
     # medium preprocessor (media configuration and model files in; media file out) and the
     # grid, metric, source and station preprocessors (configuration in; coord_, metric_,
-    # source_ and station_ files out)
+    # source_ and station_ files out) and the kernel assembly (kernel files and inversion
+    # blocks in; compact kernel rows out)
     for exe, srcs in ((EXE, EXE_SOURCES), (KER_EXE, KER_SOURCES), (LSQR_EXE, LSQR_SOURCES),
-                      (MEDIA_EXE, MEDIA_SOURCES), (PREP_EXE, PREP_SOURCES)):
+                      (MEDIA_EXE, MEDIA_SOURCES), (PREP_EXE, PREP_SOURCES), (ASSM_EXE, ASSM_SOURCES)):
         exe_src = [os.path.join(CSRC, f) for f in srcs]
         if force or _stale(exe, exe_src + hdrs + [LIB]):
             os.makedirs(os.path.dirname(exe), exist_ok=True)
