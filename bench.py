@@ -57,12 +57,15 @@ def parse_args():
     p.add_argument("--steps", type=int, default=32)
     p.add_argument("--warmup", type=int, default=8)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--config", choices=["c2", "c1", "c3", "c5", "lsqr", "media", "ker"], default="c2",
+    p.add_argument("--config", choices=["c2", "c1", "c3", "c5", "lsqr", "media", "ker", "assm"], default="c2",
                    help="c5: train the waveform surrogate on 512 FD solves and screen 64 held-out models; "
                         "lsqr: LSQR iterations of the damped, smoothed inversion (inv.LSQR) on a synthetic system; "
                         "media: the effective-medium preprocessor (seis3d_media) on the C2 grid; "
-                        "ker: the sensitivity-kernel accumulation (SI_ker_sta sgt2scatter3) of one SGT block")
+                        "ker: the sensitivity-kernel accumulation (SI_ker_sta sgt2scatter3) of one SGT block; "
+                        "assm: the kernel assembly onto inversion blocks (SI_ker2assm) of two kernel volumes")
     p.add_argument("--ker-points", type=int, default=16384, help="kernel points of the --config ker block")
+    p.add_argument("--assm-shuffle", action="store_true",
+                   help="--config assm: list each block's pixels in a random order instead of i fastest")
     p.add_argument("--lsqr-scale", type=float, default=1.0,
                    help="fraction of the LSQR system's measurements and blocks (profiling)")
     p.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU baseline sample")
@@ -323,6 +326,8 @@ def run_reference(args, rank, world):
         return run_reference_lsqr(args)
     if args.config == "ker":
         return run_reference_ker(args)
+    if args.config == "assm":
+        return run_reference_assm(args)
     models, desc = make_models(args.config, seed=0, grid=args.grid, sims=args.sims)
     from fwant_gb300 import inputs
     from oracle import oracle as O
@@ -553,6 +558,108 @@ def run_media(args, rank):
     return 0
 
 
+def assm_workload(grid=None, brick=4, seed=0, shuffle=False):
+    """Inversion blocks of brick^3 kernel points tiling a kernel volume of the C2 grid's size,
+    random cell volumes, and two kernel volumes (phase Vp and Vs) in Fortran order.  Each
+    block lists its pixels i fastest, the order a generator looping over k, j, i writes
+    (shuffle: one random order, the worst case for cache reuse)."""
+    ki, kj, kk = (int(v) for v in (grid or "400x400x200").lower().split("x"))
+    if ki % brick or kj % brick or kk % brick:
+        raise SystemExit(f"the kernel volume must be a multiple of {brick} in every direction")
+    rng = np.random.default_rng(seed)
+    nb = (ki // brick, kj // brick, kk // brick)
+    nblk, max_pix = nb[0] * nb[1] * nb[2], brick ** 3
+    order = rng.permutation(max_pix) if shuffle else np.arange(max_pix)
+    loc = np.array(np.unravel_index(order, (brick,) * 3, order="F"), np.int32)
+    bidx = np.array(np.unravel_index(np.arange(nblk), nb, order="F"), np.int32)
+    pixs = np.empty((3, max_pix, nblk), np.int32)
+    for d in range(3):
+        pixs[d] = loc[d][:, None] + brick * bidx[d][None, :] + 1
+    npix = np.full(nblk, max_pix, np.int32)
+    volume = (rng.uniform(0.5, 2.0, (max_pix, nblk)) * 1.0e6).astype(np.float32)
+    kernels = [np.asfortranarray(rng.standard_normal((ki, kj, kk), np.float32) * np.float32(1e-10)) for _ in range(2)]
+    desc = (f"projection of two {ki}x{kj}x{kk} kernel volumes (phase Vp, Vs) onto {nblk} inversion blocks of "
+            f"{brick}x{brick}x{brick} points (pixels {'in a shuffled order' if shuffle else 'i fastest'})")
+    return (ki, kj, kk), volume, npix, pixs, kernels, desc
+
+
+# Algorithmic DRAM bytes of one projection: per pixel its offset and volume (8 B) and the
+# kernel values (4 B per volume); per block its pixel count, B written and S read and written
+def assm_bytes(nvol, nblk, nq):
+    return nvol * (8 + 4 * nq) + nblk * (4 + 12 * nq)
+
+
+def run_assm(args, rank):
+    """The kernel assembly (fwant_assm_*): K projections of two kernel volumes on the device
+    (kernel time from CUDA events around the projection launch), the restatement's projection
+    on the host, and the end-to-end call with host kernels (upload, projection, blocks back)."""
+    import fwant_gb300 as fw
+    if rank != 0:
+        return 0
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    shape, volume, npix, pixs, ks, desc = assm_workload(args.grid, shuffle=args.assm_shuffle)
+    nvol, nblk = int(np.prod(shape)), volume.shape[1]
+    A = fw.Assm(shape, volume, npix, pixs, device=dev)
+    warm = max(args.warmup, 3)
+    for _ in range(warm):
+        A.project(ks)
+    clocks = Clocks(dev)
+    clocks.start()
+    ms, walls = [], []
+    for _ in range(args.steps):
+        t1 = time.perf_counter()
+        B = A.project(ks)
+        walls.append(time.perf_counter() - t1)
+        ms.append(A.last_ms())
+    clk = clocks.stop()
+    dev_ms = float(np.sum(ms))
+    value = 2 * nvol * args.steps / (dev_ms * 1e-3) / 1e9
+    achieved = assm_bytes(nvol, nblk, 2) * args.steps / (dev_ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    out = {
+        "metric": "kernel points assembled per second", "value": value, "unit": "GPts/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": warm, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+        "scaling": "replicas only", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": desc, "l2": f"kernels and pixel lists ({(8 + 8) * nvol / 1e6:.0f} MB) larger than L2 "
+                                            f"(no flush)", "step": "one pick: both volumes onto every block"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_launch": assm_bytes(nvol, nblk, 2)},
+        "clocks": clk, "gpu_launches": args.steps,
+        "e2e": {"value": 2 * nvol * args.steps / float(np.sum(walls)) / 1e9, "unit": "GPts/s",
+                "h2d_bytes_per_step": 2 * 4 * nvol, "d2h_bytes_per_step": 2 * 4 * nblk,
+                "includes": "kernel upload from host arrays, projection, block values read back"},
+    }
+    if not args.no_cpu_baseline:
+        from oracle import assm_oracle as AO
+        t1 = time.perf_counter()
+        want = AO.project(ks[0], volume, npix, pixs)
+        dt = time.perf_counter() - t1
+        out["config"]["matches_restatement"] = bool(np.array_equal(B[0], want))
+        out["cpu_baseline"] = {"value": nvol / dt / 1e9, "unit": "GPts/s", "cores": 1, "kind": "port",
+                               "sample": f"one volume's projection by the numpy restatement, {dt:.1f} s"}
+    A.close()
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def run_reference_assm(args):
+    """the restatement's projection (numpy, one thread), each step one kernel volume"""
+    from oracle import assm_oracle as AO
+    shape, volume, npix, pixs, ks, desc = assm_workload(args.grid, shuffle=args.assm_shuffle)
+    nvol = int(np.prod(shape))
+    steps = max(1, min(args.steps, 4))
+    for _ in range(1):
+        AO.project(ks[0], volume, npix, pixs)
+    t0 = time.perf_counter()
+    for s in range(steps):
+        AO.project(ks[s % 2], volume, npix, pixs)
+    dt = time.perf_counter() - t0
+    sample = f"{steps} single-volume projections of the restatement (numpy, 1 thread)"
+    return _reference_line(args, "kernel points assembled per second", "GPts/s", nvol * steps / dt / 1e9, dt, desc,
+                           sample, 1, "f32")
+
+
 # GB300's FP64 FMA rate: no measured figure is available to the benchmark, so the nominal
 # dense FP64 rate stands as the denominator of the kernel-accumulation roofline
 FP64_NOMINAL_TFLOPS = 1.25
@@ -675,6 +782,8 @@ def run_ours(args, rank, world):
         return run_media(args, rank)
     if args.config == "ker":
         return run_ker(args, rank)
+    if args.config == "assm":
+        return run_assm(args, rank)
     dist = Dist(world)
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     fw.load_library()

@@ -38,11 +38,14 @@ __global__ void __launch_bounds__(AS_THREADS) project_kernel(int nblk, const int
 #pragma unroll
   for (int q = 0; q < NQ; ++q) b[q] = 0.0f;
   const int np = npix[n];
+  const int* lp = lin + n;
+  const float* vp = vol + n;
 #pragma unroll 4
   for (int m = 0; m < np; ++m) {
-    const size_t o = size_t(m) * size_t(nblk) + size_t(n);
-    const int idx = lin[o];
-    const float v = vol[o];
+    const int idx = __ldg(lp);
+    const float v = __ldg(vp);
+    lp += nblk;
+    vp += nblk;
 #pragma unroll
     for (int q = 0; q < NQ; ++q) b[q] = __fadd_rn(b[q], __fmul_rn(__ldg(K.p[q] + idx), v));
   }
