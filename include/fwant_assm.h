@@ -38,8 +38,9 @@ const char* fwant_assm_last_error(fwant_assm* a);
  * (num_blk, nq) receives B for each volume, and |B| is added to the sums of slots 0..nq-1. */
 fwant_status fwant_assm_project(fwant_assm* a, int nq, const float* const* kernels, float* blocks);
 
-/* The same with the kernel volumes in device memory of the handle's GPU, e.g. the
- * accumulation of fwant_sgtker without a round trip through the host. */
+/* The same with the kernel volumes already in device memory of the handle's GPU (a
+ * caller's own device arrays, ki*kj*kk floats each, Fortran order): no upload.  Pointers
+ * that are not device memory of that GPU are refused before any access. */
 fwant_status fwant_assm_project_device(fwant_assm* a, int nq, const float* const* d_kernels, float* blocks);
 
 /* The running sums of |B| (num_blk, 4), slots beyond the largest nq used are zero. */
