@@ -22,6 +22,7 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 WAVE = os.path.join(ROOT, "fwant_gb300", "bin", "fwant_wave")
 KER = os.path.join(ROOT, "fwant_gb300", "bin", "fwant_ker")
+ASSM = os.path.join(ROOT, "fwant_gb300", "bin", "fwant_assm")
 NT = 40                                  # 48 steps executed: 24 frames at tinv 2
 SNAP = ((3, 4, 5), (6, 5, 4), (2, 2, 2), 2, 5, "T")
 KNT = 20                                 # frames used: files n00001-n00004
@@ -214,6 +215,52 @@ def test_kernel_files_equal_the_restatement(runs, oracle_mod):
             assert got[name].shape == (SNAP[1][2], SNAP[1][1], SNAP[1][0])
             np.testing.assert_array_equal(got[name], w[q], err_msg=f"{d}:{name}")
             assert np.any(w[q])
+
+
+def test_assembly_of_the_kernel_files(runs):
+    """The kernel files this program writes are the assembly's input: fwant_assm (SI_ker2assm)
+    run on them writes the compact rows of the restatement's projection byte for byte."""
+    from scipy.io import netcdf_file
+
+    import assm_case as ac
+    from fwant_gb300 import inputs
+    from oracle import assm_oracle as A
+    tmp = runs["tmp"]
+    shape = tuple(SNAP[1])
+    volume, npix, pixs = ac.blocks(shape, brick=(2, 2, 2), seed=5)
+    nblk, max_pix = volume.shape[1], volume.shape[0]
+    blk = os.path.join(tmp, "blocks.nc")
+    with netcdf_file(blk, "w", version=1) as f:
+        f.createDimension("block", nblk)
+        f.createDimension("max_pix", max_pix)
+        f.createDimension("geo", 3)
+        f.createVariable("volume", "f4", ("block", "max_pix"))[:] = volume.T
+        f.createVariable("num_of_pix", "i4", ("block",))[:] = npix
+        f.createVariable("indx_of_pix", "i4", ("block", "max_pix", "geo"))[:] = pixs.transpose(2, 1, 0)
+    # the picks that have kernel files (the one after the series was skipped)
+    events = [dict(e, picks=[[p for p in comp if os.path.exists(os.path.join(p[4], "kernel_001_mpi000000_n00000.nc"))]
+                             for comp in e["picks"]]) for e in runs["events"]]
+    evt = os.path.join(tmp, "evt_assm.lst")
+    inputs.write_event_list(evt, events)
+    sta = os.path.join(tmp, "sta_assm.lst")
+    with open(sta, "w") as f:
+        f.write(f"STA {evt}\n")
+    spool = os.path.join(tmp, "spool")
+    os.makedirs(spool)
+    r = subprocess.run([ASSM, runs["conf"]], input=f"{sta}\n{blk}\n{spool}\n1.0 1.0 1.0 1.0\n0.0 0.0 0.0 0.0\n",
+                       capture_output=True, text=True, cwd=tmp)
+    assert r.returncode == 0, r.stdout + r.stderr
+    dirs = [p[4] for e in events for comp in e["picks"] for p in comp]
+    assert len(dirs) == 6
+    for d in dirs:
+        ker, _ = _read(os.path.join(d, "kernel_001_mpi000000_n00000.nc"))
+        part = d.lstrip("./").replace("/", "_")
+        for name, tag in (("phase_Vp", "Kap"), ("phase_Vs", "Kbp")):
+            B = A.project(ker[name].transpose(2, 1, 0), volume, npix, pixs)
+            idx, val = A.compact(B, 1.0, 0.0)
+            assert len(idx) > 0
+            with open(os.path.join(spool, f"{part}.{tag}.unformat"), "rb") as f:
+                assert f.read() == A.row_file_bytes(nblk, 0.0, idx, val), (d, tag)
 
 
 def test_resumed_blocks_rewrite_the_same_files(runs):
