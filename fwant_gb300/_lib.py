@@ -68,6 +68,7 @@ EXPORTS = [
     ("fwant_sgtker_set_sgt", C.c_int, [_vp, C.c_int, _fp]),
     ("fwant_sgtker_take_sgt", C.c_int, [_vp, C.c_int, _vp]),
     ("fwant_sgtker_scatter", C.c_int, [_vp, C.c_int, C.c_int, C.c_int]),
+    ("fwant_sgtker_set_param", C.c_int, [_vp, C.c_int]),
     ("fwant_sgtker_get_scatter", C.c_int, [_vp, C.c_int, C.POINTER(C.c_double)]),
     ("fwant_sgtker_kernel", C.c_int, [_vp, C.c_int, _fp, _fp, C.c_int, C.c_int, C.c_double,
                                       C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
@@ -541,6 +542,10 @@ class SgtKernel:
 
     def take_sgt(self, which, solver):
         self._chk(self._lib.fwant_sgtker_take_sgt(self._h, int(which), solver._h))
+
+    def set_param(self, param):
+        """0: Vp/Vs kernels (SI_ker_sta); 1: lambda/mu kernels (SI_ker_sta_lamu)."""
+        self._chk(self._lib.fwant_sgtker_set_param(self._h, int(param)))
 
     def scatter(self, flags, nt1=1, nt2=None):
         nt2 = self.knt if nt2 is None else int(nt2)

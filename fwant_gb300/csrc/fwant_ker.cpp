@@ -18,7 +18,9 @@
 // filter of the pick's band (:756-773) and the window kernels, written into
 // <pick directory>/kernel_NNN_mpi000000_n00000.nc (phase_Vp amplitude_Vp phase_Vs
 // amplitude_Vs over the snapshot's I J K), created at the first block of a first run and
-// updated in place by the later blocks.
+// updated in place by the later blocks.  With --lamu the program is SI_ker_sta_lamu: the
+// lambda/mu kernels (SI_ker_sta_lamu.F90:1299-1300) into kernel_lamu_NNN_mpi000000_n00000.nc
+// (phase_la amplitude_la phase_mu amplitude_mu); everything else is the same.
 //
 // Tool modes (format checks): --nc-slab FILE VAR START COUNT STRIDE prints a strided
 // sub-array as JSON; --nc-fill-slab FILE VAR START COUNT STRIDE writes 1, 2, ... into one
@@ -323,9 +325,11 @@ int main(int argc, char** argv) {
   if (argc >= 2 && std::strncmp(argv[1], "--nc-", 5) == 0) return nc_tool(argc, argv);
   std::string ker_conf = "TomoKernel.conf";
   int device = 0;
+  bool lamu = false;  // --lamu: the lambda/mu kernels of SI_ker_sta_lamu
   for (int a = 1; a < argc; ++a) {
     const std::string s = argv[a];
     if (s == "--device" && a + 1 < argc) device = std::atoi(argv[++a]);
+    else if (s == "--lamu") lamu = true;
     else ker_conf = s;
   }
   // init_kernel (SI_ker_sta.F90:1047-1082)
@@ -427,7 +431,11 @@ int main(int argc, char** argv) {
   size_t k_npts = 0;
   long long written = 0;
   std::vector<float> lam, mu, stress;
-  static const char* const kname[4] = {"phase_Vp", "amplitude_Vp", "phase_Vs", "amplitude_Vs"};
+  // variable names and file prefix: SI_ker_sta.F90:736-743, SI_ker_sta_lamu.F90:736-743
+  static const char* const kname_vpvs[4] = {"phase_Vp", "amplitude_Vp", "phase_Vs", "amplitude_Vs"};
+  static const char* const kname_lamu[4] = {"phase_la", "amplitude_la", "phase_mu", "amplitude_mu"};
+  const char* const* kname = lamu ? kname_lamu : kname_vpvs;
+  const std::string kprefix = lamu ? "/kernel_lamu_" : "/kernel_";
   while (std::getline(sl, line)) {
     const auto w = words(line);
     if (w.empty()) continue;
@@ -455,6 +463,7 @@ int main(int argc, char** argv) {
             if (K) fwant_sgtker_destroy(K);
             K = nullptr;
             check(fwant_sgtker_create((long long)np, knt, double(kdt), device, &K), nullptr, "sgtker_create");
+            if (lamu) check(fwant_sgtker_set_param(K, 1), K, "sgtker_set_param");
             k_npts = np;
           }
           {  // lambda and mu at the block's points (nfseis_varget with subs/subc/subt)
@@ -517,7 +526,7 @@ int main(int argc, char** argv) {
                     if (T[size_t(n - 1)] >= pk.t2 && (nt2 == 0 || T[size_t(n - 1)] < T[size_t(nt2 - 1)])) nt2 = n;
                 }
                 if (nt1 < 1 || nt2 < 1 || nt1 > nt2) die("window of pick " + pk.dir + " selects no sample");
-                const std::string path = pk.dir + "/kernel_" + seisfd::pad(kid, 3) + "_" + seisfd::MPI_SUFFIX + "_n00000.nc";
+                const std::string path = pk.dir + kprefix + seisfd::pad(kid, 3) + "_" + seisfd::MPI_SUFFIX + "_n00000.nc";
                 if (first_run && first_block) {  // nfseis_grid3d_def over the snapshot's points
                   nc3::Writer wr;
                   const int di = wr.add_dim("I", uint64_t(sp->subc[0])), dj = wr.add_dim("J", uint64_t(sp->subc[1])),
@@ -525,7 +534,7 @@ int main(int argc, char** argv) {
                   wr.add_gatt_text("title", "Finite frequency kernel");
                   const size_t n3 = size_t(sp->subc[0]) * sp->subc[1] * sp->subc[2];
                   const std::vector<float> zero(n3, 0.0f);
-                  for (const char* nm : kname) wr.add_var_f(nm, {dk, dj, di}, zero.data(), n3);
+                  for (int q = 0; q < 4; ++q) wr.add_var_f(kname[q], {dk, dj, di}, zero.data(), n3);
                   if (!wr.write(path, &err)) die(err);
                 }
                 if (pk.freq < 1 || (pk.filt != 0 && filters[size_t(pk.freq - 1)].nod1 == 0))

@@ -210,6 +210,7 @@ struct ScatterArgs {
   const float* rsgt[3];  // receiver SGT per force component, [6][knt][npts] stresses (null: skipped)
   const float* ssgt;     // source SGT, [6][knt][npts]
   double* out;           // [6][knt][npts]: X -> (0, 3), Y -> (1, 5), Z -> (2, 4)
+  int param;             // 0: Vp/Vs kernels, 1: lambda/mu kernels
 };
 int launch_sgt_scatter(const ScatterArgs& a, int sm_count, void* stream);
 struct KernelArgs {

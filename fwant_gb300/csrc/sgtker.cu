@@ -104,8 +104,16 @@ __global__ void __launch_bounds__(SC_THREADS) sgt_scatter_kernel(const ScatterAr
   }
   if (n > n_hi) return;
   const double lam = a.lam[p], mu = a.mu[p];
-  const double ka = (x1 * a.dt) * (2.0 * (lam + 2.0 * mu));
-  const double kb = ((x2 - x1) * a.dt) * (4.0 * mu);
+  // Vp/Vs: Ka = x1 2 (lam + 2 mu), Kb = 2 (x2 - x1) 2 mu (SI_ker_sta.F90:1297-1298);
+  // lambda/mu: Ka = x1 lam, Kb = 2 x2 mu (SI_ker_sta_lamu.F90:1299-1300)
+  double ka, kb;
+  if (a.param == 1) {
+    ka = (x1 * a.dt) * lam;
+    kb = (2.0 * (x2 * a.dt)) * mu;
+  } else {
+    ka = (x1 * a.dt) * (2.0 * (lam + 2.0 * mu));
+    kb = ((x2 - x1) * a.dt) * (4.0 * mu);
+  }
   // X -> (Exx, Exy), Y -> (Eyy, Eyz), Z -> (Ezz, Exz); component slots Exx Eyy Ezz Exy Exz Eyz
   const int slot_a = comp, slot_b = comp == 0 ? 3 : (comp == 1 ? 5 : 4);
   const long long o = (long long)(n - 1) * a.npts + p;

@@ -29,6 +29,7 @@ struct fwant_sgtker {
   float* sgt[4] = {nullptr, nullptr, nullptr, nullptr};  // X, Y, Z receiver SGT; source SGT
   double* series = nullptr;                              // [6][knt][npts]
   int scatter_nt1 = 0, scatter_nt2 = 0, scatter_flags = 0;
+  int param = 0;                                         // 0 Vp/Vs, 1 lambda/mu kernels
   double* wts = nullptr;                                 // wv[knt], wu[knt]
   double* kout = nullptr;                                // 4 x [npts]
   double* filtered = nullptr;                            // 2 x [knt][npts]: filtered Ka, Kb
@@ -150,6 +151,13 @@ fwant_status fwant_sgtker_take_sgt(fwant_sgtker* k, int which, fwant_solver* s) 
   return FWANT_OK;
 }
 
+fwant_status fwant_sgtker_set_param(fwant_sgtker* k, int param) {
+  if (!k) return FWANT_ERR_INVALID_ARG;
+  if (param != 0 && param != 1) return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_set_param: param must be 0 or 1");
+  k->param = param;
+  return FWANT_OK;
+}
+
 fwant_status fwant_sgtker_scatter(fwant_sgtker* k, int flags, int nt1, int nt2) {
   if (!k) return FWANT_ERR_INVALID_ARG;
   if ((flags & 7) == 0 || (flags & ~7)) return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_scatter: flags must be 1..7");
@@ -173,6 +181,7 @@ fwant_status fwant_sgtker_scatter(fwant_sgtker* k, int flags, int nt1, int nt2) 
   for (int c = 0; c < 3; ++c) a.rsgt[c] = (flags >> c & 1) ? k->sgt[c] : nullptr;
   a.ssgt = k->sgt[3];
   a.out = k->series;
+  a.param = k->param;
   cudaEventRecord(k->ev0, k->st);
   int le = fw::launch_sgt_scatter(a, 0, k->st);
   cudaEventRecord(k->ev1, k->st);

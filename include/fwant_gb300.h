@@ -265,6 +265,10 @@ fwant_status fwant_sgtker_take_sgt(fwant_sgtker* k, int which, fwant_solver* s);
  * into the series slots of the reference's in-place outputs: X -> (0 Exx, 3 Exy),
  * Y -> (1 Eyy, 5 Eyz), Z -> (2 Ezz, 4 Exz).  Slots of components not computed hold 0. */
 fwant_status fwant_sgtker_scatter(fwant_sgtker* k, int flags, int nt1, int nt2);
+/* Kernel parameterisation of later fwant_sgtker_scatter calls: 0 (the default) the Vp/Vs
+ * kernels above (SI_ker_sta.F90:1297-1298); 1 the lambda/mu kernels of SI_ker_sta_lamu
+ * (SI_ker_sta_lamu.F90:1299-1300): Ka(n) = x1 * lambda, Kb(n) = 2 x2 * mu. */
+fwant_status fwant_sgtker_set_param(fwant_sgtker* k, int param);
 /* One series slot (0..5: Exx Eyy Ezz Exy Exz Eyz positions), [knt][npts] FP64. */
 fwant_status fwant_sgtker_get_scatter(fwant_sgtker* k, int slot, double* out);
 /* scatter2kernel (SI_ker_sta.F90:1375-1431) for component ncmp (1 X, 2 Y, 3 Z: the

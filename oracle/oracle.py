@@ -54,7 +54,7 @@ _SIGS = [
     ("orc_metric_dd", None, [C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, _dp, _dp, _dp, _dp, _dp]),
     ("orc_stress2strain", None, [C.c_longlong, C.c_int, _fp, _fp, _fp, _fp]),
     ("orc_sgt2scatter3", None, [C.c_longlong, C.c_int, C.c_int, C.c_int, C.c_double, _fp, _fp, _fp, _fp, _fp, _fp,
-                                C.c_int, _dp]),
+                                C.c_int, C.c_int, _dp]),
     ("orc_scatter2kernel", None, [C.c_longlong, C.c_int, C.c_int, C.c_int, C.c_double, _fp, _fp, _dp, _dp,
                                   C.c_double, C.c_int, _dp, _dp, _dp, _dp]),
     ("orc_lsqr", C.c_longlong, [C.c_longlong, C.c_longlong, C.POINTER(C.c_longlong), _ip, _dp, _dp, C.c_double,
@@ -134,9 +134,11 @@ def stress2strain(lam, mu, stress):
     return out.reshape(st.shape)
 
 
-def sgt2scatter3(lam, mu, rsgt, ssgt, dt, nt1=None, nt2=None, mode=1):
+def sgt2scatter3(lam, mu, rsgt, ssgt, dt, nt1=None, nt2=None, mode=1, param=0):
     """rsgt: [X, Y, Z] receiver SGT stresses (6, knt, npts) or None; ssgt the source SGT.
-    mode 0: the reference's FP32 arithmetic; mode 1: FP64 accumulation.  Returns
+    mode 0: the reference's FP32 arithmetic; mode 1: FP64 accumulation.  param 0: Vp/Vs
+    kernels (SI_ker_sta.F90:1297-1298); param 1: lambda/mu kernels (SI_ker_sta_lamu.F90:
+    1299-1300).  Returns
     (6, knt, npts) float64 series (slots X -> 0, 3; Y -> 1, 5; Z -> 2, 4)."""
     s = _f(ssgt)
     _, knt, npts = np.asarray(ssgt).shape
@@ -147,7 +149,7 @@ def sgt2scatter3(lam, mu, rsgt, ssgt, dt, nt1=None, nt2=None, mode=1):
     lam_, mu_ = _f(lam), _f(mu)
     ptrs = [None if r is None else _p(r, C.c_float) for r in rs]
     lib().orc_sgt2scatter3(npts, knt, nt1, nt2, float(dt), _p(lam_, C.c_float), _p(mu_, C.c_float), *ptrs,
-                           _p(s, C.c_float), int(mode), _p(out))
+                           _p(s, C.c_float), int(mode), int(param), _p(out))
     return out.reshape(6, knt, npts)
 
 

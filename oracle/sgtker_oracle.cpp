@@ -71,8 +71,11 @@ void orc_stress2strain(long long npts, int knt, const float* lam, const float* m
 
 // sgt2scatter3: rsgt[3] receiver SGT stresses (null = flag off), ssgt source SGT; out
 // [6][knt][npts] FP64 (slots X -> 0, 3; Y -> 1, 5; Z -> 2, 4); nt1, nt2 1-based.
+// param 0: Vp/Vs kernels, Ka = x1 2 (lambda + 2 mu), Kb = 2 (x2 - x1) 2 mu (SI_ker_sta.F90:1297-1298);
+// param 1: lambda/mu kernels, Ka = x1 lambda, Kb = 2 x2 mu (SI_ker_sta_lamu.F90:1299-1300).
 void orc_sgt2scatter3(long long npts, int knt, int nt1, int nt2, double dt, const float* lam, const float* mu,
-                      const float* rx, const float* ry, const float* rz, const float* ssgt, int mode, double* out) {
+                      const float* rx, const float* ry, const float* rz, const float* ssgt, int mode, int param,
+                      double* out) {
   const float* rs[3] = {rx, ry, rz};
   const int slot_b[3] = {3, 5, 4};
   const size_t cs = size_t(knt) * size_t(npts);
@@ -98,8 +101,13 @@ void orc_sgt2scatter3(long long npts, int knt, int nt1, int nt2, double dt, cons
                                        (2.0f * R[4]) * S[4]) +
                                       (2.0f * R[5]) * S[5]);
           }
-          ka = (x1 * 2.0f) * (lam[p] + 2.0f * mu[p]);
-          kb = ((2.0f * (x2 - x1)) * 2.0f) * mu[p];
+          if (param == 1) {
+            ka = x1 * lam[p];
+            kb = (2.0f * x2) * mu[p];
+          } else {
+            ka = (x1 * 2.0f) * (lam[p] + 2.0f * mu[p]);
+            kb = ((2.0f * (x2 - x1)) * 2.0f) * mu[p];
+          }
         } else {
           double x1 = 0.0, x2 = 0.0;
           for (int m = 1; m <= n - 1; ++m) {
@@ -116,8 +124,13 @@ void orc_sgt2scatter3(long long npts, int knt, int nt1, int nt2, double dt, cons
             x2 = std::fma(2.0 * double(R[5]), double(S[5]), x2);
           }
           const double l = lam[p], u = mu[p];
-          ka = (x1 * dt) * (2.0 * (l + 2.0 * u));
-          kb = ((x2 - x1) * dt) * (4.0 * u);
+          if (param == 1) {
+            ka = (x1 * dt) * l;
+            kb = (2.0 * (x2 * dt)) * u;
+          } else {
+            ka = (x1 * dt) * (2.0 * (l + 2.0 * u));
+            kb = ((x2 - x1) * dt) * (4.0 * u);
+          }
         }
         const size_t o = size_t(n - 1) * size_t(npts) + size_t(p);
         out[size_t(comp) * cs + o] = ka;

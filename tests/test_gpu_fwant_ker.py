@@ -132,8 +132,9 @@ def runs(tmp_path_factory, native_lib):
                 sgt_root=sgt_root, evt_root=evt_root, kd=kd, stdout=r.stdout)
 
 
-def _expected(R, oracle_mod):
-    """Kernels of every pick over all selected points, float32, in file (K, J, I) layout."""
+def _expected(R, oracle_mod, param=0):
+    """Kernels of every pick over all selected points, float32, in file (K, J, I) layout
+    (param 0 Vp/Vs kernels, 1 lambda/mu kernels)."""
     m, kdt, t = R["m"], R["kdt"], R["t"]
     subs, subc, subt = SNAP[0], SNAP[1], SNAP[2]
     # selected sample indices (0-based) per axis: start, stride, count of the kernel selection
@@ -161,7 +162,8 @@ def _expected(R, oracle_mod):
     for e, syn in ((R["events"][0], R["syn"][:3]), (R["events"][1], [R["syn"][3]] * 3)):
         rot_any = any(len(p) for p in e["picks"][3:])
         ud = [len(e["picks"][c]) > 0 or rot_any for c in range(3)]
-        scat = oracle_mod.sgt2scatter3(lam, mu, [rs[c] if ud[c] else None for c in range(3)], ss, dt, mode=1)
+        scat = oracle_mod.sgt2scatter3(lam, mu, [rs[c] if ud[c] else None for c in range(3)], ss, dt, mode=1,
+                                       param=param)
         V = [s[1].copy() for s in syn]
         U = [s[2].copy() for s in syn]
         rot = np.asarray(e["rot"], np.float32).reshape(3, 3)
@@ -261,6 +263,36 @@ def test_assembly_of_the_kernel_files(runs):
             assert len(idx) > 0
             with open(os.path.join(spool, f"{part}.{tag}.unformat"), "rb") as f:
                 assert f.read() == A.row_file_bytes(nblk, 0.0, idx, val), (d, tag)
+
+
+def test_lamu_kernel_files_equal_the_restatement(runs, oracle_mod):
+    """--lamu (SI_ker_sta_lamu): the same inputs give the lambda/mu kernels, written to
+    kernel_lamu_NNN files under phase_la amplitude_la phase_mu amplitude_mu, equal to the
+    restatement's; the Vp/Vs files of the same picks are left as they were."""
+    before = {d: _read(os.path.join(d, "kernel_001_mpi000000_n00000.nc"))[0]
+              for d in _expected(runs, oracle_mod) if os.path.exists(os.path.join(d, "kernel_001_mpi000000_n00000.nc"))}
+    for e in runs["events"]:
+        for comp in e["picks"]:
+            for p in comp:
+                os.makedirs(p[4], exist_ok=True)
+    r = subprocess.run([KER, "--lamu", runs["conf"]], input=f"{runs['sta']}\n0 0 0\n", capture_output=True,
+                       text=True, cwd=runs["tmp"])
+    assert r.returncode == 0, r.stderr
+    want = _expected(runs, oracle_mod, param=1)
+    names = ("phase_la", "amplitude_la", "phase_mu", "amplitude_mu")
+    for d, w in want.items():
+        path = os.path.join(d, "kernel_lamu_001_mpi000000_n00000.nc")
+        if w is None:
+            assert not os.path.exists(path)
+            continue
+        got, _ = _read(path)
+        for q, name in enumerate(names):
+            np.testing.assert_array_equal(got[name], w[q], err_msg=f"{d}:{name}")
+            assert np.any(w[q])
+    for d, b in before.items():
+        after, _ = _read(os.path.join(d, "kernel_001_mpi000000_n00000.nc"))
+        for name in NAMES:
+            np.testing.assert_array_equal(after[name], b[name])
 
 
 def test_resumed_blocks_rewrite_the_same_files(runs):

@@ -33,6 +33,33 @@ def _series(rng, npts, knt):
     return (1e5 * (env * np.sin(2 * np.pi * f * t + ph) + noise)).astype(np.float32)
 
 
+def test_lamu_scatter_bitwise_against_fp64_restatement(oracle_mod, native_lib):
+    """set_param(1): the lambda/mu series of SI_ker_sta_lamu, bit for bit the restatement's."""
+    import fwant_gb300 as fw
+    rng = np.random.default_rng(77)
+    npts, knt, dt = 41, 600, 0.1
+    lam, mu = _media(rng, npts)
+    r = [_series(rng, npts, knt) for _ in range(3)]
+    s = _series(rng, npts, knt)
+    k = fw.SgtKernel(npts, knt, dt)
+    k.set_media(lam, mu)
+    for c in range(3):
+        k.set_sgt(c, r[c])
+    k.set_sgt(3, s)
+    with pytest.raises(fw.FwantError):
+        k.set_param(2)
+    k.set_param(1)
+    k.scatter(7, 3, 590)
+    want = oracle_mod.sgt2scatter3(lam, mu, r, s, dt, nt1=3, nt2=590, mode=1, param=1)
+    for slot in range(6):
+        np.testing.assert_array_equal(k.get_scatter(slot), want[slot], err_msg=f"slot {slot}")
+        assert np.any(want[slot])
+    k.set_param(0)
+    k.scatter(4, 3, 590)
+    vpvs = oracle_mod.sgt2scatter3(lam, mu, [None, None, r[2]], s, dt, nt1=3, nt2=590, mode=1)
+    np.testing.assert_array_equal(k.get_scatter(2), vpvs[2])
+
+
 # knt 700 spans two lag chunks (512) and three output chunks (256) of the device kernel
 @pytest.mark.parametrize("flags,nt1,nt2", [(7, 1, 700), (5, 37, 651), (2, 300, 300)])
 def test_scatter_bitwise_against_fp64_restatement(flags, nt1, nt2, oracle_mod, native_lib):

@@ -50,13 +50,16 @@ def _strains64(lam, mu, sgt, oracle_mod):
     return oracle_mod.stress2strain(lam, mu, sgt).astype(np.float64)
 
 
-def test_scatter_fp64_matches_convolution(oracle_mod):
+@pytest.mark.parametrize("param", [0, 1], ids=["vpvs", "lamu"])
+def test_scatter_fp64_matches_convolution(param, oracle_mod):
+    """param 0: Vp/Vs kernels (SI_ker_sta.F90:1297-1298); param 1: lambda/mu kernels
+    (SI_ker_sta_lamu.F90:1299-1300), against numpy convolutions of the strains."""
     rng = np.random.default_rng(5)
     npts, knt, dt = 13, 140, 0.2
     lam, mu = _media(rng, npts)
     r = [_series(rng, npts, knt) for _ in range(3)]
     s = _series(rng, npts, knt)
-    out = oracle_mod.sgt2scatter3(lam, mu, r, s, dt, mode=1)
+    out = oracle_mod.sgt2scatter3(lam, mu, r, s, dt, mode=1, param=param)
     es = _strains64(lam, mu, s, oracle_mod)
     for comp, slot_b in ((0, 3), (1, 5), (2, 4)):
         er = _strains64(lam, mu, r[comp], oracle_mod)
@@ -69,8 +72,12 @@ def test_scatter_fp64_matches_convolution(oracle_mod):
                        ((0, 1.0), (1, 1.0), (2, 1.0), (3, 2.0), (4, 2.0), (5, 2.0)))
             x2 = np.zeros(knt)
             x2[1:] = dt * full[: knt - 1]
-            ka = x1 * 2.0 * (float(lam[p]) + 2.0 * float(mu[p]))
-            kb = (x2 - x1) * 4.0 * float(mu[p])
+            if param == 1:
+                ka = x1 * float(lam[p])
+                kb = 2.0 * x2 * float(mu[p])
+            else:
+                ka = x1 * 2.0 * (float(lam[p]) + 2.0 * float(mu[p]))
+                kb = (x2 - x1) * 4.0 * float(mu[p])
             scale = np.max(np.abs(ka)) + np.max(np.abs(kb))
             np.testing.assert_allclose(out[comp, :, p], ka, rtol=0, atol=1e-12 * scale)
             np.testing.assert_allclose(out[slot_b, :, p], kb, rtol=0, atol=1e-12 * scale)
