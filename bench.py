@@ -71,6 +71,9 @@ def parse_args():
     p.add_argument("--cpu-steps", type=int, default=2, help="steps of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-c3", action="store_true",
+                   help="skip the C3 batched-vs-single comparison of the default (C2) line")
+    p.add_argument("--c3-steps", type=int, default=16, help="timed steps of each C3 leg (multiple of 8)")
     p.add_argument("--grid", default=None, help="override the C2 interior size, e.g. 200x200x100 (profiling)")
     p.add_argument("--sims", type=int, default=3, help="number of force components simulated (C2)")
     p.add_argument("--autotune", action="store_true",
@@ -232,9 +235,9 @@ def cpu_sample(models, steps):
     from fwant_gb300 import inputs
     from oracle import oracle as O
     O.build()
-    threads = O.set_threads(os.cpu_count() or 1)
+    threads = O.set_threads(os.cpu_count() or 1, timing=True)
     m = models[0]
-    o = O.Oracle(m.ni, m.nj, m.nk, m.stept)
+    o = O.Oracle(m.ni, m.nj, m.nk, m.stept, timing=True)
     inputs.attach(o, m, metric=O.metric(m.x, m.y, m.z))
     o.run(1)  # first touch of every array
     t0 = time.perf_counter()
@@ -244,6 +247,16 @@ def cpu_sample(models, steps):
     return m.npoints * steps / dt / 1e9, threads, dt
 
 
+def _timing_flags():
+    from oracle import oracle as O
+    return O.build_flags(timing=True)
+
+
+def _checker_flags():
+    from oracle import oracle as O
+    return O.build_flags()
+
+
 def _reference_line(args, metric, unit, v, dt, desc, sample, threads, dtype):
     out = {
         "impl": "reference", "metric": metric, "value": v, "unit": unit,
@@ -251,7 +264,8 @@ def _reference_line(args, metric, unit, v, dt, desc, sample, threads, dtype):
         "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "replicas only",
         "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded)",
         "config": {"workload": desc, "sample": sample},
-        "cpu_baseline": {"value": v, "unit": unit, "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": v, "unit": unit, "cores": threads, "kind": "port", "sample": sample,
+                         "build": _timing_flags()},
         "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
@@ -263,10 +277,10 @@ def run_reference_media(args):
     planes of the bench's grid"""
     from oracle import oracle as O
     O.build()
-    threads = O.set_threads(os.cpu_count() or 1)
+    threads = O.set_threads(os.cpu_count() or 1, timing=True)
     ni, nj, nk, x, y, z, zt, calls, desc = media_workload(args.grid)
     kk = min(nk, 8)
-    o = O.MediaOracle(ni, nj, kk, x, y, z[nk - kk:], zt, (1, 1, 1))
+    o = O.MediaOracle(ni, nj, kk, x, y, z[nk - kk:], zt, (1, 1, 1), timing=True)
     for name, a in calls:
         getattr(o, name)(*a)
     for _ in range(max(args.warmup, 1)):
@@ -287,7 +301,7 @@ def run_reference_lsqr(args):
     rp, col, val, rhs, ncol = lsqr_system(args.lsqr_scale)
     nnz = int(rp[-1])
     t0 = time.perf_counter()
-    O.lsqr(rp, col, val, rhs, ncol, atol=0.0, btol=0.0, maxit=args.steps)
+    O.lsqr(rp, col, val, rhs, ncol, atol=0.0, btol=0.0, maxit=args.steps, timing=True)
     dt = time.perf_counter() - t0
     sample = f"{args.steps} iterations of the sequential restatement (setup and |A|_F included), 1 thread"
     return _reference_line(args, "LSQR matrix entries per second", "Gentries/s", nnz * args.steps / dt / 1e9, dt,
@@ -299,16 +313,16 @@ def run_reference_ker(args):
     sample of the block's points"""
     from oracle import oracle as O
     O.build()
-    threads = O.set_threads(os.cpu_count() or 1)
+    threads = O.set_threads(os.cpu_count() or 1, timing=True)
     npts, knt = args.ker_points, 500
     lam, mu, sgt = ker_block(npts, knt)
     ns = min(npts, 1024)
     sub = [a[:, :, :ns].copy() for a in sgt]
     for _ in range(max(args.warmup, 1)):
-        O.sgt2scatter3(lam[:ns], mu[:ns], sub[:3], sub[3], 0.1, mode=1)
+        O.sgt2scatter3(lam[:ns], mu[:ns], sub[:3], sub[3], 0.1, mode=1, timing=True)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        O.sgt2scatter3(lam[:ns], mu[:ns], sub[:3], sub[3], 0.1, mode=1)
+        O.sgt2scatter3(lam[:ns], mu[:ns], sub[:3], sub[3], 0.1, mode=1, timing=True)
     dt = time.perf_counter() - t0
     dfma = ns * 3 * 7 * knt * (knt - 1) / 2
     sample = f"{ns} of the {npts} kernel points per step, {threads} threads"
@@ -332,9 +346,9 @@ def run_reference(args, rank, world):
     from fwant_gb300 import inputs
     from oracle import oracle as O
     O.build()
-    threads = O.set_threads(os.cpu_count() or 1)
+    threads = O.set_threads(os.cpu_count() or 1, timing=True)
     m = models[0]
-    o = O.Oracle(m.ni, m.nj, m.nk, m.stept)
+    o = O.Oracle(m.ni, m.nj, m.nk, m.stept, timing=True)
     inputs.attach(o, m, metric=O.metric(m.x, m.y, m.z))
     o.run(max(args.warmup, 1))
     t0 = time.perf_counter()
@@ -349,7 +363,8 @@ def run_reference(args, rank, world):
         "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": desc, "sample": sample, "l2": "inputs larger than L2 (no flush)"},
-        "cpu_baseline": {"value": v, "unit": "GPts/s", "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": v, "unit": "GPts/s", "cores": threads, "kind": "port", "sample": sample,
+                         "build": _timing_flags(), "checker_build": _checker_flags()},
         "e2e": {"value": v, "unit": "GPts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
@@ -445,9 +460,10 @@ def run_lsqr(args, rank):
         O.build()
         k = 2
         t1 = time.perf_counter()
-        O.lsqr(rp, col, val, rhs, ncol, atol=0.0, btol=0.0, maxit=k)
+        O.lsqr(rp, col, val, rhs, ncol, atol=0.0, btol=0.0, maxit=k, timing=True)
         dt = time.perf_counter() - t1
         out["cpu_baseline"] = {"value": nnz * k / dt / 1e9, "unit": "Gentries/s", "cores": 1, "kind": "port",
+                               "build": O.build_flags(timing=True),
                                "sample": f"{k} iterations of the sequential restatement on the same system, "
                                          f"{dt:.1f} s (setup and |A|_F included)"}
     if not args.no_e2e:
@@ -528,16 +544,17 @@ def run_media(args, rank):
     if not args.no_cpu_baseline:
         from oracle import oracle as O
         O.build()
-        threads = O.set_threads(os.cpu_count() or 1)
+        threads = O.set_threads(os.cpu_count() or 1, timing=True)
         kk = min(nk, 20)
         zs = z[nk - kk:]  # the top kk planes of the same grid (with their ghosts)
-        o = O.MediaOracle(ni, nj, kk, x, y, zs, zt, (1, 1, 1))
+        o = O.MediaOracle(ni, nj, kk, x, y, zs, zt, (1, 1, 1), timing=True)
         for name, a in calls:
             getattr(o, name)(*a)
         t1 = time.perf_counter()
         o.eval()
         dt = time.perf_counter() - t1
         out["cpu_baseline"] = {"value": ni * nj * kk / dt / 1e9, "unit": "GPts/s", "cores": threads, "kind": "port",
+                               "build": O.build_flags(timing=True),
                                "sample": f"the top {kk} planes of the same grid ({ni}x{nj}x{kk} points, "
                                          f"same models), {dt:.1f} s"}
     if not args.no_e2e:
@@ -720,14 +737,15 @@ def run_ker(args, rank):
     if not args.no_cpu_baseline:
         from oracle import oracle as O
         O.build()
-        threads = O.set_threads(os.cpu_count() or 1)
+        threads = O.set_threads(os.cpu_count() or 1, timing=True)
         ns = min(npts, 2048)
         sub = [a[:, :, :ns].copy() for a in sgt]
         t1 = time.perf_counter()
-        O.sgt2scatter3(lam[:ns], mu[:ns], sub[:3], sub[3], kdt, mode=1)
+        O.sgt2scatter3(lam[:ns], mu[:ns], sub[:3], sub[3], kdt, mode=1, timing=True)
         dt = time.perf_counter() - t1
         out["cpu_baseline"] = {"value": 2 * dfma * ns / npts / dt / 1e12, "unit": "TFLOP/s", "cores": threads,
-                               "kind": "port", "sample": f"{ns} of the {npts} points, same series, {dt:.1f} s"}
+                               "kind": "port", "sample": f"{ns} of the {npts} points, same series, {dt:.1f} s",
+                               "build": O.build_flags(timing=True)}
     if not args.no_e2e:
         v = np.sin(np.arange(knt, dtype=np.float32) * np.float32(0.05))
         u = np.cos(np.arange(knt, dtype=np.float32) * np.float32(0.05))
@@ -746,6 +764,45 @@ def run_ker(args, rank):
                       "includes": "handle creation, media and SGT upload, one scatter, window integrals, kernels read back"}
     print(json.dumps(out), flush=True)
     return 0
+
+
+def c3_batched_vs_single(dev, steps):
+    """C3's 32 seeded virtual sources of uneven sizes (160-320 x 160-320 x 80-160, C2
+    physics, one surface force each): device time per source and step when the members
+    are stepped as one batch (one launch per RK stage and group of up to 16 members, the
+    interior-only and full forms where a stage has both) against each member stepped
+    alone (its own launches).  Both legs replay 8-step CUDA graphs; CUDA events."""
+    import fwant_gb300 as fw
+    from fwant_gb300 import inputs
+    t0 = time.perf_counter()
+    models = inputs.config_c3(seed=0)
+    sims = [inputs.attach(fw.Solver(m.ni, m.nj, m.nk, m.stept, device=dev), m) for m in models]
+    npts = sum(m.npoints for m in models)
+    n = len(models)
+    b = fw.Batch(sims)
+    b.run(8)  # warm-up block (graph capture)
+    b.run(steps)
+    batched_ms = b.last_run_ms()
+    launches = b.launches_per_step()
+    b.close()
+    single_ms = 0.0
+    for s in sims:
+        s.run(8)
+        s.run(steps)
+        single_ms += s.last_run_ms()
+    for s in sims:
+        s.close()
+    return {
+        "workload": f"C3: {n} virtual sources, {npts / 1e6:.1f} M interior points in all, {steps} steps per leg",
+        "batched_ms_per_source_step": batched_ms / steps / n,
+        "single_ms_per_source_step": single_ms / steps / n,
+        "batched_value": npts * steps / (batched_ms * 1e-3) / 1e9,
+        "single_value": npts * steps / (single_ms * 1e-3) / 1e9,
+        "unit": "GPts/s",
+        "speedup": single_ms / batched_ms,
+        "batched_launches_per_step": launches,
+        "wall_s": time.perf_counter() - t0,
+    }
 
 
 def run_surrogate(args, rank):
@@ -901,9 +958,12 @@ def run_ours(args, rank, world):
         out["e2e"] = {"value": world * npts * args.steps / t_e2e / 1e9, "unit": "GPts/s",
                       "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps,
                       "wall_s": t_e2e, "includes": "solver creation, model upload, run, seismogram download"}
+    if args.config == "c2" and not args.grid and not args.no_c3 and world == 1:
+        out["batched_vs_single"] = c3_batched_vs_single(dev, max(8, args.c3_steps // 8 * 8))
     if rank == 0 and not args.no_cpu_baseline:
         v, thr, dt = cpu_sample(models, args.cpu_steps)
         out["cpu_baseline"] = {"value": v, "unit": "GPts/s", "cores": thr, "kind": "port",
+                               "build": _timing_flags(), "checker_build": _checker_flags(),
                                "sample": f"{args.cpu_steps} time steps of one simulation "
                                          f"({m0.ni}x{m0.nj}x{m0.nk}), {dt:.1f} s"}
     if rank == 0:

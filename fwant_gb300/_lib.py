@@ -51,6 +51,8 @@ EXPORTS = [
     ("fwant_set_receivers", C.c_int, [_vp, C.c_int, _ip, C.c_int]),
     ("fwant_run", C.c_int, [_vp, C.c_int]),
     ("fwant_reference_steps", C.c_int, [C.c_int]),
+    ("fwant_source_time_function", C.c_int, [C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_int, C.c_float,
+                                              _fp]),
     ("fwant_get_ntime", C.c_int, [_vp, _ip]),
     ("fwant_get_seismo", C.c_int, [_vp, _fp, C.c_int, _ip]),
     ("fwant_get_field", C.c_int, [_vp, C.c_int, _fp]),
@@ -828,6 +830,18 @@ class Assm:
             self.close()
         except Exception:
             pass
+
+
+def source_time_function(which: int, stf_id: int, t: float, t0: float, f0: float, ntime: int = 1,
+                         stept: float = 0.01) -> float:
+    """src_stf (which = 0) or src_svf (which = 1) as the solver tabulates it (host code,
+    FP32); raises FwantError for an id the function does not define."""
+    out = C.c_float()
+    rc = load_library().fwant_source_time_function(int(which), int(stf_id), float(t), float(t0), float(f0),
+                                                     int(ntime), float(stept), C.byref(out))
+    if rc != 0:
+        raise FwantError(rc, f"source time function {stf_id} is not defined for which={which}")
+    return float(out.value)
 
 
 def reference_steps(nt: int) -> int:

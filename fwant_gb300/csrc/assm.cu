@@ -9,6 +9,7 @@
 // rounded before the add (__fmul_rn / __fadd_rn), which is the reference's single-precision
 // arithmetic; the sweep over all blocks reads every kernel point about once, so the launch is
 // bound by the gathers' DRAM traffic.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -188,6 +189,27 @@ fwant_status fwant_assm_project(fwant_assm* a, int nq, const float* const* kerne
   return a->run(nq, K, blocks);
 }
 
+// Bytes from p to the end of the device allocation holding it (driver entry point
+// cuMemGetAddressRange, looked up through the runtime so the library needs no -lcuda).
+static int device_room(const void* p, size_t* room) {
+  using RangeFn = CUresult (*)(CUdeviceptr*, size_t*, CUdeviceptr);
+  static RangeFn fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuMemGetAddressRange", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<RangeFn>(f);
+  }();
+  if (!fn) return -1;
+  CUdeviceptr base = 0;
+  size_t size = 0;
+  const CUresult r = fn(&base, &size, reinterpret_cast<CUdeviceptr>(p));
+  if (r != CUDA_SUCCESS) return int(r);
+  *room = size_t(base + size - reinterpret_cast<CUdeviceptr>(p));
+  return 0;
+}
+
 fwant_status fwant_assm_project_device(fwant_assm* a, int nq, const float* const* d_kernels, float* blocks) {
   if (!a || nq < 1 || nq > AS_MAXQ || !d_kernels || !blocks) return FWANT_ERR_INVALID_ARG;
   cudaError_t e = cudaSetDevice(a->device);
@@ -200,6 +222,15 @@ fwant_status fwant_assm_project_device(fwant_assm* a, int nq, const float* const
       cudaGetLastError();
       return a->fail(FWANT_ERR_INVALID_ARG, "kernel volumes must be device memory of the handle's GPU");
     }
+    // the allocation must hold the whole volume from the given pointer on: the gather
+    // kernel reads any of its ki*kj*kk values
+    size_t room = 0;
+    if (int ce = device_room(d_kernels[q], &room))
+      return a->fail(FWANT_ERR_INVALID_ARG, "kernel volume: cuMemGetAddressRange failed (" + std::to_string(ce) + ")");
+    if (room < a->nvol * sizeof(float))
+      return a->fail(FWANT_ERR_INVALID_ARG, "kernel volume " + std::to_string(q) + ": its allocation holds " +
+                                                std::to_string(room / sizeof(float)) + " floats past the pointer, " +
+                                                std::to_string(a->nvol) + " needed");
     K.p[q] = d_kernels[q];
   }
   return a->run(nq, K, blocks);

@@ -3,8 +3,6 @@
 // copied to the host.
 #include <cuda_runtime.h>
 
-#include <mutex>
-
 #include "kernels.h"
 #include "storage.cuh"
 
@@ -72,21 +70,16 @@ void launch_record_sgt(const SgtRecArgs& a, void* stream) {
 // needs clearing between calls.
 static __device__ __align__(256) float g_snapshot_staging[SNAPSHOT_NOALLOC_MAX];
 
-// Device address of the staging array on `device`, resolved once per device (with that
-// device current, which the caller guarantees) and cached.
-static std::mutex g_staging_mutex;
-static float* g_staging_ptr[64] = {};
-
+// Device address of the staging array on the current device.  It is resolved on every
+// call (cudaGetSymbolAddress allocates nothing and is cheap), so a device reset or a
+// re-created primary context, after which the module may load at another address, never
+// leaves a stale pointer behind.
 int snapshot_noalloc_staging(int device, float** ptr) {
-  if (device < 0 || device >= 64) return int(cudaErrorInvalidDevice);
-  std::lock_guard<std::mutex> lock(g_staging_mutex);
-  if (!g_staging_ptr[device]) {
-    float* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_snapshot_staging);
-    if (e != cudaSuccess) return int(e);
-    g_staging_ptr[device] = p;
-  }
-  *ptr = g_staging_ptr[device];
+  (void)device;  // the caller has made `device` current
+  float* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_snapshot_staging);
+  if (e != cudaSuccess) return int(e);
+  *ptr = p;
   return 0;
 }
 

@@ -451,6 +451,7 @@ struct fwant_solver {
     const int cap_steps = std::max(steps + 8, 1024);
     const int G = cap_steps * 4;
     const float incr[4] = {0.0f, RKA[0], RKA[1], RKA[2]};  // set_cur_time(ntime, firRKa(s))
+    const bool surf_rate = g.freesurf && cfg.src_surface;
     const ForceDesc& F = forces;
     const MomentDesc& Mo = moments;
     const int nwf = F.num * F.ntwin, nwm = Mo.num * Mo.ntwin;
@@ -462,9 +463,11 @@ struct fwant_solver {
         const float t = (float(n) + incr[s]) * stept;
         for (int q = 0; q < F.num; ++q)
           for (int m = 0; m < F.ntwin; ++m) {
-            float dv, rv;
+            // src_surface evaluates both functions of every force, and only under a free
+            // surface (mod_src.F90:384-396); src_force needs the STF alone (:312)
+            float dv, rv = 0.0f;
             if (!fw::hm::stf(t - F.t0[q], F.stf_time[m], F.stf_freq[m], F.stf_id, n, stept, &dv) ||
-                !fw::hm::svf(t - F.t0[q], F.stf_time[m], F.stf_freq[m], F.stf_id, n, stept, &rv))
+                (surf_rate && !fw::hm::svf(t - F.t0[q], F.stf_time[m], F.stf_freq[m], F.stf_id, n, stept, &rv)))
               return fail(FWANT_ERR_INVALID_ARG, "unknown force stf id");
             disp[size_t(gs) * nwf + q * F.ntwin + m] = dv;
             rate[size_t(gs) * nwf + q * F.ntwin + m] = rv;
@@ -796,7 +799,9 @@ struct fwant_solver {
     const int lo[3] = {g.i1, g.j1, g.k1}, hi[3] = {g.i2, g.j2, g.k2};
     for (int d = 0; d < 3; ++d) {
       if (subc[d] < 1 || subt[d] < 1) return fail(FWANT_ERR_INVALID_ARG, "snapshot: counts and strides must be >= 1");
-      const int s0 = subs[d] - 1, e0 = s0 + subt[d] * (subc[d] - 1);
+      // 64-bit end index: a large stride x count must not wrap back into the interior
+      const long long s0 = (long long)subs[d] - 1;
+      const long long e0 = s0 + (long long)subt[d] * ((long long)subc[d] - 1);
       if (s0 < lo[d] || e0 > hi[d]) return fail(FWANT_ERR_INVALID_ARG, "snapshot: sub-volume outside the interior");
       a.start[d] = s0; a.cnt[d] = subc[d]; a.stride[d] = subt[d];
     }
@@ -925,6 +930,14 @@ struct fwant_solver {
 extern "C" {
 
 const char* fwant_version(void) { return "fwant_gb300 0.1 (sm_103a)"; }
+
+fwant_status fwant_source_time_function(int which, int stf_id, float t, float t0, float f0, int ntime, float stept,
+                                        float* out) {
+  if (!out || (which != 0 && which != 1)) return FWANT_ERR_INVALID_ARG;
+  const bool ok = which == 0 ? fw::hm::stf(t, t0, f0, stf_id, ntime, stept, out)
+                             : fw::hm::svf(t, t0, f0, stf_id, ntime, stept, out);
+  return ok ? FWANT_OK : FWANT_ERR_INVALID_ARG;
+}
 
 fwant_status fwant_create(const fwant_config* cfg, fwant_solver** out) {
   if (!cfg || !out) return FWANT_ERR_INVALID_ARG;

@@ -77,6 +77,16 @@ typedef struct fwant_config {
                           0: fast form (FMA, precomputed reciprocals) */
 } fwant_config;
 
+/* One value of the source time function (which = 0: src_stf, the displacement/moment
+ * history, code/srcF/mod_src.F90:464-487) or of its rate (which = 1: src_svf,
+ * :438-463) at time t for window start t0 and frequency or rise time f0; ntime and stept
+ * feed the delta function (:617-622).  These are the values the solver tabulates per RK
+ * stage.  Host-only: needs no GPU.  FWANT_ERR_INVALID_ARG for an id the function does
+ * not define (the reference stops there). */
+fwant_status fwant_source_time_function(int which, int stf_id, float t, float t0, float f0, int ntime, float stept,
+                                        float* out);
+
+
 typedef struct fwant_solver fwant_solver;
 
 /* Library version string. */
@@ -216,8 +226,9 @@ fwant_status fwant_get_snapshot(fwant_solver* s, const int subs[3], const int su
  * device array of 4,194,304 floats (16 MiB) that the library holds on every GPU it is
  * loaded on until the process exits; a request for more values (ncomp * subc[0] *
  * subc[1] * subc[2]) is rejected with FWANT_ERR_INVALID_ARG, so large volumes are read in
- * pieces (e.g. k-ranges).  The first call on a device resolves that array's device
- * address; make it before any stream capture.  All calls on one device share the array:
+ * pieces (e.g. k-ranges).  Every call looks up that array's device address, which
+ * allocates nothing; the first call on a device may load the library's device code there,
+ * so make it before any stream capture.  All calls on one device share the array:
  * each call overwrites every value it returns, but calls that overlap on the GPU (other
  * threads or handles on the same device) race with each other. */
 fwant_status fwant_get_snapshot_noalloc(fwant_solver* s, const int subs[3], const int subc[3], const int subt[3],

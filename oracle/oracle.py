@@ -76,35 +76,59 @@ _SIGS = [
 ]
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile the oracle (g++, OpenMP, no FP contraction)."""
-    os.makedirs(os.path.dirname(LIB), exist_ok=True)
-    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(s) for s in SRCS):
-        return LIB
-    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-o", LIB, *SRCS]
+# The checker: every product and sum rounds separately (no FP contraction), as the
+# reference's FP32 source expressions do, so the GPU's reference-order form can be compared
+# bit for bit.
+CHECK_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off"]
+# The timed CPU baseline: the same sources built for speed (-O3 vectorisation and unrolling,
+# fused multiply-adds allowed).  Results differ from the checker by rounding only; it is
+# never used to check anything.  Generic target ISA (no -march=native), so one recipe
+# builds on x86-64 and aarch64 hosts alike.
+TIMING_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=fast", "-funroll-loops"]
+TIMING_LIB = os.path.join(HERE, "_build", "libfwant_oracle_timing.so")
+
+
+def _build_one(target, flags, force, verbose):
+    os.makedirs(os.path.dirname(target), exist_ok=True)
+    if not force and os.path.exists(target) and all(os.path.getmtime(target) >= os.path.getmtime(s) for s in SRCS):
+        return target
+    cmd = ["g++", *flags, "-o", target, *SRCS]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stderr}")
-    return LIB
+    return target
 
 
-_LIB = None
+def build(force: bool = False, verbose: bool = False, timing: bool = True) -> str:
+    """Compile the oracle checker (g++, OpenMP, no FP contraction) and, unless timing is
+    False, the timing-only build of the same sources."""
+    if timing:
+        _build_one(TIMING_LIB, TIMING_FLAGS, force, verbose)
+    return _build_one(LIB, CHECK_FLAGS, force, verbose)
 
 
-def lib():
-    global _LIB
-    if _LIB is None:
-        if not os.path.exists(LIB):
-            build()
-        L = C.CDLL(LIB)
+_LIBS = {}
+
+
+def lib(timing: bool = False):
+    """The checker library, or with timing=True the timing-only build (CPU baselines)."""
+    path = TIMING_LIB if timing else LIB
+    if path not in _LIBS:
+        if not os.path.exists(path):
+            _build_one(path, TIMING_FLAGS if timing else CHECK_FLAGS, False, False)
+        L = C.CDLL(path)
         for name, res, args in _SIGS:
             fn = getattr(L, name)
             fn.restype = res
             fn.argtypes = args
-        _LIB = L
-    return _LIB
+        _LIBS[path] = L
+    return _LIBS[path]
+
+
+def build_flags(timing: bool = False) -> str:
+    return " ".join(TIMING_FLAGS if timing else CHECK_FLAGS)
 
 
 def _d(a):
@@ -115,8 +139,8 @@ def _p(a, t=C.c_double):
     return a.ctypes.data_as(C.POINTER(t))
 
 
-def set_threads(n: int) -> int:
-    return lib().orc_set_threads(int(n))
+def set_threads(n: int, timing: bool = False) -> int:
+    return lib(timing).orc_set_threads(int(n))
 
 
 def _f(a):
@@ -134,7 +158,7 @@ def stress2strain(lam, mu, stress):
     return out.reshape(st.shape)
 
 
-def sgt2scatter3(lam, mu, rsgt, ssgt, dt, nt1=None, nt2=None, mode=1, param=0):
+def sgt2scatter3(lam, mu, rsgt, ssgt, dt, nt1=None, nt2=None, mode=1, param=0, timing=False):
     """rsgt: [X, Y, Z] receiver SGT stresses (6, knt, npts) or None; ssgt the source SGT.
     mode 0: the reference's FP32 arithmetic; mode 1: FP64 accumulation.  param 0: Vp/Vs
     kernels (SI_ker_sta.F90:1297-1298); param 1: lambda/mu kernels (SI_ker_sta_lamu.F90:
@@ -148,7 +172,7 @@ def sgt2scatter3(lam, mu, rsgt, ssgt, dt, nt1=None, nt2=None, mode=1, param=0):
     out = np.zeros(6 * knt * npts, np.float64)
     lam_, mu_ = _f(lam), _f(mu)
     ptrs = [None if r is None else _p(r, C.c_float) for r in rs]
-    lib().orc_sgt2scatter3(npts, knt, nt1, nt2, float(dt), _p(lam_, C.c_float), _p(mu_, C.c_float), *ptrs,
+    lib(timing).orc_sgt2scatter3(npts, knt, nt1, nt2, float(dt), _p(lam_, C.c_float), _p(mu_, C.c_float), *ptrs,
                            _p(s, C.c_float), int(mode), int(param), _p(out))
     return out.reshape(6, knt, npts)
 
@@ -195,7 +219,7 @@ def scatter2kernel_filtered(v, u, ka, kb, dt, nt1, nt2, sgt_m0, b, a, mode):
     return tuple(outs)
 
 
-def lsqr(row_ptr, col, val, b, ncol, atol=1e-7, btol=1e-7, maxit=30000):
+def lsqr(row_ptr, col, val, b, ncol, atol=1e-7, btol=1e-7, maxit=30000, timing=False):
     """slsqr + lgtsol of inv.LSQR/mod_LSQR.f90 on a compressed-row matrix (0-based).
     Returns dict(x, serr, sig, itct, flag, anorm, res2, test1, test2, phibar, xnorm); serr
     for all ncol unknowns."""
@@ -208,7 +232,7 @@ def lsqr(row_ptr, col, val, b, ncol, atol=1e-7, btol=1e-7, maxit=30000):
     sig = np.zeros(int(ncol))
     info = np.zeros(6)
     flag = C.c_int()
-    it = lib().orc_lsqr(nrow, int(ncol), rp.ctypes.data_as(C.POINTER(C.c_longlong)), _p(ci, C.c_int), _p(va), _p(b_),
+    it = lib(timing).orc_lsqr(nrow, int(ncol), rp.ctypes.data_as(C.POINTER(C.c_longlong)), _p(ci, C.c_int), _p(va), _p(b_),
                         float(atol), float(btol), int(maxit), _p(x), _p(sig), _p(info), C.byref(flag))
     serr = np.zeros(int(ncol))
     lib().orc_lgtsol(nrow, int(ncol), float(info[1]), _p(sig), _p(serr))
@@ -228,8 +252,8 @@ class MediaOracle:
     with the same set-up methods as `fwant_gb300.Media` (arrays in Fortran index order:
     a[i, j, k])."""
 
-    def __init__(self, ni, nj, nk, x, y, z, ztopo, half_sample=(1, 1, 1)):
-        self._L = lib()
+    def __init__(self, ni, nj, nk, x, y, z, ztopo, half_sample=(1, 1, 1), timing=False):
+        self._L = lib(timing)
         self.shape = (ni + 6, nj + 6, nk + 6)
         self._keep = [_fo(x), _fo(y), _fo(z)]
         hs = np.ascontiguousarray(half_sample, np.int32)
@@ -289,8 +313,8 @@ class MediaOracle:
 class Oracle:
     """CPU restatement of seis3d_wave; dbl=True gives the FP64 (-DDataTypeDouble) solver."""
 
-    def __init__(self, ni, nj, nk, stept, free_surface=True, src_surface=True, dbl=False):
-        self._L = lib()
+    def __init__(self, ni, nj, nk, stept, free_surface=True, src_surface=True, dbl=False, timing=False):
+        self._L = lib(timing)
         self._h = self._L.orc_create(int(ni), int(nj), int(nk), float(stept), int(bool(free_surface)), int(bool(dbl)))
         self._L.orc_set_srcsurface(self._h, int(bool(src_surface)))
         self.ni, self.nj, self.nk = int(ni), int(nj), int(nk)

@@ -59,6 +59,32 @@ def test_projection_errors(native_lib):
         a.project_device([ks[0].ctypes.data])           # a host address is refused, not read
 
 
+def test_device_volume_past_the_end_of_its_allocation_is_refused(native_lib):
+    """A device pointer whose allocation ends before ki*kj*kk floats is refused on the host
+    (cuMemGetAddressRange), before any launch could read past the allocation."""
+    import ctypes as C
+    import fwant_gb300 as fw
+    volume, npix, pixs = ac.blocks(SHAPE)
+    a = fw.Assm(SHAPE, volume, npix, pixs)
+    nvol = SHAPE[0] * SHAPE[1] * SHAPE[2]
+    rt = C.CDLL("libcudart.so.13")
+    rt.cudaMalloc.argtypes = [C.POINTER(C.c_void_p), C.c_size_t]
+    rt.cudaMemset.argtypes = [C.c_void_p, C.c_int, C.c_size_t]
+    rt.cudaFree.argtypes = [C.c_void_p]
+    size = 8 << 20                      # a multiple of the allocation granularity
+    base = C.c_void_p()
+    assert rt.cudaMalloc(C.byref(base), size) == 0
+    try:
+        assert rt.cudaMemset(base, 0, size) == 0
+        short = base.value + size - 4 * (nvol // 2)   # half a volume left in the allocation
+        with pytest.raises(fw.FwantError, match="floats past the pointer"):
+            a.project_device([short])
+        got = a.project_device([base.value])         # the whole volume fits
+        assert not np.any(got)
+    finally:
+        rt.cudaFree(base)
+
+
 def _write_kernel(path, names, vols):
     from scipy.io import netcdf_file
     os.makedirs(os.path.dirname(path), exist_ok=True)

@@ -38,3 +38,11 @@ def test_snapshot_rejects_bad_requests(native_lib):
         s.get_snapshot((4, 4, 4), (m.ni + 1, 1, 1), (1, 1, 1))  # runs past the interior
     with pytest.raises(fw.FwantError):
         s.get_snapshot((4, 4, 4), (2, 2, 2), (0, 1, 1))  # zero stride
+    # stride x (count - 1) = 2^32 wraps a 32-bit end index back to the start: every entry
+    # point that takes a sub-volume refuses it on the host, before any launch
+    wrap = dict(subs=(4, 4, 4), subc=(65537, 1, 1), subt=(65536, 1, 1))
+    for call in (lambda: s.get_snapshot(**wrap), lambda: s.get_snapshot_noalloc(**wrap),
+                 lambda: s.set_sgt_record(wrap["subs"], wrap["subc"], wrap["subt"], 1, 4)):
+        with pytest.raises(fw.FwantError) as e:
+            call()
+        assert e.value.code == 1
