@@ -73,7 +73,11 @@ constexpr int STAGE_TX = 32, STAGE_TY = 8;
 // 4-byte storage, 8 for 2-byte storage.
 constexpr int tile_halo_x(int elem_bytes) { return elem_bytes >= 4 ? 4 : 8; }
 constexpr int tile_box_x(int elem_bytes) { return STAGE_TX + 2 * tile_halo_x(elem_bytes); }
-constexpr int TILE_BY = STAGE_TY + 6;
+// Rows of the halo'd tile: a one-sided y operator reads one row on one side and three on
+// the other (forward: -1..+3, backward: -3..+1), so the box holds the CTA's rows plus
+// four; its first row is tile_halo_y(FY) rows above the CTA's first row.
+constexpr int TILE_BY = STAGE_TY + 4;
+constexpr int tile_halo_y(int fwd) { return fwd ? 1 : 3; }
 // wavefield storage kinds inside the kernels
 enum { ST_F32 = 0, ST_BF16 = 1, ST_F16 = 2 };
 constexpr int storage_bytes(int st) { return st == ST_F32 ? 4 : 2; }

@@ -14,7 +14,8 @@
 // Data movement (2.5-D, TMA pipeline): a CTA owns a 32 x 8 (i, j) tile and marches along
 // k over kc planes.  For every plane one elected thread issues TMA tensor loads
 // (cp.async.bulk.tensor) of
-//   * the stage input W around the tile (40 x 14 columns, all nine components),
+//   * the stage input W around the tile (40 x 12 columns: the halo rows on the side the
+//     one-sided y operator reads; all nine components),
 //   * the six k-differentiated components of plane k+LEAD (the z-queue feed),
 //   * lambda, mu, rho and the RK registers m and t of the tile,
 // into one of two shared-memory buffers, one plane ahead of the compute; completion is
@@ -36,7 +37,6 @@ namespace fw {
 
 constexpr int TX = STAGE_TX, TY = STAGE_TY;
 constexpr int TBY = TILE_BY;
-constexpr int HY = 3;  // row of the CTA's first row inside the tile box
 constexpr int WAIT_SPINS = 1 << 22;
 
 // Shared-memory layout of one pipeline buffer for storage type S (byte offsets,
@@ -56,7 +56,7 @@ struct Lay {
   static constexpr int SZ_PT = NF * TY * TX * ES;
   static constexpr int OFF_T = OFF_M + SZ_PT;
   static constexpr int BUF_BYTES = ((OFF_T + SZ_PT + 1023) / 1024) * 1024;
-  static constexpr int SMEM_BYTES = 2 * BUF_BYTES + 64;
+  static constexpr int SMEM_BYTES = 2 * BUF_BYTES + 64;  // + the mbarriers (up to 5 x 8 bytes)
   // Interior-only (lean) form: the tile holds the eight x/y-differentiated components
   // (Tzz comes from the z queue) as two boxes, components 0-2 and 4-8, each starting on a
   // 128-byte boundary; the RK registers m and t of the current plane are staged in one
@@ -259,6 +259,7 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
   constexpr int BUF_BYTES = LEAN ? L::BUF_BYTES_LEAN : L::BUF_BYTES, OFF_Q = LEAN ? L::OFF_Q_L : L::OFF_Q,
                 OFF_MED = LEAN ? L::OFF_MED_L : L::OFF_MED, OFF_M = L::OFF_M, OFF_T = L::OFF_T;
   constexpr int OFF_BAR = LEAN ? L::OFF_MT_L + L::template SZ_MT_L<RK> : 2 * L::BUF_BYTES;
+  constexpr int HY = FY ? 1 : 3;  // row of the CTA's first row inside the tile box (tile_halo_y)
   const Geom& g = A.g;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
   const int i0 = g.i1 + bx * TX, j0 = g.j1 + by * TY;
@@ -292,16 +293,25 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
 
   constexpr int LEAD = FZ ? 3 : 1;   // planes ahead of k in the z operator
   constexpr int TRAIL = FZ ? 1 : 3;  // planes behind k
-  constexpr uint32_t TX_BYTES = (LEAN ? 8 * L::SZ_PLANE : L::SZ_TILE) + L::SZ_Q + L::SZ_MED +
-                                 (!LEAN && RK == 1 ? L::SZ_PT : 0) + (!LEAN && RK >= 1 ? L::SZ_PT : 0);
+  // Full form, RK inn/fin: the RK registers of a plane complete on a barrier of their own
+  // (one per buffer), so the stencil starts as soon as the tile, the z-queue plane and the
+  // medium are in, while m and t are still arriving; they are waited for at the RK update.
+  constexpr bool SPLIT = !LEAN && RK >= 1;
+  constexpr uint32_t TX_BYTES = (LEAN ? 8 * L::SZ_PLANE : L::SZ_TILE) + L::SZ_Q + L::SZ_MED;
+  constexpr uint32_t RKR_BYTES = SPLIT ? (RK == 1 ? 2 : 1) * L::SZ_PT : 0;
   constexpr uint32_t MT_BYTES = L::template SZ_MT_L<RK>;  // lean: m and t of one plane
 
   const uint32_t bar0 = smem_u32(smem + OFF_BAR);
   const uint32_t bar_mt = bar0 + 16;
+  auto bar_rk = [&](int b) -> uint32_t { return bar0 + 24 + 8 * b; };
   if (tid == 0) {
     mbar_init(bar0, 1);
     mbar_init(bar0 + 8, 1);
     if (LEAN && RK >= 1) mbar_init(bar_mt, 1);
+    if (SPLIT) {
+      mbar_init(bar_rk(0), 1);
+      mbar_init(bar_rk(1), 1);
+    }
     fence_barrier_init();
   }
   __syncthreads();
@@ -322,8 +332,12 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
     // plane kp+LEAD comes back as the tile of a later iteration: keep it in L2
     tma_load_4d_hint(base + OFF_Q, &A.tm_q, i0 + PADL, j0, kp + LEAD, 0, bar, pol_keep);
     tma_load_4d_hint(base + OFF_MED, &A.tm_med, i0 + PADL, j0, kp, 0, bar, pol_stream);
-    if (!LEAN && RK == 1) tma_load_4d_hint(base + OFF_M, &A.tm_m, i0 + PADL, j0, kp, 0, bar, pol_stream);
-    if (!LEAN && RK >= 1) tma_load_4d_hint(base + OFF_T, &A.tm_t, i0 + PADL, j0, kp, 0, bar, pol_stream);
+    if (SPLIT) {
+      const uint32_t brk = bar_rk(b);
+      mbar_expect_tx(brk, RKR_BYTES);
+      if (RK == 1) tma_load_4d_hint(base + OFF_M, &A.tm_m, i0 + PADL, j0, kp, 0, brk, pol_stream);
+      tma_load_4d_hint(base + OFF_T, &A.tm_t, i0 + PADL, j0, kp, 0, brk, pol_stream);
+    }
   };
   if (tid == 0) issue(kb, 0);
   // lean form: m and t of plane kp into the single RK buffer
@@ -700,6 +714,7 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
 
       // ---- RK update (mod_macdrp.F90:291-393); m of stage 1 is the stored input value
       if (LEAN && RK >= 1) ok_mt = mbar_wait(bar_mt, it & 1);
+      if (SPLIT) ok_mt = mbar_wait(bar_rk(cur), (it >> 1) & 1);
       float hh[NF];
       hh[VX] = hVx; hh[VY] = hVy; hh[VZ] = hVz; hh[TZZ] = hTzz; hh[TXZ] = hTxz; hh[TYZ] = hTyz;
       hh[TXX] = hTxx; hh[TYY] = hTyy; hh[TXY] = hTxy;
@@ -727,6 +742,10 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
         atomicExch(A.err, DEVERR_TMA_TIMEOUT);
         if (k < ke) mbar_wait(bar0 + 8 * (cur ^ 1), ((it + 1) >> 1) & 1);  // copies still in flight
         if (LEAN && RK >= 1) mbar_wait(bar_mt, it & 1);
+        if (SPLIT) {
+          mbar_wait(bar_rk(cur), (it >> 1) & 1);
+          if (k < ke) mbar_wait(bar_rk(cur ^ 1), ((it + 1) >> 1) & 1);
+        }
       }
       return false;
     }
@@ -736,6 +755,10 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
     mbar_inval(bar0);
     mbar_inval(bar0 + 8);
     if (LEAN && RK >= 1) mbar_inval(bar_mt);
+    if (SPLIT) {
+      mbar_inval(bar_rk(0));
+      mbar_inval(bar_rk(1));
+    }
   }
   return true;
 }

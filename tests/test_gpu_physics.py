@@ -1,0 +1,52 @@
+"""The physics checks of test_physics_oracle.py on the GPU's fast arithmetic form, with
+finer levels than the CPU can afford: the reciprocity asymmetry of the horizontal-vertical
+pairs must keep shrinking at a 0.25 km surface spacing, and the convergence study adds a
+0.125 km level (257^3 points)."""
+import numpy as np
+import pytest
+
+import physics as P
+
+pytestmark = pytest.mark.gpu
+
+
+def _make():
+    import fwant_gb300 as fw
+    return lambda ni, nj, nk, stept, fs: fw.Solver(ni, nj, nk, stept, free_surface=fs)
+
+
+def test_reciprocity_of_surface_forces_gpu(native_lib):
+    errs = {}
+    for top, bottom, nk in ((1.0, 1.0, 24), (0.5, 2.0, 28), (0.25, 2.0, 36)):
+        m, a, b, nsteps = P.reciprocity_model(z_top_km=top, z_bottom_km=bottom, nk=nk)
+        g = P.reciprocity_gathers(_make(), m, a, b, nsteps)
+        errs[top] = P.reciprocity_errors(g, a, b)
+        print(top, {k: round(v, 4) for k, v in errs[top].items()})
+    for k in (("x", "x"), ("y", "y"), ("z", "z"), ("x", "y"), ("y", "x")):
+        assert errs[0.5][k] < 0.01 and errs[0.25][k] < 0.01, k
+    for k in (("x", "z"), ("z", "x"), ("y", "z"), ("z", "y")):
+        assert errs[0.5][k] < 0.10, k
+        assert errs[1.0][k] > 1.6 * errs[0.5][k], k
+        assert errs[0.25][k] < errs[0.5][k], k
+
+
+def test_energy_decays_in_the_pml_gpu(native_lib):
+    out = {}
+    for npml in (8, 0):
+        m = P.energy_model(npml)
+        _, e = P.energy_history(_make(), m, 10, 1200, 20)
+        out[npml] = e / e.max()
+    e = out[8]
+    peak = int(np.argmax(e))
+    after = e[peak:]
+    assert np.all(after[1:] <= after[:-1] * (1 + 1e-3)), after
+    assert after[-1] < 1e-7
+    assert out[0][-1] > 100 * after[-1]
+
+
+def test_convergence_under_refinement_gpu(native_lib):
+    sols = [P.convergence_solution(_make(), level) for level in range(4)]
+    errs, orders = P.convergence_orders(sols)
+    print("differences", errs, "orders", orders)
+    assert all(errs[l + 1] < errs[l] for l in range(len(errs) - 1))
+    assert min(orders) > 1.2

@@ -72,8 +72,13 @@ def test_stf_id_against_oracle(kind, stf_id, runs, exact, oracle_mod, native_lib
         live += 1
         assert rel_l2(a, b) < tol, f"component {c}: {rel_l2(a, b):.3e}"
     assert live > 0, "the source never acted"
-    sg, so = g.get_seismo(), o.get_seismo()
+    # Seismogram errors relative to the norm of their group (velocities, stresses): the
+    # free-surface condition holds Tzz, Txz and Tyz of surface receivers at rounding level
+    # away from the source, and a component-wise ratio of two rounding residues says nothing.
+    sg, so = g.get_seismo().astype(np.float64), o.get_seismo()
     assert sg.shape == so.shape
-    for c in range(9):
-        if np.any(so[c]):
-            assert rel_l2(sg[c], so[c]) < tol, f"seismogram {c}: {rel_l2(sg[c], so[c]):.3e}"
+    for grp in (slice(0, 3), slice(3, 9)):
+        den = np.sqrt(np.sum(so[grp] ** 2))
+        for c in range(grp.start, grp.stop):
+            e = np.sqrt(np.sum((sg[c] - so[c]) ** 2)) / den
+            assert e < tol, f"seismogram {c}: {e:.3e} of its group's norm"
