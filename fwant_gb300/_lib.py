@@ -42,6 +42,8 @@ EXPORTS = [
     ("fwant_set_coord", C.c_int, [_vp, _fp, _fp, _fp]),
     ("fwant_set_metric", C.c_int, [_vp, _fp, _fp, _fp, _fp, _fp]),
     ("fwant_compute_metric", C.c_int, [_vp]),
+    ("fwant_set_topography", C.c_int, [_vp, _fp]),
+    ("fwant_get_topography_array", C.c_int, [_vp, C.c_int, _fp]),
     ("fwant_get_metric", C.c_int, [_vp, _fp, _fp, _fp, _fp, _fp]),
     ("fwant_metric_arrays", C.c_int, [C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, C.c_int, _fp, _fp, _fp, _fp, _fp]),
     ("fwant_set_media", C.c_int, [_vp, _fp, _fp, _fp]),
@@ -338,6 +340,31 @@ class Solver:
         self._chk(self._lib.fwant_get_seismo(self._h, _ptr(out), int(max_samples), C.byref(ns)))
         n = ns.value
         return out[: 9 * n * self.num_pt].reshape(9, n, self.num_pt)
+
+    def set_topography(self, h):
+        """Terrain-following grid: heights h (nx, ny) in m, r = z(k) + h s(k) (after the
+        coordinates and the metric)."""
+        a = _f32(np.asarray(h, np.float32).reshape(-1, order="F"), self.nx * self.ny)
+        self._chk(self._lib.fwant_set_topography(self._h, _ptr(a)))
+
+    def topography_array(self, which):
+        """0..3: (nx, ny, nz) r, zeta_r, zeta_theta/r, zeta_phi/(r sin theta); 4, 5: the
+        surface normal's m1, m2 (nx, ny); 6: the traction-condition inverses (nx, ny, 9)."""
+        n2 = self.nx * self.ny
+        if which < 4:
+            out = np.zeros(n2 * self.nz, np.float32)
+            self._chk(self._lib.fwant_get_topography_array(self._h, int(which), _ptr(out)))
+            return out.reshape(self.shape, order="F")
+        if which < 6:
+            out = np.zeros(n2, np.float32)
+            self._chk(self._lib.fwant_get_topography_array(self._h, int(which), _ptr(out)))
+            return out.reshape(self.nx, self.ny, order="F")
+        outs = []
+        for e in range(9):
+            o = np.zeros(n2, np.float32)
+            self._chk(self._lib.fwant_get_topography_array(self._h, 6 + e, _ptr(o)))
+            outs.append(o.reshape(self.nx, self.ny, order="F"))
+        return np.stack(outs, axis=-1)
 
     def get_field(self, component):
         c = COMPONENTS.index(component) if isinstance(component, str) else int(component)

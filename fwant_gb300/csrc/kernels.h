@@ -89,8 +89,17 @@ struct StageArgs {
   CUtensorMap tm_m;     // RK register m: box TX x TY x 1 x 9
   CUtensorMap tm_t;     // RK register t: box TX x TY x 1 x 9
   CUtensorMap tm_med;   // lambda, mu, rho: box TX x TY x 1 x 3
-  CUtensorMap tm_tile_lo;  // stage input W, lean form: box TILE_BX x TILE_BY x 1 x 3 (Vx Vy Vz)
+  // The lean form's tile boxes; the terrain form (never lean) uses the first slot for the
+  // terrain-following grid's per-point 1/r, zeta_r, zeta_theta / r, zeta_phi / (r sin theta)
+  // (box TX x TY x 1 x 4).
+  union {
+    CUtensorMap tm_tile_lo;  // stage input W, lean form: box TILE_BX x TILE_BY x 1 x 3 (Vx Vy Vz)
+    CUtensorMap tm_topo;
+  };
   CUtensorMap tm_tile_hi;  // stage input W, lean form: box TILE_BX x TILE_BY x 1 x 5 (Txz .. Txy)
+  // terrain form: per surface column (padded plane layout, g.plane apart) m1, m2 of the
+  // surface normal and the row-major 3x3 inverse of the traction condition (11 planes)
+  const float* topo_sf;
   Geom g;
   const void* win;    // stage input W (9 components, storage type)
   void* wout;         // stage output W
@@ -146,6 +155,29 @@ static_assert(sizeof(BatchArgs) <= 32764, "kernel parameter space");
 // lean = 1: the interior-only form (items without PML points, sources or free surface).
 int launch_stage_batch(const BatchArgs& b, int variant, int rk, int exact, int storage, int lean, int ctas,
                        void* stream);
+// The terrain form (FP32 storage, full form only; exact = 1 the reference-order arithmetic).
+int launch_stage_batch_topo(const BatchArgs& b, int variant, int rk, int exact, int ctas, void* stream);
+// FP64 metric of the terrain-following grid (r = z + h s): per point r, zeta_r,
+// zeta_theta / r, zeta_phi / (r sin theta) into out (4 components fstride apart), from
+// float heights h (nx*ny, i fastest), the 1-D arrays (0-based Fortran index with ghosts)
+// and the double tables s(k), z_zeta(k).
+struct TopoMetricArgs {
+  Geom g;
+  const float* h;        // [ny][nx]
+  const double* hxi;     // [ny][nx] dh/dxi
+  const double* heta;    // [ny][nx] dh/deta
+  const float* z; const float* xi_x; const float* eta_y; const float* zeta_z; const float* xsin;
+  const double* sk;      // [nz]
+  const double* rzf;     // [nz]
+  float* out;
+};
+void launch_topo_metric(const TopoMetricArgs& a, void* stream);
+// Surface arrays (11 planes of the padded plane layout): m1, m2, the 3x3 inverse, from the
+// metric at k = nk2 and the medium's lambda, mu there (FP64).
+void launch_topo_surface(const Geom& g, const float* metric, const float* lam, const float* mu, float* out,
+                         void* stream);
+// dh/dxi, dh/deta of the heights (FP64, the metric's stencil with clamped ends)
+void launch_topo_slopes(const Geom& g, const float* h, double* hxi, double* heta, void* stream);
 // Work items of one simulation split into the lean (interior) list and the full list.
 // force_c / mom_c: 0-based source centres (3 per source).
 void stage_items(const Geom& g, int kc, const Slab slab[6], const int* force_c, int nforce, const int* mom_c,

@@ -117,6 +117,15 @@ struct fwant_solver {
   fw::SgtRecArgs sgt{};
   bool sgt_on = false;
 
+  // terrain-following grid (Gaussian-hill extension): heights, their FP64 slopes, the
+  // per-point metric (4 components, fstride apart) and the 11 surface planes
+  bool topo_on = false, topo_sf_dirty = true;
+  float* d_h = nullptr;
+  double *d_hxi = nullptr, *d_heta = nullptr, *d_sk = nullptr, *d_rzf = nullptr;
+  float* d_topo = nullptr;
+  float* d_topo_sf = nullptr;
+  CUtensorMap tm_topo{};
+
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one per (rA,rT) assignment
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;
@@ -130,6 +139,7 @@ struct fwant_solver {
     cudaFree(d_xi); cudaFree(d_eta); cudaFree(d_zeta); cudaFree(d_prof); cudaFree(d_rzinv); cudaFree(d_rsinv);
     for (int f = 0; f < 6; ++f) cudaFree(aux[f]);
     cudaFree(d_rec); cudaFree(d_seis); cudaFree(d_ntime); cudaFree(d_maxbits); cudaFree(d_snap); cudaFree(d_conv); cudaFree(d_sgt); cudaFree(d_items);
+    cudaFree(d_h); cudaFree(d_hxi); cudaFree(d_heta); cudaFree(d_sk); cudaFree(d_rzf); cudaFree(d_topo); cudaFree(d_topo_sf);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (st) cudaStreamDestroy(st);
@@ -673,7 +683,7 @@ struct fwant_solver {
   }
   // Items of one launch of RK kind rk: lean = 1 the interior items, lean = 0 the others,
   // or all items in launch order when the lean form is off for rk.
-  bool lean_on(int rk) const { return (lean_mask >> rk & 1) != 0; }
+  bool lean_on(int rk) const { return !topo_on && (lean_mask >> rk & 1) != 0; }
   const int* items(bool lean, int rk) const {
     if (!lean_on(rk)) return d_items + n_lean + n_full;
     return d_items + (lean ? 0 : n_lean);
@@ -693,6 +703,11 @@ struct fwant_solver {
     a.win = set(in_of[s]); a.wout = set(out_of[s]); a.wt = set(rt); a.wm = set(ra);
     a.tm_tile = tm_tile[in_of[s]]; a.tm_q = tm_q[in_of[s]]; a.tm_m = tm_pt[ra]; a.tm_t = tm_pt[rt];
     a.tm_tile_lo = tm_tile_lo[in_of[s]]; a.tm_tile_hi = tm_tile_hi[in_of[s]];
+    if (topo_on) {  // the terrain form queues all nine components
+      a.tm_q = tm_pt[in_of[s]];
+      a.tm_topo = tm_topo;
+      a.topo_sf = d_topo_sf;
+    }
     for (int f = 0; f < 6; ++f) {
       if (!slab[f].on) continue;
       a.ain[f] = aset(f, in_of[s]); a.am[f] = aset(f, ra); a.aout[f] = aset(f, out_of[s]); a.at[f] = aset(f, rt);
@@ -751,6 +766,7 @@ struct fwant_solver {
     put(&n_lean, sizeof(n_lean));
     put(&n_full, sizeof(n_full));
     put(&lean_mask, sizeof(lean_mask));
+    put(&topo_on, sizeof(topo_on));
   }
   void finish_step_host() {
     std::swap(rA, rT);
@@ -774,8 +790,10 @@ struct fwant_solver {
         b.off[0] = 0;
         b.off[1] = cnt;
         b.total = cnt;
-        const int le = fw::launch_stage_batch(b, stage_variant(cycle_pos, s), stage_rk(s), cfg.exact_arith, stor,
-                                              lean, cnt, st);
+        const int le = topo_on ? fw::launch_stage_batch_topo(b, stage_variant(cycle_pos, s), stage_rk(s),
+                                                             cfg.exact_arith, cnt, st)
+                               : fw::launch_stage_batch(b, stage_variant(cycle_pos, s), stage_rk(s), cfg.exact_arith,
+                                                        stor, lean, cnt, st);
         if (le && !lerr) lerr = le;
       }
     }
@@ -825,6 +843,94 @@ struct fwant_solver {
     return FWANT_OK;
   }
 
+  // ---- terrain-following grid (Gaussian-hill extension) ----------------------------------
+  // Metric of r = z(k) + h(i,j) s(k) from the current coordinates and 1-D metric (FP64 on
+  // the device); s(k) and z_zeta(k) are formed here in double, in the order the CPU
+  // restatement uses.
+  fwant_status topo_compute() {
+    const int nz = g.nz;
+    std::vector<double> zd(nz), sk(nz), rzf(nz);
+    for (int k = 0; k < nz; ++k) zd[k] = double(hz[k]);
+    const double cF[5] = {-0.30874, -0.6326, 1.2330, -0.3334, 0.04168};
+    const double cB[5] = {-0.04168, 0.3334, -1.2330, 0.6326, 0.30874};
+    for (int k = 0; k < nz; ++k) {
+      sk[k] = (zd[k] - zd[0]) / (zd[g.k2] - zd[0]);
+      const int kk = std::min(std::max(k, g.k1), g.k2);
+      double sb = 0.0, sf = 0.0;
+      for (int q = 0; q < 5; ++q) {
+        sb = sb + zd[kk - 3 + q] * cB[q];
+        sf = sf + zd[kk - 1 + q] * cF[q];
+      }
+      rzf[k] = (sb + sf) * 0.5;
+    }
+    cudaError_t e = cudaMemcpy(d_sk, sk.data(), nz * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_rzf, rzf.data(), nz * sizeof(double), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "topography tables");
+    fw::launch_topo_slopes(g, d_h, d_hxi, d_heta, st);
+    fw::TopoMetricArgs a{};
+    a.g = g; a.h = d_h; a.hxi = d_hxi; a.heta = d_heta;
+    a.z = d_z; a.xi_x = d_xi; a.eta_y = d_eta; a.zeta_z = d_zeta; a.xsin = d_xsin;
+    a.sk = d_sk; a.rzf = d_rzf; a.out = d_topo;
+    fw::launch_topo_metric(a, st);
+    e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "topography metric");
+    topo_sf_dirty = true;
+    drop_graphs();
+    return FWANT_OK;
+  }
+
+  fwant_status set_topography(const float* h) {
+    if (!have_coord || !have_metric)
+      return fail(FWANT_ERR_STATE, "fwant_set_topography needs the coordinates and the metric first");
+    if (stor != fw::ST_F32) return fail(FWANT_ERR_INVALID_ARG, "the terrain-following grid runs with FP32 storage");
+    for (size_t q = 0; q < size_t(g.nx) * g.ny; ++q)
+      if (!std::isfinite(h[q])) return fail(FWANT_ERR_INVALID_ARG, "topography: non-finite height");
+    const size_t n2 = size_t(g.nx) * g.ny;
+    if (!d_topo) {
+      d_h = dalloc<float>(n2); d_hxi = dalloc<double>(n2); d_heta = dalloc<double>(n2);
+      d_sk = dalloc<double>(g.nz); d_rzf = dalloc<double>(g.nz);
+      d_topo = dalloc<float>(4 * size_t(g.fstride));
+      d_topo_sf = dalloc<float>(11 * size_t(g.plane));
+      if (!d_h || !d_hxi || !d_heta || !d_sk || !d_rzf || !d_topo || !d_topo_sf)
+        return fail(FWANT_ERR_OOM, "topography arrays");
+      cudaMemset(d_topo, 0, 4 * size_t(g.fstride) * sizeof(float));
+      cudaMemset(d_topo_sf, 0, 11 * size_t(g.plane) * sizeof(float));
+      using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+      void* fn = nullptr;
+      cudaDriverEntryPointQueryResult qr;
+      if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &qr) !=
+              cudaSuccess || !fn || qr != cudaDriverEntryPointSuccess)
+        return fail(FWANT_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+      const cuuint64_t dims[4] = {cuuint64_t(g.px), cuuint64_t(g.ny), cuuint64_t(g.nz), 4};
+      const cuuint64_t strides[3] = {cuuint64_t(g.px) * 4, cuuint64_t(g.plane) * 4, cuuint64_t(g.fstride) * 4};
+      const cuuint32_t box[4] = {fw::STAGE_TX, fw::STAGE_TY, 1, 4};
+      const cuuint32_t el[4] = {1, 1, 1, 1};
+      if (reinterpret_cast<EncodeFn>(fn)(&tm_topo, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, d_topo, dims, strides, box, el,
+                                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                         CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return fail(FWANT_ERR_CUDA, "tensor map encoding failed");
+    }
+    cudaError_t e = cudaMemcpy(d_h, h, n2 * sizeof(float), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "topography upload");
+    topo_on = true;
+    return topo_compute();
+  }
+
+  // surface arrays of the terrain form (they need the medium)
+  fwant_status topo_prepare() {
+    if (!topo_on || !topo_sf_dirty) return FWANT_OK;
+    fw::launch_topo_surface(g, d_topo, lam, mu, d_topo_sf, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "topography surface arrays");
+    topo_sf_dirty = false;
+    return FWANT_OK;
+  }
+
   fwant_status run(int nsteps) {
     if (nsteps < 0) return fail(FWANT_ERR_INVALID_ARG, "nsteps < 0");
     if (!have_coord || !have_metric || !have_media)
@@ -834,6 +940,7 @@ struct fwant_solver {
     if (rc != FWANT_OK) return rc;
     if ((rc = prepare_receivers(ntime + nsteps)) != FWANT_OK) return rc;
     if ((rc = ensure_items()) != FWANT_OK) return rc;
+    if ((rc = topo_prepare()) != FWANT_OK) return rc;
     cudaEventRecord(ev0, st);
     int left = nsteps;
     while (left > 0) {
@@ -902,6 +1009,7 @@ struct fwant_solver {
     if (rc != FWANT_OK) return rc;
     if ((rc = prepare_receivers(ntime + nsteps)) != FWANT_OK) return rc;
     if ((rc = ensure_items()) != FWANT_OK) return rc;
+    if ((rc = topo_prepare()) != FWANT_OK) return rc;
     std::vector<cudaEvent_t> ev(size_t(6) * nsteps);
     for (auto& e : ev) cudaEventCreate(&e);
     int lerr = 0;
@@ -969,7 +1077,7 @@ fwant_status fwant_set_coord(fwant_solver* s, const float* x, const float* y, co
   if (e != cudaSuccess) return s->cuda_fail(e, "set_coord");
   s->have_coord = true;
   s->src_dirty = true;
-  return FWANT_OK;
+  return (s->topo_on && s->have_metric) ? s->topo_compute() : FWANT_OK;
 }
 
 fwant_status fwant_set_metric(fwant_solver* s, const float* xsin, const float* xcot, const float* xi_x,
@@ -986,7 +1094,7 @@ fwant_status fwant_set_metric(fwant_solver* s, const float* xsin, const float* x
   if (e != cudaSuccess) return s->cuda_fail(e, "set_metric");
   s->have_metric = true;
   s->src_dirty = true;
-  return FWANT_OK;
+  return s->topo_on ? s->topo_compute() : FWANT_OK;
 }
 
 fwant_status fwant_compute_metric(fwant_solver* s) {
@@ -1006,7 +1114,30 @@ fwant_status fwant_compute_metric(fwant_solver* s) {
   cudaMemcpy(s->hxcot.data(), s->d_xcot, g.nx * 4, cudaMemcpyDeviceToHost);
   s->have_metric = true;
   s->src_dirty = true;
-  return FWANT_OK;
+  return s->topo_on ? s->topo_compute() : FWANT_OK;
+}
+
+fwant_status fwant_set_topography(fwant_solver* s, const float* h) {
+  if (!s || !h) return FWANT_ERR_INVALID_ARG;
+  cudaSetDevice(s->cfg.device);
+  return s->set_topography(h);
+}
+
+fwant_status fwant_get_topography_array(fwant_solver* s, int which, float* out) {
+  if (!s || !out || which < 0 || which > 14) return FWANT_ERR_INVALID_ARG;
+  if (!s->topo_on) return s->fail(FWANT_ERR_STATE, "no topography set");
+  cudaSetDevice(s->cfg.device);
+  fwant_status rc = s->topo_prepare();
+  if (rc != FWANT_OK) return rc;
+  const auto& g = s->g;
+  cudaError_t e;
+  if (which < 4) {
+    e = s->get3(out, s->d_topo + size_t(which) * g.fstride);
+  } else {
+    e = cudaMemcpy2D(out, size_t(g.nx) * 4, s->d_topo_sf + size_t(which - 4) * g.plane + fw::PADL, size_t(g.px) * 4,
+                     size_t(g.nx) * 4, size_t(g.ny), cudaMemcpyDeviceToHost);
+  }
+  return e == cudaSuccess ? FWANT_OK : s->cuda_fail(e, "get_topography_array");
 }
 
 fwant_status fwant_metric_arrays(int ni, int nj, int nk, const float* x, const float* y, const float* z, int device,
@@ -1109,6 +1240,7 @@ static fwant_status load_media(fwant_solver* s, const float* lambda, const float
   cudaFree(staging);
   if (e != cudaSuccess) return s->cuda_fail(e, "set_media");
   s->have_media = true;
+  s->topo_sf_dirty = true;
   s->src_dirty = true;
   return FWANT_OK;
 }
@@ -1911,6 +2043,7 @@ fwant_status fwant_batch_create(fwant_solver* const* sims, int n, fwant_batch** 
     if (sims[q]->cfg.device != sims[0]->cfg.device || sims[q]->stor != sims[0]->stor ||
         sims[q]->cfg.exact_arith != sims[0]->cfg.exact_arith)
       return FWANT_ERR_INVALID_ARG;
+    if (sims[q]->topo_on) return FWANT_ERR_INVALID_ARG;  // terrain-following grids step alone
   }
   auto* b = new fwant_batch();
   b->sims.assign(sims, sims + n);

@@ -19,6 +19,27 @@ FW_DECL(exact)
 FW_DECL(bf16)
 FW_DECL(fp16)
 #undef FW_DECL
+#define FW_DECL_TOPO(mode)                                                  \
+  int launch_stage_batch_##mode##_rk0(const BatchArgs&, int, int, cudaStream_t); \
+  int launch_stage_batch_##mode##_rk1(const BatchArgs&, int, int, cudaStream_t); \
+  int launch_stage_batch_##mode##_rk2(const BatchArgs&, int, int, cudaStream_t); \
+  int configure_stage_##mode##_rk0();                                           \
+  int configure_stage_##mode##_rk1();                                           \
+  int configure_stage_##mode##_rk2();
+FW_DECL_TOPO(topo)
+FW_DECL_TOPO(topo_exact)
+#undef FW_DECL_TOPO
+
+int launch_stage_batch_topo(const BatchArgs& b, int variant, int rk, int exact, int ctas, void* stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  if (exact)
+    return rk == 0 ? launch_stage_batch_topo_exact_rk0(b, variant, ctas, st)
+                   : (rk == 1 ? launch_stage_batch_topo_exact_rk1(b, variant, ctas, st)
+                              : launch_stage_batch_topo_exact_rk2(b, variant, ctas, st));
+  return rk == 0 ? launch_stage_batch_topo_rk0(b, variant, ctas, st)
+                 : (rk == 1 ? launch_stage_batch_topo_rk1(b, variant, ctas, st)
+                            : launch_stage_batch_topo_rk2(b, variant, ctas, st));
+}
 
 int launch_stage_batch(const BatchArgs& b, int variant, int rk, int exact, int storage, int lean, int ctas,
                        void* stream) {
@@ -38,7 +59,10 @@ int stage_configure() {
   int (*const fns[])() = {configure_stage_fast_rk0, configure_stage_fast_rk1, configure_stage_fast_rk2,
                           configure_stage_exact_rk0, configure_stage_exact_rk1, configure_stage_exact_rk2,
                           configure_stage_bf16_rk0, configure_stage_bf16_rk1, configure_stage_bf16_rk2,
-                          configure_stage_fp16_rk0, configure_stage_fp16_rk1, configure_stage_fp16_rk2};
+                          configure_stage_fp16_rk0, configure_stage_fp16_rk1, configure_stage_fp16_rk2,
+                          configure_stage_topo_rk0, configure_stage_topo_rk1, configure_stage_topo_rk2,
+                          configure_stage_topo_exact_rk0, configure_stage_topo_exact_rk1,
+                          configure_stage_topo_exact_rk2};
   for (auto fn : fns)
     if (int e = fn()) return e;
   return 0;

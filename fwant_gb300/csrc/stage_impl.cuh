@@ -42,17 +42,22 @@ constexpr int WAIT_SPINS = 1 << 22;
 // Shared-memory layout of one pipeline buffer for storage type S (byte offsets,
 // 128-byte aligned).  The tile box starts HX columns left of the CTA's first column so
 // that its x origin stays 16-byte aligned (4 columns of 4 bytes, 8 columns of 2 bytes).
-template <class S>
+// TOPO (terrain-following grid): the z queue holds all nine components, and the plane's
+// terrain metric (r, zeta_r, zeta_theta/r, zeta_phi/(r sin theta)) follows the medium.
+template <class S, bool TOPO = false>
 struct Lay {
   static constexpr int ES = sizeof(S);
   static constexpr int HX = tile_halo_x(ES);
   static constexpr int TBX = tile_box_x(ES);
   static constexpr int SZ_TILE = NF * TBY * TBX * ES;
   static constexpr int OFF_Q = ((SZ_TILE + 127) / 128) * 128;
-  static constexpr int SZ_Q = 6 * TY * TX * ES;
+  static constexpr int NQ = TOPO ? NF : 6;  // components of the z queue
+  static constexpr int SZ_Q = NQ * TY * TX * ES;
   static constexpr int OFF_MED = OFF_Q + SZ_Q;
   static constexpr int SZ_MED = 3 * TY * TX * 4;  // the medium stays FP32
-  static constexpr int OFF_M = OFF_MED + SZ_MED;
+  static constexpr int OFF_TOPO = OFF_MED + SZ_MED;
+  static constexpr int SZ_TOPO = TOPO ? 4 * TY * TX * 4 : 0;
+  static constexpr int OFF_M = OFF_TOPO + SZ_TOPO;
   static constexpr int SZ_PT = NF * TY * TX * ES;
   static constexpr int OFF_T = OFF_M + SZ_PT;
   static constexpr int BUF_BYTES = ((OFF_T + SZ_PT + 1023) / 1024) * 1024;
@@ -251,10 +256,12 @@ __device__ __forceinline__ float surf_val(const Sources& S, const float* tab, in
 // surface (the host classifies the items); that code is compiled out, and the RK
 // registers m and t are read from global memory instead of being staged, so that the
 // lean form fits three CTAs per SM (registers and shared memory).
-template <class S, bool EXACT, int FX, int FY, int FZ, int RK, bool LEAN>
+template <class S, bool EXACT, int FX, int FY, int FZ, int RK, bool LEAN, bool TOPO>
 __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, int bz, unsigned char* smem) {
   static_assert(!EXACT || is_f32_v<S>, "the reference-order form exists for FP32 storage only");
-  using L = Lay<S>;
+  static_assert(!TOPO || (is_f32_v<S> && !LEAN), "the terrain form is FP32, full form");
+  using L = Lay<S, TOPO>;
+  constexpr int NQ = L::NQ;
   constexpr int TBX = L::TBX, HX = L::HX;
   constexpr int BUF_BYTES = LEAN ? L::BUF_BYTES_LEAN : L::BUF_BYTES, OFF_Q = LEAN ? L::OFF_Q_L : L::OFF_Q,
                 OFF_MED = LEAN ? L::OFF_MED_L : L::OFF_MED, OFF_M = L::OFF_M, OFF_T = L::OFF_T;
@@ -297,7 +304,7 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
   // (one per buffer), so the stencil starts as soon as the tile, the z-queue plane and the
   // medium are in, while m and t are still arriving; they are waited for at the RK update.
   constexpr bool SPLIT = !LEAN && RK >= 1;
-  constexpr uint32_t TX_BYTES = (LEAN ? 8 * L::SZ_PLANE : L::SZ_TILE) + L::SZ_Q + L::SZ_MED;
+  constexpr uint32_t TX_BYTES = (LEAN ? 8 * L::SZ_PLANE : L::SZ_TILE) + L::SZ_Q + L::SZ_MED + L::SZ_TOPO;
   constexpr uint32_t RKR_BYTES = SPLIT ? (RK == 1 ? 2 : 1) * L::SZ_PT : 0;
   constexpr uint32_t MT_BYTES = L::template SZ_MT_L<RK>;  // lean: m and t of one plane
 
@@ -332,6 +339,7 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
     // plane kp+LEAD comes back as the tile of a later iteration: keep it in L2
     tma_load_4d_hint(base + OFF_Q, &A.tm_q, i0 + PADL, j0, kp + LEAD, 0, bar, pol_keep);
     tma_load_4d_hint(base + OFF_MED, &A.tm_med, i0 + PADL, j0, kp, 0, bar, pol_stream);
+    if (TOPO) tma_load_4d_hint(base + L::OFF_TOPO, &A.tm_topo, i0 + PADL, j0, kp, 0, bar, pol_stream);
     if (SPLIT) {
       const uint32_t brk = bar_rk(b);
       mbar_expect_tx(brk, RKR_BYTES);
@@ -358,22 +366,75 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
   }
   // value pushed into the z queue for component qf (0..5 = storage index) at plane kk
   auto qval = [&](int qf, float raw, int kk) -> float {
-    if (qf >= TZZ && fsurf && kk >= g.k2) {  // free_timg image (mod_macdrp.F90:3414-3436)
+    if (qf >= TZZ && qf <= TYZ && fsurf && kk >= g.k2) {  // free_timg image (mod_macdrp.F90:3414-3436)
       const float ts = qf == TZZ ? tsz : (qf == TXZ ? tsx : tsy);
       if (kk == g.k2) return ts;
       return 2.0f * ts - dec(W[qf * fs + col + (2 * g.k2 - kk) * plane], qf);
     }
     return raw;
   };
-
-  float q[6][5];
+  // Terrain form: the column's surface normal m = (m1, m2, 1) scaled to a unit radial
+  // part; a column slopes when m1 or m2 is non-zero (flat columns run the flat path).
+  float m1s = 0.0f, m2s = 0.0f;
+  if (TOPO && act) {
+    m1s = __ldg(A.topo_sf + col);
+    m2s = __ldg(A.topo_sf + plane + col);
+  }
+  const bool slope = TOPO && (m1s != 0.0f || m2s != 0.0f);
+  // Terrain form, one plane's nine values as the queue holds them.  In a sloping column
+  // the planes above the free surface carry the traction image G = sigma . m (slots Txz,
+  // Tyz, Tzz: G_x, G_y, G_z, antisymmetric about the surface around T*Src; slots Txx,
+  // Tyy, Txy: zero), and the surface plane's Txz, Tyz, Tzz are set so that sigma . m =
+  // T*Src there.  Flat columns take free_timg's images.
+  auto topo_img = [&](float* v, int kk) {
+    if (!(fsurf && kk >= g.k2)) return;
+    if (!slope) {
 #pragma unroll
-  for (int f = 0; f < 6; ++f) {
-    q[f][0] = 0.0f;
+      for (int f = TZZ; f <= TYZ; ++f) v[f] = qval(f, v[f], kk);
+      return;
+    }
+    if (kk == g.k2) {
+      const float sxz = tsx - m1s * v[TXX] - m2s * v[TXY];
+      const float syz = tsy - m1s * v[TXY] - m2s * v[TYY];
+      v[TXZ] = sxz;
+      v[TYZ] = syz;
+      v[TZZ] = tsz - m1s * sxz - m2s * syz;
+      return;
+    }
+    const long long pm = col + (long long)(2 * g.k2 - kk) * plane;
+    const float xx = dec(W[TXX * fs + pm], TXX), yy = dec(W[TYY * fs + pm], TYY), xy = dec(W[TXY * fs + pm], TXY);
+    const float xz = dec(W[TXZ * fs + pm], TXZ), yz = dec(W[TYZ * fs + pm], TYZ), zz = dec(W[TZZ * fs + pm], TZZ);
+    v[TXZ] = 2.0f * tsx - (xz + m1s * xx + m2s * xy);
+    v[TYZ] = 2.0f * tsy - (yz + m1s * xy + m2s * yy);
+    v[TZZ] = 2.0f * tsz - (zz + m1s * xz + m2s * yz);
+    v[TXX] = 0.0f;
+    v[TYY] = 0.0f;
+    v[TXY] = 0.0f;
+  };
+
+  float q[NQ][5];
+  if constexpr (TOPO) {
+#pragma unroll
+    for (int f = 0; f < NQ; ++f) q[f][0] = 0.0f;
 #pragma unroll
     for (int d = 1; d < 5; ++d) {
       const int kk = kb - TRAIL + d - 1;
-      q[f][d] = act ? qval(f, dec(W[f * fs + col + kk * plane], f), kk) : 0.0f;
+      float v[NF];
+#pragma unroll
+      for (int f = 0; f < NF; ++f) v[f] = act ? dec(W[f * fs + col + kk * plane], f) : 0.0f;
+      if (act) topo_img(v, kk);
+#pragma unroll
+      for (int f = 0; f < NF; ++f) q[f][d] = v[f];
+    }
+  } else {
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+      q[f][0] = 0.0f;
+#pragma unroll
+      for (int d = 1; d < 5; ++d) {
+        const int kk = kb - TRAIL + d - 1;
+        q[f][d] = act ? qval(f, dec(W[f * fs + col + kk * plane], f), kk) : 0.0f;
+      }
     }
   }
 
@@ -458,9 +519,27 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
           const int r = e / TBX, cc = e % TBX;
           const int ii = i0 - HX + cc, jj = j0 - HY + r;
           if (ii >= g.i1 && ii <= g.i2 && jj >= g.j1 && jj <= g.j2) {
-            tl(TXZ)[r][cc] = enc(surf_val(Src, Src.disp, gst, 0, ii, jj), TXZ);
-            tl(TYZ)[r][cc] = enc(surf_val(Src, Src.disp, gst, 1, ii, jj), TYZ);
-            tl(TZZ)[r][cc] = enc(surf_val(Src, Src.disp, gst, 2, ii, jj), TZZ);
+            const float ux = surf_val(Src, Src.disp, gst, 0, ii, jj);
+            const float uy = surf_val(Src, Src.disp, gst, 1, ii, jj);
+            const float uz = surf_val(Src, Src.disp, gst, 2, ii, jj);
+            float e1 = 0.0f, e2 = 0.0f;
+            if (TOPO) {
+              const int cq = (ii + PADL) + px * jj;
+              e1 = __ldg(A.topo_sf + cq);
+              e2 = __ldg(A.topo_sf + plane + cq);
+            }
+            if (TOPO && (e1 != 0.0f || e2 != 0.0f)) {  // sloping column: sigma . m = T*Src
+              const float xx = dec(tl(TXX)[r][cc], TXX), yy = dec(tl(TYY)[r][cc], TYY);
+              const float xy = dec(tl(TXY)[r][cc], TXY);
+              const float sxz = ux - e1 * xx - e2 * xy, syz = uy - e1 * xy - e2 * yy;
+              tl(TXZ)[r][cc] = enc(sxz, TXZ);
+              tl(TYZ)[r][cc] = enc(syz, TYZ);
+              tl(TZZ)[r][cc] = enc(uz - e1 * sxz - e2 * syz, TZZ);
+            } else {
+              tl(TXZ)[r][cc] = enc(ux, TXZ);
+              tl(TYZ)[r][cc] = enc(uy, TYZ);
+              tl(TZZ)[r][cc] = enc(uz, TZZ);
+            }
           }
         }
       __syncthreads();
@@ -470,15 +549,29 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
     if (ok && act) {
       // advance the z queue with plane k+LEAD (the image applies on and above the surface)
       const bool img = fsurf && k + LEAD >= g.k2;
+      if constexpr (TOPO) {
+        float v[NF];
 #pragma unroll
-      for (int f = 0; f < 6; ++f) {
-        q[f][0] = q[f][1]; q[f][1] = q[f][2]; q[f][2] = q[f][3]; q[f][3] = q[f][4];
-        q[f][4] = img ? qval(f, dec(qs[f][ty][tx], f), k + LEAD) : dec(qs[f][ty][tx], f);
+        for (int f = 0; f < NF; ++f) v[f] = dec(qs[f][ty][tx], f);
+        if (img) topo_img(v, k + LEAD);
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          q[f][0] = q[f][1]; q[f][1] = q[f][2]; q[f][2] = q[f][3]; q[f][3] = q[f][4];
+          q[f][4] = v[f];
+        }
+      } else {
+#pragma unroll
+        for (int f = 0; f < 6; ++f) {
+          q[f][0] = q[f][1]; q[f][1] = q[f][2]; q[f][2] = q[f][3]; q[f][3] = q[f][4];
+          q[f][4] = img ? qval(f, dec(qs[f][ty][tx], f), k + LEAD) : dec(qs[f][ty][tx], f);
+        }
       }
       const unsigned pmask = slab_mask(k);
       const int p = col + k * plane;
       const float lam = med[0][ty][tx], miu = med[1][ty][tx], rhov = med[2][ty][tx];
-      const float ze = __ldg(A.zeta_z + k);
+      // terrain form: r, zeta_r, zeta_theta / r, zeta_phi / (r sin theta) of the point
+      const float(*tpo)[TY][TX] = reinterpret_cast<const float(*)[TY][TX]>(buf + L::OFF_TOPO);
+      const float ze = TOPO ? tpo[1][ty][tx] : __ldg(A.zeta_z + k);
       const int r0 = ty + HY, c0 = tx + HX;
       // stencil sums along x (tile rows), y (tile columns), z (queue)
       const float sxTxx = unscale(dopS<FX>(&tl(TXX)[r0][c0], 1), TXX);
@@ -515,9 +608,48 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
       float dx_[6], dy_[6], dz_[6];
       const float lam2mu = lam + 2.0f * miu;
       float rrho;
+      // Terrain form, sloping column: the zeta parts of the theta and phi derivatives (in
+      // the top three planes the stress terms use the column's surface normal, so that
+      // with the traction images they form d(sigma . m)/dzeta), and on the free surface the
+      // traction condition sigma . m = T*Src: the velocity's zeta-derivatives u solve
+      // M u = dT*Src/dt - S0 . m (M^-1 precomputed), S0 the stress of the strain without
+      // its zeta parts (e13z, e23z: E13, E23 without them; E11, E12, E22 have none).
+      auto topo_slope = [&](auto& hVx_, auto& hVy_, auto& hVz_, auto& E11_, auto& E22_, auto& E12_, auto& E33_,
+                            auto& E13_, auto& E23_, float e13z, float e23z, float rrho_) {
+        const float bxv = tpo[2][ty][tx], byv = tpo[3][ty][tx];
+        const bool top3 = fsurf && k >= g.k2 - 2;
+        const float bxm = top3 ? ze * m1s : bxv, bym = top3 ? ze * m2s : byv;
+        const float szTxx = dopq<FZ>(q[TXX]), szTyy = dopq<FZ>(q[TYY]), szTxy = dopq<FZ>(q[TXY]);
+        hVx_ = hVx_ + rrho_ * (szTxx * bxm + (water ? 0.0f : szTxy * bym));
+        hVy_ = hVy_ + rrho_ * ((water ? 0.0f : szTxy * bxm) + szTyy * bym);
+        hVz_ = hVz_ + rrho_ * ((water ? 0.0f : szTxz * bxm) + (water ? 0.0f : szTyz * bym));
+        if (top) {
+          const float S11 = lam2mu * E11_ + lam * E22_, S22 = lam2mu * E22_ + lam * E11_, S33 = lam * (E11_ + E22_);
+          const float S12 = 2.0f * miu * E12_, S13 = 2.0f * miu * e13z, S23 = 2.0f * miu * e23z;
+          const float r0 = surf_val(Src, Src.rate, gst, 0, i, j) - (S11 * m1s + S12 * m2s + S13);
+          const float r1 = surf_val(Src, Src.rate, gst, 1, i, j) - (S12 * m1s + S22 * m2s + S23);
+          const float r2 = surf_val(Src, Src.rate, gst, 2, i, j) - (S13 * m1s + S23 * m2s + S33);
+          const float* mi = A.topo_sf + 2 * plane + col;
+          const float ux = __ldg(mi) * r0 + __ldg(mi + plane) * r1 + __ldg(mi + 2 * plane) * r2;
+          const float uy = __ldg(mi + 3 * plane) * r0 + __ldg(mi + 4 * plane) * r1 + __ldg(mi + 5 * plane) * r2;
+          const float uz = __ldg(mi + 6 * plane) * r0 + __ldg(mi + 7 * plane) * r1 + __ldg(mi + 8 * plane) * r2;
+          E11_ = E11_ + bxv * ux;
+          E22_ = E22_ + byv * uy;
+          E12_ = E12_ + 0.5f * (bxv * uy + byv * ux);
+          E33_ = ze * uz;
+          E13_ = e13z + 0.5f * (bxv * uz + ze * ux);
+          E23_ = e23z + 0.5f * (byv * uz + ze * uy);
+        } else {
+          E11_ = E11_ + bxv * szVx;
+          E22_ = E22_ + byv * szVy;
+          E12_ = E12_ + 0.5f * (bxv * szVy + byv * szVx);
+          E13_ = E13_ + 0.5f * bxv * szVz;
+          E23_ = E23_ + 0.5f * byv * szVz;
+        }
+      };
       if constexpr (EXACT) {
         // reference operand order, IEEE division (mod_macdrp.F90:928-957)
-        const float r = __ldg(A.zc + k);
+        const float r = TOPO ? tpo[0][ty][tx] : __ldg(A.zc + k);
         rrho = 1.0f / rhov;
         const float DxTxx = sxTxx * xi, DxTxy = sxTxy * xi, DxTxz = sxTxz * xi;
         const float DxVx = sxVx * xi, DxVy = sxVy * xi, DxVz = sxVz * xi;
@@ -531,13 +663,17 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
         hVx = rrho * (DxTxx / r + wDyTxy / r / xs + wDzTxz + (3.0f * Txz + Txx * c - Tyy * c) / r);
         hVy = rrho * (wDxTxy / r + DyTyy / r / xs + wDzTyz + (2.0f * Txy * c + 3.0f * Tyz) / r);
         hVz = rrho * (wDxTxz / r + wDyTyz / r / xs + DzTzz + (2.0f * Tzz - Txx - Tyy + Txz * c) / r);
-        const float E11 = (DxVx + Vz) / r;
-        const float E22 = (Vx * c + DyVy / xs + Vz) / r;
-        const float E12 = (DxVy + DyVx / xs - Vy * c) / r / 2.0f;
+        float E11 = (DxVx + Vz) / r;
+        float E22 = (Vx * c + DyVy / xs + Vz) / r;
+        float E12 = (DxVy + DyVx / xs - Vy * c) / r / 2.0f;
         float E33 = DzVz;
         float E13 = (DxVz / r + DzVx - Vx / r) / 2.0f;
         float E23 = (DyVz / r / xs + DzVy - Vy / r) / 2.0f;
-        if (top) {
+        if constexpr (TOPO)
+          if (slope)
+            topo_slope(hVx, hVy, hVz, E11, E22, E12, E33, E13, E23, (DxVz / r - Vx / r) / 2.0f,
+                       (DyVz / r / xs - Vy / r) / 2.0f, rrho);
+        if (top && !(TOPO && slope)) {
           E33 = -(lam / lam2mu * (E11 + E22)) + surf_val(Src, Src.rate, gst, 2, i, j) / lam2mu;
           E13 = surf_val(Src, Src.rate, gst, 0, i, j) / miu / 2.0f;
           E23 = surf_val(Src, Src.rate, gst, 1, i, j) / miu / 2.0f;
@@ -560,7 +696,7 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
         }
       } else {
         // same equations with the metric folded into one factor per axis
-        const float rr = __ldg(A.rzinv + k);
+        const float rr = TOPO ? __frcp_rn(tpo[0][ty][tx]) : __ldg(A.rzinv + k);
         rrho = __frcp_rn(rhov);
         const float ax = xi * rr, ay = et * rr * rs;
         const float gxTxx = sxTxx * ax, gxTxy = sxTxy * ax, gxTxz = sxTxz * ax;
@@ -575,13 +711,17 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
         hVx = rrho * (gxTxx + wyTxy + wzTxz + (3.0f * Txz + (Txx - Tyy) * c) * rr);
         hVy = rrho * (wxTxy + gyTyy + wzTyz + (2.0f * Txy * c + 3.0f * Tyz) * rr);
         hVz = rrho * (wxTxz + wyTyz + gzTzz + (2.0f * Tzz - Txx - Tyy + Txz * c) * rr);
-        const float E11 = gxVx + Vz * rr;
-        const float E22 = (Vx * c + Vz) * rr + gyVy;
-        const float E12 = 0.5f * (gxVy + gyVx - Vy * c * rr);
+        float E11 = gxVx + Vz * rr;
+        float E22 = (Vx * c + Vz) * rr + gyVy;
+        float E12 = 0.5f * (gxVy + gyVx - Vy * c * rr);
         float E33 = gzVz;
         float E13 = 0.5f * (gxVz + gzVx - Vx * rr);
         float E23 = 0.5f * (gyVz + gzVy - Vy * rr);
-        if (top) {
+        if constexpr (TOPO)
+          if (slope)
+            topo_slope(hVx, hVy, hVz, E11, E22, E12, E33, E13, E23, 0.5f * (gxVz - Vx * rr), 0.5f * (gyVz - Vy * rr),
+                       rrho);
+        if (top && !(TOPO && slope)) {
           E33 = (surf_val(Src, Src.rate, gst, 2, i, j) - lam * (E11 + E22)) / lam2mu;
           E13 = 0.5f * surf_val(Src, Src.rate, gst, 0, i, j) / miu;
           E23 = 0.5f * surf_val(Src, Src.rate, gst, 1, i, j) / miu;
@@ -767,7 +907,7 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
 // bx | by << 10 | bz << 20) of all simulations are numbered simulation after simulation,
 // and CTA b runs items b, b + gridDim.x, ... (one item each when the grid covers them
 // all).  Lean launches get the interior items, full launches the others.
-template <class S, bool EXACT, int FX, int FY, int FZ, int RK, bool LEAN>
+template <class S, bool EXACT, int FX, int FY, int FZ, int RK, bool LEAN, bool TOPO = false>
 __global__ void __launch_bounds__(TX* TY, LEAN ? 3 : 2) stage_batch_kernel(const __grid_constant__ BatchArgs B) {
   extern __shared__ __align__(1024) unsigned char smem[];
   for (int item = blockIdx.x; item < B.total; item += gridDim.x) {
@@ -775,15 +915,15 @@ __global__ void __launch_bounds__(TX* TY, LEAN ? 3 : 2) stage_batch_kernel(const
     while (item >= B.off[s + 1]) ++s;
     const int packed = B.items[s][item - B.off[s]];
     const int bx = packed & 1023, by = (packed >> 10) & 1023, bz = packed >> 20;
-    if (!stage_body<S, EXACT, FX, FY, FZ, RK, LEAN>(B.sims[s], bx, by, bz, smem)) return;
+    if (!stage_body<S, EXACT, FX, FY, FZ, RK, LEAN, TOPO>(B.sims[s], bx, by, bz, smem)) return;
     __syncthreads();  // the next item re-initialises the barriers and reuses the buffers
   }
 }
 
-template <class S, bool EXACT, int FX, int FY, int FZ, int RK, bool LEAN>
+template <class S, bool EXACT, int FX, int FY, int FZ, int RK, bool LEAN, bool TOPO = false>
 static int launch_batch_one(const BatchArgs& b, int ctas, cudaStream_t st) {
-  stage_batch_kernel<S, EXACT, FX, FY, FZ, RK, LEAN>
-      <<<ctas, dim3(TX, TY, 1), Lay<S>::smem_bytes(LEAN, RK), st>>>(b);
+  stage_batch_kernel<S, EXACT, FX, FY, FZ, RK, LEAN, TOPO>
+      <<<ctas, dim3(TX, TY, 1), Lay<S, TOPO>::smem_bytes(LEAN, RK), st>>>(b);
   return int(cudaGetLastError());
 }
 
@@ -823,6 +963,35 @@ template <class S, bool EXACT, int RK>
 static int launch_batch_rk_variant(const BatchArgs& b, int variant, int lean, int ctas, cudaStream_t st) {
   return lean ? launch_batch_lean<S, EXACT, RK, true>(b, variant, ctas, st)
               : launch_batch_lean<S, EXACT, RK, false>(b, variant, ctas, st);
+}
+
+// Terrain form (FP32 storage, full form; EXACT selects the reference-order arithmetic):
+// opt in and launch.
+template <bool EXACT, int RK>
+static int configure_topo_rk() {
+  cudaError_t e = cudaSuccess;
+#define FW_CFG(FX, FY, FZ)                                                                                 \
+  if (e == cudaSuccess)                                                                                    \
+    e = cudaFuncSetAttribute(stage_batch_kernel<float, EXACT, FX, FY, FZ, RK, false, true>,                \
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, Lay<float, true>::smem_bytes(false, RK));
+  FW_CFG(0, 0, 0) FW_CFG(0, 0, 1) FW_CFG(0, 1, 0) FW_CFG(0, 1, 1)
+  FW_CFG(1, 0, 0) FW_CFG(1, 0, 1) FW_CFG(1, 1, 0) FW_CFG(1, 1, 1)
+#undef FW_CFG
+  return int(e);
+}
+
+template <bool EXACT, int RK>
+static int launch_batch_topo_variant(const BatchArgs& b, int variant, int ctas, cudaStream_t st) {
+  switch (variant) {
+    case 0: return launch_batch_one<float, EXACT, 0, 0, 0, RK, false, true>(b, ctas, st);
+    case 1: return launch_batch_one<float, EXACT, 0, 0, 1, RK, false, true>(b, ctas, st);
+    case 2: return launch_batch_one<float, EXACT, 0, 1, 0, RK, false, true>(b, ctas, st);
+    case 3: return launch_batch_one<float, EXACT, 0, 1, 1, RK, false, true>(b, ctas, st);
+    case 4: return launch_batch_one<float, EXACT, 1, 0, 0, RK, false, true>(b, ctas, st);
+    case 5: return launch_batch_one<float, EXACT, 1, 0, 1, RK, false, true>(b, ctas, st);
+    case 6: return launch_batch_one<float, EXACT, 1, 1, 0, RK, false, true>(b, ctas, st);
+    default: return launch_batch_one<float, EXACT, 1, 1, 1, RK, false, true>(b, ctas, st);
+  }
 }
 
 }  // namespace fw

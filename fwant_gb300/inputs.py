@@ -235,6 +235,30 @@ def make_model(ni, nj, nk, seed=0, dh_km=1.0, theta_c_deg=50.0, phi_c_deg=100.0,
     return m
 
 
+def gaussian_hill(m: Model, amplitude_m: float, width_km: float | None = None, seed: int = 0,
+                  centre: tuple | None = None) -> np.ndarray:
+    """Heights (nx, ny) float32, Fortran order, of a seeded Gaussian hill for the terrain-
+    following grid: h = A exp(-d^2 / w^2), d the arc distance (at the top radius) from the
+    centre.  Seeded: the centre within the middle fifth of the surface, the width w in
+    [0.12, 0.18] of the smaller horizontal extent (unless given)."""
+    rng = np.random.default_rng(seed + 2718)
+    r_top = float(m.z[-1 - LENFD])
+    th = m.x.astype(np.float64)
+    ph = m.y.astype(np.float64)
+    if centre is None:
+        ci = LENFD + m.ni // 2 + int(rng.integers(-m.ni // 10, m.ni // 10 + 1))
+        cj = LENFD + m.nj // 2 + int(rng.integers(-m.nj // 10, m.nj // 10 + 1))
+    else:
+        ci, cj = centre
+    if width_km is None:
+        ext = min(m.ni * (th[LENFD + 1] - th[LENFD]), m.nj * (ph[LENFD + 1] - ph[LENFD]) * np.sin(th[ci])) * r_top
+        width_km = float(rng.uniform(0.12, 0.18)) * ext / 1000.0
+    dth = (th - th[ci])[:, None] * r_top
+    dph = (ph - ph[cj])[None, :] * r_top * np.sin(th[ci])
+    d2 = (dth ** 2 + dph ** 2) / (width_km * 1000.0) ** 2
+    return np.asfortranarray((amplitude_m * np.exp(-d2)).astype(np.float32))
+
+
 def config_c1(seed=0, **kw) -> Model:
     """Config 1: 100x100x60, 1 km horizontal, 0.5-2 km vertical, layered Vp 5.8-8.0,
     12-cell PML on 5 faces, free surface, vertical Ricker force (0.2 Hz) at the surface

@@ -116,6 +116,30 @@ fwant_status fwant_set_metric(fwant_solver* s, const float* xsin, const float* x
  * replaces the seis3d_metric preprocessor (code/srcF/seis3d_metric.F90:83-112). */
 fwant_status fwant_compute_metric(fwant_solver* s);
 
+/* Terrain-following grid (the Gaussian-hill extension of the workload).  No counterpart in
+ * the reference: its grid is orthogonal spherical with a flat top at k = nk2
+ * (code/srcF/mod_grid.F90:36-38, code/srcF/seis3d_metric.F90:83-112, the radial term of
+ * code/srcF/mod_macdrp.F90:928-957) and cannot represent topography.
+ *
+ * h: nx*ny heights in m (i fastest, ghosts included).  The radius becomes
+ * r(i,j,k) = z(k) + h(i,j) s(k) with s(k) = (z(k) - z(1)) / (z(nk2) - z(1)), so the free
+ * surface follows h and the bottom stays flat.  Every theta and phi derivative gains its
+ * zeta part (metric terms zeta_theta, zeta_phi; zeta_r becomes three-dimensional), computed
+ * in FP64 on the device.  On a sloping free surface the stress images are the traction
+ * combination sigma . m (m the surface normal) and the velocity's zeta-derivatives solve the
+ * traction condition sigma . m = T*Src; columns with zero slope run the reference's flat
+ * formulas, so h = 0 reproduces the flat solver bit for bit.  Surface-force areas and
+ * body-force cell volumes keep the flat grid's values; the cross-metric terms are not
+ * damped by the PML, so the slopes must vanish inside the PML slabs.  Needs FP32 storage
+ * (either arithmetic form); call after the coordinates and the metric (setting either again
+ * recomputes the terrain metric).  A solver with topography steps alone (not in a batch). */
+fwant_status fwant_set_topography(fwant_solver* s, const float* h);
+
+/* The terrain metric as stored (FP32): which 0..3 give nx*ny*nz values (r, zeta_r,
+ * zeta_theta / r, zeta_phi / (r sin theta)); 4 and 5 the surface normal's m1, m2 and 6..14
+ * the row-major inverse of the traction condition, nx*ny values each (i fastest). */
+fwant_status fwant_get_topography_array(fwant_solver* s, int which, float* out);
+
 /* The metric of a grid without a solver: the seis3d_metric program
  * (code/srcF/seis3d_metric.F90:83-112; the fwant_prep program's metric stage) on the device in
  * FP64, rounded to FP32, the same values as fwant_compute_metric.  x[ni+6], y[nj+6], z[nk+6]

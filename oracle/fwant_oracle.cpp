@@ -271,6 +271,16 @@ template <class T> struct Solver {
   std::vector<T> seismo;  // [var][sample][pt]
   int nsamp = 0, nsamp_cap = 0;
 
+  // Gaussian-hill extension (no counterpart in the reference, whose grid is orthogonal
+  // spherical with a flat top): terrain-following radius r(i,j,k) = z(k) + h(i,j) s(k),
+  // s(k) = (z(k) - z(1)) / (z(nk2) - z(1)), so the free surface k = nk2 follows h and the
+  // bottom of the grid stays flat.
+  bool topo_on = false, topo_bc_dirty = true;
+  std::vector<double> topo_h, topo_hx, topo_hy;  // (nx,ny): heights (m), d/dxi, d/deta
+  std::vector<T> t_r, t_az, t_bx, t_by;  // (nx,ny,nz): r, zeta_r, zeta_theta / r, zeta_phi / (r sin theta)
+  std::vector<T> t_m1, t_m2, t_minv;     // (nx,ny): surface normal / its radial part; 3x3 inverse (x 9)
+  std::vector<unsigned char> t_slope;    // (nx,ny): the column's surface has a non-zero slope
+
   size_t id(int i, int j, int k) const {
     return size_t(i - 1) + size_t(nx) * (size_t(j - 1) + size_t(ny) * size_t(k - 1));
   }
@@ -559,7 +569,7 @@ template <class T> struct Solver {
             T b1 = T(1) / Bv;
             T b1_1 = b1 - T(1);
             T ad = Av + Dv;
-            const T r = z[k], s = xsin[i], c = xcot[i];
+            const T r = topo_on ? t_r[p] : z[k], s = xsin[i], c = xcot[i];
             const T Txx = W[TXX][p], Tyy = W[TYY][p], Tzz = W[TZZ][p];
             const T Txy = W[TXY][p], Txz = W[TXZ][p], Tyz = W[TYZ][p];
             const T Vx = W[VX][p], Vy = W[VY][p], Vz = W[VZ][p];
@@ -585,7 +595,7 @@ template <class T> struct Solver {
               d4 = op(fy, &W[VY][p], sy) * et; d4 = (d4 / s + Vx * c + Vz) / r;
               d5 = op(fy, &W[VZ][p], sy) * et; d5 = (d5 / s - Vy) / r;
             } else {
-              const T ze = zeta_z[k];
+              const T ze = topo_on ? t_az[p] : zeta_z[k];
               d0 = op(fz, &W[TXZ][p], sz) * ze;
               d1 = op(fz, &W[TYZ][p], sz) * ze;
               d2 = op(fz, &W[TZZ][p], sz) * ze;
@@ -815,6 +825,236 @@ template <class T> struct Solver {
     nsamp = std::max(nsamp, m);
   }
 
+  // ---- Gaussian-hill extension -----------------------------------------------------
+  // Derivative along one index of a coordinate-like array, as seis3d_metric forms x_xi
+  // (seis3d_metric.F90:83-112): the mean of the backward and forward DRP/opt operators,
+  // in double; indices outside [lo, hi] take the value at the nearest of them.
+  static double dmetric(const std::vector<double>& f, ptrdiff_t stride, ptrdiff_t base, int i, int lo, int hi) {
+    static const double cF[5] = {-0.30874, -0.6326, 1.2330, -0.3334, 0.04168};
+    static const double cB[5] = {-0.04168, 0.3334, -1.2330, 0.6326, 0.30874};
+    const int ii = i < lo ? lo : (i > hi ? hi : i);
+    double sb = 0.0, sf = 0.0;
+    for (int q = 0; q < 5; ++q) {
+      sb = sb + f[base + (ii - 3 + q) * stride] * cB[q];
+      sf = sf + f[base + (ii - 1 + q) * stride] * cF[q];
+    }
+    return (sb + sf) * 0.5;
+  }
+
+  // Metric of the terrain-following grid, in double from the coordinates, the 1-D metric
+  // and the heights, rounded once to T:
+  //   r       = z(k) + h s(k)
+  //   zeta_r  = zeta_z(k) * z_zeta(k) / r_zeta(i,j,k)    (1 where h = 0)
+  //   zeta_theta / r          = -r_xi  xi_x  zeta_r / r
+  //   zeta_phi / (r sin theta) = -r_eta eta_y zeta_r / (r sin theta)
+  // with r_xi = h_xi s(k), r_eta = h_eta s(k) and r_zeta the metric derivative of r along k.
+  void set_topography(const double* h) {
+    const size_t n2 = size_t(nx) * ny, n3 = n2 * nz;
+    topo_h.assign(h, h + n2);
+    topo_hx.assign(n2, 0.0); topo_hy.assign(n2, 0.0);
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        topo_hx[id2(i, j)] = dmetric(topo_h, 1, ptrdiff_t(nx) * (j - 1) - 1, i, ni1, ni2);
+        topo_hy[id2(i, j)] = dmetric(topo_h, nx, ptrdiff_t(i) - 1 - nx, j, nj1, nj2);
+      }
+    std::vector<double> zd(nz), sk(nz), rzf(nz);
+    for (int k = 1; k <= nz; ++k) zd[k - 1] = double(z[k]);
+    for (int k = 1; k <= nz; ++k) {
+      sk[k - 1] = (zd[k - 1] - zd[0]) / (zd[nk2 - 1] - zd[0]);
+      rzf[k - 1] = dmetric(zd, 1, -1, k, nk1, nk2);
+    }
+    t_r.assign(n3, T(0)); t_az.assign(n3, T(0)); t_bx.assign(n3, T(0)); t_by.assign(n3, T(0));
+    std::vector<double> col(nz);
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        const size_t q = id2(i, j);
+        const double hh = topo_h[q], hx = topo_hx[q], hy = topo_hy[q];
+        for (int k = 1; k <= nz; ++k) col[k - 1] = zd[k - 1] + hh * sk[k - 1];
+        for (int k = 1; k <= nz; ++k) {
+          const double r = col[k - 1];
+          const double rz = dmetric(col, 1, -1, k, nk1, nk2);
+          const double az = double(zeta_z[k]) * (rzf[k - 1] / rz);
+          const double bx = -((hx * sk[k - 1]) * double(xi_x[i])) * az / r;
+          const double by = -((hy * sk[k - 1]) * double(eta_y[j])) * az / (r * double(xsin[i]));
+          const size_t p = id(i, j, k);
+          t_r[p] = T(r); t_az[p] = T(az); t_bx[p] = T(bx); t_by[p] = T(by);
+        }
+      }
+    topo_on = true;
+    topo_bc_dirty = true;
+  }
+
+  // Surface arrays of the extension (they need the medium): the normal m = (m1, m2, 1) of
+  // the surface k = nk2 (grad zeta scaled to a unit radial part) and the inverse of the
+  // 3x3 map from the velocity's zeta-derivatives to the traction rate on that surface,
+  // both in double, rounded to T.
+  void topo_surface() {
+    const size_t n2 = size_t(nx) * ny;
+    t_m1.assign(n2, T(0)); t_m2.assign(n2, T(0)); t_minv.assign(9 * n2, T(0)); t_slope.assign(n2, 0);
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        const size_t q = id2(i, j), p = id(i, j, nk2);
+        const double az = double(t_az[p]), bx = double(t_bx[p]), by = double(t_by[p]);
+        const double m1 = bx / az, m2 = by / az;
+        t_m1[q] = T(m1); t_m2[q] = T(m2);
+        t_slope[q] = (t_m1[q] != T(0) || t_m2[q] != T(0)) ? 1 : 0;  // zero slope: the flat path
+        const double la = double(lam[p]), mu_ = double(mu[p]), l2 = la + 2.0 * mu_;
+        double M[3][3];
+        M[0][0] = l2 * bx * m1 + mu_ * by * m2 + mu_ * az;
+        M[1][0] = mu_ * by * m1 + la * bx * m2;
+        M[2][0] = mu_ * az * m1 + la * bx;
+        M[0][1] = la * by * m1 + mu_ * bx * m2;
+        M[1][1] = mu_ * bx * m1 + l2 * by * m2 + mu_ * az;
+        M[2][1] = mu_ * az * m2 + la * by;
+        M[0][2] = la * az * m1 + mu_ * bx;
+        M[1][2] = la * az * m2 + mu_ * by;
+        M[2][2] = mu_ * bx * m1 + mu_ * by * m2 + l2 * az;
+        const double c00 = M[1][1] * M[2][2] - M[1][2] * M[2][1];
+        const double c01 = M[1][2] * M[2][0] - M[1][0] * M[2][2];
+        const double c02 = M[1][0] * M[2][1] - M[1][1] * M[2][0];
+        const double det = M[0][0] * c00 + M[0][1] * c01 + M[0][2] * c02;
+        const double inv[9] = {c00 / det, (M[0][2] * M[2][1] - M[0][1] * M[2][2]) / det,
+                               (M[0][1] * M[1][2] - M[0][2] * M[1][1]) / det,
+                               c01 / det, (M[0][0] * M[2][2] - M[0][2] * M[2][0]) / det,
+                               (M[0][2] * M[1][0] - M[0][0] * M[1][2]) / det,
+                               c02 / det, (M[0][1] * M[2][0] - M[0][0] * M[2][1]) / det,
+                               (M[0][0] * M[1][1] - M[0][1] * M[1][0]) / det};
+        for (int e = 0; e < 9; ++e) t_minv[9 * q + e] = T(inv[e]);
+      }
+    topo_bc_dirty = false;
+  }
+
+  // Traction image of the extension (free_timg generalised): in a column whose surface
+  // slopes, the images above k = nk2 hold the traction combination G = sigma . m with the
+  // column's surface normal, antisymmetric about the surface around the source traction
+  // (G(nk2+q) = 2 T*Src - G(nk2-q)), in the slots of Txz, Tyz, Tzz (G_x, G_y, G_z; the
+  // Txx, Tyy, Txy ghosts stay zero), and the surface values of Txz, Tyz, Tzz are set so
+  // that sigma . m = T*Src there.  Flat columns take free_timg's values.
+  void free_timg_topo() {
+    if (!freenode) return;
+    for (int j = nj1; j <= nj2; ++j)
+      for (int i = ni1; i <= ni2; ++i) {
+        const size_t q = id2(i, j);
+        if (!t_slope[q]) {
+          for (int m = 1; m <= 3; ++m) {
+            W[TZZ][id(i, j, nk2 + m)] = T(2) * TzSrc[q] - W[TZZ][id(i, j, nk2 - m)];
+            W[TXZ][id(i, j, nk2 + m)] = T(2) * TxSrc[q] - W[TXZ][id(i, j, nk2 - m)];
+            W[TYZ][id(i, j, nk2 + m)] = T(2) * TySrc[q] - W[TYZ][id(i, j, nk2 - m)];
+          }
+          W[TZZ][id(i, j, nk2)] = TzSrc[q];
+          W[TXZ][id(i, j, nk2)] = TxSrc[q];
+          W[TYZ][id(i, j, nk2)] = TySrc[q];
+          continue;
+        }
+        const T m1 = t_m1[q], m2 = t_m2[q];
+        for (int m = 1; m <= 3; ++m) {
+          const size_t pm = id(i, j, nk2 - m);
+          const T gx = W[TXZ][pm] + m1 * W[TXX][pm] + m2 * W[TXY][pm];
+          const T gy = W[TYZ][pm] + m1 * W[TXY][pm] + m2 * W[TYY][pm];
+          const T gz = W[TZZ][pm] + m1 * W[TXZ][pm] + m2 * W[TYZ][pm];
+          const size_t pu = id(i, j, nk2 + m);
+          W[TXZ][pu] = T(2) * TxSrc[q] - gx;
+          W[TYZ][pu] = T(2) * TySrc[q] - gy;
+          W[TZZ][pu] = T(2) * TzSrc[q] - gz;
+        }
+        const size_t p = id(i, j, nk2);
+        const T sxz = TxSrc[q] - m1 * W[TXX][p] - m2 * W[TXY][p];
+        const T syz = TySrc[q] - m1 * W[TXY][p] - m2 * W[TYY][p];
+        W[TXZ][p] = sxz;
+        W[TYZ][p] = syz;
+        W[TZZ][p] = TzSrc[q] - m1 * sxz - m2 * syz;
+      }
+  }
+
+  // The stencil on the terrain-following grid.  Every theta and phi derivative gains its
+  // zeta part (cross terms zeta_theta d/dzeta, zeta_phi d/dzeta); in the top three planes
+  // of a sloping column the stress cross terms use the column's surface normal, so that
+  // with the traction images they form d(sigma . m)/dzeta.  On a sloping free surface the
+  // velocity's zeta-derivatives come from the traction condition sigma . m = T*Src (the
+  // 3x3 inverse of topo_surface), generalising mod_macdrp.F90:944-948.
+  void stencil_topo(bool fx, bool fy, bool fz) {
+    const ptrdiff_t sx = 1, sy = nx, sz = ptrdiff_t(nx) * ny;
+#pragma omp parallel for schedule(static)
+    for (int k = nk1; k <= nk2; ++k)
+      for (int j = nj1; j <= nj2; ++j)
+        for (int i = ni1; i <= ni2; ++i) {
+          const size_t p = id(i, j, k), q2 = id2(i, j);
+          const T lam_ = lam[p], miu = mu[p];
+          const T lam2mu = lam_ + T(2) * miu;
+          const T rrho = T(1) / rho[p];
+          const T r = t_r[p], az = t_az[p], s = xsin[i], c = xcot[i];
+          const bool slope = t_slope[q2] != 0;
+          const bool top3 = freenode && slope && k >= nk2 - 2;
+          const T bxv = t_bx[p], byv = t_by[p];                          // strain cross terms
+          const T bxm = top3 ? az * t_m1[q2] : bxv, bym = top3 ? az * t_m2[q2] : byv;  // momentum
+          const T ax = xi_x[i] / r, ay = eta_y[j] / r / s;
+          auto D = [&](int f, bool fw, ptrdiff_t st) { return op(fw, &W[f][p], st); };
+          auto Dz = [&](int f) { return op(fz, &W[f][p], sz); };
+          auto DzV = [&](int f) {
+            if (freenode && k == nk2 - 1) return op22(fz, &W[f][p], sz);
+            if (freenode && k == nk2 - 2) return op24(fz, &W[f][p], sz);
+            return op(fz, &W[f][p], sz);
+          };
+          const bool water = miu <= T(1.0e-20f);
+          const T w = water ? T(0) : T(1);
+          // stress derivatives: theta (x), phi (y), r (z) parts
+          const T xTxx = D(TXX, fx, sx) * ax + Dz(TXX) * bxm;
+          const T xTxy = w * (D(TXY, fx, sx) * ax + Dz(TXY) * bxm);
+          const T xTxz = w * (D(TXZ, fx, sx) * ax + Dz(TXZ) * bxm);
+          const T yTyy = D(TYY, fy, sy) * ay + Dz(TYY) * bym;
+          const T yTxy = w * (D(TXY, fy, sy) * ay + Dz(TXY) * bym);
+          const T yTyz = w * (D(TYZ, fy, sy) * ay + Dz(TYZ) * bym);
+          const T zTzz = Dz(TZZ) * az, zTxz = w * (Dz(TXZ) * az), zTyz = w * (Dz(TYZ) * az);
+          const T Txx = W[TXX][p], Tyy = W[TYY][p], Tzz = W[TZZ][p];
+          const T Txy = W[TXY][p], Txz = W[TXZ][p], Tyz = W[TYZ][p];
+          const T Vx = W[VX][p], Vy = W[VY][p], Vz = W[VZ][p];
+          H[VX][p] = rrho * (xTxx + yTxy + zTxz + (T(3) * Txz + Txx * c - Tyy * c) / r);
+          H[VY][p] = rrho * (xTxy + yTyy + zTyz + (T(2) * Txy * c + T(3) * Tyz) / r);
+          H[VZ][p] = rrho * (xTxz + yTyz + zTzz + (T(2) * Tzz - Txx - Tyy + Txz * c) / r);
+          // velocity derivatives without their zeta parts, then the zeta parts
+          const T gxVx = D(VX, fx, sx) * ax, gxVy = D(VY, fx, sx) * ax, gxVz = D(VZ, fx, sx) * ax;
+          const T gyVx = D(VX, fy, sy) * ay, gyVy = D(VY, fy, sy) * ay, gyVz = D(VZ, fy, sy) * ay;
+          T E11 = gxVx + Vz / r;
+          T E22 = (Vx * c + Vz) / r + gyVy;
+          T E12 = (gxVy + gyVx - Vy * c / r) / T(2);
+          T E33 = T(0);
+          T E13 = (gxVz - Vx / r) / T(2);
+          T E23 = (gyVz - Vy / r) / T(2);
+          T ux, uy, uz;  // d(Vx, Vy, Vz)/dzeta
+          if (freenode && k == nk2 && slope) {
+            const T S11 = lam2mu * E11 + lam_ * E22, S22 = lam2mu * E22 + lam_ * E11, S33 = lam_ * (E11 + E22);
+            const T S12 = T(2) * miu * E12, S13 = T(2) * miu * E13, S23 = T(2) * miu * E23;
+            const T m1 = t_m1[q2], m2 = t_m2[q2];
+            const T r0 = VxSrc[q2] - (S11 * m1 + S12 * m2 + S13);
+            const T r1 = VySrc[q2] - (S12 * m1 + S22 * m2 + S23);
+            const T r2 = VzSrc[q2] - (S13 * m1 + S23 * m2 + S33);
+            const T* mi = &t_minv[9 * q2];
+            ux = mi[0] * r0 + mi[1] * r1 + mi[2] * r2;
+            uy = mi[3] * r0 + mi[4] * r1 + mi[5] * r2;
+            uz = mi[6] * r0 + mi[7] * r1 + mi[8] * r2;
+          } else {
+            ux = DzV(VX); uy = DzV(VY); uz = DzV(VZ);
+          }
+          E11 = E11 + bxv * ux;
+          E22 = E22 + byv * uy;
+          E12 = E12 + (bxv * uy + byv * ux) / T(2);
+          E33 = az * uz;
+          E13 = E13 + (bxv * uz + az * ux) / T(2);
+          E23 = E23 + (byv * uz + az * uy) / T(2);
+          if (freenode && k == nk2 && !slope) {  // mod_macdrp.F90:944-948
+            E33 = -(lam_ / lam2mu * (E11 + E22)) + VzSrc[q2] / lam2mu;
+            E13 = VxSrc[q2] / miu / T(2);
+            E23 = VySrc[q2] / miu / T(2);
+          }
+          H[TXX][p] = lam2mu * E11 + lam_ * (E22 + E33);
+          H[TYY][p] = lam2mu * E22 + lam_ * (E11 + E33);
+          H[TZZ][p] = lam2mu * E33 + lam_ * (E11 + E22);
+          H[TXY][p] = T(2) * miu * E12;
+          H[TXZ][p] = T(2) * miu * E13;
+          H[TYZ][p] = T(2) * miu * E23;
+        }
+  }
+
   // The 8-step cycle of seis3d_wave_8op_p3.F90:82-591: stage-1/3 operator per step
   // (bit 2 = x, bit 1 = y, bit 0 = z; 1 = forward); stages 2/4 use the mirror.
   static int cycle_variant(int pos) {
@@ -831,8 +1071,14 @@ template <class T> struct Solver {
       if (srcsurface && !src_surface(incr)) return false;
       const int v = (s % 2 == 0) ? X : (~X & 7);
       const bool fx = (v >> 2) & 1, fy = (v >> 1) & 1, fz = v & 1;
-      free_timg();
-      stencil(fx, fy, fz);
+      if (topo_on) {
+        if (topo_bc_dirty) topo_surface();
+        free_timg_topo();
+        stencil_topo(fx, fy, fz);
+      } else {
+        free_timg();
+        stencil(fx, fy, fz);
+      }
       abs_stencil(fx, fy, fz);
       if (!src_stress(incr)) return false;
       if (!src_force(incr)) return false;
@@ -962,6 +1208,27 @@ void orc_set_media(void* hv, const double* lam, const double* mu, const double* 
   DISPATCH(h, {
     size_t n = size_t(S.nx) * S.ny * S.nz;
     cpy(S.lam, lam, n, 0); cpy(S.mu, mu, n, 0); cpy(S.rho, rho, n, 0);
+    S.topo_bc_dirty = true;
+  });
+}
+
+// Gaussian-hill extension: heights h (nx*ny, i fastest, m) of the terrain-following
+// radius; set after the coordinates and the metric.
+void orc_set_topography(void* hv, const double* h) {
+  OrcHandle* hd = (OrcHandle*)hv;
+  DISPATCH(hd, { S.set_topography(h); });
+}
+
+// Metric arrays of the extension as T values in double: which 0 r, 1 zeta_r,
+// 2 zeta_theta / r, 3 zeta_phi / (r sin theta) (nx*ny*nz); 4 m1, 5 m2 (nx*ny); 6 the 3x3
+// inverses (9*nx*ny) (computed on demand).
+void orc_topography_array(void* hv, int which, double* out) {
+  OrcHandle* hd = (OrcHandle*)hv;
+  DISPATCH(hd, {
+    if (which >= 4 && S.topo_bc_dirty) S.topo_surface();
+    const auto& v = which == 0 ? S.t_r : which == 1 ? S.t_az : which == 2 ? S.t_bx : which == 3 ? S.t_by
+                  : which == 4 ? S.t_m1 : which == 5 ? S.t_m2 : S.t_minv;
+    for (size_t q = 0; q < v.size(); ++q) out[q] = double(v[q]);
   });
 }
 

@@ -33,6 +33,8 @@ _SIGS = [
     ("orc_set_media", None, [_vp, _dp, _dp, _dp]),
     ("orc_set_pml", C.c_int, [_vp, _ip, _dp, _dp, _dp]),
     ("orc_set_srcsurface", None, [_vp, C.c_int]),
+    ("orc_set_topography", None, [_vp, _dp]),
+    ("orc_topography_array", None, [_vp, C.c_int, _dp]),
     ("orc_set_forces", None, [_vp, C.c_int, C.c_int, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.c_int]),
     ("orc_set_moments", None, [_vp, C.c_int, C.c_int, _ip, _dp, _dp, _dp, _dp, _dp, C.c_int]),
     ("orc_set_receivers", None, [_vp, C.c_int, _ip, C.c_int]),
@@ -348,6 +350,25 @@ class Oracle:
     def compute_metric(self):
         m = metric(self.x, self.y, self.z)
         self.set_metric(m["xsin"], m["xcot"], m["xi_x"], m["eta_y"], m["zeta_z"])
+
+    def set_topography(self, h):
+        """Gaussian-hill extension: heights h (nx, ny) in m of the terrain-following radius
+        r = z(k) + h s(k); after set_coord and the metric."""
+        a = _d(np.asarray(h, np.float32).reshape(-1, order="F"))
+        self._L.orc_set_topography(self._h, _p(a))
+
+    def topography_array(self, which):
+        """0 r, 1 zeta_r, 2 zeta_theta/r, 3 zeta_phi/(r sin theta) as (nx, ny, nz); 4, 5 the
+        surface normal's m1, m2 (nx, ny); 6 the 3x3 inverses (nx, ny, 9)."""
+        n2 = self.nx * self.ny
+        n = n2 * self.nz if which < 4 else (n2 if which < 6 else 9 * n2)
+        out = np.zeros(n)
+        self._L.orc_topography_array(self._h, int(which), _p(out))
+        if which < 4:
+            return out.reshape(self.shape, order="F")
+        if which < 6:
+            return out.reshape(self.nx, self.ny, order="F")
+        return out.reshape(9, self.nx, self.ny, order="F").transpose(1, 2, 0)
 
     def set_media(self, lam, mu, rho):
         a = [_d(np.asarray(v, np.float32).reshape(-1, order="F")) for v in (lam, mu, rho)]
