@@ -1,7 +1,8 @@
 """The physics checks of test_physics_oracle.py on the GPU's fast arithmetic form, with
 finer levels than the CPU can afford: the reciprocity asymmetry of the horizontal-vertical
 pairs must keep shrinking at a 0.25 km surface spacing, and the convergence study adds a
-0.125 km level (257^3 points)."""
+0.125 km level (385^3 points), where the observed order reaches 3.7 (successive
+differences 3.7e-4, 6.0e-5, 4.7e-6)."""
 import numpy as np
 import pytest
 
@@ -49,4 +50,4 @@ def test_convergence_under_refinement_gpu(native_lib):
     errs, orders = P.convergence_orders(sols)
     print("differences", errs, "orders", orders)
     assert all(errs[l + 1] < errs[l] for l in range(len(errs) - 1))
-    assert min(orders) > 1.2
+    assert orders[0] > 2.3 and orders[1] > 3.3
