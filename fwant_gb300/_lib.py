@@ -79,6 +79,7 @@ EXPORTS = [
                                       C.POINTER(C.c_double)]),
     ("fwant_sgtker_last_scatter_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
     ("fwant_sgtker_rotate", C.c_int, [_vp, C.POINTER(C.c_double)]),
+    ("fwant_sgtker_convert", C.c_int, [_vp, C.c_int, _fp, _fp, _fp, _fp]),
     ("fwant_sgtker_kernel_filtered", C.c_int, [_vp, C.c_int, _fp, _fp, C.c_int, C.c_int, C.c_double, C.c_int,
                                                C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                                C.POINTER(C.c_double), C.POINTER(C.c_double),
@@ -606,6 +607,13 @@ class SgtKernel:
         """Rotate the three force components' series by the 3x3 matrix rot (rot[d, c])."""
         r = np.ascontiguousarray(np.asarray(rot, np.float64).reshape(3, 3).T.reshape(-1))  # column-major
         self._chk(self._lib.fwant_sgtker_rotate(self._h, _ptr(r, C.c_double)))
+
+    def convert(self, mode, kap, kaq, kbp, kbq):
+        """Kernel parameter conversion (mode 1 lamu2kamu, 2 lamu2vpvs, 3 vpvs2kamu) of four
+        [npts] kernels with the media of set_media; returns the converted four (float32)."""
+        arrs = [np.array(np.asarray(x, np.float32).reshape(-1), np.float32) for x in (kap, kaq, kbp, kbq)]
+        self._chk(self._lib.fwant_sgtker_convert(self._h, int(mode), *[_ptr(a) for a in arrs]))
+        return tuple(arrs)
 
     def last_scatter_ms(self):
         ms = C.c_double()

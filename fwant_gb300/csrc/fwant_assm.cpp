@@ -1,6 +1,8 @@
 // fwant_assm: the kernel assembly program over the C ABI, a drop-in for the reference's
 // SI_ker2assm (code/srcF.kernel/SI_ker2assm.F90, phase-delay kernels) and, with --kamu,
-// SI_ker_kamu2assm (kernel_kamu_ files, phase_ka / phase_mu) on one rank.
+// SI_ker_kamu2assm (kernel_kamu_ files, phase_ka / phase_mu) or, with --lamu,
+// SI_ker_lamu2assm (kernel_lamu_ files, phase_la / phase_mu; SI_ker_lamu2assm.F90:290-297)
+// on one rank.
 //
 // Inputs as the reference reads them: TomoKernel.conf (MAIN_CONF, snap_id: init_kernel
 // :437-449) and the main configuration's snapshot snap_id, whose subc is the kernel volume;
@@ -17,7 +19,7 @@
 // and .Kbp.unformat; at the end inv_G_band.conf (export_inv_info :573-585) and the scaled
 // sums inv_G_sum.Kap.unformat / .Kbp.unformat (export_G_sum :587-598).
 //
-// Usage: fwant_assm [TomoKernel.conf] [--kamu] [--device N] < answers
+// Usage: fwant_assm [TomoKernel.conf] [--kamu | --lamu] [--device N] < answers
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -215,13 +217,15 @@ std::vector<Pick> read_picks(const std::string& path) {
 int run(int argc, char** argv) {
   std::string ker_conf = "TomoKernel.conf";
   int device = 0;
-  bool kamu = false;
+  bool kamu = false, lamu = false;
   for (int a = 1; a < argc; ++a) {
     const std::string s = argv[a];
     if (s == "--device" && a + 1 < argc) device = std::atoi(argv[++a]);
     else if (s == "--kamu") kamu = true;
+    else if (s == "--lamu") lamu = true;
     else ker_conf = s;
   }
+  if (kamu && lamu) die("--kamu and --lamu exclude each other");
   const conf::Text kc(ker_conf);
   const std::string main_conf = kc.get("MAIN_CONF", 2);
   const int kid = kc.get_int("snap_id", 2);
@@ -253,8 +257,9 @@ int run(int argc, char** argv) {
   if (rc != FWANT_OK) die(std::string("inversion blocks: ") + (A ? fwant_assm_last_error(A) : "create failed"));
   std::printf("assemble phase-delay kernel ...\n");
 
-  const std::string prefix = kamu ? "kernel_kamu_" : "kernel_";
-  const char* const vname[2] = {kamu ? "phase_ka" : "phase_Vp", kamu ? "phase_mu" : "phase_Vs"};
+  const std::string prefix = kamu ? "kernel_kamu_" : (lamu ? "kernel_lamu_" : "kernel_");
+  const char* const vname[2] = {kamu ? "phase_ka" : (lamu ? "phase_la" : "phase_Vp"),
+                                (kamu || lamu) ? "phase_mu" : "phase_Vs"};
   int max_bdap = 0, max_bdbp = 0;
   double gpu_ms = 0.0;
   long npicks = 0;

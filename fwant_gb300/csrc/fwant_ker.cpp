@@ -22,6 +22,20 @@
 // lambda/mu kernels (SI_ker_sta_lamu.F90:1299-1300) into kernel_lamu_NNN_mpi000000_n00000.nc
 // (phase_la amplitude_la phase_mu amplitude_mu); everything else is the same.
 //
+// With --convert MODE the program is one of the kernel conversions, which walk the same
+// stations, blocks, events and picks (TomoKernel_conv.conf by default; on standard input the
+// input directory, the station list file, the rank id) but read each pick's kernel file
+// <input directory><pick directory>/<input file> block by block instead of forming it from
+// SGTs, convert it point by point with the block's lambda and mu on the device, and write
+// <pick directory>/<output file>:
+//   lamu2kamu  SI_ker_lamu2kamu: kernel_lamu_ (la, mu) -> kernel_ (kappa, mu, under the
+//              Vp/Vs variable names the reference gives them)
+//   lamu2vpvs  SI_ker_lamu2vpvs: kernel_lamu_ (la, mu) -> kernel_ (Vp, Vs)
+//   vpvs2kamu  SI_ker_vpvs2kamu: kernel_ (Vp, Vs) -> kernel_kamu_ (phase_ka amplitude_ka
+//              phase_mu amplitude_mu)
+// The time axis is T(n) = n kdt (SI_ker_lamu2kamu.F90:260-263): the synthetics are listed
+// but not read, and a pick whose window lies outside it is skipped as in the kernel run.
+//
 // Tool modes (format checks): --nc-slab FILE VAR START COUNT STRIDE prints a strided
 // sub-array as JSON; --nc-fill-slab FILE VAR START COUNT STRIDE writes 1, 2, ... into one
 // (comma-separated lists, slowest dimension first, 0-based starts).
@@ -319,19 +333,108 @@ int nc_tool(int argc, char** argv) {
   die("unknown tool mode " + mode);
 }
 
+// Window indices of a pick over T(n) = n kdt (maxloc(T, T <= t1), minloc(T, T >= t2);
+// SI_ker_sta.F90:676-704); false (with the reference's warning) when the pick is skipped.
+bool pick_window(const Pick& pk, const std::vector<float>& T, float tmin, float tmax, int* nt1, int* nt2) {
+  const int knt = int(T.size());
+  *nt1 = 0;
+  *nt2 = 0;
+  if (pk.t1 > tmax) {
+    std::fprintf(stderr, "fwant_ker: t1>Tmax, skip this rcd %s\n", pk.dir.c_str());
+    return false;
+  } else if (pk.t1 <= tmin) {
+    *nt1 = 1;
+  } else {
+    for (int n = 1; n <= knt; ++n)
+      if (T[size_t(n - 1)] <= pk.t1 && (*nt1 == 0 || T[size_t(n - 1)] > T[size_t(*nt1 - 1)])) *nt1 = n;
+  }
+  if (pk.t2 < tmin) {
+    std::fprintf(stderr, "fwant_ker: t2<Tmin, skip this rcd %s\n", pk.dir.c_str());
+    return false;
+  } else if (pk.t2 >= tmax) {
+    *nt2 = knt;
+  } else {
+    for (int n = 1; n <= knt; ++n)
+      if (T[size_t(n - 1)] >= pk.t2 && (*nt2 == 0 || T[size_t(n - 1)] < T[size_t(*nt2 - 1)])) *nt2 = n;
+  }
+  if (*nt1 < 1 || *nt2 < 1 || *nt1 > *nt2) die("window of pick " + pk.dir + " selects no sample");
+  return true;
+}
+
+// One block of the conversion programs (SI_ker_lamu2kamu.F90:346-836 and its two siblings):
+// every pick of every event, in the kernel run's order, has its input kernel block read,
+// converted on the device with the block's lambda and mu (already in K) and written into
+// its output file, which the first block of a first run creates.  Returns the picks done.
+long long convert_block(fwant_sgtker* K, int conv, const std::vector<Event>& events, const Geometry& g,
+                        const seisfd::SnapDef& sp, int kid, int knt, float kdt, float tmin, float tmax, bool create,
+                        const std::string& indir, const std::string& iprefix, const char* const* iname,
+                        const std::string& oprefix, const char* const* oname) {
+  std::vector<float> T(static_cast<size_t>(knt));
+  for (int n = 0; n < knt; ++n) T[size_t(n)] = float(n + 1) * kdt;  // T = (/1:knt/)*kdt
+  const size_t np = g.npts();
+  const std::vector<uint64_t> st = {uint64_t(g.bsubs[2] - 1), uint64_t(g.bsubs[1] - 1), uint64_t(g.bsubs[0] - 1)};
+  const std::vector<uint64_t> ct = {uint64_t(g.bsubc[2]), uint64_t(g.bsubc[1]), uint64_t(g.bsubc[0])};
+  const std::vector<uint64_t> sd = {uint64_t(g.bsubt[2]), uint64_t(g.bsubt[1]), uint64_t(g.bsubt[0])};
+  const std::string fname = seisfd::pad(kid, 3) + "_" + seisfd::MPI_SUFFIX + "_n00000.nc";
+  long long done = 0;
+  std::string err;
+  for (const Event& e : events) {
+    bool any = false;
+    for (int c = 0; c < 6; ++c) any = any || e.picknum[c] > 0;
+    if (!any) continue;
+    for (int ncmp = 1; ncmp <= 6; ++ncmp)
+      for (const Pick& pk : e.picks[ncmp - 1]) {
+        int nt1, nt2;
+        if (!pick_window(pk, T, tmin, tmax, &nt1, &nt2)) continue;
+        const std::string out = pk.dir + oprefix + fname;
+        if (create) {  // nfseis_grid3d_def over the snapshot's points
+          nc3::Writer wr;
+          const int di = wr.add_dim("I", uint64_t(sp.subc[0])), dj = wr.add_dim("J", uint64_t(sp.subc[1])),
+                    dk = wr.add_dim("K", uint64_t(sp.subc[2]));
+          wr.add_gatt_text("title", "Finite frequency kernel");
+          const size_t n3 = size_t(sp.subc[0]) * sp.subc[1] * sp.subc[2];
+          const std::vector<float> zero(n3, 0.0f);
+          for (int q = 0; q < 4; ++q) wr.add_var_f(oname[q], {dk, dj, di}, zero.data(), n3);
+          if (!wr.write(out, &err)) die(err);
+        }
+        const std::string in = indir + pk.dir + iprefix + fname;
+        nc3::Reader r;
+        if (!r.open(in, &err)) die(err);
+        std::vector<float> v[4];
+        for (int q = 0; q < 4; ++q) {
+          if (!r.read_slab(iname[q], st, ct, sd, &v[q], &err)) die(in + ": " + err);
+          if (v[q].size() != np) die(in + ": block size mismatch");
+        }
+        // kernel order of the files: phase a, amplitude a, phase b, amplitude b
+        check(fwant_sgtker_convert(K, conv, v[0].data(), v[1].data(), v[2].data(), v[3].data()), K, "convert");
+        for (int q = 0; q < 4; ++q)
+          if (!nc3::update_slab(out, oname[q], st, ct, sd, v[q].data(), &err)) die(err);
+        ++done;
+      }
+  }
+  return done;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
   if (argc >= 2 && std::strncmp(argv[1], "--nc-", 5) == 0) return nc_tool(argc, argv);
-  std::string ker_conf = "TomoKernel.conf";
+  std::string ker_conf;
   int device = 0;
   bool lamu = false;  // --lamu: the lambda/mu kernels of SI_ker_sta_lamu
+  int conv = 0;       // --convert: 1 lamu2kamu, 2 lamu2vpvs, 3 vpvs2kamu
   for (int a = 1; a < argc; ++a) {
     const std::string s = argv[a];
     if (s == "--device" && a + 1 < argc) device = std::atoi(argv[++a]);
     else if (s == "--lamu") lamu = true;
-    else ker_conf = s;
+    else if (s == "--convert" && a + 1 < argc) {
+      const std::string m = argv[++a];
+      conv = m == "lamu2kamu" ? 1 : (m == "lamu2vpvs" ? 2 : (m == "vpvs2kamu" ? 3 : 0));
+      if (!conv) die("--convert: mode must be lamu2kamu, lamu2vpvs or vpvs2kamu");
+    } else ker_conf = s;
   }
+  if (conv && lamu) die("--lamu and --convert exclude each other");
+  if (ker_conf.empty()) ker_conf = conv ? "TomoKernel_conv.conf" : "TomoKernel.conf";
   // init_kernel (SI_ker_sta.F90:1047-1082)
   conf::File kc;
   std::string err;
@@ -384,8 +487,13 @@ int main(int argc, char** argv) {
   }
   const std::vector<Filter> filters = read_filters(ker_conf, num_freq);
 
-  // standard input: the station list file, then the rank id (read *, n_i, n_j, n_k)
-  std::string sgt_list, line;
+  // standard input: (conversions: the input directory, one line, may be blank) the station
+  // list file, then the rank id (read *, n_i, n_j, n_k)
+  std::string sgt_list, line, indir;
+  if (conv) {
+    if (!std::getline(std::cin, line)) die("standard input: input directory line missing");
+    indir = unquote(trim(line));
+  }
   while (sgt_list.empty() && std::getline(std::cin, line)) sgt_list = unquote(trim(line));
   if (sgt_list.empty()) die("standard input: station list file name missing");
   {
@@ -434,8 +542,13 @@ int main(int argc, char** argv) {
   // variable names and file prefix: SI_ker_sta.F90:736-743, SI_ker_sta_lamu.F90:736-743
   static const char* const kname_vpvs[4] = {"phase_Vp", "amplitude_Vp", "phase_Vs", "amplitude_Vs"};
   static const char* const kname_lamu[4] = {"phase_la", "amplitude_la", "phase_mu", "amplitude_mu"};
-  const char* const* kname = lamu ? kname_lamu : kname_vpvs;
-  const std::string kprefix = lamu ? "/kernel_lamu_" : "/kernel_";
+  static const char* const kname_kamu[4] = {"phase_ka", "amplitude_ka", "phase_mu", "amplitude_mu"};
+  const char* const* kname = (lamu || conv == 1 || conv == 2) ? kname_lamu : kname_vpvs;  // kernel run / input
+  const std::string kprefix = (lamu || conv == 1 || conv == 2) ? "/kernel_lamu_" : "/kernel_";
+  // conversions: output names and file prefix (SI_ker_lamu2kamu.F90:741-748, SI_ker_lamu2vpvs.F90:741-748,
+  // SI_ker_vpvs2kamu.F90:741-748)
+  const char* const* oname = conv == 3 ? kname_kamu : kname_vpvs;
+  const std::string oprefix = conv == 3 ? "/kernel_kamu_" : "/kernel_";
   while (std::getline(sl, line)) {
     const auto w = words(line);
     if (w.empty()) continue;
@@ -474,6 +587,11 @@ int main(int argc, char** argv) {
               die(media_path + ": " + err);
             check(fwant_sgtker_set_media(K, lam.data(), mu.data()), K, "media");
           }
+          if (conv) {  // the conversion programs: kernel files in, converted kernel files out
+            written += convert_block(K, conv, events, g, *sp, kid, knt, kdt, tmin, tmax, first_run && first_block,
+                                     indir, kprefix, kname, oprefix, oname);
+            continue;
+          }
           bool have[3] = {false, false, false};  // station SGTs on the device for this block
           for (const Event& e : events) {
             const bool rot_any = e.picknum[3] > 0 || e.picknum[4] > 0 || e.picknum[5] > 0;
@@ -505,27 +623,8 @@ int main(int argc, char** argv) {
               }
               const int comp = (ncmp - 1) % 3;
               for (const Pick& pk : e.picks[ncmp - 1]) {
-                // window indices (maxloc(T, T <= t1), minloc(T, T >= t2); SI_ker_sta.F90:676-704)
-                int nt1 = 0, nt2 = 0;
-                if (pk.t1 > tmax) {
-                  std::fprintf(stderr, "fwant_ker: t1>Tmax, skip this rcd %s\n", pk.dir.c_str());
-                  continue;
-                } else if (pk.t1 <= tmin) {
-                  nt1 = 1;
-                } else {
-                  for (int n = 1; n <= knt; ++n)
-                    if (T[size_t(n - 1)] <= pk.t1 && (nt1 == 0 || T[size_t(n - 1)] > T[size_t(nt1 - 1)])) nt1 = n;
-                }
-                if (pk.t2 < tmin) {
-                  std::fprintf(stderr, "fwant_ker: t2<Tmin, skip this rcd %s\n", pk.dir.c_str());
-                  continue;
-                } else if (pk.t2 >= tmax) {
-                  nt2 = knt;
-                } else {
-                  for (int n = 1; n <= knt; ++n)
-                    if (T[size_t(n - 1)] >= pk.t2 && (nt2 == 0 || T[size_t(n - 1)] < T[size_t(nt2 - 1)])) nt2 = n;
-                }
-                if (nt1 < 1 || nt2 < 1 || nt1 > nt2) die("window of pick " + pk.dir + " selects no sample");
+                int nt1, nt2;
+                if (!pick_window(pk, T, tmin, tmax, &nt1, &nt2)) continue;
                 const std::string path = pk.dir + kprefix + seisfd::pad(kid, 3) + "_" + seisfd::MPI_SUFFIX + "_n00000.nc";
                 if (first_run && first_block) {  // nfseis_grid3d_def over the snapshot's points
                   nc3::Writer wr;
@@ -563,6 +662,6 @@ int main(int argc, char** argv) {
         }
   }
   if (K) fwant_sgtker_destroy(K);
-  std::printf("fwant_ker: %lld kernel blocks written\n", written);
+  std::printf("fwant_ker: %lld kernel blocks %s\n", written, conv ? "converted" : "written");
   return 0;
 }

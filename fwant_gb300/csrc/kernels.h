@@ -29,12 +29,17 @@ struct Geom {
   int freesurf;           // free surface on k = k2
 };
 
-// One PML slab (face x1 x2 y1 y2 z1 z2).  Its six memory variables are stored compactly:
-// element (i,j,k) at (i-i1) + sx*((j-j1) + sy*(k-k1)), variables vstride apart.
+// One PML slab (face x1 x2 y1 y2 z1 z2), points i1..i2 x j1..j2 x k1..k2.  Its six memory
+// variables are stored as rows padded to 16 bytes: element (i,j,k) at
+// (i-ox) + sx*((j-j1) + sy*(k-k1)), variables vstride apart, with the row origin ox <= i1
+// congruent to the first interior column mod 4 and sx a multiple of 4, so that the part of
+// a row under any 32-column tile is a 16-byte-aligned run of whole 16-byte units (the stage
+// kernel copies it with cp.async.bulk).
 struct Slab {
   int on;
   int i1, i2, j1, j2, k1, k2;
   int sx, sy;
+  int ox;
   long long vstride;
 };
 
@@ -122,6 +127,11 @@ struct StageArgs {
   const float* pad[3];
   const float* pD[3];
   Slab slab[6];
+  // TMA descriptors of the six faces' memory variables (device memory, one 5-D tensor per
+  // face: x, y, z of the slab, variable, register set; null without PML) and the register
+  // sets this stage reads as input, m and t
+  const CUtensorMap* pml_map;
+  int pml_set[3];
   const float* ain[6];
   const float* am[6];
   float* aout[6];
@@ -276,6 +286,10 @@ void launch_iir(const IirArgs& a, void* stream);
 // Rotation of the three force components of the series: slots (0,1,2) and (3,5,4),
 // new_c = sum_d rot[d + 3c] old_d (rot column-major, SI_ker_sta.F90:1339-1373).
 void launch_rotate_series(double* series, long long slot_len, const double rot[9], void* stream);
+// Kernel parameter conversion in place over n points (mode 1 lambda/mu -> kappa/mu, 2
+// lambda/mu -> Vp/Vs, 3 Vp/Vs -> kappa/mu), phase and amplitude pairs (ka0, kb0), (ka1, kb1).
+void launch_convert_kernel(int mode, long long n, const float* lam, const float* mu, float* ka0, float* ka1,
+                           float* kb0, float* kb1, void* stream);
 
 void launch_metric_fp64(int n, const float* coord, float* metric_out, int lo, int hi, void* stream);
 void launch_sincot_fp64(int n, const float* x, float* xsin, float* xcot, void* stream);

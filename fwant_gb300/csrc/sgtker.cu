@@ -214,6 +214,42 @@ __global__ void rotate_series_kernel(double* s, long long len, const double r0, 
   }
 }
 
+// Kernel parameter conversions of the kernel-file programs, one thread per point, FP32
+// with every operation rounded separately in the reference's operand order (no
+// contraction), so the device equals the reference's single-precision loops.
+//   mode 1 SI_ker_lamu2kamu.F90:823-830, 2 SI_ker_lamu2vpvs.F90:823-830,
+//   3 SI_ker_vpvs2kamu.F90:823-831.
+__global__ void convert_kernel_kernel(int mode, long long n, const float* __restrict__ lam,
+                                      const float* __restrict__ mu, float* __restrict__ ka0, float* __restrict__ ka1,
+                                      float* __restrict__ kb0, float* __restrict__ kb1) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const float l = lam[e], m = mu[e];
+  float* const ka[2] = {ka0, ka1};
+  float* const kb[2] = {kb0, kb1};
+  for (int q = 0; q < 2; ++q) {  // phase (p) then amplitude (q) pair
+    float a = ka[q][e], b = kb[q][e];
+    if (mode == 1) {
+      a = __fdiv_rn(a, l);
+      b = __fdiv_rn(__fdiv_rn(b, m), 2.0f);
+      b = __fmul_rn(__fsub_rn(__fmul_rn(2.0f, b), __fdiv_rn(__fmul_rn(2.0f, a), 3.0f)), m);
+      a = __fmul_rn(a, __fadd_rn(l, __fdiv_rn(__fmul_rn(2.0f, m), 3.0f)));
+    } else if (mode == 2) {
+      a = __fdiv_rn(a, l);
+      b = __fdiv_rn(__fdiv_rn(b, m), 2.0f);
+      b = __fmul_rn(__fmul_rn(__fmul_rn(2.0f, __fsub_rn(b, a)), 2.0f), m);
+      a = __fmul_rn(__fmul_rn(a, 2.0f), __fadd_rn(l, __fmul_rn(2.0f, m)));
+    } else {
+      a = __fdiv_rn(a, __fmul_rn(2.0f, __fadd_rn(l, __fmul_rn(2.0f, m))));
+      b = __fadd_rn(__fdiv_rn(__fdiv_rn(b, m), 4.0f), a);
+      b = __fmul_rn(__fsub_rn(__fmul_rn(2.0f, b), __fdiv_rn(__fmul_rn(2.0f, a), 3.0f)), m);
+      a = __fmul_rn(a, __fadd_rn(l, __fdiv_rn(__fmul_rn(2.0f, m), 3.0f)));
+    }
+    ka[q][e] = a;
+    kb[q][e] = b;
+  }
+}
+
 }  // namespace
 
 void launch_iir(const IirArgs& a, void* stream) {
@@ -235,6 +271,13 @@ int launch_sgt_scatter(const ScatterArgs& a, int /*sm_count*/, void* stream) {
   dim3 grid((unsigned)a.npts, 3, (unsigned)((nout + SC_THREADS - 1) / SC_THREADS));
   sgt_scatter_kernel<<<grid, SC_THREADS, smem, (cudaStream_t)stream>>>(a);
   return int(cudaGetLastError());
+}
+
+void launch_convert_kernel(int mode, long long n, const float* lam, const float* mu, float* ka0, float* ka1,
+                           float* kb0, float* kb1, void* stream) {
+  if (n <= 0) return;
+  convert_kernel_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(mode, n, lam, mu, ka0, ka1,
+                                                                                      kb0, kb1);
 }
 
 void launch_scatter_kernel(const KernelArgs& a, void* stream) {

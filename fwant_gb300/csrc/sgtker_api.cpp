@@ -251,6 +251,31 @@ fwant_status fwant_sgtker_kernel_filtered(fwant_sgtker* k, int ncmp, const float
                                           int nt2, double sgt_m0, int mode, int nod1, const double* b,
                                           const double* a, double* kap, double* kaq, double* kbp, double* kbq);
 
+fwant_status fwant_sgtker_convert(fwant_sgtker* k, int mode, float* kap, float* kaq, float* kbp, float* kbq) {
+  if (!k || !kap || !kaq || !kbp || !kbq) return FWANT_ERR_INVALID_ARG;
+  if (mode < 1 || mode > 3) return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_convert: mode must be 1, 2 or 3");
+  if (!k->have_media) return k->fail(FWANT_ERR_STATE, "sgtker_convert: media not set");
+  cudaSetDevice(k->device);
+  // the four arrays share one device buffer (the window-kernel outputs' FP64 space holds them)
+  fwant_status rc = k->alloc(&k->kout, 4 * size_t(k->npts), "kernel outputs");
+  if (rc != FWANT_OK) return rc;
+  float* d = reinterpret_cast<float*>(k->kout);
+  const size_t n = size_t(k->npts), bytes = n * sizeof(float);
+  float* const host[4] = {kap, kaq, kbp, kbq};
+  cudaError_t e = cudaSuccess;
+  for (int q = 0; q < 4 && e == cudaSuccess; ++q)
+    e = cudaMemcpyAsync(d + q * n, host[q], bytes, cudaMemcpyHostToDevice, k->st);
+  if (e == cudaSuccess) {
+    fw::launch_convert_kernel(mode, k->npts, k->lam, k->mu, d, d + n, d + 2 * n, d + 3 * n, k->st);
+    e = cudaGetLastError();
+  }
+  for (int q = 0; q < 4 && e == cudaSuccess; ++q)
+    e = cudaMemcpyAsync(host[q], d + q * n, bytes, cudaMemcpyDeviceToHost, k->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(k->st);
+  if (e != cudaSuccess) return k->cuda_fail(e, "sgtker_convert");
+  return FWANT_OK;
+}
+
 fwant_status fwant_sgtker_kernel(fwant_sgtker* k, int ncmp, const float* v, const float* u, int nt1, int nt2,
                                  double sgt_m0, double* kap, double* kaq, double* kbp, double* kbq) {
   return fwant_sgtker_kernel_filtered(k, ncmp, v, u, nt1, nt2, sgt_m0, 0, 0, nullptr, nullptr, kap, kaq, kbp, kbq);

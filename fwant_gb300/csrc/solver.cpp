@@ -80,6 +80,7 @@ struct fwant_solver {
   int absn[6] = {0, 0, 0, 0, 0, 0};
   fw::Slab slab[6]{};
   float* aux[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // 4 sets each
+  CUtensorMap* d_pml_map = nullptr;  // per face: x, y, z, variable, register set (device memory)
   long long aux_set[6] = {0, 0, 0, 0, 0, 0};                               // elements per set
   std::vector<float> hA[3], hB[3], hD[3];
 
@@ -138,6 +139,7 @@ struct fwant_solver {
     cudaFree(d_x); cudaFree(d_y); cudaFree(d_z); cudaFree(d_xsin); cudaFree(d_xcot);
     cudaFree(d_xi); cudaFree(d_eta); cudaFree(d_zeta); cudaFree(d_prof); cudaFree(d_rzinv); cudaFree(d_rsinv);
     for (int f = 0; f < 6; ++f) cudaFree(aux[f]);
+    cudaFree(d_pml_map);
     cudaFree(d_rec); cudaFree(d_seis); cudaFree(d_ntime); cudaFree(d_maxbits); cudaFree(d_snap); cudaFree(d_conv); cudaFree(d_sgt); cudaFree(d_items);
     cudaFree(d_h); cudaFree(d_hxi); cudaFree(d_heta); cudaFree(d_sk); cudaFree(d_rzf); cudaFree(d_topo); cudaFree(d_topo_sf);
     if (ev0) cudaEventDestroy(ev0);
@@ -326,6 +328,50 @@ struct fwant_solver {
     return FWANT_OK;
   }
 
+  // TMA descriptors of the PML faces, in device memory: per face a 5-D tensor over its four
+  // register sets (x: sx, y: sy, z: the slab's planes, the six variables vstride apart, the
+  // sets 6 vstride apart); the stage kernel loads TX x TY x 1 x 6 x 1 boxes of them.
+  fwant_status make_pml_maps() {
+    using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || !fn || q != cudaDriverEntryPointSuccess)
+      return fail(FWANT_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+    CUtensorMap maps[6];
+    std::memset(maps, 0, sizeof(maps));
+    bool any = false;
+    for (int f = 0; f < 6; ++f) {
+      const fw::Slab& s = slab[f];
+      if (!s.on) continue;
+      any = true;
+      const cuuint64_t sz = cuuint64_t(s.k2 - s.k1 + 1), vs = cuuint64_t(s.vstride);
+      const cuuint64_t dims[5] = {cuuint64_t(s.sx), cuuint64_t(s.sy), sz, 6, 4};
+      const cuuint64_t strides[4] = {cuuint64_t(s.sx) * 4, cuuint64_t(s.sx) * s.sy * 4, vs * 4, 6 * vs * 4};
+      const cuuint32_t box[5] = {fw::STAGE_TX, fw::STAGE_TY, 1, 6, 1};
+      const cuuint32_t el[5] = {1, 1, 1, 1, 1};
+      if (reinterpret_cast<EncodeFn>(fn)(&maps[f], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, aux[f], dims, strides, box, el,
+                                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                         CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return fail(FWANT_ERR_CUDA, "PML tensor map encoding failed");
+    }
+    if (!any) return FWANT_OK;
+    if (!d_pml_map) {
+      void* p = nullptr;
+      if (cudaMalloc(&p, sizeof(maps)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(FWANT_ERR_OOM, "PML descriptors");
+      }
+      d_pml_map = static_cast<CUtensorMap*>(p);
+    }
+    e = cudaMemcpy(d_pml_map, maps, sizeof(maps), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "PML descriptors");
+    return FWANT_OK;
+  }
+
   // 1/z and 1/xsin for the fast arithmetic form
   cudaError_t upload_reciprocals() {
     std::vector<float> rz(g.nz), rs(g.nx);
@@ -439,7 +485,8 @@ struct fwant_solver {
       if (absn[f] <= 0) continue;
       s.on = 1;
       s.i1 = b[f][0]; s.i2 = b[f][1]; s.j1 = b[f][2]; s.j2 = b[f][3]; s.k1 = b[f][4]; s.k2 = b[f][5];
-      s.sx = s.i2 - s.i1 + 1; s.sy = s.j2 - s.j1 + 1;
+      s.ox = s.i1 - ((s.i1 - g.i1) & 3);                 // rows start 16-byte aligned under every tile
+      s.sx = ((s.i2 - s.ox + 1) + 3) / 4 * 4; s.sy = s.j2 - s.j1 + 1;
       const long long n = (long long)s.sx * s.sy * (s.k2 - s.k1 + 1);
       s.vstride = ((n + 31) / 32) * 32;
       aux_set[f] = 6 * s.vstride;
@@ -447,6 +494,7 @@ struct fwant_solver {
       if (!aux[f]) return fail(FWANT_ERR_OOM, "PML allocation failed");
       cudaMemset(aux[f], 0, size_t(4) * aux_set[f] * sizeof(float));
     }
+    if (fwant_status rc = make_pml_maps(); rc != FWANT_OK) return rc;
     drop_graphs();
     src_dirty = true;  // the surface-source list depends on the free-surface flag
     return FWANT_OK;
@@ -708,6 +756,8 @@ struct fwant_solver {
       a.tm_topo = tm_topo;
       a.topo_sf = d_topo_sf;
     }
+    a.pml_map = d_pml_map;
+    a.pml_set[0] = in_of[s]; a.pml_set[1] = ra; a.pml_set[2] = rt;
     for (int f = 0; f < 6; ++f) {
       if (!slab[f].on) continue;
       a.ain[f] = aset(f, in_of[s]); a.am[f] = aset(f, ra); a.aout[f] = aset(f, out_of[s]); a.at[f] = aset(f, rt);

@@ -75,8 +75,29 @@ struct Lay {
   static constexpr int OFF_MT_L = 2 * BUF_BYTES_LEAN;
   template <int RK>
   static constexpr int SZ_MT_L = RK == 1 ? 2 * SZ_PT : (RK == 2 ? SZ_PT : 0);
+  // Full form: the PML memory variables of staged slab faces (up to pml_slots per item; the
+  // terrain form stages none).  The stage input's six variables of a face (TX x TY x 6 FP32)
+  // ride in the pipeline buffer with the tile, one plane ahead: RK_beg and RK_fin put them
+  // in the buffer's m / t space that they do not use (when it is large enough), RK_inn after
+  // t.  The RK registers m and t of the variables (RK_inn: both, RK_fin: t), needed only for
+  // the final update, go to one area after the two buffers, loaded at the start of their
+  // plane on a barrier of their own.
+  static constexpr int SZ_PML_PLANE = 6 * TY * TX * 4;
+  __host__ __device__ static constexpr int pml_slots(int rk) { return TOPO ? 0 : (rk == 0 ? 3 : 1); }
+  __host__ __device__ static constexpr int pml_single_roles(int rk) { return rk == 1 ? 2 : (rk == 2 ? 1 : 0); }
+  __host__ __device__ static constexpr bool pml_in_mt(int rk) {  // the input slots reuse the m / t space
+    return rk != 1 && pml_slots(rk) * SZ_PML_PLANE <= (rk == 0 ? 2 : 1) * SZ_PT;
+  }
+  __host__ __device__ static constexpr int off_pa(int rk) { return pml_in_mt(rk) ? OFF_M : OFF_T + SZ_PT; }
+  __host__ __device__ static constexpr int buf_full(int rk) {
+    return pml_in_mt(rk) ? BUF_BYTES : ((OFF_T + SZ_PT + pml_slots(rk) * SZ_PML_PLANE + 1023) / 1024) * 1024;
+  }
+  __host__ __device__ static constexpr int pml_single_bytes(int rk) {
+    return pml_slots(rk) * pml_single_roles(rk) * SZ_PML_PLANE;
+  }
   static int smem_bytes(bool lean, int rk) {
-    return lean ? OFF_MT_L + (rk == 1 ? 2 * SZ_PT : (rk == 2 ? SZ_PT : 0)) + 64 : SMEM_BYTES;
+    return lean ? OFF_MT_L + (rk == 1 ? 2 * SZ_PT : (rk == 2 ? SZ_PT : 0)) + 64
+                : 2 * buf_full(rk) + pml_single_bytes(rk) + 64;
   }
 };
 
@@ -132,6 +153,16 @@ __device__ __forceinline__ void fence_barrier_init() {
 }
 __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// 5-D tiled load (the PML faces: x, y, z, variable, register set); the descriptor may sit
+// in device memory.
+__device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap* map, int x, int y, int z, int v, int r,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], "
+      "[%7];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(v), "r"(r), "r"(bar)
+      : "memory");
 }
 __device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, int x, int y, int z, int w,
                                             uint32_t bar) {
@@ -263,9 +294,15 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
   using L = Lay<S, TOPO>;
   constexpr int NQ = L::NQ;
   constexpr int TBX = L::TBX, HX = L::HX;
-  constexpr int BUF_BYTES = LEAN ? L::BUF_BYTES_LEAN : L::BUF_BYTES, OFF_Q = LEAN ? L::OFF_Q_L : L::OFF_Q,
+  constexpr int BUF_BYTES = LEAN ? L::BUF_BYTES_LEAN : L::buf_full(RK), OFF_Q = LEAN ? L::OFF_Q_L : L::OFF_Q,
                 OFF_MED = LEAN ? L::OFF_MED_L : L::OFF_MED, OFF_M = L::OFF_M, OFF_T = L::OFF_T;
-  constexpr int OFF_BAR = LEAN ? L::OFF_MT_L + L::template SZ_MT_L<RK> : 2 * L::BUF_BYTES;
+  // PML staging (full form): faces staged per item; the input variables at OFF_PA of each
+  // pipeline buffer, the m / t variables (NROLE_S roles) in the area at OFF_PS
+  constexpr int NSLOT = LEAN ? 0 : L::pml_slots(RK);
+  constexpr int NROLE_S = L::pml_single_roles(RK);
+  constexpr int OFF_PA = L::off_pa(RK);
+  constexpr int OFF_PS = 2 * BUF_BYTES;
+  constexpr int OFF_BAR = LEAN ? L::OFF_MT_L + L::template SZ_MT_L<RK> : OFF_PS + L::pml_single_bytes(RK);
   constexpr int HY = FY ? 1 : 3;  // row of the CTA's first row inside the tile box (tile_halo_y)
   const Geom& g = A.g;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
@@ -311,10 +348,12 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
   const uint32_t bar0 = smem_u32(smem + OFF_BAR);
   const uint32_t bar_mt = bar0 + 16;
   auto bar_rk = [&](int b) -> uint32_t { return bar0 + 24 + 8 * b; };
+  const uint32_t bar_pml = bar0 + 40;
   if (tid == 0) {
     mbar_init(bar0, 1);
     mbar_init(bar0 + 8, 1);
     if (LEAN && RK >= 1) mbar_init(bar_mt, 1);
+    if (NSLOT > 0 && NROLE_S > 0) mbar_init(bar_pml, 1);
     if (SPLIT) {
       mbar_init(bar_rk(0), 1);
       mbar_init(bar_rk(1), 1);
@@ -323,13 +362,58 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
   }
   __syncthreads();
 
+  // PML faces whose memory variables this item stages through shared memory (the first
+  // NSLOT faces, in face order, that overlap the item): slot per face in 4-bit fields, 15
+  // for a face read from global memory.
+  unsigned slots = 0xFFFFFFu, staged = 0u;
+  if (NSLOT > 0) {
+    const int ie = min(i0 + TX - 1, g.i2), je = min(j0 + TY - 1, g.j2);
+    int nq = 0;
+#pragma unroll 1
+    for (int sidx = 0; sidx < 6 && nq < NSLOT; ++sidx) {
+      const Slab& sl = A.slab[sidx];
+      if (sl.on && sl.i1 <= ie && sl.i2 >= i0 && sl.j1 <= je && sl.j2 >= j0 && sl.k1 <= ke && sl.k2 >= kb) {
+        slots = (slots & ~(15u << (4 * sidx))) | (unsigned(nq) << (4 * sidx));
+        staged |= 1u << sidx;
+        ++nq;
+      }
+    }
+  }
+  // Staged faces holding plane kp (the same count in every thread).
+  auto n_staged = [&](int kp) -> uint32_t {
+    uint32_t n = 0;
+#pragma unroll 1
+    for (unsigned mk = staged; mk; mk &= mk - 1) {
+      const Slab& sl = A.slab[__ffs(mk) - 1];
+      n += (kp >= sl.k1 && kp <= sl.k2) ? 1u : 0u;
+    }
+    return n;
+  };
+  // One TMA box (TX x TY x 1 plane x 6 variables) of register set `set` of every staged face
+  // holding plane kp, face slot q at dst + q * SZ_PML_PLANE * per_slot.  The box origin
+  // (i0 - ox) is 16-byte aligned by the padded slab layout; parts outside the face read 0
+  // and are never used.
+  auto load_faces = [&](uint32_t dst, int per_slot, int kp, int set, uint32_t bar) {
+#pragma unroll 1
+    for (unsigned mk = staged; mk; mk &= mk - 1) {
+      const int sidx = __ffs(mk) - 1;
+      const Slab& sl = A.slab[sidx];
+      if (kp < sl.k1 || kp > sl.k2) continue;
+      const int q = int((slots >> (4 * sidx)) & 15u);
+      tma_load_5d(dst + uint32_t(q * per_slot * L::SZ_PML_PLANE), A.pml_map + sidx, i0 - sl.ox, j0 - sl.j1,
+                  kp - sl.k1, 0, set, bar);
+    }
+  };
   const uint64_t pol_stream = policy_evict_first();
   const uint64_t pol_keep = policy_evict_last();
   auto issue = [&](int kp, int b) {
     const uint32_t base = smem_u32(smem + b * BUF_BYTES);
     const uint32_t bar = bar0 + 8 * b;
     fence_proxy_async();
-    mbar_expect_tx(bar, TX_BYTES);
+    // the staged faces' input variables of plane kp ride with the tile
+    const uint32_t npa = NSLOT > 0 ? n_staged(kp) : 0u;
+    mbar_expect_tx(bar, TX_BYTES + npa * uint32_t(L::SZ_PML_PLANE));
+    if (npa) load_faces(base + OFF_PA, 1, kp, A.pml_set[0], bar);
     if (LEAN) {
       tma_load_4d(base, &A.tm_tile_lo, i0 - HX + PADL, j0 - HY, kp, 0, bar);
       tma_load_4d(base + L::OFF_HI_L, &A.tm_tile_hi, i0 - HX + PADL, j0 - HY, kp, 4, bar);
@@ -476,10 +560,10 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
   // loads then hit L1 instead of exposing DRAM latency inside the compute).
   auto prefetch_pml = [&](int kp) {
 #pragma unroll 1
-    for (unsigned mk = slab_mask(kp); mk; mk &= mk - 1) {
+    for (unsigned mk = slab_mask(kp) & ~staged; mk; mk &= mk - 1) {
       const int sidx = __ffs(mk) - 1;
       const Slab& sl = A.slab[sidx];
-      const int qa = (i - sl.i1) + sl.sx * ((j - sl.j1) + sl.sy * (kp - sl.k1));
+      const int qa = (i - sl.ox) + sl.sx * ((j - sl.j1) + sl.sy * (kp - sl.k1));
 #pragma unroll
       for (int v = 0; v < 6; ++v) {
         asm volatile("prefetch.global.L1 [%0];" ::"l"(A.ain[sidx] + qa + v * sl.vstride));
@@ -490,12 +574,27 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
   };
   if (!LEAN) prefetch_pml(kb);
 
+  // m / t variables of plane kp into the single area (thread 0); bytes (all threads)
+  auto issue_pml_mt = [&](int kp) -> uint32_t {
+    const uint32_t bytes = NROLE_S > 0 ? n_staged(kp) * uint32_t(NROLE_S * L::SZ_PML_PLANE) : 0u;
+    if (bytes == 0 || tid != 0) return bytes;
+    fence_proxy_async();
+    mbar_expect_tx(bar_pml, bytes);
+    const uint32_t base = smem_u32(smem + OFF_PS);
+    load_faces(base, NROLE_S, kp, A.pml_set[RK == 1 ? 1 : 2], bar_pml);
+    if (RK == 1) load_faces(base + uint32_t(L::SZ_PML_PLANE), NROLE_S, kp, A.pml_set[2], bar_pml);
+    return bytes;
+  };
+  int pml_ph = 0;  // completed PML staging phases
+
   int it = 0;
   for (int k = kb; k <= ke; ++k, ++it) {
     const int cur = it & 1;
     // (every thread finished the previous plane, so the RK buffer is free)
     if (LEAN && RK >= 1 && tid == 0) issue_mt(k);
     if (tid == 0 && k < ke) issue(k + 1, cur ^ 1);
+    // this plane's staged PML m / t variables (the previous plane's readers are done)
+    const uint32_t pml_k = NSLOT > 0 ? issue_pml_mt(k) : 0u;
     if (!LEAN && k < ke) prefetch_pml(k + 1);
     const bool ok = mbar_wait(bar0 + 8 * cur, (it >> 1) & 1);
     unsigned char* buf = smem + cur * BUF_BYTES;
@@ -545,7 +644,7 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
       __syncthreads();
     }
 
-    bool ok_mt = true;
+    bool ok_mt = true, ok_p = true;
     if (ok && act) {
       // advance the z queue with plane k+LEAD (the image applies on and above the surface)
       const bool img = fsurf && k + LEAD >= g.k2;
@@ -744,6 +843,11 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
       }
 
       // ---- CFS-PML slabs in the reference's order x1 x2 y1 y2 z1 z2 (additive at corners)
+      // staged faces: the input variables in this plane's buffer, m / t in the single area
+      // (waited for at their first use)
+      const float* pml_a = reinterpret_cast<const float*>(buf + OFF_PA) + ty * TX + tx;
+      const float* pml_s = reinterpret_cast<const float*>(smem + OFF_PS) + ty * TX + tx;
+      bool waited_s = false;
       const float tc13 = lam, tc66 = miu;
       const float tc11 = tc13 + 2.0f * tc66;
       const float tc12 = tc13, tc22 = tc11, tc23 = tc13, tc33 = tc11, tc44 = tc66, tc55 = tc66;
@@ -752,18 +856,23 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
         const int sidx = __ffs(mk) - 1;
         const Slab& sl = A.slab[sidx];
         const int axis = sidx >> 1;
+        // staged face: slot q in shared memory, variable v (role r of the m / t area)
+        const int q = int((slots >> (4 * sidx)) & 15u);
+        const bool stg = NSLOT > 0 && q != 15;
+        auto PA = [&](int v) -> float { return pml_a[(q * 6 + v) * TY * TX]; };
+        auto PS = [&](int r, int v) -> float { return pml_s[((q * NROLE_S + r) * 6 + v) * TY * TX]; };
         const int ia = axis == 0 ? i : (axis == 1 ? j : k);
         const float b1 = __ldg(A.pb1[axis] + ia), b1_1 = __ldg(A.pb11[axis] + ia);
         const float ad = __ldg(A.pad[axis] + ia), Dv = __ldg(A.pD[axis] + ia);
         float d[6];
 #pragma unroll
         for (int v = 0; v < 6; ++v) d[v] = axis == 0 ? dx_[v] : (axis == 1 ? dy_[v] : dz_[v]);
-        const int qa = (i - sl.i1) + sl.sx * ((j - sl.j1) + sl.sy * (k - sl.k1));
+        const int qa = (i - sl.ox) + sl.sx * ((j - sl.j1) + sl.sy * (k - sl.k1));
         const long long vs = sl.vstride;
         const float* __restrict__ ai = A.ain[sidx] + qa;
         float av[6], h[6];
 #pragma unroll
-        for (int v = 0; v < 6; ++v) av[v] = ld_stream(ai + v * vs, pol_stream);
+        for (int v = 0; v < 6; ++v) av[v] = stg ? PA(v) : ld_stream(ai + v * vs, pol_stream);
         hVx = hVx + (b1_1 * d[0] - b1 * av[0]) * rrho; h[0] = Dv * d[0] - ad * av[0];
         hVy = hVy + (b1_1 * d[1] - b1 * av[1]) * rrho; h[1] = Dv * d[1] - ad * av[1];
         hVz = hVz + (b1_1 * d[2] - b1 * av[2]) * rrho; h[2] = Dv * d[2] - ad * av[2];
@@ -806,16 +915,23 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
         // abs_RK_* (mod_abs_npml.F90:738-1105)
         float* __restrict__ ao = A.aout[sidx] + qa;
         float* __restrict__ at = A.at[sidx] + qa;
+        if (NROLE_S > 0 && stg && !waited_s) {
+          ok_p = mbar_wait(bar_pml, pml_ph & 1);
+          waited_s = true;
+        }
 #pragma unroll
-        for (int v = 0; v < 6; ++v) {
+        for (int v = 0; v < 6 && ok_p; ++v) {
           if (RK == 0) {
             st_stream(ao + v * vs, av[v] + A.a * h[v], pol_stream);
             st_stream(at + v * vs, av[v] + A.b * h[v], pol_stream);
           } else if (RK == 1) {
-            st_stream(ao + v * vs, ld_stream(A.am[sidx] + qa + v * vs, pol_stream) + A.a * h[v], pol_stream);
-            st_stream(at + v * vs, ld_rw_stream(at + v * vs, pol_stream) + A.b * h[v], pol_stream);
+            const float mv = stg ? PS(0, v) : ld_stream(A.am[sidx] + qa + v * vs, pol_stream);
+            const float tv = stg ? PS(1, v) : ld_rw_stream(at + v * vs, pol_stream);
+            st_stream(ao + v * vs, mv + A.a * h[v], pol_stream);
+            st_stream(at + v * vs, tv + A.b * h[v], pol_stream);
           } else {
-            st_stream(at + v * vs, ld_rw_stream(at + v * vs, pol_stream) + A.b * h[v], pol_stream);
+            const float tv = stg ? PS(0, v) : ld_rw_stream(at + v * vs, pol_stream);
+            st_stream(at + v * vs, tv + A.b * h[v], pol_stream);
           }
         }
       }
@@ -859,7 +975,7 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
       hh[VX] = hVx; hh[VY] = hVy; hh[VZ] = hVz; hh[TZZ] = hTzz; hh[TXZ] = hTxz; hh[TYZ] = hTyz;
       hh[TXX] = hTxx; hh[TYY] = hTyy; hh[TXY] = hTxy;
 #pragma unroll
-      for (int f = 0; f < NF && ok_mt; ++f) {
+      for (int f = 0; f < NF && ok_mt && ok_p; ++f) {
         const long long o = f * fs + p;
         if (RK == 0) {
           // the tile holds the stored input; on the surface the imaged components were
@@ -877,10 +993,11 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
       }
     }
     // all threads agree on a timeout before leaving the pipeline
-    if (__syncthreads_or(!ok || !ok_mt)) {
+    if (__syncthreads_or(!ok || !ok_mt || !ok_p)) {
       if (tid == 0) {
         atomicExch(A.err, DEVERR_TMA_TIMEOUT);
         if (k < ke) mbar_wait(bar0 + 8 * (cur ^ 1), ((it + 1) >> 1) & 1);  // copies still in flight
+        if (NSLOT > 0 && pml_k) mbar_wait(bar_pml, pml_ph & 1);
         if (LEAN && RK >= 1) mbar_wait(bar_mt, it & 1);
         if (SPLIT) {
           mbar_wait(bar_rk(cur), (it >> 1) & 1);
@@ -889,11 +1006,13 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
       }
       return false;
     }
+    if (pml_k) ++pml_ph;
   }
   // every issued copy has been waited for (the last plane issues none)
   if (tid == 0) {
     mbar_inval(bar0);
     mbar_inval(bar0 + 8);
+    if (NSLOT > 0 && NROLE_S > 0) mbar_inval(bar_pml);
     if (LEAN && RK >= 1) mbar_inval(bar_mt);
     if (SPLIT) {
       mbar_inval(bar_rk(0));

@@ -328,6 +328,13 @@ fwant_status fwant_sgtker_rotate(fwant_sgtker* k, const double rot[9]);
 fwant_status fwant_sgtker_kernel_filtered(fwant_sgtker* k, int ncmp, const float* v, const float* u, int nt1,
                                           int nt2, double sgt_m0, int mode, int nod1, const double* b,
                                           const double* a, double* kap, double* kaq, double* kbp, double* kbq);
+/* Kernel parameter conversion of the kernel-file programs, in place over the block's npts
+ * points with the lambda, mu of fwant_sgtker_set_media (FP32, the reference's operand
+ * order): kap/kbp the phase kernels of the two parameters, kaq/kbq the amplitude kernels.
+ *   mode 1 lambda/mu -> kappa/mu  SI_ker_lamu2kamu (code/srcF.kernel/SI_ker_lamu2kamu.F90:823-830)
+ *   mode 2 lambda/mu -> Vp/Vs     SI_ker_lamu2vpvs (code/srcF.kernel/SI_ker_lamu2vpvs.F90:823-830)
+ *   mode 3 Vp/Vs -> kappa/mu      SI_ker_vpvs2kamu (code/srcF.kernel/SI_ker_vpvs2kamu.F90:823-831) */
+fwant_status fwant_sgtker_convert(fwant_sgtker* k, int mode, float* kap, float* kaq, float* kbp, float* kbq);
 /* Device time of the last fwant_sgtker_scatter in milliseconds.  No counterpart in the
  * reference. */
 fwant_status fwant_sgtker_last_scatter_ms(fwant_sgtker* k, double* ms);

@@ -101,7 +101,7 @@ def _f(v):
     return repr(float(np.float32(v)))
 
 
-@pytest.mark.parametrize("kamu", [False, True], ids=["vpvs", "kamu"])
+@pytest.mark.parametrize("kamu", [False, True, "lamu"], ids=["vpvs", "kamu", "lamu"])
 def test_program_writes_the_reference_files(kamu, native_lib, tmp_path):
     from scipy.io import netcdf_file
 
@@ -131,8 +131,8 @@ def test_program_writes_the_reference_files(kamu, native_lib, tmp_path):
     with open(os.path.join(tmp, "sta.lst"), "w") as f:
         f.write("STA1 evt1.lst\n# STA9 skipped.lst\nSTA2 evt2.lst\n")
     os.makedirs(os.path.join(tmp, "spool"))
-    names = ["phase_ka", "phase_mu"] if kamu else ["phase_Vp", "phase_Vs"]
-    prefix = "kernel_kamu_" if kamu else "kernel_"
+    names = (["phase_la", "phase_mu"] if kamu == "lamu" else ["phase_ka", "phase_mu"]) if kamu else ["phase_Vp", "phase_Vs"]
+    prefix = ("kernel_lamu_" if kamu == "lamu" else "kernel_kamu_") if kamu else "kernel_"
     ker = []
     for p, d in enumerate(picks):
         ks = ac.kernels(SHAPE, 2, seed=20 + p)
@@ -144,7 +144,7 @@ def test_program_writes_the_reference_files(kamu, native_lib, tmp_path):
     ka = np.float32(np.median(np.abs(B0 * Ca)))    # about half the blocks above the threshold
     kb = np.float32(np.median(np.abs(A.project(ker[0][1], volume, npix, pixs) * Cb)))
     answers = f"sta.lst\nblocks.nc\nspool\n{_f(Ca)}, 1.0 {_f(Cb)}\n1.0\n{_f(ka)} 0.0 {_f(kb)} 0.0\n"
-    args = [EXE, os.path.join(tmp, "TomoKernel.conf")] + (["--kamu"] if kamu else [])
+    args = [EXE, os.path.join(tmp, "TomoKernel.conf")] + ((["--lamu"] if kamu == "lamu" else ["--kamu"]) if kamu else [])
     r = subprocess.run(args, input=answers, capture_output=True, text=True, cwd=tmp)
     assert r.returncode == 0, r.stdout + r.stderr
     S = np.zeros((2, nblk), np.float32)

@@ -132,6 +132,23 @@ def runs(tmp_path_factory, native_lib):
                 sgt_root=sgt_root, evt_root=evt_root, kd=kd, stdout=r.stdout)
 
 
+def _selection(m):
+    """0-based sample indices (per axis) of the kernel selection in the snapshot's grid and
+    lambda, mu at those points in file (K, J, I) layout."""
+    subs, subc, subt = SNAP[0], SNAP[1], SNAP[2]
+    sel = []
+    for d in range(3):
+        st, cnt, sd = SUB["sub_start"][d], SUB["sub_count"][d], SUB["sub_stride"][d]
+        n = (subc[d] - st) // sd + 1
+        if cnt != -1:
+            n = min(n, cnt)
+        sel.append(np.arange(st - 1, st - 1 + n * sd, sd))
+    gi = [LENFD + subs[d] - 1 + sel[d] * subt[d] for d in range(3)]
+    lam = m.lam[np.ix_(*gi)].transpose(2, 1, 0)
+    mu = m.mu[np.ix_(*gi)].transpose(2, 1, 0)
+    return sel, lam, mu
+
+
 def _expected(R, oracle_mod, param=0):
     """Kernels of every pick over all selected points, float32, in file (K, J, I) layout
     (param 0 Vp/Vs kernels, 1 lambda/mu kernels)."""
@@ -293,6 +310,71 @@ def test_lamu_kernel_files_equal_the_restatement(runs, oracle_mod):
         after, _ = _read(os.path.join(d, "kernel_001_mpi000000_n00000.nc"))
         for name in NAMES:
             np.testing.assert_array_equal(after[name], b[name])
+
+
+def test_kernel_conversions(runs):
+    """--convert lamu2vpvs, vpvs2kamu, lamu2kamu (SI_ker_lamu2vpvs, SI_ker_vpvs2kamu,
+    SI_ker_lamu2kamu) over lambda/mu kernel files that --lamu wrote into fresh pick
+    directories: every output block equals the restatement (oracle/kconv_oracle.py) applied
+    to the input file with the block's lambda and mu, bit for bit; points outside the
+    selection stay zero; lamu2vpvs then vpvs2kamu agrees with lamu2kamu to rounding; the
+    skipped pick gets no file."""
+    from fwant_gb300 import inputs
+    from oracle import kconv_oracle as KC
+    tmp = runs["tmp"]
+    cd = lambda name: os.path.join(tmp, "conv", name)  # noqa: E731
+    events = [dict(e, picks=[[(p[0], p[1], p[2], p[3], cd(os.path.basename(p[4]))) for p in comp]
+                             for comp in e["picks"]]) for e in runs["events"]]
+    dirs = sorted({p[4] for e in events for comp in e["picks"] for p in comp})
+    for d in dirs:
+        os.makedirs(d, exist_ok=True)
+    evt = os.path.join(tmp, "evt_conv.lst")
+    inputs.write_event_list(evt, events)
+    sta = os.path.join(tmp, "sta_conv.lst")
+    with open(sta, "w") as f:
+        f.write(f"STA {evt}\n")
+
+    def run(*args, stdin):
+        r = subprocess.run([KER, *args, runs["conf"]], input=stdin, capture_output=True, text=True, cwd=tmp)
+        assert r.returncode == 0, r.stdout + r.stderr
+        return r
+
+    run("--lamu", stdin=f"{sta}\n0 0 0\n")
+    sel, lam, mu = _selection(runs["m"])
+    ix = np.ix_(sel[2], sel[1], sel[0])
+    lam_names = ("phase_la", "amplitude_la", "phase_mu", "amplitude_mu")
+    kamu_names = ("phase_ka", "amplitude_ka", "phase_mu", "amplitude_mu")
+    skipped = cd("F")
+
+    def check(mode, in_file, in_names, out_file, out_names):
+        run("--convert", mode, stdin=f"\n{sta}\n0 0 0\n")
+        outs = {}
+        for d in dirs:
+            if d == skipped:
+                assert not os.path.exists(os.path.join(d, out_file))
+                continue
+            src, _ = _read(os.path.join(d, in_file))
+            got, att = _read(os.path.join(d, out_file))
+            assert att["title"] == b"Finite frequency kernel"
+            for ph in (0, 1):  # phase pair, amplitude pair
+                a, b = KC.convert(mode, lam, mu, src[in_names[ph]][ix], src[in_names[2 + ph]][ix])
+                for q, want in ((ph, a), (2 + ph, b)):
+                    full = np.zeros(SNAP[1][::-1], np.float32)
+                    full[ix] = want
+                    np.testing.assert_array_equal(got[out_names[q]], full, err_msg=f"{mode} {d} {out_names[q]}")
+                    assert np.any(want)
+            outs[d] = got
+        return outs
+
+    check("lamu2vpvs", "kernel_lamu_001_mpi000000_n00000.nc", lam_names, "kernel_001_mpi000000_n00000.nc", NAMES)
+    via = check("vpvs2kamu", "kernel_001_mpi000000_n00000.nc", NAMES, "kernel_kamu_001_mpi000000_n00000.nc",
+                kamu_names)
+    direct = check("lamu2kamu", "kernel_lamu_001_mpi000000_n00000.nc", lam_names, "kernel_001_mpi000000_n00000.nc",
+                   NAMES)
+    for d in via:
+        for qa, qb in zip(kamu_names, NAMES):
+            a, b = via[d][qa].astype(np.float64), direct[d][qb].astype(np.float64)
+            np.testing.assert_allclose(a, b, rtol=0, atol=2e-6 * np.abs(b).max())
 
 
 def test_resumed_blocks_rewrite_the_same_files(runs):

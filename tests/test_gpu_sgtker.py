@@ -276,3 +276,30 @@ def test_rotation_of_the_force_components(oracle_mod, native_lib):
         for c in range(3):
             want = (v[0] * rot[0, c] + v[1] * rot[1, c]) + v[2] * rot[2, c]
             np.testing.assert_array_equal(k.get_scatter(group[c]), want)
+
+
+@pytest.mark.parametrize("mode", [1, 2, 3])
+def test_parameter_conversion_bitwise(mode, native_lib):
+    """fwant_sgtker_convert (SI_ker_lamu2kamu / SI_ker_lamu2vpvs / SI_ker_vpvs2kamu) equals the
+    single-precision restatement bit for bit on random kernels and media; a mode outside 1..3
+    is refused."""
+    import fwant_gb300 as fw
+    from oracle import kconv_oracle as KC
+    rng = np.random.default_rng(40 + mode)
+    n = 5000
+    vp = rng.uniform(5.5e3, 8.0e3, n)
+    vs = vp / rng.uniform(1.65, 1.85, n)
+    rho = rng.uniform(2.5e3, 3.3e3, n)
+    mu = (rho * vs * vs).astype(np.float32)
+    lam = (rho * vp * vp - 2 * rho * vs * vs).astype(np.float32)
+    kern = [(rng.normal(size=n) * 1e-9).astype(np.float32) for _ in range(4)]
+    k = fw.SgtKernel(n, 4, 0.1)
+    k.set_media(lam, mu)
+    got = k.convert(mode, *kern)
+    for ph in (0, 1):
+        a, b = KC.convert(mode, lam, mu, kern[ph], kern[2 + ph])
+        np.testing.assert_array_equal(got[ph], a)
+        np.testing.assert_array_equal(got[2 + ph], b)
+    with pytest.raises(Exception):
+        k.convert(4, *kern)
+    k.close()
