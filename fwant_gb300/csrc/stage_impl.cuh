@@ -79,18 +79,25 @@ struct Lay {
   // terrain form stages none).  The stage input's six variables of a face (TX x TY x 6 FP32)
   // ride in the pipeline buffer with the tile, one plane ahead: RK_beg and RK_fin put them
   // in the buffer's m / t space that they do not use (when it is large enough), RK_inn after
-  // t.  The RK registers m and t of the variables (RK_inn: both, RK_fin: t), needed only for
-  // the final update, go to one area after the two buffers, loaded at the start of their
-  // plane on a barrier of their own.
+  // t.  RK_fin's t variables follow in the buffer (at off_pb); RK_inn's m and t variables,
+  // for which two CTAs per SM leave no room in the buffers, go to one area after the two
+  // buffers, loaded at the start of their plane on a barrier of their own and waited for at
+  // the final update.
   static constexpr int SZ_PML_PLANE = 6 * TY * TX * 4;
   __host__ __device__ static constexpr int pml_slots(int rk) { return TOPO ? 0 : (rk == 0 ? 3 : 1); }
-  __host__ __device__ static constexpr int pml_single_roles(int rk) { return rk == 1 ? 2 : (rk == 2 ? 1 : 0); }
+  __host__ __device__ static constexpr int pml_single_roles(int rk) { return rk == 1 ? 2 : 0; }
+  __host__ __device__ static constexpr int pml_buf_roles(int rk) { return rk == 2 ? 1 : 0; }  // t in the buffer
   __host__ __device__ static constexpr bool pml_in_mt(int rk) {  // the input slots reuse the m / t space
     return rk != 1 && pml_slots(rk) * SZ_PML_PLANE <= (rk == 0 ? 2 : 1) * SZ_PT;
   }
   __host__ __device__ static constexpr int off_pa(int rk) { return pml_in_mt(rk) ? OFF_M : OFF_T + SZ_PT; }
+  __host__ __device__ static constexpr int off_pb(int rk) {
+    return pml_in_mt(rk) ? OFF_T + SZ_PT : OFF_T + SZ_PT + pml_slots(rk) * SZ_PML_PLANE;
+  }
   __host__ __device__ static constexpr int buf_full(int rk) {
-    return pml_in_mt(rk) ? BUF_BYTES : ((OFF_T + SZ_PT + pml_slots(rk) * SZ_PML_PLANE + 1023) / 1024) * 1024;
+    return (pml_in_mt(rk) && pml_buf_roles(rk) == 0)
+               ? BUF_BYTES
+               : ((off_pb(rk) + pml_slots(rk) * pml_buf_roles(rk) * SZ_PML_PLANE + 1023) / 1024) * 1024;
   }
   __host__ __device__ static constexpr int pml_single_bytes(int rk) {
     return pml_slots(rk) * pml_single_roles(rk) * SZ_PML_PLANE;
@@ -300,7 +307,8 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
   // pipeline buffer, the m / t variables (NROLE_S roles) in the area at OFF_PS
   constexpr int NSLOT = LEAN ? 0 : L::pml_slots(RK);
   constexpr int NROLE_S = L::pml_single_roles(RK);
-  constexpr int OFF_PA = L::off_pa(RK);
+  constexpr int NROLE_B = L::pml_buf_roles(RK);
+  constexpr int OFF_PA = L::off_pa(RK), OFF_PB = L::off_pb(RK);
   constexpr int OFF_PS = 2 * BUF_BYTES;
   constexpr int OFF_BAR = LEAN ? L::OFF_MT_L + L::template SZ_MT_L<RK> : OFF_PS + L::pml_single_bytes(RK);
   constexpr int HY = FY ? 1 : 3;  // row of the CTA's first row inside the tile box (tile_halo_y)
@@ -412,8 +420,11 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
     fence_proxy_async();
     // the staged faces' input variables of plane kp ride with the tile
     const uint32_t npa = NSLOT > 0 ? n_staged(kp) : 0u;
-    mbar_expect_tx(bar, TX_BYTES + npa * uint32_t(L::SZ_PML_PLANE));
-    if (npa) load_faces(base + OFF_PA, 1, kp, A.pml_set[0], bar);
+    mbar_expect_tx(bar, TX_BYTES + npa * uint32_t((1 + NROLE_B) * L::SZ_PML_PLANE));
+    if (npa) {
+      load_faces(base + OFF_PA, 1, kp, A.pml_set[0], bar);
+      if (NROLE_B > 0) load_faces(base + OFF_PB, 1, kp, A.pml_set[2], bar);
+    }
     if (LEAN) {
       tma_load_4d(base, &A.tm_tile_lo, i0 - HX + PADL, j0 - HY, kp, 0, bar);
       tma_load_4d(base + L::OFF_HI_L, &A.tm_tile_hi, i0 - HX + PADL, j0 - HY, kp, 4, bar);
@@ -581,8 +592,8 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
     fence_proxy_async();
     mbar_expect_tx(bar_pml, bytes);
     const uint32_t base = smem_u32(smem + OFF_PS);
-    load_faces(base, NROLE_S, kp, A.pml_set[RK == 1 ? 1 : 2], bar_pml);
-    if (RK == 1) load_faces(base + uint32_t(L::SZ_PML_PLANE), NROLE_S, kp, A.pml_set[2], bar_pml);
+    load_faces(base, NROLE_S, kp, A.pml_set[1], bar_pml);                              // m
+    load_faces(base + uint32_t(L::SZ_PML_PLANE), NROLE_S, kp, A.pml_set[2], bar_pml);  // t
     return bytes;
   };
   int pml_ph = 0;  // completed PML staging phases
@@ -846,6 +857,7 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
       // staged faces: the input variables in this plane's buffer, m / t in the single area
       // (waited for at their first use)
       const float* pml_a = reinterpret_cast<const float*>(buf + OFF_PA) + ty * TX + tx;
+      const float* pml_b = reinterpret_cast<const float*>(buf + OFF_PB) + ty * TX + tx;
       const float* pml_s = reinterpret_cast<const float*>(smem + OFF_PS) + ty * TX + tx;
       bool waited_s = false;
       const float tc13 = lam, tc66 = miu;
@@ -860,6 +872,7 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
         const int q = int((slots >> (4 * sidx)) & 15u);
         const bool stg = NSLOT > 0 && q != 15;
         auto PA = [&](int v) -> float { return pml_a[(q * 6 + v) * TY * TX]; };
+        auto PB = [&](int v) -> float { return pml_b[(q * 6 + v) * TY * TX]; };
         auto PS = [&](int r, int v) -> float { return pml_s[((q * NROLE_S + r) * 6 + v) * TY * TX]; };
         const int ia = axis == 0 ? i : (axis == 1 ? j : k);
         const float b1 = __ldg(A.pb1[axis] + ia), b1_1 = __ldg(A.pb11[axis] + ia);
@@ -930,7 +943,7 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
             st_stream(ao + v * vs, mv + A.a * h[v], pol_stream);
             st_stream(at + v * vs, tv + A.b * h[v], pol_stream);
           } else {
-            const float tv = stg ? PS(0, v) : ld_rw_stream(at + v * vs, pol_stream);
+            const float tv = stg ? PB(v) : ld_rw_stream(at + v * vs, pol_stream);
             st_stream(at + v * vs, tv + A.b * h[v], pol_stream);
           }
         }
