@@ -36,6 +36,10 @@
 // The time axis is T(n) = n kdt (SI_ker_lamu2kamu.F90:260-263): the synthetics are listed
 // but not read, and a pick whose window lies outside it is skipped as in the kernel run.
 //
+// With --eq the program is SI_ker_EQ (code/srcF.kernel/SI_ker_EQ.F90): SI_ker_sta with the
+// station's Z-force SGT moved 9 frames earlier in time, the last 9 frames zero
+// (eoshift(., shift=9) along time, SI_ker_EQ.F90:580-586); everything else is the same.
+//
 // Tool modes (format checks): --nc-slab FILE VAR START COUNT STRIDE prints a strided
 // sub-array as JSON; --nc-fill-slab FILE VAR START COUNT STRIDE writes 1, 2, ... into one
 // (comma-separated lists, slowest dimension first, 0-based starts).
@@ -302,6 +306,18 @@ void read_sgt(const std::string& root, const seisfd::SnapDef& sp, const Geometry
   }
 }
 
+// SI_ker_EQ's shift of the station's Z-force SGT: frame n takes frame n + shift, the last
+// `shift` frames 0 (eoshift along time; SI_ker_EQ.F90:580-586).  s is (6, knt, np).
+constexpr int EQ_SHIFT = 9;
+void shift_frames(std::vector<float>& s, int knt, size_t np, int shift) {
+  for (int q = 0; q < 6; ++q)
+    for (int n = 0; n < knt; ++n) {
+      float* dst = s.data() + (size_t(q) * knt + size_t(n)) * np;
+      if (n + shift < knt) std::copy_n(s.data() + (size_t(q) * knt + size_t(n + shift)) * np, np, dst);
+      else std::fill_n(dst, np, 0.0f);
+    }
+}
+
 int nc_tool(int argc, char** argv) {
   const std::string mode = argv[1];
   if (argc < 7) die("usage: " + mode + " FILE VAR START COUNT STRIDE");
@@ -423,17 +439,19 @@ int main(int argc, char** argv) {
   int device = 0;
   bool lamu = false;  // --lamu: the lambda/mu kernels of SI_ker_sta_lamu
   int conv = 0;       // --convert: 1 lamu2kamu, 2 lamu2vpvs, 3 vpvs2kamu
+  bool eq = false;    // --eq: SI_ker_EQ's time shift of the Z-force SGT
   for (int a = 1; a < argc; ++a) {
     const std::string s = argv[a];
     if (s == "--device" && a + 1 < argc) device = std::atoi(argv[++a]);
     else if (s == "--lamu") lamu = true;
+    else if (s == "--eq") eq = true;
     else if (s == "--convert" && a + 1 < argc) {
       const std::string m = argv[++a];
       conv = m == "lamu2kamu" ? 1 : (m == "lamu2vpvs" ? 2 : (m == "vpvs2kamu" ? 3 : 0));
       if (!conv) die("--convert: mode must be lamu2kamu, lamu2vpvs or vpvs2kamu");
     } else ker_conf = s;
   }
-  if (conv && lamu) die("--lamu and --convert exclude each other");
+  if (conv && (lamu || eq)) die("--convert excludes --lamu and --eq");
   if (ker_conf.empty()) ker_conf = conv ? "TomoKernel_conv.conf" : "TomoKernel.conf";
   // init_kernel (SI_ker_sta.F90:1047-1082)
   conf::File kc;
@@ -607,6 +625,7 @@ int main(int argc, char** argv) {
             for (int c = 0; c < 3; ++c)
               if (ud[c] && !have[c]) {
                 read_sgt(sgt_root + "/" + sta + "/" + sgt_sta[c], *sp, g, knt, stress);
+                if (eq && c == 2) shift_frames(stress, knt, g.npts(), EQ_SHIFT);
                 check(fwant_sgtker_set_sgt(K, c, stress.data()), K, "station SGT");
                 have[c] = true;
               }

@@ -149,9 +149,10 @@ def _selection(m):
     return sel, lam, mu
 
 
-def _expected(R, oracle_mod, param=0):
+def _expected(R, oracle_mod, param=0, eq=False):
     """Kernels of every pick over all selected points, float32, in file (K, J, I) layout
-    (param 0 Vp/Vs kernels, 1 lambda/mu kernels)."""
+    (param 0 Vp/Vs kernels, 1 lambda/mu kernels; eq: the Z-force SGT moved 9 frames
+    earlier, SI_ker_EQ)."""
     m, kdt, t = R["m"], R["kdt"], R["t"]
     subs, subc, subt = SNAP[0], SNAP[1], SNAP[2]
     # selected sample indices (0-based) per axis: start, stride, count of the kernel selection
@@ -171,6 +172,8 @@ def _expected(R, oracle_mod, param=0):
     def block(series):  # (6, KNT, K, J, I) -> (6, KNT, points) with i fastest
         return np.ascontiguousarray(series[:, :, sk][:, :, :, sj][:, :, :, :, si].reshape(6, KNT, -1))
     rs = [block(_sgt_series(os.path.join(R["sgt_root"], "STA", c))) for c in ("FX", "FY", "FZ")]
+    if eq:  # eoshift(., shift=9) along time (SI_ker_EQ.F90:580-586)
+        rs[2] = np.concatenate([rs[2][:, 9:], np.zeros_like(rs[2][:, :9])], axis=1)
     ss = block(_sgt_series(os.path.join(R["evt_root"], "EV1", "OUT")))
     dt = float(kdt)
     m0 = float(np.float32(M0))
@@ -375,6 +378,41 @@ def test_kernel_conversions(runs):
         for qa, qb in zip(kamu_names, NAMES):
             a, b = via[d][qa].astype(np.float64), direct[d][qb].astype(np.float64)
             np.testing.assert_allclose(a, b, rtol=0, atol=2e-6 * np.abs(b).max())
+
+
+def test_eq_kernel_files_equal_the_restatement(runs, oracle_mod):
+    """--eq (SI_ker_EQ): the station's Z-force SGT moved 9 frames earlier before the
+    accumulation; every kernel file equals the restatement's on the shifted series, and the
+    picks that use the Z component differ from the plain run's."""
+    from fwant_gb300 import inputs
+    tmp = runs["tmp"]
+    ed = lambda name: os.path.join(tmp, "eq", name)  # noqa: E731
+    events = [dict(e, picks=[[(p[0], p[1], p[2], p[3], ed(os.path.basename(p[4]))) for p in comp]
+                             for comp in e["picks"]]) for e in runs["events"]]
+    for e in events:
+        for comp in e["picks"]:
+            for p in comp:
+                os.makedirs(p[4], exist_ok=True)
+    evt = os.path.join(tmp, "evt_eq.lst")
+    inputs.write_event_list(evt, events)
+    sta = os.path.join(tmp, "sta_eq.lst")
+    with open(sta, "w") as f:
+        f.write(f"STA {evt}\n")
+    r = subprocess.run([KER, "--eq", runs["conf"]], input=f"{sta}\n0 0 0\n", capture_output=True, text=True, cwd=tmp)
+    assert r.returncode == 0, r.stderr
+    want = _expected(dict(runs, events=events), oracle_mod, eq=True)
+    plain = _expected(dict(runs, events=events), oracle_mod)
+    differs = 0
+    for d, w in want.items():
+        path = os.path.join(d, "kernel_001_mpi000000_n00000.nc")
+        if w is None:
+            assert not os.path.exists(path)
+            continue
+        got, _ = _read(path)
+        for q, name in enumerate(NAMES):
+            np.testing.assert_array_equal(got[name], w[q], err_msg=f"{d}:{name}")
+        differs += any(not np.array_equal(w[q], plain[d][q]) for q in range(4))
+    assert differs >= 2
 
 
 def test_resumed_blocks_rewrite_the_same_files(runs):
