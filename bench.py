@@ -77,8 +77,10 @@ def parse_args():
     p.add_argument("--grid", default=None, help="override the C2 interior size, e.g. 200x200x100 (profiling)")
     p.add_argument("--sims", type=int, default=3, help="number of force components simulated (C2)")
     p.add_argument("--autotune", action="store_true",
-                   help="run the project's autotuner (planes per CTA of every member, the batch's CTA "
+                   help="run the project's autotuner (tile shape and planes per CTA of every member, the batch's CTA "
                         "schedule) before timing; the end-to-end leg applies the tuned settings")
+    p.add_argument("--tile-rows", type=int, choices=[8, 16], default=None,
+                   help="rows of the stage kernel's 32-column tile (default 8; 16 for FP32 storage)")
     p.add_argument("--storage", choices=["fp32", "bf16", "fp16"], default="fp32",
                    help="storage of the wavefield registers (arithmetic stays FP32)")
     return p.parse_args()
@@ -852,6 +854,8 @@ def run_ours(args, rank, world):
         if args.storage == "fp16":
             # a 1e15 N surface force on 1 km cells peaks near 50 m/s and 1.2e9 Pa at the source
             s.set_storage_scale(2.0 ** 9, 2.0 ** -15)
+        if args.tile_rows:
+            s.tile_rows = args.tile_rows
         return s
 
     sims = [inputs.attach(make_solver(m), m) for m in models]
@@ -863,8 +867,8 @@ def run_ours(args, rank, world):
     if args.autotune:
         t_tune = time.perf_counter()
         ctas = batch.autotune(4)
-        tuned = {"planes_per_cta": [s.planes_per_cta for s in sims], "ctas": ctas,
-                 "lean_stages": sims[0].lean_stages,
+        tuned = {"planes_per_cta": [s.planes_per_cta for s in sims], "tile_rows": sims[0].tile_rows,
+                 "tile": f"32x{sims[0].tile_rows}", "ctas": ctas, "lean_stages": sims[0].lean_stages,
                  "tune_s": time.perf_counter() - t_tune}
     # per-launch timing of the stage kernel (CUDA events around each launch, eager)
     stage_ms, end_ms = batch.profile_stages(8)
@@ -909,7 +913,7 @@ def run_ours(args, rank, world):
         "steps": args.steps, "warmup": warm, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": desc, "points_per_step": npts, "l2": "inputs larger than L2 (no flush)",
-                   "storage": args.storage, "fields_finite_after_run": finite,
+                   "storage": args.storage, "tile": f"32x{sims[0].tile_rows}", "fields_finite_after_run": finite,
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
         "host_wall_s": t_host, "roofline": roof, "clocks": clk, "autotune": tuned,
         # per step, as the batch counts them: per group of up to 16 simulations and per stage
@@ -942,6 +946,7 @@ def run_ours(args, rank, world):
             if tuned:
                 s.planes_per_cta = tuned["planes_per_cta"][len(esims)]
                 s.lean_stages = tuned["lean_stages"]
+                s.tile_rows = tuned["tile_rows"]
             esims.append(s)
             h2d += 3 * m.lam.nbytes + m.x.nbytes + m.y.nbytes + m.z.nbytes
         eb = fw.Batch(esims)

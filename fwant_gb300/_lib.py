@@ -88,6 +88,8 @@ EXPORTS = [
     ("fwant_batch_autotune", C.c_int, [_vp, C.c_int, _ip]),
     ("fwant_set_planes_per_cta", C.c_int, [_vp, C.c_int]),
     ("fwant_get_planes_per_cta", C.c_int, [_vp, _ip]),
+    ("fwant_set_tile_rows", C.c_int, [_vp, C.c_int]),
+    ("fwant_get_tile_rows", C.c_int, [_vp, _ip]),
     ("fwant_set_lean_stages", C.c_int, [_vp, C.c_int]),
     ("fwant_check_wait_timeout", C.c_int, [_vp, C.c_int]),
     ("fwant_get_lean_stages", C.c_int, [_vp, _ip]),
@@ -429,7 +431,8 @@ class Solver:
         return out[: 6 * n * npts].reshape(6, n, npts)
 
     def autotune(self, trial_steps=4):
-        """Pick the fastest planes-per-CTA (before the first step); returns it."""
+        """Pick the fastest tile shape and planes-per-CTA (before the first step); returns
+        the planes (tile_rows reads the shape)."""
         v = C.c_int()
         self._chk(self._lib.fwant_autotune(self._h, int(trial_steps), C.byref(v)))
         return v.value
@@ -443,6 +446,16 @@ class Solver:
     @planes_per_cta.setter
     def planes_per_cta(self, planes):
         self._chk(self._lib.fwant_set_planes_per_cta(self._h, int(planes)))
+
+    @property
+    def tile_rows(self):
+        v = C.c_int()
+        self._chk(self._lib.fwant_get_tile_rows(self._h, C.byref(v)))
+        return v.value
+
+    @tile_rows.setter
+    def tile_rows(self, rows):
+        self._chk(self._lib.fwant_set_tile_rows(self._h, int(rows)))
 
     def check_wait_timeout(self, spins=1000):
         """Run the bounded-wait deadline check; raises FwantError (TIMEOUT) as designed."""

@@ -29,7 +29,8 @@ EXACT_FLAGS = ["-fmad=false"]
 CPP_FLAGS = ["-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
 
 SOURCES = ["stage_fast_rk0.cu", "stage_fast_rk1.cu", "stage_fast_rk2.cu", "stage_exact_rk0.cu",
-           "stage_exact_rk1.cu", "stage_exact_rk2.cu", "stage_bf16_rk0.cu", "stage_bf16_rk1.cu",
+           "stage_exact_rk1.cu", "stage_exact_rk2.cu", "stage_fast16_rk0.cu", "stage_fast16_rk1.cu",
+           "stage_fast16_rk2.cu", "stage_exact16_rk0.cu", "stage_exact16_rk1.cu", "stage_exact16_rk2.cu", "stage_bf16_rk0.cu", "stage_bf16_rk1.cu",
            "stage_bf16_rk2.cu", "stage_fp16_rk0.cu", "stage_fp16_rk1.cu", "stage_fp16_rk2.cu",
            "stage_topo_rk0.cu", "stage_topo_rk1.cu", "stage_topo_rk2.cu", "stage_topo_exact_rk0.cu",
            "stage_topo_exact_rk1.cu", "stage_topo_exact_rk2.cu", "topo.cu",

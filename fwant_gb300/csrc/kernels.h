@@ -71,8 +71,10 @@ struct Sources {
   const float* mom_M;     // [nmom][ntwin][6] Mxx Myy Mzz Mxy Mxz Myz
 };
 
-// Stage-kernel tiling: a CTA owns TX x TY columns and marches along k.
-constexpr int STAGE_TX = 32, STAGE_TY = 8;
+// Stage-kernel tiling: a CTA owns TX x TY columns and marches along k.  TY = STAGE_TY is
+// the default tile height; the FP32 forms also exist with TY = STAGE_TY_TALL (the tile
+// shape is a tuning choice of the solver, fwant_set_tile_rows).
+constexpr int STAGE_TX = 32, STAGE_TY = 8, STAGE_TY_TALL = 16;
 // TMA boxes (x, y, 1 plane, components).  The halo'd tile starts tile_halo_x columns left
 // of the CTA's first column so that its x origin stays 16-byte aligned: 4 columns for
 // 4-byte storage, 8 for 2-byte storage.
@@ -81,7 +83,8 @@ constexpr int tile_box_x(int elem_bytes) { return STAGE_TX + 2 * tile_halo_x(ele
 // Rows of the halo'd tile: a one-sided y operator reads one row on one side and three on
 // the other (forward: -1..+3, backward: -3..+1), so the box holds the CTA's rows plus
 // four; its first row is tile_halo_y(FY) rows above the CTA's first row.
-constexpr int TILE_BY = STAGE_TY + 4;
+constexpr int tile_by(int ty) { return ty + 4; }
+constexpr int TILE_BY = tile_by(STAGE_TY);
 constexpr int tile_halo_y(int fwd) { return fwd ? 1 : 3; }
 // wavefield storage kinds inside the kernels
 enum { ST_F32 = 0, ST_BF16 = 1, ST_F16 = 2 };
@@ -163,8 +166,10 @@ static_assert(sizeof(BatchArgs) <= 32764, "kernel parameter space");
 // of the same expressions); 0 the fast form (FMA, reciprocals).
 // storage: ST_F32 / ST_BF16 / ST_F16 (the exact form exists for ST_F32 only).
 // lean = 1: the interior-only form (items without PML points, sources or free surface).
+// ty: tile rows (STAGE_TY, or STAGE_TY_TALL for FP32 storage); another value returns
+// cudaErrorInvalidValue.
 int launch_stage_batch(const BatchArgs& b, int variant, int rk, int exact, int storage, int lean, int ctas,
-                       void* stream);
+                       void* stream, int ty = STAGE_TY);
 // The terrain form (FP32 storage, full form only; exact = 1 the reference-order arithmetic).
 int launch_stage_batch_topo(const BatchArgs& b, int variant, int rk, int exact, int ctas, void* stream);
 // FP64 metric of the terrain-following grid (r = z + h s): per point r, zeta_r,
@@ -190,10 +195,10 @@ void launch_topo_surface(const Geom& g, const float* metric, const float* lam, c
 void launch_topo_slopes(const Geom& g, const float* h, double* hxi, double* heta, void* stream);
 // Work items of one simulation split into the lean (interior) list and the full list.
 // force_c / mom_c: 0-based source centres (3 per source).
-void stage_items(const Geom& g, int kc, const Slab slab[6], const int* force_c, int nforce, const int* mom_c,
+void stage_items(const Geom& g, int kc, int ty, const Slab slab[6], const int* force_c, int nforce, const int* mom_c,
                  int nmom, int* lean, int* nlean, int* full, int* nfull);
-long long stage_item_count(const Geom& g, int kc);
-int stage_planes_per_cta(const Geom& g, int sm_count);
+long long stage_item_count(const Geom& g, int kc, int ty = STAGE_TY);
+int stage_planes_per_cta(const Geom& g, int sm_count, int ty = STAGE_TY);
 int stage_configure();  // set the dynamic shared-memory attribute of every instantiation
 
 struct RecvArgs {

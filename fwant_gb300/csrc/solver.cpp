@@ -73,6 +73,7 @@ struct fwant_solver {
   float* d_prof = nullptr;  // b1, b1-1, A+D, D for x (nx each), y (ny), z (nz)
   float *d_rzinv = nullptr, *d_rsinv = nullptr;
   int kc = 8;                // planes per CTA of the stage kernel
+  int tile_ty = fw::STAGE_TY;  // rows of the stage kernel's 32-column tile (fw::STAGE_TY or STAGE_TY_TALL)
   std::vector<float> hx, hy, hz, hxsin, hxcot;
   bool have_coord = false, have_metric = false, have_media = false;
 
@@ -313,19 +314,37 @@ struct fwant_solver {
     };
     const CUtensorMapL2promotion line = CU_TENSOR_MAP_L2_PROMOTION_L2_128B;  // line-aligned boxes
     for (int r = 0; r < 4; ++r) {
-      if (make(&tm_tile[r], set(r), wtype, esz, fw::NF, fw::tile_box_x(esz), fw::TILE_BY, fw::NF, tile_promo) !=
+      const cuuint32_t ty = cuuint32_t(tile_ty), tby = cuuint32_t(fw::tile_by(tile_ty));
+      if (make(&tm_tile[r], set(r), wtype, esz, fw::NF, fw::tile_box_x(esz), tby, fw::NF, tile_promo) !=
               CUDA_SUCCESS ||
-          make(&tm_q[r], set(r), wtype, esz, fw::NF, fw::STAGE_TX, fw::STAGE_TY, 6, line) != CUDA_SUCCESS ||
-          make(&tm_pt[r], set(r), wtype, esz, fw::NF, fw::STAGE_TX, fw::STAGE_TY, fw::NF, line) != CUDA_SUCCESS ||
-          make(&tm_tile_lo[r], set(r), wtype, esz, fw::NF, fw::tile_box_x(esz), fw::TILE_BY, 3, tile_promo) !=
+          make(&tm_q[r], set(r), wtype, esz, fw::NF, fw::STAGE_TX, ty, 6, line) != CUDA_SUCCESS ||
+          make(&tm_pt[r], set(r), wtype, esz, fw::NF, fw::STAGE_TX, ty, fw::NF, line) != CUDA_SUCCESS ||
+          make(&tm_tile_lo[r], set(r), wtype, esz, fw::NF, fw::tile_box_x(esz), tby, 3, tile_promo) !=
               CUDA_SUCCESS ||
-          make(&tm_tile_hi[r], set(r), wtype, esz, fw::NF, fw::tile_box_x(esz), fw::TILE_BY, 5, tile_promo) !=
+          make(&tm_tile_hi[r], set(r), wtype, esz, fw::NF, fw::tile_box_x(esz), tby, 5, tile_promo) !=
               CUDA_SUCCESS)
         return fail(FWANT_ERR_CUDA, "tensor map encoding failed");
     }
-    if (make(&tm_med, med, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, 3, fw::STAGE_TX, fw::STAGE_TY, 3, line) != CUDA_SUCCESS)
+    if (make(&tm_med, med, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, 3, fw::STAGE_TX, cuuint32_t(tile_ty), 3, line) !=
+        CUDA_SUCCESS)
       return fail(FWANT_ERR_CUDA, "tensor map encoding failed");
     return FWANT_OK;
+  }
+
+  // Tile shape of the stage kernel: rows 8 (every storage and form) or 16 (FP32 storage,
+  // flat grid); the tensor maps' boxes follow it.
+  bool tile_rows_allowed(int rows) const {
+    return rows == fw::STAGE_TY || (rows == fw::STAGE_TY_TALL && stor == fw::ST_F32 && !topo_on);
+  }
+  fwant_status set_tile_rows(int rows) {
+    if (!tile_rows_allowed(rows))
+      return fail(FWANT_ERR_INVALID_ARG, "tile rows: 8, or 16 with FP32 storage and no topography");
+    if (rows == tile_ty) return FWANT_OK;
+    tile_ty = rows;
+    fwant_status rc = make_tensor_maps();
+    if (rc == FWANT_OK) rc = make_pml_maps();
+    drop_graphs();
+    return rc;
   }
 
   // TMA descriptors of the PML faces, in device memory: per face a 5-D tensor over its four
@@ -350,7 +369,7 @@ struct fwant_solver {
       const cuuint64_t sz = cuuint64_t(s.k2 - s.k1 + 1), vs = cuuint64_t(s.vstride);
       const cuuint64_t dims[5] = {cuuint64_t(s.sx), cuuint64_t(s.sy), sz, 6, 4};
       const cuuint64_t strides[4] = {cuuint64_t(s.sx) * 4, cuuint64_t(s.sx) * s.sy * 4, vs * 4, 6 * vs * 4};
-      const cuuint32_t box[5] = {fw::STAGE_TX, fw::STAGE_TY, 1, 6, 1};
+      const cuuint32_t box[5] = {fw::STAGE_TX, cuuint32_t(tile_ty), 1, 6, 1};
       const cuuint32_t el[5] = {1, 1, 1, 1, 1};
       if (reinterpret_cast<EncodeFn>(fn)(&maps[f], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, aux[f], dims, strides, box, el,
                                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -703,16 +722,16 @@ struct fwant_solver {
   // Work-item lists of the stage launches for the current k-chunk, PML and sources
   // (rebuilt, and the graphs dropped, when they change).
   fwant_status ensure_items() {
-    const long long n = fw::stage_item_count(g, kc);
+    const long long n = fw::stage_item_count(g, kc, tile_ty);
     std::vector<int> lean(static_cast<size_t>(n)), full(static_cast<size_t>(n));
     int nl = 0, nf = 0;
-    fw::stage_items(g, kc, slab, h_force_c.data(), int(h_force_c.size() / 3), h_mom_c.data(),
+    fw::stage_items(g, kc, tile_ty, slab, h_force_c.data(), int(h_force_c.size() / 3), h_mom_c.data(),
                     int(h_mom_c.size() / 3), lean.data(), &nl, full.data(), &nf);
     // lean items, full items, then every item in launch order (x fastest, then y, k)
     std::vector<int> all(lean.begin(), lean.begin() + nl);
     all.insert(all.end(), full.begin(), full.begin() + nf);
     {
-      const int nbx = (g.ni + fw::STAGE_TX - 1) / fw::STAGE_TX, nby = (g.nj + fw::STAGE_TY - 1) / fw::STAGE_TY;
+      const int nbx = (g.ni + fw::STAGE_TX - 1) / fw::STAGE_TX, nby = (g.nj + tile_ty - 1) / tile_ty;
       for (int bz = 0; bz * kc < g.nk; ++bz)
         for (int by = 0; by < nby; ++by)
           for (int bx = 0; bx < nbx; ++bx) all.push_back(bx | (by << 10) | (bz << 20));
@@ -843,7 +862,7 @@ struct fwant_solver {
         const int le = topo_on ? fw::launch_stage_batch_topo(b, stage_variant(cycle_pos, s), stage_rk(s),
                                                              cfg.exact_arith, cnt, st)
                                : fw::launch_stage_batch(b, stage_variant(cycle_pos, s), stage_rk(s), cfg.exact_arith,
-                                                        stor, lean, cnt, st);
+                                                        stor, lean, cnt, st, tile_ty);
         if (le && !lerr) lerr = le;
       }
     }
@@ -934,6 +953,7 @@ struct fwant_solver {
     if (!have_coord || !have_metric)
       return fail(FWANT_ERR_STATE, "fwant_set_topography needs the coordinates and the metric first");
     if (stor != fw::ST_F32) return fail(FWANT_ERR_INVALID_ARG, "the terrain-following grid runs with FP32 storage");
+    if (tile_ty != fw::STAGE_TY) return fail(FWANT_ERR_INVALID_ARG, "the terrain-following grid runs with 32 x 8 tiles");
     for (size_t q = 0; q < size_t(g.nx) * g.ny; ++q)
       if (!std::isfinite(h[q])) return fail(FWANT_ERR_INVALID_ARG, "topography: non-finite height");
     const size_t n2 = size_t(g.nx) * g.ny;
@@ -1770,7 +1790,7 @@ struct TuneKey {
   bool operator<(const TuneKey& o) const { return std::memcmp(this, &o, sizeof(TuneKey)) < 0; }
 };
 std::mutex g_tune_mutex;
-std::map<TuneKey, int> g_tune_cache;
+std::map<TuneKey, std::pair<int, int>> g_tune_cache;  // planes per CTA, tile rows
 
 TuneKey tune_key(const fwant_solver* s) {
   TuneKey k;
@@ -1792,35 +1812,55 @@ fwant_status fwant_autotune(fwant_solver* s, int trial_steps, int* planes_out) {
     std::lock_guard<std::mutex> lock(g_tune_mutex);
     auto it = g_tune_cache.find(key);
     if (it != g_tune_cache.end()) {
-      s->kc = it->second;
+      s->kc = it->second.first;
+      if (fwant_status rc = s->set_tile_rows(it->second.second); rc != FWANT_OK) return rc;
       s->drop_graphs();
       if (planes_out) *planes_out = s->kc;
       return FWANT_OK;
     }
   }
+  // tile shape (32 x 8, and 32 x 16 where the storage and grid allow it) x planes per CTA
+  std::vector<int> shapes = {fw::STAGE_TY};
+  if (s->tile_rows_allowed(fw::STAGE_TY_TALL)) shapes.push_back(fw::STAGE_TY_TALL);
   const int cand[] = {4, 6, 8, 12, 16, 24, 32, 48, 64, 96, 128};
   double best = 1e30;
-  int best_kc = s->kc;
-  for (int kc : cand) {
-    if (kc > s->cfg.nk && kc != cand[0]) break;
-    s->kc = kc;
-    s->drop_graphs();
-    double st[4], other;
-    fwant_status rc = s->profile(1, st, &other);  // first touch of this configuration
-    if (rc == FWANT_OK) rc = s->profile(trial_steps, st, &other);
-    cudaError_t e = s->reset_state();
-    if (rc != FWANT_OK) return rc;
-    if (e != cudaSuccess) return s->cuda_fail(e, "autotune reset");
-    const double t = st[0] + st[1] + st[2] + st[3];
-    if (t < best) { best = t; best_kc = kc; }
+  int best_kc = s->kc, best_ty = s->tile_ty;
+  for (int ty : shapes) {
+    if (fwant_status rc = s->set_tile_rows(ty); rc != FWANT_OK) return rc;
+    for (int kc : cand) {
+      if (kc > s->cfg.nk && kc != cand[0]) break;
+      s->kc = kc;
+      s->drop_graphs();
+      double st[4], other;
+      fwant_status rc = s->profile(1, st, &other);  // first touch of this configuration
+      if (rc == FWANT_OK) rc = s->profile(trial_steps, st, &other);
+      cudaError_t e = s->reset_state();
+      if (rc != FWANT_OK) return rc;
+      if (e != cudaSuccess) return s->cuda_fail(e, "autotune reset");
+      const double t = st[0] + st[1] + st[2] + st[3];
+      if (t < best) { best = t; best_kc = kc; best_ty = ty; }
+    }
   }
   s->kc = best_kc;
+  if (fwant_status rc = s->set_tile_rows(best_ty); rc != FWANT_OK) return rc;
   s->drop_graphs();
   {
     std::lock_guard<std::mutex> lock(g_tune_mutex);
-    g_tune_cache[key] = best_kc;
+    g_tune_cache[key] = {best_kc, best_ty};
   }
   if (planes_out) *planes_out = best_kc;
+  return FWANT_OK;
+}
+
+fwant_status fwant_set_tile_rows(fwant_solver* s, int rows) {
+  if (!s) return FWANT_ERR_INVALID_ARG;
+  cudaSetDevice(s->cfg.device);
+  return s->set_tile_rows(rows);
+}
+
+fwant_status fwant_get_tile_rows(fwant_solver* s, int* rows) {
+  if (!s || !rows) return FWANT_ERR_INVALID_ARG;
+  *rows = s->tile_ty;
   return FWANT_OK;
 }
 
@@ -1935,7 +1975,7 @@ struct fwant_batch {
           const int nct = ctas > 0 ? std::min(b.total, ctas) : b.total;
           const int le = fw::launch_stage_batch(b, fwant_solver::stage_variant(s0->cycle_pos, s),
                                                 fwant_solver::stage_rk(s), s0->cfg.exact_arith, s0->stor, lean,
-                                                std::max(1, nct), st);
+                                                std::max(1, nct), st, s0->tile_ty);
           if (le && !lerr) lerr = le;
           ++nlaunch;
         }
@@ -2094,6 +2134,7 @@ fwant_status fwant_batch_create(fwant_solver* const* sims, int n, fwant_batch** 
         sims[q]->cfg.exact_arith != sims[0]->cfg.exact_arith)
       return FWANT_ERR_INVALID_ARG;
     if (sims[q]->topo_on) return FWANT_ERR_INVALID_ARG;  // terrain-following grids step alone
+    if (sims[q]->tile_ty != sims[0]->tile_ty) return FWANT_ERR_INVALID_ARG;  // one tile shape per launch
   }
   auto* b = new fwant_batch();
   b->sims.assign(sims, sims + n);
@@ -2153,22 +2194,32 @@ fwant_status fwant_batch_autotune(fwant_batch* b, int trial_steps, int* ctas_out
   // items share each launch, so a member's fastest value alone is not the batch's)
   int min_nk = b->sims[0]->cfg.nk;
   for (fwant_solver* m : b->sims) min_nk = std::min(min_nk, m->cfg.nk);
+  // tile shape (32 x 8, and 32 x 16 where every member allows it) x planes per CTA
+  std::vector<int> shapes = {fw::STAGE_TY};
+  bool tall = true;
+  for (fwant_solver* m : b->sims) tall = tall && m->tile_rows_allowed(fw::STAGE_TY_TALL);
+  if (tall) shapes.push_back(fw::STAGE_TY_TALL);
   const int kcand[] = {4, 6, 8, 12, 16, 24, 32};
   double best_t = 1e30;
-  int best_kc = b->sims[0]->kc;
+  int best_kc = b->sims[0]->kc, best_ty = b->sims[0]->tile_ty;
   b->ctas = 0;
-  for (int kc : kcand) {
-    if (kc > min_nk && kc != kcand[0]) break;
-    for (fwant_solver* m : b->sims) {
-      m->kc = kc;
-      m->drop_graphs();
+  for (int ty : shapes) {
+    for (fwant_solver* m : b->sims)
+      if (fwant_status rc = m->set_tile_rows(ty); rc != FWANT_OK) return b->fail(rc, "member: " + m->err);
+    for (int kc : kcand) {
+      if (kc > min_nk && kc != kcand[0]) break;
+      for (fwant_solver* m : b->sims) {
+        m->kc = kc;
+        m->drop_graphs();
+      }
+      double t = 0.0;
+      fwant_status rc = trial(&t);
+      if (rc != FWANT_OK) return rc;
+      if (t < best_t) { best_t = t; best_kc = kc; best_ty = ty; }
     }
-    double t = 0.0;
-    fwant_status rc = trial(&t);
-    if (rc != FWANT_OK) return rc;
-    if (t < best_t) { best_t = t; best_kc = kc; }
   }
   for (fwant_solver* m : b->sims) {
+    if (fwant_status rc = m->set_tile_rows(best_ty); rc != FWANT_OK) return b->fail(rc, "member: " + m->err);
     m->kc = best_kc;
     m->drop_graphs();
   }

@@ -16,6 +16,8 @@ namespace fw {
   int configure_stage_##mode##_rk2();
 FW_DECL(fast)
 FW_DECL(exact)
+FW_DECL(fast16)
+FW_DECL(exact16)
 FW_DECL(bf16)
 FW_DECL(fp16)
 #undef FW_DECL
@@ -42,12 +44,18 @@ int launch_stage_batch_topo(const BatchArgs& b, int variant, int rk, int exact, 
 }
 
 int launch_stage_batch(const BatchArgs& b, int variant, int rk, int exact, int storage, int lean, int ctas,
-                       void* stream) {
+                       void* stream, int ty) {
   cudaStream_t st = (cudaStream_t)stream;
 #define FW_RK(mode)                                                                         \
   return rk == 0 ? launch_stage_batch_##mode##_rk0(b, variant, lean, ctas, st)              \
                  : (rk == 1 ? launch_stage_batch_##mode##_rk1(b, variant, lean, ctas, st)   \
                             : launch_stage_batch_##mode##_rk2(b, variant, lean, ctas, st));
+  if (ty == STAGE_TY_TALL) {
+    if (storage != ST_F32) return int(cudaErrorInvalidValue);
+    if (exact) { FW_RK(exact16) }
+    FW_RK(fast16)
+  }
+  if (ty != STAGE_TY) return int(cudaErrorInvalidValue);
   if (storage == ST_BF16) { FW_RK(bf16) }
   if (storage == ST_F16) { FW_RK(fp16) }
   if (exact) { FW_RK(exact) }
@@ -58,6 +66,8 @@ int launch_stage_batch(const BatchArgs& b, int variant, int rk, int exact, int s
 int stage_configure() {
   int (*const fns[])() = {configure_stage_fast_rk0, configure_stage_fast_rk1, configure_stage_fast_rk2,
                           configure_stage_exact_rk0, configure_stage_exact_rk1, configure_stage_exact_rk2,
+                          configure_stage_fast16_rk0, configure_stage_fast16_rk1, configure_stage_fast16_rk2,
+                          configure_stage_exact16_rk0, configure_stage_exact16_rk1, configure_stage_exact16_rk2,
                           configure_stage_bf16_rk0, configure_stage_bf16_rk1, configure_stage_bf16_rk2,
                           configure_stage_fp16_rk0, configure_stage_fp16_rk1, configure_stage_fp16_rk2,
                           configure_stage_topo_rk0, configure_stage_topo_rk1, configure_stage_topo_rk2,
@@ -68,16 +78,16 @@ int stage_configure() {
   return 0;
 }
 
-long long stage_item_count(const Geom& g, int kc) {
-  return (long long)((g.ni + STAGE_TX - 1) / STAGE_TX) * ((g.nj + STAGE_TY - 1) / STAGE_TY) * ((g.nk + kc - 1) / kc);
+long long stage_item_count(const Geom& g, int kc, int ty) {
+  return (long long)((g.ni + STAGE_TX - 1) / STAGE_TX) * ((g.nj + ty - 1) / ty) * ((g.nk + kc - 1) / kc);
 }
 
 // An item is lean when none of its points lies in a PML slab, within reach (3 points) of
 // a smoothed source box, or within four planes of a free surface (images, VLOW rows,
 // T*Src): exactly the code the lean form compiles out.
-void stage_items(const Geom& g, int kc, const Slab slab[6], const int* force_c, int nforce, const int* mom_c,
+void stage_items(const Geom& g, int kc, int ty, const Slab slab[6], const int* force_c, int nforce, const int* mom_c,
                  int nmom, int* lean, int* nlean, int* full, int* nfull) {
-  const int nbx = (g.ni + STAGE_TX - 1) / STAGE_TX, nby = (g.nj + STAGE_TY - 1) / STAGE_TY;
+  const int nbx = (g.ni + STAGE_TX - 1) / STAGE_TX, nby = (g.nj + ty - 1) / ty;
   const int nbz = (g.nk + kc - 1) / kc;
   auto overlap = [](int a0, int a1, int b0, int b1) { return a0 <= b1 && b0 <= a1; };
   int nl = 0, nf = 0;
@@ -85,7 +95,7 @@ void stage_items(const Geom& g, int kc, const Slab slab[6], const int* force_c, 
     for (int by = 0; by < nby; ++by)
       for (int bx = 0; bx < nbx; ++bx) {
         const int i0 = g.i1 + bx * STAGE_TX, i1 = std::min(i0 + STAGE_TX - 1, g.i2);
-        const int j0 = g.j1 + by * STAGE_TY, j1 = std::min(j0 + STAGE_TY - 1, g.j2);
+        const int j0 = g.j1 + by * ty, j1 = std::min(j0 + ty - 1, g.j2);
         const int k0 = g.k1 + bz * kc, k1 = std::min(k0 + kc - 1, g.k2);
         bool is_lean = !(g.freesurf && k1 > g.k2 - 4);
         for (int f = 0; f < 6 && is_lean; ++f) {
@@ -116,9 +126,9 @@ void stage_items(const Geom& g, int kc, const Slab slab[6], const int* force_c, 
 // re-reads; measured on 400x400x200: 16 planes 1.68 ms per RK_inn stage, 32 planes 1.78,
 // 64 planes 2.01, the whole column 3.04.  Small grids get shorter chunks so that there
 // are at least ~4 CTAs per SM.
-int stage_planes_per_cta(const Geom& g, int sm_count) {
-  const long long tiles = (long long)((g.ni + STAGE_TX - 1) / STAGE_TX) * ((g.nj + STAGE_TY - 1) / STAGE_TY);
-  const long long want = 4LL * sm_count;
+int stage_planes_per_cta(const Geom& g, int sm_count, int ty) {
+  const long long tiles = (long long)((g.ni + STAGE_TX - 1) / STAGE_TX) * ((g.nj + ty - 1) / ty);
+  const long long want = 4LL * sm_count * STAGE_TY / ty;  // ~4 CTAs of 256 threads per SM
   long long chunks = (want + tiles - 1) / tiles;
   if (chunks < 1) chunks = 1;
   int kc = int((g.nk + chunks - 1) / chunks);

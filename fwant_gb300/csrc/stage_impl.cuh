@@ -35,8 +35,7 @@
 
 namespace fw {
 
-constexpr int TX = STAGE_TX, TY = STAGE_TY;
-constexpr int TBY = TILE_BY;
+constexpr int TX = STAGE_TX;  // tile columns (one warp per tile row); the rows TY are a template parameter
 constexpr int WAIT_SPINS = 1 << 22;
 
 // Shared-memory layout of one pipeline buffer for storage type S (byte offsets,
@@ -44,8 +43,9 @@ constexpr int WAIT_SPINS = 1 << 22;
 // that its x origin stays 16-byte aligned (4 columns of 4 bytes, 8 columns of 2 bytes).
 // TOPO (terrain-following grid): the z queue holds all nine components, and the plane's
 // terrain metric (r, zeta_r, zeta_theta/r, zeta_phi/(r sin theta)) follows the medium.
-template <class S, bool TOPO = false>
+template <class S, bool TOPO = false, int TY = STAGE_TY>
 struct Lay {
+  static constexpr int TBY = tile_by(TY);
   static constexpr int ES = sizeof(S);
   static constexpr int HX = tile_halo_x(ES);
   static constexpr int TBX = tile_box_x(ES);
@@ -294,11 +294,12 @@ __device__ __forceinline__ float surf_val(const Sources& S, const float* tab, in
 // surface (the host classifies the items); that code is compiled out, and the RK
 // registers m and t are read from global memory instead of being staged, so that the
 // lean form fits three CTAs per SM (registers and shared memory).
-template <class S, bool EXACT, int FX, int FY, int FZ, int RK, bool LEAN, bool TOPO>
+template <class S, bool EXACT, int FX, int FY, int FZ, int RK, bool LEAN, bool TOPO, int TY>
 __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, int bz, unsigned char* smem) {
   static_assert(!EXACT || is_f32_v<S>, "the reference-order form exists for FP32 storage only");
   static_assert(!TOPO || (is_f32_v<S> && !LEAN), "the terrain form is FP32, full form");
-  using L = Lay<S, TOPO>;
+  using L = Lay<S, TOPO, TY>;
+  constexpr int TBY = L::TBY;
   constexpr int NQ = L::NQ;
   constexpr int TBX = L::TBX, HX = L::HX;
   constexpr int BUF_BYTES = LEAN ? L::BUF_BYTES_LEAN : L::buf_full(RK), OFF_Q = LEAN ? L::OFF_Q_L : L::OFF_Q,
@@ -1039,62 +1040,66 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
 // bx | by << 10 | bz << 20) of all simulations are numbered simulation after simulation,
 // and CTA b runs items b, b + gridDim.x, ... (one item each when the grid covers them
 // all).  Lean launches get the interior items, full launches the others.
-template <class S, bool EXACT, int FX, int FY, int FZ, int RK, bool LEAN, bool TOPO = false>
-__global__ void __launch_bounds__(TX* TY, LEAN ? 3 : 2) stage_batch_kernel(const __grid_constant__ BatchArgs B) {
+// Tile rows TY: 8 (the default, 256 threads; 3 interior-only or 2 full CTAs per SM) or 16
+// (512 threads, one CTA per SM).
+template <class S, bool EXACT, int FX, int FY, int FZ, int RK, bool LEAN, bool TOPO = false, int TY = STAGE_TY>
+__global__ void __launch_bounds__(TX* TY, (LEAN ? 24 : 16) / TY > 0 ? (LEAN ? 24 : 16) / TY : 1)
+    stage_batch_kernel(const __grid_constant__ BatchArgs B) {
   extern __shared__ __align__(1024) unsigned char smem[];
   for (int item = blockIdx.x; item < B.total; item += gridDim.x) {
     int s = 0;
     while (item >= B.off[s + 1]) ++s;
     const int packed = B.items[s][item - B.off[s]];
     const int bx = packed & 1023, by = (packed >> 10) & 1023, bz = packed >> 20;
-    if (!stage_body<S, EXACT, FX, FY, FZ, RK, LEAN, TOPO>(B.sims[s], bx, by, bz, smem)) return;
+    if (!stage_body<S, EXACT, FX, FY, FZ, RK, LEAN, TOPO, TY>(B.sims[s], bx, by, bz, smem)) return;
     __syncthreads();  // the next item re-initialises the barriers and reuses the buffers
   }
 }
 
-template <class S, bool EXACT, int FX, int FY, int FZ, int RK, bool LEAN, bool TOPO = false>
+template <class S, bool EXACT, int FX, int FY, int FZ, int RK, bool LEAN, bool TOPO = false, int TY = STAGE_TY>
 static int launch_batch_one(const BatchArgs& b, int ctas, cudaStream_t st) {
-  stage_batch_kernel<S, EXACT, FX, FY, FZ, RK, LEAN, TOPO>
-      <<<ctas, dim3(TX, TY, 1), Lay<S, TOPO>::smem_bytes(LEAN, RK), st>>>(b);
+  stage_batch_kernel<S, EXACT, FX, FY, FZ, RK, LEAN, TOPO, TY>
+      <<<ctas, dim3(TX, TY, 1), Lay<S, TOPO, TY>::smem_bytes(LEAN, RK), st>>>(b);
   return int(cudaGetLastError());
 }
 
 // Opt every instantiation of one (storage, form, RK) into the dynamic shared memory it
 // needs; called once per device before any launch or stream capture.
-template <class S, bool EXACT, int RK>
+template <class S, bool EXACT, int RK, int TY = STAGE_TY>
 static int configure_rk() {
   cudaError_t e = cudaSuccess;
-#define FW_CFG(FX, FY, FZ)                                                                           \
-  if (e == cudaSuccess)                                                                              \
-    e = cudaFuncSetAttribute(stage_batch_kernel<S, EXACT, FX, FY, FZ, RK, false>,                    \
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, Lay<S>::smem_bytes(false, RK)); \
-  if (e == cudaSuccess)                                                                              \
-    e = cudaFuncSetAttribute(stage_batch_kernel<S, EXACT, FX, FY, FZ, RK, true>,                     \
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, Lay<S>::smem_bytes(true, RK));
+#define FW_CFG(FX, FY, FZ)                                                                               \
+  if (e == cudaSuccess)                                                                                  \
+    e = cudaFuncSetAttribute(stage_batch_kernel<S, EXACT, FX, FY, FZ, RK, false, false, TY>,             \
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,                                \
+                             Lay<S, false, TY>::smem_bytes(false, RK));                                  \
+  if (e == cudaSuccess)                                                                                  \
+    e = cudaFuncSetAttribute(stage_batch_kernel<S, EXACT, FX, FY, FZ, RK, true, false, TY>,              \
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, Lay<S, false, TY>::smem_bytes(true, RK));
   FW_CFG(0, 0, 0) FW_CFG(0, 0, 1) FW_CFG(0, 1, 0) FW_CFG(0, 1, 1)
   FW_CFG(1, 0, 0) FW_CFG(1, 0, 1) FW_CFG(1, 1, 0) FW_CFG(1, 1, 1)
 #undef FW_CFG
   return int(e);
 }
 
-template <class S, bool EXACT, int RK, bool LEAN>
+template <class S, bool EXACT, int RK, bool LEAN, int TY>
 static int launch_batch_lean(const BatchArgs& b, int variant, int ctas, cudaStream_t st) {
   switch (variant) {
-    case 0: return launch_batch_one<S, EXACT, 0, 0, 0, RK, LEAN>(b, ctas, st);
-    case 1: return launch_batch_one<S, EXACT, 0, 0, 1, RK, LEAN>(b, ctas, st);
-    case 2: return launch_batch_one<S, EXACT, 0, 1, 0, RK, LEAN>(b, ctas, st);
-    case 3: return launch_batch_one<S, EXACT, 0, 1, 1, RK, LEAN>(b, ctas, st);
-    case 4: return launch_batch_one<S, EXACT, 1, 0, 0, RK, LEAN>(b, ctas, st);
-    case 5: return launch_batch_one<S, EXACT, 1, 0, 1, RK, LEAN>(b, ctas, st);
-    case 6: return launch_batch_one<S, EXACT, 1, 1, 0, RK, LEAN>(b, ctas, st);
-    default: return launch_batch_one<S, EXACT, 1, 1, 1, RK, LEAN>(b, ctas, st);
+    case 0: return launch_batch_one<S, EXACT, 0, 0, 0, RK, LEAN, false, TY>(b, ctas, st);
+    case 1: return launch_batch_one<S, EXACT, 0, 0, 1, RK, LEAN, false, TY>(b, ctas, st);
+    case 2: return launch_batch_one<S, EXACT, 0, 1, 0, RK, LEAN, false, TY>(b, ctas, st);
+    case 3: return launch_batch_one<S, EXACT, 0, 1, 1, RK, LEAN, false, TY>(b, ctas, st);
+    case 4: return launch_batch_one<S, EXACT, 1, 0, 0, RK, LEAN, false, TY>(b, ctas, st);
+    case 5: return launch_batch_one<S, EXACT, 1, 0, 1, RK, LEAN, false, TY>(b, ctas, st);
+    case 6: return launch_batch_one<S, EXACT, 1, 1, 0, RK, LEAN, false, TY>(b, ctas, st);
+    default: return launch_batch_one<S, EXACT, 1, 1, 1, RK, LEAN, false, TY>(b, ctas, st);
   }
 }
 
-template <class S, bool EXACT, int RK>
+template <class S, bool EXACT, int RK, int TY = STAGE_TY>
 static int launch_batch_rk_variant(const BatchArgs& b, int variant, int lean, int ctas, cudaStream_t st) {
-  return lean ? launch_batch_lean<S, EXACT, RK, true>(b, variant, ctas, st)
-              : launch_batch_lean<S, EXACT, RK, false>(b, variant, ctas, st);
+  return lean ? launch_batch_lean<S, EXACT, RK, true, TY>(b, variant, ctas, st)
+              : launch_batch_lean<S, EXACT, RK, false, TY>(b, variant, ctas, st);
 }
 
 // Terrain form (FP32 storage, full form; EXACT selects the reference-order arithmetic):

@@ -368,6 +368,12 @@ fwant_status fwant_last_run_ms(fwant_solver* s, double* ms);
  * the grid size; a tuning knob of the autotuner).  No counterpart in the reference. */
 fwant_status fwant_set_planes_per_cta(fwant_solver* s, int planes);
 fwant_status fwant_get_planes_per_cta(fwant_solver* s, int* planes);
+/* Rows of the stage kernel's 32-column tile: 8 (the default; every storage and form) or 16
+ * (FP32 storage without topography; 512-thread CTAs, one per SM).  Same results as the
+ * default in the reference-order form; a tuning knob of the autotuners.  Batch members
+ * must share it.  No counterpart in the reference. */
+fwant_status fwant_set_tile_rows(fwant_solver* s, int rows);
+fwant_status fwant_get_tile_rows(fwant_solver* s, int* rows);
 /* Which RK stages split their work items into an interior-only launch and a full launch
  * (bit 0: stage 1, bit 2: stage 4; default 5); 0 runs every stage as one full launch.
  * No counterpart in the reference (a tuning knob of the stage kernel, set by
@@ -380,8 +386,10 @@ fwant_status fwant_set_lean_stages(fwant_solver* s, int mask);
 fwant_status fwant_check_wait_timeout(fwant_solver* s, int spins);
 fwant_status fwant_get_lean_stages(fwant_solver* s, int* mask);
 
-/* Autotuner: times every planes-per-CTA candidate (4 ... 128, up to nk) over trial_steps
- * eager steps with CUDA events, keeps the fastest and returns it in *planes (may be NULL).
+/* Autotuner: times every tile shape (32 x 8, and 32 x 16 where fwant_set_tile_rows allows
+ * it) with every planes-per-CTA candidate (4 ... 128, up to nk) over trial_steps eager
+ * steps with CUDA events, keeps the fastest pair (fwant_get_tile_rows reads the shape) and
+ * returns the planes in *planes (may be NULL).
  * Call before the first time step: the trial steps run from the initial state, which is
  * restored afterwards (wavefield, memory variables, receiver and SGT records).  Results
  * are cached per process by problem shape.  No counterpart in the reference. */
