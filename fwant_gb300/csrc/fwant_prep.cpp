@@ -10,6 +10,9 @@
 //   fwant_prep source  [SeisFD3D.conf]               SOURCE_CONF + coord -> SOURCE_ROOT/source_mpi000000.nc
 //   fwant_prep station [SeisFD3D.conf]               receivers of SeisFD3D.conf + coord
 //                                                    -> STATION_ROOT/station_mpi000000.nc
+//   fwant_prep stitch  [SeisFD3D.conf] --out DIR     the per-rank files of a dims > 1 input set
+//                                                    -> DIR/{coord,metric,media,source,station}_mpi000000.nc
+//                                                       and DIR/SeisFD3D.conf (one rank)
 //
 // grid, source and station run on the host (a few thousand coordinates and a handful of
 // points); metric evaluates the FP64 metric on the GPU (fwant_metric_arrays).  Every FP32
@@ -18,6 +21,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <fstream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -449,15 +453,315 @@ void stage_station(const conf::Text& cf) {
   std::printf("%zu of %zu receivers located\n", nrec, num_pt);
 }
 
+
+// ---- stitch: a multi-rank input set (dims > 1) as the one-rank set of the same grid -------
+//
+// The reference's preprocessors write one file per rank (set_mpi_subfix, mod_mpi.F90:415-423:
+// coord_mpiIIJJKK.nc ...), each over the rank's local arrays with ghosts: rank (a, b, c) of
+// dims (da, db, dc) holds global points a*ni + l, l = 0 .. ni+5 (0-based, ghosts included;
+// swmpi_globi, mod_mpi.F90:450-454), with ni the per-rank size of SeisFD3D.conf.  The
+// stitched grid has NI = ni*da points and takes every point from the rank that owns it as
+// an interior point (the outer ghost planes from the edge ranks): a rank's own ghost values
+// can differ from its neighbour's interior ones (seis3d_metric's one-sided stencils at the
+// local ends).  Sources are listed by every rank whose points with ghosts hold their centre
+// (seis3d_source.F90:186-293) with local indices: they are mapped to global indices and
+// kept once, in rank order.  Receivers are listed by the one rank whose interior holds them
+// (seis3d_station.F90:64-105): mapped and concatenated in rank order.
+std::string rank_suffix(int a, int b, int c) {
+  char buf[40];  // dims are at most 99 per direction: two digits each (i2.2)
+  std::snprintf(buf, sizeof buf, "mpi%02d%02d%02d", a, b, c);
+  return buf;
+}
+
+struct RankFile {
+  int r[3];
+  nc3::Reader f;
+  std::string path;
+};
+
+void stage_stitch(const std::string& conf_path, const std::string& out_dir) {
+  const conf::Text cf(conf_path);
+  const int n[3] = {cf.get_int("ni", 2), cf.get_int("nj", 2), cf.get_int("nk", 2)};
+  int dims[3] = {1, 1, 1};
+  if (cf.has("dims"))
+    for (int d = 0; d < 3; ++d) dims[d] = cf.get_int("dims", d + 2);
+  for (int d = 0; d < 3; ++d)
+    if (n[d] < 2 || dims[d] < 1 || dims[d] > 99) die(conf_path + ": ni, nj, nk >= 2 and dims 1 .. 99");
+  const int N[3] = {n[0] * dims[0], n[1] * dims[1], n[2] * dims[2]};
+  const int X[3] = {N[0] + 2 * LENFD, N[1] + 2 * LENFD, N[2] + 2 * LENFD};       // stitched with ghosts
+  const int lx[3] = {n[0] + 2 * LENFD, n[1] + 2 * LENFD, n[2] + 2 * LENFD};      // one rank with ghosts
+  // owner rank and local index of global index G (0-based with ghosts) along axis d
+  auto owner = [&](int d, int G, int* l) {
+    int r = (G - LENFD) / n[d];
+    if (G < LENFD) r = 0;
+    if (r > dims[d] - 1) r = dims[d] - 1;
+    *l = G - r * n[d];
+    return r;
+  };
+  auto open_all = [&](const std::string& root, const std::string& prefix) {
+    std::vector<RankFile> files;
+    files.reserve(size_t(dims[0]) * dims[1] * dims[2]);  // the readers own open files: never relocated
+    for (int a = 0; a < dims[0]; ++a)
+      for (int b = 0; b < dims[1]; ++b)
+        for (int c = 0; c < dims[2]; ++c) {
+          files.emplace_back();
+          RankFile& rf = files.back();
+          rf.r[0] = a; rf.r[1] = b; rf.r[2] = c;
+          rf.path = root + "/" + prefix + "_" + rank_suffix(a, b, c) + ".nc";
+          std::string err;
+          if (!rf.f.open(rf.path, &err)) die(err);
+        }
+    return files;
+  };
+  auto rank_of = [&](const std::vector<RankFile>& files, int a, int b, int c) -> const RankFile& {
+    return files[size_t((a * dims[1] + b) * dims[2] + c)];
+  };
+  auto read_d = [&](const RankFile& rf, const std::string& name) {
+    std::vector<double> v;
+    std::string err;
+    if (!rf.f.read(name, &v, &err)) die(rf.path + ": " + err);
+    return v;
+  };
+  const std::string grid_atts[] = {"ni1", "ni2", "nj1", "nj2", "nk1", "nk2", "ni", "nj", "nk", "nx1", "nx2",
+                                   "ny1", "ny2", "nz1", "nz2", "nx", "ny", "nz", "ngi1", "ngi2", "ngj1", "ngj2",
+                                   "ngk1", "ngk2", "ngx1", "ngx2", "ngy1", "ngy2", "ngz1", "ngz2"};
+  auto grid_att_value = [&](const std::string& name) -> double {
+    const int ax = name.find('i') != std::string::npos || name.find('x') != std::string::npos ? 0
+                   : (name.find('j') != std::string::npos || name.find('y') != std::string::npos ? 1 : 2);
+    const bool ghosts = name.find('x') != std::string::npos || name.find('y') != std::string::npos ||
+                        name.find('z') != std::string::npos;
+    const char last = name.back();
+    if (last == '1') return ghosts ? 1 : LENFD + 1;
+    if (last == '2') return ghosts ? X[ax] : LENFD + N[ax];
+    return ghosts ? X[ax] : N[ax];
+  };
+  // grid-shaped files: every variable over I, J and/or K is assembled point by point
+  auto stitch_grid = [&](const std::string& root, const std::string& prefix) {
+    std::vector<RankFile> files = open_all(root, prefix);
+    const nc3::Reader& f0 = files[0].f;
+    nc3::Writer w;
+    std::vector<int> dim_axis;  // per dimension of rank 0's file: axis 0..2 or -1
+    for (const nc3::Dim& dm : f0.dims) {
+      const int ax = dm.name == "I" ? 0 : (dm.name == "J" ? 1 : (dm.name == "K" ? 2 : -1));
+      if (ax >= 0 && dm.len != uint64_t(lx[ax])) die(files[0].path + ": dimension " + dm.name + " is not n + 6");
+      dim_axis.push_back(ax);
+      w.add_dim(dm.name, ax >= 0 ? uint64_t(X[ax]) : dm.len);
+    }
+    for (const nc3::Att& at : f0.gatts) {
+      bool grid = false;
+      for (const std::string& g : grid_atts) grid = grid || at.name == g;
+      if (at.type == nc3::NC_CHAR) w.add_gatt_text(at.name, at.text);
+      else if (grid) w.add_gatt(at.name, at.type, {grid_att_value(at.name)});
+      else if (at.name == "point_in_this")
+        w.add_gatt(at.name, at.type, {double(LENFD + 1), double(LENFD + N[0]), double(LENFD + 1), double(LENFD + N[1]),
+                                      double(LENFD + 1), double(LENFD + N[2])});
+      else if (at.name == "count") w.add_gatt(at.name, at.type, {double(X[0]), double(X[1]), double(X[2])});
+      else w.add_gatt(at.name, at.type, at.num);
+    }
+    for (const nc3::Var& v : f0.vars) {
+      // the variable's axes, slowest first; a dimension that is not I, J, K must have length 1
+      std::vector<int> axes;
+      for (int d : v.dims) {
+        if (dim_axis[size_t(d)] < 0 && f0.dims[size_t(d)].len != 1)
+          die(files[0].path + ": variable " + v.name + " has a non-grid dimension");
+        axes.push_back(dim_axis[size_t(d)]);
+      }
+      std::vector<std::vector<double>> local(files.size());
+      for (size_t q = 0; q < files.size(); ++q) local[q] = read_d(files[q], v.name);
+      size_t total = 1;
+      for (int ax : axes) total *= ax >= 0 ? size_t(X[ax]) : 1;
+      std::vector<double> out(total);
+      std::vector<int> G(axes.size(), 0);
+      for (size_t e = 0; e < total; ++e) {
+        // decompose e (last dimension fastest) into global indices
+        size_t rem = e;
+        for (size_t q = axes.size(); q-- > 0;) {
+          const int len = axes[q] >= 0 ? X[axes[q]] : 1;
+          G[q] = int(rem % size_t(len));
+          rem /= size_t(len);
+        }
+        int r[3] = {0, 0, 0}, l[3] = {0, 0, 0};
+        for (size_t q = 0; q < axes.size(); ++q)
+          if (axes[q] >= 0) r[axes[q]] = owner(axes[q], G[q], &l[axes[q]]);
+        const RankFile& rf = rank_of(files, r[0], r[1], r[2]);
+        size_t le = 0;
+        for (size_t q = 0; q < axes.size(); ++q) le = le * size_t(axes[q] >= 0 ? lx[axes[q]] : 1) + size_t(axes[q] >= 0 ? l[axes[q]] : 0);
+        out[e] = local[size_t(&rf - files.data())][le];
+      }
+      std::vector<int> vdims(v.dims.begin(), v.dims.end());
+      w.add_var(v.name, v.type, vdims, out);
+    }
+    write_or_die(w, out_dir + "/" + prefix + "_" + SUFFIX + ".nc");
+  };
+  stitch_grid(cf.get("GRID_ROOT", 2), "coord");
+  stitch_grid(cf.get("GRID_ROOT", 2), "metric");
+  stitch_grid(cf.get("MEDIA_ROOT", 2), "media");
+
+  // list-shaped files: the records of every rank, indices mapped to the stitched grid
+  auto map_indx = [&](std::vector<double>& v, const RankFile& rf) {
+    for (size_t e = 0; e < v.size(); ++e) v[e] += double(rf.r[e % 3] * n[e % 3]);
+  };
+  // sources: per kind (force, moment), the records in rank order, each kept once
+  {
+    std::vector<RankFile> files = open_all(cf.get("SOURCE_ROOT", 2), "source");
+    const nc3::Reader& f0 = files[0].f;
+    nc3::Writer w;
+    std::vector<int> dmap(f0.dims.size());
+    struct Kind {
+      std::string k;
+      std::vector<std::vector<double>> recs;  // per kept source: all its values, variable after variable
+      int ntw = 0;
+    };
+    Kind kinds[2] = {{"force"}, {"moment"}};
+    for (Kind& kd : kinds) {
+      const nc3::Dim* tw = f0.dim(kd.k + "_time_window");
+      if (!tw) continue;
+      kd.ntw = int(tw->len);
+    }
+    // per kind the point-dimensioned variables in rank 0's order
+    auto point_vars = [&](const std::string& k) {
+      std::vector<const nc3::Var*> vs;
+      const nc3::Dim* pd = f0.dim(k + "_point");
+      if (!pd) return vs;
+      const int pid = int(pd - f0.dims.data());
+      for (const nc3::Var& v : f0.vars)
+        if (!v.dims.empty() && v.dims[0] == pid) vs.push_back(&v);
+      return vs;
+    };
+    for (Kind& kd : kinds) {
+      if (!f0.dim(kd.k + "_point")) continue;
+      const std::vector<const nc3::Var*> vs = point_vars(kd.k);
+      for (const RankFile& rf : files) {
+        const nc3::Dim* pd = rf.f.dim(kd.k + "_point");
+        const size_t np = pd ? size_t(pd->len) : 0;
+        if (np == 0) continue;
+        std::vector<std::vector<double>> vals;
+        for (const nc3::Var* v : vs) {
+          std::vector<double> a = read_d(rf, v->name);
+          if (v->name == kd.k + "_indx") map_indx(a, rf);
+          vals.push_back(std::move(a));
+        }
+        for (size_t p = 0; p < np; ++p) {
+          std::vector<double> rec;
+          for (const std::vector<double>& a : vals) {
+            const size_t per = a.size() / np;
+            rec.insert(rec.end(), a.begin() + ptrdiff_t(p * per), a.begin() + ptrdiff_t((p + 1) * per));
+          }
+          bool seen = false;
+          for (const auto& r : kd.recs) seen = seen || r == rec;
+          if (!seen) kd.recs.push_back(std::move(rec));
+        }
+      }
+    }
+    for (size_t d = 0; d < f0.dims.size(); ++d) {
+      const nc3::Dim& dm = f0.dims[d];
+      uint64_t len = dm.len;
+      for (const Kind& kd : kinds)
+        if (dm.name == kd.k + "_point") len = kd.recs.size();
+      dmap[d] = w.add_dim(dm.name, len);
+    }
+    for (const nc3::Att& at : f0.gatts) {
+      if (at.type == nc3::NC_CHAR) w.add_gatt_text(at.name, at.text);
+      else if (at.name == "number_of_force") w.add_gatt(at.name, at.type, {double(kinds[0].recs.size())});
+      else if (at.name == "number_of_moment") w.add_gatt(at.name, at.type, {double(kinds[1].recs.size())});
+      else w.add_gatt(at.name, at.type, at.num);
+    }
+    for (const nc3::Var& v : f0.vars) {
+      std::vector<int> vdims;
+      for (int d : v.dims) vdims.push_back(dmap[size_t(d)]);
+      const Kind* kd = nullptr;
+      size_t off = 0, per = 0;
+      for (const Kind& k : kinds) {
+        const std::vector<const nc3::Var*> vs = point_vars(k.k);
+        size_t o = 0;
+        for (const nc3::Var* pv : vs) {
+          size_t each = 1;
+          for (size_t q = 1; q < pv->dims.size(); ++q) each *= size_t(f0.dims[size_t(pv->dims[q])].len);
+          if (pv == &v) { kd = &k; off = o; per = each; }
+          o += each;
+        }
+      }
+      std::vector<double> out;
+      if (kd) {
+        for (const auto& rec : kd->recs) out.insert(out.end(), rec.begin() + ptrdiff_t(off), rec.begin() + ptrdiff_t(off + per));
+      } else {
+        out = read_d(files[0], v.name);  // per-window tables, the same in every rank's file
+      }
+      w.add_var(v.name, v.type, vdims, out);
+    }
+    write_or_die(w, out_dir + "/source_" + SUFFIX + ".nc");
+  }
+  // receivers: every rank's records in rank order
+  {
+    std::vector<RankFile> files = open_all(cf.get("STATION_ROOT", 2), "station");
+    const nc3::Reader& f0 = files[0].f;
+    nc3::Writer w;
+    std::vector<std::vector<double>> cols(f0.vars.size());
+    size_t total = 0;
+    for (const RankFile& rf : files) {
+      const size_t np = size_t(rf.f.numrecs());
+      total += np;
+      for (size_t q = 0; q < f0.vars.size(); ++q) {
+        if (np == 0) continue;
+        std::vector<double> a = read_d(rf, f0.vars[q].name);
+        if (f0.vars[q].name == "indx") map_indx(a, rf);
+        cols[q].insert(cols[q].end(), a.begin(), a.end());
+      }
+    }
+    std::vector<int> dmap;
+    for (const nc3::Dim& dm : f0.dims) dmap.push_back(w.add_dim(dm.name, dm.len));
+    for (const nc3::Att& at : f0.gatts) {
+      if (at.type == nc3::NC_CHAR) w.add_gatt_text(at.name, at.text);
+      else w.add_gatt(at.name, at.type, at.num);
+    }
+    for (size_t q = 0; q < f0.vars.size(); ++q) {
+      std::vector<int> vdims;
+      for (int d : f0.vars[q].dims) vdims.push_back(dmap[size_t(d)]);
+      w.add_var(f0.vars[q].name, f0.vars[q].type, vdims, cols[q]);
+    }
+    w.set_numrecs(total);
+    write_or_die(w, out_dir + "/station_" + SUFFIX + ".nc");
+  }
+  // the one-rank configuration: the same file with the stitched sizes, dims 1 1 1 and the
+  // input roots pointing at out_dir
+  {
+    std::ifstream in(conf_path);
+    std::ofstream out(out_dir + "/SeisFD3D.conf");
+    if (!in || !out) die("cannot copy " + conf_path + " to " + out_dir);
+    const std::string nv[3] = {std::to_string(N[0]), std::to_string(N[1]), std::to_string(N[2])};
+    for (std::string line; std::getline(in, line);) {
+      const size_t eq = line.find('=');
+      std::string key = eq == std::string::npos ? "" : line.substr(0, eq);
+      key.erase(0, key.find_first_not_of(" \t"));
+      key.erase(key.find_last_not_of(" \t") + 1);
+      if (key == "ni" || key == "nj" || key == "nk")
+        line = key + " = " + nv[key == "ni" ? 0 : (key == "nj" ? 1 : 2)];
+      else if (key == "dims")
+        line = "dims = 1 1 1";
+      else if (key == "GRID_ROOT" || key == "MEDIA_ROOT" || key == "SOURCE_ROOT" || key == "STATION_ROOT")
+        line = key + " = " + out_dir;
+      out << line << "\n";
+    }
+  }
+  std::printf("stitched %d x %d x %d ranks into one %d x %d x %d grid in %s\n", dims[0], dims[1], dims[2], N[0], N[1],
+              N[2], out_dir.c_str());
+}
+
 int run(int argc, char** argv) {
-  if (argc < 2) die("usage: fwant_prep grid|metric|source|station [SeisFD3D.conf] [--device N]");
+  if (argc < 2) die("usage: fwant_prep grid|metric|source|station|stitch [SeisFD3D.conf] [--device N] [--out DIR]");
   const std::string stage = argv[1];
-  std::string conf_path = "SeisFD3D.conf";
+  std::string conf_path = "SeisFD3D.conf", out_dir;
   int device = 0;
   for (int a = 2; a < argc; ++a) {
     const std::string s = argv[a];
     if (s == "--device" && a + 1 < argc) device = std::atoi(argv[++a]);
+    else if (s == "--out" && a + 1 < argc) out_dir = argv[++a];
     else conf_path = s;
+  }
+  if (stage == "stitch") {
+    if (out_dir.empty()) die("stitch: --out DIR is required");
+    stage_stitch(conf_path, out_dir);
+    return 0;
   }
   const conf::Text cf(conf_path);
   if (stage == "grid") stage_grid(cf);

@@ -287,7 +287,7 @@ int main(int argc, char** argv) {
   const double stept = need_d("stept", 2);
   if (cf.has("dims"))
     for (int d = 0; d < 3; ++d)
-      if (need_i("dims", d + 2) != 1) die("dims must be 1 1 1: one GPU runs the whole grid");
+      if (need_i("dims", d + 2) != 1) die("dims must be 1 1 1: one GPU runs the whole grid (fwant_prep stitch turns a multi-rank input set into one rank)");
   const std::string grid_root = need_s("GRID_ROOT"), media_root = need_s("MEDIA_ROOT"),
                     source_root = need_s("SOURCE_ROOT"), station_root = need_s("STATION_ROOT"),
                     out_root = need_s("OUTPUT_ROOT");
