@@ -5,8 +5,8 @@ sm_103a plus the C++ host driver); this package only binds it (``_lib``) and bui
 the reference's input arrays (``inputs``).
 """
 from ._lib import (COMPONENTS, STF_RICKER, STORAGE_BF16, STORAGE_FP16, STORAGE_FP32, STORAGE_FP64, FwantError,
-                   Assm, Batch, Lsqr, Media, SgtKernel, Solver, load_library, metric, reference_steps,
+                   Assm, Batch, KerInfo, Lsqr, Media, SgtKernel, Solver, load_library, metric, reference_steps,
                    source_time_function)
 
-__all__ = ["Solver", "Batch", "Assm", "SgtKernel", "Lsqr", "Media", "FwantError", "load_library", "metric", "reference_steps", "source_time_function", "COMPONENTS", "STF_RICKER",
+__all__ = ["Solver", "Batch", "Assm", "KerInfo", "SgtKernel", "Lsqr", "Media", "FwantError", "load_library", "metric", "reference_steps", "source_time_function", "COMPONENTS", "STF_RICKER",
            "STORAGE_FP32", "STORAGE_BF16", "STORAGE_FP16", "STORAGE_FP64"]

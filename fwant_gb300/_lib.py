@@ -138,6 +138,16 @@ EXPORTS = [
     ("fwant_assm_project_device", C.c_int, [_vp, C.c_int, C.POINTER(C.c_void_p), _fp]),
     ("fwant_assm_sums", C.c_int, [_vp, _fp]),
     ("fwant_assm_last_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
+    # kernel statistics (include/fwant_kerinfo.h)
+    ("fwant_kerinfo_create", C.c_int, [C.c_longlong, _fp, C.c_int, C.POINTER(C.c_void_p)]),
+    ("fwant_kerinfo_destroy", None, [_vp]),
+    ("fwant_kerinfo_last_error", C.c_char_p, [_vp]),
+    ("fwant_kerinfo_add_pick", C.c_int, [_vp, C.POINTER(_fp)]),
+    ("fwant_kerinfo_end_event", C.c_int, [_vp, C.c_int, C.c_int]),
+    ("fwant_kerinfo_records", C.c_int, [_vp, C.POINTER(C.c_int)]),
+    ("fwant_kerinfo_totals", C.c_int, [_vp, _fp, C.POINTER(C.c_int)]),
+    ("fwant_kerinfo_record", C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    ("fwant_kerinfo_last_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
     # medium preprocessor (include/fwant_media.h)
     ("fwant_media_create", C.c_int, [C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, C.c_float, C.POINTER(C.c_int), C.c_int,
                                      C.POINTER(C.c_void_p)]),
@@ -871,6 +881,71 @@ class Assm:
     def close(self):
         if getattr(self, "_h", None):
             self._lib.fwant_assm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class KerInfo:
+    """Kernel statistics on the GPU (SI_ker2info's per-point sums, counts and records) over
+    volumes of npts points; thresholds kap0 kaq0 kbp0 kbq0."""
+
+    def __init__(self, npts, thresholds, device=0):
+        self._lib = load_library()
+        self.npts = int(npts)
+        th = np.ascontiguousarray(np.asarray(thresholds, np.float32).reshape(4))
+        h = C.c_void_p()
+        rc = self._lib.fwant_kerinfo_create(self.npts, _ptr(th), int(device), C.byref(h))
+        if rc != 0:
+            msg = self._lib.fwant_kerinfo_last_error(h).decode() if h.value else "fwant_kerinfo_create failed"
+            if h.value:
+                self._lib.fwant_kerinfo_destroy(h)
+            raise FwantError(rc, msg)
+        self._h = h
+
+    def _chk(self, rc):
+        if rc != 0:
+            raise FwantError(rc, self._lib.fwant_kerinfo_last_error(self._h).decode())
+
+    def add_pick(self, kernels):
+        """The four volumes of one pick (any shape of npts points, in point order)."""
+        ks = [np.ascontiguousarray(np.asarray(k, np.float32).reshape(self.npts)) for k in kernels]
+        arr = (_fp * 4)(*[_ptr(k) for k in ks])
+        self._chk(self._lib.fwant_kerinfo_add_pick(self._h, arr))
+
+    def end_event(self, station_tag, event_tag):
+        self._chk(self._lib.fwant_kerinfo_end_event(self._h, int(station_tag), int(event_tag)))
+
+    def records(self):
+        n = C.c_int()
+        self._chk(self._lib.fwant_kerinfo_records(self._h, C.byref(n)))
+        return n.value
+
+    def totals(self):
+        """(S, N): (4, npts) float32 and int32."""
+        S = np.zeros((4, self.npts), np.float32)
+        N = np.zeros((4, self.npts), np.int32)
+        self._chk(self._lib.fwant_kerinfo_totals(self._h, _ptr(S), _ptr(N, C.c_int)))
+        return S, N
+
+    def record(self, r):
+        """(M, station tags, event tags) of record r, each (4, npts) int32."""
+        out = [np.zeros((4, self.npts), np.int32) for _ in range(3)]
+        self._chk(self._lib.fwant_kerinfo_record(self._h, int(r), *[_ptr(o, C.c_int) for o in out]))
+        return tuple(out)
+
+    def last_ms(self):
+        ms = C.c_double()
+        self._chk(self._lib.fwant_kerinfo_last_ms(self._h, C.byref(ms)))
+        return ms.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.fwant_kerinfo_destroy(self._h)
             self._h = None
 
     def __del__(self):

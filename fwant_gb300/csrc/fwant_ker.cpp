@@ -55,6 +55,7 @@
 #include <vector>
 
 #include "../../include/fwant_gb300.h"
+#include "../../include/fwant_kerinfo.h"
 #include "conf.h"
 #include "netcdf3.h"
 #include "seisfd_conf.h"
@@ -190,7 +191,9 @@ struct Event {
 };
 
 // One event list (SI_ker_sta.F90:350-400, 650-715): comment lines start with '#'.
-std::vector<Event> read_events(const std::string& path, int num_freq) {
+// strict false: SI_ker2info's reading (SI_ker2info.F90:193-262), which takes the pick's
+// band and filter name as they stand.
+std::vector<Event> read_events(const std::string& path, int num_freq, bool strict = true) {
   std::ifstream in(path);
   if (!in) die("evt_list open err: " + path);
   std::vector<Event> out;
@@ -223,10 +226,10 @@ std::vector<Event> read_events(const std::string& path, int num_freq) {
           if (pw.size() < 5) die(path + ": pick line needs band, filter, t1, t2 and a directory: " + pl);
           Pick pk;
           pk.freq = to_i(pw[0], path);
-          if (pk.freq > num_freq) die("frequency band id overflow");
+          if (strict && pk.freq > num_freq) die("frequency band id overflow");
           if (pw[1] == "P1") pk.filt = 1;
           else if (pw[1] == "P2") pk.filt = 2;
-          else if (pw[1] == "N") pk.filt = 0;
+          else if (pw[1] == "N" || !strict) pk.filt = 0;
           else die(path + ": pickfilt error: " + pw[1]);
           pk.t1 = to_f(pw[2], path);
           pk.t2 = to_f(pw[3], path);
@@ -433,6 +436,165 @@ long long convert_block(fwant_sgtker* K, int conv, const std::vector<Event>& eve
 
 }  // namespace
 
+// --info: the kernel statistics of SI_ker2info (code/srcF.kernel/SI_ker2info.F90).
+// TomoKernel.conf gives MAIN_CONF and snap_id (init_kernel :422-433); standard input the
+// station list, the output directory, the thresholds kap0 kaq0 kbp0 kbq0 and the rank id,
+// each read list-directed (:116-129).  Every pick's kernel file
+// <pick directory>/kernel_NNN_mpi000000_n00000.nc is read over the snapshot's whole I J K
+// (:268-274) and folded in on the device (fwant_kerinfo); the result is
+// <output directory>/kerinfo_NNN_mpi000000_n00000.nc (kernelinfo_skel :435-483).
+int run_info(const std::string& ker_conf, int device) {
+  conf::File kc;
+  std::string err;
+  if (!kc.load(ker_conf, &err)) die(err);
+  std::string main_conf, kid_s;
+  if (!kc.get("MAIN_CONF", 2, &main_conf) || !kc.get("snap_id", 2, &kid_s))
+    die(ker_conf + ": keys MAIN_CONF and snap_id needed");
+  const int kid = to_i(kid_s, "snap_id");
+  conf::File cf;
+  if (!cf.load(main_conf, &err)) die(err);
+  std::vector<seisfd::SnapDef> snaps;
+  try {
+    const int ni = seisfd::need_int(cf, "ni", 2), nj = seisfd::need_int(cf, "nj", 2), nk = seisfd::need_int(cf, "nk", 2);
+    if (cf.has("dims"))
+      for (int d = 0; d < 3; ++d)
+        if (seisfd::need_int(cf, "dims", d + 2) != 1) die("dims must be 1 1 1: one GPU holds the whole grid");
+    snaps = seisfd::read_snaps(cf, ni, nj, nk);
+  } catch (const std::exception& e) {
+    die(main_conf + ": " + e.what());
+  }
+  // list-directed records of standard input: a character value is the record's first item
+  // (quotes removed), numbers may continue over further records; blank records hold none
+  std::string line;
+  auto first_item = [&](const char* what) {
+    while (std::getline(std::cin, line)) {
+      const auto w = words(line);
+      if (!w.empty()) return unquote(w[0]);
+    }
+    die(std::string("standard input: ") + what + " missing");
+  };
+  auto numbers = [&](size_t n, const char* what) {
+    std::vector<std::string> w;
+    while (w.size() < n && std::getline(std::cin, line))
+      for (const std::string& t : words(line)) w.push_back(t);
+    if (w.size() < n) die(std::string("standard input: ") + what + " missing");
+    w.resize(n);
+    return w;
+  };
+  const std::string sgt_list = first_item("station list file name");
+  const std::string pnm_info = first_item("output directory");
+  float k0[4];
+  {
+    const auto w = numbers(4, "thresholds kap0 kaq0 kbp0 kbq0");
+    for (int q = 0; q < 4; ++q) k0[q] = to_f(w[size_t(q)], "threshold");
+  }
+  std::printf(" input mpi id:\n");
+  for (const std::string& t : numbers(3, "rank id (n_i n_j n_k)"))
+    if (to_i(t, "rank id") != 0) die("rank id must be 0 0 0: one rank holds the whole grid");
+
+  const seisfd::SnapDef* sp = nullptr;
+  for (const seisfd::SnapDef& q : snaps)
+    if (q.id == kid) sp = &q;
+  if (!sp) die(main_conf + ": snap_" + seisfd::pad(kid, 3) + " missing");
+  if (!sp->sgt) {  // kernode_if (:147)
+    std::printf("fwant_ker: snapshot series %d holds no stresses: nothing to do\n", kid);
+    return 0;
+  }
+  const int I = sp->subc[0], J = sp->subc[1], Kd = sp->subc[2];
+  const size_t np = size_t(I) * J * Kd;
+  std::ifstream sl(sgt_list);
+  if (!sl) die("sgt_list open err:" + sgt_list);
+  fwant_kerinfo* info = nullptr;
+  if (fwant_kerinfo_create((long long)np, k0, device, &info) != FWANT_OK)
+    die(std::string("kerinfo_create: ") + (info ? fwant_kerinfo_last_error(info) : "error"));
+  auto kcheck = [&](fwant_status rc, const char* what) {
+    if (rc != FWANT_OK) die(std::string(what) + ": " + fwant_kerinfo_last_error(info));
+  };
+  // names of the record variables (MAXKSTNM 8, MAXKEVNM 20, :34): a longer or empty name is
+  // not stored (the library refuses the write, the reference ignores the error)
+  std::vector<std::string> sta_names, evt_names;
+  auto tag = [](std::vector<std::string>& names, const std::string& n, size_t maxlen) {
+    if (n.empty() || n.size() > maxlen) return 0;
+    names.push_back(n);
+    return int(names.size());
+  };
+  static const char* const vname[4] = {"phase_Vp", "amplitude_Vp", "phase_Vs", "amplitude_Vs"};
+  const std::string kfile = "/kernel_" + seisfd::pad(kid, 3) + "_" + seisfd::MPI_SUFFIX + "_n00000.nc";
+  const std::vector<uint64_t> st0 = {0, 0, 0}, ct = {uint64_t(Kd), uint64_t(J), uint64_t(I)}, sd1 = {1, 1, 1};
+  std::vector<float> vol[4];
+  long long picks = 0, nevents = 0;
+  while (std::getline(sl, line)) {  // sta_loop (:162-340)
+    const auto w = words(line);
+    if (w.empty() || w[0][0] == '#') continue;
+    // KSTNM up to the first blank, the event list next; a single item is the event list
+    const std::string sta = w.size() >= 2 ? w[0] : std::string();
+    const std::string evt_list = w.size() >= 2 ? w[1] : w[0];
+    const std::vector<Event> events = read_events(evt_list, 0, false);
+    const int sta_tag = tag(sta_names, sta, 8);
+    for (const Event& e : events) {
+      bool any = false;
+      for (int c = 0; c < 6; ++c) any = any || e.picknum[c] > 0;
+      if (!any) continue;  // (:225)
+      const int evt_tag = tag(evt_names, e.name, 20);
+      for (int c = 0; c < 6; ++c)
+        for (const Pick& pk : e.picks[c]) {
+          const std::string path = pk.dir + kfile;
+          nc3::Reader rd;
+          if (!rd.open(path, &err)) die("nfseis_varget: " + err);
+          for (int q = 0; q < 4; ++q)
+            if (!rd.read_slab(vname[q], st0, ct, sd1, &vol[q], &err)) die(path + ": " + err);
+          const float* kp[4] = {vol[0].data(), vol[1].data(), vol[2].data(), vol[3].data()};
+          kcheck(fwant_kerinfo_add_pick(info, kp), "add_pick");
+          ++picks;
+        }
+      kcheck(fwant_kerinfo_end_event(info, sta_tag, evt_tag), "end_event");
+      ++nevents;
+    }
+  }
+  int nrec = 0;
+  kcheck(fwant_kerinfo_records(info, &nrec), "records");
+  std::vector<float> S(4 * np);
+  std::vector<int> N(4 * np);
+  kcheck(fwant_kerinfo_totals(info, S.data(), N.data()), "totals");
+  std::vector<int> M[4], rm(4 * np), rs(4 * np), re(4 * np);
+  std::vector<char> CS[4], CE[4];
+  for (int q = 0; q < 4; ++q) {
+    M[q].reserve(size_t(nrec) * np);
+    CS[q].assign(size_t(nrec) * np * 8, 0);
+    CE[q].assign(size_t(nrec) * np * 20, 0);
+  }
+  for (int r = 0; r < nrec; ++r) {
+    kcheck(fwant_kerinfo_record(info, r, rm.data(), rs.data(), re.data()), "record");
+    for (int q = 0; q < 4; ++q) {
+      M[q].insert(M[q].end(), rm.begin() + q * np, rm.begin() + (q + 1) * np);
+      for (size_t p = 0; p < np; ++p) {
+        const int a = rs[q * np + p], b = re[q * np + p];
+        if (a > 0) std::memcpy(&CS[q][(size_t(r) * np + p) * 8], sta_names[size_t(a - 1)].data(), sta_names[size_t(a - 1)].size());
+        if (b > 0) std::memcpy(&CE[q][(size_t(r) * np + p) * 20], evt_names[size_t(b - 1)].data(), evt_names[size_t(b - 1)].size());
+      }
+    }
+  }
+  fwant_kerinfo_destroy(info);
+  nc3::Writer wr;
+  const int di = wr.add_dim("I", uint64_t(I)), dj = wr.add_dim("J", uint64_t(J)), dk = wr.add_dim("K", uint64_t(Kd));
+  const int ds = wr.add_dim("maxkstnm", 8), de = wr.add_dim("maxkevnm", 20), dn = wr.add_dim("N", 0);
+  static const char* const sfx[4] = {"ap", "aq", "bp", "bq"};
+  static const char* const thn[4] = {"threshold_Kap", "threshold_Kaq", "threshold_Kbp", "threshold_Kbq"};
+  for (int q = 0; q < 4; ++q) wr.add_gatt(thn[q], nc3::NC_FLOAT, {double(k0[q])});
+  for (int q = 0; q < 4; ++q) wr.add_var_f(std::string("S") + sfx[q], {dk, dj, di}, S.data() + q * np, np);
+  for (int q = 0; q < 4; ++q) wr.add_var_i(std::string("N") + sfx[q], {dk, dj, di}, N.data() + q * np, np);
+  for (int q = 0; q < 4; ++q) wr.add_var_i(std::string("M") + sfx[q], {dn, dk, dj, di}, M[q].data(), M[q].size());
+  for (int q = 0; q < 4; ++q)
+    wr.add_var_c(std::string("KSTNM") + sfx[q], {dn, dk, dj, di, ds}, CS[q].data(), CS[q].size());
+  for (int q = 0; q < 4; ++q)
+    wr.add_var_c(std::string("KEVNM") + sfx[q], {dn, dk, dj, di, de}, CE[q].data(), CE[q].size());
+  wr.set_numrecs(uint64_t(nrec));
+  const std::string out = pnm_info + "/kerinfo_" + seisfd::pad(kid, 3) + "_" + seisfd::MPI_SUFFIX + "_n00000.nc";
+  if (!wr.write(out, &err)) die(err);
+  std::printf("fwant_ker: %lld picks of %lld events, %d records into %s\n", picks, nevents, nrec, out.c_str());
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc >= 2 && std::strncmp(argv[1], "--nc-", 5) == 0) return nc_tool(argc, argv);
   std::string ker_conf;
@@ -440,10 +602,12 @@ int main(int argc, char** argv) {
   bool lamu = false;  // --lamu: the lambda/mu kernels of SI_ker_sta_lamu
   int conv = 0;       // --convert: 1 lamu2kamu, 2 lamu2vpvs, 3 vpvs2kamu
   bool eq = false;    // --eq: SI_ker_EQ's time shift of the Z-force SGT
+  bool info = false;  // --info: the kernel statistics of SI_ker2info
   for (int a = 1; a < argc; ++a) {
     const std::string s = argv[a];
     if (s == "--device" && a + 1 < argc) device = std::atoi(argv[++a]);
     else if (s == "--lamu") lamu = true;
+    else if (s == "--info") info = true;
     else if (s == "--eq") eq = true;
     else if (s == "--convert" && a + 1 < argc) {
       const std::string m = argv[++a];
@@ -452,7 +616,9 @@ int main(int argc, char** argv) {
     } else ker_conf = s;
   }
   if (conv && (lamu || eq)) die("--convert excludes --lamu and --eq");
+  if (info && (conv || lamu || eq)) die("--info excludes --convert, --lamu and --eq");
   if (ker_conf.empty()) ker_conf = conv ? "TomoKernel_conv.conf" : "TomoKernel.conf";
+  if (info) return run_info(ker_conf, device);
   // init_kernel (SI_ker_sta.F90:1047-1082)
   conf::File kc;
   std::string err;

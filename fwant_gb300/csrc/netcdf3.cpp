@@ -391,6 +391,30 @@ int Writer::add_var_f(const std::string& name, const std::vector<int>& dims, con
   return int(vars_.size()) - 1;
 }
 
+int Writer::add_var_i(const std::string& name, const std::vector<int>& dims, const int* data, size_t n) {
+  Var v;
+  v.name = name;
+  v.type = NC_INT;
+  v.dims = dims;
+  v.record = !dims.empty() && dims_[dims[0]].len == 0;
+  vars_.push_back(v);
+  std::vector<unsigned char> b;
+  b.reserve(n * 4);
+  for (size_t i = 0; i < n; ++i) put_be(b, uint32_t(data[i]), 4);
+  data_.push_back(std::move(b));
+  return int(vars_.size()) - 1;
+}
+int Writer::add_var_c(const std::string& name, const std::vector<int>& dims, const char* data, size_t n) {
+  Var v;
+  v.name = name;
+  v.type = NC_CHAR;
+  v.dims = dims;
+  v.record = !dims.empty() && dims_[dims[0]].len == 0;
+  vars_.push_back(v);
+  data_.emplace_back(reinterpret_cast<const unsigned char*>(data), reinterpret_cast<const unsigned char*>(data) + n);
+  return int(vars_.size()) - 1;
+}
+
 bool Writer::write(const std::string& path, std::string* err) const {
   // sizes: fixed variables whole, record variables one record slice
   std::vector<Var> vars = vars_;

@@ -80,6 +80,8 @@ class Writer {
   // data: elements in file order (for a record variable all records, numrecs of them)
   int add_var(const std::string& name, int type, const std::vector<int>& dims, const std::vector<double>& data);
   int add_var_f(const std::string& name, const std::vector<int>& dims, const float* data, size_t n);
+  int add_var_i(const std::string& name, const std::vector<int>& dims, const int* data, size_t n);
+  int add_var_c(const std::string& name, const std::vector<int>& dims, const char* data, size_t n);
   void set_numrecs(uint64_t n) { numrecs_ = n; }
   bool write(const std::string& path, std::string* err) const;
 
