@@ -39,16 +39,27 @@ sys.path.insert(0, ROOT)
 #   stage 2, 3: read W 9 + medium 3 + m 9 + t 9, write W' 9 + t 9  = 48 floats each
 #   stage 4: read W 9 + medium 3 + t 9, write W 9                  = 30 floats
 # Of the 156 values, 12 are the medium (always FP32) and 144 are wavefield registers,
-# which --storage bf16/fp16 holds in 2 bytes.
-FIELD_VALUES_PT_STEP, MEDIUM_VALUES_PT_STEP = 144, 12
-BYTES_PT_STEP = (FIELD_VALUES_PT_STEP + MEDIUM_VALUES_PT_STEP) * 4
+# which --storage bf16/fp16 holds in 2 bytes.  That is RK form 0 (fwant_set_rk_scheme), the
+# reference's registers.  Form 1, the default of the fast FP32 form, runs stages 1-3
+# without the accumulator t and forms it at stage 3:
+#   stage 1: read W 9 + medium 3, write W' 9                        = 21 floats
+#   stage 2: read W 9 + medium 3 + m 9, write W' 9                  = 30 floats
+#   stage 3: read W 9 + medium 3 + m 9 + W2 9, write W' 9 + t 9     = 48 floats
+#   stage 4: read W 9 + medium 3 + t 9, write W 9                   = 30 floats
+# 129 values, 117 of them wavefield registers.
+FIELD_VALUES_PT_STEP = {0: 144, 1: 117}
+MEDIUM_VALUES_PT_STEP = 12
 STORAGE_BYTES = {"fp32": 4, "bf16": 2, "fp16": 2}
 
 
-def bytes_pt_step(storage):
-    return FIELD_VALUES_PT_STEP * STORAGE_BYTES[storage] + MEDIUM_VALUES_PT_STEP * 4
-# CFS-PML memory variables, per slab point per step: 6 variables x (18+30+30+18) floats
-BYTES_PML_PT_STEP = 6 * 16 * 4
+def bytes_pt_step(storage, scheme=0):
+    return FIELD_VALUES_PT_STEP[scheme] * STORAGE_BYTES[storage] + MEDIUM_VALUES_PT_STEP * 4
+
+
+# CFS-PML memory variables, per slab point per step: 6 variables x (3+5+5+3) floats (form 0)
+# or x (2+3+5+3) floats (form 1)
+def bytes_pml_pt_step(scheme=0):
+    return 6 * (16 if scheme == 0 else 13) * 4
 
 
 def parse_args():
@@ -895,8 +906,9 @@ def run_ours(args, rank, world):
 
     # roofline of the stage kernel: one launch covers one stage of every simulation
     m0 = models[0]
-    algo_bytes_step = sum(bytes_pt_step(args.storage) * int(m.npoints) + BYTES_PML_PT_STEP * slab_points(m)
-                          for m in models)
+    scheme = sims[0].rk_scheme
+    algo_bytes_step = sum(bytes_pt_step(args.storage, scheme) * int(m.npoints) + bytes_pml_pt_step(scheme) *
+                          slab_points(m) for m in models)
     launch_ms = float(np.mean(stage_ms))
     achieved = algo_bytes_step / 4.0 / (launch_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
@@ -906,7 +918,7 @@ def run_ours(args, rank, world):
             "traffic_note": "bytes per stage (its interior-only and full launches): ncu DRAM/algorithmic "
                             "ratio (profiles/stage_batch_kernel_c2.md) x algorithmic bytes of the stage",
             "stage_ms": stage_ms, "step_end_ms": end_ms,
-            "algorithmic_bytes_per_stage": algo_bytes_step / 4.0}
+            "algorithmic_bytes_per_stage": algo_bytes_step / 4.0, "rk_scheme": scheme}
 
     out = {
         "metric": "grid-point updates per second", "value": value, "unit": "GPts/s", "n_gpus": world,

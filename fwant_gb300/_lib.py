@@ -93,6 +93,8 @@ EXPORTS = [
     ("fwant_set_lean_stages", C.c_int, [_vp, C.c_int]),
     ("fwant_check_wait_timeout", C.c_int, [_vp, C.c_int]),
     ("fwant_get_lean_stages", C.c_int, [_vp, _ip]),
+    ("fwant_set_rk_scheme", C.c_int, [_vp, C.c_int]),
+    ("fwant_get_rk_scheme", C.c_int, [_vp, _ip]),
     ("fwant_batch_create", C.c_int, [C.POINTER(_vp), C.c_int, C.POINTER(_vp)]),
     ("fwant_batch_destroy", None, [_vp]),
     ("fwant_batch_last_error", C.c_char_p, [_vp]),
@@ -481,6 +483,18 @@ class Solver:
     @lean_stages.setter
     def lean_stages(self, mask):
         self._chk(self._lib.fwant_set_lean_stages(self._h, int(mask)))
+
+    @property
+    def rk_scheme(self):
+        """1: the fast FP32 form runs stages 1-3 without t (t formed at stage 3), 0: t
+        carried as the reference does (always 0 where the form does not allow 1)."""
+        v = C.c_int()
+        self._chk(self._lib.fwant_get_rk_scheme(self._h, C.byref(v)))
+        return v.value
+
+    @rk_scheme.setter
+    def rk_scheme(self, scheme):
+        self._chk(self._lib.fwant_set_rk_scheme(self._h, int(scheme)))
 
     def set_storage_scale(self, velocity_scale, stress_scale):
         """Power-of-two scales of 2-byte storage (stored value = physical value * scale)."""

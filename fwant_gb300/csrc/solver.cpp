@@ -74,6 +74,7 @@ struct fwant_solver {
   float *d_rzinv = nullptr, *d_rsinv = nullptr;
   int kc = 8;                // planes per CTA of the stage kernel
   int tile_ty = fw::STAGE_TY;  // rows of the stage kernel's 32-column tile (fw::STAGE_TY or STAGE_TY_TALL)
+  int rk_scheme = 1;           // 1: stages 1-3 without t where the form allows it (RK kinds 3-5), 0: reference
   std::vector<float> hx, hy, hz, hxsin, hxcot;
   bool have_coord = false, have_metric = false, have_media = false;
 
@@ -111,7 +112,7 @@ struct fwant_solver {
   // on C2 (stage ms, full form -> split): beg 2.93 -> 2.66, fin 3.11 -> 3.08, inn 4.08 ->
   // 4.23 (the inn stage moves the most bytes and is DRAM-bound either way; the split only
   // adds a second launch and its tail).
-  int lean_mask = 5;
+  int lean_mask = -1;  // stages split into interior-only and full launches; -1: the form's default
   std::vector<int> h_items;
   std::vector<int> h_force_c, h_mom_c;  // 0-based source centres (item classification)
   // strain Green's tensor recording: sgt_ snapshot frames kept on the device
@@ -218,6 +219,10 @@ struct fwant_solver {
     if (const char* env = std::getenv("FWANT_PLANES_PER_CTA")) {  // tuning override
       const int v = std::atoi(env);
       if (v >= 1 && (nk + v - 1) / v <= 2047) kc = v;
+    }
+    if (const char* env = std::getenv("FWANT_RK_SCHEME")) {  // measurement override
+      const int v = std::atoi(env);
+      if (v == 0 || v == 1) rk_scheme = v;
     }
     if ((e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
     cudaEventCreate(&ev0);
@@ -750,7 +755,10 @@ struct fwant_solver {
   }
   // Items of one launch of RK kind rk: lean = 1 the interior items, lean = 0 the others,
   // or all items in launch order when the lean form is off for rk.
-  bool lean_on(int rk) const { return !topo_on && (lean_mask >> rk & 1) != 0; }
+  // Default split: stages 1 and 4 (mask 5); with the stages without t also stages 2 and 3
+  // (7: stage 2 then moves 30 floats per point and gains from the interior-only form).
+  int lean_stages() const { return lean_mask >= 0 ? lean_mask : (recon_on() ? 7 : 5); }
+  bool lean_on(int rk) const { return !topo_on && (lean_stages() >> fw::rk_base(rk) & 1) != 0; }
   const int* items(bool lean, int rk) const {
     if (!lean_on(rk)) return d_items + n_lean + n_full;
     return d_items + (lean ? 0 : n_lean);
@@ -777,6 +785,10 @@ struct fwant_solver {
     }
     a.pml_map = d_pml_map;
     a.pml_set[0] = in_of[s]; a.pml_set[1] = ra; a.pml_set[2] = rt;
+    if (s == 2 && recon_on()) {  // stage 3 reads W2 (register set rB, its output) as t-in
+      a.tm_t = tm_pt[rB];
+      a.pml_set[2] = rB;
+    }
     for (int f = 0; f < 6; ++f) {
       if (!slab[f].on) continue;
       a.ain[f] = aset(f, in_of[s]); a.am[f] = aset(f, ra); a.aout[f] = aset(f, out_of[s]); a.at[f] = aset(f, rt);
@@ -790,7 +802,13 @@ struct fwant_solver {
     const int X = CYCLE[cpos & 7];
     return (s % 2 == 0) ? X : (~X & 7);
   }
-  static int stage_rk(int s) { return s == 0 ? 0 : (s == 3 ? 2 : 1); }
+  // The classical RK4 step without carrying t through stages 1-3 (RK kinds 3, 4, 5, then
+  // RK_fin): the fast form with FP32 storage on a flat grid.
+  bool recon_on() const { return rk_scheme == 1 && !cfg.exact_arith && stor == fw::ST_F32 && !topo_on; }
+  int stage_rk(int s) const {
+    if (recon_on()) return s == 0 ? 3 : (s == 1 ? 4 : (s == 2 ? 5 : 2));
+    return s == 0 ? 0 : (s == 3 ? 2 : 1);
+  }
 
   // Step-end work of one simulation: receivers, step counter, SGT frame.
   fw::RecvArgs recv_args(int rt) const {
@@ -836,6 +854,7 @@ struct fwant_solver {
     put(&n_full, sizeof(n_full));
     put(&lean_mask, sizeof(lean_mask));
     put(&topo_on, sizeof(topo_on));
+    put(&rk_scheme, sizeof(rk_scheme));
   }
   void finish_step_host() {
     std::swap(rA, rT);
@@ -1890,7 +1909,7 @@ fwant_status fwant_check_wait_timeout(fwant_solver* s, int spins) {
 }
 
 fwant_status fwant_set_lean_stages(fwant_solver* s, int mask) {
-  if (!s || (mask & ~5) != 0) return FWANT_ERR_INVALID_ARG;
+  if (!s || (mask & ~7) != 0) return FWANT_ERR_INVALID_ARG;
   s->lean_mask = mask;
   s->drop_graphs();
   return FWANT_OK;
@@ -1898,7 +1917,20 @@ fwant_status fwant_set_lean_stages(fwant_solver* s, int mask) {
 
 fwant_status fwant_get_lean_stages(fwant_solver* s, int* mask) {
   if (!s || !mask) return FWANT_ERR_INVALID_ARG;
-  *mask = s->lean_mask;
+  *mask = s->lean_stages();
+  return FWANT_OK;
+}
+
+fwant_status fwant_set_rk_scheme(fwant_solver* s, int scheme) {
+  if (!s || (scheme != 0 && scheme != 1)) return FWANT_ERR_INVALID_ARG;
+  s->rk_scheme = scheme;  // t lives within a step only: switching between steps is safe
+  s->drop_graphs();
+  return FWANT_OK;
+}
+
+fwant_status fwant_get_rk_scheme(fwant_solver* s, int* scheme) {
+  if (!s || !scheme) return FWANT_ERR_INVALID_ARG;
+  *scheme = s->recon_on() ? 1 : 0;
   return FWANT_OK;
 }
 
@@ -1947,7 +1979,7 @@ struct fwant_batch {
   void batch_args(fw::BatchArgs& b, int first, int count, int ra, int s, bool lean) const {
     b.nsims = count;
     int off = 0;
-    const int rk = fwant_solver::stage_rk(s);
+    const int rk = sims[0]->stage_rk(s);
     for (int q = 0; q < count; ++q) {
       const fwant_solver* m = sims[first + q];
       b.sims[q] = m->stage_args(s, ra);
@@ -1974,7 +2006,7 @@ struct fwant_batch {
           if (b.total == 0) continue;
           const int nct = ctas > 0 ? std::min(b.total, ctas) : b.total;
           const int le = fw::launch_stage_batch(b, fwant_solver::stage_variant(s0->cycle_pos, s),
-                                                fwant_solver::stage_rk(s), s0->cfg.exact_arith, s0->stor, lean,
+                                                s0->stage_rk(s), s0->cfg.exact_arith, s0->stor, lean,
                                                 std::max(1, nct), st, s0->tile_ty);
           if (le && !lerr) lerr = le;
           ++nlaunch;
@@ -1994,6 +2026,7 @@ struct fwant_batch {
     for (fwant_solver* m : sims) {
       if (m->ntime != s0->ntime || m->cycle_pos != s0->cycle_pos || m->rA != s0->rA)
         return fail(FWANT_ERR_STATE, "batch members must be at the same time step");
+      if (m->rk_scheme != s0->rk_scheme) return fail(FWANT_ERR_STATE, "batch members must share the RK scheme");
       if (!m->have_coord || !m->have_metric || !m->have_media)
         return fail(FWANT_ERR_STATE, "coordinates, metric and media must be set for every member");
       fwant_status rc = m->prepare_sources(m->ntime + nsteps);
@@ -2235,10 +2268,11 @@ fwant_status fwant_batch_autotune(fwant_batch* b, int trial_steps, int* ctas_out
     if (t < best) { best = t; best_ctas = c; }
   }
   b->ctas = best_ctas;
-  // interior-only launches for stages 1 and 4 (mask 5), for one of them, or none: on small
-  // grids most items touch a boundary and the extra launches can cost more than they save
-  const int masks[] = {5, 1, 4, 0};
-  int best_mask = b->sims[0]->lean_mask;
+  // interior-only launches for every stage (7), for stages 1 and 4 (5), for one of them, or
+  // none: on small grids most items touch a boundary and the extra launches can cost more
+  // than they save
+  const int masks[] = {7, 5, 1, 4, 0};
+  int best_mask = b->sims[0]->lean_stages();
   double best_m = 1e30;
   for (int mk : masks) {
     for (fwant_solver* m : b->sims) {

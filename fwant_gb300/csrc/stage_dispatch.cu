@@ -16,6 +16,17 @@ namespace fw {
   int configure_stage_##mode##_rk2();
 FW_DECL(fast)
 FW_DECL(exact)
+// the stages of the fast FP32 form without t (RK kinds 3-5)
+#define FW_DECL_NOT(mode)                                                                   \
+  int launch_stage_batch_##mode##_rk3(const BatchArgs&, int, int, int, cudaStream_t);       \
+  int launch_stage_batch_##mode##_rk4(const BatchArgs&, int, int, int, cudaStream_t);       \
+  int launch_stage_batch_##mode##_rk5(const BatchArgs&, int, int, int, cudaStream_t);       \
+  int configure_stage_##mode##_rk3();                                                       \
+  int configure_stage_##mode##_rk4();                                                       \
+  int configure_stage_##mode##_rk5();
+FW_DECL_NOT(fast)
+FW_DECL_NOT(fast16)
+#undef FW_DECL_NOT
 FW_DECL(fast16)
 FW_DECL(exact16)
 FW_DECL(bf16)
@@ -46,6 +57,16 @@ int launch_stage_batch_topo(const BatchArgs& b, int variant, int rk, int exact, 
 int launch_stage_batch(const BatchArgs& b, int variant, int rk, int exact, int storage, int lean, int ctas,
                        void* stream, int ty) {
   cudaStream_t st = (cudaStream_t)stream;
+  if (rk >= 3) {  // fast FP32 form only
+    if (rk > 5 || exact || storage != ST_F32 || (ty != STAGE_TY && ty != STAGE_TY_TALL)) return int(cudaErrorInvalidValue);
+#define FW_RKN(mode)                                                                        \
+  return rk == 3 ? launch_stage_batch_##mode##_rk3(b, variant, lean, ctas, st)              \
+                 : (rk == 4 ? launch_stage_batch_##mode##_rk4(b, variant, lean, ctas, st)   \
+                            : launch_stage_batch_##mode##_rk5(b, variant, lean, ctas, st));
+    if (ty == STAGE_TY_TALL) { FW_RKN(fast16) }
+    FW_RKN(fast)
+#undef FW_RKN
+  }
 #define FW_RK(mode)                                                                         \
   return rk == 0 ? launch_stage_batch_##mode##_rk0(b, variant, lean, ctas, st)              \
                  : (rk == 1 ? launch_stage_batch_##mode##_rk1(b, variant, lean, ctas, st)   \
@@ -72,7 +93,9 @@ int stage_configure() {
                           configure_stage_fp16_rk0, configure_stage_fp16_rk1, configure_stage_fp16_rk2,
                           configure_stage_topo_rk0, configure_stage_topo_rk1, configure_stage_topo_rk2,
                           configure_stage_topo_exact_rk0, configure_stage_topo_exact_rk1,
-                          configure_stage_topo_exact_rk2};
+                          configure_stage_topo_exact_rk2,
+                          configure_stage_fast_rk3,   configure_stage_fast_rk4,   configure_stage_fast_rk5,
+                          configure_stage_fast16_rk3, configure_stage_fast16_rk4, configure_stage_fast16_rk5};
   for (auto fn : fns)
     if (int e = fn()) return e;
   return 0;

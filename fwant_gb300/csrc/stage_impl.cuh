@@ -102,7 +102,8 @@ struct Lay {
   __host__ __device__ static constexpr int pml_single_bytes(int rk) {
     return pml_slots(rk) * pml_single_roles(rk) * SZ_PML_PLANE;
   }
-  static int smem_bytes(bool lean, int rk) {
+  static int smem_bytes(bool lean, int rk_kind) {
+    const int rk = rk_base(rk_kind);  // the layout of the reference kind it follows
     return lean ? OFF_MT_L + (rk == 1 ? 2 * SZ_PT : (rk == 2 ? SZ_PT : 0)) + 64
                 : 2 * buf_full(rk) + pml_single_bytes(rk) + 64;
   }
@@ -294,10 +295,18 @@ __device__ __forceinline__ float surf_val(const Sources& S, const float* tab, in
 // surface (the host classifies the items); that code is compiled out, and the RK
 // registers m and t are read from global memory instead of being staged, so that the
 // lean form fits three CTAs per SM (registers and shared memory).
-template <class S, bool EXACT, int FX, int FY, int FZ, int RK, bool LEAN, bool TOPO, int TY>
+template <class S, bool EXACT, int FX, int FY, int FZ, int RKV, bool LEAN, bool TOPO, int TY>
 __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, int bz, unsigned char* smem) {
   static_assert(!EXACT || is_f32_v<S>, "the reference-order form exists for FP32 storage only");
   static_assert(!TOPO || (is_f32_v<S> && !LEAN), "the terrain form is FP32, full form");
+  static_assert(RKV <= 2 || (is_f32_v<S> && !EXACT && !TOPO), "the stages without t are fast FP32 flat forms");
+  // RK: the reference kind whose data movement this stage follows (kinds in kernels.h);
+  // NO_T: the stage neither reads nor writes t; RECON: stage 3 forming t from W2, W3, W4, m
+  // (A.tm_t / PML set pml_set[2] then hold W2, which the stage overwrites with W4, and
+  // A.wt / A.at receive t)
+  constexpr int RK = rk_base(RKV);
+  constexpr bool NO_T = RKV == 3 || RKV == 4;
+  constexpr bool RECON = RKV == 5;
   using L = Lay<S, TOPO, TY>;
   constexpr int TBY = L::TBY;
   constexpr int NQ = L::NQ;
@@ -351,8 +360,8 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
   // medium are in, while m and t are still arriving; they are waited for at the RK update.
   constexpr bool SPLIT = !LEAN && RK >= 1;
   constexpr uint32_t TX_BYTES = (LEAN ? 8 * L::SZ_PLANE : L::SZ_TILE) + L::SZ_Q + L::SZ_MED + L::SZ_TOPO;
-  constexpr uint32_t RKR_BYTES = SPLIT ? (RK == 1 ? 2 : 1) * L::SZ_PT : 0;
-  constexpr uint32_t MT_BYTES = L::template SZ_MT_L<RK>;  // lean: m and t of one plane
+  constexpr uint32_t RKR_BYTES = SPLIT ? (RK == 1 && !NO_T ? 2 : 1) * L::SZ_PT : 0;
+  constexpr uint32_t MT_BYTES = NO_T ? (RK == 1 ? L::SZ_PT : 0) : L::template SZ_MT_L<RK>;  // lean: m and t of one plane
 
   const uint32_t bar0 = smem_u32(smem + OFF_BAR);
   const uint32_t bar_mt = bar0 + 16;
@@ -440,7 +449,7 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
       const uint32_t brk = bar_rk(b);
       mbar_expect_tx(brk, RKR_BYTES);
       if (RK == 1) tma_load_4d_hint(base + OFF_M, &A.tm_m, i0 + PADL, j0, kp, 0, brk, pol_stream);
-      tma_load_4d_hint(base + OFF_T, &A.tm_t, i0 + PADL, j0, kp, 0, brk, pol_stream);
+      if (!NO_T) tma_load_4d_hint(base + OFF_T, &A.tm_t, i0 + PADL, j0, kp, 0, brk, pol_stream);
     }
   };
   if (tid == 0) issue(kb, 0);
@@ -450,7 +459,7 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
     fence_proxy_async();
     mbar_expect_tx(bar_mt, MT_BYTES);
     if (RK == 1) tma_load_4d_hint(base, &A.tm_m, i0 + PADL, j0, kp, 0, bar_mt, pol_stream);
-    tma_load_4d_hint(base + (RK == 1 ? L::SZ_PT : 0), &A.tm_t, i0 + PADL, j0, kp, 0, bar_mt, pol_stream);
+    if (!NO_T) tma_load_4d_hint(base + (RK == 1 ? L::SZ_PT : 0), &A.tm_t, i0 + PADL, j0, kp, 0, bar_mt, pol_stream);
   };
 
   // T*Src of this column (read on the top planes only)
@@ -579,7 +588,8 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
 #pragma unroll
       for (int v = 0; v < 6; ++v) {
         asm volatile("prefetch.global.L1 [%0];" ::"l"(A.ain[sidx] + qa + v * sl.vstride));
-        if (RK >= 1) asm volatile("prefetch.global.L1 [%0];" ::"l"(A.at[sidx] + qa + v * sl.vstride));
+        if (RK >= 1 && !NO_T)
+          asm volatile("prefetch.global.L1 [%0];" ::"l"((RECON ? A.aout[sidx] : A.at[sidx]) + qa + v * sl.vstride));
         if (RK == 1) asm volatile("prefetch.global.L1 [%0];" ::"l"(A.am[sidx] + qa + v * sl.vstride));
       }
     }
@@ -588,13 +598,14 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
 
   // m / t variables of plane kp into the single area (thread 0); bytes (all threads)
   auto issue_pml_mt = [&](int kp) -> uint32_t {
-    const uint32_t bytes = NROLE_S > 0 ? n_staged(kp) * uint32_t(NROLE_S * L::SZ_PML_PLANE) : 0u;
+    constexpr int NLOAD = NO_T ? (NROLE_S > 0 ? 1 : 0) : NROLE_S;  // roles loaded (no t: m only)
+    const uint32_t bytes = NLOAD > 0 ? n_staged(kp) * uint32_t(NLOAD * L::SZ_PML_PLANE) : 0u;
     if (bytes == 0 || tid != 0) return bytes;
     fence_proxy_async();
     mbar_expect_tx(bar_pml, bytes);
     const uint32_t base = smem_u32(smem + OFF_PS);
-    load_faces(base, NROLE_S, kp, A.pml_set[1], bar_pml);                              // m
-    load_faces(base + uint32_t(L::SZ_PML_PLANE), NROLE_S, kp, A.pml_set[2], bar_pml);  // t
+    load_faces(base, NROLE_S, kp, A.pml_set[1], bar_pml);  // m
+    if (!NO_T) load_faces(base + uint32_t(L::SZ_PML_PLANE), NROLE_S, kp, A.pml_set[2], bar_pml);  // t
     return bytes;
   };
   int pml_ph = 0;  // completed PML staging phases
@@ -937,7 +948,16 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
         for (int v = 0; v < 6 && ok_p; ++v) {
           if (RK == 0) {
             st_stream(ao + v * vs, av[v] + A.a * h[v], pol_stream);
-            st_stream(at + v * vs, av[v] + A.b * h[v], pol_stream);
+            if (!NO_T) st_stream(at + v * vs, av[v] + A.b * h[v], pol_stream);
+          } else if (RK == 1 && NO_T) {
+            const float mv = stg ? PS(0, v) : ld_stream(A.am[sidx] + qa + v * vs, pol_stream);
+            st_stream(ao + v * vs, mv + A.a * h[v], pol_stream);
+          } else if (RK == 1 && RECON) {  // t-in (W2) is the output register set: read first
+            const float mv = stg ? PS(0, v) : ld_stream(A.am[sidx] + qa + v * vs, pol_stream);
+            const float w2 = stg ? PS(1, v) : ld_rw_stream(ao + v * vs, pol_stream);
+            const float d = (w2 - mv) + 2.0f * (av[v] - mv) + A.a * h[v];  // increments, then m
+            st_stream(ao + v * vs, mv + A.a * h[v], pol_stream);
+            st_stream(at + v * vs, mv + d * (1.0f / 3.0f), pol_stream);
           } else if (RK == 1) {
             const float mv = stg ? PS(0, v) : ld_stream(A.am[sidx] + qa + v * vs, pol_stream);
             const float tv = stg ? PS(1, v) : ld_rw_stream(at + v * vs, pol_stream);
@@ -997,7 +1017,19 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
           const float m = (LEAN && f == TZZ) ? q[TZZ][TRAIL]
                           : dec((top && (f == TZZ || f == TXZ || f == TYZ)) ? W[o] : tl(f)[r0][c0], f);
           st_stream_s(Wout + o, enc(m + A.a * hh[f], f), pol_stream);
-          st_stream_s(Wt + o, enc(m + A.b * hh[f], f), pol_stream);
+          if (!NO_T) st_stream_s(Wt + o, enc(m + A.b * hh[f], f), pol_stream);
+        } else if (RK == 1 && NO_T) {
+          st_stream_s(Wout + o, enc(dec(mbuf[f][ty][tx], f) + A.a * hh[f], f), pol_stream);
+        } else if (RK == 1 && RECON) {
+          // W3 at the point as RK_beg reads its m (the surface's imaged stresses from memory)
+          const float w3 = (LEAN && f == TZZ) ? q[TZZ][TRAIL]
+                           : dec((top && (f == TZZ || f == TXZ || f == TYZ)) ? W[o] : tl(f)[r0][c0], f);
+          // t = m + (a1 h1 + 2 a2 h2 + a3 h3) / 3 from the increments W2 - m, W3 - m and a3 h3
+          // (added before m, so that t rounds once at the magnitude of m)
+          const float m = dec(mbuf[f][ty][tx], f), inc = A.a * hh[f];
+          const float d = (dec(tbuf[f][ty][tx], f) - m) + 2.0f * (w3 - m) + inc;
+          st_stream_s(Wout + o, enc(m + inc, f), pol_stream);
+          st_stream_s(Wt + o, enc(m + d * (1.0f / 3.0f), f), pol_stream);
         } else if (RK == 1) {
           st_stream_s(Wout + o, enc(dec(mbuf[f][ty][tx], f) + A.a * hh[f], f), pol_stream);
           st_stream_s(Wt + o, enc(dec(tbuf[f][ty][tx], f) + A.b * hh[f], f), pol_stream);

@@ -375,7 +375,8 @@ fwant_status fwant_get_planes_per_cta(fwant_solver* s, int* planes);
 fwant_status fwant_set_tile_rows(fwant_solver* s, int rows);
 fwant_status fwant_get_tile_rows(fwant_solver* s, int* rows);
 /* Which RK stages split their work items into an interior-only launch and a full launch
- * (bit 0: stage 1, bit 2: stage 4; default 5); 0 runs every stage as one full launch.
+ * (bit 0: stage 1, bit 1: stages 2 and 3, bit 2: stage 4; default 5, or 7 where the RK
+ * stages run without t, fwant_set_rk_scheme); 0 runs every stage as one full launch.
  * No counterpart in the reference (a tuning knob of the stage kernel, set by
  * fwant_batch_autotune). */
 fwant_status fwant_set_lean_stages(fwant_solver* s, int mask);
@@ -385,6 +386,17 @@ fwant_status fwant_set_lean_stages(fwant_solver* s, int mask);
  * FWANT_ERR_TIMEOUT and the solver stays usable.  No counterpart in the reference. */
 fwant_status fwant_check_wait_timeout(fwant_solver* s, int spins);
 fwant_status fwant_get_lean_stages(fwant_solver* s, int* mask);
+/* RK4 step form of the fast arithmetic: 1 (the default) runs stages 1-3 without the
+ * accumulator t, which stage 3 then forms from the stage values, t = m + ((W2 - m) +
+ * 2 (W3 - m) + a3 h3) / 3 (algebraically the reference's m + b1 h1 + b2 h2 + b3 h3,
+ * mod_macdrp.F90:291-393;
+ * the same results up to FP32 rounding, 129 instead of 156 floats moved per point and
+ * step); 0 carries t as the reference does.  Applies to FP32 storage on a flat grid in the
+ * fast form; the reference-order form, 2-byte storage and terrain-following grids always
+ * carry t (fwant_get_rk_scheme then reads 0).  May change between steps.  No counterpart
+ * in the reference. */
+fwant_status fwant_set_rk_scheme(fwant_solver* s, int scheme);
+fwant_status fwant_get_rk_scheme(fwant_solver* s, int* scheme);
 
 /* Autotuner: times every tile shape (32 x 8, and 32 x 16 where fwant_set_tile_rows allows
  * it) with every planes-per-CTA candidate (4 ... 128, up to nk) over trial_steps eager

@@ -132,17 +132,19 @@ def test_autotune_keeps_results(oracle_mod, native_lib):
 
 
 def test_lean_stage_split_keeps_results(oracle_mod, native_lib):
-    """Running every stage as one full launch (lean stages 0) instead of splitting stages 1
-    and 4 into interior-only and full launches moves work between kernels only: the same
-    fields bit for bit in the reference-order form.  Masks other than subsets of stages 1
-    and 4 are refused."""
+    """Running every stage as one full launch (lean stages 0), or splitting every stage
+    into interior-only and full launches (7), instead of splitting stages 1 and 4 (the
+    default 5) moves work between kernels only: the same fields bit for bit in the
+    reference-order form.  Masks beyond the three stage bits are refused."""
     import fwant_gb300 as fw
-    one, split = _members(oracle_mod, True)[0]
+    (one, split), (three, ref3) = _members(oracle_mod, True)[:2]
     assert split.lean_stages == 5
     one.lean_stages = 0
-    for s in (one, split):
+    three.lean_stages = 7
+    for s in (one, split, three, ref3):
         s.run(16)
     for c in range(9):
         np.testing.assert_array_equal(one.get_field(c), split.get_field(c))
+        np.testing.assert_array_equal(three.get_field(c), ref3.get_field(c))
     with pytest.raises(fw.FwantError):
-        one.lean_stages = 2
+        one.lean_stages = 8

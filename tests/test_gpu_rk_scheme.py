@@ -1,0 +1,116 @@
+"""RK step form 1 of the fast FP32 form (fwant_set_rk_scheme): stages 1-3 without the
+accumulator t, which stage 3 forms as m + ((W2 - m) + 2 (W3 - m) + a3 h3) / 3, against form 0 (t carried
+as the reference does, mod_macdrp.F90:291-393) and the FP32 oracle:
+
+* on every boundary path (free surface, buried and surface forces, moment tensor, six-face
+  PML, fluid layer) form 1 agrees with the FP32 oracle within 1e-5 relative L2 on fields
+  and seismograms, no further than form 0 does (within 3x, or 2e-6), and with form 0
+  within 1e-5;
+* form 1 with the tall tile, with interior-only launches for the RK_inn stages, batched,
+  and with the form changed between steps agrees with form 0 within 1e-5;
+* the forms that always carry t report 0: the reference-order form, 2-byte storage, a
+  terrain-following grid."""
+import numpy as np
+import pytest
+
+from helpers import feed, interior, rel_l2, small_model
+
+pytestmark = pytest.mark.gpu
+
+KINDS = ["surface", "buried", "nofree", "moment", "water"]
+
+
+def _solver(m, met, kind, scheme, rows=8, exact=False):
+    import fwant_gb300 as fw
+    s = fw.Solver(m.ni, m.nj, m.nk, m.stept, free_surface=m.free_surface, exact_arith=exact)
+    s.tile_rows = rows
+    s.rk_scheme = scheme
+    return feed(s, m, met, kind)
+
+
+def _close(a, b, tol, what):
+    for c in range(9):
+        x = interior(b.get_field(c))
+        if np.any(x):
+            r = rel_l2(interior(a.get_field(c)), x)
+            assert r < tol, (what, c, r)
+    assert rel_l2(a.get_seismo(), b.get_seismo()) < tol, what
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_form1_against_form0_and_the_oracle(kind, oracle_mod, native_lib):
+    m = small_model(kind, nj=30)
+    met = oracle_mod.metric(m.x, m.y, m.z)
+    s1 = _solver(m, met, kind, 1)
+    s0 = _solver(m, met, kind, 0)
+    assert s1.rk_scheme == 1 and s0.rk_scheme == 0
+    o = feed(oracle_mod.Oracle(m.ni, m.nj, m.nk, m.stept, free_surface=m.free_surface), m, met, kind)
+    for s in (s1, s0, o):
+        s.run(48)
+    _close(s1, s0, 1e-5, kind)
+    pairs = [(interior(s1.get_field(c)), interior(s0.get_field(c)), interior(o.get_field(c)).astype(np.float32))
+             for c in range(9)]
+    pairs.append((s1.get_seismo(), s0.get_seismo(), o.get_seismo().astype(np.float32)))
+    for n, (a1, a0, x) in enumerate(pairs):
+        if np.any(x):
+            r1, r0 = rel_l2(a1, x), rel_l2(a0, x)
+            assert r1 < 1e-5 and r1 < max(3.0 * r0, 2e-6), (kind, n, r1, r0)
+    s1.close()
+    s0.close()
+
+
+def test_form1_tall_tile_lean_inner_stages_and_batch(oracle_mod, native_lib):
+    import fwant_gb300 as fw
+    kinds = ("buried", "nofree", "moment")
+    models = [small_model(k, ni=70, nj=44, nk=36, seed=11) for k in kinds]
+    mets = [oracle_mod.metric(m.x, m.y, m.z) for m in models]
+    ref = [_solver(m, met, k, 0) for m, met, k in zip(models, mets, kinds)]
+    tall = [_solver(m, met, k, 1, rows=16) for m, met, k in zip(models, mets, kinds)]
+    lean = [_solver(m, met, k, 1) for m, met, k in zip(models, mets, kinds)]
+    for s in lean:
+        s.lean_stages = 7      # interior-only launches for the RK_inn stages too
+        assert s.lean_stages == 7
+    batched = [_solver(m, met, k, 1) for m, met, k in zip(models, mets, kinds)]
+    for s in ref + tall + lean:
+        s.run(40)
+    fw.Batch(batched).run(40)
+    for r, a, b, q in zip(ref, tall, lean, batched):
+        _close(a, r, 1e-5, "tall")
+        _close(b, r, 1e-5, "lean RK_inn")
+        _close(q, r, 1e-5, "batched")
+    for s in ref + tall + lean + batched:
+        s.close()
+
+
+def test_form_change_between_steps(oracle_mod, native_lib):
+    m = small_model("buried", nj=26)
+    met = oracle_mod.metric(m.x, m.y, m.z)
+    a = _solver(m, met, "buried", 1)
+    b = _solver(m, met, "buried", 0)
+    a.run(13)
+    a.rk_scheme = 0
+    a.run(11)
+    a.rk_scheme = 1
+    a.run(16)
+    b.run(40)
+    _close(a, b, 1e-5, "switched")
+    a.close()
+    b.close()
+
+
+def test_forms_that_carry_t(oracle_mod, native_lib):
+    import fwant_gb300 as fw
+    m = small_model("buried")
+    met = oracle_mod.metric(m.x, m.y, m.z)
+    ex = _solver(m, met, "buried", 1, exact=True)
+    assert ex.rk_scheme == 0
+    bf = fw.Solver(m.ni, m.nj, m.nk, m.stept, storage=fw.STORAGE_BF16)
+    bf.rk_scheme = 1
+    assert bf.rk_scheme == 0
+    tp = _solver(m, met, "buried", 1)
+    tp.set_topography(np.zeros((m.ni + 6, m.nj + 6), np.float32))
+    assert tp.rk_scheme == 0
+    with pytest.raises(fw.FwantError):
+        tp.rk_scheme = 2
+    for s in (ex, bf, tp):
+        s.close()
