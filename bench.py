@@ -195,13 +195,14 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic_ratio():
-    """Measured DRAM bytes over algorithmic bytes of the stage kernel, from the committed
-    ncu summary (captured on a smaller grid of the same kernel), or None."""
+def ncu_traffic_ratio(scheme=1):
+    """Measured DRAM bytes over algorithmic bytes of the stage kernel in RK form `scheme`,
+    from the committed ncu summary (captured on a smaller grid of the same kernel), or None."""
     path = os.path.join(ROOT, "profiles", "stage_batch_kernel_c2.md")
     if not os.path.exists(path):
         return None
-    m = re.search(r"dram_traffic_over_algorithmic:\s*([0-9.eE+-]+)", open(path).read())
+    key = "dram_traffic_over_algorithmic" if scheme == 1 else "dram_traffic_over_algorithmic_form0"
+    m = re.search(key + r":\s*([0-9.eE+-]+)", open(path).read())
     return float(m.group(1)) if m else None
 
 
@@ -912,7 +913,7 @@ def run_ours(args, rank, world):
     launch_ms = float(np.mean(stage_ms))
     achieved = algo_bytes_step / 4.0 / (launch_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
-    tr = ncu_traffic_ratio() if args.storage == "fp32" else None
+    tr = ncu_traffic_ratio(scheme) if args.storage == "fp32" else None
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "peak_source": peak_kind, "traffic": (tr * algo_bytes_step / 4.0) if tr else None,
             "traffic_note": "bytes per stage (its interior-only and full launches): ncu DRAM/algorithmic "
