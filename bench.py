@@ -920,6 +920,14 @@ def run_ours(args, rank, world):
                             "ratio (profiles/stage_batch_kernel_c2.md) x algorithmic bytes of the stage",
             "stage_ms": stage_ms, "step_end_ms": end_ms,
             "algorithmic_bytes_per_stage": algo_bytes_step / 4.0, "rk_scheme": scheme}
+    if scheme == 1:
+        # the same time against the bytes of RK form 0 (t carried, the reference's registers):
+        # how close the step comes to what the carried-t scheme could reach at the copy peak
+        ref_bytes_step = sum(bytes_pt_step(args.storage, 0) * int(m.npoints) + bytes_pml_pt_step(0) *
+                             slab_points(m) for m in models)
+        ach0 = ref_bytes_step / 4.0 / (launch_ms * 1e-3) / 1e9
+        roof["form0_equivalent"] = {"achieved": ach0, "frac": ach0 / peak, "unit": "GB/s",
+                                    "algorithmic_bytes_per_stage": ref_bytes_step / 4.0}
 
     out = {
         "metric": "grid-point updates per second", "value": value, "unit": "GPts/s", "n_gpus": world,

@@ -142,6 +142,7 @@ struct StageArgs {
   float a, b;     // rka*stept, rkb*stept
   int stage;      // 0..3 inside the step
   int kc;         // planes per CTA along k
+  int kz_lo, kz_hi;  // k-chunk boundaries (stage_chunk)
   const int* ntime;  // device step counter
   int* err;          // device error word (bounded-wait timeouts)
   Sources src;
@@ -205,11 +206,41 @@ void launch_topo_surface(const Geom& g, const float* metric, const float* lam, c
                          void* stream);
 // dh/dxi, dh/deta of the heights (FP64, the metric's stencil with clamped ends)
 void launch_topo_slopes(const Geom& g, const float* h, double* hxi, double* heta, void* stream);
+// k-chunks of the work items.  The planes split into three bands at kz_lo (the first plane
+// above the bottom PML slab, or k1) and kz_hi (the first plane of the free surface's band of
+// four, or of the top PML slab, or k2 + 1), so that no chunk straddles a band edge: the
+// chunks of the middle band then hold no slab or surface plane and can run in the
+// interior-only form.  A band of len planes is cut into ceil(len / kc) chunks of nearly
+// equal length (at most kc planes); chunk bz covers planes [kb, ke].
+__host__ __device__ inline int stage_chunk_count(const Geom& g, int kc, int kz_lo, int kz_hi) {
+  return (kz_lo - g.k1 + kc - 1) / kc + (kz_hi - kz_lo + kc - 1) / kc + (g.k2 + 1 - kz_hi + kc - 1) / kc;
+}
+__host__ __device__ inline void stage_chunk(const Geom& g, int kc, int kz_lo, int kz_hi, int bz, int* kb, int* ke) {
+  int base = g.k1, len = kz_lo - g.k1, c = bz;
+  int n = (len + kc - 1) / kc;
+  if (c >= n) {
+    c -= n;
+    base = kz_lo;
+    len = kz_hi - kz_lo;
+    n = (len + kc - 1) / kc;
+    if (c >= n) {
+      c -= n;
+      base = kz_hi;
+      len = g.k2 + 1 - kz_hi;
+      n = (len + kc - 1) / kc;
+    }
+  }
+  // n >= 1 here for every bz below stage_chunk_count
+  *kb = base + (c * len) / n;
+  *ke = base + ((c + 1) * len) / n - 1;
+}
+// The band edges kz_lo, kz_hi of a simulation (absolute plane indices).
+void stage_z_bands(const Geom& g, const Slab slab[6], int* kz_lo, int* kz_hi);
 // Work items of one simulation split into the lean (interior) list and the full list.
 // force_c / mom_c: 0-based source centres (3 per source).
-void stage_items(const Geom& g, int kc, int ty, const Slab slab[6], const int* force_c, int nforce, const int* mom_c,
-                 int nmom, int* lean, int* nlean, int* full, int* nfull);
-long long stage_item_count(const Geom& g, int kc, int ty = STAGE_TY);
+void stage_items(const Geom& g, int kc, int ty, int kz_lo, int kz_hi, const Slab slab[6], const int* force_c,
+                 int nforce, const int* mom_c, int nmom, int* lean, int* nlean, int* full, int* nfull);
+long long stage_item_count(const Geom& g, int kc, int ty, int kz_lo, int kz_hi);
 int stage_planes_per_cta(const Geom& g, int sm_count, int ty = STAGE_TY);
 int stage_configure();  // set the dynamic shared-memory attribute of every instantiation
 

@@ -45,6 +45,39 @@ T* dalloc(size_t n) {
   return (T*)p;
 }
 
+// A second stream on which a stage's full-form launch runs beside its interior-only launch:
+// the two cover disjoint work items (disjoint output points; both only read the stage
+// input), so they may overlap, which overlaps their tails and lets an SM hold CTAs of both
+// forms.  The side stream forks from the main stream before the stage's launches and joins
+// it after them, eagerly and inside a captured graph alike.
+struct FormFork {
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  bool on = true;
+  cudaError_t init() {
+    if (const char* env = std::getenv("FWANT_CONCURRENT_FORMS")) on = std::atoi(env) != 0;  // measurement override
+    cudaError_t e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join, cudaEventDisableTiming);
+    return e;
+  }
+  void destroy() {
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
+    if (side) cudaStreamDestroy(side);
+    fork = join = nullptr;
+    side = nullptr;
+  }
+  void begin(cudaStream_t main) {
+    cudaEventRecord(fork, main);
+    cudaStreamWaitEvent(side, fork, 0);
+  }
+  void end(cudaStream_t main) {
+    cudaEventRecord(join, side);
+    cudaStreamWaitEvent(main, join, 0);
+  }
+};
+
 }  // namespace
 
 struct fwant_solver {
@@ -52,6 +85,7 @@ struct fwant_solver {
   fw::Geom g{};
   float stept = 0.0f;
   cudaStream_t st = nullptr;
+  FormFork fork;  // side stream of the full-form launches
   std::string err;
 
   // four register sets of nine components each (W ping-pong, m, t; see run_step)
@@ -146,6 +180,7 @@ struct fwant_solver {
     cudaFree(d_h); cudaFree(d_hxi); cudaFree(d_heta); cudaFree(d_sk); cudaFree(d_rzf); cudaFree(d_topo); cudaFree(d_topo_sf);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
+    fork.destroy();
     if (st) cudaStreamDestroy(st);
   }
 
@@ -225,6 +260,7 @@ struct fwant_solver {
       if (v == 0 || v == 1) rk_scheme = v;
     }
     if ((e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
+    if ((e = fork.init()) != cudaSuccess) return cuda_fail(e, "side stream");
     cudaEventCreate(&ev0);
     cudaEventCreate(&ev1);
     const size_t nreg = size_t(4) * fw::NF * g.fstride;
@@ -714,6 +750,7 @@ struct fwant_solver {
       a.pb1[ax] = prof(ax, 0); a.pb11[ax] = prof(ax, 1); a.pad[ax] = prof(ax, 2); a.pD[ax] = prof(ax, 3);
     }
     a.kc = kc;
+    fw::stage_z_bands(g, slab, &a.kz_lo, &a.kz_hi);
     for (int f = 0; f < 6; ++f) a.slab[f] = slab[f];
     a.ntime = d_ntime;
     a.src = S;
@@ -727,19 +764,22 @@ struct fwant_solver {
   // Work-item lists of the stage launches for the current k-chunk, PML and sources
   // (rebuilt, and the graphs dropped, when they change).
   fwant_status ensure_items() {
-    const long long n = fw::stage_item_count(g, kc, tile_ty);
+    int kz_lo, kz_hi;
+    fw::stage_z_bands(g, slab, &kz_lo, &kz_hi);
+    const long long n = fw::stage_item_count(g, kc, tile_ty, kz_lo, kz_hi);
     std::vector<int> lean(static_cast<size_t>(n)), full(static_cast<size_t>(n));
     int nl = 0, nf = 0;
-    fw::stage_items(g, kc, tile_ty, slab, h_force_c.data(), int(h_force_c.size() / 3), h_mom_c.data(),
-                    int(h_mom_c.size() / 3), lean.data(), &nl, full.data(), &nf);
+    fw::stage_items(g, kc, tile_ty, kz_lo, kz_hi, slab, h_force_c.data(), int(h_force_c.size() / 3),
+                    h_mom_c.data(), int(h_mom_c.size() / 3), lean.data(), &nl, full.data(), &nf);
     // lean items, full items, then every item in launch order (x fastest, then y, k)
     std::vector<int> all(lean.begin(), lean.begin() + nl);
     all.insert(all.end(), full.begin(), full.begin() + nf);
     {
       const int nbx = (g.ni + fw::STAGE_TX - 1) / fw::STAGE_TX, nby = (g.nj + tile_ty - 1) / tile_ty;
-      for (int bz = 0; bz * kc < g.nk; ++bz)
+      const int nbz = fw::stage_chunk_count(g, kc, kz_lo, kz_hi);
+      for (int bz = 0; bz < nbz; ++bz)
         for (int by = 0; by < nby; ++by)
-          for (int bx = 0; bx < nbx; ++bx) all.push_back(bx | (by << 10) | (bz << 20));
+          for (int bx = 0; bx < nbx; ++bx) all.push_back(int(unsigned(bx) | unsigned(by) << 10 | unsigned(bz) << 20));
     }
     if (d_items && nl == n_lean && all == h_items) return FWANT_OK;
     cudaFree(d_items);
@@ -871,19 +911,24 @@ struct fwant_solver {
       if (ev) cudaEventRecord(ev[s], st);
       b.sims[0] = stage_args(s, rA);
       b.nsims = 1;
-      for (int lean = 1; lean >= 0; --lean) {
-        const int cnt = item_count(lean, stage_rk(s));
+      const int rk = stage_rk(s);
+      const bool both = fork.on && item_count(true, rk) > 0 && item_count(false, rk) > 0;
+      if (both) fork.begin(st);
+      for (int lean = 0; lean <= 1; ++lean) {  // the full form first, on the side stream
+        const int cnt = item_count(lean, rk);
         if (cnt == 0) continue;
-        b.items[0] = items(lean, stage_rk(s));
+        b.items[0] = items(lean, rk);
         b.off[0] = 0;
         b.off[1] = cnt;
         b.total = cnt;
-        const int le = topo_on ? fw::launch_stage_batch_topo(b, stage_variant(cycle_pos, s), stage_rk(s),
-                                                             cfg.exact_arith, cnt, st)
-                               : fw::launch_stage_batch(b, stage_variant(cycle_pos, s), stage_rk(s), cfg.exact_arith,
-                                                        stor, lean, cnt, st, tile_ty);
+        cudaStream_t ls = (both && !lean) ? fork.side : st;
+        const int le = topo_on ? fw::launch_stage_batch_topo(b, stage_variant(cycle_pos, s), rk, cfg.exact_arith,
+                                                             cnt, ls)
+                               : fw::launch_stage_batch(b, stage_variant(cycle_pos, s), rk, cfg.exact_arith, stor,
+                                                        lean, cnt, ls, tile_ty);
         if (le && !lerr) lerr = le;
       }
+      if (both) fork.end(st);
     }
     if (ev) cudaEventRecord(ev[4], st);
     enqueue_step_end(st);
@@ -1946,6 +1991,7 @@ struct fwant_batch {
   int ctas = 0;                              // persistent CTAs per launch (0: 2 per SM)
   int sm_count = 152;
   cudaStream_t st = nullptr;
+  FormFork fork;  // side stream of the full-form launches
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   std::vector<unsigned char> graph_sig;      // launch arguments the graphs were captured with
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -1958,6 +2004,7 @@ struct fwant_batch {
     drop_graphs();
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
+    fork.destroy();
     if (st) cudaStreamDestroy(st);
   }
   fwant_status fail(fwant_status c, const std::string& m) {
@@ -2001,16 +2048,22 @@ struct fwant_batch {
       if (ev) cudaEventRecord(ev[s], st);
       for (int first = 0; first < n(); first += fw::BATCH_PER_LAUNCH) {
         const int count = std::min(fw::BATCH_PER_LAUNCH, n() - first);
-        for (int lean = 1; lean >= 0; --lean) {
+        int cnt[2] = {0, 0};  // full, interior-only items of the group
+        for (int q = 0; q < count; ++q)
+          for (int lean = 0; lean <= 1; ++lean) cnt[lean] += sims[first + q]->item_count(lean != 0, s0->stage_rk(s));
+        const bool both = fork.on && cnt[0] > 0 && cnt[1] > 0;
+        if (both) fork.begin(st);
+        for (int lean = 0; lean <= 1; ++lean) {  // the full form first, on the side stream
           batch_args(b, first, count, s0->rA, s, lean != 0);
           if (b.total == 0) continue;
           const int nct = ctas > 0 ? std::min(b.total, ctas) : b.total;
           const int le = fw::launch_stage_batch(b, fwant_solver::stage_variant(s0->cycle_pos, s),
                                                 s0->stage_rk(s), s0->cfg.exact_arith, s0->stor, lean,
-                                                std::max(1, nct), st, s0->tile_ty);
+                                                std::max(1, nct), (both && !lean) ? fork.side : st, s0->tile_ty);
           if (le && !lerr) lerr = le;
           ++nlaunch;
         }
+        if (both) fork.end(st);
       }
     }
     if (ev) cudaEventRecord(ev[4], st);
@@ -2177,6 +2230,7 @@ fwant_status fwant_batch_create(fwant_solver* const* sims, int n, fwant_batch** 
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, b->device);
   if (nsm > 0) b->sm_count = nsm;
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = b->fork.init();
   if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
   if (e != cudaSuccess) {

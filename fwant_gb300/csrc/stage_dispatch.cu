@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "kernels.h"
 
@@ -101,17 +102,36 @@ int stage_configure() {
   return 0;
 }
 
-long long stage_item_count(const Geom& g, int kc, int ty) {
-  return (long long)((g.ni + STAGE_TX - 1) / STAGE_TX) * ((g.nj + ty - 1) / ty) * ((g.nk + kc - 1) / kc);
+long long stage_item_count(const Geom& g, int kc, int ty, int kz_lo, int kz_hi) {
+  return (long long)((g.ni + STAGE_TX - 1) / STAGE_TX) * ((g.nj + ty - 1) / ty) *
+         stage_chunk_count(g, kc, kz_lo, kz_hi);
+}
+
+void stage_z_bands(const Geom& g, const Slab slab[6], int* kz_lo, int* kz_hi) {
+  static const bool bands = [] {  // measurement override: FWANT_Z_BANDS=0 cuts the planes as one band
+    const char* env = std::getenv("FWANT_Z_BANDS");
+    return !(env && std::atoi(env) == 0);
+  }();
+  int lo = g.k1, hi = g.k2 + 1;
+  if (!bands) {
+    *kz_lo = lo;
+    *kz_hi = hi;
+    return;
+  }
+  if (slab[4].on) lo = std::min(std::max(slab[4].k2 + 1, g.k1), g.k2 + 1);
+  if (g.freesurf) hi = g.k2 - 3;
+  else if (slab[5].on) hi = slab[5].k1;
+  *kz_lo = lo;
+  *kz_hi = std::min(std::max(hi, lo), g.k2 + 1);
 }
 
 // An item is lean when none of its points lies in a PML slab, within reach (3 points) of
 // a smoothed source box, or within four planes of a free surface (images, VLOW rows,
 // T*Src): exactly the code the lean form compiles out.
-void stage_items(const Geom& g, int kc, int ty, const Slab slab[6], const int* force_c, int nforce, const int* mom_c,
-                 int nmom, int* lean, int* nlean, int* full, int* nfull) {
+void stage_items(const Geom& g, int kc, int ty, int kz_lo, int kz_hi, const Slab slab[6], const int* force_c,
+                 int nforce, const int* mom_c, int nmom, int* lean, int* nlean, int* full, int* nfull) {
   const int nbx = (g.ni + STAGE_TX - 1) / STAGE_TX, nby = (g.nj + ty - 1) / ty;
-  const int nbz = (g.nk + kc - 1) / kc;
+  const int nbz = stage_chunk_count(g, kc, kz_lo, kz_hi);
   auto overlap = [](int a0, int a1, int b0, int b1) { return a0 <= b1 && b0 <= a1; };
   int nl = 0, nf = 0;
   for (int bz = 0; bz < nbz; ++bz)
@@ -119,7 +139,8 @@ void stage_items(const Geom& g, int kc, int ty, const Slab slab[6], const int* f
       for (int bx = 0; bx < nbx; ++bx) {
         const int i0 = g.i1 + bx * STAGE_TX, i1 = std::min(i0 + STAGE_TX - 1, g.i2);
         const int j0 = g.j1 + by * ty, j1 = std::min(j0 + ty - 1, g.j2);
-        const int k0 = g.k1 + bz * kc, k1 = std::min(k0 + kc - 1, g.k2);
+        int k0, k1;
+        stage_chunk(g, kc, kz_lo, kz_hi, bz, &k0, &k1);
         bool is_lean = !(g.freesurf && k1 > g.k2 - 4);
         for (int f = 0; f < 6 && is_lean; ++f) {
           const Slab& s = slab[f];
@@ -136,7 +157,7 @@ void stage_items(const Geom& g, int kc, int ty, const Slab slab[6], const int* f
               overlap(j0, j1, mom_c[3 * n + 1] - 3, mom_c[3 * n + 1] + 3) &&
               overlap(k0, k1, mom_c[3 * n + 2] - 3, mom_c[3 * n + 2] + 3))
             is_lean = false;
-        const int packed = bx | (by << 10) | (bz << 20);
+        const int packed = int(unsigned(bx) | unsigned(by) << 10 | unsigned(bz) << 20);
         if (is_lean) lean[nl++] = packed;
         else full[nf++] = packed;
       }

@@ -327,9 +327,9 @@ __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, i
   const int i0 = g.i1 + bx * TX, j0 = g.j1 + by * TY;
   const int i = i0 + tx, j = j0 + ty;
   const bool act = i <= g.i2 && j <= g.j2;  // interior point owned by this thread
-  const int kb = g.k1 + bz * A.kc;
-  if (kb > g.k2) return true;
-  const int ke = min(kb + A.kc - 1, g.k2);
+  int kb, ke;
+  stage_chunk(g, A.kc, A.kz_lo, A.kz_hi, bz, &kb, &ke);
+  if (kb > ke) return true;
   const int px = g.px, plane = int(g.plane);
   const long long fs = g.fstride;
   const int col = (i + PADL) + px * j;
@@ -1082,7 +1082,7 @@ __global__ void __launch_bounds__(TX* TY, (LEAN ? 24 : 16) / TY > 0 ? (LEAN ? 24
     int s = 0;
     while (item >= B.off[s + 1]) ++s;
     const int packed = B.items[s][item - B.off[s]];
-    const int bx = packed & 1023, by = (packed >> 10) & 1023, bz = packed >> 20;
+    const int bx = packed & 1023, by = (packed >> 10) & 1023, bz = int(unsigned(packed) >> 20);
     if (!stage_body<S, EXACT, FX, FY, FZ, RK, LEAN, TOPO, TY>(B.sims[s], bx, by, bz, smem)) return;
     __syncthreads();  // the next item re-initialises the barriers and reuses the buffers
   }
