@@ -85,6 +85,11 @@ def parse_args():
     p.add_argument("--no-c3", action="store_true",
                    help="skip the C3 batched-vs-single comparison of the default (C2) line")
     p.add_argument("--c3-steps", type=int, default=16, help="timed steps of each C3 leg (multiple of 8)")
+    p.add_argument("--hill", action="store_true",
+                   help="--config c1: the seeded 2 km Gaussian hill on top (terrain-following grid, one solver)")
+    p.add_argument("--no-companions", action="store_true",
+                   help="skip the short runs of the other hot-path rows (C1, media, ker, assm, LSQR) that the "
+                        "default (C2) line carries under 'companions'")
     p.add_argument("--grid", default=None, help="override the C2 interior size, e.g. 200x200x100 (profiling)")
     p.add_argument("--sims", type=int, default=3, help="number of force components simulated (C2)")
     p.add_argument("--autotune", action="store_true",
@@ -819,6 +824,86 @@ def c3_batched_vs_single(dev, steps):
     }
 
 
+# The other rows of the hot path, each run briefly as its own process (own device memory,
+# own CUDA context) with the same flags a user would give it; the default C2 line carries
+# their measured figures so that every row has a number from the same run.
+COMPANIONS = (("c1", "c1", ["--steps", "2008", "--warmup", "8"]),
+              ("c1_hill", "c1", ["--steps", "2008", "--warmup", "8", "--hill"]),
+              ("media", "media", ["--steps", "3", "--warmup", "3"]),
+              ("ker", "ker", ["--steps", "3", "--warmup", "3"]),
+              ("assm", "assm", ["--steps", "5", "--warmup", "3"]),
+              ("lsqr", "lsqr", ["--steps", "20", "--warmup", "3"]))
+
+
+def companions():
+    import subprocess
+    out = {}
+    for name, cfg, extra in COMPANIONS:
+        t0 = time.perf_counter()
+        cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--config", cfg, "--no-cpu-baseline", "--no-e2e",
+               *extra]
+        r = subprocess.run(cmd, capture_output=True, text=True, env={k: v for k, v in os.environ.items()
+                                                                         if k not in ("RANK", "WORLD_SIZE")})
+        line = next((x for x in reversed(r.stdout.splitlines()) if x.startswith("{")), None)
+        if r.returncode != 0 or line is None:
+            out[name] = {"failed": (r.stderr or r.stdout)[-300:]}
+            continue
+        d = json.loads(line)
+        roof = d.get("roofline") or {}
+        out[name] = {"metric": d.get("metric"), "value": d.get("value"), "unit": d.get("unit"),
+                    "ms_per_step": d.get("ms_per_step"), "roofline_frac": roof.get("frac"),
+                    "roofline_bound": roof.get("bound"), "workload": (d.get("config") or {}).get("workload"),
+                    "flags": " ".join(extra), "wall_s": time.perf_counter() - t0}
+    return out
+
+
+def run_c1_hill(args, rank):
+    """C1 as specified: the 100x100x60 model with the seeded 2 km Gaussian hill on top (the
+    terrain-following extension, which steps one solver alone), 2008 steps by default.  Device
+    time of the time loop (8-step CUDA graphs), per-stage CUDA events."""
+    import fwant_gb300 as fw
+    from fwant_gb300 import inputs
+    if rank != 0:
+        return 0
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    m = inputs.config_c1(seed=0)
+    h = inputs.gaussian_hill(m, 2000.0, seed=0)
+    s = inputs.attach(fw.Solver(m.ni, m.nj, m.nk, m.stept, device=dev), m)
+    s.set_topography(h)
+    stage_ms, end_ms = s.profile_stages(8)
+    warm = max(args.warmup, 3)
+    s.run(warm)
+    clocks = Clocks(dev)
+    clocks.start()
+    s.run(args.steps)
+    dev_ms = s.last_run_ms()
+    clk = clocks.stop()
+    scheme = s.rk_scheme
+    s.check()
+    s.close()
+    npts = int(m.npoints)
+    # the terrain form also reads the plane's four metric values per point and stage
+    algo = (bytes_pt_step("fp32", scheme) + 4 * 4 * 4) * npts + bytes_pml_pt_step(scheme) * slab_points(m)
+    launch_ms = float(np.mean(stage_ms))
+    peak, peak_kind = peaks()
+    achieved = algo / 4.0 / (launch_ms * 1e-3) / 1e9
+    out = {
+        "metric": "grid-point updates per second", "value": npts * args.steps / (dev_ms * 1e-3) / 1e9,
+        "unit": "GPts/s", "n_gpus": 1, "steps": args.steps, "warmup": warm, "ms_per_step": dev_ms / args.steps,
+        "higher_is_better": True, "scaling": "replicas only", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "C1: 100x100x60 with a seeded 2 km Gaussian hill (terrain-following grid), FP32, "
+                               "12-cell CFS-PML x5, free surface, Fz Ricker 0.2 Hz, 16 receivers",
+                   "l2": "inputs smaller than L2 (the C1 size)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": None, "stage_ms": stage_ms, "step_end_ms": end_ms,
+                     "rk_scheme": scheme},
+        "clocks": clk, "gpu_launches": (4 + 1) * args.steps,
+    }
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_surrogate(args, rank):
     """Config 5: the surrogate's screening speedup over FD solves at 1% waveform error."""
     from fwant_gb300 import surrogate
@@ -845,6 +930,8 @@ def run_surrogate(args, rank):
 def run_ours(args, rank, world):
     import fwant_gb300 as fw
     from fwant_gb300 import inputs
+    if args.config == "c1" and args.hill:
+        return run_c1_hill(args, rank)
     if args.config == "c5":
         return run_surrogate(args, rank)
     if args.config == "lsqr":
@@ -986,6 +1073,8 @@ def run_ours(args, rank, world):
                       "wall_s": t_e2e, "includes": "solver creation, model upload, run, seismogram download"}
     if args.config == "c2" and not args.grid and not args.no_c3 and world == 1:
         out["batched_vs_single"] = c3_batched_vs_single(dev, max(8, args.c3_steps // 8 * 8))
+    if args.config == "c2" and not args.grid and not args.no_companions and world == 1:
+        out["companions"] = companions()
     if rank == 0 and not args.no_cpu_baseline:
         v, thr, dt = cpu_sample(models, args.cpu_steps)
         out["cpu_baseline"] = {"value": v, "unit": "GPts/s", "cores": thr, "kind": "port",

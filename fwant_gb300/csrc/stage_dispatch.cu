@@ -43,9 +43,21 @@ FW_DECL(fp16)
 FW_DECL_TOPO(topo)
 FW_DECL_TOPO(topo_exact)
 #undef FW_DECL_TOPO
+int launch_stage_batch_topo_rk3(const BatchArgs&, int, int, cudaStream_t);
+int launch_stage_batch_topo_rk4(const BatchArgs&, int, int, cudaStream_t);
+int launch_stage_batch_topo_rk5(const BatchArgs&, int, int, cudaStream_t);
+int configure_stage_topo_rk3();
+int configure_stage_topo_rk4();
+int configure_stage_topo_rk5();
 
 int launch_stage_batch_topo(const BatchArgs& b, int variant, int rk, int exact, int ctas, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
+  if (rk >= 3) {  // fast form only
+    if (rk > 5 || exact) return int(cudaErrorInvalidValue);
+    return rk == 3 ? launch_stage_batch_topo_rk3(b, variant, ctas, st)
+                   : (rk == 4 ? launch_stage_batch_topo_rk4(b, variant, ctas, st)
+                              : launch_stage_batch_topo_rk5(b, variant, ctas, st));
+  }
   if (exact)
     return rk == 0 ? launch_stage_batch_topo_exact_rk0(b, variant, ctas, st)
                    : (rk == 1 ? launch_stage_batch_topo_exact_rk1(b, variant, ctas, st)
@@ -96,7 +108,8 @@ int stage_configure() {
                           configure_stage_topo_exact_rk0, configure_stage_topo_exact_rk1,
                           configure_stage_topo_exact_rk2,
                           configure_stage_fast_rk3,   configure_stage_fast_rk4,   configure_stage_fast_rk5,
-                          configure_stage_fast16_rk3, configure_stage_fast16_rk4, configure_stage_fast16_rk5};
+                          configure_stage_fast16_rk3, configure_stage_fast16_rk4, configure_stage_fast16_rk5,
+                          configure_stage_topo_rk3,   configure_stage_topo_rk4,   configure_stage_topo_rk5};
   for (auto fn : fns)
     if (int e = fn()) return e;
   return 0;
