@@ -79,6 +79,9 @@ EXPORTS = [
                                       C.POINTER(C.c_double)]),
     ("fwant_sgtker_last_scatter_ms", C.c_int, [_vp, C.POINTER(C.c_double)]),
     ("fwant_sgtker_rotate", C.c_int, [_vp, C.POINTER(C.c_double)]),
+    ("fwant_sgtker_scatter_pair", C.c_int, [_vp]),
+    ("fwant_sgtker_kernel_pair", C.c_int, [_vp, _fp, _fp, C.c_int, C.c_int, C.c_float, C.c_int, C.c_int,
+                                           C.POINTER(C.c_double), C.POINTER(C.c_double), _fp, _fp, _fp, _fp]),
     ("fwant_sgtker_convert", C.c_int, [_vp, C.c_int, _fp, _fp, _fp, _fp]),
     ("fwant_sgtker_kernel_filtered", C.c_int, [_vp, C.c_int, _fp, _fp, C.c_int, C.c_int, C.c_double, C.c_int,
                                                C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
@@ -651,6 +654,28 @@ class SgtKernel:
         arrs = [np.array(np.asarray(x, np.float32).reshape(-1), np.float32) for x in (kap, kaq, kbp, kbq)]
         self._chk(self._lib.fwant_sgtker_convert(self._h, int(mode), *[_ptr(a) for a in arrs]))
         return tuple(arrs)
+
+    def scatter_pair(self):
+        """SI_ker_pair's single-precision scatter of the receiver SGT (slot 0) against the
+        source SGT (slot 3) over all frames."""
+        self._chk(self._lib.fwant_sgtker_scatter_pair(self._h))
+
+    def kernel_pair(self, v, u, nt1, nt2, sgt_m0, mode=0, b=None, a=None):
+        """SI_ker_pair's window kernel (FP32): filter mode 0 none, 1 one pass, 2
+        forward-backward; returns (Kap, Kaq, Kbp, Kbq) float32 [npts]."""
+        vv, uu = _f32(v, self.knt), _f32(u, self.knt)
+        nod1 = 0
+        bp = ap = None
+        if mode:
+            bb = np.ascontiguousarray(np.asarray(b, np.float64).reshape(-1))
+            aa = np.ascontiguousarray(np.asarray(a, np.float64).reshape(-1))
+            nod1 = bb.size
+            bp, ap = _ptr(bb, C.c_double), _ptr(aa, C.c_double)
+        outs = [np.zeros(self.npts, np.float32) for _ in range(4)]
+        self._chk(self._lib.fwant_sgtker_kernel_pair(self._h, _ptr(vv), _ptr(uu), int(nt1), int(nt2),
+                                                     float(sgt_m0), int(mode), int(nod1), bp, ap,
+                                                     *[_ptr(o) for o in outs]))
+        return tuple(outs)
 
     def last_scatter_ms(self):
         ms = C.c_double()

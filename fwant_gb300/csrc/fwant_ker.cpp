@@ -595,6 +595,228 @@ int run_info(const std::string& ker_conf, int device) {
   return 0;
 }
 
+// --pair: SI_ker_pair (code/srcF.kernel/SI_ker_pair.F90), the kernels of one source-receiver
+// pair.  TomoKernel.conf (init_kernel :542-602): MAIN_CONF, SGT_ROOT (the receiver's sgt_
+// series), SGT_M0, WAVE_ROOT (the source's sgt_ series), snap_id, block_size, fnm_syn (the
+// synthetic: knt, then T V U per line, init_synthetic :633-645), number_of_freqband,
+// number_of_measured and the <time_window> list (per measurement a line "band filter t1
+// t2", filter 1 one-pass, 2 forward-backward, 3 none, and a line with the output
+// directory), then the <filter_file> list.  Standard input: the rank id.  Per block the
+// strains of both series, the single-precision scatter (sgt2scatter :738-780) and per band,
+// filter and window the kernels (:322-357) into <directory>/kernel_NNN_mpi000000_n00000.nc
+// (kernel_phase_Vp kernel_amplitude_Vp kernel_phase_Vs kernel_amplitude_Vs over the
+// snapshot's I J K).  The debug exports of export_info (kernel.para.log and the filtered
+// synthetics) are not written.
+int run_pair(const std::string& ker_conf, int device) {
+  conf::File kc;
+  std::string err;
+  if (!kc.load(ker_conf, &err)) die(err);
+  auto kget = [&](const std::string& key, int col) {
+    std::string v;
+    if (!kc.get(key, col, &v)) die(ker_conf + ": key " + key + " column " + std::to_string(col) + " missing");
+    return v;
+  };
+  const std::string main_conf = kget("MAIN_CONF", 2), pnm_sgt = kget("SGT_ROOT", 2), pnm_wave = kget("WAVE_ROOT", 2);
+  const float sgt_m0 = to_f(kget("SGT_M0", 2), "SGT_M0");
+  const int kid = to_i(kget("snap_id", 2), "snap_id");
+  int blksiz[3];
+  for (int d = 0; d < 3; ++d) {
+    blksiz[d] = to_i(kget("block_size", d + 2), "block_size");
+    if (blksiz[d] == 0 || blksiz[d] < -1) die(ker_conf + ": block_size must be -1 or >= 1");
+  }
+  const std::string fnm_syn = kget("fnm_syn", 2);
+  const int num_freq = to_i(kget("number_of_freqband", 2), "number_of_freqband");
+  const int num_meas = to_i(kget("number_of_measured", 2), "number_of_measured");
+  // <time_window>: num_meas pairs of lines
+  struct Window {
+    int freq, filt;  // filt 1 P1, 2 P2, 3 none
+    float t1, t2;
+    std::string dir;
+    int nt1 = 0, nt2 = 0;
+  };
+  std::vector<Window> wins;
+  {
+    std::ifstream in(ker_conf);
+    std::string line;
+    bool found = false;
+    while (std::getline(in, line)) {
+      const auto w = words(line.substr(0, line.find('#')));
+      if (!w.empty() && w[0] == "<time_window>") { found = true; break; }
+    }
+    if (!found) die(ker_conf + ": <time_window> missing");
+    for (int q = 0; q < num_meas; ++q) {
+      std::vector<std::string> w;
+      while (w.empty()) {
+        if (!std::getline(in, line)) die(ker_conf + ": fewer time windows than number_of_measured");
+        w = words(line);
+      }
+      if (w.size() < 4) die(ker_conf + ": a time window needs band, filter, t1 and t2: " + line);
+      Window win;
+      win.freq = to_i(w[0], "band");
+      win.filt = to_i(w[1], "filter");
+      win.t1 = to_f(w[2], "t1");
+      win.t2 = to_f(w[3], "t2");
+      if (win.freq < 1 || win.freq > num_freq || win.filt < 1 || win.filt > 3)
+        die(ker_conf + ": band outside 1..number_of_freqband or filter outside 1..3: " + line);
+      if (!std::getline(in, line)) die(ker_conf + ": output directory of a time window missing");
+      win.dir = trim(line);
+      wins.push_back(win);
+    }
+  }
+  const std::vector<Filter> filters = read_filters(ker_conf, num_freq);
+  // the synthetic
+  std::vector<float> T, V, U;
+  int knt = 0;
+  {
+    std::ifstream f(fnm_syn);
+    if (!f) die("cannot open synthetic " + fnm_syn);
+    std::string line;
+    std::vector<std::string> w;
+    while (w.empty() && std::getline(f, line)) w = words(line);
+    if (w.empty()) die(fnm_syn + ": knt missing");
+    knt = to_i(w[0], fnm_syn);
+    if (knt < 2) die(fnm_syn + ": knt must be >= 2");
+    std::vector<std::string> vals;
+    while (int(vals.size()) < 3 * knt && std::getline(f, line))
+      for (const std::string& t : words(line)) vals.push_back(t);
+    if (int(vals.size()) < 3 * knt) die(fnm_syn + ": fewer than knt lines of T V U");
+    for (int n = 0; n < knt; ++n) {
+      T.push_back(to_f(vals[size_t(3 * n)], fnm_syn));
+      V.push_back(to_f(vals[size_t(3 * n + 1)], fnm_syn));
+      U.push_back(to_f(vals[size_t(3 * n + 2)], fnm_syn));
+    }
+  }
+  // twinlim2num (:647-665): the last T <= t1 and the first T >= t2
+  for (Window& w : wins) {
+    for (int n = 1; n <= knt; ++n)
+      if (T[size_t(n - 1)] <= w.t1 && (w.nt1 == 0 || T[size_t(n - 1)] > T[size_t(w.nt1 - 1)])) w.nt1 = n;
+    for (int n = 1; n <= knt; ++n)
+      if (T[size_t(n - 1)] >= w.t2 && (w.nt2 == 0 || T[size_t(n - 1)] < T[size_t(w.nt2 - 1)])) w.nt2 = n;
+    if (w.nt1 == 0 || w.nt2 == 0 || w.nt1 > w.nt2)
+      die(w.dir + ": time window outside the synthetic's time axis");
+    const Filter& F = filters[size_t(w.freq - 1)];
+    if (w.filt != 3 && F.nod1 < 2) die(w.dir + ": band without filter coefficients");
+  }
+  conf::File cf;
+  if (!cf.load(main_conf, &err)) die(err);
+  std::vector<seisfd::SnapDef> snaps;
+  double stept_d = 0.0;
+  std::string media_root;
+  try {
+    const int ni = seisfd::need_int(cf, "ni", 2), nj = seisfd::need_int(cf, "nj", 2), nk = seisfd::need_int(cf, "nk", 2);
+    if (cf.has("dims"))
+      for (int d = 0; d < 3; ++d)
+        if (seisfd::need_int(cf, "dims", d + 2) != 1) die("dims must be 1 1 1: one GPU holds the whole grid");
+    if (!cf.get_double("stept", 2, &stept_d)) throw std::runtime_error("key stept missing");
+    if (!cf.get("MEDIA_ROOT", 2, &media_root)) throw std::runtime_error("key MEDIA_ROOT missing");
+    snaps = seisfd::read_snaps(cf, ni, nj, nk);
+  } catch (const std::exception& e) {
+    die(main_conf + ": " + e.what());
+  }
+  std::printf(" input mpi id:\n");
+  {
+    std::vector<std::string> w;
+    std::string line;
+    while (w.size() < 3 && std::getline(std::cin, line))
+      for (const std::string& t : words(line)) w.push_back(t);
+    if (w.size() < 3) die("standard input: rank id (n_i n_j n_k) missing");
+    for (int d = 0; d < 3; ++d)
+      if (to_i(w[size_t(d)], "rank id") != 0) die("rank id must be 0 0 0: one rank holds the whole grid");
+  }
+  const seisfd::SnapDef* sp = nullptr;
+  for (const seisfd::SnapDef& q : snaps)
+    if (q.id == kid) sp = &q;
+  if (!sp) die(main_conf + ": snap_" + seisfd::pad(kid, 3) + " missing");
+  if (!sp->sgt) {  // kernode_if (:172)
+    std::printf("fwant_ker: snapshot series %d holds no stresses: nothing to do\n", kid);
+    return 0;
+  }
+  const float kdt = float(sp->tinv) * float(stept_d);
+  if (std::fabs((T[1] - T[0]) - kdt) > 1e-6f)
+    std::printf("fwant_ker: synthetic time step %g differs from the snapshot's %g\n", double(T[1] - T[0]), double(kdt));
+  static const char* const kname[4] = {"kernel_phase_Vp", "kernel_amplitude_Vp", "kernel_phase_Vs",
+                                       "kernel_amplitude_Vs"};
+  const std::string kfile = "/kernel_" + seisfd::pad(kid, 3) + "_" + seisfd::MPI_SUFFIX + "_n00000.nc";
+  {  // nfseis_grid3d_def of every measured window's file (:183-198)
+    const size_t n3 = size_t(sp->subc[0]) * sp->subc[1] * sp->subc[2];
+    const std::vector<float> zero(n3, 0.0f);
+    for (const Window& w : wins) {
+      nc3::Writer wr;
+      const int di = wr.add_dim("I", uint64_t(sp->subc[0])), dj = wr.add_dim("J", uint64_t(sp->subc[1])),
+                dk = wr.add_dim("K", uint64_t(sp->subc[2]));
+      wr.add_gatt_text("title", "Finite frequency kernel");
+      for (int q = 0; q < 4; ++q) wr.add_var_f(kname[q], {dk, dj, di}, zero.data(), n3);
+      if (!wr.write(w.dir + kfile, &err)) die(err);
+    }
+  }
+  int bsz[3], blknum[3];
+  for (int d = 0; d < 3; ++d) {
+    bsz[d] = blksiz[d] == -1 ? sp->subc[d] : std::min(blksiz[d], sp->subc[d]);
+    blknum[d] = (sp->subc[d] + bsz[d] - 1) / bsz[d];
+  }
+  const std::string media_path = media_root + "/media_" + seisfd::MPI_SUFFIX + ".nc";
+  nc3::Reader media;
+  if (!media.open(media_path, &err)) die(err);
+  fwant_sgtker* K = nullptr;
+  size_t k_npts = 0;
+  std::vector<float> lam, mu, stress, out[4];
+  long long written = 0;
+  for (int bk = 1; bk <= blknum[2]; ++bk)
+    for (int bj = 1; bj <= blknum[1]; ++bj)
+      for (int bi = 1; bi <= blknum[0]; ++bi) {
+        const int blk[3] = {bi, bj, bk};
+        Geometry g;
+        for (int d = 0; d < 3; ++d) {
+          g.bsubs[d] = (blk[d] - 1) * bsz[d] + 1;
+          g.bsubc[d] = std::min(bsz[d], sp->subc[d] - g.bsubs[d] + 1);
+          g.bsubt[d] = 1;
+          g.subs[d] = sp->subs[d] + (g.bsubs[d] - 1) * sp->subt[d];
+          g.subt[d] = sp->subt[d];
+        }
+        const size_t np = g.npts();
+        if (!K || k_npts != np) {
+          if (K) fwant_sgtker_destroy(K);
+          K = nullptr;
+          check(fwant_sgtker_create((long long)np, knt, double(kdt), device, &K), nullptr, "sgtker_create");
+          k_npts = np;
+        }
+        const std::vector<uint64_t> st = {uint64_t(g.subs[2] - 1), uint64_t(g.subs[1] - 1), uint64_t(g.subs[0] - 1)};
+        const std::vector<uint64_t> ct = {uint64_t(g.bsubc[2]), uint64_t(g.bsubc[1]), uint64_t(g.bsubc[0])};
+        const std::vector<uint64_t> sd = {uint64_t(g.subt[2]), uint64_t(g.subt[1]), uint64_t(g.subt[0])};
+        if (!media.read_slab("lambda", st, ct, sd, &lam, &err) || !media.read_slab("mu", st, ct, sd, &mu, &err))
+          die(media_path + ": " + err);
+        check(fwant_sgtker_set_media(K, lam.data(), mu.data()), K, "media");
+        read_sgt(pnm_sgt, *sp, g, knt, stress);  // the receiver (SGT_ROOT)
+        check(fwant_sgtker_set_sgt(K, 0, stress.data()), K, "receiver SGT");
+        read_sgt(pnm_wave, *sp, g, knt, stress);  // the source (WAVE_ROOT)
+        check(fwant_sgtker_set_sgt(K, 3, stress.data()), K, "source SGT");
+        check(fwant_sgtker_scatter_pair(K), K, "scatter_pair");
+        for (auto& o : out) o.assign(np, 0.0f);
+        const std::vector<uint64_t> kst = {uint64_t(g.bsubs[2] - 1), uint64_t(g.bsubs[1] - 1), uint64_t(g.bsubs[0] - 1)};
+        const std::vector<uint64_t> kct = {uint64_t(g.bsubc[2]), uint64_t(g.bsubc[1]), uint64_t(g.bsubc[0])};
+        const std::vector<uint64_t> ksd = {1, 1, 1};
+        // bands, filter types P1 P2 none, windows in the reference's order (:322-357)
+        for (int nfq = 1; nfq <= num_freq; ++nfq)
+          for (int npt = 1; npt <= 3; ++npt)
+            for (const Window& w : wins) {
+              if (w.freq != nfq || w.filt != npt) continue;
+              const Filter& F = filters[size_t(nfq - 1)];
+              const int mode = npt == 3 ? 0 : npt;
+              check(fwant_sgtker_kernel_pair(K, V.data(), U.data(), w.nt1, w.nt2, sgt_m0, mode,
+                                             mode ? F.nod1 : 0, mode ? F.b.data() : nullptr,
+                                             mode ? F.a.data() : nullptr, out[0].data(), out[1].data(),
+                                             out[2].data(), out[3].data()),
+                    K, "kernel_pair");
+              for (int q = 0; q < 4; ++q)
+                if (!nc3::update_slab(w.dir + kfile, kname[q], kst, kct, ksd, out[q].data(), &err)) die(err);
+              ++written;
+            }
+      }
+  if (K) fwant_sgtker_destroy(K);
+  std::printf("fwant_ker: %lld pair kernel blocks written\n", written);
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc >= 2 && std::strncmp(argv[1], "--nc-", 5) == 0) return nc_tool(argc, argv);
   std::string ker_conf;
@@ -603,11 +825,13 @@ int main(int argc, char** argv) {
   int conv = 0;       // --convert: 1 lamu2kamu, 2 lamu2vpvs, 3 vpvs2kamu
   bool eq = false;    // --eq: SI_ker_EQ's time shift of the Z-force SGT
   bool info = false;  // --info: the kernel statistics of SI_ker2info
+  bool pair = false;  // --pair: SI_ker_pair, one source-receiver pair
   for (int a = 1; a < argc; ++a) {
     const std::string s = argv[a];
     if (s == "--device" && a + 1 < argc) device = std::atoi(argv[++a]);
     else if (s == "--lamu") lamu = true;
     else if (s == "--info") info = true;
+    else if (s == "--pair") pair = true;
     else if (s == "--eq") eq = true;
     else if (s == "--convert" && a + 1 < argc) {
       const std::string m = argv[++a];
@@ -617,8 +841,10 @@ int main(int argc, char** argv) {
   }
   if (conv && (lamu || eq)) die("--convert excludes --lamu and --eq");
   if (info && (conv || lamu || eq)) die("--info excludes --convert, --lamu and --eq");
+  if (pair && (conv || lamu || eq || info)) die("--pair excludes --convert, --lamu, --eq and --info");
   if (ker_conf.empty()) ker_conf = conv ? "TomoKernel_conv.conf" : "TomoKernel.conf";
   if (info) return run_info(ker_conf, device);
+  if (pair) return run_pair(ker_conf, device);
   // init_kernel (SI_ker_sta.F90:1047-1082)
   conf::File kc;
   std::string err;

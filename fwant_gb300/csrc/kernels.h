@@ -318,9 +318,41 @@ struct KernelArgs {
   double* kap; double* kaq; double* kbp; double* kbq;  // [npts]
 };
 void launch_scatter_kernel(const KernelArgs& a, void* stream);
+// SI_ker_pair (SI_ker_pair.F90:710-780): the strains of one receiver SGT and of the source
+// SGT (stress2strain), then the single-precision scatter series of the pair over 1..knt
+// (sgt2scatter), every operation rounded in the reference's order:
+//   out[0] = Sa = x1 2 (lam + 2 mu), out[1] = Sb = 2 (x2 - x1) 2 mu   ([2][knt][npts], FP64
+//   holding the FP32 values); strain scratch [14][knt][npts] floats.
+struct PairArgs {
+  long long npts;
+  int knt;
+  float dt;
+  const float* lam;
+  const float* mu;
+  const float* rsgt;  // receiver SGT [6][knt][npts]
+  const float* ssgt;  // source SGT [6][knt][npts]
+  float* strain;      // scratch
+  double* out;
+};
+int launch_pair_scatter(const PairArgs& a, void* stream);
+// scatter2kernel of SI_ker_pair (:782-838) in single precision: the series rounded to FP32,
+// trapezoid sums V(n) Ka(n) dt in order, divided by v0 / u0.
+struct PairKernelArgs {
+  long long npts;
+  int nt1, nt2;
+  float dt, v0, u0;
+  const double* ka;  // [knt][npts]
+  const double* kb;
+  const float* v;    // [knt]
+  const float* u;
+  float* kap; float* kaq; float* kbp; float* kbq;
+};
+void launch_pair_kernel(const PairKernelArgs& a, void* stream);
 // IIR filtering of npts series of knt samples ([knt][npts] FP64) as scatter_filter (mode 1)
-// or scatter_filtfilt (mode 2) of SI_ker_sta.F90:1433-1558; nod1 coefficients b[], a[];
-// scratch holds (knt + 6 (nod1-1)) x npts doubles.
+// or scatter_filtfilt (mode 2) of SI_ker_sta.F90:1433-1558, or the forward-backward filter
+// of SI_ker_pair (mode 3: zero padding, (nod1 - 1) samples in front and 2 nod1 behind,
+// SI_ker_pair.F90:906-932); nod1 coefficients b[], a[]; scratch holds (knt + 6 (nod1-1))
+// x npts doubles (modes 1, 2) or (knt + 3 (nod1-1) + 2) x npts (mode 3).
 struct IirArgs {
   long long npts;
   int knt, mode, nod1;

@@ -155,10 +155,15 @@ __global__ void window_integral_kernel(const KernelArgs a) {
 __global__ void iir_kernel(const IirArgs A) {
   const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (p >= A.npts) return;
-  const int nod = A.nod1 - 1, nfact = 3 * nod, nt = A.knt, nel = nt + 2 * nfact;
+  const int nod = A.nod1 - 1, nt = A.knt;
+  // padding in front / behind: 3 nod reflected samples (modes 1, 2), or zeros: nod in
+  // front, 2 (nod + 1) behind (mode 3)
+  const int nfact = A.mode == 3 ? nod : 3 * nod;
+  const int nel = A.mode == 3 ? nt + 3 * nod + 2 : nt + 2 * nfact;
   const long long ld = A.npts;
   const double* in = A.in + p;
   auto x_at = [&](int n) -> double {  // 1-based padded input
+    if (A.mode == 3) return (n > nfact && n <= nfact + nt) ? in[(long long)(n - nfact - 1) * ld] : 0.0;
     if (n <= nfact) {
       if (A.mode == 1) return 0.0;
       return __dsub_rn(__dmul_rn(2.0, in[0]), in[(long long)(nfact + 1 - n) * ld]);
@@ -172,6 +177,12 @@ __global__ void iir_kernel(const IirArgs A) {
   double* scr = A.scratch + p;
   double* out = A.out + p;
   auto step = [&](double x, int n) -> double {
+    if (A.mode == 3 && n <= nod) {  // SI_ker_pair's filter sets y(1:NOD) = 0 (:924)
+      for (int m = nod - 1; m > 0; --m) { xs[m] = xs[m - 1]; ys[m] = ys[m - 1]; }
+      xs[0] = x;
+      ys[0] = 0.0;
+      return 0.0;
+    }
     double y = __dmul_rn(A.b[0], x);
     const int mm = min(nod + 1, n);
     for (int m = 2; m <= mm; ++m) y = __dsub_rn(__dadd_rn(y, __dmul_rn(A.b[m - 1], xs[m - 2])), __dmul_rn(A.a[m - 1], ys[m - 2]));
@@ -189,7 +200,7 @@ __global__ void iir_kernel(const IirArgs A) {
       scr[(long long)(n - 1) * ld] = y;
     }
   }
-  if (A.mode != 2) return;
+  if (A.mode == 1) return;
   for (int m = 0; m < IIR_MAX_COEF; ++m) xs[m] = ys[m] = 0.0;
   for (int m = 1; m <= nel; ++m) {
     const double y = step(scr[(long long)(nel - m) * ld], m);
@@ -250,7 +261,139 @@ __global__ void convert_kernel_kernel(int mode, long long n, const float* __rest
   }
 }
 
+// stress2strain of SI_ker_pair (:710-736, the same FP32 expressions as SI_ker_sta's) for
+// one (frame, point) of the receiver and the source SGT; stores per side the trace
+// (E11 + E22) + E33 and the six strains, the receiver's shear strains doubled
+// (2 E12R E12S in sgt2scatter is (2 E12R) E12S).  Layout [14][knt][npts].
+__global__ void pair_strain_kernel(const PairArgs a) {
+  const long long len = (long long)a.knt * a.npts;
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= len) return;
+  const long long p = e % a.npts;
+  const Compliance c = compliance(a.lam[p], a.mu[p]);
+  for (int side = 0; side < 2; ++side) {
+    const float* g = side == 0 ? a.rsgt : a.ssgt;
+    const float txx = g[e], tyy = g[e + len], tzz = g[e + 2 * len];
+    const float txy = g[e + 3 * len], txz = g[e + 4 * len], tyz = g[e + 5 * len];
+    const float e0 = __fmul_rn(c.e2, __fadd_rn(__fadd_rn(txx, tyy), tzz));
+    const float d = __fsub_rn(c.e2, c.e1);
+    const float h = __fmul_rn(0.5f, c.e3);
+    const float exx = __fsub_rn(e0, __fmul_rn(d, txx));
+    const float eyy = __fsub_rn(e0, __fmul_rn(d, tyy));
+    const float ezz = __fsub_rn(e0, __fmul_rn(d, tzz));
+    const float sh = side == 0 ? 2.0f : 1.0f;
+    float* o = a.strain + (long long)side * 7 * len + e;
+    o[0] = __fadd_rn(__fadd_rn(exx, eyy), ezz);
+    o[len] = exx;
+    o[2 * len] = eyy;
+    o[3 * len] = ezz;
+    o[4 * len] = __fmul_rn(sh, __fmul_rn(h, txy));
+    o[5 * len] = __fmul_rn(sh, __fmul_rn(h, txz));
+    o[6 * len] = __fmul_rn(sh, __fmul_rn(h, tyz));
+  }
+}
+
+// sgt2scatter of SI_ker_pair (:738-780): for every output n, in order of the lag m = 1 ..
+// n-1, x1 += (dt trR(m)) trS(n-m) and x2 += dt (E11R E11S + E22R E22S + E33R E33S +
+// 2E12R E12S + 2E13R E13S + 2E23R E23S), FP32 with each operation rounded.  One CTA per
+// point, one thread per output n; the receiver's lags and the source's window are staged
+// in shared memory chunk by chunk (lags ascend across chunks, so each thread's sums keep
+// the reference's order).
+constexpr int PS_THREADS = 256, PS_MCHUNK = 512;
+__global__ void __launch_bounds__(PS_THREADS) pair_scatter_kernel(const PairArgs a) {
+  extern __shared__ float psm[];
+  const long long p = blockIdx.x;
+  const int n_lo = 1 + blockIdx.y * PS_THREADS;
+  const int n_hi = min(a.knt, n_lo + PS_THREADS - 1);
+  const int n = n_lo + threadIdx.x;
+  const long long len = (long long)a.knt * a.npts;
+  constexpr int LDR = PS_MCHUNK, LDS = PS_THREADS + PS_MCHUNK;
+  float* R = psm;
+  float* Sw = psm + 7 * LDR;
+  const float* rs = a.strain;
+  const float* ss = a.strain + 7 * len;
+  float x1 = 0.0f, x2 = 0.0f;
+  for (int m0 = 1; m0 <= n_hi - 1; m0 += PS_MCHUNK) {
+    const int m1 = min(m0 + PS_MCHUNK, n_hi);  // exclusive
+    const int s_lo = max(1, n_lo - m1 + 1);
+    const int s_hi = n_hi - m0;
+    __syncthreads();
+    for (int m = m0 + threadIdx.x; m < m1; m += PS_THREADS)
+      for (int q = 0; q < 7; ++q) R[q * LDR + (m - m0)] = rs[q * len + (long long)(m - 1) * a.npts + p];
+    for (int t = s_lo + threadIdx.x; t <= s_hi; t += PS_THREADS)
+      for (int q = 0; q < 7; ++q) Sw[q * LDS + (t - s_lo)] = ss[q * len + (long long)(t - 1) * a.npts + p];
+    __syncthreads();
+    if (n <= n_hi) {
+      const int mend = min(m1, n);  // m < n
+      for (int m = m0; m < mend; ++m) {
+        const float* r = R + (m - m0);
+        const float* q = Sw + (n - m - s_lo);
+        x1 = __fadd_rn(x1, __fmul_rn(__fmul_rn(a.dt, r[0]), q[0]));
+        float sum = __fmul_rn(r[LDR], q[LDS]);
+        sum = __fadd_rn(sum, __fmul_rn(r[2 * LDR], q[2 * LDS]));
+        sum = __fadd_rn(sum, __fmul_rn(r[3 * LDR], q[3 * LDS]));
+        sum = __fadd_rn(sum, __fmul_rn(r[4 * LDR], q[4 * LDS]));
+        sum = __fadd_rn(sum, __fmul_rn(r[5 * LDR], q[5 * LDS]));
+        sum = __fadd_rn(sum, __fmul_rn(r[6 * LDR], q[6 * LDS]));
+        x2 = __fadd_rn(x2, __fmul_rn(a.dt, sum));
+      }
+    }
+  }
+  if (n > n_hi) return;
+  const float lam = a.lam[p], mu = a.mu[p];
+  const float sa = __fmul_rn(__fmul_rn(x1, 2.0f), __fadd_rn(lam, __fmul_rn(2.0f, mu)));
+  const float sb = __fmul_rn(__fmul_rn(__fmul_rn(2.0f, __fsub_rn(x2, x1)), 2.0f), mu);
+  const long long o = (long long)(n - 1) * a.npts + p;
+  a.out[o] = sa;
+  a.out[len + o] = sb;
+}
+
+// scatter2kernel of SI_ker_pair (:782-838), FP32, one thread per point.
+__global__ void pair_kernel_kernel(const PairKernelArgs a) {
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= a.npts) return;
+  const long long ld = a.npts;
+  auto ka = [&](int n) { return float(a.ka[(long long)(n - 1) * ld + p]); };
+  auto kb = [&](int n) { return float(a.kb[(long long)(n - 1) * ld + p]); };
+  const int n1 = a.nt1, n2 = a.nt2;
+  const float hdt = __fmul_rn(0.5f, a.dt);
+  const float v1 = a.v[n1 - 1], v2 = a.v[n2 - 1], u1 = a.u[n1 - 1], u2 = a.u[n2 - 1];
+  const float ka1 = ka(n1), ka2 = ka(n2), kb1 = kb(n1), kb2 = kb(n2);
+  float sap = __fmul_rn(hdt, __fadd_rn(__fmul_rn(v1, ka1), __fmul_rn(v2, ka2)));
+  float saq = __fmul_rn(hdt, __fadd_rn(__fmul_rn(u1, ka1), __fmul_rn(u2, ka2)));
+  float sbp = __fmul_rn(hdt, __fadd_rn(__fmul_rn(v1, kb1), __fmul_rn(v2, kb2)));
+  float sbq = __fmul_rn(hdt, __fadd_rn(__fmul_rn(u1, kb1), __fmul_rn(u2, kb2)));
+  for (int n = n1 + 1; n < n2; ++n) {
+    const float vn = a.v[n - 1], un = a.u[n - 1], an = ka(n), bn = kb(n);
+    sap = __fadd_rn(sap, __fmul_rn(__fmul_rn(vn, an), a.dt));
+    saq = __fadd_rn(saq, __fmul_rn(__fmul_rn(un, an), a.dt));
+    sbp = __fadd_rn(sbp, __fmul_rn(__fmul_rn(vn, bn), a.dt));
+    sbq = __fadd_rn(sbq, __fmul_rn(__fmul_rn(un, bn), a.dt));
+  }
+  a.kap[p] = __fdiv_rn(sap, a.v0);
+  a.kaq[p] = __fdiv_rn(saq, a.u0);
+  a.kbp[p] = __fdiv_rn(sbp, a.v0);
+  a.kbq[p] = __fdiv_rn(sbq, a.u0);
+}
+
 }  // namespace
+
+int launch_pair_scatter(const PairArgs& a, void* stream) {
+  if (a.npts <= 0 || a.knt <= 0) return 0;
+  const long long len = (long long)a.knt * a.npts;
+  pair_strain_kernel<<<(unsigned)((len + 255) / 256), 256, 0, (cudaStream_t)stream>>>(a);
+  const size_t smem = sizeof(float) * 7 * (PS_MCHUNK + PS_THREADS + PS_MCHUNK);
+  cudaError_t e = cudaFuncSetAttribute(pair_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e != cudaSuccess) return int(e);
+  dim3 grid((unsigned)a.npts, (unsigned)((a.knt + PS_THREADS - 1) / PS_THREADS));
+  pair_scatter_kernel<<<grid, PS_THREADS, smem, (cudaStream_t)stream>>>(a);
+  return int(cudaGetLastError());
+}
+
+void launch_pair_kernel(const PairKernelArgs& a, void* stream) {
+  if (a.npts <= 0) return;
+  pair_kernel_kernel<<<(unsigned)((a.npts + 255) / 256), 256, 0, (cudaStream_t)stream>>>(a);
+}
 
 void launch_iir(const IirArgs& a, void* stream) {
   iir_kernel<<<(unsigned)((a.npts + 127) / 128), 128, 0, (cudaStream_t)stream>>>(a);

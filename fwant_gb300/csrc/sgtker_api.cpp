@@ -35,6 +35,9 @@ struct fwant_sgtker {
   double* filtered = nullptr;                            // 2 x [knt][npts]: filtered Ka, Kb
   double* iir_scratch = nullptr;                         // [knt + 6 nod][npts]
   size_t iir_scratch_len = 0;
+  float* pstrain = nullptr;                              // SI_ker_pair strains [14][knt][npts]
+  float* pvu = nullptr;                                  // SI_ker_pair V, U [2][knt]
+  bool pair_done = false;                                // series slots 0, 1 hold the pair's Sa, Sb
   bool have_media = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;
@@ -45,6 +48,7 @@ struct fwant_sgtker {
     cudaFree(lam); cudaFree(mu);
     for (float* p : sgt) cudaFree(p);
     cudaFree(series); cudaFree(wts); cudaFree(kout); cudaFree(filtered); cudaFree(iir_scratch);
+    cudaFree(pstrain); cudaFree(pvu);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (st) cudaStreamDestroy(st);
@@ -233,7 +237,153 @@ std::vector<double> host_iir(const float* w0, int nt, int mode, int nod1, const 
   }
   return std::vector<double>(y.begin() + nfact + 1, y.begin() + nfact + 1 + nt);
 }
+
+// syn_filter / syn_filtfilt of SI_ker_pair (SI_ker_pair.F90:882-932): the series between
+// zero padding (NOD samples in front, 2 (NOD + 1) behind), each pass with y(1:NOD) = 0, in
+// FP64; the result rounded to FP32.
+std::vector<float> host_pair_filter(const float* w0, int nt, int mode, int nod1, const double* b, const double* a) {
+  const int nod = nod1 - 1, nel = nt + 3 * nod + 2;
+  std::vector<double> x(nel + 1, 0.0), y(nel + 1, 0.0), w(nel + 1, 0.0);
+  for (int n = 1; n <= nt; ++n) x[nod + n] = w0[n - 1];
+  auto filter = [&](const std::vector<double>& in, std::vector<double>& out) {
+    for (int n = 1; n <= nod; ++n) out[n] = 0.0;
+    for (int n = nod + 1; n <= nel; ++n) {
+      double yy = b[0] * in[n];
+      for (int m = 2; m <= nod + 1; ++m) yy = (yy + b[m - 1] * in[n - m + 1]) - a[m - 1] * out[n - m + 1];
+      out[n] = yy / a[0];
+    }
+  };
+  filter(x, y);
+  if (mode == 2) {
+    for (int n = 1; n <= nel; ++n) w[n] = y[nel + 1 - n];
+    filter(w, x);
+    for (int n = 1; n <= nel; ++n) y[n] = x[nel + 1 - n];
+  }
+  std::vector<float> out(static_cast<size_t>(nt));
+  for (int n = 1; n <= nt; ++n) out[size_t(n - 1)] = float(y[nod + n]);
+  return out;
+}
 }  // namespace
+
+fwant_status fwant_sgtker_scatter_pair(fwant_sgtker* k) {
+  if (!k) return FWANT_ERR_INVALID_ARG;
+  if (!k->have_media) return k->fail(FWANT_ERR_STATE, "sgtker_scatter_pair: media not set");
+  if (!k->sgt[0] || !k->sgt[3])
+    return k->fail(FWANT_ERR_STATE, "sgtker_scatter_pair: the receiver SGT (slot 0) and the source SGT (slot 3) are needed");
+  cudaSetDevice(k->device);
+  fwant_status rc = k->alloc(&k->series, 6 * k->series_len(), "scatter series");
+  if (rc == FWANT_OK) rc = k->alloc(&k->pstrain, 14 * k->series_len(), "pair strains");
+  if (rc != FWANT_OK) return rc;
+  fw::PairArgs pa{};
+  pa.npts = k->npts;
+  pa.knt = k->knt;
+  pa.dt = float(k->kdt);
+  pa.lam = k->lam;
+  pa.mu = k->mu;
+  pa.rsgt = k->sgt[0];
+  pa.ssgt = k->sgt[3];
+  pa.strain = k->pstrain;
+  pa.out = k->series;
+  cudaError_t e = cudaEventRecord(k->ev0, k->st);
+  if (e == cudaSuccess) e = cudaError_t(fw::launch_pair_scatter(pa, k->st));
+  if (e == cudaSuccess) e = cudaEventRecord(k->ev1, k->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(k->st);
+  float ms = 0.0f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, k->ev0, k->ev1);
+  if (e != cudaSuccess) return k->cuda_fail(e, "sgtker_scatter_pair");
+  k->last_ms = ms;
+  k->scatter_flags = 0;  // the series now hold the pair's Sa, Sb
+  k->pair_done = true;
+  return FWANT_OK;
+}
+
+fwant_status fwant_sgtker_kernel_pair(fwant_sgtker* k, const float* v, const float* u, int nt1, int nt2, float sgt_m0,
+                                      int mode, int nod1, const double* b, const double* a, float* kap, float* kaq,
+                                      float* kbp, float* kbq) {
+  if (!k || !v || !u || !kap || !kaq || !kbp || !kbq) return FWANT_ERR_INVALID_ARG;
+  if (mode < 0 || mode > 2) return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_kernel_pair: filter mode must be 0, 1 or 2");
+  if (mode != 0 && (!b || !a || nod1 < 2 || nod1 > fw::IIR_MAX_COEF || !(a[0] != 0.0)))
+    return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_kernel_pair: filter needs 2..16 coefficients with a[0] != 0");
+  if (!k->pair_done) return k->fail(FWANT_ERR_STATE, "sgtker_kernel_pair: fwant_sgtker_scatter_pair first");
+  if (nt1 < 1 || nt2 > k->knt || nt1 > nt2)
+    return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_kernel_pair: window outside 1..knt");
+  const double* ser_a = k->series;
+  const double* ser_b = k->series + k->series_len();
+  std::vector<float> vf(v, v + k->knt), uf(u, u + k->knt);
+  cudaSetDevice(k->device);
+  if (mode != 0) {  // syn_filter(filtfilt) of V, U on the host; scatter_filter(filtfilt) on the device
+    vf = host_pair_filter(v, k->knt, mode, nod1, b, a);
+    uf = host_pair_filter(u, k->knt, mode, nod1, b, a);
+    const size_t nel = size_t(k->knt) + 3 * size_t(nod1 - 1) + 2;
+    fwant_status rc = k->alloc(&k->filtered, 2 * k->series_len(), "filtered series");
+    if (rc != FWANT_OK) return rc;
+    if (k->iir_scratch_len < nel * size_t(k->npts)) {
+      cudaFree(k->iir_scratch);
+      k->iir_scratch = nullptr;
+      k->iir_scratch_len = 0;
+      if ((rc = k->alloc(&k->iir_scratch, nel * size_t(k->npts), "filter scratch")) != FWANT_OK) return rc;
+      k->iir_scratch_len = nel * size_t(k->npts);
+    }
+    fw::IirArgs ia{};
+    ia.npts = k->npts;
+    ia.knt = k->knt;
+    ia.mode = mode == 1 ? 1 : 3;
+    ia.nod1 = nod1;
+    for (int q = 0; q < nod1; ++q) { ia.b[q] = b[q]; ia.a[q] = a[q]; }
+    ia.scratch = k->iir_scratch;
+    for (int s = 0; s < 2; ++s) {
+      ia.in = s == 0 ? ser_a : ser_b;
+      ia.out = k->filtered + size_t(s) * k->series_len();
+      fw::launch_iir(ia, k->st);
+    }
+    ser_a = k->filtered;
+    ser_b = k->filtered + k->series_len();
+  }
+  // normalisation (SI_ker_pair.F90:802-808), FP32 in the reference's order
+  const float dt = float(k->kdt);
+  float v0 = (0.5f * (vf[size_t(nt1 - 1)] * vf[size_t(nt1 - 1)]) + 0.5f * (vf[size_t(nt2 - 1)] * vf[size_t(nt2 - 1)])) * dt;
+  float u0 = (0.5f * (uf[size_t(nt1 - 1)] * uf[size_t(nt1 - 1)]) + 0.5f * (uf[size_t(nt2 - 1)] * uf[size_t(nt2 - 1)])) * dt;
+  for (int n = nt1 + 1; n <= nt2 - 1; ++n) {
+    v0 = v0 + (vf[size_t(n - 1)] * vf[size_t(n - 1)]) * dt;
+    u0 = u0 + (uf[size_t(n - 1)] * uf[size_t(n - 1)]) * dt;
+  }
+  v0 = v0 * sgt_m0;
+  u0 = u0 * sgt_m0;
+  if (!(v0 != 0.0f) || !(u0 != 0.0f)) return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_kernel_pair: zero normalisation");
+  fwant_status rc = k->alloc(&k->pvu, 2 * size_t(k->knt), "pair synthetics");
+  if (rc == FWANT_OK) rc = k->alloc(&k->kout, 4 * size_t(k->npts), "kernels");
+  if (rc != FWANT_OK) return rc;
+  cudaError_t e = cudaMemcpyAsync(k->pvu, vf.data(), size_t(k->knt) * sizeof(float), cudaMemcpyHostToDevice, k->st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(k->pvu + k->knt, uf.data(), size_t(k->knt) * sizeof(float), cudaMemcpyHostToDevice, k->st);
+  float* ko = reinterpret_cast<float*>(k->kout);
+  const size_t np = size_t(k->npts);
+  fw::PairKernelArgs pk{};
+  pk.npts = k->npts;
+  pk.nt1 = nt1;
+  pk.nt2 = nt2;
+  pk.dt = dt;
+  pk.v0 = v0;
+  pk.u0 = u0;
+  pk.ka = ser_a;
+  pk.kb = ser_b;
+  pk.v = k->pvu;
+  pk.u = k->pvu + k->knt;
+  pk.kap = ko;
+  pk.kaq = ko + np;
+  pk.kbp = ko + 2 * np;
+  pk.kbq = ko + 3 * np;
+  if (e == cudaSuccess) {
+    fw::launch_pair_kernel(pk, k->st);
+    e = cudaGetLastError();
+  }
+  float* const host[4] = {kap, kaq, kbp, kbq};
+  for (int q = 0; q < 4 && e == cudaSuccess; ++q)
+    e = cudaMemcpyAsync(host[q], ko + q * np, np * sizeof(float), cudaMemcpyDeviceToHost, k->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(k->st);
+  if (e != cudaSuccess) return k->cuda_fail(e, "sgtker_kernel_pair");
+  return FWANT_OK;
+}
 
 fwant_status fwant_sgtker_rotate(fwant_sgtker* k, const double rot[9]) {
   if (!k || !rot) return FWANT_ERR_INVALID_ARG;

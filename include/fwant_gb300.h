@@ -335,6 +335,20 @@ fwant_status fwant_sgtker_kernel_filtered(fwant_sgtker* k, int ncmp, const float
  *   mode 2 lambda/mu -> Vp/Vs     SI_ker_lamu2vpvs (code/srcF.kernel/SI_ker_lamu2vpvs.F90:823-830)
  *   mode 3 Vp/Vs -> kappa/mu      SI_ker_vpvs2kamu (code/srcF.kernel/SI_ker_vpvs2kamu.F90:823-831) */
 fwant_status fwant_sgtker_convert(fwant_sgtker* k, int mode, float* kap, float* kaq, float* kbp, float* kbq);
+/* SI_ker_pair (code/srcF.kernel/SI_ker_pair.F90), the single source-receiver pair: the
+ * scattering series of the receiver SGT (fwant_sgtker_set_sgt slot 0) against the source
+ * SGT (slot 3) over all knt frames, stress2strain and sgt2scatter (:710-780) in single
+ * precision with every operation rounded in the reference's order (Sa = x1 2 (lam + 2 mu),
+ * Sb = 2 (x2 - x1) 2 mu).  Replaces the series of fwant_sgtker_scatter. */
+fwant_status fwant_sgtker_scatter_pair(fwant_sgtker* k);
+/* The pair's window kernel (scatter2kernel :782-838, FP32) over frames nt1..nt2 (1-based)
+ * with the synthetics v, u (knt values), after the pair program's filter of the band (mode
+ * 0 none, 1 one pass, 2 forward-backward with zero padding, :840-932; nod1 coefficients b,
+ * a in FP64) applied to the series and the synthetics; kap kaq kbp kbq receive npts
+ * values each. */
+fwant_status fwant_sgtker_kernel_pair(fwant_sgtker* k, const float* v, const float* u, int nt1, int nt2, float sgt_m0,
+                                      int mode, int nod1, const double* b, const double* a, float* kap, float* kaq,
+                                      float* kbp, float* kbq);
 /* Device time of the last fwant_sgtker_scatter in milliseconds.  No counterpart in the
  * reference. */
 fwant_status fwant_sgtker_last_scatter_ms(fwant_sgtker* k, double* ms);

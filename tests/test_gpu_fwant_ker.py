@@ -435,3 +435,60 @@ def test_resumed_blocks_rewrite_the_same_files(runs):
         for name in NAMES:
             np.testing.assert_array_equal(got[name], b[name])
     shutil.rmtree(os.path.join(runs["tmp"], "kernels"), ignore_errors=True)
+
+
+def test_pair_kernel_files_equal_the_restatement(runs):
+    """--pair, SI_ker_pair: one receiver (the station's Z-force SGT series) against the
+    event's series, read block by block (2 x 3 x all points), kernels of five windows (both
+    filter passes, no filter, two windows sharing a band and filter) written under the
+    kernel_phase_Vp ... names; every file equals the restatement (oracle/kpair_oracle.py) of
+    the whole snapshot bit for bit."""
+    from oracle import kpair_oracle as KP
+    R = runs
+    tmp, m, kdt = R["tmp"], R["m"], R["kdt"]
+    subs, subc, subt = SNAP[0], SNAP[1], SNAP[2]
+    pd = lambda name: os.path.join(tmp, "pair", name)  # noqa: E731
+    wins = [(1, 1, 2.5 * kdt, 15.2 * kdt, pd("A")), (1, 2, 3 * kdt, 17 * kdt, pd("B")),
+            (1, 2, 1.5 * kdt, 12 * kdt, pd("C")), (2, 3, 2 * kdt, 18 * kdt, pd("D")),
+            (1, 3, 4 * kdt, 19 * kdt, pd("E"))]
+    for w in wins:
+        os.makedirs(w[4], exist_ok=True)
+    t, (_, v, u) = R["t"], R["syn"][0]
+    syn = os.path.join(tmp, "pair_syn.txt")
+    with open(syn, "w") as f:
+        f.write(f"{KNT}\n" + "".join(f"{float(a)!r} {float(b)!r} {float(c)!r}\n" for a, b, c in zip(t, v, u)))
+    main = os.path.join(tmp, "run_ev", "SeisFD3D.conf")
+    conf = os.path.join(tmp, "TomoKernel_pair.conf")
+    lines = [f"MAIN_CONF = {main}", f"SGT_ROOT = {os.path.join(R['sgt_root'], 'STA', 'FZ')}", f"SGT_M0 = {M0!r}",
+             f"WAVE_ROOT = {os.path.join(R['evt_root'], 'EV1', 'OUT')}", "snap_id = 1", "block_size = 2 3 -1",
+             f"fnm_syn = {syn}", "number_of_freqband = 2", f"number_of_measured = {len(wins)}", "<time_window>"]
+    for band, filt, t1, t2, d in wins:
+        lines += [f"{band} {filt} {float(np.float32(t1))!r} {float(np.float32(t2))!r}", d]
+    lines += ["<filter_file>", os.path.join(tmp, "bp1.txt"), "none"]
+    with open(conf, "w") as f:
+        f.write("\n".join(lines) + "\n")
+    r = subprocess.run([KER, "--pair", conf], input="0 0 0\n", capture_output=True, text=True, cwd=tmp)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert f"{len(wins) * 3 * 2} pair kernel blocks" in r.stdout     # 3 x 2 x 1 blocks
+    # the restatement over every snapshot point
+    gi = [LENFD + subs[d] - 1 + np.arange(subc[d]) * subt[d] for d in range(3)]
+    lam = m.lam[np.ix_(*gi)].transpose(2, 1, 0).reshape(-1)
+    mu = m.mu[np.ix_(*gi)].transpose(2, 1, 0).reshape(-1)
+    rs = _sgt_series(os.path.join(R["sgt_root"], "STA", "FZ")).reshape(6, KNT, -1)
+    ss = _sgt_series(os.path.join(R["evt_root"], "EV1", "OUT")).reshape(6, KNT, -1)
+    sa, sb = KP.scatter_pair(lam, mu, rs, ss, float(kdt))
+    fb, fa = R["filt"]
+    t32 = np.asarray(t, np.float32)
+    for band, filt, t1, t2, d in wins:
+        t1, t2 = np.float32(t1), np.float32(t2)
+        nt1 = int(np.flatnonzero(t32 <= t1)[-1]) + 1
+        nt2 = int(np.flatnonzero(t32 >= t2)[0]) + 1
+        mode = 0 if filt == 3 else filt
+        want = KP.kernel_pair(v, u, sa, sb, float(kdt), nt1, nt2, M0, mode=mode, b=fb, a=fa)
+        got, att = _read(os.path.join(d, "kernel_001_mpi000000_n00000.nc"))
+        assert att["title"] == b"Finite frequency kernel"
+        for q, name in enumerate(("kernel_phase_Vp", "kernel_amplitude_Vp", "kernel_phase_Vs",
+                                  "kernel_amplitude_Vs")):
+            w = np.asarray(want[q]).astype(np.float32).reshape(subc[2], subc[1], subc[0])
+            np.testing.assert_array_equal(got[name], w, err_msg=f"{d} {name}")
+            assert np.any(w)

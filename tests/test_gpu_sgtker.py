@@ -303,3 +303,38 @@ def test_parameter_conversion_bitwise(mode, native_lib):
     with pytest.raises(Exception):
         k.convert(4, *kern)
     k.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_pair_bitwise_against_the_restatement(mode, native_lib):
+    """SI_ker_pair on the device: the single-precision scatter series of one receiver SGT
+    against the source SGT, and the window kernels after each filter mode, equal the
+    restatement (oracle/kpair_oracle.py) bit for bit; lags across several staging chunks
+    (knt 700)."""
+    import fwant_gb300 as fw
+    from oracle import kpair_oracle as KP
+    signal = pytest.importorskip("scipy.signal")
+    rng = np.random.default_rng(31 + mode)
+    npts, knt, dt = 29, 700 if mode == 0 else 160, np.float32(0.1)
+    lam, mu = _media(rng, npts)
+    rs, ss = _series(rng, npts, knt), _series(rng, npts, knt)
+    K = fw.SgtKernel(npts, knt, float(dt))
+    K.set_media(lam, mu)
+    K.set_sgt(0, rs)
+    K.set_sgt(3, ss)
+    K.scatter_pair()
+    sa, sb = KP.scatter_pair(lam, mu, rs, ss, float(dt))
+    np.testing.assert_array_equal(K.get_scatter(0), sa)
+    np.testing.assert_array_equal(K.get_scatter(1), sb)
+    b, a = signal.butter(2, [0.05, 0.3], btype="band")
+    v = rng.normal(size=knt).astype(np.float32)
+    u = np.cumsum(v).astype(np.float32) * dt
+    for nt1, nt2 in ((1, knt), (7, knt // 2), (knt // 3, knt - 5)):
+        got = K.kernel_pair(v, u, nt1, nt2, 1.0e15, mode=mode, b=b, a=a)
+        want = KP.kernel_pair(v, u, sa, sb, float(dt), nt1, nt2, 1.0e15, mode=mode, b=b, a=a)
+        for q in range(4):
+            np.testing.assert_array_equal(got[q], np.asarray(want[q]).astype(np.float32), err_msg=f"{nt1} {nt2} {q}")
+            assert np.any(got[q])
+    with pytest.raises(fw.FwantError):
+        K.kernel_pair(v, u, 0, knt, 1.0e15)
+    K.close()
