@@ -35,7 +35,8 @@ SOURCES = ["stage_fast_rk0.cu", "stage_fast_rk1.cu", "stage_fast_rk2.cu", "stage
            "stage_topo_rk0.cu", "stage_topo_rk1.cu", "stage_topo_rk2.cu", "stage_topo_exact_rk0.cu",
            "stage_topo_exact_rk1.cu", "stage_topo_exact_rk2.cu", "stage_fast_rk3.cu", "stage_fast_rk4.cu",
            "stage_fast_rk5.cu", "stage_fast16_rk3.cu", "stage_fast16_rk4.cu", "stage_fast16_rk5.cu", "stage_topo_rk3.cu",
-           "stage_topo_rk4.cu", "stage_topo_rk5.cu", "topo.cu",
+           "stage_topo_rk4.cu", "stage_topo_rk5.cu", "stage_bf16_rk3.cu", "stage_bf16_rk4.cu", "stage_bf16_rk5.cu",
+           "stage_fp16_rk3.cu", "stage_fp16_rk4.cu", "stage_fp16_rk5.cu", "topo.cu",
            "stage_dispatch.cu", "waits.cu", "aux.cu", "snapshot.cu", "sgtker.cu", "surrogate.cu", "lsqr.cu", "media.cu", "assm.cu", "kerinfo.cu", "solver.cpp", "sgtker_api.cpp"]
 # units whose FP32 expressions must round like the reference's source (no contraction)
 EXACT_SOURCES = {"media.cu"}

@@ -163,7 +163,7 @@ static_assert(sizeof(BatchArgs) <= 32764, "kernel parameter space");
 
 // RK kinds of the stage kernel.  0 RK_beg, 1 RK_inn, 2 RK_fin update the reference's
 // registers (W, the stage start m and the accumulator t; mod_macdrp.F90:291-393).  The fast
-// FP32 form also runs the classical RK4 step without carrying t through stages 1-3:
+// form also runs the classical RK4 step without carrying t through stages 1-3:
 //   3  stage 1: W2 = m + a1 h                               (no t)
 //   4  stage 2: W3 = m + a2 h                               (no t)
 //   5  stage 3: W4 = m + a3 h, t = m + ((W2 - m) + 2 (W3 - m) + a3 h) / 3
@@ -174,7 +174,7 @@ static_assert(sizeof(BatchArgs) <= 32764, "kernel parameter space");
 __host__ __device__ constexpr int rk_base(int rk) { return rk == 3 ? 0 : (rk >= 4 ? 1 : rk); }
 
 // Stage launchers (stage_*.cu).  variant bit 2 = x, bit 1 = y, bit 0 = z; 1 = forward
-// operator.  rk: the kinds above (3-5 for FP32 storage, fast form only).  exact = 1 selects the reference's
+// operator.  rk: the kinds above (3-5 in the fast form only).  exact = 1 selects the reference's
 // operand order with IEEE division and no FMA (bit-reproducible against FP32 CPU runs
 // of the same expressions); 0 the fast form (FMA, reciprocals).
 // storage: ST_F32 / ST_BF16 / ST_F16 (the exact form exists for ST_F32 only).

@@ -843,8 +843,8 @@ struct fwant_solver {
     return (s % 2 == 0) ? X : (~X & 7);
   }
   // The classical RK4 step without carrying t through stages 1-3 (RK kinds 3, 4, 5, then
-  // RK_fin): the fast form with FP32 storage.
-  bool recon_on() const { return rk_scheme == 1 && !cfg.exact_arith && stor == fw::ST_F32; }
+  // RK_fin): the fast form, every storage.
+  bool recon_on() const { return rk_scheme == 1 && !cfg.exact_arith; }
   int stage_rk(int s) const {
     if (recon_on()) return s == 0 ? 3 : (s == 1 ? 4 : (s == 2 ? 5 : 2));
     return s == 0 ? 0 : (s == 3 ? 2 : 1);

@@ -27,6 +27,8 @@ FW_DECL(exact)
   int configure_stage_##mode##_rk5();
 FW_DECL_NOT(fast)
 FW_DECL_NOT(fast16)
+FW_DECL_NOT(bf16)
+FW_DECL_NOT(fp16)
 #undef FW_DECL_NOT
 FW_DECL(fast16)
 FW_DECL(exact16)
@@ -70,13 +72,16 @@ int launch_stage_batch_topo(const BatchArgs& b, int variant, int rk, int exact, 
 int launch_stage_batch(const BatchArgs& b, int variant, int rk, int exact, int storage, int lean, int ctas,
                        void* stream, int ty) {
   cudaStream_t st = (cudaStream_t)stream;
-  if (rk >= 3) {  // fast FP32 form only
-    if (rk > 5 || exact || storage != ST_F32 || (ty != STAGE_TY && ty != STAGE_TY_TALL)) return int(cudaErrorInvalidValue);
+  if (rk >= 3) {  // fast forms only
+    if (rk > 5 || exact || (ty != STAGE_TY && ty != STAGE_TY_TALL) || (storage != ST_F32 && ty != STAGE_TY))
+      return int(cudaErrorInvalidValue);
 #define FW_RKN(mode)                                                                        \
   return rk == 3 ? launch_stage_batch_##mode##_rk3(b, variant, lean, ctas, st)              \
                  : (rk == 4 ? launch_stage_batch_##mode##_rk4(b, variant, lean, ctas, st)   \
                             : launch_stage_batch_##mode##_rk5(b, variant, lean, ctas, st));
     if (ty == STAGE_TY_TALL) { FW_RKN(fast16) }
+    if (storage == ST_BF16) { FW_RKN(bf16) }
+    if (storage == ST_F16) { FW_RKN(fp16) }
     FW_RKN(fast)
 #undef FW_RKN
   }
@@ -109,7 +114,9 @@ int stage_configure() {
                           configure_stage_topo_exact_rk2,
                           configure_stage_fast_rk3,   configure_stage_fast_rk4,   configure_stage_fast_rk5,
                           configure_stage_fast16_rk3, configure_stage_fast16_rk4, configure_stage_fast16_rk5,
-                          configure_stage_topo_rk3,   configure_stage_topo_rk4,   configure_stage_topo_rk5};
+                          configure_stage_topo_rk3,   configure_stage_topo_rk4,   configure_stage_topo_rk5,
+                          configure_stage_bf16_rk3,   configure_stage_bf16_rk4,   configure_stage_bf16_rk5,
+                          configure_stage_fp16_rk3,   configure_stage_fp16_rk4,   configure_stage_fp16_rk5};
   for (auto fn : fns)
     if (int e = fn()) return e;
   return 0;

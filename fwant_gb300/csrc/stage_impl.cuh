@@ -299,7 +299,7 @@ template <class S, bool EXACT, int FX, int FY, int FZ, int RKV, bool LEAN, bool 
 __device__ __forceinline__ bool stage_body(const StageArgs& A, int bx, int by, int bz, unsigned char* smem) {
   static_assert(!EXACT || is_f32_v<S>, "the reference-order form exists for FP32 storage only");
   static_assert(!TOPO || (is_f32_v<S> && !LEAN), "the terrain form is FP32, full form");
-  static_assert(RKV <= 2 || (is_f32_v<S> && !EXACT), "the stages without t are fast FP32 forms");
+  static_assert(RKV <= 2 || !EXACT, "the stages without t are fast forms");
   // RK: the reference kind whose data movement this stage follows (kinds in kernels.h);
   // NO_T: the stage neither reads nor writes t; RECON: stage 3 forming t from W2, W3, W4, m
   // (A.tm_t / PML set pml_set[2] then hold W2, which the stage overwrites with W4, and

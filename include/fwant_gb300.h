@@ -405,8 +405,8 @@ fwant_status fwant_get_lean_stages(fwant_solver* s, int* mask);
  * 2 (W3 - m) + a3 h3) / 3 (algebraically the reference's m + b1 h1 + b2 h2 + b3 h3,
  * mod_macdrp.F90:291-393;
  * the same results up to FP32 rounding, 129 instead of 156 floats moved per point and
- * step); 0 carries t as the reference does.  Applies to FP32 storage in the fast form (flat
- * or terrain-following grid); the reference-order form and 2-byte storage always carry t
+ * step); 0 carries t as the reference does.  Applies to the fast form (every storage, flat
+ * or terrain-following grid); the reference-order form always carries t
  * (fwant_get_rk_scheme then reads 0).  May change between steps.  No counterpart in the
  * reference. */
 fwant_status fwant_set_rk_scheme(fwant_solver* s, int scheme);
