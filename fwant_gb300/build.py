@@ -104,7 +104,8 @@ def build(verbose: bool = False, force: bool = False, jobs: int | None = None) -
                 flags = flags + EXACT_FLAGS
             jobs_todo.append([nvcc, *flags, "-I", CSRC, "-I", INCLUDE, "-c", path, "-o", obj])
     if jobs_todo:
-        with ThreadPoolExecutor(max_workers=jobs or min(8, len(jobs_todo))) as ex:
+        # one nvcc per core, up to 24 (each stage unit takes ~15 s and a few hundred MB)
+        with ThreadPoolExecutor(max_workers=jobs or max(1, min(24, os.cpu_count() or 8, len(jobs_todo)))) as ex:
             list(ex.map(lambda c: _run(c, verbose), jobs_todo))
     if force or jobs_todo or _stale(LIB, objs):
         _run([nvcc, "-shared", *ARCH, "-o", LIB, *objs, "-lcudart"], verbose)
