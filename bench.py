@@ -842,8 +842,12 @@ def companions():
         t0 = time.perf_counter()
         cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--config", cfg, "--no-cpu-baseline", "--no-e2e",
                *extra]
-        r = subprocess.run(cmd, capture_output=True, text=True, env={k: v for k, v in os.environ.items()
-                                                                         if k not in ("RANK", "WORLD_SIZE")})
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=600,
+                               env={k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE")})
+        except subprocess.TimeoutExpired:
+            out[name] = {"failed": "timed out after 600 s"}
+            continue
         line = next((x for x in reversed(r.stdout.splitlines()) if x.startswith("{")), None)
         if r.returncode != 0 or line is None:
             out[name] = {"failed": (r.stderr or r.stdout)[-300:]}

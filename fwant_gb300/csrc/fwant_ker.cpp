@@ -695,7 +695,7 @@ int run_pair(const std::string& ker_conf, int device) {
     if (w.nt1 == 0 || w.nt2 == 0 || w.nt1 > w.nt2)
       die(w.dir + ": time window outside the synthetic's time axis");
     const Filter& F = filters[size_t(w.freq - 1)];
-    if (w.filt != 3 && F.nod1 < 2) die(w.dir + ": band without filter coefficients");
+    if (w.filt != 3 && F.nod1 < 1) die(w.dir + ": band without filter coefficients");
   }
   conf::File cf;
   if (!cf.load(main_conf, &err)) die(err);

@@ -302,8 +302,8 @@ fwant_status fwant_sgtker_kernel_pair(fwant_sgtker* k, const float* v, const flo
                                       float* kbp, float* kbq) {
   if (!k || !v || !u || !kap || !kaq || !kbp || !kbq) return FWANT_ERR_INVALID_ARG;
   if (mode < 0 || mode > 2) return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_kernel_pair: filter mode must be 0, 1 or 2");
-  if (mode != 0 && (!b || !a || nod1 < 2 || nod1 > fw::IIR_MAX_COEF || !(a[0] != 0.0)))
-    return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_kernel_pair: filter needs 2..16 coefficients with a[0] != 0");
+  if (mode != 0 && (!b || !a || nod1 < 1 || nod1 > fw::IIR_MAX_COEF || !(a[0] != 0.0)))
+    return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_kernel_pair: filter needs 1..16 coefficients with a[0] != 0");
   if (!k->pair_done) return k->fail(FWANT_ERR_STATE, "sgtker_kernel_pair: fwant_sgtker_scatter_pair first");
   if (nt1 < 1 || nt2 > k->knt || nt1 > nt2)
     return k->fail(FWANT_ERR_INVALID_ARG, "sgtker_kernel_pair: window outside 1..knt");
