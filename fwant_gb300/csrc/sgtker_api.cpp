@@ -173,6 +173,8 @@ fwant_status fwant_sgtker_scatter(fwant_sgtker* k, int flags, int nt1, int nt2) 
   cudaSetDevice(k->device);
   fwant_status rc = k->alloc(&k->series, 6 * k->series_len(), "scatter series");
   if (rc != FWANT_OK) return rc;
+  k->pair_done = false;
+  k->scatter_flags = 0;  // until this scatter completes
   cudaMemsetAsync(k->series, 0, 6 * k->series_len() * sizeof(double), k->st);
   fw::ScatterArgs a{};
   a.npts = k->npts;
@@ -198,6 +200,7 @@ fwant_status fwant_sgtker_scatter(fwant_sgtker* k, int flags, int nt1, int nt2) 
   k->scatter_nt1 = nt1;
   k->scatter_nt2 = nt2;
   k->scatter_flags = flags;
+  k->pair_done = false;  // the series are now this scatter's
   return FWANT_OK;
 }
 
@@ -274,6 +277,8 @@ fwant_status fwant_sgtker_scatter_pair(fwant_sgtker* k) {
   fwant_status rc = k->alloc(&k->series, 6 * k->series_len(), "scatter series");
   if (rc == FWANT_OK) rc = k->alloc(&k->pstrain, 14 * k->series_len(), "pair strains");
   if (rc != FWANT_OK) return rc;
+  k->pair_done = false;  // until this scatter completes
+  k->scatter_flags = 0;
   fw::PairArgs pa{};
   pa.npts = k->npts;
   pa.knt = k->knt;

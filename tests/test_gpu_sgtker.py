@@ -337,4 +337,8 @@ def test_pair_bitwise_against_the_restatement(mode, native_lib):
             assert np.any(got[q])
     with pytest.raises(fw.FwantError):
         K.kernel_pair(v, u, 0, knt, 1.0e15)
+    # a scatter of SI_ker_sta replaces the pair's series: the pair kernel is refused after it
+    K.scatter(1)
+    with pytest.raises(fw.FwantError):
+        K.kernel_pair(v, u, 1, knt, 1.0e15)
     K.close()
