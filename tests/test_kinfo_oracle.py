@@ -72,3 +72,18 @@ def test_sums_are_single_precision_in_pick_order():
     info.end_event("S", "E")
     assert info.S[0, 0] == np.float32(1.0e8)
     assert info.N[0, 0] == 1 and info.rec_M[0][0, 0] == 3
+
+
+def test_name_field_boundaries():
+    """Names of exactly 8 (station) and 20 (event) characters are stored whole; one more
+    character and the write is refused (the slot keeps its earlier name)."""
+    info = KI.KerInfo((1,), [0.0] * 4)
+    one = [np.array([1.0], np.float32)] * 4
+    info.add_pick(one)
+    info.end_event("ABCDEFGH", "E" * 20)
+    assert bytes(info.char_record(0, 0, 0)[0]) == b"ABCDEFGH"
+    assert bytes(info.char_record(0, 0, 1)[0]) == b"E" * 20
+    info.add_pick(one)
+    info.end_event("ABCDEFGHI", "F" * 21)           # record 2: names refused
+    assert not info.char_record(1, 0, 0).any() and not info.char_record(1, 0, 1).any()
+    assert info.rec_M[1][0, 0] == 1
