@@ -171,7 +171,7 @@ def source_shift(coord: np.ndarray, i: int, v: float) -> float:
 def make_model(ni, nj, nk, seed=0, dh_km=1.0, theta_c_deg=50.0, phi_c_deg=100.0, z_top_km=0.5,
                z_bottom_km=2.0, npml=12, free_surface=True, nrecv=16, cfl=0.5, perturb=0.0,
                source="surface", force=(0.0, 0.0, 1.0e15), fc=0.2, t0=7.5, name="") -> Model:
-    """A seeded model of the BASELINE workloads: 1 km horizontal spacing (in degrees at
+    """A seeded model of the benchmark workloads (C1-C5): 1 km horizontal spacing (in degrees at
     the top radius), vertical spacing stretched from z_top_km to z_bottom_km, layered
     medium, CFS-PML of npml cells on x1 x2 y1 y2 z1 (+z2 without a free surface), one
     Ricker point force and nrecv seeded surface receivers."""
