@@ -204,10 +204,16 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic_ratio(scheme=1):
+def ncu_traffic_ratio(scheme=1, storage="fp32"):
     """Measured DRAM bytes over algorithmic bytes of the stage kernel in RK form `scheme`,
-    from the committed ncu summary (captured on a smaller grid of the same kernel), or None."""
-    path = os.path.join(ROOT, "profiles", "stage_batch_kernel_c2.md")
+    from the committed ncu summary (captured on a smaller grid of the same kernel), or None.
+    BF16 storage has its own capture (form 1); FP16 shares its layout and halo."""
+    if storage == "fp32":
+        path = os.path.join(ROOT, "profiles", "stage_batch_kernel_c2.md")
+    elif scheme == 1:
+        path = os.path.join(ROOT, "profiles", "stage_batch_kernel_bf16_c2.md")
+    else:
+        return None
     if not os.path.exists(path):
         return None
     key = "dram_traffic_over_algorithmic" if scheme == 1 else "dram_traffic_over_algorithmic_form0"
@@ -1008,11 +1014,12 @@ def run_ours(args, rank, world):
     launch_ms = float(np.mean(stage_ms))
     achieved = algo_bytes_step / 4.0 / (launch_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
-    tr = ncu_traffic_ratio(scheme) if args.storage == "fp32" else None
+    tr = ncu_traffic_ratio(scheme, args.storage)
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "peak_source": peak_kind, "traffic": (tr * algo_bytes_step / 4.0) if tr else None,
             "traffic_note": "bytes per stage (its interior-only and full launches): ncu DRAM/algorithmic "
-                            "ratio (profiles/stage_batch_kernel_c2.md) x algorithmic bytes of the stage",
+                            "ratio (profiles/stage_batch_kernel_" + ("c2" if args.storage == "fp32" else "bf16_c2")
+                            + ".md) x algorithmic bytes of the stage",
             "stage_ms": stage_ms, "step_end_ms": end_ms,
             "algorithmic_bytes_per_stage": algo_bytes_step / 4.0, "rk_scheme": scheme}
     if scheme == 1:
