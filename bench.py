@@ -919,7 +919,7 @@ def run_c1_hill(args, rank):
 
 
 def run_surrogate(args, rank):
-    """Config 5: the surrogate's screening speedup over FD solves at 1% waveform error."""
+    """C5 workload: the surrogate's screening speedup over FD solves at 1% waveform error."""
     from fwant_gb300 import surrogate
     if rank != 0:
         return 0

@@ -260,14 +260,14 @@ def gaussian_hill(m: Model, amplitude_m: float, width_km: float | None = None, s
 
 
 def config_c1(seed=0, **kw) -> Model:
-    """Config 1: 100x100x60, 1 km horizontal, 0.5-2 km vertical, layered Vp 5.8-8.0,
+    """C1 workload: 100x100x60, 1 km horizontal, 0.5-2 km vertical, layered Vp 5.8-8.0,
     12-cell PML on 5 faces, free surface, vertical Ricker force (0.2 Hz) at the surface
     centre, 16 seeded surface receivers, CFL 0.5 (flat top)."""
     return make_model(100, 100, 60, seed=seed, name="C1 100x100x60", **kw)
 
 
 def config_c2(seed=0, component=2, **kw) -> Model:
-    """Config 2: 400x400x200 with a +/-5% Gaussian-correlated (10 km) Vp/Vs perturbation,
+    """C2 workload: 400x400x200 with a +/-5% Gaussian-correlated (10 km) Vp/Vs perturbation,
     64 surface receivers; component selects the force direction (0 Fx, 1 Fy, 2 Fz)."""
     f = [0.0, 0.0, 0.0]
     f[component] = 1.0e15
@@ -279,7 +279,7 @@ C4_STATIONS = ((-40, 0), (40, 0))  # (di, dj) of stations A and B from the surfa
 
 
 def config_c4(seed=0, station=0, **kw) -> Model:
-    """Config 4 (precision study): 256x256x128 with the C2 physics (+/-5% perturbation),
+    """C4 workload (precision study): 256x256x128 with the C2 physics (+/-5% perturbation),
     a vertical surface force at station A (station=0) or B (station=1), 80 km apart on the
     surface; receivers: A, B, then 16 seeded surface receivers.  The two simulations are
     the source-side and receiver-side strain Green's tensors of the station pair."""
@@ -294,7 +294,7 @@ def config_c4(seed=0, station=0, **kw) -> Model:
 
 
 def config_c3(seed=0, count=32, **kw) -> list:
-    """Config 3: `count` virtual sources of seeded uneven sizes (horizontal 160-320 cells,
+    """C3 workload: `count` virtual sources of seeded uneven sizes (horizontal 160-320 cells,
     depth 80-160 cells), the C2 physics (+/-5% perturbation), one vertical surface force
     at a seeded station each, 16 surface receivers."""
     rng = np.random.default_rng(seed + 104729)

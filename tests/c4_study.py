@@ -1,4 +1,4 @@
-"""Config 4 precision study: one station pair on a 256x256x128 grid.
+"""C4 precision study: one station pair on a 256x256x128 grid.
 
 Simulation A (vertical surface force at station A) is the source side and simulation B
 (vertical force at station B) the receiver side of the pair's ZZ sensitivity kernel.

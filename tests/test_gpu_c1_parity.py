@@ -1,7 +1,7 @@
-"""Full-length parity on config 1: 100x100x60, 1 km horizontal / 0.5-2 km vertical spacing,
+"""Full-length parity on the C1 case: 100x100x60, 1 km horizontal / 0.5-2 km vertical spacing,
 layered medium, 12-cell CFS-PML on five faces, free surface, vertical Ricker force at the
 surface centre, 16 surface receivers, nt = 2000 (the reference runs 2008 steps: whole
-8-step blocks).  Tolerance from the benchmark spec: 1e-4 relative L2 on the receiver seismograms
+8-step blocks).  Tolerance of the drop-in: 1e-4 relative L2 on the receiver seismograms
 (velocities and stresses as two groups; on the free surface Txz and Tyz vanish and Tzz is
 rounding noise)."""
 import numpy as np

@@ -7,7 +7,7 @@ is compared.  Two arithmetic forms of the same kernel are checked:
   FMA; it must agree with the oracle to within 1e-6 relative L2 per field (in practice
   it is bit-identical);
 * the default fast form (FMA, precomputed reciprocals) must agree within 1e-5 relative
-  L2 after 75 steps (the benchmark spec tolerance for full runs: 1e-4 on seismograms).
+  L2 after 75 steps (the drop-in's tolerance for full runs: 1e-4 on seismograms).
 """
 import numpy as np
 import pytest

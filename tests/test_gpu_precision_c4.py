@@ -1,4 +1,4 @@
-"""Config 4 precision study on the GPU against the FP64 reference run.
+"""C4 precision study on the GPU against the FP64 reference run.
 
 For each wavefield storage kind (FP32, BF16, FP16 with FP32 arithmetic) both simulations
 of the station pair run on the GPU with device SGT recording, the ZZ kernel is
