@@ -1886,7 +1886,7 @@ fwant_status fwant_autotune(fwant_solver* s, int trial_steps, int* planes_out) {
   // tile shape (32 x 8, and 32 x 16 where the storage and grid allow it) x planes per CTA
   std::vector<int> shapes = {fw::STAGE_TY};
   if (s->tile_rows_allowed(fw::STAGE_TY_TALL)) shapes.push_back(fw::STAGE_TY_TALL);
-  const int cand[] = {4, 6, 8, 12, 16, 24, 32, 48, 64, 96, 128};
+  const int cand[] = {3, 4, 6, 8, 12, 16, 24, 32, 48, 64, 96, 128};
   double best = 1e30;
   int best_kc = s->kc, best_ty = s->tile_ty;
   for (int ty : shapes) {
@@ -2286,7 +2286,7 @@ fwant_status fwant_batch_autotune(fwant_batch* b, int trial_steps, int* ctas_out
   bool tall = true;
   for (fwant_solver* m : b->sims) tall = tall && m->tile_rows_allowed(fw::STAGE_TY_TALL);
   if (tall) shapes.push_back(fw::STAGE_TY_TALL);
-  const int kcand[] = {4, 6, 8, 12, 16, 24, 32};
+  const int kcand[] = {3, 4, 6, 8, 12, 16, 24, 32};
   double best_t = 1e30;
   int best_kc = b->sims[0]->kc, best_ty = b->sims[0]->tile_ty;
   b->ctas = 0;

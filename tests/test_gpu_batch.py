@@ -111,7 +111,7 @@ def test_autotune_keeps_results(oracle_mod, native_lib):
     pairs = _members(oracle_mod, False)[:3]
     tuned, plain = pairs[0]
     kc = tuned.autotune(2)
-    assert kc >= 4 and tuned.ntime == 0 and tuned.planes_per_cta == kc
+    assert kc >= 3 and tuned.ntime == 0 and tuned.planes_per_cta == kc
     for s in (tuned, plain):
         s.run(20)
     for c in range(9):
