@@ -190,3 +190,85 @@ def convergence_orders(sols):
     errs = [float(np.sqrt(np.sum((coarse[l] - coarse[l + 1]) ** 2)) / ref) for l in range(len(sols) - 1)]
     orders = [float(np.log2(errs[l] / errs[l + 1])) for l in range(len(errs) - 1)]
     return errs, orders
+
+
+# ---- wave speeds ---------------------------------------------------------------------------
+def _uniform_solver(make, n, th, ph, r, dr, dang, stept):
+    """A solver on the uniform spherical grid of convergence_grid with the exact metric,
+    the homogeneous medium (VP, VS, RHO), no PML, no free surface."""
+    s = make(n, n, n, stept, False)
+    s.set_coord(th.astype(np.float32), ph.astype(np.float32), r.astype(np.float32))
+    nx = n + 2 * LENFD
+    s.set_metric(np.sin(th).astype(np.float32), (1.0 / np.tan(th)).astype(np.float32),
+                 np.full(nx, 1.0 / dang, np.float32), np.full(nx, 1.0 / dang, np.float32),
+                 np.full(nx, 1.0 / dr, np.float32))
+    shape = (nx, nx, nx)
+    mu = RHO * VS * VS
+    lam = RHO * VP * VP - 2 * mu
+    s.set_media(np.full(shape, lam, np.float32, order="F"), np.full(shape, mu, np.float32, order="F"),
+                np.full(shape, RHO, np.float32, order="F"))
+    s.set_pml(np.zeros(6, np.int32), np.zeros(6, np.float32), np.ones(6, np.float32), np.zeros(6, np.float32))
+    return s
+
+
+def pulse_line(make, kind, level=1, width_km=3.0, t_end=2.4):
+    """A pure P or pure S pulse in the homogeneous cube of convergence_grid (48 km, spacing
+    1 km / 2^level, CFL 0.3 steps to t_end) against the closed-form solution of the wave
+    equation at VP or VS, on the theta line through the centre (a > 0).
+
+    P: an isotropic stress pulse sigma_ii = g = 1e6 exp(-d^2/w^2) Pa at rest.  The motion
+    stays irrotational, v = grad(psi) with rho psi_tt = (lambda + 2 mu) lap(psi), psi(0) = 0,
+    psi_t(0) = g / rho, so psi = 1e6 w^2 / (4 r VP rho) (exp(-(r - VP t)^2/w^2) -
+    exp(-(r + VP t)^2/w^2)) and the radial velocity (v_theta on the line) is dpsi/dr.
+    S: a rotational velocity pulse v = (dq/db, -dq/da, 0), q = exp(-d^2/w^2) (a, b the
+    distances along theta and phi), at zero stress.  The motion stays divergence-free, each
+    velocity component obeys the scalar wave equation at VS with zero initial rate, so
+    v_phi = -dQ/da with Q = ((r - VS t) q(r - VS t) + (r + VS t) q(r + VS t)) / (2 r), and on
+    the line d/da = d/dr.
+    Returns (distances, numerical, closed-form) float64 arrays along the line."""
+    n, th, ph, r, dr, dang = convergence_grid(level)
+    stept = 0.3 * dr / VP
+    c = LENFD + (n - 1) // 2
+    # Cartesian offsets from the centre node in its local frame (theta, phi, r unit vectors)
+    T, P_, Rr = np.meshgrid(th, ph, r, indexing="ij")
+    X = np.stack([Rr * np.sin(T) * np.cos(P_), Rr * np.sin(T) * np.sin(P_), Rr * np.cos(T)])
+    t0, p0 = th[c], ph[c]
+    et = np.array([np.cos(t0) * np.cos(p0), np.cos(t0) * np.sin(p0), -np.sin(t0)])
+    ep = np.array([-np.sin(p0), np.cos(p0), 0.0])
+    er = np.array([np.sin(t0) * np.cos(p0), np.sin(t0) * np.sin(p0), np.cos(t0)])
+    D = X - X[:, c, c, c][:, None, None, None]
+    A = np.tensordot(et, D, axes=1)
+    B = np.tensordot(ep, D, axes=1)
+    H = np.tensordot(er, D, axes=1)
+    w = width_km * 1000.0
+    g = np.exp(-(A * A + B * B + H * H) / (w * w))
+    s = _uniform_solver(make, n, th, ph, r, dr, dang, stept)
+    if kind == "P":
+        p = np.asfortranarray((1.0e6 * g).astype(np.float32))
+        for comp in ("Txx", "Tyy", "Tzz"):
+            s.set_field(comp, p)
+        comp = 0
+    else:
+        s.set_field("Vx", np.asfortranarray((-2.0 * B / (w * w) * g).astype(np.float32)))
+        s.set_field("Vy", np.asfortranarray((2.0 * A / (w * w) * g).astype(np.float32)))
+        comp = 1
+    steps = int(round(t_end / stept))
+    s.run(steps)
+    t = steps * stept
+    line = slice(c + 1, LENFD + n)
+    num = np.asarray(s.get_field(comp), np.float64)[line, c, c]
+    if hasattr(s, "close"):
+        s.close()
+    d = np.sqrt(A[line, c, c] ** 2 + B[line, c, c] ** 2 + H[line, c, c] ** 2)
+    if kind == "P":
+        def psi(x):
+            return 1.0e6 * w * w / (4.0 * x * VP * RHO) * (np.exp(-((x - VP * t) / w) ** 2) -
+                                                             np.exp(-((x + VP * t) / w) ** 2))
+        f = psi
+    else:
+        def f(x):
+            q = lambda y: np.exp(-(y / w) ** 2)  # noqa: E731
+            return -((x - VS * t) * q(x - VS * t) + (x + VS * t) * q(x + VS * t)) / (2.0 * x)
+    e = 1.0e-3 * dr
+    exact = (f(d + e) - f(d - e)) / (2.0 * e)
+    return d, num, exact
