@@ -272,3 +272,57 @@ def pulse_line(make, kind, level=1, width_km=3.0, t_end=2.4):
     e = 1.0e-3 * dr
     exact = (f(d + e) - f(d - e)) / (2.0 * e)
     return d, num, exact
+
+
+# ---- Rayleigh waves on the free surface ----------------------------------------------------
+def rayleigh_ratio(kappa):
+    """c_R / Vs of a homogeneous half-space with Vp / Vs = kappa: the root in (0.5, 1) of
+    (2 - x^2)^2 = 4 sqrt(1 - x^2) sqrt(1 - x^2 / kappa^2), by bisection."""
+    f = lambda x: (2 - x * x) ** 2 - 4 * np.sqrt(1 - x * x) * np.sqrt(1 - x * x / (kappa * kappa))  # noqa: E731
+    lo, hi = 0.5, 0.99
+    for _ in range(100):
+        mid = 0.5 * (lo + hi)
+        if f(lo) * f(mid) <= 0:
+            hi = mid
+        else:
+            lo = mid
+    return 0.5 * (lo + hi)
+
+
+def rayleigh_speed(make, dh_km):
+    """Speed of the Rayleigh pulse of a vertical surface force (0.5 Hz Ricker centred at
+    2.5 s) on a homogeneous half-space (VP, VS, RHO), 70 x 24 x 20 km at spacing dh_km,
+    CFS-PML of 5 km on five faces, free surface on top: vertical velocity at surface
+    receivers 8, 10, ..., 26 km from the source along theta; the delay of each trace
+    against the nearest one by cross-correlation (parabolic peak), and the speed from a
+    least-squares line of distance against delay.  Returns (measured, theoretical c_R) in
+    m/s."""
+    n_h, n_j, n_k = int(round(70 / dh_km)), int(round(24 / dh_km)), int(round(20 / dh_km))
+    m = inputs.make_model(n_h, n_j, n_k, seed=1, dh_km=dh_km, z_top_km=dh_km, z_bottom_km=dh_km,
+                          npml=int(round(5 / dh_km)), nrecv=0, source="surface", fc=0.5, t0=2.5, cfl=0.3)
+    mu = RHO * VS * VS
+    m.lam[:] = RHO * VP * VP - 2 * mu
+    m.mu[:] = mu
+    m.rho[:] = RHO
+    m.stept = float(np.float32(0.3 * dh_km * 1000.0 * np.sin(m.x[LENFD:-LENFD]).min() / VP))
+    m.pml_velocity[:] = VP
+    ic, jc, kc = (int(v) for v in m.force_indx[0])
+    step = int(round(2 / dh_km))
+    offs = np.arange(int(round(8 / dh_km)), int(round(26 / dh_km)) + 1, step)
+    rec = np.array([[ic + o, jc, kc] for o in offs], np.int32)
+    s = make(m.ni, m.nj, m.nk, m.stept, True)
+    inputs.attach(s, m)
+    s.set_receivers(rec, 1)
+    s.run(int(13.0 / m.stept))
+    vz = np.asarray(s.get_seismo()[2], np.float64)      # (samples, receivers)
+    if hasattr(s, "close"):
+        s.close()
+    r_top = float(m.z[-1 - LENFD])
+    d = (m.x[rec[:, 0] - 1].astype(np.float64) - float(m.x[ic - 1])) * r_top
+    lag = []
+    for q in range(len(offs)):
+        cc = np.correlate(vz[:, q], vz[:, 0], "full")
+        k = int(np.argmax(cc))
+        y0, y1, y2 = cc[k - 1], cc[k], cc[k + 1]
+        lag.append((k - (vz.shape[0] - 1) + 0.5 * (y0 - y2) / (y0 - 2.0 * y1 + y2)) * m.stept)
+    return float(np.polyfit(np.array(lag), d, 1)[0]), rayleigh_ratio(VP / VS) * VS

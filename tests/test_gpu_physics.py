@@ -4,7 +4,9 @@ pairs must keep shrinking at a 0.25 km surface spacing, and the convergence stud
 0.125 km level (385^3 points), where the observed order reaches 3.7 (successive
 differences 3.7e-4, 6.0e-5, 4.7e-6).  The P and S pulses of the oracle test, against
 their closed-form solutions, add a 0.25 km level: P 1.8%, 0.17%, 0.015%; S 2.2%, 0.17%,
-0.021% at 1, 0.5 and 0.25 km (an observed order of 3.2-3.5)."""
+0.021% at 1, 0.5 and 0.25 km (an observed order of 3.2-3.5).  The Rayleigh pulse of the
+oracle test runs at 0.5, 0.25 and 0.125 km spacing and must approach the half-space's
+Rayleigh speed: 1.43%, 0.36% and 0.24% slow."""
 import numpy as np
 import pytest
 
@@ -64,3 +66,13 @@ def test_pulses_travel_at_the_medium_speeds_gpu(kind, native_lib):
     print(kind, errs)
     assert errs[0] < 0.03 and errs[1] < 0.004 and errs[1] < errs[0] / 5, errs
     assert errs[2] < errs[1], errs
+
+
+def test_rayleigh_wave_speed_gpu(native_lib):
+    errs = []
+    for dh in (0.5, 0.25, 0.125):
+        c, cr = P.rayleigh_speed(_make(), dh)
+        errs.append(c / cr - 1)
+    print(errs)
+    assert abs(errs[0]) < 0.025 and abs(errs[1]) < 0.006, errs
+    assert abs(errs[2]) < abs(errs[1]), errs

@@ -18,7 +18,11 @@ Measured on the oracle (FP32, seeded models of tests/physics.py):
 * a pure P pulse (isotropic stress) and a pure S pulse (rotational velocity) in a
   homogeneous cube against the closed-form solutions of the wave equation at Vp and Vs
   along a line through the centre: 1.8% / 2.2% relative L2 at 1 km spacing, 0.17% / 0.17%
-  at 0.5 km (a 1% error in either speed would move the pulse 140 m and cost ~7%)."""
+  at 0.5 km (a 1% error in either speed would move the pulse 140 m and cost ~7%);
+* the Rayleigh pulse of a vertical surface force on a homogeneous half-space travels at
+  the half-space's Rayleigh speed (0.919 Vs): 1.4% slow at 0.5 km spacing, 0.35% at
+  0.25 km (measured on the oracle; a surface without the traction condition has no such
+  wave)."""
 import numpy as np
 import pytest
 
@@ -83,3 +87,10 @@ def test_pulses_travel_at_the_medium_speeds(kind, oracle_mod):
         errs.append(float(np.linalg.norm(num - exact) / np.linalg.norm(exact)))
     print(kind, errs)
     assert errs[0] < 0.03 and errs[1] < 0.004 and errs[1] < errs[0] / 5, errs
+
+
+def test_rayleigh_wave_speed(oracle_mod):
+    oracle_mod.set_threads(0)
+    c, cr = P.rayleigh_speed(_make(oracle_mod), 0.5)
+    print(c, cr, c / cr - 1)
+    assert abs(c / cr - 1) < 0.025, (c, cr)
