@@ -185,23 +185,4 @@ void stage_items(const Geom& g, int kc, int ty, int kz_lo, int kz_hi, const Slab
   *nfull = nf;
 }
 
-// Planes per CTA.  Short chunks keep the CTAs that share halo rows marching through the
-// same planes at the same time, which is what lets L2 serve the halo and z-queue
-// re-reads; measured on 400x400x200 (RK form 0): 16 planes 1.68 ms per RK_inn stage, 32
-// planes 1.78, 64 planes 2.01, the whole column 3.04; with RK form 1 and concurrent
-// interior-only / full launches, 24 planes per step 11.33 ms against 11.37 for 16 and 11.34
-// for 20 (the autotuner picks 24 there too).  Small grids get shorter chunks so that there
-// are at least ~4 CTAs per SM, down to 3 planes: on 100x100x60 (C1, its working set held in
-// L2) 3 planes run 0.263 ms per step, 4 planes 0.280, 6 planes 0.278, 8 planes 0.297.
-int stage_planes_per_cta(const Geom& g, int sm_count, int ty) {
-  const long long tiles = (long long)((g.ni + STAGE_TX - 1) / STAGE_TX) * ((g.nj + ty - 1) / ty);
-  const long long want = 4LL * sm_count * STAGE_TY / ty;  // ~4 CTAs of 256 threads per SM
-  long long chunks = (want + tiles - 1) / tiles;
-  if (chunks < 1) chunks = 1;
-  int kc = int((g.nk + chunks - 1) / chunks);
-  if (kc < 3) kc = 3;
-  if (kc > 24) kc = 24;
-  return std::max(kc, (g.nk + 2046) / 2047);  // at most 2047 chunks, as fwant_set_planes_per_cta allows
-}
-
 }  // namespace fw
